@@ -1,0 +1,380 @@
+"""Benchmark of the 5-pathtrace hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload soup]
+                    [--bvh bvh8] [--impl solrt|reference]
+
+A step is one render launch of the workload (all samples of one frame)
+through the C ABI. Default workload: the 1M-triangle soup at 1920x1080,
+64 spp, max depth 4, gradient sky, Lambertian, per-sample PCG streams
+(seed 2). Metric: Mrays/s = ray segments traced (primary + bounce, counted on
+the device) / device time.
+
+  value     device-timed throughput, scene + BVH resident in HBM
+  e2e       the same metric through solrt_render + solrt_image_read with the
+            image read back into pinned host memory every step (wall clock)
+  roofline  the extend (traversal) kernel: algorithmic bytes per segment
+            (32 ray + 16 hit + node bytes x nodes visited + 48 x triangles
+            tested, visit counts from a counting pass) / its event-timed
+            duration, against the measured HBM copy bandwidth
+  cpu_baseline  the CPU oracle (scalar C++ port of the reference shaders
+            with its LBVH), all host cores, on a bounded band of rows at 1 spp
+
+--impl reference times that CPU port alone (the reference itself is Rust +
+Vulkan RT and cannot run here) on the same metric and config.
+Multi-GPU: replicas (each rank renders the full workload; weak scaling).
+"""
+import argparse
+import importlib
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mrays/s at RMSE≤1e-3 vs FP64 oracle, batched vs plain on 1 GB300; p99 job latency"
+UNIT = "Mrays/s"
+
+NODE_BYTES = {0: 64, 1: 80}
+
+
+def workload(name):
+    solrt = importlib.import_module("sol-rs_gb300")
+    S = solrt.scenes
+    if name == "soup":
+        data = S.soup(1_000_000, seed=2)
+        kw = dict(width=1920, height=1080, spp=64, max_bounces=4, miss_mode=solrt.MISS_GRADIENT,
+                  material_mode=solrt.MATERIAL_LAMBERT, rng_mode=solrt.RNG_PER_SAMPLE, seed=2,
+                  accum_mode=solrt.ACCUM_REF_MIX)
+        cfg = {"workload": "triangle soup 1M tris, 1920x1080, 64 spp, max depth 4, gradient sky, Lambert",
+               "tris": 1_000_000, "width": 1920, "height": 1080, "spp": 64, "max_depth": 4}
+    elif name == "cornell":
+        data = S.cornell()
+        kw = dict(width=256, height=256, spp=16, max_bounces=5, miss_mode=solrt.MISS_BLACK,
+                  material_mode=solrt.MATERIAL_LAMBERT, rng_mode=solrt.RNG_PER_SAMPLE, seed=1,
+                  accum_mode=solrt.ACCUM_REF_MIX)
+        cfg = {"workload": "procedural Cornell box 32 tris, 256x256, 16 spp, max depth 5, Lambert",
+               "tris": 32, "width": 256, "height": 256, "spp": 16, "max_depth": 5}
+    elif name == "tunnel":
+        data = S.tunnel()
+        kw = dict(width=2560, height=1440, spp=128, max_bounces=8, miss_mode=solrt.MISS_REF_SKY,
+                  material_mode=solrt.MATERIAL_LAMBERT, rng_mode=solrt.RNG_PER_SAMPLE, seed=3,
+                  accum_mode=solrt.ACCUM_KAHAN)
+        cfg = {"workload": "procedural tunnel 2048x1024 segments (4.19M tris), 2560x1440, 128 spp, max depth 8, "
+                           "Kahan accumulation, sky", "tris": data.tri_count, "width": 2560, "height": 1440,
+               "spp": 128, "max_depth": 8}
+    else:
+        raise SystemExit("unknown workload %s" % name)
+    return data, kw, cfg
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_id):
+        self.device_id = device_id
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", self.device_id], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, v):
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if pg.get_backend() == "nccl" else "cpu")
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(pg, v):
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda" if pg.get_backend() == "nccl" else "cpu")
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+def cpu_baseline(data, kw, cam, budget_s=12.0, threads=0):
+    """Oracle FP32 render (its LBVH, all host cores) on a band of rows at
+    1 spp: Mrays/s over the band. Grows the band until ~budget_s."""
+    import oracle
+    solrt = importlib.import_module("sol-rs_gb300")
+    o = oracle.OracleScene(data)
+    p = solrt.render_params(**dict(kw, spp=1))
+    h = kw["height"]
+    rows = max(1, h // 64)
+    total_seg, total_t, total_rows = 0, 0.0, 0
+    while True:
+        r0 = (h // 2 - rows // 2)
+        t0 = time.perf_counter()
+        _, _, st = o.render(cam, p, rows=(r0, r0 + rows), threads=threads)
+        dt = time.perf_counter() - t0
+        total_seg += st.segments
+        total_t += dt
+        total_rows += rows
+        if total_t > budget_s * 0.3 or rows >= h:
+            break
+        rows = min(h, int(rows * max(2.0, budget_s * 0.6 / max(dt, 1e-3))))
+    cores = threads if threads > 0 else (os.cpu_count() or 1)
+    sample = "%d rows x %d px x 1 spp (central band), FP32 oracle with its LBVH" % (total_rows, kw["width"])
+    return {"value": total_seg / total_t / 1e6, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+            "segments": int(total_seg), "seconds": round(total_t, 3)}
+
+
+def run_reference(args, world, rank, pg):
+    if rank != 0:
+        return 0
+    solrt = importlib.import_module("sol-rs_gb300")
+    data, kw, cfg = workload(args.workload)
+    c = data.camera
+    cam = solrt.camera_look_at(c["eye"], c["center"], c["up"], c["vfov"], kw["width"] / kw["height"])
+    import oracle
+    o = oracle.OracleScene(data)
+    p = solrt.render_params(**dict(kw, spp=1))
+    h = kw["height"]
+    # size one step to ~2 s of CPU work: a central band of rows at 1 spp
+    t0 = time.perf_counter()
+    _, _, st = o.render(cam, p, rows=(h // 2, h // 2 + 4))
+    per_row = (time.perf_counter() - t0) / 4
+    rows = int(min(h, max(1, 2.0 / max(per_row, 1e-6))))
+    r0 = max(0, h // 2 - rows // 2)
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        o.render(cam, p, rows=(r0, r0 + rows))
+    seg, tt = 0, 0.0
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        _, _, st = o.render(cam, p, rows=(r0, r0 + rows))
+        tt += time.perf_counter() - t0
+        seg += st.segments
+    v = seg / tt / 1e6
+    cores = os.cpu_count() or 1
+    line = {"impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * tt / args.steps, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": dict(cfg, parallelism="cpu"),
+            "cpu_baseline": {"value": round(v, 3), "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "%d rows x %d px x 1 spp per step (central band), FP32 oracle port of the "
+                                       "reference shaders with its LBVH; the reference (Rust + Vulkan RT) cannot "
+                                       "run on this machine" % (rows, kw["width"])},
+            "e2e": {"value": round(v, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="solrt", choices=["solrt", "reference"])
+    ap.add_argument("--workload", default="soup", choices=["soup", "cornell", "tunnel"])
+    ap.add_argument("--bvh", default="bvh2", choices=["bvh2", "bvh8"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    world, rank, local, pg = dist_setup(args)
+    if args.impl == "reference":
+        return run_reference(args, world, rank, pg)
+
+    import torch
+    b = importlib.import_module("sol-rs_gb300.build")
+    b.build_lib()
+    solrt = importlib.import_module("sol-rs_gb300")
+    data, kw, cfg = workload(args.workload)
+    bvh = solrt.BVH8_Q8 if args.bvh == "bvh8" else solrt.BVH2
+    c = data.camera
+    cam = solrt.camera_look_at(c["eye"], c["center"], c["up"], c["vfov"], kw["width"] / kw["height"])
+    params = solrt.render_params(**kw)
+    W, H = kw["width"], kw["height"]
+
+    # visit counts per segment (one counting launch at reduced spp)
+    with solrt.Context(local, enable_counters=True) as cctx:
+        csc = solrt.SceneDescription(cctx, data, bvh=bvh)
+        cimg = solrt.Image(cctx, W, H, kw["accum_mode"])
+        cctx.reset_stats()
+        solrt.Renderer(cctx).cmd_trace_rays(csc, cam, solrt.render_params(**dict(kw, spp=min(4, kw["spp"]))), cimg)
+        cctx.synchronize()
+        cs = cctx.stats()
+        nodes_per_seg = cs.node_visits / max(cs.segments, 1)
+        tris_per_seg = cs.tri_tests / max(cs.segments, 1)
+        fb_per_seg = cs.fp64_fallbacks / max(cs.segments, 1)
+        cimg.close()
+        csc.close()
+
+    ctx = solrt.Context(local, enable_timing=True)
+    sc = solrt.SceneDescription(ctx, data, bvh=bvh)
+    info = sc.bvh_info()
+    img = solrt.Image(ctx, W, H, kw["accum_mode"])
+    r = solrt.Renderer(ctx)
+    ext = torch.cuda.ExternalStream(ctx.stream())
+    for i in range(args.warmup):
+        r.cmd_trace_rays(sc, cam, solrt.render_params(**dict(kw, frame=i)), img)
+    ctx.synchronize()
+    ctx.reset_stats()
+    uuid = None
+    try:
+        uuid = "GPU-" + str(torch.cuda.get_device_properties(local).uuid)
+    except Exception:
+        pass
+    clocks = ClockSampler(uuid or str(local))
+    clocks.start()
+    time.sleep(0.3)
+    barrier(pg)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    for i in range(args.steps):
+        r.cmd_trace_rays(sc, cam, solrt.render_params(**dict(kw, frame=args.warmup + i)), img)
+    e1.record(ext)
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    barrier(pg)
+    ms = e0.elapsed_time(e1)
+    st = ctx.stats()
+    clk = clocks.stop()
+    ms_max = max_over_ranks(pg, ms)
+    seg_total = sum_over_ranks(pg, float(st.segments))
+    value = seg_total / (ms_max / 1000.0) / 1e6
+
+    # end to end: render + read back the accumulation and RGBA8 images into pinned host memory
+    e2e = None
+    if not args.no_e2e:
+        host_acc = torch.empty((H, W, 4), dtype=torch.float32, pin_memory=True)
+        host_8 = torch.empty((H, W, 4), dtype=torch.uint8, pin_memory=True)
+        acc_np, rgba_np = host_acc.numpy(), host_8.numpy()
+        ctx.reset_stats()
+        barrier(pg)
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            p = solrt.render_params(**dict(kw, frame=args.warmup + args.steps + i))
+            r.cmd_trace_rays(sc, cam, p, img)
+            img.read_into(acc_np, rgba_np)
+        dt = time.perf_counter() - t0
+        barrier(pg)
+        est = ctx.stats()
+        dt_max = max_over_ranks(pg, dt)
+        e2e_seg = sum_over_ranks(pg, float(est.segments))
+        e2e = {"value": round(e2e_seg / dt_max / 1e6, 3), "unit": UNIT,
+               "h2d_bytes_per_step": 256 + 64, "d2h_bytes_per_step": W * H * 20,
+               "path": "solrt_render (camera + params from host) + solrt_image_read into pinned host buffers"}
+
+    # roofline of the extend kernel
+    peak, peak_kind = peaks()
+    b_seg = 32 + 16 + NODE_BYTES[info.kind] * nodes_per_seg + 48 * tris_per_seg
+    ext_s = st.extend_ms / 1000.0
+    achieved = (st.segments * b_seg) / ext_s / 1e9 if ext_s > 0 else 0.0
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind + " (MEASURED_PEAKS hbm_gbs)",
+                "kernel": "k_extend (BVH traversal)", "bytes_per_segment": round(b_seg, 1),
+                "nodes_per_segment": round(nodes_per_seg, 2), "tris_per_segment": round(tris_per_seg, 2),
+                "extend_ms_per_launch": round(st.extend_ms / max(st.extend_launches, 1), 4),
+                "extend_share_of_step": round(st.extend_ms / ms, 4) if ms > 0 else None}
+
+    out = None
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            try:
+                cpu = cpu_baseline(data, kw, cam)
+            except Exception as ex:  # the CPU leg must not hide the GPU number
+                cpu = {"error": str(ex)}
+        out = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 3), "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+               "config": dict(cfg, parallelism="replicas" if world > 1 else "single", bvh=args.bvh,
+                              l2="inputs larger than L2 (scene + BVH + path queues > 129 MB)",
+                              bvh_build_ms=round(info.build_ms, 3), bvh_node_count=info.node_count),
+               "segments_per_step": int(st.segments // args.steps), "fp64_fallbacks_per_segment": fb_per_seg,
+               "gpu_launches": int(st.launches), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+               "clocks": clk}
+        print(json.dumps(out), flush=True)
+    img.close()
+    sc.close()
+    ctx.close()
+    if pg is not None:
+        pg.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

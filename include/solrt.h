@@ -1,0 +1,336 @@
+/*
+ * solrt.h — C ABI of the GB300-native software path tracer.
+ *
+ * This library stands in for the `5-pathtrace` render path of sol-rs:
+ *   - scene upload + acceleration-structure build
+ *       replaces ray::SceneDescription::from_scene / from_meshes
+ *       (src/ray/mod.rs:49-156) and BLAS::new / TLAS::new
+ *       (src/ray/acceleration.rs:135-239, 344-400);
+ *   - one render launch
+ *       replaces the per-frame `render` of examples/5-pathtrace.rs:294-369:
+ *       UBO SceneUniforms (:7-32), push constant accum_start_frame (:306-314),
+ *       tlas_regenerate (:316) and ShaderBindingTable::cmd_trace_rays
+ *       (src/ray/sbt.rs:167-180) running pathtrace.rgen / .rchit / .rmiss;
+ *   - the RGBA32F accumulation image and RGBA8 render image
+ *       (examples/5-pathtrace.rs:222-229) become device buffers read back by
+ *       solrt_image_read.
+ *
+ * Conventions
+ *   - Every function returns solrt_status (0 = ok). No exceptions cross it.
+ *   - The caller owns host arrays; the library owns device objects until the
+ *     matching *_destroy call.
+ *   - A context owns one CUDA stream; calls on one context are serialised by
+ *     the caller (one context per host thread). Server calls are thread-safe.
+ *   - All device work of a context is asynchronous on its stream unless the
+ *     function says it synchronises.
+ *   - Plain-old-data structs mirror the reference's repr(C) Rust types and are
+ *     pinned by static_assert in the implementation (64 / 48 / 144 bytes).
+ */
+#ifndef SOLRT_H
+#define SOLRT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SOLRT_ABI_VERSION 1u
+
+typedef enum solrt_status {
+    SOLRT_OK = 0,
+    SOLRT_ERR_INVALID = 1,       /* bad argument, malformed scene */
+    SOLRT_ERR_OOM = 2,           /* device or host allocation failed */
+    SOLRT_ERR_DEVICE = 3,        /* CUDA error, or no usable device */
+    SOLRT_ERR_TIMEOUT = 4,       /* a bounded wait ran out */
+    SOLRT_ERR_CAPACITY = 5,      /* a fixed-capacity queue or stack overflowed */
+    SOLRT_ERR_NOT_READY = 6,     /* job still running (server poll) */
+    SOLRT_ERR_NOT_FOUND = 7,     /* unknown job / object */
+    SOLRT_ERR_BUDGET = 8         /* request larger than the memory budget */
+} solrt_status;
+
+/* ------------------------------------------------------------------------ */
+/* Scene types                                                              */
+/* ------------------------------------------------------------------------ */
+
+/* ModelVertex (src/scene/mesh.rs:9-14): pos, color, normal, uv as vec4. 64 B. */
+typedef struct solrt_vertex {
+    float pos[4];
+    float color[4];
+    float normal[4];
+    float uv[4];
+} solrt_vertex;
+
+/* MaterialInfo (src/scene/mod.rs:21-29). 48 B. */
+typedef struct solrt_material {
+    float base_color[4];
+    float emissive[3];
+    float padding0;
+    float metallic;
+    float roughness;
+    float padding1;
+    float padding2;
+} solrt_material;
+
+/* SceneInstance (src/ray/mod.rs:18-24): id, texture_offset, padding,
+ * transform, transform_it (inverse-transpose). Column-major mat4. 144 B. */
+typedef struct solrt_instance {
+    uint32_t id;
+    uint32_t texture_offset;
+    float padding[2];
+    float transform[16];
+    float transform_it[16];
+} solrt_instance;
+
+/* PrimitiveSection + BufferPart (src/scene/mod.rs:31-44): one section is one
+ * BLAS geometry and one instance in the reference (src/ray/mod.rs:78-134).
+ * Indices of a section are relative to its vertex_offset, as the per-section
+ * descriptors of the reference make them (src/scene/mod.rs:47-61). */
+typedef struct solrt_section {
+    uint32_t vertex_offset;
+    uint32_t vertex_count;
+    uint32_t index_offset;
+    uint32_t index_count;     /* a multiple of 3 */
+    uint32_t material_index;  /* into solrt_scene_desc.materials */
+    uint32_t reserved;
+} solrt_section;
+
+/* Everything SceneDescription::from_meshes consumes. `instances` holds one
+ * entry per section (transform + transform_it) or is NULL for identity. */
+typedef struct solrt_scene_desc {
+    const solrt_vertex* vertices;
+    uint32_t vertex_count;
+    uint32_t index_count;
+    const uint32_t* indices;
+    const solrt_section* sections;
+    uint32_t section_count;
+    uint32_t material_count;
+    const solrt_material* materials;
+    const solrt_instance* instances;
+} solrt_scene_desc;
+
+typedef enum solrt_bvh_kind {
+    SOLRT_BVH2 = 0,     /* binary LBVH, FP32 child boxes, 64 B nodes */
+    SOLRT_BVH8_Q8 = 1   /* 8-wide, 8-bit quantised child boxes, 80 B nodes */
+} solrt_bvh_kind;
+
+typedef struct solrt_bvh_desc {
+    uint32_t kind;       /* solrt_bvh_kind */
+    uint32_t leaf_max;   /* BVH8: max triangles per leaf child (1..3), 0 = 3 */
+    uint32_t reserved[2];
+} solrt_bvh_desc;
+
+typedef struct solrt_bvh_info {
+    uint32_t kind;
+    uint32_t tri_count;
+    uint32_t node_count;
+    uint32_t depth;          /* levels on the longest root-to-leaf path */
+    uint64_t node_bytes;
+    uint64_t tri_bytes;      /* intersection stream, 48 B / triangle */
+    uint64_t shade_bytes;    /* shading stream (vertices, indices, materials) */
+    double build_ms;         /* device time of the last build */
+} solrt_bvh_info;
+
+/* ------------------------------------------------------------------------ */
+/* Camera and per-launch parameters                                         */
+/* ------------------------------------------------------------------------ */
+
+/* The matrices of SceneUniforms (examples/5-pathtrace.rs:9-17) that the ray
+ * generation reads. Column-major, as glam. */
+typedef struct solrt_camera {
+    float view[16];
+    float view_inverse[16];
+    float projection[16];
+    float projection_inverse[16];
+} solrt_camera;
+
+typedef enum solrt_miss_mode {
+    SOLRT_MISS_BLACK = 0,     /* pathtrace.rmiss with ENABLE_SKYLIGHT = 0 */
+    SOLRT_MISS_REF_SKY = 1,   /* pathtrace.rmiss with ENABLE_SKYLIGHT = 1 (--sky) */
+    SOLRT_MISS_GRADIENT = 2   /* mix((1,1,1),(0.5,0.7,1),0.5*(dir.y+1)) */
+} solrt_miss_mode;
+
+typedef enum solrt_material_mode {
+    SOLRT_MATERIAL_REF = 0,     /* pathtrace.rchit: metallic GGX / Fresnel / cosine */
+    SOLRT_MATERIAL_LAMBERT = 1  /* cosine-weighted diffuse only, same 3 draws */
+} solrt_material_mode;
+
+typedef enum solrt_accum_mode {
+    SOLRT_ACCUM_REF_MIX = 0,    /* pathtrace.rgen:89-101 running mix */
+    SOLRT_ACCUM_KAHAN = 1       /* Kahan-compensated per-pixel sample sums */
+} solrt_accum_mode;
+
+typedef enum solrt_rng_mode {
+    /* One TEA-seeded stream per pixel per launch, samples drawn one after the
+     * other: rng = tea(x + y*W, frame) (pathtrace.rgen:47-52). */
+    SOLRT_RNG_REF_STREAM = 0,
+    /* One stream per (pixel, sample): rng = tea(x + y*W, frame*spp + s),
+     * xor tea(seed, job_id) when seed != 0. Samples run concurrently. */
+    SOLRT_RNG_PER_SAMPLE = 1
+} solrt_rng_mode;
+
+typedef struct solrt_render_params {
+    uint32_t width;
+    uint32_t height;
+    uint32_t spp;               /* samples per pixel per launch (reference: 8) */
+    uint32_t max_bounces;       /* reference maxBounces = 32; <= 1024 */
+    uint32_t frame;             /* SceneUniforms.frame.z (elapsed ticks) */
+    uint32_t accum_start_frame; /* push constant of pathtrace.rgen */
+    uint32_t seed;
+    uint32_t job_id;
+    uint32_t miss_mode;         /* solrt_miss_mode */
+    uint32_t material_mode;     /* solrt_material_mode */
+    uint32_t accum_mode;        /* solrt_accum_mode; must match the image */
+    uint32_t rng_mode;          /* solrt_rng_mode */
+    float tmax;                 /* 0 = reference 1e4 */
+    uint32_t reserved[3];
+} solrt_render_params;
+
+/* ------------------------------------------------------------------------ */
+/* Rays for the ray-file (hit record) API                                   */
+/* ------------------------------------------------------------------------ */
+
+typedef struct solrt_ray {
+    float origin[3];
+    float tmin;
+    float dir[3];
+    float tmax;
+} solrt_ray;
+
+/* prim = global triangle index (section triangles are numbered in section
+ * order) or SOLRT_NO_HIT; u, v = barycentrics of vertex 1 and 2 (the
+ * hitAttributeEXT of pathtrace.rchit:58). */
+typedef struct solrt_hit {
+    float t;
+    uint32_t prim;
+    float u;
+    float v;
+} solrt_hit;
+
+#define SOLRT_NO_HIT 0xffffffffu
+
+typedef struct solrt_stats {
+    uint64_t segments;        /* ray segments traced (primary + bounce) */
+    uint64_t paths;           /* camera paths started */
+    uint64_t node_visits;     /* only with counters enabled */
+    uint64_t tri_tests;       /* only with counters enabled */
+    uint64_t fp64_fallbacks;  /* watertight test edge functions recomputed in FP64 */
+    uint64_t launches;        /* kernels launched by the library */
+    uint32_t error_flags;     /* device error word (see solrt_error_bits) */
+    uint32_t reserved;
+    double render_ms;         /* device time of the last solrt_render */
+    double extend_ms;         /* summed device time of extend launches (enable_timing) */
+    double shade_ms;          /* summed device time of shade launches (enable_timing) */
+    uint64_t extend_launches; /* launches timed into extend_ms */
+    uint64_t shade_launches;  /* launches timed into shade_ms */
+} solrt_stats;
+
+typedef enum solrt_error_bits {
+    SOLRT_EFLAG_STACK = 1u,       /* traversal stack overflow (ray dropped) */
+    SOLRT_EFLAG_QUEUE = 2u,       /* wavefront queue overflow */
+    SOLRT_EFLAG_INDEX = 4u,       /* out-of-range node / triangle index */
+    SOLRT_EFLAG_TIMEOUT = 8u      /* a bounded device wait ran out */
+} solrt_error_bits;
+
+/* ------------------------------------------------------------------------ */
+/* Opaque objects                                                           */
+/* ------------------------------------------------------------------------ */
+
+typedef struct solrt_context solrt_context;
+typedef struct solrt_scene solrt_scene;
+typedef struct solrt_image solrt_image;
+typedef struct solrt_server solrt_server;
+
+typedef struct solrt_context_desc {
+    int device;                  /* CUDA ordinal */
+    uint32_t path_capacity;      /* paths in flight per pass; 0 = default (8M) */
+    uint32_t enable_counters;    /* 1 = count node visits / triangle tests */
+    uint32_t block_size;         /* extend kernel block size; 0 = default */
+    uint32_t enable_timing;      /* 1 = CUDA-event timing of every extend / shade launch */
+    uint32_t reserved[3];
+} solrt_context_desc;
+
+/* ------------------------------------------------------------------------ */
+/* Functions                                                                */
+/* ------------------------------------------------------------------------ */
+
+uint32_t solrt_abi_version(void);
+const char* solrt_status_string(solrt_status s);
+/* Message of the last error on this host thread (never NULL). */
+const char* solrt_last_error(void);
+
+/* Context: CUDA device, stream, wavefront queues. Replaces the Vulkan Context
+ * (src/context.rs:222-575) for this path. */
+solrt_status solrt_context_create(const solrt_context_desc* desc, solrt_context** out);
+solrt_status solrt_context_destroy(solrt_context* ctx);
+solrt_status solrt_synchronize(solrt_context* ctx);
+solrt_status solrt_get_stats(solrt_context* ctx, solrt_stats* out);
+solrt_status solrt_reset_stats(solrt_context* ctx);
+/* The CUDA stream (cudaStream_t) of the context, for callers that enqueue
+ * their own work around the library's. */
+void* solrt_context_stream(solrt_context* ctx);
+
+/* Scene: flattens sections to world space (transform, transform_it as in
+ * pathtrace.rchit:80-86), uploads and builds the BVH. Synchronises.
+ * Replaces SceneDescription::from_scene (src/ray/mod.rs:49-57). */
+solrt_status solrt_scene_create(solrt_context* ctx, const solrt_scene_desc* desc,
+                                const solrt_bvh_desc* bvh, solrt_scene** out);
+solrt_status solrt_scene_destroy(solrt_scene* scene);
+/* Rebuilds the BVH (kind may change). Synchronises. Replaces
+ * SceneDescription::tlas_regenerate (src/ray/mod.rs:178-181). */
+solrt_status solrt_scene_build_bvh(solrt_scene* scene, const solrt_bvh_desc* bvh);
+solrt_status solrt_scene_bvh_info(solrt_scene* scene, solrt_bvh_info* out);
+/* Copies the device BVH to host memory (for topology checks). `nodes` gets
+ * node_bytes, `tris` gets tri_bytes; either may be NULL. Synchronises. */
+solrt_status solrt_scene_bvh_export(solrt_scene* scene, void* nodes, size_t nodes_bytes,
+                                    void* tris, size_t tris_bytes);
+/* Device memory held by the scene, in bytes. */
+solrt_status solrt_scene_bytes(solrt_scene* scene, uint64_t* out);
+
+/* Camera matrices (src/scene/camera.rs:98-106: look_at_rh, perspective_rh),
+ * computed in FP64 and rounded to FP32. vfov in degrees. */
+solrt_status solrt_camera_look_at(const float eye[3], const float center[3], const float up[3],
+                                  float vfov_deg, float aspect, float znear, float zfar,
+                                  solrt_camera* out);
+/* Camera from a view matrix, as Camera::from_view (src/scene/camera.rs:73-94). */
+solrt_status solrt_camera_from_view(const float view[16], float vfov_deg, float aspect,
+                                    float znear, float zfar, solrt_camera* out);
+
+/* Images: RGBA32F accumulation + RGBA8 render target (+ Kahan sums). */
+solrt_status solrt_image_create(solrt_context* ctx, uint32_t width, uint32_t height,
+                                uint32_t accum_mode, solrt_image** out);
+solrt_status solrt_image_destroy(solrt_image* img);
+solrt_status solrt_image_clear(solrt_image* img);
+/* Synchronises; either pointer may be NULL. rgba32f: W*H*4 floats,
+ * rgba8: W*H*4 bytes, row-major from pixel (0,0) = gl_LaunchIDEXT (0,0). */
+solrt_status solrt_image_read(solrt_image* img, float* rgba32f, uint8_t* rgba8);
+/* Device pointers of the images (float4 accumulation, uchar4 render). */
+solrt_status solrt_image_device_ptrs(solrt_image* img, void** accum, void** rgba8);
+
+/* One launch of the path tracer: spp samples for every pixel, accumulated
+ * into `img`. Asynchronous on the context stream. */
+solrt_status solrt_render(solrt_context* ctx, solrt_scene* scene, const solrt_camera* camera,
+                          const solrt_render_params* params, solrt_image* img);
+
+/* Closest-hit queries (one traceRayEXT each, opaque, no culling).
+ * Host arrays; synchronises. */
+solrt_status solrt_trace_rays(solrt_context* ctx, solrt_scene* scene, const solrt_ray* rays,
+                              uint32_t n, solrt_hit* hits);
+/* Device arrays; asynchronous on the context stream. */
+solrt_status solrt_trace_rays_device(solrt_context* ctx, solrt_scene* scene,
+                                     const solrt_ray* rays_dev, uint32_t n, solrt_hit* hits_dev);
+
+/* Device-side unit functions for known-answer tests (host in, host out).
+ * op: 0 = tea(a[i], b[i]) -> out_u32; 1 = nextRand sequence of length b[0]
+ * from seed a[0] -> out_f32 + final state in out_u32[0]; 2 = sincos of
+ * in_f32[i] -> out_f32[2i], out_f32[2i+1]. Synchronises. */
+solrt_status solrt_debug_unit(solrt_context* ctx, uint32_t op, uint32_t n, const uint32_t* a,
+                              const uint32_t* b, const float* in_f32, uint32_t* out_u32,
+                              float* out_f32);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SOLRT_H */

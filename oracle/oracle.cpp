@@ -1,0 +1,925 @@
+// oracle.cpp — CPU oracle of the solrt path tracer. TEST INFRASTRUCTURE ONLY.
+//
+// Loaded (through ctypes) by the tests, the smoke check and the CPU-baseline
+// leg of the benchmark, as the checker. Product code never links it.
+//
+// Scalar C++17, templated on the real type R (float for bit-exact parity with
+// the device code, double for the converged FP64 reference images). Built
+// with -ffp-contract=off so that every a*b+c is two rounded operations, which
+// is what the device code does (nvcc -fmad=false). Each function cites the
+// reference line it restates. Parity status is stated in oracle.h.
+
+#include "oracle.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <thread>
+#include <type_traits>
+#include <vector>
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// RNG (assets/glsl/sampling.glsl:18-42)
+// ---------------------------------------------------------------------------
+
+// 16 rounds of TEA on (val0, val1); sampling.glsl:18-32.
+uint32_t tea(uint32_t val0, uint32_t val1) {
+    uint32_t v0 = val0, v1 = val1, s0 = 0;
+    for (int n = 0; n < 16; ++n) {
+        s0 += 0x9e3779b9u;
+        v0 += ((v1 << 4) + 0xa341316cu) ^ (v1 + s0) ^ ((v1 >> 5) + 0xc8013ea4u);
+        v1 += ((v0 << 4) + 0xad90777du) ^ (v0 + s0) ^ ((v0 >> 5) + 0x7e95761eu);
+    }
+    return v0;
+}
+
+// LCG step + PCG RXS-M-XS output; sampling.glsl:35-42.
+uint32_t pcg_word(uint32_t& rng) {
+    rng = rng * 747796405u + 1u;
+    uint32_t word = ((rng >> ((rng >> 28) + 4u)) ^ rng) * 277803737u;
+    word = (word >> 22) ^ word;
+    return word;
+}
+
+template <class R> R next_rand(uint32_t& rng);
+template <> float next_rand<float>(uint32_t& rng) {
+    return (float)pcg_word(rng) / 4294967295.0f;
+}
+template <> double next_rand<double>(uint32_t& rng) {
+    return (double)pcg_word(rng) / 4294967295.0;
+}
+
+// ---------------------------------------------------------------------------
+// sin / cos. The FP32 path uses one fixed polynomial evaluation shared (as a
+// specification, not as code) with the device kernels so that secondary ray
+// directions agree bit for bit: Cody-Waite reduction by pi/2 with a three-part
+// split of pi/2 (8 + 12 + 24 significant bits), then the Taylor series of sin
+// to x^9 and of cos to x^10 on |r| <= pi/4 (truncation < 2e-9), Horner order.
+// The FP64 path uses the C library.
+// ---------------------------------------------------------------------------
+
+void sincos_poly(float x, float& s_out, float& c_out) {
+    const float k = std::rint(x * 0x1.45f306p-1f);  // x * 2/pi
+    float r = x - k * 0x1.92p+0f;                   // pi/2, bits 1-8
+    r = r - k * 0x1.fb4p-12f;                       // pi/2, bits 9-20
+    r = r - k * 0x1.4442d2p-24f;                    // pi/2, next 24 bits
+    const float r2 = r * r;
+    float ps = 0x1.71de3ap-19f;                     //  1/9!
+    ps = ps * r2 + -0x1.a01a02p-13f;                // -1/7!
+    ps = ps * r2 + 0x1.111112p-7f;                  //  1/5!
+    ps = ps * r2 + -0x1.555556p-3f;                 // -1/3!
+    const float s = r + (r * r2) * ps;
+    float pc = -0x1.27e4fcp-22f;                    // -1/10!
+    pc = pc * r2 + 0x1.a01a02p-16f;                 //  1/8!
+    pc = pc * r2 + -0x1.6c16c2p-10f;                // -1/6!
+    pc = pc * r2 + 0x1.555556p-5f;                  //  1/4!
+    pc = pc * r2 + -0.5f;                           // -1/2!
+    const float c = 1.0f + r2 * pc;
+    const int q = ((int)k) & 3;
+    switch (q) {
+        case 0: s_out = s; c_out = c; break;
+        case 1: s_out = c; c_out = -s; break;
+        case 2: s_out = -s; c_out = -c; break;
+        default: s_out = -c; c_out = s; break;
+    }
+}
+
+template <class R> void sincos_r(R x, R& s, R& c);
+template <> void sincos_r<float>(float x, float& s, float& c) { sincos_poly(x, s, c); }
+template <> void sincos_r<double>(double x, double& s, double& c) {
+    s = std::sin(x);
+    c = std::cos(x);
+}
+
+// ---------------------------------------------------------------------------
+// Small vector type with GLSL component-wise semantics. Every expression is
+// written in the evaluation order of the GLSL source.
+// ---------------------------------------------------------------------------
+
+template <class R> struct V3 {
+    R x, y, z;
+    R operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+};
+template <class R> V3<R> v3(R x, R y, R z) { return V3<R>{x, y, z}; }
+template <class R> V3<R> operator+(V3<R> a, V3<R> b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+template <class R> V3<R> operator-(V3<R> a, V3<R> b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+template <class R> V3<R> operator*(V3<R> a, V3<R> b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+template <class R> V3<R> operator*(V3<R> a, R s) { return {a.x * s, a.y * s, a.z * s}; }
+template <class R> V3<R> operator*(R s, V3<R> a) { return {s * a.x, s * a.y, s * a.z}; }
+template <class R> V3<R> operator-(V3<R> a) { return {-a.x, -a.y, -a.z}; }
+template <class R> R dot(V3<R> a, V3<R> b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+template <class R> R length(V3<R> a) { return std::sqrt(dot(a, a)); }
+template <class R> V3<R> normalize(V3<R> a) {
+    const R l = length(a);
+    return {a.x / l, a.y / l, a.z / l};
+}
+template <class R> R saturate(R x) { return std::min(std::max(x, R(0)), R(1)); }
+template <class R> R glsl_sign(R x) { return x > R(0) ? R(1) : (x < R(0) ? R(-1) : R(0)); }
+// GLSL reflect(I, N) = I - 2 * dot(N, I) * N.
+template <class R> V3<R> reflect(V3<R> i, V3<R> n) {
+    const R k = R(2) * dot(n, i);
+    return i - k * n;
+}
+// GLSL mix(x, y, a) = x * (1 - a) + y * a.
+template <class R> V3<R> mix(V3<R> x, V3<R> y, R a) { return x * (R(1) - a) + y * a; }
+template <class R> R smoothstep(R e0, R e1, R x) {
+    R t = (x - e0) / (e1 - e0);
+    t = std::min(std::max(t, R(0)), R(1));
+    return (t * t) * (R(3) - R(2) * t);
+}
+
+// column-major mat4 (as float[16]) times (x, y, z, w), summed column by column.
+template <class R> void mat4_mul(const float* m, R x, R y, R z, R w, R out[4]) {
+    for (int r = 0; r < 4; ++r) {
+        out[r] = ((R(m[0 + r]) * x + R(m[4 + r]) * y) + R(m[8 + r]) * z) + R(m[12 + r]) * w;
+    }
+}
+
+template <class R> R two_pi();
+template <> float two_pi<float>() { return 6.28318530718f; }
+template <> double two_pi<double>() { return 6.28318530718; }
+
+// ---------------------------------------------------------------------------
+// Sampling (assets/glsl/sampling.glsl:52-96)
+// ---------------------------------------------------------------------------
+
+// sampling.glsl:52-64
+template <class R> R fresnel_dielectric(V3<R> i, V3<R> m, R eta) {
+    R result = R(1);
+    const R cos_i = std::abs(dot(i, m));
+    const R sin_o2 = (eta * eta) * (R(1) - cos_i * cos_i);
+    if (sin_o2 <= R(1)) {
+        const R cos_o = std::sqrt(saturate(R(1) - sin_o2));
+        const R rs = (cos_i - eta * cos_o) / (cos_i + eta * cos_o);
+        const R rp = (eta * cos_i - cos_o) / (eta * cos_i + cos_o);
+        result = R(0.5) * (rs * rs + rp * rp);
+    }
+    return result;
+}
+
+// sampling.glsl:66-73 (branchless ONB, Duff et al. 2017)
+template <class R> void onb(V3<R> n, V3<R>& u, V3<R>& v) {
+    const R s = n.z < R(0) ? R(-1) : R(1);
+    const R a = R(-1) / (s + n.z);
+    const R b = n.x * n.y * a;
+    u = V3<R>{R(1) + s * n.x * n.x * a, s * b, -s * n.x};
+    v = V3<R>{b, s + n.y * n.y * a, -n.y};
+}
+
+// sampling.glsl:75-84
+template <class R> V3<R> align_to_direction(V3<R> n, R cos_t, R phi) {
+    const R sin_t = std::sqrt(saturate(R(1) - cos_t * cos_t));
+    V3<R> u, v;
+    onb(n, u, v);
+    R sp, cp;
+    sincos_r(phi, sp, cp);
+    return (u * cp + v * sp) * sin_t + n * cos_t;
+}
+
+// sampling.glsl:86-90
+template <class R> V3<R> sample_ggx(V3<R> n, R xi0, R xi1, R alpha2) {
+    const R cos_t = std::sqrt(saturate((R(1) - xi0) / (xi0 * (alpha2 - R(1)) + R(1))));
+    return align_to_direction(n, cos_t, xi1 * two_pi<R>());
+}
+
+// sampling.glsl:92-96
+template <class R> V3<R> sample_cosine(V3<R> n, R xi0, R xi1) {
+    const R cos_t = std::sqrt(xi0);
+    return align_to_direction(n, cos_t, xi1 * two_pi<R>());
+}
+
+// pathtrace.rmiss:8-21 plus the gradient sky.
+template <class R> V3<R> miss_color(V3<R> dir, uint32_t mode) {
+    if (mode == SOLRT_MISS_REF_SKY) {
+        const V3<R> wi = normalize(dir);
+        const R t = smoothstep(R(0.35f), R(0.65f), R(0.5f) * (wi.y + R(1)));
+        const V3<R> sky = mix(V3<R>{R(0.58f), R(0.45f), R(0.25f)}, V3<R>{R(0.3f), R(0.4f), R(0.5f)}, t);
+        const V3<R> sun_dir = normalize(V3<R>{R(0), R(1), R(-0.25f)});
+        const bool is_sun = dot(wi, sun_dir) > R(0.99f);
+        return mix(sky, V3<R>{R(120), R(100), R(50)}, is_sun ? R(1) : R(0));
+    }
+    if (mode == SOLRT_MISS_GRADIENT) {
+        const V3<R> wi = normalize(dir);
+        const R t = R(0.5f) * (wi.y + R(1));
+        return mix(V3<R>{R(1), R(1), R(1)}, V3<R>{R(0.5f), R(0.7f), R(1)}, t);
+    }
+    return V3<R>{R(0), R(0), R(0)};
+}
+
+// ---------------------------------------------------------------------------
+// Scene
+// ---------------------------------------------------------------------------
+
+struct TriW {
+    V3<float> p[3];  // world-space positions
+    V3<float> n[3];  // world-space (unnormalised) normals
+    V3<float> c[3];  // vertex colours
+    uint32_t mat;
+};
+
+struct Box {
+    float lo[3], hi[3];
+};
+
+}  // namespace
+
+struct oracle_scene {
+    std::vector<TriW> tris;
+    std::vector<solrt_material> mats;
+    // LBVH
+    std::vector<uint32_t> order;         // sorted position -> triangle
+    std::vector<uint32_t> morton;        // sorted codes
+    std::vector<uint32_t> child;         // 2 per internal node
+    std::vector<Box> node_box;           // per internal node
+    std::vector<Box> leaf_box;           // per sorted position
+};
+
+namespace {
+
+// src/ray/mod.rs:113-118 gives each section transform and transform_it;
+// pathtrace.rchit:80-90 applies them to the interpolated normal and position.
+// Here they are applied per vertex before interpolation (equal in exact
+// arithmetic; the device upload does the same in the same order).
+bool flatten(const solrt_scene_desc* d, oracle_scene* s) {
+    static const float ident[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    s->mats.assign(d->materials, d->materials + d->material_count);
+    for (uint32_t si = 0; si < d->section_count; ++si) {
+        const solrt_section& sec = d->sections[si];
+        if (sec.index_count % 3 != 0) return false;
+        if ((uint64_t)sec.vertex_offset + sec.vertex_count > d->vertex_count) return false;
+        if ((uint64_t)sec.index_offset + sec.index_count > d->index_count) return false;
+        if (sec.material_index >= d->material_count) return false;
+        const float* T = d->instances ? d->instances[si].transform : ident;
+        const float* Tit = d->instances ? d->instances[si].transform_it : ident;
+        for (uint32_t t = 0; t < sec.index_count / 3; ++t) {
+            TriW tw;
+            for (int k = 0; k < 3; ++k) {
+                const uint32_t li = d->indices[sec.index_offset + 3 * t + k];
+                if (li >= sec.vertex_count) return false;
+                const solrt_vertex& v = d->vertices[sec.vertex_offset + li];
+                float o[4];
+                mat4_mul<float>(T, v.pos[0], v.pos[1], v.pos[2], 1.0f, o);
+                tw.p[k] = V3<float>{o[0], o[1], o[2]};
+                mat4_mul<float>(Tit, v.normal[0], v.normal[1], v.normal[2], 0.0f, o);
+                tw.n[k] = V3<float>{o[0], o[1], o[2]};
+                tw.c[k] = V3<float>{v.color[0], v.color[1], v.color[2]};
+            }
+            tw.mat = sec.material_index;
+            s->tris.push_back(tw);
+        }
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// LBVH (Karras 2012): 30-bit Morton codes of triangle centroids normalised to
+// the centroid bounds, stable sort, radix-tree hierarchy, bottom-up boxes.
+// ---------------------------------------------------------------------------
+
+uint32_t expand_bits10(uint32_t v) {
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+uint32_t quantise10(float c, float lo, float ext) {
+    if (!(ext > 0.0f)) return 0;
+    const float f = ((c - lo) / ext) * 1024.0f;
+    if (f >= 1023.0f) return 1023;
+    if (!(f > 0.0f)) return 0;
+    return (uint32_t)f;
+}
+
+int clz32(uint32_t x) { return x == 0 ? 32 : __builtin_clz(x); }
+
+void build_lbvh(oracle_scene* s) {
+    const uint32_t n = (uint32_t)s->tris.size();
+    s->order.clear(); s->morton.clear(); s->child.clear(); s->node_box.clear(); s->leaf_box.clear();
+    if (n == 0) return;
+    std::vector<V3<float>> cen(n);
+    float cmin[3] = {INFINITY, INFINITY, INFINITY}, cmax[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t i = 0; i < n; ++i) {
+        const TriW& t = s->tris[i];
+        cen[i] = V3<float>{((t.p[0].x + t.p[1].x) + t.p[2].x) / 3.0f,
+                           ((t.p[0].y + t.p[1].y) + t.p[2].y) / 3.0f,
+                           ((t.p[0].z + t.p[1].z) + t.p[2].z) / 3.0f};
+        for (int a = 0; a < 3; ++a) {
+            cmin[a] = std::min(cmin[a], cen[i][a]);
+            cmax[a] = std::max(cmax[a], cen[i][a]);
+        }
+    }
+    const float ext[3] = {cmax[0] - cmin[0], cmax[1] - cmin[1], cmax[2] - cmin[2]};
+    std::vector<uint32_t> code(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        const uint32_t qx = quantise10(cen[i].x, cmin[0], ext[0]);
+        const uint32_t qy = quantise10(cen[i].y, cmin[1], ext[1]);
+        const uint32_t qz = quantise10(cen[i].z, cmin[2], ext[2]);
+        code[i] = (expand_bits10(qx) << 2) | (expand_bits10(qy) << 1) | expand_bits10(qz);
+    }
+    s->order.resize(n);
+    for (uint32_t i = 0; i < n; ++i) s->order[i] = i;
+    std::stable_sort(s->order.begin(), s->order.end(),
+                     [&](uint32_t a, uint32_t b) { return code[a] < code[b]; });
+    s->morton.resize(n);
+    for (uint32_t k = 0; k < n; ++k) s->morton[k] = code[s->order[k]];
+    s->leaf_box.resize(n);
+    for (uint32_t k = 0; k < n; ++k) {
+        const TriW& t = s->tris[s->order[k]];
+        for (int a = 0; a < 3; ++a) {
+            s->leaf_box[k].lo[a] = std::min(std::min(t.p[0][a], t.p[1][a]), t.p[2][a]);
+            s->leaf_box[k].hi[a] = std::max(std::max(t.p[0][a], t.p[1][a]), t.p[2][a]);
+        }
+    }
+    if (n == 1) return;
+    const uint32_t* k = s->morton.data();
+    auto delta = [&](int64_t i, int64_t j) -> int {
+        if (j < 0 || j > (int64_t)n - 1) return -1;
+        const uint32_t a = k[i], b = k[j];
+        if (a == b) return 32 + clz32((uint32_t)i ^ (uint32_t)j);
+        return clz32(a ^ b);
+    };
+    s->child.assign(2 * (n - 1), 0);
+    std::vector<uint32_t> parent_int(n - 1, 0xffffffffu), parent_leaf(n, 0xffffffffu);
+    for (int64_t i = 0; i < (int64_t)n - 1; ++i) {
+        const int d = (delta(i, i + 1) - delta(i, i - 1)) >= 0 ? 1 : -1;
+        const int dmin = delta(i, i - d);
+        int64_t lmax = 2;
+        while (delta(i, i + lmax * d) > dmin) lmax *= 2;
+        int64_t l = 0;
+        for (int64_t t = lmax / 2; t >= 1; t /= 2)
+            if (delta(i, i + (l + t) * d) > dmin) l += t;
+        const int64_t j = i + l * d;
+        const int dnode = delta(i, j);
+        int64_t sp = 0, t = l;
+        do {
+            t = (t + 1) >> 1;
+            if (delta(i, i + (sp + t) * d) > dnode) sp += t;
+        } while (t > 1);
+        const int64_t gamma = i + sp * d + std::min(d, 0);
+        const int64_t lo = std::min(i, j), hi = std::max(i, j);
+        uint32_t left, right;
+        if (lo == gamma) { left = 0x80000000u | (uint32_t)gamma; parent_leaf[gamma] = (uint32_t)i; }
+        else { left = (uint32_t)gamma; parent_int[gamma] = (uint32_t)i; }
+        if (hi == gamma + 1) { right = 0x80000000u | (uint32_t)(gamma + 1); parent_leaf[gamma + 1] = (uint32_t)i; }
+        else { right = (uint32_t)(gamma + 1); parent_int[gamma + 1] = (uint32_t)i; }
+        s->child[2 * i] = left;
+        s->child[2 * i + 1] = right;
+    }
+    // bottom-up boxes: a node is complete when both children are.
+    s->node_box.assign(n - 1, Box{});
+    std::vector<uint8_t> arrived(n - 1, 0);
+    auto box_of = [&](uint32_t ref) -> const Box& {
+        return (ref & 0x80000000u) ? s->leaf_box[ref & 0x7fffffffu] : s->node_box[ref];
+    };
+    for (uint32_t leaf = 0; leaf < n; ++leaf) {
+        uint32_t p = parent_leaf[leaf];
+        while (p != 0xffffffffu) {
+            if (++arrived[p] < 2) break;
+            const Box& a = box_of(s->child[2 * p]);
+            const Box& b = box_of(s->child[2 * p + 1]);
+            for (int ax = 0; ax < 3; ++ax) {
+                s->node_box[p].lo[ax] = std::min(a.lo[ax], b.lo[ax]);
+                s->node_box[p].hi[ax] = std::max(a.hi[ax], b.hi[ax]);
+            }
+            p = parent_int[p];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Watertight ray-triangle test (Woop, Benthin, Wald, JCGT 2013), no culling
+// (TRIANGLE_FACING_CULL_DISABLE, src/ray/acceleration.rs:337). Zero edge
+// functions are recomputed in FP64 (products of floats are exact there).
+// Closest hit: smaller t, then lower global triangle index.
+// ---------------------------------------------------------------------------
+
+template <class R> struct RayWT {
+    V3<R> o, d;
+    R tmin;
+    int kx, ky, kz;
+    R sx, sy, sz;
+};
+
+template <class R> RayWT<R> setup_ray(V3<R> o, V3<R> d, R tmin) {
+    RayWT<R> r;
+    r.o = o; r.d = d; r.tmin = tmin;
+    int kz = 0;
+    if (std::abs(d.y) > std::abs(d[kz])) kz = 1;
+    if (std::abs(d.z) > std::abs(d[kz])) kz = 2;
+    int kx = kz + 1; if (kx == 3) kx = 0;
+    int ky = kx + 1; if (ky == 3) ky = 0;
+    if (d[kz] < R(0)) std::swap(kx, ky);
+    r.kx = kx; r.ky = ky; r.kz = kz;
+    r.sx = d[kx] / d[kz];
+    r.sy = d[ky] / d[kz];
+    r.sz = R(1) / d[kz];
+    return r;
+}
+
+template <class R> struct HitR {
+    R t;
+    uint32_t prim;
+    R u, v;
+};
+
+template <class R>
+inline void intersect_tri(const RayWT<R>& r, const TriW& tri, uint32_t prim, HitR<R>& best, uint64_t& fb) {
+    const V3<R> p0{R(tri.p[0].x), R(tri.p[0].y), R(tri.p[0].z)};
+    const V3<R> p1{R(tri.p[1].x), R(tri.p[1].y), R(tri.p[1].z)};
+    const V3<R> p2{R(tri.p[2].x), R(tri.p[2].y), R(tri.p[2].z)};
+    const V3<R> A = p0 - r.o, B = p1 - r.o, C = p2 - r.o;
+    const R ax = A[r.kx] - r.sx * A[r.kz], ay = A[r.ky] - r.sy * A[r.kz];
+    const R bx = B[r.kx] - r.sx * B[r.kz], by = B[r.ky] - r.sy * B[r.kz];
+    const R cx = C[r.kx] - r.sx * C[r.kz], cy = C[r.ky] - r.sy * C[r.kz];
+    R U = cx * by - cy * bx;
+    R V = ax * cy - ay * cx;
+    R W = bx * ay - by * ax;
+    if (std::is_same<R, float>::value && (U == R(0) || V == R(0) || W == R(0))) {
+        ++fb;
+        U = (R)((double)cx * (double)by - (double)cy * (double)bx);
+        V = (R)((double)ax * (double)cy - (double)ay * (double)cx);
+        W = (R)((double)bx * (double)ay - (double)by * (double)ax);
+    }
+    if ((U < R(0) || V < R(0) || W < R(0)) && (U > R(0) || V > R(0) || W > R(0))) return;
+    const R det = (U + V) + W;
+    if (det == R(0)) return;
+    const R az = r.sz * A[r.kz], bz = r.sz * B[r.kz], cz = r.sz * C[r.kz];
+    const R T = (U * az + V * bz) + W * cz;
+    const R t = T / det;
+    if (!(t > r.tmin)) return;
+    if (t < best.t || (t == best.t && prim < best.prim)) {
+        best.t = t;
+        best.prim = prim;
+        best.u = V / det;
+        best.v = W / det;
+    }
+}
+
+// Slab test against a float box, conservative: the far distance is widened
+// by a relative 2^-16 so rounding never culls a box that holds the hit.
+template <class R> inline bool box_hit(const Box& b, V3<R> o, V3<R> inv, R tmin, R tmax, R& tnear) {
+    R tn = tmin, tf = tmax;
+    for (int a = 0; a < 3; ++a) {
+        const R t0 = (R(b.lo[a]) - o[a]) * inv[a];
+        const R t1 = (R(b.hi[a]) - o[a]) * inv[a];
+        const R lo = std::fmin(t0, t1), hi = std::fmax(t0, t1);
+        tn = std::fmax(tn, lo);
+        tf = std::fmin(tf, hi);
+    }
+    tnear = tn;
+    return tn <= tf * R(1.0000153);
+}
+
+template <class R> HitR<R> closest_hit(const oracle_scene* s, V3<R> o, V3<R> d, R tmin, R tmax,
+                                       int mode, uint64_t& fb, uint64_t& nv, uint64_t& nt) {
+    HitR<R> best{tmax, SOLRT_NO_HIT, R(0), R(0)};
+    const RayWT<R> r = setup_ray(o, d, tmin);
+    const uint32_t n = (uint32_t)s->tris.size();
+    if (n == 0) return best;
+    if (mode == 0 || n == 1) {
+        for (uint32_t i = 0; i < n; ++i) { ++nt; intersect_tri(r, s->tris[i], i, best, fb); }
+        return best;
+    }
+    const V3<R> inv{R(1) / d.x, R(1) / d.y, R(1) / d.z};
+    // Depth-first, nearer child first; both child boxes are tested at the
+    // parent. The stack holds at most one entry per level.
+    uint32_t stack[256];
+    int sp = 0;
+    uint32_t cur = 0;
+    for (;;) {
+        if (cur & 0x80000000u) {
+            const uint32_t k = cur & 0x7fffffffu;
+            ++nt;
+            intersect_tri(r, s->tris[s->order[k]], s->order[k], best, fb);
+        } else {
+            ++nv;
+            const uint32_t a = s->child[2 * cur], b = s->child[2 * cur + 1];
+            const Box& ba = (a & 0x80000000u) ? s->leaf_box[a & 0x7fffffffu] : s->node_box[a];
+            const Box& bb = (b & 0x80000000u) ? s->leaf_box[b & 0x7fffffffu] : s->node_box[b];
+            R ta, tb;
+            const bool ha = box_hit(ba, o, inv, tmin, best.t, ta);
+            const bool hb = box_hit(bb, o, inv, tmin, best.t, tb);
+            if (ha && hb) {
+                const bool swap = tb < ta;
+                if (sp < 256) stack[sp++] = swap ? a : b;
+                cur = swap ? b : a;
+                continue;
+            }
+            if (ha) { cur = a; continue; }
+            if (hb) { cur = b; continue; }
+        }
+        if (sp == 0) break;
+        cur = stack[--sp];
+    }
+    return best;
+}
+
+// ---------------------------------------------------------------------------
+// Path tracing (pathtrace.rgen:39-104, .rchit:56-113, .rmiss:8-21)
+// ---------------------------------------------------------------------------
+
+struct Counters {
+    uint64_t seg = 0, paths = 0, fb = 0, nv = 0, nt = 0;
+};
+
+template <class R> V3<R> trace_path(const oracle_scene* s, const solrt_render_params* p, V3<R> o,
+                                    V3<R> d, R tmin, R tmax, uint32_t& rng, Counters& cn) {
+    V3<R> acc{R(1), R(1), R(1)};
+    uint32_t depth = 0;
+    for (;;) {
+        const HitR<R> h = closest_hit<R>(s, o, d, tmin, tmax, 1, cn.fb, cn.nv, cn.nt);
+        ++cn.seg;
+        if (h.prim == SOLRT_NO_HIT) {                       // pathtrace.rmiss
+            acc = acc * miss_color<R>(d, p->miss_mode);
+            break;
+        }
+        const TriW& tri = s->tris[h.prim];                  // pathtrace.rchit
+        const solrt_material& m = s->mats[tri.mat];
+        if (m.emissive[0] >= 1.0f || m.emissive[1] >= 1.0f || m.emissive[2] >= 1.0f) {
+            acc = acc * V3<R>{R(m.emissive[0]), R(m.emissive[1]), R(m.emissive[2])};
+            break;
+        }
+        const R b1 = h.u, b2 = h.v;
+        const R b0 = (R(1) - b1) - b2;
+        auto cv = [](V3<float> a) { return V3<R>{R(a.x), R(a.y), R(a.z)}; };
+        V3<R> normal = cv(tri.n[0]) * b0 + cv(tri.n[1]) * b1 + cv(tri.n[2]) * b2;
+        normal = normalize(normal);
+        const V3<R> pos = cv(tri.p[0]) * b0 + cv(tri.p[1]) * b1 + cv(tri.p[2]) * b2;
+        const V3<R> vcol = cv(tri.c[0]) * b0 + cv(tri.c[1]) * b1 + cv(tri.c[2]) * b2;
+        const V3<R> wi = normalize(d);
+        const V3<R> n_o = normal * glsl_sign(dot(normal, -wi));
+        const R alpha2 = R(m.roughness) * R(m.roughness);
+        const R xi0 = next_rand<R>(rng);
+        const R xi1 = next_rand<R>(rng);
+        const R rnd = next_rand<R>(rng);
+        const V3<R> base{R(m.base_color[0]), R(m.base_color[1]), R(m.base_color[2])};
+        o = pos + R(0.0001f) * n_o;
+        V3<R> hv;
+        if (p->material_mode == SOLRT_MATERIAL_LAMBERT) {
+            d = sample_cosine(n_o, xi0, xi1);
+            hv = base * vcol;
+        } else if (rnd < R(m.metallic)) {
+            d = sample_ggx(reflect(d, n_o), xi0, xi1, alpha2);
+            hv = base * vcol;
+        } else {
+            const V3<R> mh = sample_ggx(n_o, xi0, xi1, alpha2);
+            if (rnd < fresnel_dielectric(n_o, mh, R(1.0f / 1.5f))) {
+                d = reflect(d, mh);
+                hv = V3<R>{R(1), R(1), R(1)};
+            } else {
+                d = sample_cosine(n_o, xi0, xi1);
+                hv = base * vcol;
+            }
+        }
+        ++depth;
+        acc = acc * hv;                                     // pathtrace.rgen:77
+        if (depth > p->max_bounces) {                       // pathtrace.rgen:81-84
+            acc = V3<R>{R(0), R(0), R(0)};
+            break;
+        }
+    }
+    return acc;
+}
+
+template <class R> struct Cam {
+    const solrt_camera* c;
+};
+
+// Camera ray of pathtrace.rgen:52-60.
+template <class R> void camera_ray(const solrt_camera* cam, uint32_t x, uint32_t y, uint32_t W, uint32_t H,
+                                   uint32_t& rng, V3<R>& o, V3<R>& d, R& tmin) {
+    const R j0 = next_rand<R>(rng);
+    const R j1 = next_rand<R>(rng);
+    const R px = R(x) + j0, py = R(y) + j1;
+    const R ux = px / R(W), uy = py / R(H);
+    const R dx = ux * R(2) - R(1), dy = uy * R(2) - R(1);
+    R org[4], tgt[4], dir[4];
+    mat4_mul<R>(cam->view_inverse, R(0), R(0), R(0), R(1), org);
+    mat4_mul<R>(cam->projection_inverse, dx, dy, R(1), R(1), tgt);
+    const V3<R> tn = normalize(V3<R>{tgt[0], tgt[1], tgt[2]});
+    mat4_mul<R>(cam->view_inverse, tn.x, tn.y, tn.z, R(0), dir);
+    o = V3<R>{org[0], org[1], org[2]};
+    d = V3<R>{dir[0], dir[1], dir[2]};
+    tmin = std::max(R(1), length(o)) * R(1e-3f);            // pathtrace.rgen:35
+}
+
+inline uint32_t sample_seed(const solrt_render_params* p, uint32_t pix, uint32_t s) {
+    uint32_t rng = tea(pix, p->frame * p->spp + s);
+    if (p->seed != 0) rng ^= tea(p->seed, p->job_id);
+    return rng;
+}
+
+template <class R> bool finite3(V3<R> c) {
+    return std::isfinite(c.x) && std::isfinite(c.y) && std::isfinite(c.z);
+}
+
+float gamma_f(float c, float power) { return std::pow(c, 1.0f / power); }
+
+uint8_t to_unorm8(float c) {
+    const float cl = std::min(std::max(c, 0.0f), 1.0f);
+    return (uint8_t)(cl * 255.0f + 0.5f);
+}
+
+template <class R>
+void render_pixel(const oracle_scene* s, const solrt_camera* cam, const solrt_render_params* p, uint32_t x,
+                  uint32_t y, float* accum, float* ksum, float* kcomp, uint8_t* rgba8, float* samples_out,
+                  Counters& cn) {
+    const uint32_t W = p->width, H = p->height, pix = x + y * W;
+    const R tmax = p->tmax > 0.0f ? R(p->tmax) : R(10000.0f);
+    uint32_t rng = tea(pix, p->frame);                     // pathtrace.rgen:47
+    V3<R> sum{R(0), R(0), R(0)};
+    V3<R> kc{R(0), R(0), R(0)};
+    V3<R> ks{R(0), R(0), R(0)};
+    R kn = R(0);
+    if (ksum) {
+        ks = V3<R>{R(ksum[4 * pix]), R(ksum[4 * pix + 1]), R(ksum[4 * pix + 2])};
+        kn = R(ksum[4 * pix + 3]);
+        kc = V3<R>{R(kcomp[4 * pix]), R(kcomp[4 * pix + 1]), R(kcomp[4 * pix + 2])};
+    }
+    for (uint32_t si = 0; si < p->spp; ++si) {              // pathtrace.rgen:49
+        if (p->rng_mode == SOLRT_RNG_PER_SAMPLE) rng = sample_seed(p, pix, si);
+        V3<R> o, d;
+        R tmin;
+        camera_ray<R>(cam, x, y, W, H, rng, o, d, tmin);
+        ++cn.paths;
+        const V3<R> c = trace_path<R>(s, p, o, d, tmin, tmax, rng, cn);
+        if (samples_out) {
+            float* so = samples_out + 4 * ((size_t)pix * p->spp + si);
+            so[0] = (float)c.x; so[1] = (float)c.y; so[2] = (float)c.z; so[3] = 1.0f;
+        }
+        if (p->accum_mode == SOLRT_ACCUM_KAHAN) {
+            if (finite3(c)) {
+                const V3<R> yv = c - kc;
+                const V3<R> t = ks + yv;
+                kc = (t - ks) - yv;
+                ks = t;
+                kn = kn + R(1);
+            }
+        } else {
+            sum = sum + c;                                  // pathtrace.rgen:86
+        }
+    }
+    if (samples_out) return;
+    V3<R> out;
+    const V3<R> old{R(accum[4 * pix]), R(accum[4 * pix + 1]), R(accum[4 * pix + 2])};
+    if (p->accum_mode == SOLRT_ACCUM_KAHAN) {
+        ksum[4 * pix] = (float)ks.x; ksum[4 * pix + 1] = (float)ks.y; ksum[4 * pix + 2] = (float)ks.z;
+        ksum[4 * pix + 3] = (float)kn;
+        kcomp[4 * pix] = (float)kc.x; kcomp[4 * pix + 1] = (float)kc.y; kcomp[4 * pix + 2] = (float)kc.z;
+        kcomp[4 * pix + 3] = 0.0f;
+        out = kn > R(0) ? V3<R>{ks.x / kn, ks.y / kn, ks.z / kn} : old;
+    } else {
+        const V3<R> mean = (R(1) / R(p->spp)) * sum;        // pathtrace.rgen:88
+        const R alpha = R(1) / R((uint32_t)(p->frame + 1u - p->accum_start_frame));
+        out = mix(old, mean, alpha);                        // pathtrace.rgen:89-92
+        if (std::isnan(out.x) || std::isnan(out.y) || std::isnan(out.z)) out = old;
+        if (std::isinf(out.x) || std::isinf(out.y) || std::isinf(out.z)) out = old;
+    }
+    const float of[3] = {(float)out.x, (float)out.y, (float)out.z};
+    accum[4 * pix] = of[0]; accum[4 * pix + 1] = of[1]; accum[4 * pix + 2] = of[2]; accum[4 * pix + 3] = 1.0f;
+    for (int c = 0; c < 3; ++c) rgba8[4 * pix + c] = to_unorm8(gamma_f(of[c], 2.2f));  // pathtrace.rgen:102-103
+    rgba8[4 * pix + 3] = 255;
+}
+
+template <class F> void parallel_for(uint32_t n, int threads, F&& f) {
+    if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    if (threads == 1 || n < 2) {
+        for (uint32_t i = 0; i < n; ++i) f(i, 0);
+        return;
+    }
+    std::atomic<uint32_t> next{0};
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; ++t) {
+        pool.emplace_back([&, t]() {
+            for (;;) {
+                const uint32_t i = next.fetch_add(1);
+                if (i >= n) break;
+                f(i, t);
+            }
+        });
+    }
+    for (auto& th : pool) th.join();
+}
+
+int resolve_threads(int threads) {
+    return threads > 0 ? threads : (int)std::max(1u, std::thread::hardware_concurrency());
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C API
+// ---------------------------------------------------------------------------
+
+extern "C" {
+
+oracle_scene* oracle_scene_create(const solrt_scene_desc* desc) {
+    if (!desc) return nullptr;
+    oracle_scene* s = new oracle_scene();
+    if (!flatten(desc, s)) {
+        delete s;
+        return nullptr;
+    }
+    build_lbvh(s);
+    return s;
+}
+
+void oracle_scene_destroy(oracle_scene* s) { delete s; }
+
+uint32_t oracle_scene_tri_count(const oracle_scene* s) { return (uint32_t)s->tris.size(); }
+
+int oracle_scene_export_world(const oracle_scene* s, float* tw, uint32_t* tm) {
+    for (size_t i = 0; i < s->tris.size(); ++i) {
+        const TriW& t = s->tris[i];
+        float* o = tw + 36 * i;
+        for (int k = 0; k < 3; ++k) {
+            o[12 * k + 0] = t.p[k].x; o[12 * k + 1] = t.p[k].y; o[12 * k + 2] = t.p[k].z; o[12 * k + 3] = 0;
+            o[12 * k + 4] = t.n[k].x; o[12 * k + 5] = t.n[k].y; o[12 * k + 6] = t.n[k].z; o[12 * k + 7] = 0;
+            o[12 * k + 8] = t.c[k].x; o[12 * k + 9] = t.c[k].y; o[12 * k + 10] = t.c[k].z; o[12 * k + 11] = 0;
+        }
+        if (tm) tm[i] = t.mat;
+    }
+    return 0;
+}
+
+uint32_t oracle_bvh_export(const oracle_scene* s, uint32_t* child_refs, float* boxes, uint32_t* order,
+                           uint32_t* morton) {
+    const uint32_t n = (uint32_t)s->tris.size();
+    const uint32_t ni = n > 1 ? n - 1 : 0;
+    for (uint32_t i = 0; i < ni; ++i) {
+        if (child_refs) { child_refs[2 * i] = s->child[2 * i]; child_refs[2 * i + 1] = s->child[2 * i + 1]; }
+        if (boxes) {
+            for (int a = 0; a < 3; ++a) {
+                boxes[6 * i + a] = s->node_box[i].lo[a];
+                boxes[6 * i + 3 + a] = s->node_box[i].hi[a];
+            }
+        }
+    }
+    for (uint32_t k = 0; k < n; ++k) {
+        if (order) order[k] = s->order[k];
+        if (morton) morton[k] = s->morton[k];
+    }
+    return ni;
+}
+
+int oracle_trace(const oracle_scene* s, const solrt_ray* rays, uint32_t n, solrt_hit* hits, int mode,
+                 int threads, uint64_t* fp64_fallbacks) {
+    threads = resolve_threads(threads);
+    std::vector<uint64_t> fb(threads, 0);
+    const uint32_t chunk = 1024;
+    const uint32_t nchunks = (n + chunk - 1) / chunk;
+    parallel_for(nchunks, threads, [&](uint32_t c, int t) {
+        uint64_t nv = 0, nt = 0;
+        for (uint32_t i = c * chunk; i < std::min(n, (c + 1) * chunk); ++i) {
+            const solrt_ray& r = rays[i];
+            const HitR<float> h = closest_hit<float>(s, V3<float>{r.origin[0], r.origin[1], r.origin[2]},
+                                                     V3<float>{r.dir[0], r.dir[1], r.dir[2]}, r.tmin, r.tmax,
+                                                     mode, fb[t], nv, nt);
+            hits[i].t = h.prim == SOLRT_NO_HIT ? r.tmax : h.t;
+            hits[i].prim = h.prim;
+            hits[i].u = h.u;
+            hits[i].v = h.v;
+        }
+    });
+    if (fp64_fallbacks) {
+        uint64_t tot = 0;
+        for (uint64_t v : fb) tot += v;
+        *fp64_fallbacks = tot;
+    }
+    return 0;
+}
+
+static int render_impl(const oracle_scene* s, const solrt_camera* cam, const solrt_render_params* p, float* accum,
+                       float* ksum, float* kcomp, uint8_t* rgba8, float* samples_out, int precision,
+                       int threads, uint32_t row_begin, uint32_t row_end, oracle_render_stats* stats) {
+    if (!s || !cam || !p || p->width == 0 || p->height == 0 || p->spp == 0) return 1;
+    if (!samples_out && (!accum || !rgba8)) return 1;
+    if (!samples_out && p->accum_mode == SOLRT_ACCUM_KAHAN && (!ksum || !kcomp)) return 1;
+    if (row_end <= row_begin) { row_begin = 0; row_end = p->height; }
+    row_end = std::min(row_end, p->height);
+    threads = resolve_threads(threads);
+    std::vector<Counters> cn(threads);
+    const uint32_t rows = row_end - row_begin;
+    parallel_for(rows, threads, [&](uint32_t r, int t) {
+        const uint32_t y = row_begin + r;
+        for (uint32_t x = 0; x < p->width; ++x) {
+            if (precision == 64)
+                render_pixel<double>(s, cam, p, x, y, accum, ksum, kcomp, rgba8, samples_out, cn[t]);
+            else
+                render_pixel<float>(s, cam, p, x, y, accum, ksum, kcomp, rgba8, samples_out, cn[t]);
+        }
+    });
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        for (const Counters& c : cn) {
+            stats->segments += c.seg;
+            stats->paths += c.paths;
+            stats->fp64_fallbacks += c.fb;
+            stats->node_visits += c.nv;
+            stats->tri_tests += c.nt;
+        }
+    }
+    return 0;
+}
+
+int oracle_render(const oracle_scene* s, const solrt_camera* cam, const solrt_render_params* p, float* accum,
+                  float* kahan_sum, float* kahan_comp, uint8_t* rgba8, int precision, int threads,
+                  uint32_t row_begin, uint32_t row_end, oracle_render_stats* stats) {
+    return render_impl(s, cam, p, accum, kahan_sum, kahan_comp, rgba8, nullptr, precision, threads, row_begin,
+                       row_end, stats);
+}
+
+int oracle_render_samples(const oracle_scene* s, const solrt_camera* cam, const solrt_render_params* p,
+                          float* out, int precision, int threads) {
+    return render_impl(s, cam, p, nullptr, nullptr, nullptr, nullptr, out, precision, threads, 0, 0, nullptr);
+}
+
+uint32_t oracle_tea(uint32_t a, uint32_t b) { return tea(a, b); }
+float oracle_next_rand(uint32_t* state) { return next_rand<float>(*state); }
+void oracle_sincos(float x, float* s, float* c) { sincos_poly(x, *s, *c); }
+
+void oracle_sample_ggx(const float n[3], float xi0, float xi1, float alpha2, float out[3]) {
+    const V3<float> r = sample_ggx(V3<float>{n[0], n[1], n[2]}, xi0, xi1, alpha2);
+    out[0] = r.x; out[1] = r.y; out[2] = r.z;
+}
+void oracle_sample_cosine(const float n[3], float xi0, float xi1, float out[3]) {
+    const V3<float> r = sample_cosine(V3<float>{n[0], n[1], n[2]}, xi0, xi1);
+    out[0] = r.x; out[1] = r.y; out[2] = r.z;
+}
+float oracle_fresnel(const float i[3], const float m[3], float eta) {
+    return fresnel_dielectric(V3<float>{i[0], i[1], i[2]}, V3<float>{m[0], m[1], m[2]}, eta);
+}
+void oracle_onb(const float n[3], float u[3], float v[3]) {
+    V3<float> a, b;
+    onb(V3<float>{n[0], n[1], n[2]}, a, b);
+    u[0] = a.x; u[1] = a.y; u[2] = a.z;
+    v[0] = b.x; v[1] = b.y; v[2] = b.z;
+}
+float oracle_gamma(float c, float power) { return gamma_f(c, power); }
+void oracle_miss(const float dir[3], uint32_t mode, float out[3]) {
+    const V3<float> r = miss_color<float>(V3<float>{dir[0], dir[1], dir[2]}, mode);
+    out[0] = r.x; out[1] = r.y; out[2] = r.z;
+}
+
+// glam Mat4::look_at_rh / perspective_rh (src/scene/camera.rs:98-106), in
+// FP64, rounded to FP32; inverses by cofactor expansion in FP64.
+static void inv4(const double* m, double* o) {
+    double inv[16];
+    inv[0] = m[5] * m[10] * m[15] - m[5] * m[11] * m[14] - m[9] * m[6] * m[15] + m[9] * m[7] * m[14] + m[13] * m[6] * m[11] - m[13] * m[7] * m[10];
+    inv[4] = -m[4] * m[10] * m[15] + m[4] * m[11] * m[14] + m[8] * m[6] * m[15] - m[8] * m[7] * m[14] - m[12] * m[6] * m[11] + m[12] * m[7] * m[10];
+    inv[8] = m[4] * m[9] * m[15] - m[4] * m[11] * m[13] - m[8] * m[5] * m[15] + m[8] * m[7] * m[13] + m[12] * m[5] * m[11] - m[12] * m[7] * m[9];
+    inv[12] = -m[4] * m[9] * m[14] + m[4] * m[10] * m[13] + m[8] * m[5] * m[14] - m[8] * m[6] * m[13] - m[12] * m[5] * m[10] + m[12] * m[6] * m[9];
+    inv[1] = -m[1] * m[10] * m[15] + m[1] * m[11] * m[14] + m[9] * m[2] * m[15] - m[9] * m[3] * m[14] - m[13] * m[2] * m[11] + m[13] * m[3] * m[10];
+    inv[5] = m[0] * m[10] * m[15] - m[0] * m[11] * m[14] - m[8] * m[2] * m[15] + m[8] * m[3] * m[14] + m[12] * m[2] * m[11] - m[12] * m[3] * m[10];
+    inv[9] = -m[0] * m[9] * m[15] + m[0] * m[11] * m[13] + m[8] * m[1] * m[15] - m[8] * m[3] * m[13] - m[12] * m[1] * m[11] + m[12] * m[3] * m[9];
+    inv[13] = m[0] * m[9] * m[14] - m[0] * m[10] * m[13] - m[8] * m[1] * m[14] + m[8] * m[2] * m[13] + m[12] * m[1] * m[10] - m[12] * m[2] * m[9];
+    inv[2] = m[1] * m[6] * m[15] - m[1] * m[7] * m[14] - m[5] * m[2] * m[15] + m[5] * m[3] * m[14] + m[13] * m[2] * m[7] - m[13] * m[3] * m[6];
+    inv[6] = -m[0] * m[6] * m[15] + m[0] * m[7] * m[14] + m[4] * m[2] * m[15] - m[4] * m[3] * m[14] - m[12] * m[2] * m[7] + m[12] * m[3] * m[6];
+    inv[10] = m[0] * m[5] * m[15] - m[0] * m[7] * m[13] - m[4] * m[1] * m[15] + m[4] * m[3] * m[13] + m[12] * m[1] * m[7] - m[12] * m[3] * m[5];
+    inv[14] = -m[0] * m[5] * m[14] + m[0] * m[6] * m[13] + m[4] * m[1] * m[14] - m[4] * m[2] * m[13] - m[12] * m[1] * m[6] + m[12] * m[2] * m[5];
+    inv[3] = -m[1] * m[6] * m[11] + m[1] * m[7] * m[10] + m[5] * m[2] * m[11] - m[5] * m[3] * m[10] - m[9] * m[2] * m[7] + m[9] * m[3] * m[6];
+    inv[7] = m[0] * m[6] * m[11] - m[0] * m[7] * m[10] - m[4] * m[2] * m[11] + m[4] * m[3] * m[10] + m[8] * m[2] * m[7] - m[8] * m[3] * m[6];
+    inv[11] = -m[0] * m[5] * m[11] + m[0] * m[7] * m[9] + m[4] * m[1] * m[11] - m[4] * m[3] * m[9] - m[8] * m[1] * m[7] + m[8] * m[3] * m[5];
+    inv[15] = m[0] * m[5] * m[10] - m[0] * m[6] * m[9] - m[4] * m[1] * m[10] + m[4] * m[2] * m[9] + m[8] * m[1] * m[6] - m[8] * m[2] * m[5];
+    const double det = m[0] * inv[0] + m[1] * inv[4] + m[2] * inv[8] + m[3] * inv[12];
+    for (int i = 0; i < 16; ++i) o[i] = inv[i] / det;
+}
+
+void oracle_camera_look_at(const float eye[3], const float center[3], const float up[3], float vfov_deg,
+                           float aspect, float znear, float zfar, solrt_camera* out) {
+    double f[3] = {(double)center[0] - eye[0], (double)center[1] - eye[1], (double)center[2] - eye[2]};
+    double fl = std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+    for (double& v : f) v /= fl;
+    double s[3] = {f[1] * up[2] - f[2] * up[1], f[2] * up[0] - f[0] * up[2], f[0] * up[1] - f[1] * up[0]};
+    double sl = std::sqrt(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
+    for (double& v : s) v /= sl;
+    const double u[3] = {s[1] * f[2] - s[2] * f[1], s[2] * f[0] - s[0] * f[2], s[0] * f[1] - s[1] * f[0]};
+    const double e[3] = {eye[0], eye[1], eye[2]};
+    const double view[16] = {s[0], u[0], -f[0], 0, s[1], u[1], -f[1], 0, s[2], u[2], -f[2], 0,
+                             -(s[0] * e[0] + s[1] * e[1] + s[2] * e[2]),
+                             -(u[0] * e[0] + u[1] * e[1] + u[2] * e[2]),
+                             (f[0] * e[0] + f[1] * e[1] + f[2] * e[2]), 1};
+    const double fov = (double)vfov_deg * 3.14159265358979323846 / 180.0;
+    const double h = 1.0 / std::tan(0.5 * fov);
+    const double w = h / (double)aspect;
+    const double r = (double)zfar / ((double)znear - (double)zfar);
+    const double proj[16] = {w, 0, 0, 0, 0, h, 0, 0, 0, 0, r, -1, 0, 0, r * znear, 0};
+    double vi[16], pi[16];
+    inv4(view, vi);
+    inv4(proj, pi);
+    for (int i = 0; i < 16; ++i) {
+        out->view[i] = (float)view[i];
+        out->view_inverse[i] = (float)vi[i];
+        out->projection[i] = (float)proj[i];
+        out->projection_inverse[i] = (float)pi[i];
+    }
+}
+
+}  // extern "C"

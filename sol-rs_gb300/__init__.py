@@ -1,0 +1,15 @@
+"""solrt — GB300-native software path tracer (the 5-pathtrace path of sol-rs).
+
+Python host package over the C ABI in include/solrt.h. Import with
+importlib (the directory name is not a Python identifier):
+
+    import importlib
+    solrt = importlib.import_module("sol-rs_gb300")
+"""
+from .api import (  # noqa: F401
+    ACCUM_KAHAN, ACCUM_REF_MIX, BVH2, BVH8_Q8, HIT_DTYPE, MATERIAL_LAMBERT, MATERIAL_REF, MISS_BLACK,
+    MISS_GRADIENT, MISS_REF_SKY, NO_HIT, RAY_DTYPE, RNG_PER_SAMPLE, RNG_REF_STREAM, Camera, Context, Image,
+    RenderParams, Renderer, SceneDescription, SolrtError, camera_from_view, camera_look_at, check, lib,
+    render_params, scene_desc,
+)
+from . import scenes  # noqa: F401

@@ -1,0 +1,357 @@
+"""ctypes binding of include/solrt.h and thin Python objects over it.
+
+The objects follow the reference's names for this path:
+  SceneDescription.from_scene(context, scene)   src/ray/mod.rs:49-57
+  SceneDescription.tlas_regenerate()            src/ray/mod.rs:178-181
+  Renderer.cmd_trace_rays(...)                  src/ray/sbt.rs:167-180 + the
+                                                pathtrace shaders
+Every call goes to the CUDA library; there is no CPU fallback. A missing or
+unloadable library raises SolrtError.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "libsolrt.so")
+
+NO_HIT = 0xFFFFFFFF
+
+# enums (solrt.h)
+OK, ERR_INVALID, ERR_OOM, ERR_DEVICE, ERR_TIMEOUT, ERR_CAPACITY, ERR_NOT_READY, ERR_NOT_FOUND, ERR_BUDGET = range(9)
+BVH2, BVH8_Q8 = 0, 1
+MISS_BLACK, MISS_REF_SKY, MISS_GRADIENT = 0, 1, 2
+MATERIAL_REF, MATERIAL_LAMBERT = 0, 1
+ACCUM_REF_MIX, ACCUM_KAHAN = 0, 1
+RNG_REF_STREAM, RNG_PER_SAMPLE = 0, 1
+EFLAG_STACK, EFLAG_QUEUE, EFLAG_INDEX, EFLAG_TIMEOUT = 1, 2, 4, 8
+
+
+class SolrtError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("solrt status %d: %s" % (status, msg))
+        self.status = status
+
+
+F16 = ctypes.c_float * 16
+
+
+class Vertex(ctypes.Structure):       # ModelVertex, src/scene/mesh.rs:9-14
+    _fields_ = [("pos", ctypes.c_float * 4), ("color", ctypes.c_float * 4),
+                ("normal", ctypes.c_float * 4), ("uv", ctypes.c_float * 4)]
+
+
+class Material(ctypes.Structure):     # MaterialInfo, src/scene/mod.rs:21-29
+    _fields_ = [("base_color", ctypes.c_float * 4), ("emissive", ctypes.c_float * 3), ("padding0", ctypes.c_float),
+                ("metallic", ctypes.c_float), ("roughness", ctypes.c_float), ("padding1", ctypes.c_float),
+                ("padding2", ctypes.c_float)]
+
+
+class Instance(ctypes.Structure):     # SceneInstance, src/ray/mod.rs:18-24
+    _fields_ = [("id", ctypes.c_uint32), ("texture_offset", ctypes.c_uint32), ("padding", ctypes.c_float * 2),
+                ("transform", F16), ("transform_it", F16)]
+
+
+class Section(ctypes.Structure):
+    _fields_ = [("vertex_offset", ctypes.c_uint32), ("vertex_count", ctypes.c_uint32),
+                ("index_offset", ctypes.c_uint32), ("index_count", ctypes.c_uint32),
+                ("material_index", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class SceneDesc(ctypes.Structure):
+    _fields_ = [("vertices", ctypes.c_void_p), ("vertex_count", ctypes.c_uint32), ("index_count", ctypes.c_uint32),
+                ("indices", ctypes.c_void_p), ("sections", ctypes.c_void_p), ("section_count", ctypes.c_uint32),
+                ("material_count", ctypes.c_uint32), ("materials", ctypes.c_void_p), ("instances", ctypes.c_void_p)]
+
+
+class BvhDesc(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_uint32), ("leaf_max", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 2)]
+
+
+class BvhInfo(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_uint32), ("tri_count", ctypes.c_uint32), ("node_count", ctypes.c_uint32),
+                ("depth", ctypes.c_uint32), ("node_bytes", ctypes.c_uint64), ("tri_bytes", ctypes.c_uint64),
+                ("shade_bytes", ctypes.c_uint64), ("build_ms", ctypes.c_double)]
+
+
+class Camera(ctypes.Structure):       # SceneUniforms matrices, examples/5-pathtrace.rs:9-17
+    _fields_ = [("view", F16), ("view_inverse", F16), ("projection", F16), ("projection_inverse", F16)]
+
+
+class RenderParams(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("spp", ctypes.c_uint32),
+                ("max_bounces", ctypes.c_uint32), ("frame", ctypes.c_uint32), ("accum_start_frame", ctypes.c_uint32),
+                ("seed", ctypes.c_uint32), ("job_id", ctypes.c_uint32), ("miss_mode", ctypes.c_uint32),
+                ("material_mode", ctypes.c_uint32), ("accum_mode", ctypes.c_uint32), ("rng_mode", ctypes.c_uint32),
+                ("tmax", ctypes.c_float), ("reserved", ctypes.c_uint32 * 3)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("segments", ctypes.c_uint64), ("paths", ctypes.c_uint64), ("node_visits", ctypes.c_uint64),
+                ("tri_tests", ctypes.c_uint64), ("fp64_fallbacks", ctypes.c_uint64), ("launches", ctypes.c_uint64),
+                ("error_flags", ctypes.c_uint32), ("reserved", ctypes.c_uint32), ("render_ms", ctypes.c_double),
+                ("extend_ms", ctypes.c_double), ("shade_ms", ctypes.c_double), ("extend_launches", ctypes.c_uint64),
+                ("shade_launches", ctypes.c_uint64)]
+
+
+class ContextDesc(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("path_capacity", ctypes.c_uint32), ("enable_counters", ctypes.c_uint32),
+                ("block_size", ctypes.c_uint32), ("enable_timing", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 3)]
+
+
+RAY_DTYPE = np.dtype([("origin", "<f4", 3), ("tmin", "<f4"), ("dir", "<f4", 3), ("tmax", "<f4")])
+HIT_DTYPE = np.dtype([("t", "<f4"), ("prim", "<u4"), ("u", "<f4"), ("v", "<f4")])
+
+assert ctypes.sizeof(Vertex) == 64 and ctypes.sizeof(Material) == 48 and ctypes.sizeof(Instance) == 144
+assert RAY_DTYPE.itemsize == 32 and HIT_DTYPE.itemsize == 16
+
+_P = ctypes.c_void_p
+_U32 = ctypes.c_uint32
+_PROTOS = {
+    "solrt_abi_version": (_U32, []),
+    "solrt_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "solrt_last_error": (ctypes.c_char_p, []),
+    "solrt_context_create": (ctypes.c_int, [ctypes.POINTER(ContextDesc), ctypes.POINTER(_P)]),
+    "solrt_context_destroy": (ctypes.c_int, [_P]),
+    "solrt_synchronize": (ctypes.c_int, [_P]),
+    "solrt_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(Stats)]),
+    "solrt_reset_stats": (ctypes.c_int, [_P]),
+    "solrt_context_stream": (_P, [_P]),
+    "solrt_scene_create": (ctypes.c_int, [_P, ctypes.POINTER(SceneDesc), ctypes.POINTER(BvhDesc), ctypes.POINTER(_P)]),
+    "solrt_scene_destroy": (ctypes.c_int, [_P]),
+    "solrt_scene_build_bvh": (ctypes.c_int, [_P, ctypes.POINTER(BvhDesc)]),
+    "solrt_scene_bvh_info": (ctypes.c_int, [_P, ctypes.POINTER(BvhInfo)]),
+    "solrt_scene_bvh_export": (ctypes.c_int, [_P, _P, ctypes.c_size_t, _P, ctypes.c_size_t]),
+    "solrt_scene_bytes": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64)]),
+    "solrt_camera_look_at": (ctypes.c_int, [ctypes.POINTER(ctypes.c_float * 3)] * 3 +
+                             [ctypes.c_float] * 4 + [ctypes.POINTER(Camera)]),
+    "solrt_camera_from_view": (ctypes.c_int, [ctypes.POINTER(F16)] + [ctypes.c_float] * 4 + [ctypes.POINTER(Camera)]),
+    "solrt_image_create": (ctypes.c_int, [_P, _U32, _U32, _U32, ctypes.POINTER(_P)]),
+    "solrt_image_destroy": (ctypes.c_int, [_P]),
+    "solrt_image_clear": (ctypes.c_int, [_P]),
+    "solrt_image_read": (ctypes.c_int, [_P, _P, _P]),
+    "solrt_image_device_ptrs": (ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P)]),
+    "solrt_render": (ctypes.c_int, [_P, _P, ctypes.POINTER(Camera), ctypes.POINTER(RenderParams), _P]),
+    "solrt_trace_rays": (ctypes.c_int, [_P, _P, _P, _U32, _P]),
+    "solrt_trace_rays_device": (ctypes.c_int, [_P, _P, _P, _U32, _P]),
+    "solrt_debug_unit": (ctypes.c_int, [_P, _U32, _U32, _P, _P, _P, _P, _P]),
+}
+
+_lib = None
+
+
+def lib():
+    """Loads the CUDA library (raises SolrtError when it is missing)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise SolrtError(ERR_DEVICE, "libsolrt.so not built (run sol-rs_gb300/build.py): %s" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _PROTOS.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status):
+    if status != OK:
+        L = lib()
+        raise SolrtError(status, L.solrt_last_error().decode(errors="replace"))
+
+
+def _ptr(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+# ---------------------------------------------------------------------------
+# Objects
+# ---------------------------------------------------------------------------
+
+class Context:
+    """CUDA device + stream + wavefront queues (solrt_context)."""
+
+    def __init__(self, device=0, path_capacity=0, enable_counters=False, enable_timing=False):
+        d = ContextDesc(device=device, path_capacity=path_capacity, enable_counters=int(bool(enable_counters)),
+                        enable_timing=int(bool(enable_timing)))
+        h = ctypes.c_void_p()
+        check(lib().solrt_context_create(ctypes.byref(d), ctypes.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().solrt_context_destroy(self.handle)
+            self.handle = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def synchronize(self):
+        check(lib().solrt_synchronize(self.handle))
+
+    def stats(self):
+        s = Stats()
+        check(lib().solrt_get_stats(self.handle, ctypes.byref(s)))
+        return s
+
+    def reset_stats(self):
+        check(lib().solrt_reset_stats(self.handle))
+
+    def stream(self):
+        return lib().solrt_context_stream(self.handle)
+
+    def debug_unit(self, op, n, a=None, b=None, fin=None, out_u=None, out_f=None):
+        check(lib().solrt_debug_unit(self.handle, op, n, _ptr(a), _ptr(b), _ptr(fin), _ptr(out_u), _ptr(out_f)))
+
+
+def scene_desc(data):
+    """SceneDesc over the numpy arrays of a scenes.SceneData (kept alive by it)."""
+    d = SceneDesc()
+    d.vertices = data.vertices.ctypes.data if len(data.vertices) else None
+    d.vertex_count = len(data.vertices)
+    d.indices = data.indices.ctypes.data if len(data.indices) else None
+    d.index_count = len(data.indices)
+    d.sections = data.sections.ctypes.data if len(data.sections) else None
+    d.section_count = len(data.sections)
+    d.materials = data.materials.ctypes.data if len(data.materials) else None
+    d.material_count = len(data.materials)
+    d.instances = data.instances.ctypes.data if data.instances is not None else None
+    return d
+
+
+class SceneDescription:
+    """Device scene + BVH (solrt_scene). Mirrors ray::SceneDescription."""
+
+    def __init__(self, context, data, bvh=BVH2, leaf_max=0):
+        self.context = context
+        self.data = data
+        d = scene_desc(data)
+        bd = BvhDesc(kind=bvh, leaf_max=leaf_max)
+        h = ctypes.c_void_p()
+        check(lib().solrt_scene_create(context.handle, ctypes.byref(d), ctypes.byref(bd), ctypes.byref(h)))
+        self.handle = h
+
+    @classmethod
+    def from_scene(cls, context, scene, bvh=BVH2):
+        return cls(context, scene, bvh=bvh)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().solrt_scene_destroy(self.handle)
+            self.handle = None
+
+    __del__ = close
+
+    def build_bvh(self, bvh=BVH2, leaf_max=0):
+        check(lib().solrt_scene_build_bvh(self.handle, ctypes.byref(BvhDesc(kind=bvh, leaf_max=leaf_max))))
+
+    def tlas_regenerate(self):
+        """Rebuilds the acceleration structure with its current kind."""
+        self.build_bvh(self.bvh_info().kind)
+
+    def bvh_info(self):
+        i = BvhInfo()
+        check(lib().solrt_scene_bvh_info(self.handle, ctypes.byref(i)))
+        return i
+
+    def bvh_export(self):
+        info = self.bvh_info()
+        nodes = np.zeros(info.node_bytes, np.uint8)
+        tris = np.zeros(info.tri_bytes, np.uint8)
+        check(lib().solrt_scene_bvh_export(self.handle, _ptr(nodes), nodes.nbytes, _ptr(tris), tris.nbytes))
+        return nodes, tris
+
+    def device_bytes(self):
+        v = ctypes.c_uint64()
+        check(lib().solrt_scene_bytes(self.handle, ctypes.byref(v)))
+        return v.value
+
+    def trace_rays(self, rays):
+        """Closest hits of a RAY_DTYPE array (host memory, synchronous)."""
+        rays = np.ascontiguousarray(rays, dtype=RAY_DTYPE)
+        hits = np.zeros(len(rays), HIT_DTYPE)
+        check(lib().solrt_trace_rays(self.context.handle, self.handle, _ptr(rays), len(rays), _ptr(hits)))
+        return hits
+
+    def trace_rays_device(self, rays_ptr, n, hits_ptr):
+        check(lib().solrt_trace_rays_device(self.context.handle, self.handle, ctypes.c_void_p(rays_ptr), n,
+                                            ctypes.c_void_p(hits_ptr)))
+
+
+class Image:
+    """RGBA32F accumulation + RGBA8 render image (solrt_image)."""
+
+    def __init__(self, context, width, height, accum_mode=ACCUM_REF_MIX):
+        self.context = context
+        self.width, self.height, self.accum_mode = width, height, accum_mode
+        h = ctypes.c_void_p()
+        check(lib().solrt_image_create(context.handle, width, height, accum_mode, ctypes.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().solrt_image_destroy(self.handle)
+            self.handle = None
+
+    __del__ = close
+
+    def clear(self):
+        check(lib().solrt_image_clear(self.handle))
+
+    def read(self, rgba32f=True, rgba8=True):
+        a = np.zeros((self.height, self.width, 4), np.float32) if rgba32f else None
+        b = np.zeros((self.height, self.width, 4), np.uint8) if rgba8 else None
+        check(lib().solrt_image_read(self.handle, _ptr(a), _ptr(b)))
+        return a, b
+
+    def read_into(self, rgba32f, rgba8=None):
+        check(lib().solrt_image_read(self.handle, _ptr(rgba32f), _ptr(rgba8)))
+
+    def device_ptrs(self):
+        a, b = ctypes.c_void_p(), ctypes.c_void_p()
+        check(lib().solrt_image_device_ptrs(self.handle, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+
+def camera_look_at(eye, center, up, vfov_deg, aspect, znear=0.1, zfar=1000.0):
+    f3 = ctypes.c_float * 3
+    c = Camera()
+    check(lib().solrt_camera_look_at(f3(*eye), f3(*center), f3(*up), vfov_deg, aspect, znear, zfar, ctypes.byref(c)))
+    return c
+
+
+def camera_from_view(view16, vfov_deg, aspect, znear=0.1, zfar=1000.0):
+    c = Camera()
+    check(lib().solrt_camera_from_view(F16(*[float(x) for x in view16]), vfov_deg, aspect, znear, zfar,
+                                       ctypes.byref(c)))
+    return c
+
+
+def render_params(width, height, spp=8, max_bounces=32, frame=0, accum_start_frame=0, seed=0, job_id=0,
+                  miss_mode=MISS_BLACK, material_mode=MATERIAL_REF, accum_mode=ACCUM_REF_MIX,
+                  rng_mode=RNG_REF_STREAM, tmax=0.0):
+    """Defaults are the reference's: 8 spp per launch, 32 bounces, black miss,
+    pathtrace.rchit materials, running mix, one RNG stream per pixel."""
+    return RenderParams(width=width, height=height, spp=spp, max_bounces=max_bounces, frame=frame,
+                        accum_start_frame=accum_start_frame, seed=seed, job_id=job_id, miss_mode=miss_mode,
+                        material_mode=material_mode, accum_mode=accum_mode, rng_mode=rng_mode, tmax=tmax)
+
+
+class Renderer:
+    """One render launch = the reference's per-frame cmd_trace_rays."""
+
+    def __init__(self, context):
+        self.context = context
+
+    def cmd_trace_rays(self, scene, camera, params, image):
+        check(lib().solrt_render(self.context.handle, scene.handle, ctypes.byref(camera), ctypes.byref(params),
+                                 image.handle))
+
+    render = cmd_trace_rays

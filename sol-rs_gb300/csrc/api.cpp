@@ -1,0 +1,548 @@
+// api.cpp — the C ABI of include/solrt.h.
+//
+// Host-side counterpart of the reference's per-path Rust objects:
+//   solrt_context  ~ the Vulkan Context + queue (src/context.rs:222-575)
+//   solrt_scene    ~ SceneDescription (src/ray/mod.rs:38-156): sections are
+//                    flattened to world space with each section's transform
+//                    and transform_it, uploaded, and an LBVH replaces the
+//                    driver-built BLAS/TLAS
+//   solrt_image    ~ the accumulation (RGBA32F) and render (RGBA8) images of
+//                    examples/5-pathtrace.rs:222-229
+//   solrt_render   ~ one `render` frame of examples/5-pathtrace.rs:294-369
+// Errors are status codes with a per-thread message instead of the
+// reference's panics (unwrap/expect).
+#include <cmath>
+#include <cstdarg>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+static_assert(sizeof(solrt_vertex) == 64, "ModelVertex is 64 bytes (src/scene/mesh.rs:9-14)");
+static_assert(sizeof(solrt_material) == 48, "MaterialInfo is 48 bytes (src/scene/mod.rs:21-29)");
+static_assert(sizeof(solrt_instance) == 144, "SceneInstance is 144 bytes (src/ray/mod.rs:18-24)");
+static_assert(sizeof(solrt_ray) == 32, "solrt_ray is two float4");
+static_assert(sizeof(solrt_hit) == 16, "solrt_hit is one float4");
+static_assert(sizeof(solrt_camera) == 256, "four mat4");
+
+struct solrt_context : solrt::Context {};
+struct solrt_scene : solrt::Scene {};
+struct solrt_image : solrt::Image {};
+
+namespace solrt {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void set_error(const char* fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+}
+
+namespace {
+
+#define CHECK_ARG(cond, msg)                         \
+    do {                                             \
+        if (!(cond)) {                               \
+            ::solrt::set_error("%s", msg);           \
+            return SOLRT_ERR_INVALID;                \
+        }                                            \
+    } while (0)
+
+solrt_status check_device_flags(Context& ctx) {
+    unsigned int flags = 0;
+    DevStats* st = ctx.stats.as<DevStats>();
+    SOLRT_CUDA(cudaMemcpyAsync(&flags, &st->eflags, sizeof(flags), cudaMemcpyDeviceToHost, ctx.stream));
+    SOLRT_CUDA(cudaStreamSynchronize(ctx.stream));
+    if (flags == 0) return SOLRT_OK;
+    SOLRT_CUDA(cudaMemsetAsync(&st->eflags, 0, sizeof(unsigned int), ctx.stream));
+    SOLRT_CUDA(cudaStreamSynchronize(ctx.stream));
+    set_error("device error flags 0x%x (1 stack overflow, 2 queue overflow, 4 bad index, 8 timeout)", flags);
+    if (flags & SOLRT_EFLAG_TIMEOUT) return SOLRT_ERR_TIMEOUT;
+    if (flags & SOLRT_EFLAG_INDEX) return SOLRT_ERR_DEVICE;
+    return SOLRT_ERR_CAPACITY;
+}
+
+// glam-equivalent matrix maths in FP64 (src/scene/camera.rs:98-106).
+void inverse4(const double* m, double* o, bool* ok) {
+    double inv[16];
+    inv[0] = m[5] * m[10] * m[15] - m[5] * m[11] * m[14] - m[9] * m[6] * m[15] + m[9] * m[7] * m[14] + m[13] * m[6] * m[11] - m[13] * m[7] * m[10];
+    inv[4] = -m[4] * m[10] * m[15] + m[4] * m[11] * m[14] + m[8] * m[6] * m[15] - m[8] * m[7] * m[14] - m[12] * m[6] * m[11] + m[12] * m[7] * m[10];
+    inv[8] = m[4] * m[9] * m[15] - m[4] * m[11] * m[13] - m[8] * m[5] * m[15] + m[8] * m[7] * m[13] + m[12] * m[5] * m[11] - m[12] * m[7] * m[9];
+    inv[12] = -m[4] * m[9] * m[14] + m[4] * m[10] * m[13] + m[8] * m[5] * m[14] - m[8] * m[6] * m[13] - m[12] * m[5] * m[10] + m[12] * m[6] * m[9];
+    inv[1] = -m[1] * m[10] * m[15] + m[1] * m[11] * m[14] + m[9] * m[2] * m[15] - m[9] * m[3] * m[14] - m[13] * m[2] * m[11] + m[13] * m[3] * m[10];
+    inv[5] = m[0] * m[10] * m[15] - m[0] * m[11] * m[14] - m[8] * m[2] * m[15] + m[8] * m[3] * m[14] + m[12] * m[2] * m[11] - m[12] * m[3] * m[10];
+    inv[9] = -m[0] * m[9] * m[15] + m[0] * m[11] * m[13] + m[8] * m[1] * m[15] - m[8] * m[3] * m[13] - m[12] * m[1] * m[11] + m[12] * m[3] * m[9];
+    inv[13] = m[0] * m[9] * m[14] - m[0] * m[10] * m[13] - m[8] * m[1] * m[14] + m[8] * m[2] * m[13] + m[12] * m[1] * m[10] - m[12] * m[2] * m[9];
+    inv[2] = m[1] * m[6] * m[15] - m[1] * m[7] * m[14] - m[5] * m[2] * m[15] + m[5] * m[3] * m[14] + m[13] * m[2] * m[7] - m[13] * m[3] * m[6];
+    inv[6] = -m[0] * m[6] * m[15] + m[0] * m[7] * m[14] + m[4] * m[2] * m[15] - m[4] * m[3] * m[14] - m[12] * m[2] * m[7] + m[12] * m[3] * m[6];
+    inv[10] = m[0] * m[5] * m[15] - m[0] * m[7] * m[13] - m[4] * m[1] * m[15] + m[4] * m[3] * m[13] + m[12] * m[1] * m[7] - m[12] * m[3] * m[5];
+    inv[14] = -m[0] * m[5] * m[14] + m[0] * m[6] * m[13] + m[4] * m[1] * m[14] - m[4] * m[2] * m[13] - m[12] * m[1] * m[6] + m[12] * m[2] * m[5];
+    inv[3] = -m[1] * m[6] * m[11] + m[1] * m[7] * m[10] + m[5] * m[2] * m[11] - m[5] * m[3] * m[10] - m[9] * m[2] * m[7] + m[9] * m[3] * m[6];
+    inv[7] = m[0] * m[6] * m[11] - m[0] * m[7] * m[10] - m[4] * m[2] * m[11] + m[4] * m[3] * m[10] + m[8] * m[2] * m[7] - m[8] * m[3] * m[6];
+    inv[11] = -m[0] * m[5] * m[11] + m[0] * m[7] * m[9] + m[4] * m[1] * m[11] - m[4] * m[3] * m[9] - m[8] * m[1] * m[7] + m[8] * m[3] * m[5];
+    inv[15] = m[0] * m[5] * m[10] - m[0] * m[6] * m[9] - m[4] * m[1] * m[10] + m[4] * m[2] * m[9] + m[8] * m[1] * m[6] - m[8] * m[2] * m[5];
+    const double det = m[0] * inv[0] + m[1] * inv[4] + m[2] * inv[8] + m[3] * inv[12];
+    *ok = det != 0.0 && std::isfinite(det);
+    for (int i = 0; i < 16; ++i) o[i] = *ok ? inv[i] / det : 0.0;
+}
+
+solrt_status fill_camera(const double view[16], float vfov_deg, float aspect, float znear, float zfar,
+                         solrt_camera* out) {
+    CHECK_ARG(out, "null camera");
+    CHECK_ARG(vfov_deg > 0.0f && vfov_deg < 180.0f, "vfov must be in (0, 180) degrees");
+    CHECK_ARG(aspect > 0.0f && znear > 0.0f && zfar > znear, "bad aspect or depth range");
+    // Mat4::perspective_rh(vfov.to_radians(), aspect, near, far)
+    const double fov = (double)vfov_deg * 3.14159265358979323846 / 180.0;
+    const double h = 1.0 / std::tan(0.5 * fov);
+    const double w = h / (double)aspect;
+    const double r = (double)zfar / ((double)znear - (double)zfar);
+    const double proj[16] = {w, 0, 0, 0, 0, h, 0, 0, 0, 0, r, -1, 0, 0, r * znear, 0};
+    double vi[16], pi[16];
+    bool ok1 = false, ok2 = false;
+    inverse4(view, vi, &ok1);
+    inverse4(proj, pi, &ok2);
+    CHECK_ARG(ok1 && ok2, "singular camera matrix");
+    for (int i = 0; i < 16; ++i) {
+        out->view[i] = (float)view[i];
+        out->view_inverse[i] = (float)vi[i];
+        out->projection[i] = (float)proj[i];
+        out->projection_inverse[i] = (float)pi[i];
+    }
+    return SOLRT_OK;
+}
+
+}  // namespace
+}  // namespace solrt
+
+using namespace solrt;
+
+extern "C" {
+
+uint32_t solrt_abi_version(void) { return SOLRT_ABI_VERSION; }
+
+const char* solrt_status_string(solrt_status s) {
+    switch (s) {
+        case SOLRT_OK: return "ok";
+        case SOLRT_ERR_INVALID: return "invalid argument";
+        case SOLRT_ERR_OOM: return "out of memory";
+        case SOLRT_ERR_DEVICE: return "device error";
+        case SOLRT_ERR_TIMEOUT: return "timeout";
+        case SOLRT_ERR_CAPACITY: return "capacity exceeded";
+        case SOLRT_ERR_NOT_READY: return "not ready";
+        case SOLRT_ERR_NOT_FOUND: return "not found";
+        case SOLRT_ERR_BUDGET: return "over memory budget";
+    }
+    return "unknown status";
+}
+
+const char* solrt_last_error(void) { return g_last_error.c_str(); }
+
+solrt_status solrt_context_create(const solrt_context_desc* desc, solrt_context** out) {
+    CHECK_ARG(out, "null output");
+    *out = nullptr;
+    solrt_context_desc d{};
+    if (desc) d = *desc;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        set_error("no CUDA device");
+        return SOLRT_ERR_DEVICE;
+    }
+    CHECK_ARG(d.device >= 0 && d.device < ndev, "device ordinal out of range");
+    SOLRT_CUDA(cudaSetDevice(d.device));
+    cudaDeviceProp prop;
+    SOLRT_CUDA(cudaGetDeviceProperties(&prop, d.device));
+    if (prop.major * 10 + prop.minor != 103) {
+        set_error("solrt is built for sm_103a (GB300); device %d is sm_%d%d", d.device, prop.major, prop.minor);
+        return SOLRT_ERR_DEVICE;
+    }
+    solrt_context* c = new (std::nothrow) solrt_context();
+    if (!c) return SOLRT_ERR_OOM;
+    c->device = d.device;
+    c->sm_count = prop.multiProcessorCount;
+    c->capacity = d.path_capacity ? d.path_capacity : (8u << 20);
+    c->counters = d.enable_counters != 0;
+    c->block_size = d.block_size;
+    c->timing = d.enable_timing != 0;
+    auto fail = [&](solrt_status s) {
+        solrt_context_destroy(c);
+        return s;
+    };
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        set_error("cudaStreamCreate failed");
+        return fail(SOLRT_ERR_DEVICE);
+    }
+    if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
+        set_error("cudaEventCreate failed");
+        return fail(SOLRT_ERR_DEVICE);
+    }
+    const size_t C = c->capacity;
+    for (int i = 0; i < 2; ++i) {
+        solrt_status s;
+        if ((s = c->q_o[i].alloc(16 * C)) != SOLRT_OK) return fail(s);
+        if ((s = c->q_d[i].alloc(16 * C)) != SOLRT_OK) return fail(s);
+        if ((s = c->q_thr[i].alloc(16 * C)) != SOLRT_OK) return fail(s);
+        if ((s = c->q_meta[i].alloc(8 * C)) != SOLRT_OK) return fail(s);
+    }
+    solrt_status s;
+    if ((s = c->hits.alloc(16 * C)) != SOLRT_OK) return fail(s);
+    if ((s = c->rad.alloc(16 * C)) != SOLRT_OK) return fail(s);
+    if ((s = c->ctl.alloc(sizeof(PassCtl))) != SOLRT_OK) return fail(s);
+    if ((s = c->stats.alloc(sizeof(DevStats))) != SOLRT_OK) return fail(s);
+    if (cudaMemset(c->ctl.ptr, 0, sizeof(PassCtl)) != cudaSuccess ||
+        cudaMemset(c->stats.ptr, 0, sizeof(DevStats)) != cudaSuccess ||
+        cudaDeviceSynchronize() != cudaSuccess) {
+        set_error("device initialisation failed");
+        return fail(SOLRT_ERR_DEVICE);
+    }
+    *out = c;
+    return SOLRT_OK;
+}
+
+solrt_status solrt_context_destroy(solrt_context* ctx) {
+    if (!ctx) return SOLRT_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    for (auto& t : ctx->timed) {
+        cudaEventDestroy(t.start);
+        cudaEventDestroy(t.end);
+    }
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return SOLRT_OK;
+}
+
+void* solrt_context_stream(solrt_context* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+solrt_status solrt_synchronize(solrt_context* ctx) {
+    CHECK_ARG(ctx, "null context");
+    SOLRT_CUDA(cudaStreamSynchronize(ctx->stream));
+    return check_device_flags(*ctx);
+}
+
+solrt_status solrt_get_stats(solrt_context* ctx, solrt_stats* out) {
+    CHECK_ARG(ctx && out, "null argument");
+    DevStats d;
+    SOLRT_CUDA(cudaMemcpyAsync(&d, ctx->stats.ptr, sizeof(d), cudaMemcpyDeviceToHost, ctx->stream));
+    SOLRT_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->timing_collect();
+    std::memset(out, 0, sizeof(*out));
+    out->extend_ms = ctx->extend_ms;
+    out->shade_ms = ctx->shade_ms;
+    out->extend_launches = ctx->extend_launches;
+    out->shade_launches = ctx->shade_launches;
+    out->segments = d.segments;
+    out->paths = d.paths;
+    out->node_visits = d.node_visits;
+    out->tri_tests = d.tri_tests;
+    out->fp64_fallbacks = d.fp64_fallbacks;
+    out->launches = ctx->launches;
+    out->error_flags = d.eflags;
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) == cudaSuccess) out->render_ms = ms;
+    cudaGetLastError();
+    return SOLRT_OK;
+}
+
+solrt_status solrt_reset_stats(solrt_context* ctx) {
+    CHECK_ARG(ctx, "null context");
+    SOLRT_CUDA(cudaMemsetAsync(ctx->stats.ptr, 0, sizeof(DevStats), ctx->stream));
+    SOLRT_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->timing_collect();
+    ctx->launches = 0;
+    ctx->extend_ms = ctx->shade_ms = 0.0;
+    ctx->extend_launches = ctx->shade_launches = 0;
+    return SOLRT_OK;
+}
+
+solrt_status solrt_scene_create(solrt_context* ctx, const solrt_scene_desc* d, const solrt_bvh_desc* bvh,
+                                solrt_scene** out) {
+    CHECK_ARG(ctx && d && out, "null argument");
+    *out = nullptr;
+    CHECK_ARG(d->section_count == 0 || d->sections, "sections missing");
+    CHECK_ARG(d->vertex_count == 0 || d->vertices, "vertices missing");
+    CHECK_ARG(d->index_count == 0 || d->indices, "indices missing");
+    CHECK_ARG(d->material_count == 0 || d->materials, "materials missing");
+    static const float ident[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    // flatten: world-space vertices per section, then triangles
+    uint64_t nv = 0, nt = 0;
+    for (uint32_t s = 0; s < d->section_count; ++s) {
+        const solrt_section& sec = d->sections[s];
+        if (sec.index_count % 3 != 0 || (uint64_t)sec.vertex_offset + sec.vertex_count > d->vertex_count ||
+            (uint64_t)sec.index_offset + sec.index_count > d->index_count || sec.material_index >= d->material_count) {
+            set_error("malformed section %u", s);
+            return SOLRT_ERR_INVALID;
+        }
+        nv += sec.vertex_count;
+        nt += sec.index_count / 3;
+    }
+    CHECK_ARG(nv < (1ull << 31) && nt < (1ull << 31), "scene too large");
+    std::vector<float4> pos(nv), nrm(nv), col(nv);
+    std::vector<uint4> tri(nt);
+    uint64_t vb = 0, tb = 0;
+    for (uint32_t s = 0; s < d->section_count; ++s) {
+        const solrt_section& sec = d->sections[s];
+        const float* T = d->instances ? d->instances[s].transform : ident;
+        const float* Tit = d->instances ? d->instances[s].transform_it : ident;
+        for (uint32_t v = 0; v < sec.vertex_count; ++v) {
+            const solrt_vertex& in = d->vertices[sec.vertex_offset + v];
+            float o[4];
+            mat4_mul(T, in.pos[0], in.pos[1], in.pos[2], 1.0f, o);       // pathtrace.rchit:88-90
+            pos[vb + v] = make_float4(o[0], o[1], o[2], 0.0f);
+            mat4_mul(Tit, in.normal[0], in.normal[1], in.normal[2], 0.0f, o);  // rchit:84-86
+            nrm[vb + v] = make_float4(o[0], o[1], o[2], 0.0f);
+            col[vb + v] = make_float4(in.color[0], in.color[1], in.color[2], 0.0f);
+        }
+        for (uint32_t t = 0; t < sec.index_count / 3; ++t) {
+            uint32_t id[3];
+            for (int k = 0; k < 3; ++k) {
+                id[k] = d->indices[sec.index_offset + 3 * t + k];
+                if (id[k] >= sec.vertex_count) {
+                    set_error("section %u triangle %u: index %u >= vertex_count %u", s, t, id[k], sec.vertex_count);
+                    return SOLRT_ERR_INVALID;
+                }
+            }
+            tri[tb + t] = make_uint4((uint32_t)(vb + id[0]), (uint32_t)(vb + id[1]), (uint32_t)(vb + id[2]),
+                                     sec.material_index);
+        }
+        vb += sec.vertex_count;
+        tb += sec.index_count / 3;
+    }
+    solrt_scene* sc = new (std::nothrow) solrt_scene();
+    if (!sc) return SOLRT_ERR_OOM;
+    sc->ctx = ctx;
+    sc->tri_count = (uint32_t)nt;
+    sc->vertex_count = (uint32_t)nv;
+    sc->material_count = d->material_count;
+    auto fail = [&](solrt_status s) {
+        delete sc;
+        return s;
+    };
+    cudaStream_t st = ctx->stream;
+    solrt_status s;
+    if ((s = sc->vpos.alloc(16 * nv)) || (s = sc->vnrm.alloc(16 * nv)) || (s = sc->vcol.alloc(16 * nv)) ||
+        (s = sc->tri_idx.alloc(16 * nt)) || (s = sc->materials.alloc(48 * (size_t)d->material_count)))
+        return fail(s);
+    if (nv) {
+        if (cudaMemcpyAsync(sc->vpos.ptr, pos.data(), 16 * nv, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+            cudaMemcpyAsync(sc->vnrm.ptr, nrm.data(), 16 * nv, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+            cudaMemcpyAsync(sc->vcol.ptr, col.data(), 16 * nv, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+            set_error("scene upload failed");
+            return fail(SOLRT_ERR_DEVICE);
+        }
+    }
+    if (nt && cudaMemcpyAsync(sc->tri_idx.ptr, tri.data(), 16 * nt, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+        set_error("scene upload failed");
+        return fail(SOLRT_ERR_DEVICE);
+    }
+    if (d->material_count &&
+        cudaMemcpyAsync(sc->materials.ptr, d->materials, 48 * (size_t)d->material_count, cudaMemcpyHostToDevice,
+                        st) != cudaSuccess) {
+        set_error("scene upload failed");
+        return fail(SOLRT_ERR_DEVICE);
+    }
+    if (cudaStreamSynchronize(st) != cudaSuccess) {
+        set_error("scene upload failed");
+        return fail(SOLRT_ERR_DEVICE);
+    }
+    solrt_bvh_desc bd{};
+    if (bvh) bd = *bvh;
+    if ((s = solrt_scene_build_bvh(sc, &bd)) != SOLRT_OK) return fail(s);
+    *out = sc;
+    return SOLRT_OK;
+}
+
+solrt_status solrt_scene_destroy(solrt_scene* scene) {
+    if (!scene) return SOLRT_OK;
+    cudaStreamSynchronize(scene->ctx->stream);
+    delete scene;
+    return SOLRT_OK;
+}
+
+solrt_status solrt_scene_build_bvh(solrt_scene* scene, const solrt_bvh_desc* bvh) {
+    CHECK_ARG(scene && bvh, "null argument");
+    CHECK_ARG(bvh->kind == SOLRT_BVH2 || bvh->kind == SOLRT_BVH8_Q8, "unknown BVH kind");
+    CHECK_ARG(bvh->leaf_max <= 3, "leaf_max must be 0..3");
+    SOLRT_CUDA(cudaSetDevice(scene->ctx->device));
+    return build_bvh(*scene->ctx, *scene, *bvh);
+}
+
+solrt_status solrt_scene_bvh_info(solrt_scene* scene, solrt_bvh_info* out) {
+    CHECK_ARG(scene && out, "null argument");
+    *out = scene->info;
+    return SOLRT_OK;
+}
+
+solrt_status solrt_scene_bvh_export(solrt_scene* scene, void* nodes, size_t nodes_bytes, void* tris,
+                                    size_t tris_bytes) {
+    CHECK_ARG(scene, "null scene");
+    cudaStream_t st = scene->ctx->stream;
+    if (nodes) {
+        CHECK_ARG(nodes_bytes >= scene->info.node_bytes, "node buffer too small");
+        if (scene->info.node_bytes)
+            SOLRT_CUDA(cudaMemcpyAsync(nodes, scene->nodes.ptr, scene->info.node_bytes, cudaMemcpyDeviceToHost, st));
+    }
+    if (tris) {
+        CHECK_ARG(tris_bytes >= scene->info.tri_bytes, "triangle buffer too small");
+        if (scene->info.tri_bytes)
+            SOLRT_CUDA(cudaMemcpyAsync(tris, scene->tri_wt.ptr, scene->info.tri_bytes, cudaMemcpyDeviceToHost, st));
+    }
+    SOLRT_CUDA(cudaStreamSynchronize(st));
+    return SOLRT_OK;
+}
+
+solrt_status solrt_scene_bytes(solrt_scene* scene, uint64_t* out) {
+    CHECK_ARG(scene && out, "null argument");
+    *out = scene->vpos.bytes + scene->vnrm.bytes + scene->vcol.bytes + scene->tri_idx.bytes +
+           scene->materials.bytes + scene->nodes.bytes + scene->tri_wt.bytes;
+    return SOLRT_OK;
+}
+
+solrt_status solrt_camera_look_at(const float eye[3], const float center[3], const float up[3], float vfov_deg,
+                                  float aspect, float znear, float zfar, solrt_camera* out) {
+    CHECK_ARG(eye && center && up && out, "null argument");
+    // Mat4::look_at_rh(eye, center, up) = look_to_rh(eye, center - eye, up)
+    double f[3] = {(double)center[0] - eye[0], (double)center[1] - eye[1], (double)center[2] - eye[2]};
+    const double fl = std::sqrt(f[0] * f[0] + f[1] * f[1] + f[2] * f[2]);
+    CHECK_ARG(fl > 0.0, "eye equals center");
+    for (double& v : f) v /= fl;
+    double s[3] = {f[1] * up[2] - f[2] * up[1], f[2] * up[0] - f[0] * up[2], f[0] * up[1] - f[1] * up[0]};
+    const double sl = std::sqrt(s[0] * s[0] + s[1] * s[1] + s[2] * s[2]);
+    CHECK_ARG(sl > 0.0, "up is parallel to the view direction");
+    for (double& v : s) v /= sl;
+    const double u[3] = {s[1] * f[2] - s[2] * f[1], s[2] * f[0] - s[0] * f[2], s[0] * f[1] - s[1] * f[0]};
+    const double e[3] = {eye[0], eye[1], eye[2]};
+    const double view[16] = {s[0], u[0], -f[0], 0, s[1], u[1], -f[1], 0, s[2], u[2], -f[2], 0,
+                             -(s[0] * e[0] + s[1] * e[1] + s[2] * e[2]),
+                             -(u[0] * e[0] + u[1] * e[1] + u[2] * e[2]),
+                             (f[0] * e[0] + f[1] * e[1] + f[2] * e[2]), 1};
+    return fill_camera(view, vfov_deg, aspect, znear, zfar, out);
+}
+
+solrt_status solrt_camera_from_view(const float view[16], float vfov_deg, float aspect, float znear, float zfar,
+                                    solrt_camera* out) {
+    CHECK_ARG(view && out, "null argument");
+    double v[16];
+    for (int i = 0; i < 16; ++i) v[i] = view[i];
+    return fill_camera(v, vfov_deg, aspect, znear, zfar, out);
+}
+
+solrt_status solrt_image_create(solrt_context* ctx, uint32_t width, uint32_t height, uint32_t accum_mode,
+                                solrt_image** out) {
+    CHECK_ARG(ctx && out, "null argument");
+    *out = nullptr;
+    CHECK_ARG(width > 0 && height > 0 && (uint64_t)width * height < (1ull << 31), "bad image size");
+    CHECK_ARG(accum_mode == SOLRT_ACCUM_REF_MIX || accum_mode == SOLRT_ACCUM_KAHAN, "bad accumulation mode");
+    solrt_image* img = new (std::nothrow) solrt_image();
+    if (!img) return SOLRT_ERR_OOM;
+    img->ctx = ctx;
+    img->width = width;
+    img->height = height;
+    img->accum_mode = accum_mode;
+    const size_t np = (size_t)width * height;
+    solrt_status s;
+    if ((s = img->accum.alloc(16 * np)) || (s = img->rgba8.alloc(4 * np)) || (s = img->frame_sum.alloc(16 * np)) ||
+        (s = img->rng_state.alloc(4 * np))) {
+        delete img;
+        return s;
+    }
+    if (accum_mode == SOLRT_ACCUM_KAHAN) {
+        if ((s = img->ksum.alloc(16 * np)) || (s = img->kcomp.alloc(16 * np))) {
+            delete img;
+            return s;
+        }
+    }
+    *out = img;
+    return solrt_image_clear(img);
+}
+
+solrt_status solrt_image_destroy(solrt_image* img) {
+    if (!img) return SOLRT_OK;
+    cudaStreamSynchronize(img->ctx->stream);
+    delete img;
+    return SOLRT_OK;
+}
+
+solrt_status solrt_image_clear(solrt_image* img) {
+    CHECK_ARG(img, "null image");
+    cudaStream_t st = img->ctx->stream;
+    for (DeviceBuffer* b : {&img->accum, &img->rgba8, &img->frame_sum, &img->ksum, &img->kcomp, &img->rng_state})
+        if (b->ptr) SOLRT_CUDA(cudaMemsetAsync(b->ptr, 0, b->bytes, st));
+    SOLRT_CUDA(cudaStreamSynchronize(st));
+    return SOLRT_OK;
+}
+
+solrt_status solrt_image_read(solrt_image* img, float* rgba32f, uint8_t* rgba8) {
+    CHECK_ARG(img, "null image");
+    cudaStream_t st = img->ctx->stream;
+    const size_t np = (size_t)img->width * img->height;
+    if (rgba32f) SOLRT_CUDA(cudaMemcpyAsync(rgba32f, img->accum.ptr, 16 * np, cudaMemcpyDeviceToHost, st));
+    if (rgba8) SOLRT_CUDA(cudaMemcpyAsync(rgba8, img->rgba8.ptr, 4 * np, cudaMemcpyDeviceToHost, st));
+    SOLRT_CUDA(cudaStreamSynchronize(st));
+    return check_device_flags(*img->ctx);
+}
+
+solrt_status solrt_image_device_ptrs(solrt_image* img, void** accum, void** rgba8) {
+    CHECK_ARG(img, "null image");
+    if (accum) *accum = img->accum.ptr;
+    if (rgba8) *rgba8 = img->rgba8.ptr;
+    return SOLRT_OK;
+}
+
+solrt_status solrt_render(solrt_context* ctx, solrt_scene* scene, const solrt_camera* camera,
+                          const solrt_render_params* p, solrt_image* img) {
+    CHECK_ARG(ctx && scene && camera && p && img, "null argument");
+    CHECK_ARG(scene->ctx == ctx && img->ctx == ctx, "objects belong to another context");
+    CHECK_ARG(p->width == img->width && p->height == img->height, "params size differs from the image");
+    CHECK_ARG(p->spp >= 1, "spp must be >= 1");
+    CHECK_ARG(p->max_bounces <= SOLRT_MAX_BOUNCES, "max_bounces > 1024");
+    CHECK_ARG(p->accum_mode == img->accum_mode, "accum_mode differs from the image");
+    CHECK_ARG(p->miss_mode <= SOLRT_MISS_GRADIENT, "bad miss mode");
+    CHECK_ARG(p->material_mode <= SOLRT_MATERIAL_LAMBERT, "bad material mode");
+    CHECK_ARG(p->rng_mode <= SOLRT_RNG_PER_SAMPLE, "bad rng mode");
+    CHECK_ARG(p->accum_mode == SOLRT_ACCUM_KAHAN || p->frame + 1u - p->accum_start_frame != 0u,
+              "frame + 1 - accum_start_frame is zero");
+    CHECK_ARG(p->tmax >= 0.0f, "tmax must be >= 0");
+    return render_frame(*ctx, *scene, *camera, *p, *img);
+}
+
+solrt_status solrt_trace_rays(solrt_context* ctx, solrt_scene* scene, const solrt_ray* rays, uint32_t n,
+                              solrt_hit* hits) {
+    CHECK_ARG(ctx && scene, "null argument");
+    CHECK_ARG(n == 0 || (rays && hits), "null ray or hit array");
+    if (n == 0) return SOLRT_OK;
+    DeviceBuffer dr, dh;
+    SOLRT_TRY(dr.alloc(sizeof(solrt_ray) * (size_t)n));
+    SOLRT_TRY(dh.alloc(sizeof(solrt_hit) * (size_t)n));
+    SOLRT_CUDA(cudaMemcpyAsync(dr.ptr, rays, sizeof(solrt_ray) * (size_t)n, cudaMemcpyHostToDevice, ctx->stream));
+    SOLRT_TRY(launch_trace_rays(*ctx, *scene, dr.as<solrt_ray>(), n, dh.as<solrt_hit>()));
+    SOLRT_CUDA(cudaMemcpyAsync(hits, dh.ptr, sizeof(solrt_hit) * (size_t)n, cudaMemcpyDeviceToHost, ctx->stream));
+    SOLRT_CUDA(cudaStreamSynchronize(ctx->stream));
+    return check_device_flags(*ctx);
+}
+
+solrt_status solrt_trace_rays_device(solrt_context* ctx, solrt_scene* scene, const solrt_ray* rays_dev, uint32_t n,
+                                     solrt_hit* hits_dev) {
+    CHECK_ARG(ctx && scene, "null argument");
+    CHECK_ARG(n == 0 || (rays_dev && hits_dev), "null ray or hit array");
+    return launch_trace_rays(*ctx, *scene, rays_dev, n, hits_dev);
+}
+
+solrt_status solrt_debug_unit(solrt_context* ctx, uint32_t op, uint32_t n, const uint32_t* a, const uint32_t* b,
+                              const float* in_f32, uint32_t* out_u32, float* out_f32) {
+    CHECK_ARG(ctx, "null context");
+    return debug_unit(*ctx, op, n, a, b, in_f32, out_u32, out_f32);
+}
+
+}  // extern "C"

@@ -1,0 +1,422 @@
+// bvh_build.cu — GPU LBVH build. Replaces the driver-side BLAS/TLAS builds of
+// the reference (src/ray/acceleration.rs:44-126, 135-239, 344-400), which
+// have no source: on GB300 there are no RT cores, so the hierarchy is built
+// here from the triangles of the flattened scene.
+//
+// Pipeline (all on the context stream):
+//   1. centroids + centroid bounds (block reduction, ordered-int atomics)
+//   2. 30-bit Morton codes of centroids normalised to the centroid bounds
+//   3. stable LSD radix sort of (code, triangle) with 8-bit digits
+//   4. Karras 2012 radix-tree hierarchy over the sorted codes, equal codes
+//      split by index (delta = 32 + clz(i ^ j))
+//   5. bottom-up refit with one arrival flag per node; the second child to
+//      arrive computes the parent box
+//   6. triangle stream in leaf order (48 B per triangle)
+// Min/max are order-independent and the sort is stable, so the topology and
+// every box are a pure function of the input: they equal the CPU LBVH of the
+// oracle bit for bit.
+#include <algorithm>
+
+#include "bvh8.cuh"
+#include "internal.h"
+
+namespace solrt {
+
+namespace {
+
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortThreads * kSortItems;
+
+__device__ __forceinline__ unsigned int float_to_ordered(float f) {
+    const unsigned int b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float ordered_to_float(unsigned int o) {
+    return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
+}
+
+// centroid = ((p0 + p1) + p2) / 3 per axis; bounds as ordered ints.
+__global__ void k_centroids(const float4* __restrict__ vpos, const uint4* __restrict__ tri_idx, uint32_t n,
+                            float4* __restrict__ cen, unsigned int* __restrict__ cb) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    float c[3] = {INFINITY, INFINITY, INFINITY};
+    float mn[3], mx[3];
+    if (i < n) {
+        const uint4 t = tri_idx[i];
+        const float4 a = vpos[t.x], b = vpos[t.y], d = vpos[t.z];
+        c[0] = ((a.x + b.x) + d.x) / 3.0f;
+        c[1] = ((a.y + b.y) + d.y) / 3.0f;
+        c[2] = ((a.z + b.z) + d.z) / 3.0f;
+        cen[i] = make_float4(c[0], c[1], c[2], 0.0f);
+        for (int k = 0; k < 3; ++k) { mn[k] = c[k]; mx[k] = c[k]; }
+    } else {
+        for (int k = 0; k < 3; ++k) { mn[k] = INFINITY; mx[k] = -INFINITY; }
+    }
+    for (int k = 0; k < 3; ++k) {
+        for (int off = 16; off > 0; off >>= 1) {
+            mn[k] = fminf(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], off));
+            mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], off));
+        }
+    }
+    if ((threadIdx.x & 31) == 0) {
+        for (int k = 0; k < 3; ++k) {
+            atomicMin(cb + k, float_to_ordered(mn[k]));
+            atomicMax(cb + 3 + k, float_to_ordered(mx[k]));
+        }
+    }
+}
+
+__device__ __forceinline__ uint32_t expand_bits10(uint32_t v) {
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+__device__ __forceinline__ uint32_t quantise10(float c, float lo, float ext) {
+    if (!(ext > 0.0f)) return 0;
+    const float f = ((c - lo) / ext) * 1024.0f;
+    if (f >= 1023.0f) return 1023;
+    if (!(f > 0.0f)) return 0;
+    return (uint32_t)f;
+}
+
+__global__ void k_morton(const float4* __restrict__ cen, const unsigned int* __restrict__ cb, uint32_t n,
+                         uint32_t* __restrict__ keys, uint32_t* __restrict__ vals) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float lo[3] = {ordered_to_float(cb[0]), ordered_to_float(cb[1]), ordered_to_float(cb[2])};
+    const float hi[3] = {ordered_to_float(cb[3]), ordered_to_float(cb[4]), ordered_to_float(cb[5])};
+    const float4 c = cen[i];
+    const uint32_t qx = quantise10(c.x, lo[0], hi[0] - lo[0]);
+    const uint32_t qy = quantise10(c.y, lo[1], hi[1] - lo[1]);
+    const uint32_t qz = quantise10(c.z, lo[2], hi[2] - lo[2]);
+    keys[i] = (expand_bits10(qx) << 2) | (expand_bits10(qy) << 1) | expand_bits10(qz);
+    vals[i] = i;
+}
+
+// ---- stable LSD radix sort, 8-bit digits -------------------------------------
+// Tile = 2048 keys per block, read in 8 rounds of 256 (item = r*256 + t).
+
+__global__ void __launch_bounds__(kSortThreads) k_radix_hist(const uint32_t* __restrict__ keys, uint32_t n,
+                                                             int shift, uint32_t nblocks,
+                                                             uint32_t* __restrict__ hist) {
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t base = blockIdx.x * kSortTile;
+    for (int r = 0; r < kSortItems; ++r) {
+        const uint32_t idx = base + r * kSortThreads + threadIdx.x;
+        if (idx < n) atomicAdd(&h[(keys[idx] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+}
+
+// Exclusive scan of `len` counts with one block of 1024 threads.
+__global__ void __launch_bounds__(1024) k_scan_exclusive(uint32_t* __restrict__ data, uint32_t len) {
+    __shared__ uint32_t warp_sums[32];
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (uint32_t base = 0; base < len; base += 1024) {
+        const uint32_t idx = base + threadIdx.x;
+        const uint32_t v = idx < len ? data[idx] : 0u;
+        uint32_t x = v;
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+            if (lane >= off) x += y;
+        }
+        if (lane == 31) warp_sums[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t w = warp_sums[lane];
+            for (int off = 1; off < 32; off <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, w, off);
+                if (lane >= off) w += y;
+            }
+            warp_sums[lane] = w;
+        }
+        __syncthreads();
+        const uint32_t incl = x + (warp > 0 ? warp_sums[warp - 1] : 0u) + carry;
+        if (idx < len) data[idx] = incl - v;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = incl;
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint32_t* __restrict__ kin,
+                                                                const uint32_t* __restrict__ vin,
+                                                                uint32_t* __restrict__ kout,
+                                                                uint32_t* __restrict__ vout,
+                                                                const uint32_t* __restrict__ scan, uint32_t n,
+                                                                int shift, uint32_t nblocks) {
+    __shared__ uint32_t base[256];
+    __shared__ uint32_t wcount[kSortThreads / 32][256];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    base[t] = scan[t * nblocks + blockIdx.x];
+    const uint32_t lane_lt = (1u << lane) - 1u;
+    const uint32_t tile = blockIdx.x * kSortTile;
+    for (int r = 0; r < kSortItems; ++r) {
+        for (int d = lane; d < 256; d += 32) wcount[warp][d] = 0;
+        __syncthreads();
+        const uint32_t idx = tile + r * kSortThreads + t;
+        const bool valid = idx < n;
+        const uint32_t key = valid ? kin[idx] : 0u;
+        const uint32_t digit = valid ? ((key >> shift) & 255u) : 256u;
+        const uint32_t peers = __match_any_sync(0xffffffffu, digit);
+        const uint32_t rank = __popc(peers & lane_lt);
+        if (valid && rank == 0) wcount[warp][digit] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            uint32_t off = base[digit] + rank;
+            for (int w = 0; w < warp; ++w) off += wcount[w][digit];
+            if (off < n) {
+                kout[off] = key;
+                vout[off] = vin[idx];
+            }
+        }
+        __syncthreads();
+        uint32_t tot = 0;
+        for (int w = 0; w < kSortThreads / 32; ++w) tot += wcount[w][t];
+        base[t] += tot;
+        __syncthreads();
+    }
+}
+
+// ---- Karras hierarchy ------------------------------------------------------
+
+__device__ __forceinline__ int kdelta(const uint32_t* __restrict__ k, int64_t n, int64_t i, int64_t j) {
+    if (j < 0 || j > n - 1) return -1;
+    const uint32_t a = k[i], b = k[j];
+    if (a == b) return 32 + __clz((uint32_t)i ^ (uint32_t)j);
+    return __clz(a ^ b);
+}
+
+// child[2i], child[2i+1]: internal index, or 0x80000000 | leaf position.
+__global__ void k_karras(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ child,
+                         uint32_t* __restrict__ parent_int, uint32_t* __restrict__ parent_leaf) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= (int64_t)n - 1) return;
+    const int d = (kdelta(keys, n, i, i + 1) - kdelta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+    const int dmin = kdelta(keys, n, i, i - d);
+    int64_t lmax = 2;
+    while (kdelta(keys, n, i, i + lmax * d) > dmin) lmax *= 2;
+    int64_t l = 0;
+    for (int64_t t = lmax / 2; t >= 1; t /= 2)
+        if (kdelta(keys, n, i, i + (l + t) * d) > dmin) l += t;
+    const int64_t j = i + l * d;
+    const int dnode = kdelta(keys, n, i, j);
+    int64_t s = 0, t = l;
+    do {
+        t = (t + 1) >> 1;
+        if (kdelta(keys, n, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    const int64_t g = i + s * d + (d < 0 ? d : 0);
+    const int64_t lo = i < j ? i : j, hi = i < j ? j : i;
+    uint32_t left, right;
+    if (lo == g) { left = 0x80000000u | (uint32_t)g; parent_leaf[g] = (uint32_t)i; }
+    else { left = (uint32_t)g; parent_int[g] = (uint32_t)i; }
+    if (hi == g + 1) { right = 0x80000000u | (uint32_t)(g + 1); parent_leaf[g + 1] = (uint32_t)i; }
+    else { right = (uint32_t)(g + 1); parent_int[g + 1] = (uint32_t)i; }
+    child[2 * i] = left;
+    child[2 * i + 1] = right;
+}
+
+__device__ __forceinline__ int bvh2_ref(uint32_t r) {
+    return (r & 0x80000000u) ? ~(int)(r & 0x7fffffffu) : (int)r;
+}
+
+// Leaf boxes + refit. Each thread starts at a leaf; the second thread to
+// arrive at a node computes its box from both children and continues upward.
+// Boxes of internal nodes go to `nbox` (lo.xyz, hi.xyz as 2 float4) and into
+// the child slots of the parent's BVH2 node.
+__global__ void k_refit(const float4* __restrict__ vpos, const uint4* __restrict__ tri_idx,
+                        const uint32_t* __restrict__ order, const uint32_t* __restrict__ child,
+                        const uint32_t* __restrict__ parent_int, const uint32_t* __restrict__ parent_leaf,
+                        uint32_t n, unsigned int* __restrict__ flags, float4* __restrict__ nbox,
+                        float4* __restrict__ nodes, float4* __restrict__ tri_wt) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t prim = order[k];
+    const uint4 ti = tri_idx[prim];
+    const float4 a = vpos[ti.x], b = vpos[ti.y], c = vpos[ti.z];
+    tri_wt[3 * (size_t)k + 0] = make_float4(a.x, a.y, a.z, __uint_as_float(prim));
+    tri_wt[3 * (size_t)k + 1] = make_float4(b.x, b.y, b.z, 0.0f);
+    tri_wt[3 * (size_t)k + 2] = make_float4(c.x, c.y, c.z, 0.0f);
+    float lo[3] = {fminf(fminf(a.x, b.x), c.x), fminf(fminf(a.y, b.y), c.y), fminf(fminf(a.z, b.z), c.z)};
+    float hi[3] = {fmaxf(fmaxf(a.x, b.x), c.x), fmaxf(fmaxf(a.y, b.y), c.y), fmaxf(fmaxf(a.z, b.z), c.z)};
+    if (n == 1) {
+        // single triangle: one node whose two children are the same leaf.
+        nodes[0] = make_float4(lo[0], hi[0], lo[1], hi[1]);
+        nodes[1] = make_float4(lo[0], hi[0], lo[1], hi[1]);
+        nodes[2] = make_float4(lo[2], hi[2], lo[2], hi[2]);
+        nodes[3] = make_float4(__int_as_float(~0), __int_as_float(~0), 0.0f, 0.0f);
+        nbox[0] = make_float4(lo[0], lo[1], lo[2], 0.0f);
+        nbox[1] = make_float4(hi[0], hi[1], hi[2], 0.0f);
+        return;
+    }
+    uint32_t cur = 0x80000000u | k;
+    uint32_t p = parent_leaf[k];
+    for (uint32_t steps = 0; steps < n; ++steps) {
+        if (p >= n - 1) return;  // malformed parent link: stop (node left unset)
+        const bool is_left = child[2 * p] == cur;
+        float4* np = nodes + 4 * (size_t)p;
+        if (is_left) {
+            np[0] = make_float4(lo[0], hi[0], lo[1], hi[1]);
+            reinterpret_cast<float2*>(np + 2)[0] = make_float2(lo[2], hi[2]);
+        } else {
+            np[1] = make_float4(lo[0], hi[0], lo[1], hi[1]);
+            reinterpret_cast<float2*>(np + 2)[1] = make_float2(lo[2], hi[2]);
+        }
+        __threadfence();
+        if (atomicAdd(flags + p, 1u) == 0u) return;
+        __threadfence();
+        const float4 s0 = __ldcg(np + 0), s1 = __ldcg(np + 1), s2 = __ldcg(np + 2);
+        lo[0] = fminf(s0.x, s1.x); hi[0] = fmaxf(s0.y, s1.y);
+        lo[1] = fminf(s0.z, s1.z); hi[1] = fmaxf(s0.w, s1.w);
+        lo[2] = fminf(s2.x, s2.z); hi[2] = fmaxf(s2.y, s2.w);
+        np[3] = make_float4(__int_as_float(bvh2_ref(child[2 * p])), __int_as_float(bvh2_ref(child[2 * p + 1])),
+                            0.0f, 0.0f);
+        nbox[2 * (size_t)p + 0] = make_float4(lo[0], lo[1], lo[2], 0.0f);
+        nbox[2 * (size_t)p + 1] = make_float4(hi[0], hi[1], hi[2], 0.0f);
+        if (p == 0) return;
+        cur = p;
+        p = parent_int[p];
+    }
+}
+
+// Depth of every leaf (ancestors + 1), reduced with atomicMax.
+__global__ void k_depth(const uint32_t* __restrict__ parent_int, const uint32_t* __restrict__ parent_leaf,
+                        uint32_t n, unsigned int* __restrict__ depth) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n || n < 2) return;
+    uint32_t d = 1;
+    uint32_t p = parent_leaf[k];
+    while (p != 0 && p < n - 1 && d < n) {
+        p = parent_int[p];
+        ++d;
+    }
+    atomicMax(depth, d + 1);
+}
+
+inline uint32_t blocks_for(uint64_t n, uint32_t b) { return (uint32_t)((n + b - 1) / b); }
+
+}  // namespace
+
+// Builds the LBVH of `sc` (and the 8-wide collapse when asked). Scratch is
+// allocated for the duration of the build. Synchronises.
+solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
+    const uint32_t n = sc.tri_count;
+    cudaStream_t st = ctx.stream;
+    sc.info = solrt_bvh_info{};
+    sc.info.kind = desc.kind;
+    sc.info.tri_count = n;
+    sc.nodes.release();
+    sc.tri_wt.release();
+    if (n == 0) return SOLRT_OK;
+
+    SOLRT_CUDA(cudaEventRecord(ctx.ev0, st));
+    const uint32_t ni = n > 1 ? n - 1 : 1;  // internal nodes (one for a single triangle)
+    DeviceBuffer cen, cb, keys[2], vals[2], hist, child, par_int, par_leaf, flags, nbox, depth, bvh2_nodes;
+    SOLRT_TRY(cen.alloc(sizeof(float4) * (size_t)n));
+    SOLRT_TRY(cb.alloc(6 * sizeof(unsigned int)));
+    for (int i = 0; i < 2; ++i) {
+        SOLRT_TRY(keys[i].alloc(sizeof(uint32_t) * (size_t)n));
+        SOLRT_TRY(vals[i].alloc(sizeof(uint32_t) * (size_t)n));
+    }
+    const uint32_t nblocks = blocks_for(n, kSortTile);
+    SOLRT_TRY(hist.alloc(sizeof(uint32_t) * 256 * (size_t)nblocks));
+    SOLRT_TRY(child.alloc(sizeof(uint32_t) * 2 * (size_t)ni));
+    SOLRT_TRY(par_int.alloc(sizeof(uint32_t) * (size_t)ni));
+    SOLRT_TRY(par_leaf.alloc(sizeof(uint32_t) * (size_t)n));
+    SOLRT_TRY(flags.alloc(sizeof(unsigned int) * (size_t)ni));
+    SOLRT_TRY(nbox.alloc(2 * sizeof(float4) * (size_t)ni));
+    SOLRT_TRY(depth.alloc(sizeof(unsigned int)));
+    SOLRT_TRY(bvh2_nodes.alloc(4 * sizeof(float4) * (size_t)ni));
+    SOLRT_TRY(sc.tri_wt.alloc(3 * sizeof(float4) * (size_t)n));
+
+    const unsigned int cb_init[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
+    SOLRT_CUDA(cudaMemcpyAsync(cb.ptr, cb_init, sizeof(cb_init), cudaMemcpyHostToDevice, st));
+    SOLRT_CUDA(cudaMemsetAsync(flags.ptr, 0, flags.bytes, st));
+    SOLRT_CUDA(cudaMemsetAsync(depth.ptr, 0, depth.bytes, st));
+    SOLRT_CUDA(cudaMemsetAsync(par_int.ptr, 0xff, par_int.bytes, st));
+
+    k_centroids<<<blocks_for(n, 256), 256, 0, st>>>(sc.vpos.as<float4>(), sc.tri_idx.as<uint4>(), n,
+                                                    cen.as<float4>(), cb.as<unsigned int>());
+    k_morton<<<blocks_for(n, 256), 256, 0, st>>>(cen.as<float4>(), cb.as<unsigned int>(), n, keys[0].as<uint32_t>(),
+                                                 vals[0].as<uint32_t>());
+    int cur = 0;
+    for (int shift = 0; shift < 30; shift += 8) {
+        k_radix_hist<<<nblocks, kSortThreads, 0, st>>>(keys[cur].as<uint32_t>(), n, shift, nblocks,
+                                                       hist.as<uint32_t>());
+        k_scan_exclusive<<<1, 1024, 0, st>>>(hist.as<uint32_t>(), 256 * nblocks);
+        k_radix_scatter<<<nblocks, kSortThreads, 0, st>>>(keys[cur].as<uint32_t>(), vals[cur].as<uint32_t>(),
+                                                          keys[cur ^ 1].as<uint32_t>(), vals[cur ^ 1].as<uint32_t>(),
+                                                          hist.as<uint32_t>(), n, shift, nblocks);
+        cur ^= 1;
+        ctx.launches += 3;
+    }
+    if (n > 1) {
+        k_karras<<<blocks_for(n - 1, 256), 256, 0, st>>>(keys[cur].as<uint32_t>(), n, child.as<uint32_t>(),
+                                                         par_int.as<uint32_t>(), par_leaf.as<uint32_t>());
+        ++ctx.launches;
+    }
+    k_refit<<<blocks_for(n, 256), 256, 0, st>>>(sc.vpos.as<float4>(), sc.tri_idx.as<uint4>(), vals[cur].as<uint32_t>(),
+                                                child.as<uint32_t>(), par_int.as<uint32_t>(), par_leaf.as<uint32_t>(),
+                                                n, flags.as<unsigned int>(), nbox.as<float4>(),
+                                                bvh2_nodes.as<float4>(), sc.tri_wt.as<float4>());
+    k_depth<<<blocks_for(n, 256), 256, 0, st>>>(par_int.as<uint32_t>(), par_leaf.as<uint32_t>(), n,
+                                                depth.as<unsigned int>());
+    ctx.launches += 5;
+    SOLRT_CUDA(cudaGetLastError());
+
+    if (desc.kind == SOLRT_BVH8_Q8) {
+        Bvh8BuildInput in;
+        in.n = n;
+        in.child = child.as<uint32_t>();
+        in.nbox = nbox.as<float4>();
+        in.tri_wt_leaf = sc.tri_wt.as<float4>();
+        in.leaf_max = desc.leaf_max == 0 ? 3u : std::min(3u, desc.leaf_max);
+        DeviceBuffer tri8;
+        uint32_t node_count = 0, depth8 = 0;
+        SOLRT_TRY(build_bvh8(ctx, in, sc.nodes, tri8, &node_count, &depth8));
+        sc.tri_wt.release();
+        sc.tri_wt.ptr = tri8.ptr;
+        sc.tri_wt.bytes = tri8.bytes;
+        tri8.ptr = nullptr;
+        tri8.bytes = 0;
+        sc.info.node_count = node_count;
+        sc.info.depth = depth8;
+        sc.info.node_bytes = (uint64_t)node_count * 80u;
+    } else {
+        sc.nodes.ptr = bvh2_nodes.ptr;
+        sc.nodes.bytes = bvh2_nodes.bytes;
+        bvh2_nodes.ptr = nullptr;
+        bvh2_nodes.bytes = 0;
+        sc.info.node_count = ni;
+        sc.info.node_bytes = (uint64_t)ni * 64u;
+        unsigned int dh = 0;
+        SOLRT_CUDA(cudaMemcpyAsync(&dh, depth.ptr, sizeof(dh), cudaMemcpyDeviceToHost, st));
+        SOLRT_CUDA(cudaStreamSynchronize(st));
+        sc.info.depth = n > 1 ? dh : 1;
+    }
+    sc.info.tri_bytes = sc.tri_wt.bytes;
+    sc.info.shade_bytes = sc.vpos.bytes + sc.vnrm.bytes + sc.vcol.bytes + sc.tri_idx.bytes + sc.materials.bytes;
+    SOLRT_CUDA(cudaEventRecord(ctx.ev1, st));
+    SOLRT_CUDA(cudaEventSynchronize(ctx.ev1));
+    float ms = 0.0f;
+    SOLRT_CUDA(cudaEventElapsedTime(&ms, ctx.ev0, ctx.ev1));
+    sc.info.build_ms = ms;
+    if (sc.info.kind == SOLRT_BVH2 && sc.info.depth > SOLRT_BVH2_STACK) {
+        set_error("BVH2 depth %u exceeds the traversal stack (%d)", sc.info.depth, SOLRT_BVH2_STACK);
+        return SOLRT_ERR_CAPACITY;
+    }
+    return SOLRT_OK;
+}
+
+}  // namespace solrt

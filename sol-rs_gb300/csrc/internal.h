@@ -1,0 +1,188 @@
+// internal.h — host-side objects behind the solrt C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/solrt.h"
+#include "traverse.cuh"
+
+namespace solrt {
+
+void set_error(const char* fmt, ...);
+
+// Returns from the calling function with SOLRT_ERR_DEVICE on a CUDA error.
+#define SOLRT_CUDA(call)                                                              \
+    do {                                                                              \
+        cudaError_t e_ = (call);                                                      \
+        if (e_ != cudaSuccess) {                                                      \
+            ::solrt::set_error("%s:%d %s: %s", __FILE__, __LINE__, #call,             \
+                               cudaGetErrorString(e_));                               \
+            return e_ == cudaErrorMemoryAllocation ? SOLRT_ERR_OOM : SOLRT_ERR_DEVICE; \
+        }                                                                             \
+    } while (0)
+
+#define SOLRT_TRY(expr)                          \
+    do {                                         \
+        solrt_status s_ = (expr);                \
+        if (s_ != SOLRT_OK) return s_;           \
+    } while (0)
+
+// Owning device allocation.
+struct DeviceBuffer {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    DeviceBuffer() = default;
+    DeviceBuffer(const DeviceBuffer&) = delete;
+    DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+    ~DeviceBuffer() { release(); }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+    solrt_status alloc(size_t n) {
+        if (n <= bytes && ptr) return SOLRT_OK;
+        release();
+        if (n == 0) return SOLRT_OK;
+        cudaError_t e = cudaMalloc(&ptr, n);
+        if (e != cudaSuccess) {
+            ptr = nullptr;
+            set_error("cudaMalloc(%zu): %s", n, cudaGetErrorString(e));
+            return SOLRT_ERR_OOM;
+        }
+        bytes = n;
+        return SOLRT_OK;
+    }
+    template <class T> T* as() const { return reinterpret_cast<T*>(ptr); }
+};
+
+// Statistics and error word kept on the device.
+struct DevStats {
+    unsigned long long segments;
+    unsigned long long paths;
+    unsigned long long node_visits;
+    unsigned long long tri_tests;
+    unsigned long long fp64_fallbacks;
+    unsigned int eflags;
+    unsigned int pad;
+};
+
+// Per-pass control block: queue lengths and work counters per bounce.
+#define SOLRT_MAX_BOUNCES 1024
+struct PassCtl {
+    unsigned int count[SOLRT_MAX_BOUNCES + 2];
+    unsigned int work[SOLRT_MAX_BOUNCES + 2];
+};
+
+// Structure-of-arrays path queue (one wavefront).
+struct PathQueue {
+    float4* o_tmin;   // origin, tmin
+    float4* d_tmax;   // direction, tmax
+    float4* thr_rng;  // throughput, rng state (bits)
+    uint2* meta;      // slot within the pass, depth
+};
+
+struct Context {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    uint32_t capacity = 0;
+    bool counters = false;
+    uint32_t block_size = 0;
+    DeviceBuffer q_o[2], q_d[2], q_thr[2], q_meta[2];
+    DeviceBuffer hits, rad, ctl, stats;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    uint64_t launches = 0;
+    double last_render_ms = 0.0;
+    int extend_blocks_per_sm = 0;
+    // stage timing (enable_timing): event pairs recorded around launches
+    bool timing = false;
+    struct TimedLaunch {
+        cudaEvent_t start, end;
+        int stage;  // 0 extend, 1 shade
+    };
+    std::vector<TimedLaunch> timed;
+    size_t timed_used = 0;
+    double extend_ms = 0.0, shade_ms = 0.0;
+    uint64_t extend_launches = 0, shade_launches = 0;
+    // Records the start event of a timed launch of `stage`; returns its slot.
+    int timing_begin(int stage) {
+        if (!timing) return -1;
+        if (timed_used == timed.size()) {
+            TimedLaunch t{};
+            if (cudaEventCreate(&t.start) != cudaSuccess || cudaEventCreate(&t.end) != cudaSuccess) return -1;
+            timed.push_back(t);
+        }
+        timed[timed_used].stage = stage;
+        cudaEventRecord(timed[timed_used].start, stream);
+        return (int)timed_used++;
+    }
+    void timing_end(int slot) {
+        if (slot >= 0) cudaEventRecord(timed[slot].end, stream);
+    }
+    // Adds the elapsed times of all recorded launches (stream must be idle).
+    void timing_collect() {
+        for (size_t i = 0; i < timed_used; ++i) {
+            float ms = 0.0f;
+            if (cudaEventElapsedTime(&ms, timed[i].start, timed[i].end) == cudaSuccess) {
+                if (timed[i].stage == 0) { extend_ms += ms; ++extend_launches; }
+                else { shade_ms += ms; ++shade_launches; }
+            }
+        }
+        timed_used = 0;
+    }
+    PathQueue queue(int i) const {
+        return PathQueue{q_o[i].as<float4>(), q_d[i].as<float4>(), q_thr[i].as<float4>(), q_meta[i].as<uint2>()};
+    }
+};
+
+struct Scene {
+    Context* ctx = nullptr;
+    uint32_t tri_count = 0;
+    uint32_t vertex_count = 0;
+    uint32_t material_count = 0;
+    DeviceBuffer vpos, vnrm, vcol, tri_idx, materials;
+    DeviceBuffer nodes, tri_wt;
+    solrt_bvh_info info{};
+    DevScene view() const {
+        DevScene d;
+        d.tri_count = tri_count;
+        d.bvh_kind = info.kind;
+        d.node_count = info.node_count;
+        d.vpos = vpos.as<float4>();
+        d.vnrm = vnrm.as<float4>();
+        d.vcol = vcol.as<float4>();
+        d.tri_idx = tri_idx.as<uint4>();
+        d.materials = materials.as<float4>();
+        d.nodes = nodes.as<float4>();
+        d.tri_wt = tri_wt.as<float4>();
+        return d;
+    }
+};
+
+struct Image {
+    Context* ctx = nullptr;
+    uint32_t width = 0, height = 0, accum_mode = 0;
+    DeviceBuffer accum, rgba8, frame_sum, ksum, kcomp, rng_state;
+};
+
+// bvh_build.cu
+solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc);
+
+// trace.cu
+solrt_status launch_trace_rays(Context& ctx, const Scene& sc, const solrt_ray* rays, uint32_t n, solrt_hit* hits);
+solrt_status launch_extend(Context& ctx, const Scene& sc, const PathQueue& q, float4* hits,
+                           const unsigned int* count, unsigned int* work, uint32_t capacity);
+
+// pathtrace.cu
+solrt_status render_frame(Context& ctx, const Scene& sc, const solrt_camera& cam, const solrt_render_params& p,
+                          Image& img);
+solrt_status debug_unit(Context& ctx, uint32_t op, uint32_t n, const uint32_t* a, const uint32_t* b,
+                        const float* in_f32, uint32_t* out_u32, float* out_f32);
+
+}  // namespace solrt

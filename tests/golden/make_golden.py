@@ -1,0 +1,117 @@
+"""Generates tests/golden/glsl_sampling.json from the reference's own shaders.
+
+Builds oracle/_ref/libref_glsl.so (the reference's assets/glsl/sampling.glsl
+and postprocess.glsl compiled as C++ by oracle/ref_glsl/build_ref.py) and
+records, with float bit patterns, the outputs of:
+  tea, nextRand sequences, nextRand2, buildOrthonormalBasis,
+  fresnelDielectric, sampleGGXDistribution,
+  sampleCosineWeightedHemisphere and gammaCorrect
+on seeded inputs. Run in a checkout next to the reference:
+
+    python tests/golden/make_golden.py
+"""
+import ctypes
+import json
+import os
+import struct
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle", "ref_glsl"))
+
+import build_ref  # noqa: E402
+
+
+def fbits(x):
+    return struct.unpack("<I", struct.pack("<f", float(x)))[0]
+
+
+def main():
+    lib = ctypes.CDLL(build_ref.build())
+    f3 = ctypes.c_float * 3
+    lib.ref_tea.restype = ctypes.c_uint32
+    lib.ref_tea.argtypes = [ctypes.c_uint32, ctypes.c_uint32]
+    lib.ref_next_rand.restype = ctypes.c_float
+    lib.ref_next_rand.argtypes = [ctypes.POINTER(ctypes.c_uint32)]
+    lib.ref_fresnel.restype = ctypes.c_float
+    rng = np.random.default_rng(20261203)
+
+    out = {"source": "reference assets/glsl/sampling.glsl + postprocess.glsl compiled as C++",
+           "float_encoding": "IEEE-754 binary32 bit patterns"}
+
+    # tea on (pixel, frame) style pairs and random pairs
+    pairs = [(0, 0), (1, 0), (0, 1), (65535, 7), (0xffffffff, 0xffffffff)]
+    pairs += [(int(a), int(b)) for a, b in zip(rng.integers(0, 2**32, 59, dtype=np.uint64),
+                                               rng.integers(0, 2**32, 59, dtype=np.uint64))]
+    pairs += [(x + y * 256, f) for x, y, f in [(3, 5, 0), (255, 255, 12), (17, 200, 1000)]]
+    out["tea"] = [[a, b, lib.ref_tea(a, b)] for a, b in pairs]
+
+    # nextRand sequences from TEA seeds
+    seqs = []
+    for seed in [0, 1, lib.ref_tea(0, 0), lib.ref_tea(123, 4), 0xdeadbeef, 0xffffffff]:
+        st = ctypes.c_uint32(seed)
+        vals = []
+        for _ in range(48):
+            r = lib.ref_next_rand(ctypes.byref(st))
+            vals.append([fbits(r), st.value])
+        seqs.append({"seed": seed, "steps": vals})
+    out["next_rand"] = seqs
+
+    # nextRand2: order of the two draws
+    st = ctypes.c_uint32(lib.ref_tea(7, 9))
+    o2 = (ctypes.c_float * 2)()
+    lib.ref_next_rand2(ctypes.byref(st), o2)
+    out["next_rand2"] = {"seed": lib.ref_tea(7, 9), "out": [fbits(o2[0]), fbits(o2[1])], "state": st.value}
+
+    def rand_unit(n):
+        v = rng.normal(size=(n, 3)).astype(np.float32)
+        v /= np.linalg.norm(v, axis=1, keepdims=True)
+        return v.astype(np.float32)
+
+    normals = np.concatenate([rand_unit(60), np.array(
+        [[0, 0, 1], [0, 0, -1], [1, 0, 0], [0, 1, 0], [0, -1, 0], [0.6, 0, -0.8]], np.float32)])
+
+    onb = []
+    for n in normals:
+        u, v = f3(), f3()
+        lib.ref_onb(f3(*n), u, v)
+        onb.append([[fbits(c) for c in n], [fbits(c) for c in u], [fbits(c) for c in v]])
+    out["onb"] = onb
+
+    fres = []
+    for i, m in zip(rand_unit(64), rand_unit(64)):
+        for eta in (np.float32(1.0) / np.float32(1.5), np.float32(1.5)):
+            r = lib.ref_fresnel(f3(*i), f3(*m), ctypes.c_float(eta))
+            fres.append([[fbits(c) for c in i], [fbits(c) for c in m], fbits(eta), fbits(r)])
+    out["fresnel"] = fres
+
+    ggx, cosw = [], []
+    xis = rng.random((len(normals), 2)).astype(np.float32)
+    alphas = np.concatenate([[0.0, 1.0, 0.8002925], rng.random(len(normals) - 3)]).astype(np.float32) ** 2
+    for n, xi, a2 in zip(normals, xis, alphas):
+        o = f3()
+        lib.ref_sample_ggx(f3(*n), ctypes.c_float(xi[0]), ctypes.c_float(xi[1]), ctypes.c_float(a2), o)
+        ggx.append([[fbits(c) for c in n], fbits(xi[0]), fbits(xi[1]), fbits(a2), [fbits(c) for c in o]])
+        lib.ref_sample_cosine(f3(*n), ctypes.c_float(xi[0]), ctypes.c_float(xi[1]), o)
+        cosw.append([[fbits(c) for c in n], fbits(xi[0]), fbits(xi[1]), [fbits(c) for c in o]])
+    out["sample_ggx"] = ggx
+    out["sample_cosine"] = cosw
+
+    gam = []
+    for c in np.concatenate([[0.0, 1.0, 0.5, 1e-6, 2.0], rng.random(59) * 1.2]).astype(np.float32):
+        o = f3()
+        lib.ref_gamma(f3(c, c, c), ctypes.c_float(2.2), o)
+        gam.append([fbits(c), fbits(o[0])])
+    out["gamma"] = gam
+
+    path = os.path.join(HERE, "glsl_sampling.json")
+    with open(path, "w") as f:
+        json.dump(out, f, separators=(",", ":"))
+    print("wrote", path)
+
+
+if __name__ == "__main__":
+    main()

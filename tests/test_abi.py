@@ -1,0 +1,70 @@
+"""The C-ABI library: it loads, exports every function include/solrt.h
+declares, its structs have the reference's sizes, and host-only entry
+points behave (no device compute here)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = []
+    for hdr in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if hdr.endswith(".h"):
+            src = open(os.path.join(ROOT, "include", hdr)).read()
+            src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+            names += re.findall(r"^\s*(?:const\s+)?[\w\*\s]+?\b(solrt_\w+)\s*\(", src, flags=re.M)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol(solrt):
+    L = solrt.lib()
+    names = declared_functions()
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_struct_sizes(solrt):
+    api = solrt.api
+    assert ctypes.sizeof(api.Vertex) == 64          # ModelVertex
+    assert ctypes.sizeof(api.Material) == 48        # MaterialInfo
+    assert ctypes.sizeof(api.Instance) == 144       # SceneInstance
+    assert ctypes.sizeof(api.Camera) == 256
+    assert ctypes.sizeof(api.RenderParams) == 64
+    assert solrt.RAY_DTYPE.itemsize == 32 and solrt.HIT_DTYPE.itemsize == 16
+    assert solrt.scenes.VERTEX_DTYPE.itemsize == 64 and solrt.scenes.INSTANCE_DTYPE.itemsize == 144
+
+
+def test_abi_version_and_status_strings(solrt):
+    L = solrt.lib()
+    assert L.solrt_abi_version() == 1
+    assert L.solrt_status_string(0) == b"ok"
+    assert L.solrt_status_string(5) == b"capacity exceeded"
+
+
+def test_camera_is_host_math(solrt):
+    c = solrt.camera_look_at((0.5, 0.5, -1.4), (0.5, 0.5, 0.5), (0, -1, 0), 40.0, 1.0)
+    V = np.array(c.view, np.float64).reshape(4, 4).T
+    Vi = np.array(c.view_inverse, np.float64).reshape(4, 4).T
+    assert np.allclose(V @ Vi, np.eye(4), atol=1e-6)
+    with pytest.raises(solrt.SolrtError):
+        solrt.camera_look_at((0, 0, 0), (0, 0, 0), (0, 1, 0), 40.0, 1.0)
+    with pytest.raises(solrt.SolrtError):
+        solrt.camera_look_at((0, 0, 1), (0, 0, 0), (0, 1, 0), 0.0, 1.0)
+
+
+def test_context_without_gpu_fails_cleanly(solrt):
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("GPU present")
+    except Exception:
+        pass
+    with pytest.raises(solrt.SolrtError) as e:
+        solrt.Context(0)
+    assert e.value.status == 3   # SOLRT_ERR_DEVICE

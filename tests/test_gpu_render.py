@@ -1,0 +1,145 @@
+"""Radiance parity on identical RNG streams: the wavefront CUDA renderer
+against the oracle's sequential per-pixel evaluation of pathtrace.rgen /
+.rchit / .rmiss. The RGBA32F accumulation image must match bit for bit; the
+RGBA8 image within 1 (gamma uses powf on the device, the C library's pow on
+the host); the count of traced segments must be equal."""
+import numpy as np
+import pytest
+
+from helpers import S, camera_of, transformed_cornell
+
+pytestmark = pytest.mark.gpu
+
+
+def cornell_ref_materials():
+    """Cornell box with cornell.gltf-like materials: a mirror tall box
+    (metallic 1, roughness 0), glossy walls (roughness 0.89), light 15."""
+    d = S.cornell(light=(15.0, 15.0, 15.0))
+    d.materials["roughness"] = 0.8945907
+    d.materials["metallic"][1] = 0.0
+    # tall box is the last section; give it its own mirror material
+    mats = list(d.materials)
+    mats.append(S.material(base=(0.72, 0.72, 0.72), metallic=0.9999999776, roughness=0.0))
+    d.materials = np.array(mats, S.MATERIAL_DTYPE)
+    d.sections["material_index"][-1] = len(mats) - 1
+    return d
+
+
+def _case(name):
+    A = importlib_solrt()
+    if name == "cornell_lambert":
+        return S.cornell(), 64, 64, dict(spp=4, max_bounces=5, material_mode=A.MATERIAL_LAMBERT,
+                                         rng_mode=A.RNG_PER_SAMPLE, seed=1)
+    if name == "cornell_ref_stream":
+        return cornell_ref_materials(), 48, 40, dict(spp=3, max_bounces=32, material_mode=A.MATERIAL_REF,
+                                                     rng_mode=A.RNG_REF_STREAM)
+    if name == "cornell_ref_sky":
+        return cornell_ref_materials(), 40, 32, dict(spp=2, max_bounces=8, material_mode=A.MATERIAL_REF,
+                                                     rng_mode=A.RNG_PER_SAMPLE, miss_mode=A.MISS_REF_SKY)
+    if name == "transformed":
+        return transformed_cornell(), 32, 32, dict(spp=2, max_bounces=5, material_mode=A.MATERIAL_REF,
+                                                   rng_mode=A.RNG_PER_SAMPLE, seed=7)
+    if name == "soup_gradient":
+        return S.soup(30000, seed=2), 64, 36, dict(spp=2, max_bounces=4, material_mode=A.MATERIAL_LAMBERT,
+                                                   rng_mode=A.RNG_PER_SAMPLE, seed=2, miss_mode=A.MISS_GRADIENT)
+    if name == "tunnel_kahan":
+        return S.tunnel(n_ang=256, n_ax=128, length=25.0), 64, 36, dict(
+            spp=2, max_bounces=8, material_mode=A.MATERIAL_LAMBERT, rng_mode=A.RNG_PER_SAMPLE, seed=3,
+            miss_mode=A.MISS_REF_SKY, accum_mode=A.ACCUM_KAHAN)
+    raise KeyError(name)
+
+
+def importlib_solrt():
+    import importlib
+    return importlib.import_module("sol-rs_gb300")
+
+
+def _render_both(solrt, oracle, ctx, data, w, h, kw, frames=2, bvh=None):
+    bvh = solrt.BVH2 if bvh is None else bvh
+    cam = camera_of(data, w / h)
+    sc = solrt.SceneDescription(ctx, data, bvh=bvh)
+    mode = kw.get("accum_mode", solrt.ACCUM_REF_MIX)
+    img = solrt.Image(ctx, w, h, mode)
+    r = solrt.Renderer(ctx)
+    o = oracle.OracleScene(data)
+    acc = np.zeros((h, w, 4), np.float32)
+    ks = np.zeros((h, w, 4), np.float32) if mode == solrt.ACCUM_KAHAN else None
+    kc = np.zeros((h, w, 4), np.float32) if mode == solrt.ACCUM_KAHAN else None
+    seg_o = 0
+    ctx.reset_stats()
+    for f in range(frames):
+        p = solrt.render_params(w, h, frame=f, **kw)
+        r.cmd_trace_rays(sc, cam, p, img)
+        acc, rgba_o, st = o.render(cam, p, accum=acc, ksum=ks, kcomp=kc)
+        seg_o += st.segments
+    ctx.synchronize()
+    ga, g8 = img.read()
+    stats = ctx.stats()
+    return ga, g8, acc, rgba_o, stats, seg_o
+
+
+@pytest.mark.parametrize("name", ["cornell_lambert", "cornell_ref_stream", "cornell_ref_sky", "transformed",
+                                  "soup_gradient", "tunnel_kahan"])
+def test_render_bit_exact(solrt, oracle, ctx, name):
+    data, w, h, kw = _case(name)
+    ga, g8, oa, o8, stats, seg_o = _render_both(solrt, oracle, ctx, data, w, h, kw)
+    diff = np.nonzero(np.any(ga.view(np.uint32) != oa.view(np.uint32), axis=-1))
+    assert len(diff[0]) == 0, (len(diff[0]), list(zip(diff[0][:5], diff[1][:5])), ga[diff][:3], oa[diff][:3])
+    assert np.max(np.abs(g8.astype(int) - o8.astype(int))) <= 1
+    assert stats.segments == seg_o
+    assert stats.error_flags == 0
+    assert np.isfinite(ga).all() and ga[..., :3].mean() > 0
+
+
+def test_pass_splitting_invariance(solrt, oracle):
+    """A tiny path capacity forces many passes and pixel chunks; the image
+    must not change."""
+    data, w, h, kw = _case("cornell_lambert")
+    kw = dict(kw, spp=5)
+    out = []
+    for cap in (0, 1000, 4096 + 7):
+        c = solrt.Context(0, path_capacity=cap)
+        ga, _, oa, _, _, _ = _render_both(solrt, oracle, c, data, w, h, kw, frames=1)
+        out.append(ga)
+        c.close()
+    assert np.array_equal(out[0], out[1]) and np.array_equal(out[0], out[2])
+    assert np.array_equal(out[0].view(np.uint32), oa.view(np.uint32))
+
+
+def test_render_rejects_bad_params(solrt, ctx):
+    data = S.cornell()
+    sc = solrt.SceneDescription(ctx, data)
+    img = solrt.Image(ctx, 16, 16)
+    cam = camera_of(data, 1.0)
+    r = solrt.Renderer(ctx)
+    with pytest.raises(solrt.SolrtError):
+        r.cmd_trace_rays(sc, cam, solrt.render_params(32, 16), img)
+    with pytest.raises(solrt.SolrtError):
+        r.cmd_trace_rays(sc, cam, solrt.render_params(16, 16, spp=0), img)
+    with pytest.raises(solrt.SolrtError):
+        r.cmd_trace_rays(sc, cam, solrt.render_params(16, 16, max_bounces=5000), img)
+    with pytest.raises(solrt.SolrtError):
+        r.cmd_trace_rays(sc, cam, solrt.render_params(16, 16, accum_mode=solrt.ACCUM_KAHAN), img)
+
+
+def test_full_size_soup_properties(solrt, ctx):
+    """1M-triangle soup at 1920x1080, 1 spp, depth 4: finite, deterministic
+    across runs and pass splits, one primary segment per path."""
+    data = S.soup(1_000_000, seed=2)
+    sc = solrt.SceneDescription(ctx, data)
+    cam = camera_of(data, 1920 / 1080)
+    p = solrt.render_params(1920, 1080, spp=1, max_bounces=4, material_mode=solrt.MATERIAL_LAMBERT,
+                            rng_mode=solrt.RNG_PER_SAMPLE, seed=2, miss_mode=solrt.MISS_GRADIENT)
+    r = solrt.Renderer(ctx)
+    imgs = []
+    for _ in range(2):
+        img = solrt.Image(ctx, 1920, 1080)
+        ctx.reset_stats()
+        r.cmd_trace_rays(sc, cam, p, img)
+        ctx.synchronize()
+        imgs.append(img.read()[0])
+        st = ctx.stats()
+        assert st.paths == 1920 * 1080
+        assert 1920 * 1080 <= st.segments <= 5 * 1920 * 1080
+    assert np.array_equal(imgs[0], imgs[1])
+    assert np.isfinite(imgs[0]).all()

@@ -1,0 +1,183 @@
+"""CPU checks of the oracle itself: its LBVH against brute force, the
+watertight test on adversarial rays, LBVH invariants and render
+properties (no GPU)."""
+import numpy as np
+import pytest
+
+from helpers import S, axis_rays, edge_rays, empty_scene, hits_equal, random_rays, single_triangle, solrt
+
+
+@pytest.fixture(scope="module")
+def cornell(oracle):
+    return oracle.OracleScene(S.cornell())
+
+
+@pytest.fixture(scope="module")
+def soup(oracle):
+    return oracle.OracleScene(S.soup(30000, seed=2))
+
+
+def test_bvh_matches_brute_force_cornell(cornell):
+    rays = random_rays(20000, 0.02, 0.98, seed=1)
+    a, _ = cornell.trace(rays, brute=True)
+    b, _ = cornell.trace(rays)
+    assert hits_equal(a, b)
+    assert (a["prim"] != solrt.NO_HIT).mean() > 0.7
+
+
+def test_bvh_matches_brute_force_soup_edges(soup):
+    rays = np.concatenate([random_rays(5000, 0.0, 1.0, seed=2), edge_rays(soup.data, 5000, seed=3),
+                           axis_rays(0.0, 1.0, 3000, seed=4)])
+    a, fba = soup.trace(rays, brute=True)
+    b, fbb = soup.trace(rays)
+    assert hits_equal(a, b)
+
+
+def test_watertight_no_leak_on_shared_edges(oracle):
+    """A closed cube (12 triangles, shared edges and vertices): every ray from
+    inside must hit it, including rays through edges and vertices."""
+    d = S.cornell()
+    # close the box: add the front face (z = 0)
+    b = S._Builder()
+    m = b.add_material(S.material())
+    b.add_quads([[(0, 0, 0), (1, 0, 0), (1, 0, 1), (0, 0, 1)], [(0, 1, 0), (0, 1, 1), (1, 1, 1), (1, 1, 0)],
+                 [(0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)], [(0, 0, 0), (0, 0, 1), (0, 1, 1), (0, 1, 0)],
+                 [(1, 0, 0), (1, 1, 0), (1, 1, 1), (1, 0, 1)], [(0, 0, 0), (0, 1, 0), (1, 1, 0), (1, 0, 0)]], m)
+    cube = oracle.OracleScene(b.build())
+    rng = np.random.default_rng(5)
+    n = 4000
+    rays = np.zeros(n, solrt.RAY_DTYPE)
+    rays["origin"] = rng.uniform(0.2, 0.8, (n, 3)).astype(np.float32)
+    corners = np.array([[x, y, z] for x in (0, 1) for y in (0, 1) for z in (0, 1)], np.float32)
+    tgt = corners[rng.integers(0, 8, n)]
+    half = rng.integers(0, 2, n).astype(bool)
+    # half the rays aim at edge midpoints between two corners sharing two coordinates
+    tgt2 = tgt.copy()
+    ax = rng.integers(0, 3, n)
+    tgt2[np.arange(n), ax] = 0.5
+    tgt = np.where(half[:, None], tgt2, tgt)
+    rays["dir"] = (tgt - rays["origin"]).astype(np.float32)
+    rays["tmin"] = 0.0
+    rays["tmax"] = 1e4
+    h, _ = cube.trace(rays, brute=True)
+    assert (h["prim"] != solrt.NO_HIT).all()
+    h2, _ = cube.trace(rays)
+    assert hits_equal(h, h2)
+
+
+def test_lbvh_invariants(soup):
+    child, boxes, order, morton = soup.bvh()
+    n = soup.tri_count
+    assert np.all(np.diff(morton.astype(np.int64)) >= 0)
+    assert np.array_equal(np.sort(order), np.arange(n))
+    leaves = child[child >= 0x80000000] & 0x7FFFFFFF
+    assert np.array_equal(np.sort(leaves), np.arange(n))
+    internal = child[child < 0x80000000]
+    assert np.array_equal(np.sort(internal), np.arange(1, n - 1))
+    # every internal child box lies within its parent box
+    for i in range(0, n - 1, 97):
+        for c in child[i]:
+            if c < 0x80000000:
+                assert np.all(boxes[c, :3] >= boxes[i, :3]) and np.all(boxes[c, 3:] <= boxes[i, 3:])
+
+
+def test_empty_and_single_triangle(oracle):
+    e = oracle.OracleScene(empty_scene())
+    rays = random_rays(100, -1, 1, seed=6)
+    h, _ = e.trace(rays)
+    assert (h["prim"] == solrt.NO_HIT).all() and np.all(h["t"] == rays["tmax"])
+    t = oracle.OracleScene(single_triangle())
+    rays = np.zeros(3, solrt.RAY_DTYPE)
+    rays["origin"] = [[0.2, 0.2, -1], [0.9, 0.9, -1], [0.2, 0.2, 1]]
+    rays["dir"] = [[0, 0, 1], [0, 0, 1], [0, 0, 1]]
+    rays["tmax"] = 1e4
+    h, _ = t.trace(rays)
+    assert h["prim"][0] == 0 and h["t"][0] == 1.0
+    assert abs(h["u"][0] - 0.2) < 1e-6 and abs(h["v"][0] - 0.2) < 1e-6
+    assert h["prim"][1] == solrt.NO_HIT and h["prim"][2] == solrt.NO_HIT
+
+
+def test_tmin_tmax_respected(cornell):
+    rays = random_rays(2000, 0.1, 0.9, seed=7)
+    h, _ = cornell.trace(rays)
+    hit = h["prim"] != solrt.NO_HIT
+    rays2 = rays.copy()
+    rays2["tmax"] = np.where(hit, h["t"] * 0.999, rays["tmax"])
+    h2, _ = cornell.trace(rays2)
+    assert np.all(h2["prim"][hit] != h["prim"][hit]) or np.all(h2["t"][hit] <= rays2["tmax"][hit])
+    rays3 = rays.copy()
+    rays3["tmin"] = np.where(hit, h["t"], 0)
+    h3, _ = cornell.trace(rays3)
+    assert np.all(h3["t"][hit & (h3["prim"] != solrt.NO_HIT)] > h["t"][hit & (h3["prim"] != solrt.NO_HIT)])
+
+
+def test_camera_product_matches_oracle(oracle, solrt):
+    for eye, ctr, up, fov, asp in [((0.5, 0.5, -1.4), (0.5, 0.5, 0.5), (0, -1, 0), 40.0, 1.0),
+                                   ((10, 10, 10), (0, 0, 0), (0, -1, 0), 35.0, 16 / 9),
+                                   ((0, 0, 2), (0, 0, 12), (0, -1, 0), 60.0, 2560 / 1440)]:
+        a = solrt.camera_look_at(eye, ctr, up, fov, asp)
+        b = oracle.camera_look_at(eye, ctr, up, fov, asp)
+        for f in ("view", "view_inverse", "projection", "projection_inverse"):
+            assert list(getattr(a, f)) == list(getattr(b, f))
+    # glam look_at_rh / perspective_rh conventions
+    c = solrt.camera_look_at((0, 0, 5), (0, 0, 0), (0, 1, 0), 90.0, 1.0, 0.1, 100.0)
+    V = np.array(c.view, np.float64).reshape(4, 4).T
+    assert np.allclose(V @ [0, 0, 0, 1], [0, 0, -5, 1])
+    P = np.array(c.projection, np.float64).reshape(4, 4).T
+    assert abs(P[0, 0] - 1.0) < 1e-6 and P[3, 2] == -1.0 and abs(P[2, 2] - 100.0 / (0.1 - 100.0)) < 1e-6
+
+
+def _params(w, h, spp, **kw):
+    base = dict(max_bounces=5, material_mode=solrt.MATERIAL_LAMBERT, rng_mode=solrt.RNG_PER_SAMPLE, seed=1)
+    base.update(kw)
+    return solrt.render_params(w, h, spp=spp, **base)
+
+
+def test_render_progressive_mix_equals_mean(oracle, solrt):
+    """Two launches of 4 spp mixed with alpha 1 and 1/2 equal the mean of
+    the two launches (pathtrace.rgen:89-92)."""
+    d = S.cornell()
+    sc = oracle.OracleScene(d)
+    cam = oracle.camera_look_at(d.camera["eye"], d.camera["center"], d.camera["up"], d.camera["vfov"], 1.0)
+    a0, _, _ = sc.render(cam, _params(32, 32, 4, frame=0))
+    f0 = a0.copy()
+    acc = a0.copy()
+    sc.render(cam, _params(32, 32, 4, frame=1), accum=acc)
+    a1, _, _ = sc.render(cam, _params(32, 32, 4, frame=1, accum_start_frame=1))
+    assert np.allclose(acc[..., :3], 0.5 * (f0[..., :3] + a1[..., :3]), rtol=1e-5, atol=1e-6)
+
+
+def test_render_kahan_equals_mix_mean(oracle, solrt):
+    d = S.cornell()
+    sc = oracle.OracleScene(d)
+    cam = oracle.camera_look_at(d.camera["eye"], d.camera["center"], d.camera["up"], d.camera["vfov"], 1.0)
+    a, _, _ = sc.render(cam, _params(32, 32, 8))
+    k, _, _ = sc.render(cam, _params(32, 32, 8, accum_mode=solrt.ACCUM_KAHAN))
+    assert np.allclose(a, k, rtol=1e-5, atol=1e-6)
+
+
+def test_render_fp32_vs_fp64_close(oracle, solrt):
+    d = S.cornell()
+    sc = oracle.OracleScene(d)
+    cam = oracle.camera_look_at(d.camera["eye"], d.camera["center"], d.camera["up"], d.camera["vfov"], 1.0)
+    a32, _, s32 = sc.render(cam, _params(32, 32, 16))
+    a64, _, s64 = sc.render(cam, _params(32, 32, 16), precision=64)
+    rmse = float(np.sqrt(np.mean((a32[..., :3] - a64[..., :3]) ** 2)))
+    assert rmse < 0.05
+    assert abs(int(s32.segments) - int(s64.segments)) < 0.01 * s32.segments
+
+
+def test_ref_stream_matches_sequential_samples(oracle, solrt):
+    """REF_STREAM: sample s+1 continues the RNG where sample s stopped; the
+    per-sample radiance export and the accumulated image agree."""
+    d = S.cornell()
+    sc = oracle.OracleScene(d)
+    cam = oracle.camera_look_at(d.camera["eye"], d.camera["center"], d.camera["up"], d.camera["vfov"], 1.0)
+    p = _params(16, 16, 4, rng_mode=solrt.RNG_REF_STREAM, material_mode=solrt.MATERIAL_REF)
+    samples = sc.render_samples(cam, p)
+    acc, _, _ = sc.render(cam, p)
+    s = np.zeros((256, 3), np.float32)
+    for k in range(4):
+        s = s + samples[:, k, :3]
+    mean = np.float32(1.0 / 4) * s
+    assert np.array_equal(mean.reshape(16, 16, 3), acc[..., :3])
