@@ -463,13 +463,17 @@ inline void intersect_tri(const RayWT<R>& r, const TriW& tri, uint32_t prim, Hit
 }
 
 // Slab test against a float box, conservative: the far distance is widened
-// by a relative 2^-16 so rounding never culls a box that holds the hit.
+// by a relative 2^-16 so rounding never culls a box that holds the hit. A
+// slab distance is NaN only for 0 * inf (ray parallel to the axis, lying in
+// a box plane): that axis then constrains nothing (NaN near and far, dropped
+// by the NaN-ignoring fmax / fmin across axes).
 template <class R> inline bool box_hit(const Box& b, V3<R> o, V3<R> inv, R tmin, R tmax, R& tnear) {
     R tn = tmin, tf = tmax;
     for (int a = 0; a < 3; ++a) {
         const R t0 = (R(b.lo[a]) - o[a]) * inv[a];
         const R t1 = (R(b.hi[a]) - o[a]) * inv[a];
-        const R lo = std::fmin(t0, t1), hi = std::fmax(t0, t1);
+        const bool nan = std::isnan(t0) || std::isnan(t1);
+        const R lo = nan ? t0 + t1 : std::fmin(t0, t1), hi = nan ? t0 + t1 : std::fmax(t0, t1);
         tn = std::fmax(tn, lo);
         tf = std::fmin(tf, hi);
     }

@@ -103,14 +103,30 @@ SOLRT_D uint32_t intersect_tri(const RayWT& r, float4 q0, float4 q1, float4 q2, 
     return fb;
 }
 
+// NaN-propagating min / max (PTX min.NaN / max.NaN). A slab distance is NaN
+// only for 0 * inf: the ray is parallel to the axis and lies in a box plane.
+// Then both the near and the far distance of that axis become NaN and the
+// NaN-ignoring fminf / fmaxf across axes drop the axis: a ray in the plane of
+// a face is inside that slab for every t.
+SOLRT_D float min_nan(float a, float b) {
+    float r;
+    asm("min.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+SOLRT_D float max_nan(float a, float b) {
+    float r;
+    asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+
 // Slab test of a float box; conservative (see file comment).
 SOLRT_D bool slab(float lox, float hix, float loy, float hiy, float loz, float hiz, float ox, float oy, float oz,
                   float ix, float iy, float iz, float tmin, float tmax, float& tnear) {
     const float x0 = (lox - ox) * ix, x1 = (hix - ox) * ix;
     const float y0 = (loy - oy) * iy, y1 = (hiy - oy) * iy;
     const float z0 = (loz - oz) * iz, z1 = (hiz - oz) * iz;
-    const float tn = fmaxf(fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fminf(z0, z1)), tmin);
-    const float tf = fminf(fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fmaxf(z0, z1)), tmax);
+    const float tn = fmaxf(fmaxf(fmaxf(min_nan(x0, x1), min_nan(y0, y1)), min_nan(z0, z1)), tmin);
+    const float tf = fminf(fminf(fminf(max_nan(x0, x1), max_nan(y0, y1)), max_nan(z0, z1)), tmax);
     tnear = tn;
     return tn <= tf * 1.0000153f;
 }

@@ -33,6 +33,18 @@ def test_bvh_matches_brute_force_soup_edges(soup):
     assert hits_equal(a, b)
 
 
+def test_bvh_matches_brute_force_in_plane_rays(oracle):
+    """Rays with a zero direction component lying exactly in box planes (the
+    tunnel's angle-0 vertices have y = 0): 0 * inf in the slab test must not
+    cull the box."""
+    d = S.tunnel(n_ang=256, n_ax=128, length=25.0)
+    o = oracle.OracleScene(d)
+    rays = np.concatenate([edge_rays(d, 6000, seed=33, eye=(0.0, 0.0, 2.0)), axis_rays(-1.0, 1.0, 4000, seed=34)])
+    a, _ = o.trace(rays, brute=True)
+    b, _ = o.trace(rays)
+    assert hits_equal(a, b)
+
+
 def test_watertight_no_leak_on_shared_edges(oracle):
     """A closed cube (12 triangles, shared edges and vertices): every ray from
     inside must hit it, including rays through edges and vertices."""
