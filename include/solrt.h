@@ -329,6 +329,43 @@ solrt_status solrt_debug_unit(solrt_context* ctx, uint32_t op, uint32_t n, const
                               const uint32_t* b, const float* in_f32, uint32_t* out_u32,
                               float* out_f32);
 
+/* ------------------------------------------------------------------------ */
+/* Allocation-free BVH build (no counterpart in the reference)              */
+/* ------------------------------------------------------------------------ */
+
+/* Largest triangle count solrt_bvh2_build_noalloc accepts. */
+#define SOLRT_NOALLOC_MAX_TRIS 65536u
+
+/* Builds the same BVH2 as solrt_scene_create / solrt_scene_build_bvh, for
+ * callers that must not allocate device memory: a real-time frame loop that
+ * rebuilds a moving mesh's hierarchy every frame cannot afford cudaMalloc /
+ * cudaFree (they may synchronise the whole device and stall the frame), and
+ * a plugin that is handed device buffers by its host application may have
+ * no allocator of its own. The caller passes the inputs and outputs in
+ * device memory; the library's temporary data (sort keys, hierarchy links,
+ * boxes) lives in a fixed scratch array compiled into the library, about
+ * 5.5 MB, which every GPU that loads the library holds until the process
+ * exits.
+ *
+ *   vpos      float4 per vertex (world position in .xyz), 16-byte aligned
+ *   tri_idx   uint4 per triangle (v0, v1, v2, material), 16-byte aligned
+ *   nodes     output, 64 * max(tri_count - 1, 1) bytes (BVH2 node layout of
+ *             solrt_scene_bvh_export)
+ *   tris      output, 48 * tri_count bytes (triangles in leaf order)
+ *   stream    cudaStream_t to run on (NULL = the legacy default stream)
+ *
+ * Work is queued on `stream` and the call returns without waiting. Up to
+ * SOLRT_NOALLOC_MAX_TRIS triangles; more returns SOLRT_ERR_CAPACITY. The
+ * first call on a device looks up the scratch array's device address
+ * (once per device, with that device current), so make that first call
+ * before any stream capture. All calls share the one scratch array: calls
+ * whose work overlaps on the GPU (different streams without ordering)
+ * race and corrupt each other's result; order them on one stream or with
+ * events. The call clears the parts of the scratch that must start at zero,
+ * so leftovers of an earlier call do no harm. */
+solrt_status solrt_bvh2_build_noalloc(const void* vpos, const void* tri_idx, uint32_t tri_count, void* nodes,
+                                      size_t nodes_bytes, void* tris, size_t tris_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

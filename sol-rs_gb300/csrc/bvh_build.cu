@@ -16,6 +16,7 @@
 // every box are a pure function of the input: they equal the CPU LBVH of the
 // oracle bit for bit.
 #include <algorithm>
+#include <mutex>
 
 #include "bvh8.cuh"
 #include "internal.h"
@@ -419,4 +420,131 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
     return SOLRT_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free BVH2 build (solrt_bvh2_build_noalloc): the same kernels as
+// build_bvh, with their temporary arrays carved out of one fixed scratch
+// array that is part of the library image instead of cudaMalloc'ed buffers.
+// ---------------------------------------------------------------------------
+
+namespace {
+
+constexpr uint32_t kNoAllocTris = SOLRT_NOALLOC_MAX_TRIS;
+constexpr uint32_t kNoAllocSortBlocks = (kNoAllocTris + kSortTile - 1) / kSortTile;
+constexpr size_t round256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Byte offsets of the temporary arrays inside the scratch array.
+constexpr size_t kOffCen = 0;                                                      // float4 x n
+constexpr size_t kOffCb = kOffCen + round256(16ull * kNoAllocTris);               // 6 x u32
+constexpr size_t kOffKeys0 = kOffCb + 256;                                         // u32 x n
+constexpr size_t kOffKeys1 = kOffKeys0 + round256(4ull * kNoAllocTris);
+constexpr size_t kOffVals0 = kOffKeys1 + round256(4ull * kNoAllocTris);
+constexpr size_t kOffVals1 = kOffVals0 + round256(4ull * kNoAllocTris);
+constexpr size_t kOffHist = kOffVals1 + round256(4ull * kNoAllocTris);            // u32 x 256 x blocks
+constexpr size_t kOffChild = kOffHist + round256(4ull * 256 * kNoAllocSortBlocks);  // u32 x 2(n-1)
+constexpr size_t kOffParInt = kOffChild + round256(8ull * kNoAllocTris);
+constexpr size_t kOffParLeaf = kOffParInt + round256(4ull * kNoAllocTris);
+constexpr size_t kOffFlags = kOffParLeaf + round256(4ull * kNoAllocTris);
+constexpr size_t kOffNbox = kOffFlags + round256(4ull * kNoAllocTris);             // 2 float4 x (n-1)
+constexpr size_t kNoAllocBytes = kOffNbox + round256(32ull * kNoAllocTris);
+
+}  // namespace
+
+// Scratch of the allocation-free build. Host code must not use this name as a
+// pointer (on the host it is only a stand-in): it takes the device address
+// from cudaGetSymbolAddress, once per device.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+namespace {
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch array on the current device (looked up on
+// the first call for that device).
+solrt_status noalloc_scratch(void** out) {
+    int dev = 0;
+    SOLRT_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) {
+        set_error("device ordinal %d out of range for the allocation-free build", dev);
+        return SOLRT_ERR_DEVICE;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        SOLRT_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return SOLRT_OK;
+}
+
+}  // namespace
+
 }  // namespace solrt
+
+extern "C" solrt_status solrt_bvh2_build_noalloc(const void* vpos, const void* tri_idx, uint32_t tri_count,
+                                                 void* nodes, size_t nodes_bytes, void* tris, size_t tris_bytes,
+                                                 void* stream) {
+    using namespace solrt;
+    if (tri_count > kNoAllocTris) {
+        set_error("solrt_bvh2_build_noalloc: %u triangles exceed the limit of %u", tri_count, kNoAllocTris);
+        return SOLRT_ERR_CAPACITY;
+    }
+    if (tri_count == 0) return SOLRT_OK;
+    const uint32_t n = tri_count;
+    const uint32_t ni = n > 1 ? n - 1 : 1;
+    if (!vpos || !tri_idx || !nodes || !tris) {
+        set_error("solrt_bvh2_build_noalloc: null pointer");
+        return SOLRT_ERR_INVALID;
+    }
+    if (nodes_bytes < 64ull * ni || tris_bytes < 48ull * n) {
+        set_error("solrt_bvh2_build_noalloc: output buffers too small (%zu < %llu or %zu < %llu)", nodes_bytes,
+                  64ull * ni, tris_bytes, 48ull * n);
+        return SOLRT_ERR_INVALID;
+    }
+    if (((uintptr_t)vpos | (uintptr_t)tri_idx | (uintptr_t)nodes | (uintptr_t)tris) & 15u) {
+        set_error("solrt_bvh2_build_noalloc: buffers must be 16-byte aligned");
+        return SOLRT_ERR_INVALID;
+    }
+    void* base = nullptr;
+    SOLRT_TRY(noalloc_scratch(&base));
+    unsigned char* s = static_cast<unsigned char*>(base);
+    float4* cen = reinterpret_cast<float4*>(s + kOffCen);
+    unsigned int* cb = reinterpret_cast<unsigned int*>(s + kOffCb);
+    uint32_t* keys[2] = {reinterpret_cast<uint32_t*>(s + kOffKeys0), reinterpret_cast<uint32_t*>(s + kOffKeys1)};
+    uint32_t* vals[2] = {reinterpret_cast<uint32_t*>(s + kOffVals0), reinterpret_cast<uint32_t*>(s + kOffVals1)};
+    uint32_t* hist = reinterpret_cast<uint32_t*>(s + kOffHist);
+    uint32_t* child = reinterpret_cast<uint32_t*>(s + kOffChild);
+    uint32_t* par_int = reinterpret_cast<uint32_t*>(s + kOffParInt);
+    uint32_t* par_leaf = reinterpret_cast<uint32_t*>(s + kOffParLeaf);
+    unsigned int* flags = reinterpret_cast<unsigned int*>(s + kOffFlags);
+    float4* nbox = reinterpret_cast<float4*>(s + kOffNbox);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+
+    // The scratch keeps the previous call's contents: reset what must start
+    // at a known value (bounds accumulators, arrival flags, parent links).
+    SOLRT_CUDA(cudaMemsetAsync(cb, 0xff, 3 * sizeof(unsigned int), st));
+    SOLRT_CUDA(cudaMemsetAsync(cb + 3, 0, 3 * sizeof(unsigned int), st));
+    SOLRT_CUDA(cudaMemsetAsync(flags, 0, sizeof(unsigned int) * ni, st));
+    SOLRT_CUDA(cudaMemsetAsync(par_int, 0xff, sizeof(uint32_t) * ni, st));
+
+    const float4* vp = static_cast<const float4*>(vpos);
+    const uint4* ti = static_cast<const uint4*>(tri_idx);
+    const uint32_t nblocks = blocks_for(n, kSortTile);
+    k_centroids<<<blocks_for(n, 256), 256, 0, st>>>(vp, ti, n, cen, cb);
+    k_morton<<<blocks_for(n, 256), 256, 0, st>>>(cen, cb, n, keys[0], vals[0]);
+    int cur = 0;
+    for (int shift = 0; shift < 30; shift += 8) {
+        k_radix_hist<<<nblocks, kSortThreads, 0, st>>>(keys[cur], n, shift, nblocks, hist);
+        k_scan_exclusive<<<1, 1024, 0, st>>>(hist, 256 * nblocks);
+        k_radix_scatter<<<nblocks, kSortThreads, 0, st>>>(keys[cur], vals[cur], keys[cur ^ 1], vals[cur ^ 1], hist, n,
+                                                          shift, nblocks);
+        cur ^= 1;
+    }
+    if (n > 1) k_karras<<<blocks_for(n - 1, 256), 256, 0, st>>>(keys[cur], n, child, par_int, par_leaf);
+    k_refit<<<blocks_for(n, 256), 256, 0, st>>>(vp, ti, vals[cur], child, par_int, par_leaf, n, flags, nbox,
+                                                static_cast<float4*>(nodes), static_cast<float4*>(tris));
+    SOLRT_CUDA(cudaGetLastError());
+    return SOLRT_OK;
+}
