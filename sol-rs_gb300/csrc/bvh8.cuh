@@ -22,9 +22,13 @@ struct Bvh8BuildInput {
     uint32_t n;                // triangles
     const uint32_t* child;     // binary LBVH: 2 refs per internal node (leaf = 0x80000000 | pos)
     const float4* nbox;        // binary LBVH internal boxes: lo, hi as 2 float4
+    const uint2* range;        // binary LBVH internal nodes: first, last leaf position
     const float4* tri_wt_leaf; // triangles in LBVH leaf order (3 float4 each)
     uint32_t leaf_max;         // max triangles per leaf child (1..3)
 };
+
+// In-place exclusive scan of `len` u32 counts (bvh_build.cu).
+void launch_scan_exclusive(uint32_t* data, uint32_t len, cudaStream_t stream);
 
 // Writes the 8-wide nodes into `nodes` and the triangles in 8-wide leaf order
 // into `tris`. Synchronises.

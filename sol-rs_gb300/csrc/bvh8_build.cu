@@ -1,12 +1,314 @@
-// bvh8_build.cu — collapse of the binary LBVH into the 8-wide quantised BVH.
+// bvh8_build.cu — collapse of the binary LBVH into the 8-wide BVH with 8-bit
+// quantised child boxes (layout in bvh8.cuh).
+//
+// Level-synchronous and deterministic: each level is a list of tasks (one
+// binary node -> one 8-wide node). Per task, one thread
+//   1. gathers up to 8 children by repeatedly opening the child with the
+//      largest surface area among those holding more than `leaf_max`
+//      triangles (those cannot be leaves);
+//   2. (after an exclusive scan of the internal-child and triangle counts of
+//      all tasks of the level) assigns children to slots so that slot s
+//      holds the child whose centre lies most in direction
+//      ((s&1)?+x:-x, (s&2)?+y:-y, (s&4)?+z:-z) from the node centre, greedily
+//      by lowest cost; a ray of octant o then visits slots in the order of
+//      s ^ o, roughly near to far;
+//   3. quantises the child boxes outward on a power-of-two grid anchored at
+//      the node's minimum corner, with one extra grid step of margin on every
+//      face that is not the anchor plane (see quantise below);
+//   4. writes the node, the next level's tasks and the leaf triangles.
+// Offsets come from scans, not atomics, so the output does not depend on
+// thread scheduling.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
 #include "bvh8.cuh"
 
 namespace solrt {
 
+namespace {
+
+constexpr uint32_t kLeafFlag = 0x80000000u;
+
+struct Box3 {
+    float lo[3], hi[3];
+};
+
+__device__ __forceinline__ Box3 ref_box(uint32_t ref, const float4* __restrict__ nbox,
+                                        const float4* __restrict__ tris) {
+    Box3 b;
+    if (ref & kLeafFlag) {
+        const uint32_t k = ref & ~kLeafFlag;
+        const float4 a = tris[3 * (size_t)k], c = tris[3 * (size_t)k + 1], d = tris[3 * (size_t)k + 2];
+        b.lo[0] = fminf(fminf(a.x, c.x), d.x); b.hi[0] = fmaxf(fmaxf(a.x, c.x), d.x);
+        b.lo[1] = fminf(fminf(a.y, c.y), d.y); b.hi[1] = fmaxf(fmaxf(a.y, c.y), d.y);
+        b.lo[2] = fminf(fminf(a.z, c.z), d.z); b.hi[2] = fmaxf(fmaxf(a.z, c.z), d.z);
+    } else {
+        const float4 l = nbox[2 * (size_t)ref], h = nbox[2 * (size_t)ref + 1];
+        b.lo[0] = l.x; b.lo[1] = l.y; b.lo[2] = l.z;
+        b.hi[0] = h.x; b.hi[1] = h.y; b.hi[2] = h.z;
+    }
+    return b;
+}
+
+__device__ __forceinline__ uint32_t ref_count(uint32_t ref, const uint2* __restrict__ range) {
+    if (ref & kLeafFlag) return 1u;
+    const uint2 r = range[ref];
+    return r.y - r.x + 1u;
+}
+
+__device__ __forceinline__ uint32_t ref_first(uint32_t ref, const uint2* __restrict__ range) {
+    return (ref & kLeafFlag) ? (ref & ~kLeafFlag) : range[ref].x;
+}
+
+__device__ __forceinline__ float half_area(const Box3& b) {
+    const float dx = b.hi[0] - b.lo[0], dy = b.hi[1] - b.lo[1], dz = b.hi[2] - b.lo[2];
+    return dx * dy + dy * dz + dz * dx;
+}
+
+// Pass 1: gather children, count internal children and leaf triangles.
+__global__ void k_gather(const uint32_t* __restrict__ tasks, uint32_t ntasks, const uint32_t* __restrict__ child,
+                         const uint2* __restrict__ range, const float4* __restrict__ nbox,
+                         const float4* __restrict__ tris, uint32_t leaf_max, uint32_t* __restrict__ gathered,
+                         uint32_t* __restrict__ n_inner, uint32_t* __restrict__ n_tris) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t > ntasks) return;
+    if (t == ntasks) {  // trailing zero so the exclusive scans end with the totals
+        n_inner[t] = 0;
+        n_tris[t] = 0;
+        return;
+    }
+    const uint32_t b = tasks[t];
+    uint32_t c[8];
+    int m;
+    if (b & kLeafFlag) {  // single-triangle scene: the root holds one leaf
+        c[0] = b;
+        m = 1;
+    } else {
+        c[0] = child[2 * (size_t)b];
+        c[1] = child[2 * (size_t)b + 1];
+        m = 2;
+        while (m < 8) {
+            int best = -1;
+            float best_a = -1.0f;
+            for (int i = 0; i < m; ++i) {
+                if ((c[i] & kLeafFlag) || ref_count(c[i], range) <= leaf_max) continue;
+                const float a = half_area(ref_box(c[i], nbox, tris));
+                if (a > best_a) { best_a = a; best = i; }
+            }
+            if (best < 0) break;
+            const uint32_t r = c[best];
+            c[best] = child[2 * (size_t)r];
+            c[m++] = child[2 * (size_t)r + 1];
+        }
+    }
+    uint32_t inner = 0, ntri = 0;
+    for (int i = 0; i < 8; ++i) {
+        const uint32_t r = i < m ? c[i] : 0xffffffffu;
+        gathered[8 * (size_t)t + i] = r;
+        if (i < m) {
+            const uint32_t k = ref_count(r, range);
+            if (k > leaf_max) ++inner;
+            else ntri += k;
+        }
+    }
+    n_inner[t] = inner;
+    n_tris[t] = ntri;
+}
+
+// Smallest e with ext / 2^e <= 254, clamped to [-126, 127].
+__device__ __forceinline__ int grid_exponent(double ext) {
+    const double x = ext / 254.0;
+    if (!(x > 0.0)) return -126;
+    int k = 0;
+    const double m = frexp(x, &k);  // x = m * 2^k, m in [0.5, 1)
+    int e = (m == 0.5) ? k - 1 : k;
+    // x was rounded: make sure the grid really spans ext (scaling is exact)
+    while (e < 127 && ext * ldexp(1.0, -e) > 254.0) ++e;
+    return e < -126 ? -126 : (e > 127 ? 127 : e);
+}
+
+// Pass 2: slots, quantisation, node + next tasks + leaf triangles.
+__global__ void k_emit(const uint32_t* __restrict__ tasks, uint32_t ntasks, uint32_t node_base,
+                       uint32_t next_base, uint32_t tri_level_base, const uint32_t* __restrict__ gathered,
+                       const uint32_t* __restrict__ inner_scan, const uint32_t* __restrict__ tri_scan,
+                       const uint2* __restrict__ range, const float4* __restrict__ nbox,
+                       const float4* __restrict__ tris_in, uint32_t leaf_max, uint4* __restrict__ nodes,
+                       uint32_t* __restrict__ next_tasks, float4* __restrict__ tris_out) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntasks) return;
+    const uint32_t b = tasks[t];
+    Box3 cb[8];
+    uint32_t cr[8];
+    int m = 0;
+    for (int i = 0; i < 8; ++i) {
+        const uint32_t r = gathered[8 * (size_t)t + i];
+        if (r == 0xffffffffu) break;
+        cr[m] = r;
+        cb[m] = ref_box(r, nbox, tris_in);
+        ++m;
+    }
+    // node box = union of the children
+    Box3 nb = cb[0];
+    for (int i = 1; i < m; ++i)
+        for (int a = 0; a < 3; ++a) {
+            nb.lo[a] = fminf(nb.lo[a], cb[i].lo[a]);
+            nb.hi[a] = fmaxf(nb.hi[a], cb[i].hi[a]);
+        }
+    // slot assignment
+    int slot_of[8];
+    int child_in_slot[8];
+    for (int i = 0; i < 8; ++i) { slot_of[i] = -1; child_in_slot[i] = -1; }
+    float cost[8][8];
+    for (int i = 0; i < m; ++i) {
+        float off[3];
+        for (int a = 0; a < 3; ++a)
+            off[a] = (cb[i].lo[a] + cb[i].hi[a]) - (nb.lo[a] + nb.hi[a]);
+        for (int s = 0; s < 8; ++s) {
+            const float dx = (s & 1) ? off[0] : -off[0];
+            const float dy = (s & 2) ? off[1] : -off[1];
+            const float dz = (s & 4) ? off[2] : -off[2];
+            cost[i][s] = -((dx + dy) + dz);
+        }
+    }
+    for (int step = 0; step < m; ++step) {
+        int bi = -1, bs = -1;
+        float bc = 0.0f;
+        for (int i = 0; i < m; ++i) {
+            if (slot_of[i] >= 0) continue;
+            for (int s = 0; s < 8; ++s) {
+                if (child_in_slot[s] >= 0) continue;
+                if (bi < 0 || cost[i][s] < bc) { bi = i; bs = s; bc = cost[i][s]; }
+            }
+        }
+        slot_of[bi] = bs;
+        child_in_slot[bs] = bi;
+    }
+    // grid
+    int e[3];
+    float p[3];
+    for (int a = 0; a < 3; ++a) {
+        p[a] = nb.lo[a];
+        e[a] = grid_exponent((double)nb.hi[a] - (double)nb.lo[a]);
+    }
+    uint32_t qlo[3][2] = {{0, 0}, {0, 0}, {0, 0}}, qhi[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+    uint32_t meta[2] = {0, 0};
+    uint32_t imask = 0;
+    const uint32_t child_base = next_base + inner_scan[t];
+    const uint32_t tri_base = tri_level_base + tri_scan[t];
+    uint32_t inner_rank = 0, tri_off = 0;
+    for (int s = 0; s < 8; ++s) {
+        const int i = child_in_slot[s];
+        if (i < 0) continue;
+        for (int a = 0; a < 3; ++a) {
+            const double inv_step = ldexp(1.0, -e[a]);
+            // Outward rounding plus one grid step of margin on every face off
+            // the anchor plane: a decoded face never lies within one step of
+            // the child's triangles unless it is the anchor plane itself
+            // (q = 0), whose distance the traversal computes without
+            // cancellation.
+            const double lr = ((double)cb[i].lo[a] - (double)p[a]) * inv_step;
+            const double hr = ((double)cb[i].hi[a] - (double)p[a]) * inv_step;
+            double ql = floor(lr) - 1.0;
+            double qh = ceil(hr) + 1.0;
+            ql = ql < 0.0 ? 0.0 : ql;
+            qh = qh > 255.0 ? 255.0 : qh;
+            const uint32_t sh = 8u * (uint32_t)(s & 3);
+            qlo[a][s >> 2] |= (uint32_t)ql << sh;
+            qhi[a][s >> 2] |= (uint32_t)qh << sh;
+        }
+        const uint32_t r = cr[i];
+        const uint32_t k = ref_count(r, range);
+        uint32_t mb;
+        if (k > leaf_max) {
+            imask |= 1u << s;
+            mb = (1u << 5) | (24u + (uint32_t)s);
+            next_tasks[inner_scan[t] + inner_rank] = r;
+            ++inner_rank;
+        } else {
+            mb = (((1u << k) - 1u) << 5) | tri_off;
+            const uint32_t first = ref_first(r, range);
+            for (uint32_t j = 0; j < k; ++j) {
+                const size_t src = 3 * (size_t)(first + j), dst = 3 * (size_t)(tri_base + tri_off + j);
+                tris_out[dst] = tris_in[src];
+                tris_out[dst + 1] = tris_in[src + 1];
+                tris_out[dst + 2] = tris_in[src + 2];
+            }
+            tri_off += k;
+        }
+        meta[s >> 2] |= mb << (8u * (uint32_t)(s & 3));
+    }
+    const uint32_t packed = ((uint32_t)(uint8_t)(int8_t)e[0]) | ((uint32_t)(uint8_t)(int8_t)e[1] << 8) |
+                            ((uint32_t)(uint8_t)(int8_t)e[2] << 16) | (imask << 24);
+    uint4* out = nodes + 5 * (size_t)(node_base + t);
+    out[0] = make_uint4(__float_as_uint(p[0]), __float_as_uint(p[1]), __float_as_uint(p[2]), packed);
+    out[1] = make_uint4(child_base, tri_base, meta[0], meta[1]);
+    out[2] = make_uint4(qlo[0][0], qlo[0][1], qlo[1][0], qlo[1][1]);
+    out[3] = make_uint4(qlo[2][0], qlo[2][1], qhi[0][0], qhi[0][1]);
+    out[4] = make_uint4(qhi[1][0], qhi[1][1], qhi[2][0], qhi[2][1]);
+}
+
+inline uint32_t blocks_of(uint64_t n, uint32_t b) { return (uint32_t)((n + b - 1) / b); }
+
+}  // namespace
+
 solrt_status build_bvh8(Context& ctx, const Bvh8BuildInput& in, DeviceBuffer& nodes, DeviceBuffer& tris,
                         uint32_t* node_count, uint32_t* depth) {
-    set_error("BVH8 build not available");
-    return SOLRT_ERR_INVALID;
+    const uint32_t n = in.n;
+    cudaStream_t st = ctx.stream;
+    const uint32_t max_nodes = std::max(1u, n);
+    SOLRT_TRY(nodes.alloc(80ull * max_nodes));
+    SOLRT_TRY(tris.alloc(48ull * n));
+    DeviceBuffer task[2], gathered, inner, ntri;
+    SOLRT_TRY(task[0].alloc(4ull * max_nodes));
+    SOLRT_TRY(task[1].alloc(4ull * max_nodes));
+    SOLRT_TRY(gathered.alloc(32ull * max_nodes));
+    SOLRT_TRY(inner.alloc(4ull * (max_nodes + 1)));
+    SOLRT_TRY(ntri.alloc(4ull * (max_nodes + 1)));
+    const uint32_t root = n > 1 ? 0u : kLeafFlag;  // binary root, or the single leaf
+    SOLRT_CUDA(cudaMemcpyAsync(task[0].ptr, &root, 4, cudaMemcpyHostToDevice, st));
+    uint32_t ntasks = 1, node_base = 0, tri_level_base = 0, levels = 0;
+    int cur = 0;
+    while (ntasks > 0) {
+        if (node_base + ntasks > max_nodes) {
+            set_error("BVH8 collapse overflowed its node bound");
+            return SOLRT_ERR_CAPACITY;
+        }
+        k_gather<<<blocks_of(ntasks + 1, 128), 128, 0, st>>>(task[cur].as<uint32_t>(), ntasks, in.child, in.range,
+                                                             in.nbox, in.tri_wt_leaf, in.leaf_max,
+                                                             gathered.as<uint32_t>(), inner.as<uint32_t>(),
+                                                             ntri.as<uint32_t>());
+        launch_scan_exclusive(inner.as<uint32_t>(), ntasks + 1, st);
+        launch_scan_exclusive(ntri.as<uint32_t>(), ntasks + 1, st);
+        uint32_t totals[2] = {0, 0};
+        SOLRT_CUDA(cudaMemcpyAsync(&totals[0], inner.as<uint32_t>() + ntasks, 4, cudaMemcpyDeviceToHost, st));
+        SOLRT_CUDA(cudaMemcpyAsync(&totals[1], ntri.as<uint32_t>() + ntasks, 4, cudaMemcpyDeviceToHost, st));
+        const uint32_t next_base = node_base + ntasks;
+        k_emit<<<blocks_of(ntasks, 128), 128, 0, st>>>(task[cur].as<uint32_t>(), ntasks, node_base, next_base,
+                                                       tri_level_base, gathered.as<uint32_t>(), inner.as<uint32_t>(),
+                                                       ntri.as<uint32_t>(), in.range, in.nbox, in.tri_wt_leaf,
+                                                       in.leaf_max, nodes.as<uint4>(), task[cur ^ 1].as<uint32_t>(),
+                                                       tris.as<float4>());
+        ctx.launches += 4;
+        SOLRT_CUDA(cudaStreamSynchronize(st));
+        SOLRT_CUDA(cudaGetLastError());
+        ++levels;
+        node_base = next_base;
+        tri_level_base += totals[1];
+        ntasks = totals[0];
+        cur ^= 1;
+        if (levels > 4096) {
+            set_error("BVH8 collapse did not terminate");
+            return SOLRT_ERR_DEVICE;
+        }
+    }
+    if (tri_level_base != n) {
+        set_error("BVH8 collapse placed %u of %u triangles", tri_level_base, n);
+        return SOLRT_ERR_DEVICE;
+    }
+    *node_count = node_base;
+    *depth = levels;
+    return SOLRT_OK;
 }
 
 }  // namespace solrt

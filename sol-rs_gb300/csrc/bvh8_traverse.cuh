@@ -1,9 +1,36 @@
 // bvh8_traverse.cuh — traversal of the 8-wide quantised BVH (bvh8.cuh).
+//
+// Stack of node groups (child base index, pending-child hit bits, internal
+// mask), after the compressed-wide-BVH traversal of Ylitie, Karras and Laine
+// (HPG 2017): a node test produces one 8-bit mask of hit internal children,
+// stored in visiting order (bit s ^ octant for slot s, so slots are visited
+// roughly near to far), and a 24-bit mask of hit leaf triangles, which are
+// tested right away so that the closest distance shrinks early.
+//
+// Child box planes are decoded as p + q * 2^e from 8-bit q. The distance to
+// a plane is fma(q, 2^e / d, (p - o) / d): the build keeps every face other
+// than the anchor plane (q = 0) at least one grid step away from the child's
+// triangles, which bounds the rounding error of that form well inside the
+// margin, and the relative 2^-16 widening of the far distance covers the
+// rest. Zero direction components are replaced by +-2^-64 for these tests
+// only (the triangle test uses the exact direction).
 #pragma once
 
 #include "traverse.cuh"
 
 namespace solrt {
+
+#ifndef SOLRT_BVH8_STACK
+#define SOLRT_BVH8_STACK 32
+#endif
+
+// byte k of `word` as a float, exactly: the byte is placed in the mantissa of
+// 2^23 and 2^23 is subtracted.
+SOLRT_D float byte_as_float(uint32_t word, uint32_t k) {
+    return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7440u | k)) - 8388608.0f;
+}
+
+SOLRT_D float safe_dir(float v) { return fabsf(v) < 0x1p-64f ? copysignf(0x1p-64f, v) : v; }
 
 template <bool kCount>
 SOLRT_D void trace_bvh8(const DevScene& sc, float ox, float oy, float oz, float dx, float dy, float dz, float tmin,
@@ -12,7 +39,90 @@ SOLRT_D void trace_bvh8(const DevScene& sc, float ox, float oy, float oz, float 
     best.prim = SOLRT_NO_HIT;
     best.u = 0.0f;
     best.v = 0.0f;
-    eflags |= SOLRT_EFLAG_INDEX;
+    if (sc.tri_count == 0) return;
+    const RayWT r = setup_ray(ox, oy, oz, dx, dy, dz, tmin);
+    const float bx = safe_dir(dx), by = safe_dir(dy), bz = safe_dir(dz);
+    const float ix = 1.0f / bx, iy = 1.0f / by, iz = 1.0f / bz;
+    const bool negx = signbit(bx), negy = signbit(by), negz = signbit(bz);
+    const uint32_t oct = (negx ? 1u : 0u) | (negy ? 2u : 0u) | (negz ? 4u : 0u);
+    const uint4* nodes = reinterpret_cast<const uint4*>(sc.nodes);
+
+    uint2 stack[SOLRT_BVH8_STACK];
+    int sp = 0;
+    uint2 group = make_uint2(0u, 0u);  // (child base, pending hit bits << 24 | internal mask)
+    uint32_t node = 0;
+    uint32_t budget = 2u * (sc.node_count + sc.tri_count) + 64u;
+    for (;;) {
+        if (--budget == 0u || node >= sc.node_count) {
+            eflags |= SOLRT_EFLAG_INDEX;
+            break;
+        }
+        const uint4* np = nodes + 5 * (size_t)node;
+        const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
+        if (kCount) ++cnt.nodes;
+        const int ex = (int)(int8_t)(w0.w & 0xffu), ey = (int)(int8_t)((w0.w >> 8) & 0xffu),
+                  ez = (int)(int8_t)((w0.w >> 16) & 0xffu);
+        const uint32_t imask = w0.w >> 24;
+        const float sx = __uint_as_float((uint32_t)(ex + 127) << 23) * ix;
+        const float sy = __uint_as_float((uint32_t)(ey + 127) << 23) * iy;
+        const float sz = __uint_as_float((uint32_t)(ez + 127) << 23) * iz;
+        const float ax = (__uint_as_float(w0.x) - ox) * ix;
+        const float ay = (__uint_as_float(w0.y) - oy) * iy;
+        const float az = (__uint_as_float(w0.z) - oz) * iz;
+        // near / far plane bytes per axis: lo is near for a positive direction
+        const uint32_t nx0 = negx ? w3.z : w2.x, nx1 = negx ? w3.w : w2.y;
+        const uint32_t fx0 = negx ? w2.x : w3.z, fx1 = negx ? w2.y : w3.w;
+        const uint32_t ny0 = negy ? w4.x : w2.z, ny1 = negy ? w4.y : w2.w;
+        const uint32_t fy0 = negy ? w2.z : w4.x, fy1 = negy ? w2.w : w4.y;
+        const uint32_t nz0 = negz ? w4.z : w3.x, nz1 = negz ? w4.w : w3.y;
+        const uint32_t fz0 = negz ? w3.x : w4.z, fz1 = negz ? w3.y : w4.w;
+        uint32_t hit_inner = 0, hit_tri = 0;
+#pragma unroll
+        for (int s = 0; s < 8; ++s) {
+            const uint32_t k = (uint32_t)(s & 3);
+            const uint32_t meta = ((s < 4 ? w1.z : w1.w) >> (8u * k)) & 0xffu;
+            const float tnx = fmaf(byte_as_float(s < 4 ? nx0 : nx1, k), sx, ax);
+            const float tny = fmaf(byte_as_float(s < 4 ? ny0 : ny1, k), sy, ay);
+            const float tnz = fmaf(byte_as_float(s < 4 ? nz0 : nz1, k), sz, az);
+            const float tfx = fmaf(byte_as_float(s < 4 ? fx0 : fx1, k), sx, ax);
+            const float tfy = fmaf(byte_as_float(s < 4 ? fy0 : fy1, k), sy, ay);
+            const float tfz = fmaf(byte_as_float(s < 4 ? fz0 : fz1, k), sz, az);
+            const float tn = fmaxf(fmaxf(fmaxf(tnx, tny), tnz), tmin);
+            const float tf = fminf(fminf(fminf(tfx, tfy), tfz), best.t);
+            if (meta != 0u && tn <= tf * 1.0000153f) {
+                if (imask & (1u << s)) hit_inner |= 1u << ((uint32_t)s ^ oct);
+                else hit_tri |= (meta >> 5) << (meta & 31u);
+            }
+        }
+        const uint32_t tri_base = w1.y;
+        while (hit_tri) {
+            const uint32_t k = (uint32_t)(__ffs(hit_tri) - 1);
+            hit_tri &= hit_tri - 1u;
+            const uint32_t ti = tri_base + k;
+            if (ti < sc.tri_count) {
+                const float4* tp = sc.tri_wt + 3 * (size_t)ti;
+                if (kCount) ++cnt.tris;
+                cnt.fallbacks += intersect_tri(r, __ldg(tp), __ldg(tp + 1), __ldg(tp + 2), best);
+            } else {
+                eflags |= SOLRT_EFLAG_INDEX;
+            }
+        }
+        if (hit_inner) {
+            if (group.y >> 24) {
+                if (sp < SOLRT_BVH8_STACK) stack[sp++] = group;
+                else eflags |= SOLRT_EFLAG_STACK;
+            }
+            group = make_uint2(w1.x, (hit_inner << 24) | imask);
+        }
+        if ((group.y >> 24) == 0u) {
+            if (sp == 0) break;
+            group = stack[--sp];
+        }
+        const uint32_t j = (uint32_t)(__ffs(group.y >> 24) - 1);
+        group.y &= ~(1u << (24u + j));
+        const uint32_t s = j ^ oct;
+        node = group.x + (uint32_t)__popc(group.y & ((1u << s) - 1u) & 0xffu);
+    }
 }
 
 }  // namespace solrt

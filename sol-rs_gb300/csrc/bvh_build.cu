@@ -19,6 +19,7 @@
 #include <mutex>
 
 #include "bvh8.cuh"
+#include "bvh8_traverse.cuh"
 #include "internal.h"
 
 namespace solrt {
@@ -199,8 +200,10 @@ __device__ __forceinline__ int kdelta(const uint32_t* __restrict__ k, int64_t n,
 }
 
 // child[2i], child[2i+1]: internal index, or 0x80000000 | leaf position.
+// range[i] (optional): first and last leaf position under internal node i.
 __global__ void k_karras(const uint32_t* __restrict__ keys, uint32_t n, uint32_t* __restrict__ child,
-                         uint32_t* __restrict__ parent_int, uint32_t* __restrict__ parent_leaf) {
+                         uint32_t* __restrict__ parent_int, uint32_t* __restrict__ parent_leaf,
+                         uint2* __restrict__ range) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= (int64_t)n - 1) return;
     const int d = (kdelta(keys, n, i, i + 1) - kdelta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
@@ -226,6 +229,7 @@ __global__ void k_karras(const uint32_t* __restrict__ keys, uint32_t n, uint32_t
     else { right = (uint32_t)(g + 1); parent_int[g + 1] = (uint32_t)i; }
     child[2 * i] = left;
     child[2 * i + 1] = right;
+    if (range) range[i] = make_uint2((uint32_t)lo, (uint32_t)hi);
 }
 
 __device__ __forceinline__ int bvh2_ref(uint32_t r) {
@@ -309,6 +313,10 @@ inline uint32_t blocks_for(uint64_t n, uint32_t b) { return (uint32_t)((n + b - 
 
 }  // namespace
 
+void launch_scan_exclusive(uint32_t* data, uint32_t len, cudaStream_t stream) {
+    k_scan_exclusive<<<1, 1024, 0, stream>>>(data, len);
+}
+
 // Builds the LBVH of `sc` (and the 8-wide collapse when asked). Scratch is
 // allocated for the duration of the build. Synchronises.
 solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
@@ -323,7 +331,7 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
 
     SOLRT_CUDA(cudaEventRecord(ctx.ev0, st));
     const uint32_t ni = n > 1 ? n - 1 : 1;  // internal nodes (one for a single triangle)
-    DeviceBuffer cen, cb, keys[2], vals[2], hist, child, par_int, par_leaf, flags, nbox, depth, bvh2_nodes;
+    DeviceBuffer cen, cb, keys[2], vals[2], hist, child, par_int, par_leaf, flags, nbox, depth, bvh2_nodes, range;
     SOLRT_TRY(cen.alloc(sizeof(float4) * (size_t)n));
     SOLRT_TRY(cb.alloc(6 * sizeof(unsigned int)));
     for (int i = 0; i < 2; ++i) {
@@ -338,6 +346,7 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
     SOLRT_TRY(flags.alloc(sizeof(unsigned int) * (size_t)ni));
     SOLRT_TRY(nbox.alloc(2 * sizeof(float4) * (size_t)ni));
     SOLRT_TRY(depth.alloc(sizeof(unsigned int)));
+    SOLRT_TRY(range.alloc(sizeof(uint2) * (size_t)ni));
     SOLRT_TRY(bvh2_nodes.alloc(4 * sizeof(float4) * (size_t)ni));
     SOLRT_TRY(sc.tri_wt.alloc(3 * sizeof(float4) * (size_t)n));
 
@@ -364,7 +373,8 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
     }
     if (n > 1) {
         k_karras<<<blocks_for(n - 1, 256), 256, 0, st>>>(keys[cur].as<uint32_t>(), n, child.as<uint32_t>(),
-                                                         par_int.as<uint32_t>(), par_leaf.as<uint32_t>());
+                                                         par_int.as<uint32_t>(), par_leaf.as<uint32_t>(),
+                                                         range.as<uint2>());
         ++ctx.launches;
     }
     k_refit<<<blocks_for(n, 256), 256, 0, st>>>(sc.vpos.as<float4>(), sc.tri_idx.as<uint4>(), vals[cur].as<uint32_t>(),
@@ -381,6 +391,7 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
         in.n = n;
         in.child = child.as<uint32_t>();
         in.nbox = nbox.as<float4>();
+        in.range = range.as<uint2>();
         in.tri_wt_leaf = sc.tri_wt.as<float4>();
         in.leaf_max = desc.leaf_max == 0 ? 3u : std::min(3u, desc.leaf_max);
         DeviceBuffer tri8;
@@ -394,6 +405,10 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
         sc.info.node_count = node_count;
         sc.info.depth = depth8;
         sc.info.node_bytes = (uint64_t)node_count * 80u;
+        if (depth8 > SOLRT_BVH8_STACK) {
+            set_error("BVH8 depth %u exceeds the traversal stack (%d)", depth8, SOLRT_BVH8_STACK);
+            return SOLRT_ERR_CAPACITY;
+        }
     } else {
         sc.nodes.ptr = bvh2_nodes.ptr;
         sc.nodes.bytes = bvh2_nodes.bytes;
@@ -542,7 +557,7 @@ extern "C" solrt_status solrt_bvh2_build_noalloc(const void* vpos, const void* t
                                                           shift, nblocks);
         cur ^= 1;
     }
-    if (n > 1) k_karras<<<blocks_for(n - 1, 256), 256, 0, st>>>(keys[cur], n, child, par_int, par_leaf);
+    if (n > 1) k_karras<<<blocks_for(n - 1, 256), 256, 0, st>>>(keys[cur], n, child, par_int, par_leaf, nullptr);
     k_refit<<<blocks_for(n, 256), 256, 0, st>>>(vp, ti, vals[cur], child, par_int, par_leaf, n, flags, nbox,
                                                 static_cast<float4*>(nodes), static_cast<float4*>(tris));
     SOLRT_CUDA(cudaGetLastError());

@@ -55,6 +55,65 @@ def test_bvh2_topology_bit_exact(solrt, oracle, ctx, maker):
     assert info.tri_count == n and info.node_count == n - 1 and info.depth >= np.log2(n)
 
 
+def _decode_bvh8(nodes_u8):
+    w = nodes_u8.view(np.uint32).reshape(-1, 20)
+    p = w[:, 0:3].copy().view(np.float32).astype(np.float64)
+    e = np.stack([((w[:, 3] >> (8 * a)) & 0xFF).astype(np.uint8).view(np.int8) for a in range(3)], 1)
+    imask = w[:, 3] >> 24
+    scale = np.ldexp(1.0, e.astype(np.int64))
+
+    def bytes8(c0, c1):
+        b = np.stack([w[:, c0], w[:, c1]], 1).copy().view(np.uint8)
+        return b.reshape(-1, 8).astype(np.float64)
+
+    qlo = np.stack([bytes8(8, 9), bytes8(10, 11), bytes8(12, 13)], 2)     # node, slot, axis
+    qhi = np.stack([bytes8(14, 15), bytes8(16, 17), bytes8(18, 19)], 2)
+    lo = p[:, None, :] + qlo * scale[:, None, :]
+    hi = p[:, None, :] + qhi * scale[:, None, :]
+    meta = np.stack([w[:, 6], w[:, 7]], 1).copy().view(np.uint8).reshape(-1, 8)
+    return dict(child_base=w[:, 4], tri_base=w[:, 5], imask=imask, meta=meta, lo=lo, hi=hi)
+
+
+@pytest.mark.parametrize("maker", [lambda: S.cornell(), lambda: S.soup(40000, seed=3),
+                                   lambda: S.tunnel(n_ang=128, n_ax=64, length=20.0), lambda: single_triangle()])
+def test_bvh8_conservative_and_complete(solrt, ctx, maker):
+    """Every triangle is referenced by exactly one leaf slot and lies inside
+    the decoded (quantised) box of that slot and of every ancestor slot."""
+    d = maker()
+    sc = solrt.SceneDescription(ctx, d, bvh=solrt.BVH8_Q8)
+    nodes, tris = sc.bvh_export()
+    info = sc.bvh_info()
+    n = info.tri_count
+    dec = _decode_bvh8(nodes)
+    tv = tris.view(np.float32).reshape(-1, 3, 4)[:, :, :3].astype(np.float64)
+    prim = tris.view(np.uint32).reshape(-1, 12)[:, 3]
+    assert np.array_equal(np.sort(prim), np.arange(n))
+    seen = np.zeros(n, np.int64)
+    stack = [(0, np.full(3, -np.inf), np.full(3, np.inf))]
+    visited = 0
+    while stack:
+        node, alo, ahi = stack.pop()
+        visited += 1
+        for s in range(8):
+            m = int(dec["meta"][node, s])
+            if m == 0:
+                continue
+            blo = np.maximum(alo, dec["lo"][node, s])
+            bhi = np.minimum(ahi, dec["hi"][node, s])
+            if (int(dec["imask"][node]) >> s) & 1:
+                rank = bin(int(dec["imask"][node]) & ((1 << s) - 1)).count("1")
+                stack.append((int(dec["child_base"][node]) + rank, blo, bhi))
+            else:
+                k = bin(m >> 5).count("1")
+                off = m & 31
+                t0 = int(dec["tri_base"][node]) + off
+                v = tv[t0:t0 + k]
+                assert np.all(v >= blo - 0.0) and np.all(v <= bhi + 0.0), (node, s)
+                seen[t0:t0 + k] += 1
+    assert visited == info.node_count
+    assert np.all(seen == 1)
+
+
 def test_single_triangle_bvh(solrt, ctx):
     sc = solrt.SceneDescription(ctx, single_triangle())
     info = sc.bvh_info()

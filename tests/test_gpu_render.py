@@ -78,11 +78,13 @@ def _render_both(solrt, oracle, ctx, data, w, h, kw, frames=2, bvh=None):
     return ga, g8, acc, rgba_o, stats, seg_o
 
 
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh8"])
 @pytest.mark.parametrize("name", ["cornell_lambert", "cornell_ref_stream", "cornell_ref_sky", "transformed",
                                   "soup_gradient", "tunnel_kahan"])
-def test_render_bit_exact(solrt, oracle, ctx, name):
+def test_render_bit_exact(solrt, oracle, ctx, name, bvh):
     data, w, h, kw = _case(name)
-    ga, g8, oa, o8, stats, seg_o = _render_both(solrt, oracle, ctx, data, w, h, kw)
+    kind = solrt.BVH2 if bvh == "bvh2" else solrt.BVH8_Q8
+    ga, g8, oa, o8, stats, seg_o = _render_both(solrt, oracle, ctx, data, w, h, kw, bvh=kind)
     diff = np.nonzero(np.any(ga.view(np.uint32) != oa.view(np.uint32), axis=-1))
     assert len(diff[0]) == 0, (len(diff[0]), list(zip(diff[0][:5], diff[1][:5])), ga[diff][:3], oa[diff][:3])
     assert np.max(np.abs(g8.astype(int) - o8.astype(int))) <= 1

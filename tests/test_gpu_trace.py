@@ -18,7 +18,7 @@ def _both(solrt, oracle, ctx, data, rays, bvh):
     return g, ref
 
 
-BVHS = ["bvh2"]
+BVHS = ["bvh2", "bvh8"]
 
 
 def _kind(solrt, name):
