@@ -198,6 +198,7 @@ solrt_status solrt_context_create(const solrt_context_desc* desc, solrt_context*
     if ((s = c->rad.alloc(16 * C)) != SOLRT_OK) return fail(s);
     if ((s = c->ctl.alloc(sizeof(PassCtl))) != SOLRT_OK) return fail(s);
     if ((s = c->stats.alloc(sizeof(DevStats))) != SOLRT_OK) return fail(s);
+    if ((s = c->trace_work.alloc(sizeof(unsigned int))) != SOLRT_OK) return fail(s);
     if (cudaMemset(c->ctl.ptr, 0, sizeof(PassCtl)) != cudaSuccess ||
         cudaMemset(c->stats.ptr, 0, sizeof(DevStats)) != cudaSuccess ||
         cudaDeviceSynchronize() != cudaSuccess) {

@@ -1,0 +1,140 @@
+// bvh2_ww.cuh — BVH2 traversal organised for SIMT efficiency.
+//
+// A warp keeps 32 rays in flight. Every step of its loop is warp-uniform
+// (full-warp votes decide the phases), so lanes re-converge at each step:
+//   refill  lanes whose ray has finished take new rays from the global queue
+//           (one atomic per warp), once at least kRefill lanes are free;
+//   nodes   lanes visit inner nodes until every lane has parked a leaf or has
+//           no inner node left; a lane that already parked a leaf keeps
+//           descending until it reaches a second one ("while-while" with
+//           speculative traversal, after Aila & Laine, HPG 2009);
+//   leaves  lanes test their parked leaves together.
+// The closest hit does not depend on visiting order, so results equal those
+// of a plain per-ray loop.
+#pragma once
+
+#include "traverse.cuh"
+
+namespace solrt {
+
+constexpr int kBvh2Sentinel = 0x7fffffff;
+#ifndef SOLRT_BVH2_REFILL
+#define SOLRT_BVH2_REFILL 8
+#endif
+
+template <class IO, bool kCount>
+SOLRT_D void extend_bvh2_ww(const DevScene& sc, const IO& io, uint32_t n, unsigned int* work, TraceCounters& cnt,
+                            uint32_t& ef) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t lane_lt = (1u << lane) - 1u;
+    int stack[SOLRT_BVH2_STACK + 1];
+    int sp = 0;
+    int node = kBvh2Sentinel;  // >= 0 inner node, < 0 leaf ~k, sentinel = nothing left
+    int leaf = 0;              // parked leaf (< 0) or none (>= 0)
+    bool has = false;
+    bool drained = false;      // the queue has no more rays for this warp
+    uint32_t idx = 0, budget = 0;
+    RayWT r;
+    float ix = 0.0f, iy = 0.0f, iz = 0.0f;     // 1 / box_dir(d)
+    float nox = 0.0f, noy = 0.0f, noz = 0.0f;  // -o / box_dir(d)
+    HitRec best{0.0f, SOLRT_NO_HIT, 0.0f, 0.0f};
+    const uint32_t max_steps = 2u * (sc.node_count + sc.tri_count) + 64u;
+    for (;;) {
+        const bool idle = node == kBvh2Sentinel && leaf >= 0;
+        if (idle && has) {
+            io.store(idx, best);
+            has = false;
+        }
+        const uint32_t need = __ballot_sync(0xffffffffu, idle);
+        if (!drained && __popc(need) >= SOLRT_BVH2_REFILL) {
+            const int leader = __ffs(need) - 1;
+            uint32_t base = 0;
+            if (lane == leader) base = atomicAdd(work, (unsigned int)__popc(need));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (base + (uint32_t)__popc(need) >= n) drained = true;
+            if (idle) {
+                const uint32_t i = base + (uint32_t)__popc(need & lane_lt);
+                if (i < n) {
+                    float4 o, d;
+                    io.load(i, o, d);
+                    idx = i;
+                    has = true;
+                    r = setup_ray(o.x, o.y, o.z, d.x, d.y, d.z, o.w);
+                    ix = 1.0f / box_dir(d.x);
+                    iy = 1.0f / box_dir(d.y);
+                    iz = 1.0f / box_dir(d.z);
+                    nox = -(o.x * ix);
+                    noy = -(o.y * iy);
+                    noz = -(o.z * iz);
+                    best = HitRec{d.w, SOLRT_NO_HIT, 0.0f, 0.0f};
+                    budget = max_steps;
+                    stack[0] = kBvh2Sentinel;
+                    sp = 1;
+                    node = sc.tri_count ? 0 : kBvh2Sentinel;
+                    leaf = 0;
+                }
+            }
+        }
+        if (!__any_sync(0xffffffffu, has)) {
+            if (drained) break;
+            continue;  // fewer than kRefill free lanes but none busy: refill next round
+        }
+        // node phase
+        for (;;) {
+            const bool inner = (unsigned)node < (unsigned)kBvh2Sentinel;
+            if (!__any_sync(0xffffffffu, inner && leaf >= 0)) break;
+            if (inner) {
+                if (--budget == 0u || (uint32_t)node >= sc.node_count) {
+                    ef |= SOLRT_EFLAG_INDEX;
+                    node = kBvh2Sentinel;
+                    leaf = 0;
+                } else {
+                    const float4* np = sc.nodes + 4 * (size_t)node;
+                    const float4 n0 = __ldg(np + 0), n1 = __ldg(np + 1), n2 = __ldg(np + 2);
+                    const int4 n3 = __ldg(reinterpret_cast<const int4*>(np + 3));
+                    if (kCount) ++cnt.nodes;
+                    float t0, t1;
+                    const bool h0 = slab_fma(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, ix, iy, iz, nox, noy, noz, r.tmin,
+                                             best.t, t0);
+                    const bool h1 = slab_fma(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, ix, iy, iz, nox, noy, noz, r.tmin,
+                                             best.t, t1);
+                    if (h0 && h1) {
+                        const bool swap = t1 < t0;
+                        if (sp <= SOLRT_BVH2_STACK) stack[sp++] = swap ? n3.x : n3.y;
+                        else ef |= SOLRT_EFLAG_STACK;
+                        node = swap ? n3.y : n3.x;
+                    } else if (h0) {
+                        node = n3.x;
+                    } else if (h1) {
+                        node = n3.y;
+                    } else {
+                        node = stack[--sp];
+                    }
+                    if (node < 0 && leaf >= 0) {  // park the leaf, keep descending
+                        leaf = node;
+                        node = stack[--sp];
+                    }
+                }
+            }
+        }
+        // leaf phase
+        while (__any_sync(0xffffffffu, leaf < 0)) {
+            if (leaf < 0) {
+                const uint32_t k = (uint32_t)(~leaf);
+                if (--budget == 0u || k >= sc.tri_count) {
+                    ef |= SOLRT_EFLAG_INDEX;
+                    node = kBvh2Sentinel;
+                    leaf = 0;
+                } else {
+                    const float4* tp = sc.tri_wt + 3 * (size_t)k;
+                    if (kCount) ++cnt.tris;
+                    cnt.fallbacks += intersect_tri(r, __ldg(tp), __ldg(tp + 1), __ldg(tp + 2), best);
+                    leaf = node;
+                    if (node < 0) node = stack[--sp];
+                }
+            }
+        }
+    }
+}
+
+}  // namespace solrt

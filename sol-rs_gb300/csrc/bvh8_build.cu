@@ -12,9 +12,9 @@
 //      ((s&1)?+x:-x, (s&2)?+y:-y, (s&4)?+z:-z) from the node centre, greedily
 //      by lowest cost; a ray of octant o then visits slots in the order of
 //      s ^ o, roughly near to far;
-//   3. quantises the child boxes outward on a power-of-two grid anchored at
-//      the node's minimum corner, with one extra grid step of margin on every
-//      face that is not the anchor plane (see quantise below);
+//   3. quantises the child boxes outward on a power-of-two grid anchored
+//      just below the node's minimum corner (widen_lo), with one extra grid
+//      step of margin on every face that is not the anchor plane;
 //   4. writes the node, the next level's tasks and the leaf triangles.
 // Offsets come from scans, not atomics, so the output does not depend on
 // thread scheduling.
@@ -188,8 +188,8 @@ __global__ void k_emit(const uint32_t* __restrict__ tasks, uint32_t ntasks, uint
     int e[3];
     float p[3];
     for (int a = 0; a < 3; ++a) {
-        p[a] = nb.lo[a];
-        e[a] = grid_exponent((double)nb.hi[a] - (double)nb.lo[a]);
+        p[a] = widen_lo(nb.lo[a]);  // anchor just below the box (see widen_lo)
+        e[a] = grid_exponent((double)nb.hi[a] - (double)p[a]);
     }
     uint32_t qlo[3][2] = {{0, 0}, {0, 0}, {0, 0}}, qhi[3][2] = {{0, 0}, {0, 0}, {0, 0}};
     uint32_t meta[2] = {0, 0};

@@ -12,8 +12,9 @@
 // than the anchor plane (q = 0) at least one grid step away from the child's
 // triangles, which bounds the rounding error of that form well inside the
 // margin, and the relative 2^-16 widening of the far distance covers the
-// rest. Zero direction components are replaced by +-2^-64 for these tests
-// only (the triangle test uses the exact direction).
+// rest. The anchor plane itself sits below the node's box by widen_lo. Zero
+// direction components are replaced by box_dir for these tests only (the
+// triangle test uses the exact direction).
 #pragma once
 
 #include "traverse.cuh"
@@ -30,8 +31,6 @@ SOLRT_D float byte_as_float(uint32_t word, uint32_t k) {
     return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7440u | k)) - 8388608.0f;
 }
 
-SOLRT_D float safe_dir(float v) { return fabsf(v) < 0x1p-64f ? copysignf(0x1p-64f, v) : v; }
-
 template <bool kCount>
 SOLRT_D void trace_bvh8(const DevScene& sc, float ox, float oy, float oz, float dx, float dy, float dz, float tmin,
                         float tmax, HitRec& best, TraceCounters& cnt, uint32_t& eflags) {
@@ -41,7 +40,7 @@ SOLRT_D void trace_bvh8(const DevScene& sc, float ox, float oy, float oz, float 
     best.v = 0.0f;
     if (sc.tri_count == 0) return;
     const RayWT r = setup_ray(ox, oy, oz, dx, dy, dz, tmin);
-    const float bx = safe_dir(dx), by = safe_dir(dy), bz = safe_dir(dz);
+    const float bx = box_dir(dx), by = box_dir(dy), bz = box_dir(dz);
     const float ix = 1.0f / bx, iy = 1.0f / by, iz = 1.0f / bz;
     const bool negx = signbit(bx), negy = signbit(by), negz = signbit(bz);
     const uint32_t oct = (negx ? 1u : 0u) | (negy ? 2u : 0u) | (negz ? 4u : 0u);

@@ -238,8 +238,9 @@ __device__ __forceinline__ int bvh2_ref(uint32_t r) {
 
 // Leaf boxes + refit. Each thread starts at a leaf; the second thread to
 // arrive at a node computes its box from both children and continues upward.
-// Boxes of internal nodes go to `nbox` (lo.xyz, hi.xyz as 2 float4) and into
-// the child slots of the parent's BVH2 node.
+// Exact boxes of internal nodes go to `nbox` (lo.xyz, hi.xyz as 2 float4);
+// the child slots of each BVH2 node end up holding the children's boxes
+// widened by widen_lo / widen_hi (traverse.cuh).
 __global__ void k_refit(const float4* __restrict__ vpos, const uint4* __restrict__ tri_idx,
                         const uint32_t* __restrict__ order, const uint32_t* __restrict__ child,
                         const uint32_t* __restrict__ parent_int, const uint32_t* __restrict__ parent_leaf,
@@ -257,9 +258,11 @@ __global__ void k_refit(const float4* __restrict__ vpos, const uint4* __restrict
     float hi[3] = {fmaxf(fmaxf(a.x, b.x), c.x), fmaxf(fmaxf(a.y, b.y), c.y), fmaxf(fmaxf(a.z, b.z), c.z)};
     if (n == 1) {
         // single triangle: one node whose two children are the same leaf.
-        nodes[0] = make_float4(lo[0], hi[0], lo[1], hi[1]);
-        nodes[1] = make_float4(lo[0], hi[0], lo[1], hi[1]);
-        nodes[2] = make_float4(lo[2], hi[2], lo[2], hi[2]);
+        const float wl[3] = {widen_lo(lo[0]), widen_lo(lo[1]), widen_lo(lo[2])};
+        const float wh[3] = {widen_hi(hi[0]), widen_hi(hi[1]), widen_hi(hi[2])};
+        nodes[0] = make_float4(wl[0], wh[0], wl[1], wh[1]);
+        nodes[1] = make_float4(wl[0], wh[0], wl[1], wh[1]);
+        nodes[2] = make_float4(wl[2], wh[2], wl[2], wh[2]);
         nodes[3] = make_float4(__int_as_float(~0), __int_as_float(~0), 0.0f, 0.0f);
         nbox[0] = make_float4(lo[0], lo[1], lo[2], 0.0f);
         nbox[1] = make_float4(hi[0], hi[1], hi[2], 0.0f);
@@ -285,6 +288,11 @@ __global__ void k_refit(const float4* __restrict__ vpos, const uint4* __restrict
         lo[0] = fminf(s0.x, s1.x); hi[0] = fmaxf(s0.y, s1.y);
         lo[1] = fminf(s0.z, s1.z); hi[1] = fmaxf(s0.w, s1.w);
         lo[2] = fminf(s2.x, s2.z); hi[2] = fmaxf(s2.y, s2.w);
+        // the union above used the exact child boxes; the traversal reads
+        // them widened (see slab_fma)
+        np[0] = make_float4(widen_lo(s0.x), widen_hi(s0.y), widen_lo(s0.z), widen_hi(s0.w));
+        np[1] = make_float4(widen_lo(s1.x), widen_hi(s1.y), widen_lo(s1.z), widen_hi(s1.w));
+        np[2] = make_float4(widen_lo(s2.x), widen_hi(s2.y), widen_lo(s2.z), widen_hi(s2.w));
         np[3] = make_float4(__int_as_float(bvh2_ref(child[2 * p])), __int_as_float(bvh2_ref(child[2 * p + 1])),
                             0.0f, 0.0f);
         nbox[2 * (size_t)p + 0] = make_float4(lo[0], lo[1], lo[2], 0.0f);

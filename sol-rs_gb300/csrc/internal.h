@@ -95,7 +95,7 @@ struct Context {
     bool counters = false;
     uint32_t block_size = 0;
     DeviceBuffer q_o[2], q_d[2], q_thr[2], q_meta[2];
-    DeviceBuffer hits, rad, ctl, stats;
+    DeviceBuffer hits, rad, ctl, stats, trace_work;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     uint64_t launches = 0;
     double last_render_ms = 0.0;

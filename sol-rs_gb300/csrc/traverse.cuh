@@ -7,9 +7,9 @@
 // is exactly zero (the products of two floats are exact in FP64, so the sign
 // of each edge function is then exact). Closest hit = smaller t, ties go to
 // the lower global triangle index, so the answer does not depend on the BVH
-// or on traversal order. Box tests are conservative (NaN-ignoring min/max and
-// a relative 2^-16 widening of the far distance) so that rounding never culls
-// a box that holds the closest hit.
+// or on traversal order. Box tests are conservative (see slab_fma and the
+// 8-wide test in bvh8_traverse.cuh) so that rounding never culls a box that
+// holds the closest hit.
 #pragma once
 
 #include "device_math.cuh"
@@ -103,33 +103,44 @@ SOLRT_D uint32_t intersect_tri(const RayWT& r, float4 q0, float4 q1, float4 q2, 
     return fb;
 }
 
-// NaN-propagating min / max (PTX min.NaN / max.NaN). A slab distance is NaN
-// only for 0 * inf: the ray is parallel to the axis and lies in a box plane.
-// Then both the near and the far distance of that axis become NaN and the
-// NaN-ignoring fminf / fmaxf across axes drop the axis: a ray in the plane of
-// a face is inside that slab for every t.
-SOLRT_D float min_nan(float a, float b) {
+// Three-input min / max (PTX ISA min.f32 / max.f32 with three sources).
+SOLRT_D float max3(float a, float b, float c) {
     float r;
-    asm("min.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
     return r;
 }
-SOLRT_D float max_nan(float a, float b) {
+SOLRT_D float min3(float a, float b, float c) {
     float r;
-    asm("max.NaN.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
     return r;
 }
 
-// Slab test of a float box; conservative (see file comment).
-SOLRT_D bool slab(float lox, float hix, float loy, float hiy, float loz, float hiz, float ox, float oy, float oz,
-                  float ix, float iy, float iz, float tmin, float tmax, float& tnear) {
-    const float x0 = (lox - ox) * ix, x1 = (hix - ox) * ix;
-    const float y0 = (loy - oy) * iy, y1 = (hiy - oy) * iy;
-    const float z0 = (loz - oz) * iz, z1 = (hiz - oz) * iz;
-    const float tn = fmaxf(fmaxf(fmaxf(min_nan(x0, x1), min_nan(y0, y1)), min_nan(z0, z1)), tmin);
-    const float tf = fminf(fminf(fminf(max_nan(x0, x1), max_nan(y0, y1)), max_nan(z0, z1)), tmax);
+// Direction component for box tests: components below 2^-100 (exact zeros
+// included) become +-2^-100 (sign kept) so that 1/d and o/d stay finite for
+// |o| < 2^27. Over t < 2^20 the tilt this gives a ray lying in a box plane is
+// below 2^-80, the absolute part of the face widening, so such a ray stays
+// inside the slab.
+SOLRT_D float box_dir(float v) { return fabsf(v) < 0x1p-100f ? copysignf(0x1p-100f, v) : v; }
+
+// Slab test in the form t = fma(plane, 1/d, -o/d) (one instruction per
+// plane). Its rounding error relative to |o/d| is covered by the widening of
+// every BVH2 child box by a relative 2^-21 at build time (widen_lo /
+// widen_hi) plus the relative 2^-16 widening of the far distance.
+SOLRT_D bool slab_fma(float lox, float hix, float loy, float hiy, float loz, float hiz, float ix, float iy,
+                      float iz, float nox, float noy, float noz, float tmin, float tmax, float& tnear) {
+    const float x0 = fmaf(lox, ix, nox), x1 = fmaf(hix, ix, nox);
+    const float y0 = fmaf(loy, iy, noy), y1 = fmaf(hiy, iy, noy);
+    const float z0 = fmaf(loz, iz, noz), z1 = fmaf(hiz, iz, noz);
+    const float tn = fmaxf(max3(fminf(x0, x1), fminf(y0, y1), fminf(z0, z1)), tmin);
+    const float tf = fminf(min3(fmaxf(x0, x1), fmaxf(y0, y1), fmaxf(z0, z1)), tmax);
     tnear = tn;
     return tn <= tf * 1.0000153f;
 }
+
+// Outward widening of a box face by a relative 2^-21 (about 4 ulp) plus an
+// absolute 2^-80 (which matters only near 0).
+SOLRT_HD float widen_lo(float v) { return (v - fabsf(v) * 0x1p-21f) - 0x1p-80f; }
+SOLRT_HD float widen_hi(float v) { return (v + fabsf(v) * 0x1p-21f) + 0x1p-80f; }
 
 struct TraceCounters {
     uint32_t nodes;
@@ -146,63 +157,5 @@ struct TraceCounters {
 #ifndef SOLRT_BVH2_STACK
 #define SOLRT_BVH2_STACK 64
 #endif
-
-template <bool kCount>
-SOLRT_D void trace_bvh2(const DevScene& sc, float ox, float oy, float oz, float dx, float dy, float dz, float tmin,
-                        float tmax, HitRec& best, TraceCounters& cnt, uint32_t& eflags) {
-    best.t = tmax;
-    best.prim = SOLRT_NO_HIT;
-    best.u = 0.0f;
-    best.v = 0.0f;
-    if (sc.tri_count == 0) return;
-    const RayWT r = setup_ray(ox, oy, oz, dx, dy, dz, tmin);
-    const float ix = 1.0f / dx, iy = 1.0f / dy, iz = 1.0f / dz;
-    int stack[SOLRT_BVH2_STACK];
-    int sp = 0;
-    int node = 0;
-    // A valid BVH2 visits each node and leaf at most once; a longer walk
-    // means a malformed hierarchy: flag it and stop instead of looping.
-    uint32_t budget = 2u * (sc.node_count + sc.tri_count) + 64u;
-    for (;;) {
-        if (--budget == 0u) {
-            eflags |= SOLRT_EFLAG_INDEX;
-            break;
-        }
-        if (node >= 0) {
-            if ((uint32_t)node >= sc.node_count) {
-                eflags |= SOLRT_EFLAG_INDEX;
-                break;
-            }
-            const float4* np = sc.nodes + 4 * (size_t)node;
-            const float4 n0 = __ldg(np + 0), n1 = __ldg(np + 1), n2 = __ldg(np + 2);
-            const int4 n3 = __ldg(reinterpret_cast<const int4*>(np + 3));
-            if (kCount) ++cnt.nodes;
-            float t0, t1;
-            const bool h0 = slab(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, ox, oy, oz, ix, iy, iz, tmin, best.t, t0);
-            const bool h1 = slab(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, ox, oy, oz, ix, iy, iz, tmin, best.t, t1);
-            if (h0 && h1) {
-                int nearc = n3.x, farc = n3.y;
-                if (t1 < t0) { nearc = n3.y; farc = n3.x; }
-                if (sp < SOLRT_BVH2_STACK) stack[sp++] = farc;
-                else eflags |= SOLRT_EFLAG_STACK;
-                node = nearc;
-                continue;
-            }
-            if (h0) { node = n3.x; continue; }
-            if (h1) { node = n3.y; continue; }
-        } else {
-            const uint32_t k = (uint32_t)(~node);
-            if (k < sc.tri_count) {
-                const float4* tp = sc.tri_wt + 3 * (size_t)k;
-                if (kCount) ++cnt.tris;
-                cnt.fallbacks += intersect_tri(r, __ldg(tp), __ldg(tp + 1), __ldg(tp + 2), best);
-            } else {
-                eflags |= SOLRT_EFLAG_INDEX;
-            }
-        }
-        if (sp == 0) break;
-        node = stack[--sp];
-    }
-}
 
 }  // namespace solrt

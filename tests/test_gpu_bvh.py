@@ -47,6 +47,11 @@ def test_bvh2_topology_bit_exact(solrt, oracle, ctx, maker):
         lp = order[~r[~internal]]
         want[~internal, :3] = tri_lo[lp]
         want[~internal, 3:] = tri_hi[lp]
+        # node slots hold the exact boxes widened outward by a relative 2^-21
+        # plus an absolute 2^-80
+        step, tiny = np.float32(2.0 ** -21), np.float32(2.0 ** -80)
+        want[:, :3] = (want[:, :3] - np.abs(want[:, :3]) * step) - tiny
+        want[:, 3:] = (want[:, 3:] + np.abs(want[:, 3:]) * step) + tiny
         assert np.array_equal(cb, want)
     # triangle stream in leaf order carries the original triangle index
     prim = tris.view(np.uint32).reshape(-1, 12)[:, 3]
