@@ -201,6 +201,106 @@ def cpu_baseline(data, kw, cam, budget_s=12.0, threads=0):
             "segments": int(total_seg), "seconds": round(total_t, 3)}
 
 
+def run_batch(args, world, rank, local, pg):
+    """Batched mixed scenes (256 randomised Cornell boxes with log-uniform
+    1k-500k-triangle soups, 128^2..1024^2, 4-64 spp, depth 5): one CUDA-graph
+    replay per step vs the same jobs rendered one solrt_render at a time."""
+    import torch
+    solrt = importlib.import_module("sol-rs_gb300")
+    S = solrt.scenes
+    bvh = solrt.BVH8_Q8 if args.bvh == "bvh8" else solrt.BVH2
+    ctx = solrt.Context(local)
+    jobs, tris, pixels, samples = [], 0, 0, 0
+    t0 = time.perf_counter()
+    for i in range(args.jobs):
+        data, jp = S.mixed_scene(i)
+        sc = solrt.SceneDescription(ctx, data, bvh=bvh, keep_data=False)
+        tris += data.tri_count
+        del data
+        w, h = jp["width"], jp["height"]
+        img = solrt.Image(ctx, w, h)
+        c = S.CORNELL_CAMERA
+        cam = solrt.camera_look_at(c["eye"], c["center"], c["up"], c["vfov"], 1.0)
+        p = solrt.render_params(w, h, spp=jp["spp"], max_bounces=jp["max_bounces"], seed=jp["seed"], job_id=i,
+                                material_mode=solrt.MATERIAL_LAMBERT, rng_mode=solrt.RNG_PER_SAMPLE,
+                                miss_mode=solrt.MISS_BLACK)
+        jobs.append((sc, img, cam, p))
+        pixels += w * h
+        samples += w * h * jp["spp"]
+    setup_s = time.perf_counter() - t0
+    batch = solrt.Batch(ctx, jobs, graph=True)
+    info = batch.info()
+    ext = torch.cuda.ExternalStream(ctx.stream())
+
+    def timed(fn, steps):
+        ctx.synchronize()
+        ctx.reset_stats()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        for _ in range(steps):
+            fn()
+        e1.record(ext)
+        ctx.synchronize()
+        torch.cuda.synchronize()
+        st = ctx.stats()
+        return e0.elapsed_time(e1), st.segments, st.launches
+
+    r = solrt.Renderer(ctx)
+    mega_params = []
+    for sc, img, cam, p in jobs:
+        q = solrt.RenderParams.from_buffer_copy(p)
+        q.kernel = solrt.api.KERNEL_MEGA
+        mega_params.append(q)
+
+    def plain_wavefront():
+        for sc, img, cam, p in jobs:
+            r.cmd_trace_rays(sc, cam, p, img)
+
+    def plain_mega():
+        for (sc, img, cam, _), q in zip(jobs, mega_params):
+            r.cmd_trace_rays(sc, cam, q, img)
+
+    for _ in range(args.warmup):
+        batch.launch()
+    plain_wavefront()
+    plain_mega()
+    clocks = ClockSampler(str(local))
+    clocks.start()
+    time.sleep(0.3)
+    barrier(pg)
+    ms_b, seg_b, launches_b = timed(batch.launch, args.steps)
+    ms_w, seg_w, _ = timed(plain_wavefront, 1)
+    ms_m, seg_m, _ = timed(plain_mega, 1)
+    clk = clocks.stop()
+    ms_b_max = max_over_ranks(pg, ms_b)
+    value = sum_over_ranks(pg, float(seg_b)) / (ms_b_max / 1000.0) / 1e6
+    plain_v = seg_m / (ms_m / 1000.0) / 1e6
+    wave_v = seg_w / (ms_w / 1000.0) / 1e6
+    if rank == 0:
+        out = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": round(ms_b_max / args.steps, 3), "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+               "config": {"workload": "batched mixed scenes: %d x (randomised Cornell box + log-uniform 1k-500k-tri "
+                                      "soup), 128^2..1024^2, 4-64 spp, depth 5, one CUDA-graph replay per step"
+                                      % args.jobs, "jobs": args.jobs, "tris": tris, "pixels": pixels,
+                          "samples": samples, "bvh": args.bvh, "passes": info["passes"], "items": info["items"],
+                          "setup_s": round(setup_s, 1),
+                          "l2": "inputs larger than L2 (scenes + BVHs + queues > 129 MB)"},
+               "batched_vs_plain": {"batched": round(value, 3),
+                                    "plain_megakernel_scene_by_scene": round(plain_v, 3),
+                                    "ratio": round(value / plain_v, 3) if plain_v > 0 else None,
+                                    "wavefront_scene_by_scene": round(wave_v, 3),
+                                    "ratio_vs_wavefront": round(value / wave_v, 3) if wave_v > 0 else None},
+               "segments_per_step": int(seg_b // args.steps), "gpu_launches": int(launches_b), "clocks": clk}
+        print(json.dumps(out), flush=True)
+    batch.close()
+    for sc, img, _, _ in jobs:
+        img.close()
+        sc.close()
+    ctx.close()
+    return 0
+
+
 def run_reference(args, world, rank, pg):
     if rank != 0:
         return 0
@@ -247,14 +347,18 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="solrt", choices=["solrt", "reference"])
-    ap.add_argument("--workload", default="soup", choices=["soup", "cornell", "tunnel"])
+    ap.add_argument("--workload", default="soup", choices=["soup", "cornell", "tunnel", "batch"])
     ap.add_argument("--bvh", default="bvh2", choices=["bvh2", "bvh8"])
+    ap.add_argument("--jobs", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     world, rank, local, pg = dist_setup(args)
     if args.impl == "reference":
         return run_reference(args, world, rank, pg)
+    if args.workload == "batch":
+        importlib.import_module("sol-rs_gb300.build").build_lib()
+        return run_batch(args, world, rank, local, pg)
 
     import torch
     b = importlib.import_module("sol-rs_gb300.build")

@@ -184,8 +184,18 @@ typedef struct solrt_render_params {
     uint32_t accum_mode;        /* solrt_accum_mode; must match the image */
     uint32_t rng_mode;          /* solrt_rng_mode */
     float tmax;                 /* 0 = reference 1e4 */
-    uint32_t reserved[3];
+    uint32_t kernel;            /* solrt_kernel */
+    uint32_t reserved[2];
 } solrt_render_params;
+
+typedef enum solrt_kernel {
+    /* generate / extend / shade stages over queues shared by all paths */
+    SOLRT_KERNEL_WAVEFRONT = 0,
+    /* the reference's structure (pathtrace.rgen:39-104): one thread per pixel
+     * loops over its samples and bounces; same image, the plain kernel that
+     * the wavefront and batches are measured against. Not for batches. */
+    SOLRT_KERNEL_MEGA = 1
+} solrt_kernel;
 
 /* ------------------------------------------------------------------------ */
 /* Rays for the ray-file (hit record) API                                   */
@@ -312,6 +322,41 @@ solrt_status solrt_image_device_ptrs(solrt_image* img, void** accum, void** rgba
  * into `img`. Asynchronous on the context stream. */
 solrt_status solrt_render(solrt_context* ctx, solrt_scene* scene, const solrt_camera* camera,
                           const solrt_render_params* params, solrt_image* img);
+
+/* ------------------------------------------------------------------------ */
+/* Batched rendering: many scenes, one wavefront                            */
+/* ------------------------------------------------------------------------ */
+
+/* One render job: what one solrt_render call takes. */
+typedef struct solrt_job {
+    solrt_scene* scene;
+    solrt_image* image;
+    solrt_camera camera;
+    solrt_render_params params;
+} solrt_job;
+
+typedef struct solrt_batch solrt_batch;
+
+enum {
+    SOLRT_BATCH_GRAPH = 1u  /* capture the batch's launches once into a CUDA graph and replay it */
+};
+
+/* Plans a batch: the paths of all jobs share the wavefront queues, each pass
+ * mixes work items of several jobs, and every job's image is bit-identical
+ * to rendering that job alone with solrt_render (each path depends only on
+ * its own job; per-pixel sums run in sample order). All scenes must use the
+ * same BVH kind; every job needs width * height <= the context's path
+ * capacity. Synchronises. */
+solrt_status solrt_batch_create(solrt_context* ctx, const solrt_job* jobs, uint32_t n, uint32_t flags,
+                                solrt_batch** out);
+/* New cameras / frames / seeds for the same jobs (same scenes, images,
+ * sizes, spp, bounces and modes). */
+solrt_status solrt_batch_update(solrt_batch* batch, const solrt_job* jobs);
+/* Renders every job once (asynchronous on the context stream). */
+solrt_status solrt_batch_launch(solrt_batch* batch);
+solrt_status solrt_batch_destroy(solrt_batch* batch);
+/* Passes, work items and bounce launches of the plan. */
+solrt_status solrt_batch_info(solrt_batch* batch, uint32_t* passes, uint32_t* items, uint64_t* paths);
 
 /* Closest-hit queries (one traceRayEXT each, opaque, no culling).
  * Host arrays; synchronises. */

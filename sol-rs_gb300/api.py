@@ -25,6 +25,7 @@ MISS_BLACK, MISS_REF_SKY, MISS_GRADIENT = 0, 1, 2
 MATERIAL_REF, MATERIAL_LAMBERT = 0, 1
 ACCUM_REF_MIX, ACCUM_KAHAN = 0, 1
 RNG_REF_STREAM, RNG_PER_SAMPLE = 0, 1
+KERNEL_WAVEFRONT, KERNEL_MEGA = 0, 1
 EFLAG_STACK, EFLAG_QUEUE, EFLAG_INDEX, EFLAG_TIMEOUT = 1, 2, 4, 8
 
 
@@ -84,7 +85,14 @@ class RenderParams(ctypes.Structure):
                 ("max_bounces", ctypes.c_uint32), ("frame", ctypes.c_uint32), ("accum_start_frame", ctypes.c_uint32),
                 ("seed", ctypes.c_uint32), ("job_id", ctypes.c_uint32), ("miss_mode", ctypes.c_uint32),
                 ("material_mode", ctypes.c_uint32), ("accum_mode", ctypes.c_uint32), ("rng_mode", ctypes.c_uint32),
-                ("tmax", ctypes.c_float), ("reserved", ctypes.c_uint32 * 3)]
+                ("tmax", ctypes.c_float), ("kernel", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 2)]
+
+
+class Job(ctypes.Structure):
+    _fields_ = [("scene", ctypes.c_void_p), ("image", ctypes.c_void_p), ("camera", Camera), ("params", RenderParams)]
+
+
+BATCH_GRAPH = 1
 
 
 class Stats(ctypes.Structure):
@@ -133,6 +141,12 @@ _PROTOS = {
     "solrt_image_read": (ctypes.c_int, [_P, _P, _P]),
     "solrt_image_device_ptrs": (ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P)]),
     "solrt_render": (ctypes.c_int, [_P, _P, ctypes.POINTER(Camera), ctypes.POINTER(RenderParams), _P]),
+    "solrt_batch_create": (ctypes.c_int, [_P, ctypes.POINTER(Job), _U32, _U32, ctypes.POINTER(_P)]),
+    "solrt_batch_update": (ctypes.c_int, [_P, ctypes.POINTER(Job)]),
+    "solrt_batch_launch": (ctypes.c_int, [_P]),
+    "solrt_batch_destroy": (ctypes.c_int, [_P]),
+    "solrt_batch_info": (ctypes.c_int, [_P, ctypes.POINTER(_U32), ctypes.POINTER(_U32),
+                                        ctypes.POINTER(ctypes.c_uint64)]),
     "solrt_trace_rays": (ctypes.c_int, [_P, _P, _P, _U32, _P]),
     "solrt_trace_rays_device": (ctypes.c_int, [_P, _P, _P, _U32, _P]),
     "solrt_debug_unit": (ctypes.c_int, [_P, _U32, _U32, _P, _P, _P, _P, _P]),
@@ -229,9 +243,9 @@ def scene_desc(data):
 class SceneDescription:
     """Device scene + BVH (solrt_scene). Mirrors ray::SceneDescription."""
 
-    def __init__(self, context, data, bvh=BVH2, leaf_max=0):
+    def __init__(self, context, data, bvh=BVH2, leaf_max=0, keep_data=True):
         self.context = context
-        self.data = data
+        self.data = data if keep_data else None
         d = scene_desc(data)
         bd = BvhDesc(kind=bvh, leaf_max=leaf_max)
         h = ctypes.c_void_p()
@@ -336,12 +350,57 @@ def camera_from_view(view16, vfov_deg, aspect, znear=0.1, zfar=1000.0):
 
 def render_params(width, height, spp=8, max_bounces=32, frame=0, accum_start_frame=0, seed=0, job_id=0,
                   miss_mode=MISS_BLACK, material_mode=MATERIAL_REF, accum_mode=ACCUM_REF_MIX,
-                  rng_mode=RNG_REF_STREAM, tmax=0.0):
+                  rng_mode=RNG_REF_STREAM, tmax=0.0, kernel=0):
     """Defaults are the reference's: 8 spp per launch, 32 bounces, black miss,
-    pathtrace.rchit materials, running mix, one RNG stream per pixel."""
+    pathtrace.rchit materials, running mix, one RNG stream per pixel.
+    kernel: KERNEL_WAVEFRONT (0) or KERNEL_MEGA (1, per-pixel loop)."""
     return RenderParams(width=width, height=height, spp=spp, max_bounces=max_bounces, frame=frame,
                         accum_start_frame=accum_start_frame, seed=seed, job_id=job_id, miss_mode=miss_mode,
-                        material_mode=material_mode, accum_mode=accum_mode, rng_mode=rng_mode, tmax=tmax)
+                        material_mode=material_mode, accum_mode=accum_mode, rng_mode=rng_mode, tmax=tmax,
+                        kernel=kernel)
+
+
+def make_jobs(jobs):
+    """(scene, image, camera, params) tuples -> ctypes array of Job."""
+    arr = (Job * len(jobs))()
+    for j, (sc, img, cam, p) in enumerate(jobs):
+        arr[j].scene = sc.handle.value if hasattr(sc.handle, "value") else sc.handle
+        arr[j].image = img.handle.value if hasattr(img.handle, "value") else img.handle
+        arr[j].camera = cam
+        arr[j].params = p
+    return arr
+
+
+class Batch:
+    """Many render jobs over many scenes in shared wavefront passes
+    (solrt_batch); each job's image equals rendering it alone."""
+
+    def __init__(self, context, jobs, graph=False):
+        self.context = context
+        self._keep = list(jobs)
+        arr = make_jobs(jobs)
+        h = ctypes.c_void_p()
+        check(lib().solrt_batch_create(context.handle, arr, len(jobs), BATCH_GRAPH if graph else 0, ctypes.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().solrt_batch_destroy(self.handle)
+            self.handle = None
+
+    __del__ = close
+
+    def update(self, jobs):
+        self._keep = list(jobs)
+        check(lib().solrt_batch_update(self.handle, make_jobs(jobs)))
+
+    def launch(self):
+        check(lib().solrt_batch_launch(self.handle))
+
+    def info(self):
+        p, i, n = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint64()
+        check(lib().solrt_batch_info(self.handle, ctypes.byref(p), ctypes.byref(i), ctypes.byref(n)))
+        return dict(passes=p.value, items=i.value, paths=n.value)
 
 
 class Renderer:

@@ -31,6 +31,7 @@ static_assert(sizeof(solrt_camera) == 256, "four mat4");
 struct solrt_context : solrt::Context {};
 struct solrt_scene : solrt::Scene {};
 struct solrt_image : solrt::Image {};
+struct solrt_batch : solrt::Batch {};
 
 namespace solrt {
 
@@ -120,10 +121,36 @@ solrt_status fill_camera(const double view[16], float vfov_deg, float aspect, fl
     return SOLRT_OK;
 }
 
+std::mutex g_refs_mutex;
+
 }  // namespace
 }  // namespace solrt
 
 using namespace solrt;
+
+// Reference counting of contexts (see Context::refs).
+static void context_retain(solrt_context* c) {
+    std::lock_guard<std::mutex> lock(g_refs_mutex);
+    ++c->refs;
+}
+
+static void context_release(solrt_context* c) {
+    {
+        std::lock_guard<std::mutex> lock(g_refs_mutex);
+        if (--c->refs > 0) return;
+    }
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    for (auto& t : c->timed) {
+        cudaEventDestroy(t.start);
+        cudaEventDestroy(t.end);
+    }
+    if (c->stream) cudaStreamDestroy(c->stream);
+    cudaGetLastError();
+    delete c;
+}
 
 extern "C" {
 
@@ -211,16 +238,7 @@ solrt_status solrt_context_create(const solrt_context_desc* desc, solrt_context*
 
 solrt_status solrt_context_destroy(solrt_context* ctx) {
     if (!ctx) return SOLRT_OK;
-    cudaSetDevice(ctx->device);
-    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
-    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
-    for (auto& t : ctx->timed) {
-        cudaEventDestroy(t.start);
-        cudaEventDestroy(t.end);
-    }
-    if (ctx->stream) cudaStreamDestroy(ctx->stream);
-    delete ctx;
+    context_release(ctx);
     return SOLRT_OK;
 }
 
@@ -360,14 +378,17 @@ solrt_status solrt_scene_create(solrt_context* ctx, const solrt_scene_desc* d, c
     solrt_bvh_desc bd{};
     if (bvh) bd = *bvh;
     if ((s = solrt_scene_build_bvh(sc, &bd)) != SOLRT_OK) return fail(s);
+    context_retain(ctx);
     *out = sc;
     return SOLRT_OK;
 }
 
 solrt_status solrt_scene_destroy(solrt_scene* scene) {
     if (!scene) return SOLRT_OK;
-    cudaStreamSynchronize(scene->ctx->stream);
+    solrt_context* c = static_cast<solrt_context*>(scene->ctx);
+    cudaStreamSynchronize(c->stream);
     delete scene;
+    context_release(c);
     return SOLRT_OK;
 }
 
@@ -464,14 +485,17 @@ solrt_status solrt_image_create(solrt_context* ctx, uint32_t width, uint32_t hei
             return s;
         }
     }
+    context_retain(ctx);
     *out = img;
     return solrt_image_clear(img);
 }
 
 solrt_status solrt_image_destroy(solrt_image* img) {
     if (!img) return SOLRT_OK;
-    cudaStreamSynchronize(img->ctx->stream);
+    solrt_context* c = static_cast<solrt_context*>(img->ctx);
+    cudaStreamSynchronize(c->stream);
     delete img;
+    context_release(c);
     return SOLRT_OK;
 }
 
@@ -516,6 +540,55 @@ solrt_status solrt_render(solrt_context* ctx, solrt_scene* scene, const solrt_ca
               "frame + 1 - accum_start_frame is zero");
     CHECK_ARG(p->tmax >= 0.0f, "tmax must be >= 0");
     return render_frame(*ctx, *scene, *camera, *p, *img);
+}
+
+solrt_status solrt_batch_create(solrt_context* ctx, const solrt_job* jobs, uint32_t n, uint32_t flags,
+                                solrt_batch** out) {
+    CHECK_ARG(ctx && jobs && out, "null argument");
+    *out = nullptr;
+    CHECK_ARG((flags & ~(uint32_t)SOLRT_BATCH_GRAPH) == 0u, "unknown batch flags");
+    solrt_batch* b = new (std::nothrow) solrt_batch();
+    if (!b) return SOLRT_ERR_OOM;
+    const solrt_status s = batch_plan(*ctx, jobs, n, flags, *b);
+    if (s != SOLRT_OK) {
+        delete b;
+        return s;
+    }
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+        set_error("batch upload failed");
+        delete b;
+        return SOLRT_ERR_DEVICE;
+    }
+    context_retain(ctx);
+    *out = b;
+    return SOLRT_OK;
+}
+
+solrt_status solrt_batch_update(solrt_batch* batch, const solrt_job* jobs) {
+    CHECK_ARG(batch && jobs, "null argument");
+    return batch_set_jobs(*batch, jobs);
+}
+
+solrt_status solrt_batch_launch(solrt_batch* batch) {
+    CHECK_ARG(batch, "null batch");
+    return batch_launch(*batch);
+}
+
+solrt_status solrt_batch_destroy(solrt_batch* batch) {
+    if (!batch) return SOLRT_OK;
+    solrt_context* c = static_cast<solrt_context*>(batch->ctx);
+    cudaStreamSynchronize(c->stream);
+    delete batch;
+    context_release(c);
+    return SOLRT_OK;
+}
+
+solrt_status solrt_batch_info(solrt_batch* batch, uint32_t* passes, uint32_t* items, uint64_t* paths) {
+    CHECK_ARG(batch, "null batch");
+    if (passes) *passes = (uint32_t)batch->passes.size();
+    if (items) *items = (uint32_t)batch->items.size();
+    if (paths) *paths = batch->total_paths;
+    return SOLRT_OK;
 }
 
 solrt_status solrt_trace_rays(solrt_context* ctx, solrt_scene* scene, const solrt_ray* rays, uint32_t n,

@@ -3,14 +3,16 @@
 // A warp keeps 32 rays in flight. Every step of its loop is warp-uniform
 // (full-warp votes decide the phases), so lanes re-converge at each step:
 //   refill  lanes whose ray has finished take new rays from the global queue
-//           (one atomic per warp), once at least kRefill lanes are free;
+//           (one atomic per warp), once at least SOLRT_BVH2_REFILL lanes are
+//           free;
 //   nodes   lanes visit inner nodes until every lane has parked a leaf or has
 //           no inner node left; a lane that already parked a leaf keeps
 //           descending until it reaches a second one ("while-while" with
 //           speculative traversal, after Aila & Laine, HPG 2009);
 //   leaves  lanes test their parked leaves together.
-// The closest hit does not depend on visiting order, so results equal those
-// of a plain per-ray loop.
+// Each lane carries its own scene (IO::load), so one launch can serve rays of
+// many scenes. The closest hit does not depend on visiting order, so results
+// equal those of a plain per-ray loop.
 #pragma once
 
 #include "traverse.cuh"
@@ -23,8 +25,7 @@ constexpr int kBvh2Sentinel = 0x7fffffff;
 #endif
 
 template <class IO, bool kCount>
-SOLRT_D void extend_bvh2_ww(const DevScene& sc, const IO& io, uint32_t n, unsigned int* work, TraceCounters& cnt,
-                            uint32_t& ef) {
+SOLRT_D void extend_bvh2_ww(const IO& io, uint32_t n, unsigned int* work, TraceCounters& cnt, uint32_t& ef) {
     const int lane = threadIdx.x & 31;
     const uint32_t lane_lt = (1u << lane) - 1u;
     int stack[SOLRT_BVH2_STACK + 1];
@@ -35,10 +36,10 @@ SOLRT_D void extend_bvh2_ww(const DevScene& sc, const IO& io, uint32_t n, unsign
     bool drained = false;      // the queue has no more rays for this warp
     uint32_t idx = 0, budget = 0;
     RayWT r;
+    TravScene ts{nullptr, nullptr, 0u, 0u};
     float ix = 0.0f, iy = 0.0f, iz = 0.0f;     // 1 / box_dir(d)
     float nox = 0.0f, noy = 0.0f, noz = 0.0f;  // -o / box_dir(d)
     HitRec best{0.0f, SOLRT_NO_HIT, 0.0f, 0.0f};
-    const uint32_t max_steps = 2u * (sc.node_count + sc.tri_count) + 64u;
     for (;;) {
         const bool idle = node == kBvh2Sentinel && leaf >= 0;
         if (idle && has) {
@@ -56,7 +57,7 @@ SOLRT_D void extend_bvh2_ww(const DevScene& sc, const IO& io, uint32_t n, unsign
                 const uint32_t i = base + (uint32_t)__popc(need & lane_lt);
                 if (i < n) {
                     float4 o, d;
-                    io.load(i, o, d);
+                    io.load(i, o, d, ts);
                     idx = i;
                     has = true;
                     r = setup_ray(o.x, o.y, o.z, d.x, d.y, d.z, o.w);
@@ -67,29 +68,29 @@ SOLRT_D void extend_bvh2_ww(const DevScene& sc, const IO& io, uint32_t n, unsign
                     noy = -(o.y * iy);
                     noz = -(o.z * iz);
                     best = HitRec{d.w, SOLRT_NO_HIT, 0.0f, 0.0f};
-                    budget = max_steps;
+                    budget = 2u * (ts.node_count + ts.tri_count) + 64u;
                     stack[0] = kBvh2Sentinel;
                     sp = 1;
-                    node = sc.tri_count ? 0 : kBvh2Sentinel;
+                    node = ts.tri_count ? 0 : kBvh2Sentinel;
                     leaf = 0;
                 }
             }
         }
         if (!__any_sync(0xffffffffu, has)) {
             if (drained) break;
-            continue;  // fewer than kRefill free lanes but none busy: refill next round
+            continue;
         }
         // node phase
         for (;;) {
             const bool inner = (unsigned)node < (unsigned)kBvh2Sentinel;
             if (!__any_sync(0xffffffffu, inner && leaf >= 0)) break;
             if (inner) {
-                if (--budget == 0u || (uint32_t)node >= sc.node_count) {
+                if (--budget == 0u || (uint32_t)node >= ts.node_count) {
                     ef |= SOLRT_EFLAG_INDEX;
                     node = kBvh2Sentinel;
                     leaf = 0;
                 } else {
-                    const float4* np = sc.nodes + 4 * (size_t)node;
+                    const float4* np = ts.nodes + 4 * (size_t)node;
                     const float4 n0 = __ldg(np + 0), n1 = __ldg(np + 1), n2 = __ldg(np + 2);
                     const int4 n3 = __ldg(reinterpret_cast<const int4*>(np + 3));
                     if (kCount) ++cnt.nodes;
@@ -121,12 +122,12 @@ SOLRT_D void extend_bvh2_ww(const DevScene& sc, const IO& io, uint32_t n, unsign
         while (__any_sync(0xffffffffu, leaf < 0)) {
             if (leaf < 0) {
                 const uint32_t k = (uint32_t)(~leaf);
-                if (--budget == 0u || k >= sc.tri_count) {
+                if (--budget == 0u || k >= ts.tri_count) {
                     ef |= SOLRT_EFLAG_INDEX;
                     node = kBvh2Sentinel;
                     leaf = 0;
                 } else {
-                    const float4* tp = sc.tri_wt + 3 * (size_t)k;
+                    const float4* tp = ts.tris + 3 * (size_t)k;
                     if (kCount) ++cnt.tris;
                     cnt.fallbacks += intersect_tri(r, __ldg(tp), __ldg(tp + 1), __ldg(tp + 2), best);
                     leaf = node;
@@ -134,6 +135,58 @@ SOLRT_D void extend_bvh2_ww(const DevScene& sc, const IO& io, uint32_t n, unsign
                 }
             }
         }
+    }
+}
+
+// One ray, plain depth-first loop (nearer child first): the traversal of the
+// per-pixel megakernel.
+SOLRT_D void trace_bvh2_ray(const TravScene& ts, float ox, float oy, float oz, float dx, float dy, float dz,
+                            float tmin, float tmax, HitRec& best, TraceCounters& cnt, uint32_t& ef) {
+    best = HitRec{tmax, SOLRT_NO_HIT, 0.0f, 0.0f};
+    if (ts.tri_count == 0) return;
+    const RayWT r = setup_ray(ox, oy, oz, dx, dy, dz, tmin);
+    const float ix = 1.0f / box_dir(dx), iy = 1.0f / box_dir(dy), iz = 1.0f / box_dir(dz);
+    const float nox = -(ox * ix), noy = -(oy * iy), noz = -(oz * iz);
+    int stack[SOLRT_BVH2_STACK + 1];
+    stack[0] = kBvh2Sentinel;
+    int sp = 1;
+    int node = 0;
+    uint32_t budget = 2u * (ts.node_count + ts.tri_count) + 64u;
+    while (node != kBvh2Sentinel) {
+        if (--budget == 0u) {
+            ef |= SOLRT_EFLAG_INDEX;
+            return;
+        }
+        if (node >= 0) {
+            if ((uint32_t)node >= ts.node_count) {
+                ef |= SOLRT_EFLAG_INDEX;
+                return;
+            }
+            const float4* np = ts.nodes + 4 * (size_t)node;
+            const float4 n0 = __ldg(np + 0), n1 = __ldg(np + 1), n2 = __ldg(np + 2);
+            const int4 n3 = __ldg(reinterpret_cast<const int4*>(np + 3));
+            float t0, t1;
+            const bool h0 = slab_fma(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, ix, iy, iz, nox, noy, noz, tmin, best.t, t0);
+            const bool h1 = slab_fma(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, ix, iy, iz, nox, noy, noz, tmin, best.t, t1);
+            if (h0 && h1) {
+                const bool swap = t1 < t0;
+                if (sp <= SOLRT_BVH2_STACK) stack[sp++] = swap ? n3.x : n3.y;
+                else ef |= SOLRT_EFLAG_STACK;
+                node = swap ? n3.y : n3.x;
+                continue;
+            }
+            if (h0) { node = n3.x; continue; }
+            if (h1) { node = n3.y; continue; }
+        } else {
+            const uint32_t k = (uint32_t)(~node);
+            if (k >= ts.tri_count) {
+                ef |= SOLRT_EFLAG_INDEX;
+                return;
+            }
+            const float4* tp = ts.tris + 3 * (size_t)k;
+            cnt.fallbacks += intersect_tri(r, __ldg(tp), __ldg(tp + 1), __ldg(tp + 2), best);
+        }
+        node = stack[--sp];
     }
 }
 

@@ -32,7 +32,7 @@ SOLRT_D float byte_as_float(uint32_t word, uint32_t k) {
 }
 
 template <bool kCount>
-SOLRT_D void trace_bvh8(const DevScene& sc, float ox, float oy, float oz, float dx, float dy, float dz, float tmin,
+SOLRT_D void trace_bvh8(const TravScene& sc, float ox, float oy, float oz, float dx, float dy, float dz, float tmin,
                         float tmax, HitRec& best, TraceCounters& cnt, uint32_t& eflags) {
     best.t = tmax;
     best.prim = SOLRT_NO_HIT;
@@ -99,7 +99,7 @@ SOLRT_D void trace_bvh8(const DevScene& sc, float ox, float oy, float oz, float 
             hit_tri &= hit_tri - 1u;
             const uint32_t ti = tri_base + k;
             if (ti < sc.tri_count) {
-                const float4* tp = sc.tri_wt + 3 * (size_t)ti;
+                const float4* tp = sc.tris + 3 * (size_t)ti;
                 if (kCount) ++cnt.tris;
                 cnt.fallbacks += intersect_tri(r, __ldg(tp), __ldg(tp + 1), __ldg(tp + 2), best);
             } else {

@@ -336,6 +336,7 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
     sc.nodes.release();
     sc.tri_wt.release();
     if (n == 0) return SOLRT_OK;
+    cudaGetLastError();  // launch errors below must be this call's own
 
     SOLRT_CUDA(cudaEventRecord(ctx.ev0, st));
     const uint32_t ni = n > 1 ? n - 1 : 1;  // internal nodes (one for a single triangle)

@@ -84,10 +84,75 @@ struct PathQueue {
     float4* o_tmin;   // origin, tmin
     float4* d_tmax;   // direction, tmax
     float4* thr_rng;  // throughput, rng state (bits)
-    uint2* meta;      // slot within the pass, depth
+    uint2* meta;      // slot within the pass, job << kDepthBits | depth
+};
+
+// One job of a wavefront batch, as the device sees it.
+struct DevJob {
+    DevScene sc;
+    float vinv[16];
+    float pinv[16];
+    uint32_t width, height, spp, frame, start, seed, job_id, rng_mode;
+    uint32_t miss_mode, material_mode, max_bounces, accum_mode;
+    float tmax;
+    uint32_t pad[3];
+    float4* accum;
+    uchar4* rgba8;
+    float4* fsum;
+    float4* ksum;
+    float4* kcomp;
+    uint32_t* rng_state;
+};
+
+// A work item of one pass: samples [s0, s0 + k) of pixels [pix0, pix0 + npix)
+// of one job. Its paths occupy slots [path_base, path_base + npix * k) of the
+// pass (pixel-major), its pixels [pix_base, pix_base + npix) of the pass's
+// pixel space.
+struct DevItem {
+    uint32_t job, pix0, npix, s0, k, path_base, pix_base, pad;
+};
+
+// The depth field of a path's meta word also carries its job.
+constexpr uint32_t kDepthBits = 11;
+constexpr uint32_t kDepthMask = (1u << kDepthBits) - 1u;
+
+struct PassPlan {
+    uint32_t item_begin, item_count;
+    uint32_t paths, pixels;
+    uint32_t bounces;  // extend/shade launches of the pass
+};
+
+struct Context;
+
+// A planned batch (also a single render: a batch of one job).
+struct Batch {
+    Context* ctx = nullptr;
+    uint32_t flags = 0;
+    uint32_t kind = 0;
+    std::vector<DevJob> jobs;
+    std::vector<DevItem> items;
+    std::vector<PassPlan> passes;
+    std::vector<uint32_t> job_pix_base;  // prefix of width*height over jobs (+ total)
+    uint64_t total_paths = 0;
+    uint64_t graph_launches = 0;
+    DeviceBuffer d_jobs, d_items, d_job_pix;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    Batch() = default;
+    Batch(const Batch&) = delete;
+    Batch& operator=(const Batch&) = delete;
+    ~Batch() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+    }
 };
 
 struct Context {
+    // The handle and every scene, image and batch created on the context hold
+    // a reference; the context is freed when the last one goes, so objects
+    // destroyed after solrt_context_destroy stay valid until then.
+    int refs = 1;
+    Batch single;  // plan of the last solrt_render call
     int device = 0;
     int sm_count = 0;
     cudaStream_t stream = nullptr;
@@ -176,10 +241,14 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc);
 
 // trace.cu
 solrt_status launch_trace_rays(Context& ctx, const Scene& sc, const solrt_ray* rays, uint32_t n, solrt_hit* hits);
-solrt_status launch_extend(Context& ctx, const Scene& sc, const PathQueue& q, float4* hits,
-                           const unsigned int* count, unsigned int* work, uint32_t capacity);
+// Extend for a batched queue: the scene of ray i is jobs[meta[i].y >> kDepthBits].sc.
+solrt_status launch_extend(Context& ctx, uint32_t kind, const DevJob* jobs, const PathQueue& q, float4* hits,
+                           const unsigned int* count, unsigned int* work);
 
 // pathtrace.cu
+solrt_status batch_plan(Context& ctx, const solrt_job* jobs, uint32_t n, uint32_t flags, Batch& b);
+solrt_status batch_set_jobs(Batch& b, const solrt_job* jobs);
+solrt_status batch_launch(Batch& b);
 solrt_status render_frame(Context& ctx, const Scene& sc, const solrt_camera& cam, const solrt_render_params& p,
                           Image& img);
 solrt_status debug_unit(Context& ctx, uint32_t op, uint32_t n, const uint32_t* a, const uint32_t* b,

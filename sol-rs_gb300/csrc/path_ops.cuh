@@ -1,0 +1,119 @@
+// path_ops.cuh — the per-path operations of the pathtrace shaders, shared by
+// the wavefront kernels (one stage per launch) and the per-pixel megakernel
+// (the reference's structure: one thread loops over samples and bounces).
+#pragma once
+
+#include "internal.h"
+
+namespace solrt {
+
+// RNG state of sample s of pixel pix (pathtrace.rgen:47 for REF_STREAM's
+// first sample; later REF_STREAM samples continue the previous state).
+SOLRT_D uint32_t sample_seed(const DevJob& J, uint32_t pix, uint32_t s, uint32_t prev) {
+    if (J.rng_mode == SOLRT_RNG_PER_SAMPLE) {
+        uint32_t rng = tea(pix, J.frame * J.spp + s);
+        if (J.seed != 0) rng ^= tea(J.seed, J.job_id);
+        return rng;
+    }
+    return s == 0 ? tea(pix, J.frame) : prev;
+}
+
+// pathtrace.rgen:52-60: jitter, NDC, origin and direction through the
+// inverse matrices; tmin of preparePayload (rgen:35).
+SOLRT_D void camera_ray(const DevJob& J, uint32_t pix, uint32_t& rng, float4& o_tmin, float4& d_tmax) {
+    const uint32_t x = pix % J.width, y = pix / J.width;
+    const float j0 = next_rand(rng);
+    const float j1 = next_rand(rng);
+    const float px = __uint2float_rn(x) + j0, py = __uint2float_rn(y) + j1;
+    const float ux = px / __uint2float_rn(J.width), uy = py / __uint2float_rn(J.height);
+    const float dx = ux * 2.0f - 1.0f, dy = uy * 2.0f - 1.0f;
+    float org[4], tgt[4], dir[4];
+    mat4_mul(J.vinv, 0.0f, 0.0f, 0.0f, 1.0f, org);
+    mat4_mul(J.pinv, dx, dy, 1.0f, 1.0f, tgt);
+    const f3 tn = normalize(f3{tgt[0], tgt[1], tgt[2]});
+    mat4_mul(J.vinv, tn.x, tn.y, tn.z, 0.0f, dir);
+    const float tmin = glsl_max(1.0f, length(f3{org[0], org[1], org[2]})) * 1e-3f;
+    o_tmin = make_float4(org[0], org[1], org[2], tmin);
+    d_tmax = make_float4(dir[0], dir[1], dir[2], J.tmax);
+}
+
+// One closest-hit or miss step (pathtrace.rchit:56-113, pathtrace.rmiss:8-21
+// and pathtrace.rgen:77-84). h = (t, prim bits, u, v). Updates the path
+// throughput `acc`, the rng state and the depth; returns true when the path
+// continues with the ray (o_next, d_next).
+SOLRT_D bool shade_step(const DevJob& J, float4 o, float4 d, float4 h, f3& acc, uint32_t& rng, uint32_t& depth,
+                        float4& o_next, float4& d_next, uint32_t& ef) {
+    const DevScene& sc = J.sc;
+    const f3 dir{d.x, d.y, d.z};
+    const uint32_t prim = __float_as_uint(h.y);
+    if (prim == SOLRT_NO_HIT || prim >= sc.tri_count) {
+        if (prim != SOLRT_NO_HIT) ef |= SOLRT_EFLAG_INDEX;
+        acc = acc * miss_color(dir, J.miss_mode);                           // rmiss:8-21
+        return false;
+    }
+    const uint4 ti = __ldg(sc.tri_idx + prim);                               // rchit:63-73
+    const float4 m0 = __ldg(sc.materials + 3 * ti.w);
+    const float4 m1 = __ldg(sc.materials + 3 * ti.w + 1);
+    const float4 m2 = __ldg(sc.materials + 3 * ti.w + 2);
+    if (m1.x >= 1.0f || m1.y >= 1.0f || m1.z >= 1.0f) {                      // rchit:75-80
+        acc = acc * f3{m1.x, m1.y, m1.z};
+        return false;
+    }
+    const float b1 = h.z, b2 = h.w;
+    const float b0 = (1.0f - b1) - b2;                                       // rchit:82
+    const float4 n0 = __ldg(sc.vnrm + ti.x), n1 = __ldg(sc.vnrm + ti.y), n2 = __ldg(sc.vnrm + ti.z);
+    const float4 p0 = __ldg(sc.vpos + ti.x), p1 = __ldg(sc.vpos + ti.y), p2 = __ldg(sc.vpos + ti.z);
+    const float4 c0 = __ldg(sc.vcol + ti.x), c1 = __ldg(sc.vcol + ti.y), c2 = __ldg(sc.vcol + ti.z);
+    f3 normal = f3{n0.x, n0.y, n0.z} * b0 + f3{n1.x, n1.y, n1.z} * b1 + f3{n2.x, n2.y, n2.z} * b2;
+    normal = normalize(normal);                                              // rchit:84-86
+    const f3 pos = f3{p0.x, p0.y, p0.z} * b0 + f3{p1.x, p1.y, p1.z} * b1 + f3{p2.x, p2.y, p2.z} * b2;
+    const f3 vcol = f3{c0.x, c0.y, c0.z} * b0 + f3{c1.x, c1.y, c1.z} * b1 + f3{c2.x, c2.y, c2.z} * b2;
+    const f3 wi = normalize(dir);                                            // rchit:94-95
+    const f3 n_o = normal * glsl_sign(dot(normal, -wi));
+    const float alpha2 = m2.y * m2.y;
+    const float xi0 = next_rand(rng);                                        // rchit:97-98
+    const float xi1 = next_rand(rng);
+    const float rnd = next_rand(rng);
+    const f3 base_c{m0.x, m0.y, m0.z};
+    const f3 no = pos + 1e-4f * n_o;                                         // rchit:100
+    f3 nd, hv;
+    if (J.material_mode == SOLRT_MATERIAL_LAMBERT) {
+        nd = sample_cosine(n_o, xi0, xi1);
+        hv = base_c * vcol;
+    } else if (rnd < m2.x) {                                                 // rchit:101-104
+        nd = sample_ggx(reflect(dir, n_o), xi0, xi1, alpha2);
+        hv = base_c * vcol;
+    } else {
+        const f3 mh = sample_ggx(n_o, xi0, xi1, alpha2);                     // rchit:106-114
+        if (rnd < fresnel_dielectric(n_o, mh, 1.0f / 1.5f)) {
+            nd = reflect(dir, mh);
+            hv = f3{1.0f, 1.0f, 1.0f};
+        } else {
+            nd = sample_cosine(n_o, xi0, xi1);
+            hv = base_c * vcol;
+        }
+    }
+    depth = depth + 1u;                                                      // rchit:116
+    acc = acc * hv;                                                          // rgen:77
+    if (depth > J.max_bounces) {                                             // rgen:81-84
+        acc = f3{0.0f, 0.0f, 0.0f};
+        return false;
+    }
+    o_next = make_float4(no.x, no.y, no.z, o.w);
+    d_next = make_float4(nd.x, nd.y, nd.z, d.w);
+    return true;
+}
+
+// Per-pixel sample sums (rgen:86) and the Kahan variant.
+SOLRT_D void add_sample(f3& s, float4 c) { s = s + f3{c.x, c.y, c.z}; }
+SOLRT_D void add_sample_kahan(f3& ks, f3& kc, float& kn, float4 c) {
+    if (isfinite(c.x) && isfinite(c.y) && isfinite(c.z)) {
+        const f3 yv = f3{c.x, c.y, c.z} - kc;
+        const f3 t = ks + yv;
+        kc = (t - ks) - yv;
+        ks = t;
+        kn = kn + 1.0f;
+    }
+}
+
+}  // namespace solrt

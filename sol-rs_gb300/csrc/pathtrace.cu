@@ -1,4 +1,5 @@
-// pathtrace.cu — wavefront restatement of the 5-pathtrace shaders.
+// pathtrace.cu — wavefront restatement of the 5-pathtrace shaders, for one
+// job (solrt_render) or a batch of jobs over many scenes (solrt_batch_*).
 //
 // The reference runs one raygen invocation per pixel that loops over 8
 // samples and up to maxBounces+1 traceRayEXT calls, each resuming in the
@@ -6,81 +7,70 @@
 // pathtrace.rchit:56-113, pathtrace.rmiss:8-21). Here the loop is split into
 // stages over structure-of-arrays queues in HBM:
 //
-//   generate  camera rays for (pixel, sample) pairs of one pass  (rgen:47-61)
-//   extend    closest hit per queued ray                          (trace.cu)
+//   generate  camera rays for the (pixel, sample) pairs of a pass (rgen:47-61)
+//   extend    closest hit per queued ray                           (trace.cu)
 //   shade     miss / emissive / scatter; survivors are appended to the next
-//             queue with one atomic per warp (ballot compaction)  (rchit, rmiss)
+//             queue with one atomic per warp (ballot compaction)   (rchit, rmiss)
 //   accumulate per-pixel sums of the pass's path radiance, in sample order
-//   finalize  mean, running mix with NaN/Inf guard, gamma, RGBA8  (rgen:86-103)
+//   finalize  mean, running mix with NaN/Inf guard, gamma, RGBA8   (rgen:86-103)
 //
-// Every path writes its radiance to its own slot and the per-pixel sum runs
-// in sample order, so the result does not depend on queue order: it equals a
-// sequential per-pixel evaluation bit for bit.
+// A pass is a list of work items (job, pixel range, sample range) whose
+// paths fit the queues. Items of different jobs share a pass: each path
+// carries its job in its meta word and reads that job's scene and
+// parameters. Every path writes its radiance to its own slot and per-pixel
+// sums run in sample order, so a job's image does not depend on queue order
+// or on the other jobs: it equals a sequential per-pixel evaluation bit for
+// bit.
 #include <algorithm>
 
+#include "bvh2_ww.cuh"
+#include "bvh8_traverse.cuh"
 #include "internal.h"
+#include "path_ops.cuh"
 
 namespace solrt {
 
-int extend_blocks_per_sm(uint32_t kind, bool counters);
-
 namespace {
 
-struct GenParams {
-    float vinv[16];
-    float pinv[16];
-    uint32_t width, height, spp, frame, seed, job_id, rng_mode;
-    uint32_t pix0, npix, s0, k;
-    float tmax;
-};
+// Largest index i in [0, n) with key(i) <= v (key increasing, key(0) = 0).
+template <class F>
+SOLRT_D uint32_t find_last_le(uint32_t n, uint32_t v, F key) {
+    uint32_t lo = 0, hi = n;  // invariant: key(lo) <= v, answer in [lo, hi)
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (key(mid) <= v) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
 
-struct ShadeParams {
-    uint32_t max_bounces, miss_mode, material_mode, rng_mode;
-    uint32_t pix0, k, capacity;
-};
-
-__global__ void k_generate(GenParams g, PathQueue q, unsigned int* __restrict__ count0,
-                           const uint32_t* __restrict__ rng_state, DevStats* stats) {
+__global__ void k_generate(const DevJob* __restrict__ jobs, const DevItem* __restrict__ items, uint32_t nitems,
+                           uint32_t P, PathQueue q, unsigned int* __restrict__ count0, DevStats* stats) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t P = g.npix * g.k;
     if (i == 0) {
         *count0 = P;
         atomicAdd(&stats->paths, (unsigned long long)P);
     }
     if (i >= P) return;
-    const uint32_t lp = i / g.k, j = i - lp * g.k;
-    const uint32_t pix = g.pix0 + lp, s = g.s0 + j;
-    const uint32_t x = pix % g.width, y = pix / g.width;
-    uint32_t rng;
-    if (g.rng_mode == SOLRT_RNG_PER_SAMPLE) {
-        rng = tea(pix, g.frame * g.spp + s);
-        if (g.seed != 0) rng ^= tea(g.seed, g.job_id);
-    } else {
-        rng = s == 0 ? tea(pix, g.frame) : rng_state[pix];   // rgen:47
-    }
-    // rgen:52-58: jitter, NDC, origin and direction through the inverse matrices
-    const float j0 = next_rand(rng);
-    const float j1 = next_rand(rng);
-    const float px = __uint2float_rn(x) + j0, py = __uint2float_rn(y) + j1;
-    const float ux = px / __uint2float_rn(g.width), uy = py / __uint2float_rn(g.height);
-    const float dx = ux * 2.0f - 1.0f, dy = uy * 2.0f - 1.0f;
-    float org[4], tgt[4], dir[4];
-    mat4_mul(g.vinv, 0.0f, 0.0f, 0.0f, 1.0f, org);
-    mat4_mul(g.pinv, dx, dy, 1.0f, 1.0f, tgt);
-    const f3 tn = normalize(f3{tgt[0], tgt[1], tgt[2]});
-    mat4_mul(g.vinv, tn.x, tn.y, tn.z, 0.0f, dir);
-    const float tmin = glsl_max(1.0f, length(f3{org[0], org[1], org[2]})) * 1e-3f;  // rgen:35
-    q.o_tmin[i] = make_float4(org[0], org[1], org[2], tmin);
-    q.d_tmax[i] = make_float4(dir[0], dir[1], dir[2], g.tmax);
+    const DevItem it = items[find_last_le(nitems, i, [&](uint32_t t) { return items[t].path_base; })];
+    const DevJob& J = jobs[it.job];
+    const uint32_t local = i - it.path_base;
+    const uint32_t lp = local / it.k, j = local - lp * it.k;
+    const uint32_t pix = it.pix0 + lp, s = it.s0 + j;
+    uint32_t rng = sample_seed(J, pix, s, J.rng_mode == SOLRT_RNG_REF_STREAM && s > 0 ? J.rng_state[pix] : 0u);
+    float4 o, d;
+    camera_ray(J, pix, rng, o, d);
+    q.o_tmin[i] = o;
+    q.d_tmax[i] = d;
     q.thr_rng[i] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(rng));
-    q.meta[i] = make_uint2(i, 0u);
+    q.meta[i] = make_uint2(i, it.job << kDepthBits);
 }
 
-__global__ void __launch_bounds__(256) k_shade(DevScene sc, ShadeParams sp, PathQueue qin,
-                                               const float4* __restrict__ hits,
+__global__ void __launch_bounds__(256) k_shade(const DevJob* __restrict__ jobs, const DevItem* __restrict__ items,
+                                               uint32_t nitems, PathQueue qin, const float4* __restrict__ hits,
                                                const unsigned int* __restrict__ count_in, PathQueue qout,
-                                               unsigned int* __restrict__ count_out, float4* __restrict__ rad,
-                                               uint32_t* __restrict__ rng_state, DevStats* stats) {
+                                               unsigned int* __restrict__ count_out, uint32_t capacity,
+                                               float4* __restrict__ rad, DevStats* stats) {
     const unsigned int n = *count_in;
     const int lane = threadIdx.x & 31;
     const uint32_t lane_lt = (1u << lane) - 1u;
@@ -95,75 +85,21 @@ __global__ void __launch_bounds__(256) k_shade(DevScene sc, ShadeParams sp, Path
         if (i < n) {
             const float4 o = qin.o_tmin[i], d = qin.d_tmax[i], tr = qin.thr_rng[i];
             m = qin.meta[i];
-            const float4 h = hits[i];
+            const uint32_t job = m.y >> kDepthBits;
+            const DevJob& J = jobs[job];
             uint32_t rng = __float_as_uint(tr.w);
+            uint32_t depth = m.y & kDepthMask;
             f3 acc{tr.x, tr.y, tr.z};
-            const f3 dir{d.x, d.y, d.z};
-            const uint32_t prim = __float_as_uint(h.y);
-            bool done = true;
-            if (prim == SOLRT_NO_HIT || prim >= sc.tri_count) {
-                if (prim != SOLRT_NO_HIT) ef |= SOLRT_EFLAG_INDEX;
-                acc = acc * miss_color(dir, sp.miss_mode);                      // rmiss:8-21
-            } else {
-                const uint4 ti = __ldg(sc.tri_idx + prim);                       // rchit:63-73
-                const float4 m0 = __ldg(sc.materials + 3 * ti.w);
-                const float4 m1 = __ldg(sc.materials + 3 * ti.w + 1);
-                const float4 m2 = __ldg(sc.materials + 3 * ti.w + 2);
-                if (m1.x >= 1.0f || m1.y >= 1.0f || m1.z >= 1.0f) {              // rchit:75-80
-                    acc = acc * f3{m1.x, m1.y, m1.z};
-                } else {
-                    const float b1 = h.z, b2 = h.w;
-                    const float b0 = (1.0f - b1) - b2;                           // rchit:82
-                    const float4 n0 = __ldg(sc.vnrm + ti.x), n1 = __ldg(sc.vnrm + ti.y), n2 = __ldg(sc.vnrm + ti.z);
-                    const float4 p0 = __ldg(sc.vpos + ti.x), p1 = __ldg(sc.vpos + ti.y), p2 = __ldg(sc.vpos + ti.z);
-                    const float4 c0 = __ldg(sc.vcol + ti.x), c1 = __ldg(sc.vcol + ti.y), c2 = __ldg(sc.vcol + ti.z);
-                    f3 normal = f3{n0.x, n0.y, n0.z} * b0 + f3{n1.x, n1.y, n1.z} * b1 + f3{n2.x, n2.y, n2.z} * b2;
-                    normal = normalize(normal);                                  // rchit:84-86
-                    const f3 pos = f3{p0.x, p0.y, p0.z} * b0 + f3{p1.x, p1.y, p1.z} * b1 + f3{p2.x, p2.y, p2.z} * b2;
-                    const f3 vcol = f3{c0.x, c0.y, c0.z} * b0 + f3{c1.x, c1.y, c1.z} * b1 + f3{c2.x, c2.y, c2.z} * b2;
-                    const f3 wi = normalize(dir);                                // rchit:94-95
-                    const f3 n_o = normal * glsl_sign(dot(normal, -wi));
-                    const float alpha2 = m2.y * m2.y;
-                    const float xi0 = next_rand(rng);                            // rchit:97-98
-                    const float xi1 = next_rand(rng);
-                    const float rnd = next_rand(rng);
-                    const f3 base_c{m0.x, m0.y, m0.z};
-                    const f3 no = pos + 1e-4f * n_o;                             // rchit:100
-                    f3 nd, hv;
-                    if (sp.material_mode == SOLRT_MATERIAL_LAMBERT) {
-                        nd = sample_cosine(n_o, xi0, xi1);
-                        hv = base_c * vcol;
-                    } else if (rnd < m2.x) {                                     // rchit:101-104
-                        nd = sample_ggx(reflect(dir, n_o), xi0, xi1, alpha2);
-                        hv = base_c * vcol;
-                    } else {
-                        const f3 mh = sample_ggx(n_o, xi0, xi1, alpha2);         // rchit:106-114
-                        if (rnd < fresnel_dielectric(n_o, mh, 1.0f / 1.5f)) {
-                            nd = reflect(dir, mh);
-                            hv = f3{1.0f, 1.0f, 1.0f};
-                        } else {
-                            nd = sample_cosine(n_o, xi0, xi1);
-                            hv = base_c * vcol;
-                        }
-                    }
-                    const uint32_t depth = m.y + 1u;                             // rchit:116
-                    acc = acc * hv;                                              // rgen:77
-                    if (depth > sp.max_bounces) {                                // rgen:81-84
-                        acc = f3{0.0f, 0.0f, 0.0f};
-                    } else {
-                        done = false;
-                        out_o = make_float4(no.x, no.y, no.z, o.w);
-                        out_d = make_float4(nd.x, nd.y, nd.z, d.w);
-                        out_t = make_float4(acc.x, acc.y, acc.z, __uint_as_float(rng));
-                        m.y = depth;
-                    }
-                }
-            }
-            if (done) {
-                rad[m.x] = make_float4(acc.x, acc.y, acc.z, 0.0f);
-                if (sp.rng_mode == SOLRT_RNG_REF_STREAM) rng_state[sp.pix0 + m.x / sp.k] = rng;
-            } else {
+            if (shade_step(J, o, d, hits[i], acc, rng, depth, out_o, out_d, ef)) {
                 alive = true;
+                out_t = make_float4(acc.x, acc.y, acc.z, __uint_as_float(rng));
+                m.y = (job << kDepthBits) | depth;
+            } else {
+                rad[m.x] = make_float4(acc.x, acc.y, acc.z, 0.0f);
+                if (J.rng_mode == SOLRT_RNG_REF_STREAM) {
+                    const DevItem it = items[find_last_le(nitems, m.x, [&](uint32_t t) { return items[t].path_base; })];
+                    J.rng_state[it.pix0 + (m.x - it.path_base) / it.k] = rng;
+                }
             }
         }
         const uint32_t mask = __ballot_sync(0xffffffffu, alive);
@@ -174,7 +110,7 @@ __global__ void __launch_bounds__(256) k_shade(DevScene sc, ShadeParams sp, Path
             pos0 = __shfl_sync(0xffffffffu, pos0, leader);
             if (alive) {
                 const uint32_t pos = pos0 + __popc(mask & lane_lt);
-                if (pos < sp.capacity) {
+                if (pos < capacity) {
                     qout.o_tmin[pos] = out_o;
                     qout.d_tmax[pos] = out_d;
                     qout.thr_rng[pos] = out_t;
@@ -189,37 +125,101 @@ __global__ void __launch_bounds__(256) k_shade(DevScene sc, ShadeParams sp, Path
 }
 
 // Per-pixel sums of one pass, samples in order (rgen:86).
-__global__ void k_accumulate(const float4* __restrict__ rad, uint32_t pix0, uint32_t npix, uint32_t k,
-                             uint32_t accum_mode, float4* __restrict__ fsum, float4* __restrict__ ksum,
-                             float4* __restrict__ kcomp) {
-    const uint32_t lp = blockIdx.x * blockDim.x + threadIdx.x;
-    if (lp >= npix) return;
-    const uint32_t pix = pix0 + lp;
-    if (accum_mode == SOLRT_ACCUM_KAHAN) {
-        const float4 s4 = ksum[pix], c4 = kcomp[pix];
+__global__ void k_accumulate(const DevJob* __restrict__ jobs, const DevItem* __restrict__ items, uint32_t nitems,
+                             uint32_t pixels, const float4* __restrict__ rad) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= pixels) return;
+    const DevItem it = items[find_last_le(nitems, t, [&](uint32_t i) { return items[i].pix_base; })];
+    const DevJob& J = jobs[it.job];
+    const uint32_t lp = t - it.pix_base;
+    const uint32_t pix = it.pix0 + lp;
+    const float4* r = rad + it.path_base + (size_t)lp * it.k;
+    if (J.accum_mode == SOLRT_ACCUM_KAHAN) {
+        const float4 s4 = J.ksum[pix], c4 = J.kcomp[pix];
         f3 ks{s4.x, s4.y, s4.z}, kc{c4.x, c4.y, c4.z};
         float kn = s4.w;
-        for (uint32_t j = 0; j < k; ++j) {
-            const float4 c = rad[(size_t)lp * k + j];
-            if (isfinite(c.x) && isfinite(c.y) && isfinite(c.z)) {
-                const f3 yv = f3{c.x, c.y, c.z} - kc;
-                const f3 t = ks + yv;
-                kc = (t - ks) - yv;
-                ks = t;
-                kn = kn + 1.0f;
-            }
-        }
-        ksum[pix] = make_float4(ks.x, ks.y, ks.z, kn);
-        kcomp[pix] = make_float4(kc.x, kc.y, kc.z, 0.0f);
+        for (uint32_t j = 0; j < it.k; ++j) add_sample_kahan(ks, kc, kn, r[j]);
+        J.ksum[pix] = make_float4(ks.x, ks.y, ks.z, kn);
+        J.kcomp[pix] = make_float4(kc.x, kc.y, kc.z, 0.0f);
     } else {
-        const float4 s4 = fsum[pix];
+        const float4 s4 = J.fsum[pix];
         f3 s{s4.x, s4.y, s4.z};
-        for (uint32_t j = 0; j < k; ++j) {
-            const float4 c = rad[(size_t)lp * k + j];
-            s = s + f3{c.x, c.y, c.z};
-        }
-        fsum[pix] = make_float4(s.x, s.y, s.z, 0.0f);
+        for (uint32_t j = 0; j < it.k; ++j) add_sample(s, r[j]);
+        J.fsum[pix] = make_float4(s.x, s.y, s.z, 0.0f);
     }
+}
+
+// The reference's structure (pathtrace.rgen:39-104): one thread per pixel
+// loops over its samples and their bounces, tracing each segment itself.
+// Same arithmetic as the wavefront stages, so the same image; used as the
+// plain kernel the wavefront and the batched path are measured against.
+template <int KIND>
+__global__ void __launch_bounds__(128) k_megakernel(const DevJob* __restrict__ job, DevStats* stats) {
+    const DevJob& J = *job;
+    const uint32_t npix = J.width * J.height;
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t segs = 0, fb_ef[2] = {0, 0};
+    TraceCounters cnt{0, 0, 0};
+    if (pix < npix) {
+        const TravScene ts = trav_scene(J.sc);
+        f3 s{0.0f, 0.0f, 0.0f}, ks{0.0f, 0.0f, 0.0f}, kc{0.0f, 0.0f, 0.0f};
+        float kn = 0.0f;
+        if (J.accum_mode == SOLRT_ACCUM_KAHAN) {
+            const float4 s4 = J.ksum[pix], c4 = J.kcomp[pix];
+            ks = f3{s4.x, s4.y, s4.z};
+            kc = f3{c4.x, c4.y, c4.z};
+            kn = s4.w;
+        }
+        uint32_t rng = 0;
+        for (uint32_t smp = 0; smp < J.spp; ++smp) {
+            rng = sample_seed(J, pix, smp, rng);
+            float4 o, d;
+            camera_ray(J, pix, rng, o, d);
+            f3 acc{1.0f, 1.0f, 1.0f};
+            uint32_t depth = 0;
+            for (;;) {
+                HitRec h;
+                if (KIND == SOLRT_BVH8_Q8) trace_bvh8<false>(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, fb_ef[1]);
+                else trace_bvh2_ray(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, fb_ef[1]);
+                ++segs;
+                float4 on, dn;
+                if (!shade_step(J, o, d, make_float4(h.t, __uint_as_float(h.prim), h.u, h.v), acc, rng, depth, on,
+                                dn, fb_ef[1]))
+                    break;
+                o = on;
+                d = dn;
+            }
+            const float4 c = make_float4(acc.x, acc.y, acc.z, 0.0f);
+            if (J.accum_mode == SOLRT_ACCUM_KAHAN) add_sample_kahan(ks, kc, kn, c);
+            else add_sample(s, c);
+        }
+        if (J.accum_mode == SOLRT_ACCUM_KAHAN) {
+            J.ksum[pix] = make_float4(ks.x, ks.y, ks.z, kn);
+            J.kcomp[pix] = make_float4(kc.x, kc.y, kc.z, 0.0f);
+        } else {
+            J.fsum[pix] = make_float4(s.x, s.y, s.z, 0.0f);
+        }
+    }
+    const uint32_t wsegs = __reduce_add_sync(0xffffffffu, segs);
+    const uint32_t wfb = __reduce_add_sync(0xffffffffu, cnt.fallbacks);
+    const uint32_t wef = __reduce_or_sync(0xffffffffu, fb_ef[1]);
+    const uint32_t wpaths = __reduce_add_sync(0xffffffffu, pix < npix ? J.spp : 0u);
+    if ((threadIdx.x & 31) == 0) {
+        if (wsegs) atomicAdd(&stats->segments, (unsigned long long)wsegs);
+        if (wpaths) atomicAdd(&stats->paths, (unsigned long long)wpaths);
+        if (wfb) atomicAdd(&stats->fp64_fallbacks, (unsigned long long)wfb);
+        if (wef) atomicOr(&stats->eflags, wef);
+    }
+}
+
+// Zeroes the per-frame sample sums of running-mix jobs.
+__global__ void k_begin(const DevJob* __restrict__ jobs, const uint32_t* __restrict__ job_pix, uint32_t njobs,
+                        uint32_t pixels) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= pixels) return;
+    const uint32_t j = find_last_le(njobs, t, [&](uint32_t i) { return job_pix[i]; });
+    const DevJob& J = jobs[j];
+    if (J.accum_mode != SOLRT_ACCUM_KAHAN) J.fsum[t - job_pix[j]] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
 __device__ __forceinline__ unsigned char to_unorm8(float c) {
@@ -227,30 +227,32 @@ __device__ __forceinline__ unsigned char to_unorm8(float c) {
     return (unsigned char)(cl * 255.0f + 0.5f);
 }
 
-// rgen:88-103 (REF_MIX) or the Kahan mean.
-__global__ void k_finalize(uint32_t npix, uint32_t spp, uint32_t frame, uint32_t start, uint32_t accum_mode,
-                           const float4* __restrict__ fsum, const float4* __restrict__ ksum,
-                           float4* __restrict__ accum, uchar4* __restrict__ rgba8) {
-    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pix >= npix) return;
-    const float4 a = accum[pix];
+// rgen:88-103 (REF_MIX) or the Kahan mean, for every pixel of every job.
+__global__ void k_finalize(const DevJob* __restrict__ jobs, const uint32_t* __restrict__ job_pix, uint32_t njobs,
+                           uint32_t pixels) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= pixels) return;
+    const uint32_t j = find_last_le(njobs, t, [&](uint32_t i) { return job_pix[i]; });
+    const DevJob& J = jobs[j];
+    const uint32_t pix = t - job_pix[j];
+    const float4 a = J.accum[pix];
     const f3 old{a.x, a.y, a.z};
     f3 out;
-    if (accum_mode == SOLRT_ACCUM_KAHAN) {
-        const float4 s = ksum[pix];
+    if (J.accum_mode == SOLRT_ACCUM_KAHAN) {
+        const float4 s = J.ksum[pix];
         out = s.w > 0.0f ? f3{s.x / s.w, s.y / s.w, s.z / s.w} : old;
     } else {
-        const float4 s = fsum[pix];
-        const float inv = 1.0f / __uint2float_rn(spp);
+        const float4 s = J.fsum[pix];
+        const float inv = 1.0f / __uint2float_rn(J.spp);
         const f3 mean = inv * f3{s.x, s.y, s.z};
-        const float alpha = 1.0f / __uint2float_rn(frame + 1u - start);
+        const float alpha = 1.0f / __uint2float_rn(J.frame + 1u - J.start);
         out = mix(old, mean, alpha);
         if (isnan(out.x) || isnan(out.y) || isnan(out.z)) out = old;
         if (isinf(out.x) || isinf(out.y) || isinf(out.z)) out = old;
     }
-    accum[pix] = make_float4(out.x, out.y, out.z, 1.0f);
+    J.accum[pix] = make_float4(out.x, out.y, out.z, 1.0f);
     const float g = 1.0f / 2.2f;
-    rgba8[pix] = make_uchar4(to_unorm8(powf(out.x, g)), to_unorm8(powf(out.y, g)), to_unorm8(powf(out.z, g)), 255);
+    J.rgba8[pix] = make_uchar4(to_unorm8(powf(out.x, g)), to_unorm8(powf(out.y, g)), to_unorm8(powf(out.z, g)), 255);
 }
 
 // Known-answer kernels for the unit functions.
@@ -291,89 +293,250 @@ __global__ void k_debug_unit(uint32_t op, uint32_t n, const uint32_t* a, const u
 
 inline uint32_t cdiv(uint64_t a, uint32_t b) { return (uint32_t)((a + b - 1) / b); }
 
+solrt_status check_params(const Context& ctx, const Scene& sc, const Image& img, const solrt_render_params& p) {
+    if (sc.ctx != &ctx || img.ctx != &ctx) { set_error("objects belong to another context"); return SOLRT_ERR_INVALID; }
+    if (p.width != img.width || p.height != img.height) { set_error("params size differs from the image"); return SOLRT_ERR_INVALID; }
+    if (p.spp < 1) { set_error("spp must be >= 1"); return SOLRT_ERR_INVALID; }
+    if (p.max_bounces > SOLRT_MAX_BOUNCES) { set_error("max_bounces > 1024"); return SOLRT_ERR_INVALID; }
+    if (p.accum_mode != img.accum_mode) { set_error("accum_mode differs from the image"); return SOLRT_ERR_INVALID; }
+    if (p.miss_mode > SOLRT_MISS_GRADIENT || p.material_mode > SOLRT_MATERIAL_LAMBERT || p.rng_mode > SOLRT_RNG_PER_SAMPLE) {
+        set_error("bad miss, material or rng mode");
+        return SOLRT_ERR_INVALID;
+    }
+    if (p.accum_mode != SOLRT_ACCUM_KAHAN && p.frame + 1u - p.accum_start_frame == 0u) {
+        set_error("frame + 1 - accum_start_frame is zero");
+        return SOLRT_ERR_INVALID;
+    }
+    if (!(p.tmax >= 0.0f)) { set_error("tmax must be >= 0"); return SOLRT_ERR_INVALID; }
+    if (p.kernel > SOLRT_KERNEL_MEGA) { set_error("unknown kernel"); return SOLRT_ERR_INVALID; }
+    return SOLRT_OK;
+}
+
+DevJob make_job(const Scene& sc, const Image& img, const solrt_camera& cam, const solrt_render_params& p) {
+    DevJob J{};
+    J.sc = sc.view();
+    std::copy(cam.view_inverse, cam.view_inverse + 16, J.vinv);
+    std::copy(cam.projection_inverse, cam.projection_inverse + 16, J.pinv);
+    J.width = p.width;
+    J.height = p.height;
+    J.spp = p.spp;
+    J.frame = p.frame;
+    J.start = p.accum_start_frame;
+    J.seed = p.seed;
+    J.job_id = p.job_id;
+    J.rng_mode = p.rng_mode;
+    J.miss_mode = p.miss_mode;
+    J.material_mode = p.material_mode;
+    J.max_bounces = p.max_bounces;
+    J.accum_mode = p.accum_mode;
+    J.tmax = p.tmax > 0.0f ? p.tmax : 10000.0f;
+    J.accum = img.accum.as<float4>();
+    J.rgba8 = img.rgba8.as<uchar4>();
+    J.fsum = img.frame_sum.as<float4>();
+    J.ksum = img.ksum.as<float4>();
+    J.kcomp = img.kcomp.as<float4>();
+    J.rng_state = img.rng_state.as<uint32_t>();
+    return J;
+}
+
+// Issues the batch's launches on the context stream.
+solrt_status batch_issue(Batch& b, bool record_timing) {
+    Context& ctx = *b.ctx;
+    cudaStream_t st = ctx.stream;
+    const DevJob* dj = b.d_jobs.as<DevJob>();
+    const DevItem* di = b.d_items.as<DevItem>();
+    const uint32_t* jp = b.d_job_pix.as<uint32_t>();
+    DevStats* stats = ctx.stats.as<DevStats>();
+    PassCtl* ctl = ctx.ctl.as<PassCtl>();
+    const uint32_t njobs = (uint32_t)b.jobs.size();
+    const uint32_t total_pix = b.job_pix_base[njobs];
+    const int shade_grid = ctx.sm_count * 8;
+    k_begin<<<cdiv(total_pix, 256), 256, 0, st>>>(dj, jp, njobs, total_pix);
+    ++ctx.launches;
+    for (const PassPlan& pp : b.passes) {
+        const size_t ctl_bytes = sizeof(unsigned int) * (pp.bounces + 1);
+        SOLRT_CUDA(cudaMemsetAsync(ctl->count, 0, ctl_bytes, st));
+        SOLRT_CUDA(cudaMemsetAsync(ctl->work, 0, ctl_bytes, st));
+        const DevItem* items = di + pp.item_begin;
+        k_generate<<<cdiv(pp.paths, 256), 256, 0, st>>>(dj, items, pp.item_count, pp.paths, ctx.queue(0), ctl->count,
+                                                        stats);
+        ++ctx.launches;
+        for (uint32_t bnc = 0; bnc < pp.bounces; ++bnc) {
+            const PathQueue qin = ctx.queue(bnc & 1), qout = ctx.queue((bnc + 1) & 1);
+            const int te = record_timing ? ctx.timing_begin(0) : -1;
+            SOLRT_TRY(launch_extend(ctx, b.kind, dj, qin, ctx.hits.as<float4>(), ctl->count + bnc, ctl->work + bnc));
+            ctx.timing_end(te);
+            const int ts = record_timing ? ctx.timing_begin(1) : -1;
+            k_shade<<<shade_grid, 256, 0, st>>>(dj, items, pp.item_count, qin, ctx.hits.as<float4>(), ctl->count + bnc,
+                                                qout, ctl->count + bnc + 1, ctx.capacity, ctx.rad.as<float4>(), stats);
+            ctx.timing_end(ts);
+            ++ctx.launches;
+        }
+        k_accumulate<<<cdiv(pp.pixels, 256), 256, 0, st>>>(dj, items, pp.item_count, pp.pixels, ctx.rad.as<float4>());
+        ++ctx.launches;
+    }
+    k_finalize<<<cdiv(total_pix, 256), 256, 0, st>>>(dj, jp, njobs, total_pix);
+    ++ctx.launches;
+    SOLRT_CUDA(cudaGetLastError());
+    return SOLRT_OK;
+}
+
 }  // namespace
+
+// Plans passes for `jobs` and uploads the job table and the work items.
+solrt_status batch_plan(Context& ctx, const solrt_job* jobs, uint32_t n, uint32_t flags, Batch& b) {
+    if (n == 0 || !jobs) { set_error("empty batch"); return SOLRT_ERR_INVALID; }
+    if (n > (1u << (32 - kDepthBits))) { set_error("too many jobs in one batch"); return SOLRT_ERR_CAPACITY; }
+    b.ctx = &ctx;
+    b.flags = flags;
+    b.jobs.clear();
+    b.items.clear();
+    b.passes.clear();
+    b.job_pix_base.assign(1, 0u);
+    const uint32_t cap = ctx.capacity;
+    for (uint32_t j = 0; j < n; ++j) {
+        const solrt_job& jb = jobs[j];
+        if (!jb.scene || !jb.image) { set_error("job %u: null scene or image", j); return SOLRT_ERR_INVALID; }
+        const Scene& sc = *static_cast<const Scene*>(reinterpret_cast<const void*>(jb.scene));
+        const Image& img = *static_cast<const Image*>(reinterpret_cast<const void*>(jb.image));
+        SOLRT_TRY(check_params(ctx, sc, img, jb.params));
+        if (jb.params.kernel != SOLRT_KERNEL_WAVEFRONT) { set_error("job %u: batches run the wavefront kernel", j); return SOLRT_ERR_INVALID; }
+        if (j == 0) b.kind = sc.info.kind;
+        if (sc.info.kind != b.kind) { set_error("job %u: all scenes of a batch need the same BVH kind", j); return SOLRT_ERR_INVALID; }
+        b.jobs.push_back(make_job(sc, img, jb.camera, jb.params));
+        const uint64_t np = (uint64_t)jb.params.width * jb.params.height;
+        if (b.job_pix_base.back() + np >= (1ull << 31)) { set_error("batch has too many pixels"); return SOLRT_ERR_CAPACITY; }
+        b.job_pix_base.push_back(b.job_pix_base.back() + (uint32_t)np);
+    }
+    // work items, round-robin over jobs so that passes mix jobs
+    struct Chunk { uint32_t job, pix0, npix, k, spp; };
+    std::vector<Chunk> chunks;
+    for (uint32_t j = 0; j < n; ++j) {
+        const DevJob& J = b.jobs[j];
+        const uint32_t np = J.width * J.height;
+        const uint32_t k = J.rng_mode == SOLRT_RNG_REF_STREAM ? 1u : std::max(1u, std::min(J.spp, cap / std::max(np, 1u)));
+        for (uint32_t p0 = 0; p0 < np; p0 += cap) chunks.push_back(Chunk{j, p0, std::min(cap, np - p0), k, J.spp});
+    }
+    std::vector<DevItem> order;
+    for (uint32_t round = 0;; ++round) {
+        bool any = false;
+        for (const Chunk& c : chunks) {
+            const uint64_t s0 = (uint64_t)round * c.k;
+            if (s0 >= c.spp) continue;
+            any = true;
+            order.push_back(DevItem{c.job, c.pix0, c.npix, (uint32_t)s0, std::min(c.k, c.spp - (uint32_t)s0), 0, 0, 0});
+        }
+        if (!any) break;
+    }
+    PassPlan cur{0, 0, 0, 0, 0};
+    auto close_pass = [&]() {
+        if (cur.item_count) b.passes.push_back(cur);
+        cur = PassPlan{(uint32_t)b.items.size(), 0, 0, 0, 0};
+    };
+    for (const DevItem& it0 : order) {
+        const uint64_t paths = (uint64_t)it0.npix * it0.k;
+        bool conflict = false;
+        for (uint32_t t = cur.item_begin; t < cur.item_begin + cur.item_count; ++t)
+            if (b.items[t].job == it0.job && b.items[t].pix0 == it0.pix0) conflict = true;
+        if (conflict || cur.paths + paths > cap) close_pass();
+        DevItem it = it0;
+        it.path_base = cur.paths;
+        it.pix_base = cur.pixels;
+        b.items.push_back(it);
+        cur.item_count += 1;
+        cur.paths += (uint32_t)paths;
+        cur.pixels += it.npix;
+        cur.bounces = std::max(cur.bounces, b.jobs[it.job].max_bounces + 1u);
+        b.total_paths += paths;
+    }
+    close_pass();
+    SOLRT_TRY(b.d_jobs.alloc(sizeof(DevJob) * b.jobs.size()));
+    SOLRT_TRY(b.d_items.alloc(sizeof(DevItem) * b.items.size()));
+    SOLRT_TRY(b.d_job_pix.alloc(sizeof(uint32_t) * b.job_pix_base.size()));
+    cudaStream_t st = ctx.stream;
+    SOLRT_CUDA(cudaMemcpyAsync(b.d_jobs.ptr, b.jobs.data(), sizeof(DevJob) * b.jobs.size(), cudaMemcpyHostToDevice, st));
+    SOLRT_CUDA(cudaMemcpyAsync(b.d_items.ptr, b.items.data(), sizeof(DevItem) * b.items.size(), cudaMemcpyHostToDevice, st));
+    SOLRT_CUDA(cudaMemcpyAsync(b.d_job_pix.ptr, b.job_pix_base.data(), sizeof(uint32_t) * b.job_pix_base.size(),
+                               cudaMemcpyHostToDevice, st));
+    return SOLRT_OK;
+}
+
+// Replaces cameras / frames / seeds (the plan's structure must not change).
+solrt_status batch_set_jobs(Batch& b, const solrt_job* jobs) {
+    for (size_t j = 0; j < b.jobs.size(); ++j) {
+        const solrt_job& jb = jobs[j];
+        const Scene& sc = *static_cast<const Scene*>(reinterpret_cast<const void*>(jb.scene));
+        const Image& img = *static_cast<const Image*>(reinterpret_cast<const void*>(jb.image));
+        SOLRT_TRY(check_params(*b.ctx, sc, img, jb.params));
+        const DevJob nj = make_job(sc, img, jb.camera, jb.params);
+        const DevJob& oj = b.jobs[j];
+        if (nj.width != oj.width || nj.height != oj.height || nj.spp != oj.spp || nj.max_bounces != oj.max_bounces ||
+            nj.rng_mode != oj.rng_mode || nj.accum_mode != oj.accum_mode || sc.info.kind != b.kind) {
+            set_error("job %zu changed size, spp, bounces or modes: plan a new batch", j);
+            return SOLRT_ERR_INVALID;
+        }
+        b.jobs[j] = nj;
+    }
+    SOLRT_CUDA(cudaMemcpyAsync(b.d_jobs.ptr, b.jobs.data(), sizeof(DevJob) * b.jobs.size(), cudaMemcpyHostToDevice,
+                               b.ctx->stream));
+    return SOLRT_OK;
+}
+
+solrt_status batch_launch(Batch& b) {
+    Context& ctx = *b.ctx;
+    cudaGetLastError();  // launch errors below must be this call's own
+    if (!(b.flags & SOLRT_BATCH_GRAPH)) {
+        SOLRT_CUDA(cudaEventRecord(ctx.ev0, ctx.stream));
+        SOLRT_TRY(batch_issue(b, true));
+        SOLRT_CUDA(cudaEventRecord(ctx.ev1, ctx.stream));
+        return SOLRT_OK;
+    }
+    if (!b.exec) {
+        const uint64_t launches0 = ctx.launches;
+        SOLRT_CUDA(cudaStreamBeginCapture(ctx.stream, cudaStreamCaptureModeThreadLocal));
+        const solrt_status s = batch_issue(b, false);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(ctx.stream, &g);
+        if (s != SOLRT_OK) {
+            if (g) cudaGraphDestroy(g);
+            return s;
+        }
+        SOLRT_CUDA(e);
+        b.graph = g;
+        SOLRT_CUDA(cudaGraphInstantiate(&b.exec, b.graph, 0));
+        b.graph_launches = ctx.launches - launches0;
+        ctx.launches = launches0;
+    }
+    SOLRT_CUDA(cudaEventRecord(ctx.ev0, ctx.stream));
+    SOLRT_CUDA(cudaGraphLaunch(b.exec, ctx.stream));
+    SOLRT_CUDA(cudaEventRecord(ctx.ev1, ctx.stream));
+    ctx.launches += b.graph_launches;
+    return SOLRT_OK;
+}
 
 solrt_status render_frame(Context& ctx, const Scene& sc, const solrt_camera& cam, const solrt_render_params& p,
                           Image& img) {
-    cudaStream_t st = ctx.stream;
+    solrt_job jb;
+    jb.scene = reinterpret_cast<solrt_scene*>(const_cast<Scene*>(&sc));
+    jb.image = reinterpret_cast<solrt_image*>(&img);
+    jb.camera = cam;
+    jb.params = p;
+    jb.params.kernel = SOLRT_KERNEL_WAVEFRONT;
+    SOLRT_TRY(batch_plan(ctx, &jb, 1, 0, ctx.single));
+    if (p.kernel != SOLRT_KERNEL_MEGA) return batch_launch(ctx.single);
+    // per-pixel megakernel + the shared finalize
+    Batch& b = ctx.single;
+    cudaGetLastError();
     const uint32_t npix = p.width * p.height;
-    const bool ref_stream = p.rng_mode == SOLRT_RNG_REF_STREAM;
-    const uint32_t cap = ctx.capacity;
-    uint32_t k, chunk;
-    if (ref_stream) {
-        k = 1;
-        chunk = std::min(npix, cap);
-    } else if (npix <= cap) {
-        k = std::max(1u, std::min(p.spp, cap / npix));
-        chunk = npix;
-    } else {
-        k = 1;
-        chunk = cap;
-    }
-    GenParams g;
-    std::copy(cam.view_inverse, cam.view_inverse + 16, g.vinv);
-    std::copy(cam.projection_inverse, cam.projection_inverse + 16, g.pinv);
-    g.width = p.width;
-    g.height = p.height;
-    g.spp = p.spp;
-    g.frame = p.frame;
-    g.seed = p.seed;
-    g.job_id = p.job_id;
-    g.rng_mode = p.rng_mode;
-    g.tmax = p.tmax > 0.0f ? p.tmax : 10000.0f;
-    ShadeParams sp;
-    sp.max_bounces = p.max_bounces;
-    sp.miss_mode = p.miss_mode;
-    sp.material_mode = p.material_mode;
-    sp.rng_mode = p.rng_mode;
-    sp.capacity = cap;
-    const DevScene dsc = sc.view();
-    DevStats* stats = ctx.stats.as<DevStats>();
-    PassCtl* ctl = ctx.ctl.as<PassCtl>();
-    const size_t ctl_bytes = sizeof(unsigned int) * (p.max_bounces + 2);
-    const int shade_grid = ctx.sm_count * 8;
-
-    SOLRT_CUDA(cudaEventRecord(ctx.ev0, st));
-    if (p.accum_mode != SOLRT_ACCUM_KAHAN) SOLRT_CUDA(cudaMemsetAsync(img.frame_sum.ptr, 0, img.frame_sum.bytes, st));
-    for (uint32_t s0 = 0; s0 < p.spp; s0 += k) {
-        const uint32_t kk = std::min(k, p.spp - s0);
-        for (uint32_t pix0 = 0; pix0 < npix; pix0 += chunk) {
-            const uint32_t np = std::min(chunk, npix - pix0);
-            SOLRT_CUDA(cudaMemsetAsync(ctl->count, 0, ctl_bytes, st));
-            SOLRT_CUDA(cudaMemsetAsync(ctl->work, 0, ctl_bytes, st));
-            g.pix0 = pix0;
-            g.npix = np;
-            g.s0 = s0;
-            g.k = kk;
-            sp.pix0 = pix0;
-            sp.k = kk;
-            k_generate<<<cdiv((uint64_t)np * kk, 256), 256, 0, st>>>(g, ctx.queue(0), ctl->count,
-                                                                    img.rng_state.as<uint32_t>(), stats);
-            ++ctx.launches;
-            for (uint32_t b = 0; b <= p.max_bounces; ++b) {
-                const PathQueue qin = ctx.queue(b & 1), qout = ctx.queue((b + 1) & 1);
-                const int te = ctx.timing_begin(0);
-                SOLRT_TRY(launch_extend(ctx, sc, qin, ctx.hits.as<float4>(), ctl->count + b, ctl->work + b, cap));
-                ctx.timing_end(te);
-                const int ts = ctx.timing_begin(1);
-                k_shade<<<shade_grid, 256, 0, st>>>(dsc, sp, qin, ctx.hits.as<float4>(), ctl->count + b, qout,
-                                                    ctl->count + b + 1, ctx.rad.as<float4>(),
-                                                    img.rng_state.as<uint32_t>(), stats);
-                ctx.timing_end(ts);
-                ++ctx.launches;
-            }
-            k_accumulate<<<cdiv(np, 256), 256, 0, st>>>(ctx.rad.as<float4>(), pix0, np, kk, p.accum_mode,
-                                                        img.frame_sum.as<float4>(), img.ksum.as<float4>(),
-                                                        img.kcomp.as<float4>());
-            ++ctx.launches;
-        }
-    }
-    k_finalize<<<cdiv(npix, 256), 256, 0, st>>>(npix, p.spp, p.frame, p.accum_start_frame, p.accum_mode,
-                                                img.frame_sum.as<float4>(), img.ksum.as<float4>(),
-                                                img.accum.as<float4>(), img.rgba8.as<uchar4>());
-    ++ctx.launches;
+    SOLRT_CUDA(cudaEventRecord(ctx.ev0, ctx.stream));
+    if (b.kind == SOLRT_BVH8_Q8)
+        k_megakernel<SOLRT_BVH8_Q8><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(b.d_jobs.as<DevJob>(), ctx.stats.as<DevStats>());
+    else
+        k_megakernel<SOLRT_BVH2><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(b.d_jobs.as<DevJob>(), ctx.stats.as<DevStats>());
+    k_finalize<<<cdiv(npix, 256), 256, 0, ctx.stream>>>(b.d_jobs.as<DevJob>(), b.d_job_pix.as<uint32_t>(), 1u, npix);
+    ctx.launches += 2;
     SOLRT_CUDA(cudaGetLastError());
-    SOLRT_CUDA(cudaEventRecord(ctx.ev1, st));
+    SOLRT_CUDA(cudaEventRecord(ctx.ev1, ctx.stream));
     return SOLRT_OK;
 }
 

@@ -31,27 +31,37 @@ SOLRT_D void flush_counters(DevStats* stats, const TraceCounters& cnt, uint32_t 
     }
 }
 
-// Wavefront queue: o_tmin / d_tmax SoA, hit = (t, prim bits, u, v).
+// Wavefront queue: o_tmin / d_tmax SoA, hit = (t, prim bits, u, v); the
+// scene of ray i is that of its job (meta[i].y >> kDepthBits).
 struct QueueIO {
     const float4* __restrict__ o_tmin;
     const float4* __restrict__ d_tmax;
+    const uint2* __restrict__ meta;
+    const DevJob* __restrict__ jobs;
     float4* __restrict__ hits;
-    SOLRT_D void load(uint32_t i, float4& o, float4& d) const {
+    SOLRT_D void load(uint32_t i, float4& o, float4& d, TravScene& ts) const {
         o = o_tmin[i];
         d = d_tmax[i];
+        const DevScene* s = &jobs[meta[i].y >> kDepthBits].sc;
+        ts.nodes = s->nodes;
+        ts.tris = s->tri_wt;
+        ts.node_count = s->node_count;
+        ts.tri_count = s->tri_count;
     }
     SOLRT_D void store(uint32_t i, const HitRec& h) const {
         hits[i] = make_float4(h.t, __uint_as_float(h.prim), h.u, h.v);
     }
 };
 
-// Ray-file API: AoS solrt_ray (2 float4) -> solrt_hit (float4).
+// Ray-file API: AoS solrt_ray (2 float4) -> solrt_hit (float4), one scene.
 struct RayFileIO {
     const float4* __restrict__ rays;
     float4* __restrict__ hits;
-    SOLRT_D void load(uint32_t i, float4& o, float4& d) const {
+    TravScene scene;
+    SOLRT_D void load(uint32_t i, float4& o, float4& d, TravScene& ts) const {
         o = rays[2 * (size_t)i];
         d = rays[2 * (size_t)i + 1];
+        ts = scene;
     }
     SOLRT_D void store(uint32_t i, const HitRec& h) const {
         hits[i] = make_float4(h.t, __uint_as_float(h.prim), h.u, h.v);
@@ -60,7 +70,7 @@ struct RayFileIO {
 
 // n = *count when count != nullptr (queue length on the device), else n_static.
 template <int KIND, class IO, bool kCount>
-__global__ void __launch_bounds__(kExtendBlock) k_extend(DevScene sc, IO io, const unsigned int* __restrict__ count,
+__global__ void __launch_bounds__(kExtendBlock) k_extend(IO io, const unsigned int* __restrict__ count,
                                                          uint32_t n_static, unsigned int* __restrict__ work,
                                                          DevStats* stats) {
     const uint32_t n = count ? *count : n_static;
@@ -68,7 +78,7 @@ __global__ void __launch_bounds__(kExtendBlock) k_extend(DevScene sc, IO io, con
     TraceCounters cnt{0, 0, 0};
     uint32_t ef = 0;
     if (KIND == SOLRT_BVH2) {
-        extend_bvh2_ww<IO, kCount>(sc, io, n, work, cnt, ef);
+        extend_bvh2_ww<IO, kCount>(io, n, work, cnt, ef);
     } else {
         const int lane = threadIdx.x & 31;
         for (;;) {
@@ -79,9 +89,10 @@ __global__ void __launch_bounds__(kExtendBlock) k_extend(DevScene sc, IO io, con
             const unsigned int i = base + lane;
             if (i < n) {
                 float4 o, d;
-                io.load(i, o, d);
+                TravScene ts;
+                io.load(i, o, d, ts);
                 HitRec h;
-                trace_bvh8<kCount>(sc, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, ef);
+                trace_bvh8<kCount>(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, ef);
                 io.store(i, h);
             }
         }
@@ -90,12 +101,12 @@ __global__ void __launch_bounds__(kExtendBlock) k_extend(DevScene sc, IO io, con
 }
 
 template <int KIND, class IO>
-void launch_kind(const Context& ctx, uint32_t grid, const DevScene& d, const IO& io, const unsigned int* count,
-                 uint32_t n_static, unsigned int* work, DevStats* st) {
+void launch_kind(const Context& ctx, uint32_t grid, const IO& io, const unsigned int* count, uint32_t n_static,
+                 unsigned int* work, DevStats* st) {
     if (ctx.counters)
-        k_extend<KIND, IO, true><<<grid, kExtendBlock, 0, ctx.stream>>>(d, io, count, n_static, work, st);
+        k_extend<KIND, IO, true><<<grid, kExtendBlock, 0, ctx.stream>>>(io, count, n_static, work, st);
     else
-        k_extend<KIND, IO, false><<<grid, kExtendBlock, 0, ctx.stream>>>(d, io, count, n_static, work, st);
+        k_extend<KIND, IO, false><<<grid, kExtendBlock, 0, ctx.stream>>>(io, count, n_static, work, st);
 }
 
 template <class IO>
@@ -114,14 +125,13 @@ int blocks_per_sm(uint32_t kind, bool counters) {
 
 int extend_blocks_per_sm(uint32_t kind, bool counters) { return blocks_per_sm<QueueIO>(kind, counters); }
 
-solrt_status launch_extend(Context& ctx, const Scene& sc, const PathQueue& q, float4* hits, const unsigned int* count,
-                           unsigned int* work, uint32_t /*capacity*/) {
-    const DevScene d = sc.view();
-    const uint32_t grid = (uint32_t)(ctx.sm_count * blocks_per_sm<QueueIO>(d.bvh_kind, ctx.counters));
-    const QueueIO io{q.o_tmin, q.d_tmax, hits};
+solrt_status launch_extend(Context& ctx, uint32_t kind, const DevJob* jobs, const PathQueue& q, float4* hits,
+                           const unsigned int* count, unsigned int* work) {
+    const uint32_t grid = (uint32_t)(ctx.sm_count * blocks_per_sm<QueueIO>(kind, ctx.counters));
+    const QueueIO io{q.o_tmin, q.d_tmax, q.meta, jobs, hits};
     DevStats* st = ctx.stats.as<DevStats>();
-    if (d.bvh_kind == SOLRT_BVH8_Q8) launch_kind<SOLRT_BVH8_Q8>(ctx, grid, d, io, count, 0, work, st);
-    else launch_kind<SOLRT_BVH2>(ctx, grid, d, io, count, 0, work, st);
+    if (kind == SOLRT_BVH8_Q8) launch_kind<SOLRT_BVH8_Q8>(ctx, grid, io, count, 0, work, st);
+    else launch_kind<SOLRT_BVH2>(ctx, grid, io, count, 0, work, st);
     ++ctx.launches;
     SOLRT_CUDA(cudaGetLastError());
     return SOLRT_OK;
@@ -134,12 +144,12 @@ solrt_status launch_trace_rays(Context& ctx, const Scene& sc, const solrt_ray* r
     const uint32_t want = (n + kExtendBlock - 1) / kExtendBlock;
     const uint32_t cap = (uint32_t)ctx.sm_count * per_sm;
     const uint32_t grid = want < cap ? want : cap;
-    const RayFileIO io{reinterpret_cast<const float4*>(rays), reinterpret_cast<float4*>(hits)};
+    const RayFileIO io{reinterpret_cast<const float4*>(rays), reinterpret_cast<float4*>(hits), trav_scene(d)};
     unsigned int* work = ctx.trace_work.as<unsigned int>();
     SOLRT_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned int), ctx.stream));
     DevStats* st = ctx.stats.as<DevStats>();
-    if (d.bvh_kind == SOLRT_BVH8_Q8) launch_kind<SOLRT_BVH8_Q8>(ctx, grid, d, io, nullptr, n, work, st);
-    else launch_kind<SOLRT_BVH2>(ctx, grid, d, io, nullptr, n, work, st);
+    if (d.bvh_kind == SOLRT_BVH8_Q8) launch_kind<SOLRT_BVH8_Q8>(ctx, grid, io, nullptr, n, work, st);
+    else launch_kind<SOLRT_BVH2>(ctx, grid, io, nullptr, n, work, st);
     ++ctx.launches;
     SOLRT_CUDA(cudaGetLastError());
     return SOLRT_OK;

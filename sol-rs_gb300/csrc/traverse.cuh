@@ -32,6 +32,17 @@ struct DevScene {
     const float4* tri_wt;     // 3 float4 per triangle in leaf order; p0.w = prim bits
 };
 
+// What the traversal needs of a scene (per ray: rays of one launch may belong
+// to different scenes).
+struct TravScene {
+    const float4* nodes;
+    const float4* tris;
+    uint32_t node_count;
+    uint32_t tri_count;
+};
+
+SOLRT_HD TravScene trav_scene(const DevScene& s) { return TravScene{s.nodes, s.tri_wt, s.node_count, s.tri_count}; }
+
 struct HitRec {
     float t;
     uint32_t prim;

@@ -1,0 +1,124 @@
+"""Batched rendering: jobs of different scenes, sizes, spp, bounce limits and
+modes share wavefront passes; every job's image must equal (bit for bit)
+the image of the same job rendered alone with solrt_render, with and
+without CUDA-graph replay, and with a tiny path capacity that forces many
+mixed passes. Alone-vs-mixed invariance is the serving property of the
+batched path."""
+import numpy as np
+import pytest
+
+from helpers import S, camera_of, empty_scene, single_triangle, transformed_cornell
+
+pytestmark = pytest.mark.gpu
+
+
+def _specs(solrt):
+    L, R = solrt.MATERIAL_LAMBERT, solrt.MATERIAL_REF
+    PS, RS = solrt.RNG_PER_SAMPLE, solrt.RNG_REF_STREAM
+    return [
+        (S.cornell(), 48, 40, dict(spp=3, max_bounces=5, material_mode=L, rng_mode=PS, seed=1, job_id=0)),
+        (S.cornell(light=(15, 15, 15)), 32, 32, dict(spp=2, max_bounces=32, material_mode=R, rng_mode=RS)),
+        (S.soup(20000, seed=2), 64, 36, dict(spp=5, max_bounces=4, material_mode=L, rng_mode=PS, seed=2, job_id=2,
+                                             miss_mode=solrt.MISS_GRADIENT)),
+        (S.tunnel(n_ang=128, n_ax=64, length=20.0), 40, 24, dict(spp=2, max_bounces=8, material_mode=L, rng_mode=PS,
+                                                                 seed=3, job_id=3, miss_mode=solrt.MISS_REF_SKY,
+                                                                 accum_mode=solrt.ACCUM_KAHAN)),
+        (transformed_cornell(), 24, 24, dict(spp=7, max_bounces=3, material_mode=R, rng_mode=PS, seed=5, job_id=4,
+                                             miss_mode=solrt.MISS_REF_SKY)),
+        (single_triangle(), 16, 16, dict(spp=1, max_bounces=2, material_mode=L, rng_mode=PS, seed=6, job_id=5)),
+        (empty_scene(), 8, 8, dict(spp=2, max_bounces=1, material_mode=L, rng_mode=PS, seed=7, job_id=6,
+                                   miss_mode=solrt.MISS_GRADIENT)),
+    ]
+
+
+def _make(solrt, ctx, bvh, frame=0):
+    out = []
+    for data, w, h, kw in _specs(solrt):
+        sc = solrt.SceneDescription(ctx, data, bvh=bvh)
+        img = solrt.Image(ctx, w, h, kw.get("accum_mode", solrt.ACCUM_REF_MIX))
+        out.append((sc, img, camera_of(data, w / h), solrt.render_params(w, h, frame=frame, **kw)))
+    return out
+
+
+def _alone(solrt, ctx, jobs, frames=1):
+    res = []
+    r = solrt.Renderer(ctx)
+    for sc, img, cam, p in jobs:
+        solo = solrt.Image(ctx, p.width, p.height, p.accum_mode)
+        for f in range(frames):
+            q = solrt.RenderParams.from_buffer_copy(p)
+            q.frame = f
+            r.cmd_trace_rays(sc, cam, q, solo)
+        ctx.synchronize()
+        res.append(solo.read())
+    return res
+
+
+@pytest.mark.parametrize("graph", [False, True])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh8"])
+def test_batch_equals_alone(solrt, ctx, bvh, graph):
+    kind = solrt.BVH2 if bvh == "bvh2" else solrt.BVH8_Q8
+    jobs = _make(solrt, ctx, kind)
+    batch = solrt.Batch(ctx, jobs, graph=graph)
+    ctx.reset_stats()
+    batch.launch()
+    ctx.synchronize()
+    assert ctx.stats().error_flags == 0
+    if graph:   # second frame through the same plan (graph replay)
+        upd = []
+        for sc, img, cam, p in jobs:
+            q = solrt.RenderParams.from_buffer_copy(p)
+            q.frame = 1
+            upd.append((sc, img, cam, q))
+        batch.update(upd)
+        batch.launch()
+        ctx.synchronize()
+    alone = _alone(solrt, ctx, jobs, frames=2 if graph else 1)
+    for (sc, img, cam, p), (a32, a8) in zip(jobs, alone):
+        b32, b8 = img.read()
+        assert np.array_equal(b32.view(np.uint32), a32.view(np.uint32))
+        assert np.array_equal(b8, a8)
+    batch.close()
+
+
+def test_batch_many_passes(solrt):
+    """Capacity of 2000 paths: every pass mixes partial jobs; images still
+    equal the unconstrained batch."""
+    big = solrt.Context(0)
+    small = solrt.Context(0, path_capacity=2000)
+    res = []
+    for c in (big, small):
+        jobs = _make(solrt, c, solrt.BVH2)
+        b = solrt.Batch(c, jobs)
+        b.launch()
+        c.synchronize()
+        info = b.info()
+        res.append(([img.read()[0] for _, img, _, _ in jobs], info))
+        b.close()
+    assert res[1][1]["passes"] > res[0][1]["passes"] >= 1
+    for x, y in zip(res[0][0], res[1][0]):
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+    big.close()
+    small.close()
+
+
+def test_batch_matches_oracle(solrt, oracle, ctx):
+    jobs = _make(solrt, ctx, solrt.BVH2)
+    b = solrt.Batch(ctx, jobs)
+    b.launch()
+    ctx.synchronize()
+    for (data, w, h, kw), (sc, img, cam, p) in list(zip(_specs(solrt), jobs))[:3]:
+        want, _, _ = oracle.OracleScene(data).render(cam, p)
+        got, _ = img.read()
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_batch_rejects_mixed_bvh_kinds(solrt, ctx):
+    d = S.cornell()
+    a = solrt.SceneDescription(ctx, d, bvh=solrt.BVH2)
+    b = solrt.SceneDescription(ctx, d, bvh=solrt.BVH8_Q8)
+    ia, ib = solrt.Image(ctx, 8, 8), solrt.Image(ctx, 8, 8)
+    cam = camera_of(d, 1.0)
+    p = solrt.render_params(8, 8)
+    with pytest.raises(solrt.SolrtError):
+        solrt.Batch(ctx, [(a, ia, cam, p), (b, ib, cam, p)])

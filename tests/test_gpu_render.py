@@ -93,6 +93,19 @@ def test_render_bit_exact(solrt, oracle, ctx, name, bvh):
     assert np.isfinite(ga).all() and ga[..., :3].mean() > 0
 
 
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh8"])
+@pytest.mark.parametrize("name", ["cornell_lambert", "cornell_ref_stream", "soup_gradient", "tunnel_kahan"])
+def test_megakernel_equals_wavefront(solrt, oracle, ctx, name, bvh):
+    """The per-pixel megakernel (the reference's loop structure) renders the
+    same image as the wavefront and as the oracle."""
+    data, w, h, kw = _case(name)
+    kind = solrt.BVH2 if bvh == "bvh2" else solrt.BVH8_Q8
+    ga, g8, oa, o8, stats, seg_o = _render_both(solrt, oracle, ctx, data, w, h, dict(kw, kernel=solrt.api.KERNEL_MEGA),
+                                                bvh=kind)
+    assert np.array_equal(ga.view(np.uint32), oa.view(np.uint32))
+    assert stats.segments == seg_o and stats.error_flags == 0
+
+
 def test_pass_splitting_invariance(solrt, oracle):
     """A tiny path capacity forces many passes and pixel chunks; the image
     must not change."""
