@@ -358,6 +358,56 @@ solrt_status solrt_batch_destroy(solrt_batch* batch);
 /* Passes, work items and bounce launches of the plan. */
 solrt_status solrt_batch_info(solrt_batch* batch, uint32_t* passes, uint32_t* items, uint64_t* paths);
 
+/* ------------------------------------------------------------------------ */
+/* Serving: continuous batching of render jobs                              */
+/* ------------------------------------------------------------------------ */
+
+typedef struct solrt_server_desc {
+    uint64_t memory_budget;   /* bytes of job images + scenes in use; 0 = 150 GB */
+    uint32_t tick_paths;      /* paths per tick; 0 = the context's path capacity */
+    uint32_t reserved[5];
+} solrt_server_desc;
+
+typedef struct solrt_job_result {
+    uint32_t status;          /* SOLRT_OK when done, SOLRT_ERR_NOT_READY before */
+    uint32_t spp_done;
+    uint64_t latency_ns;      /* submit -> last sample accumulated and image final */
+    uint64_t queue_ns;        /* submit -> admitted */
+    solrt_image* image;       /* owned by the server until released or evicted */
+} solrt_job_result;
+
+typedef struct solrt_server_stats {
+    uint64_t submitted, admitted, completed, evicted;
+    uint64_t ticks;
+    uint64_t segments;
+    uint32_t queue_depth;     /* submitted, not yet admitted */
+    uint32_t active;          /* admitted, not yet complete */
+    uint64_t bytes_in_use;
+    double busy_ms;           /* device time of all ticks */
+} solrt_server_stats;
+
+/* A serving thread owns the context's stream until solrt_server_destroy.
+ * Each tick it admits waiting jobs in arrival order while their image (and
+ * scene, when not already counted) fits the memory budget, evicting the
+ * least recently completed unreleased results first; then it runs one
+ * wavefront pass in which every active job advances by its share of
+ * tick_paths (at least one sample), and finalizes the jobs that reached
+ * their spp. A job's image equals solrt_render of the same job alone. */
+solrt_status solrt_server_create(solrt_context* ctx, const solrt_server_desc* desc, solrt_server** out);
+/* Queues a job: the server allocates its image (params.width x height). */
+solrt_status solrt_server_submit(solrt_server* srv, solrt_scene* scene, const solrt_camera* camera,
+                                 const solrt_render_params* params, uint64_t* ticket);
+/* SOLRT_OK with the result when done; SOLRT_ERR_NOT_READY while queued or
+ * running; SOLRT_ERR_NOT_FOUND for an unknown, released or evicted ticket. */
+solrt_status solrt_server_poll(solrt_server* srv, uint64_t ticket, solrt_job_result* out);
+/* Waits up to timeout_ms for the ticket (bounded wait). */
+solrt_status solrt_server_wait(solrt_server* srv, uint64_t ticket, uint32_t timeout_ms, solrt_job_result* out);
+/* Frees a completed job's image. */
+solrt_status solrt_server_release(solrt_server* srv, uint64_t ticket);
+solrt_status solrt_server_get_stats(solrt_server* srv, solrt_server_stats* out);
+/* Stops the serving thread (unfinished jobs are dropped) and frees images. */
+solrt_status solrt_server_destroy(solrt_server* srv);
+
 /* Closest-hit queries (one traceRayEXT each, opaque, no culling).
  * Host arrays; synchronises. */
 solrt_status solrt_trace_rays(solrt_context* ctx, solrt_scene* scene, const solrt_ray* rays,

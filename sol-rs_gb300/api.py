@@ -95,6 +95,23 @@ class Job(ctypes.Structure):
 BATCH_GRAPH = 1
 
 
+class ServerDesc(ctypes.Structure):
+    _fields_ = [("memory_budget", ctypes.c_uint64), ("tick_paths", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32 * 5)]
+
+
+class JobResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_uint32), ("spp_done", ctypes.c_uint32), ("latency_ns", ctypes.c_uint64),
+                ("queue_ns", ctypes.c_uint64), ("image", ctypes.c_void_p)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("admitted", ctypes.c_uint64), ("completed", ctypes.c_uint64),
+                ("evicted", ctypes.c_uint64), ("ticks", ctypes.c_uint64), ("segments", ctypes.c_uint64),
+                ("queue_depth", ctypes.c_uint32), ("active", ctypes.c_uint32), ("bytes_in_use", ctypes.c_uint64),
+                ("busy_ms", ctypes.c_double)]
+
+
 class Stats(ctypes.Structure):
     _fields_ = [("segments", ctypes.c_uint64), ("paths", ctypes.c_uint64), ("node_visits", ctypes.c_uint64),
                 ("tri_tests", ctypes.c_uint64), ("fp64_fallbacks", ctypes.c_uint64), ("launches", ctypes.c_uint64),
@@ -147,6 +164,14 @@ _PROTOS = {
     "solrt_batch_destroy": (ctypes.c_int, [_P]),
     "solrt_batch_info": (ctypes.c_int, [_P, ctypes.POINTER(_U32), ctypes.POINTER(_U32),
                                         ctypes.POINTER(ctypes.c_uint64)]),
+    "solrt_server_create": (ctypes.c_int, [_P, ctypes.POINTER(ServerDesc), ctypes.POINTER(_P)]),
+    "solrt_server_submit": (ctypes.c_int, [_P, _P, ctypes.POINTER(Camera), ctypes.POINTER(RenderParams),
+                                           ctypes.POINTER(ctypes.c_uint64)]),
+    "solrt_server_poll": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.POINTER(JobResult)]),
+    "solrt_server_wait": (ctypes.c_int, [_P, ctypes.c_uint64, _U32, ctypes.POINTER(JobResult)]),
+    "solrt_server_release": (ctypes.c_int, [_P, ctypes.c_uint64]),
+    "solrt_server_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(ServerStats)]),
+    "solrt_server_destroy": (ctypes.c_int, [_P]),
     "solrt_trace_rays": (ctypes.c_int, [_P, _P, _P, _U32, _P]),
     "solrt_trace_rays_device": (ctypes.c_int, [_P, _P, _P, _U32, _P]),
     "solrt_debug_unit": (ctypes.c_int, [_P, _U32, _U32, _P, _P, _P, _P, _P]),
@@ -401,6 +426,59 @@ class Batch:
         p, i, n = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint64()
         check(lib().solrt_batch_info(self.handle, ctypes.byref(p), ctypes.byref(i), ctypes.byref(n)))
         return dict(passes=p.value, items=i.value, paths=n.value)
+
+
+class Server:
+    """Continuous-batching render server (solrt_server): a serving thread
+    admits jobs by memory budget and advances all active jobs each tick."""
+
+    def __init__(self, context, memory_budget=0, tick_paths=0):
+        self.context = context
+        h = ctypes.c_void_p()
+        check(lib().solrt_server_create(context.handle, ctypes.byref(ServerDesc(memory_budget, tick_paths)),
+                                        ctypes.byref(h)))
+        self.handle = h
+        self._scenes = {}
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().solrt_server_destroy(self.handle)
+            self.handle = None
+
+    __del__ = close
+
+    def submit(self, scene, camera, params):
+        t = ctypes.c_uint64()
+        check(lib().solrt_server_submit(self.handle, scene.handle, ctypes.byref(camera), ctypes.byref(params),
+                                        ctypes.byref(t)))
+        self._scenes[t.value] = (scene, params.width, params.height)
+        return t.value
+
+    def poll(self, ticket):
+        r = JobResult()
+        s = lib().solrt_server_poll(self.handle, ticket, ctypes.byref(r))
+        return s, r
+
+    def wait(self, ticket, timeout_ms=60000):
+        r = JobResult()
+        check(lib().solrt_server_wait(self.handle, ticket, timeout_ms, ctypes.byref(r)))
+        return r
+
+    def read(self, ticket, result):
+        _, w, h = self._scenes[ticket]
+        a = np.zeros((h, w, 4), np.float32)
+        b = np.zeros((h, w, 4), np.uint8)
+        check(lib().solrt_image_read(ctypes.c_void_p(result.image), _ptr(a), _ptr(b)))
+        return a, b
+
+    def release(self, ticket):
+        self._scenes.pop(ticket, None)
+        return lib().solrt_server_release(self.handle, ticket)
+
+    def stats(self):
+        s = ServerStats()
+        check(lib().solrt_server_get_stats(self.handle, ctypes.byref(s)))
+        return s
 
 
 class Renderer:

@@ -251,6 +251,13 @@ solrt_status batch_set_jobs(Batch& b, const solrt_job* jobs);
 solrt_status batch_launch(Batch& b);
 solrt_status render_frame(Context& ctx, const Scene& sc, const solrt_camera& cam, const solrt_render_params& p,
                           Image& img);
+struct TickBuffers {
+    DeviceBuffer jobs, items, fin_jobs, fin_pix;
+};
+solrt_status serve_tick(Context& ctx, TickBuffers& tb, uint32_t kind, const std::vector<DevJob>& jobs,
+                        const std::vector<DevItem>& items, const PassPlan& pp, const std::vector<DevJob>& fin);
+DevJob job_for(const Scene& sc, const Image& img, const solrt_camera& cam, const solrt_render_params& p);
+solrt_status check_job(const Context& ctx, const Scene& sc, const Image& img, const solrt_render_params& p);
 solrt_status debug_unit(Context& ctx, uint32_t op, uint32_t n, const uint32_t* a, const uint32_t* b,
                         const float* in_f32, uint32_t* out_u32, float* out_f32);
 

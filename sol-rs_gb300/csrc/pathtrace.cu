@@ -339,6 +339,35 @@ DevJob make_job(const Scene& sc, const Image& img, const solrt_camera& cam, cons
     return J;
 }
 
+// One pass: generate, (extend, shade) x bounces, accumulate.
+solrt_status issue_pass(Context& ctx, uint32_t kind, const DevJob* dj, const DevItem* items, const PassPlan& pp,
+                        bool record_timing) {
+    cudaStream_t st = ctx.stream;
+    DevStats* stats = ctx.stats.as<DevStats>();
+    PassCtl* ctl = ctx.ctl.as<PassCtl>();
+    const size_t ctl_bytes = sizeof(unsigned int) * (pp.bounces + 1);
+    SOLRT_CUDA(cudaMemsetAsync(ctl->count, 0, ctl_bytes, st));
+    SOLRT_CUDA(cudaMemsetAsync(ctl->work, 0, ctl_bytes, st));
+    k_generate<<<cdiv(pp.paths, 256), 256, 0, st>>>(dj, items, pp.item_count, pp.paths, ctx.queue(0), ctl->count,
+                                                    stats);
+    ++ctx.launches;
+    const int shade_grid = ctx.sm_count * 8;
+    for (uint32_t bnc = 0; bnc < pp.bounces; ++bnc) {
+        const PathQueue qin = ctx.queue(bnc & 1), qout = ctx.queue((bnc + 1) & 1);
+        const int te = record_timing ? ctx.timing_begin(0) : -1;
+        SOLRT_TRY(launch_extend(ctx, kind, dj, qin, ctx.hits.as<float4>(), ctl->count + bnc, ctl->work + bnc));
+        ctx.timing_end(te);
+        const int ts = record_timing ? ctx.timing_begin(1) : -1;
+        k_shade<<<shade_grid, 256, 0, st>>>(dj, items, pp.item_count, qin, ctx.hits.as<float4>(), ctl->count + bnc,
+                                            qout, ctl->count + bnc + 1, ctx.capacity, ctx.rad.as<float4>(), stats);
+        ctx.timing_end(ts);
+        ++ctx.launches;
+    }
+    k_accumulate<<<cdiv(pp.pixels, 256), 256, 0, st>>>(dj, items, pp.item_count, pp.pixels, ctx.rad.as<float4>());
+    ++ctx.launches;
+    return SOLRT_OK;
+}
+
 // Issues the batch's launches on the context stream.
 solrt_status batch_issue(Batch& b, bool record_timing) {
     Context& ctx = *b.ctx;
@@ -346,35 +375,11 @@ solrt_status batch_issue(Batch& b, bool record_timing) {
     const DevJob* dj = b.d_jobs.as<DevJob>();
     const DevItem* di = b.d_items.as<DevItem>();
     const uint32_t* jp = b.d_job_pix.as<uint32_t>();
-    DevStats* stats = ctx.stats.as<DevStats>();
-    PassCtl* ctl = ctx.ctl.as<PassCtl>();
     const uint32_t njobs = (uint32_t)b.jobs.size();
     const uint32_t total_pix = b.job_pix_base[njobs];
-    const int shade_grid = ctx.sm_count * 8;
     k_begin<<<cdiv(total_pix, 256), 256, 0, st>>>(dj, jp, njobs, total_pix);
     ++ctx.launches;
-    for (const PassPlan& pp : b.passes) {
-        const size_t ctl_bytes = sizeof(unsigned int) * (pp.bounces + 1);
-        SOLRT_CUDA(cudaMemsetAsync(ctl->count, 0, ctl_bytes, st));
-        SOLRT_CUDA(cudaMemsetAsync(ctl->work, 0, ctl_bytes, st));
-        const DevItem* items = di + pp.item_begin;
-        k_generate<<<cdiv(pp.paths, 256), 256, 0, st>>>(dj, items, pp.item_count, pp.paths, ctx.queue(0), ctl->count,
-                                                        stats);
-        ++ctx.launches;
-        for (uint32_t bnc = 0; bnc < pp.bounces; ++bnc) {
-            const PathQueue qin = ctx.queue(bnc & 1), qout = ctx.queue((bnc + 1) & 1);
-            const int te = record_timing ? ctx.timing_begin(0) : -1;
-            SOLRT_TRY(launch_extend(ctx, b.kind, dj, qin, ctx.hits.as<float4>(), ctl->count + bnc, ctl->work + bnc));
-            ctx.timing_end(te);
-            const int ts = record_timing ? ctx.timing_begin(1) : -1;
-            k_shade<<<shade_grid, 256, 0, st>>>(dj, items, pp.item_count, qin, ctx.hits.as<float4>(), ctl->count + bnc,
-                                                qout, ctl->count + bnc + 1, ctx.capacity, ctx.rad.as<float4>(), stats);
-            ctx.timing_end(ts);
-            ++ctx.launches;
-        }
-        k_accumulate<<<cdiv(pp.pixels, 256), 256, 0, st>>>(dj, items, pp.item_count, pp.pixels, ctx.rad.as<float4>());
-        ++ctx.launches;
-    }
+    for (const PassPlan& pp : b.passes) SOLRT_TRY(issue_pass(ctx, b.kind, dj, di + pp.item_begin, pp, record_timing));
     k_finalize<<<cdiv(total_pix, 256), 256, 0, st>>>(dj, jp, njobs, total_pix);
     ++ctx.launches;
     SOLRT_CUDA(cudaGetLastError());
@@ -512,6 +517,41 @@ solrt_status batch_launch(Batch& b) {
     SOLRT_CUDA(cudaEventRecord(ctx.ev1, ctx.stream));
     ctx.launches += b.graph_launches;
     return SOLRT_OK;
+}
+
+// One serving tick: uploads the active jobs and this tick's items, runs one
+// pass, then finalizes the jobs listed in `fin` (their last samples were in
+// this pass). Asynchronous on the context stream.
+solrt_status serve_tick(Context& ctx, TickBuffers& tb, uint32_t kind, const std::vector<DevJob>& jobs,
+                        const std::vector<DevItem>& items, const PassPlan& pp, const std::vector<DevJob>& fin) {
+    cudaStream_t st = ctx.stream;
+    cudaGetLastError();
+    SOLRT_TRY(tb.jobs.alloc(sizeof(DevJob) * std::max<size_t>(jobs.size(), 1)));
+    SOLRT_TRY(tb.items.alloc(sizeof(DevItem) * std::max<size_t>(items.size(), 1)));
+    SOLRT_CUDA(cudaMemcpyAsync(tb.jobs.ptr, jobs.data(), sizeof(DevJob) * jobs.size(), cudaMemcpyHostToDevice, st));
+    SOLRT_CUDA(cudaMemcpyAsync(tb.items.ptr, items.data(), sizeof(DevItem) * items.size(), cudaMemcpyHostToDevice, st));
+    if (pp.item_count) SOLRT_TRY(issue_pass(ctx, kind, tb.jobs.as<DevJob>(), tb.items.as<DevItem>(), pp, false));
+    if (!fin.empty()) {
+        std::vector<uint32_t> pix(1, 0u);
+        for (const DevJob& J : fin) pix.push_back(pix.back() + J.width * J.height);
+        SOLRT_TRY(tb.fin_jobs.alloc(sizeof(DevJob) * fin.size()));
+        SOLRT_TRY(tb.fin_pix.alloc(sizeof(uint32_t) * pix.size()));
+        SOLRT_CUDA(cudaMemcpyAsync(tb.fin_jobs.ptr, fin.data(), sizeof(DevJob) * fin.size(), cudaMemcpyHostToDevice, st));
+        SOLRT_CUDA(cudaMemcpyAsync(tb.fin_pix.ptr, pix.data(), sizeof(uint32_t) * pix.size(), cudaMemcpyHostToDevice, st));
+        k_finalize<<<cdiv(pix.back(), 256), 256, 0, st>>>(tb.fin_jobs.as<DevJob>(), tb.fin_pix.as<uint32_t>(),
+                                                          (uint32_t)fin.size(), pix.back());
+        ++ctx.launches;
+    }
+    SOLRT_CUDA(cudaGetLastError());
+    return SOLRT_OK;
+}
+
+DevJob job_for(const Scene& sc, const Image& img, const solrt_camera& cam, const solrt_render_params& p) {
+    return make_job(sc, img, cam, p);
+}
+
+solrt_status check_job(const Context& ctx, const Scene& sc, const Image& img, const solrt_render_params& p) {
+    return check_params(ctx, sc, img, p);
 }
 
 solrt_status render_frame(Context& ctx, const Scene& sc, const solrt_camera& cam, const solrt_render_params& p,

@@ -1,0 +1,106 @@
+"""Serving: jobs submitted while others run are admitted at tick
+boundaries, advance together, and each result equals the same job rendered
+alone (continuous batching must not change images). Admission by memory
+budget, LRU eviction of completed results and the bounded wait are
+exercised with small budgets."""
+import time
+
+import numpy as np
+import pytest
+
+from helpers import S, camera_of
+
+pytestmark = pytest.mark.gpu
+
+
+def _scenes(solrt, ctx):
+    return [solrt.SceneDescription(ctx, S.cornell()), solrt.SceneDescription(ctx, S.soup(20000, seed=2)),
+            solrt.SceneDescription(ctx, S.tunnel(n_ang=128, n_ax=64, length=20.0))]
+
+
+def _job(solrt, i):
+    rng = np.random.default_rng(100 + i)
+    w = int(rng.choice([16, 24, 40]))
+    h = int(rng.choice([16, 32]))
+    kw = dict(spp=int(rng.integers(1, 9)), max_bounces=int(rng.integers(1, 6)), seed=7 + i, job_id=i,
+              material_mode=solrt.MATERIAL_LAMBERT if i % 2 else solrt.MATERIAL_REF,
+              rng_mode=solrt.RNG_PER_SAMPLE if i % 3 else solrt.RNG_REF_STREAM,
+              miss_mode=int(i % 3), accum_mode=solrt.ACCUM_KAHAN if i % 4 == 1 else solrt.ACCUM_REF_MIX)
+    return int(rng.integers(0, 3)), solrt.render_params(w, h, **kw)
+
+
+def test_served_results_equal_alone(solrt):
+    ctx = solrt.Context(0)
+    scenes = _scenes(solrt, ctx)
+    datas = [S.cornell(), S.soup(20000, seed=2), S.tunnel(n_ang=128, n_ax=64, length=20.0)]
+    srv = solrt.Server(ctx, tick_paths=3000)   # small ticks: jobs span many ticks and overlap
+    tickets = []
+    for i in range(24):
+        si, p = _job(solrt, i)
+        cam = camera_of(datas[si], p.width / p.height)
+        tickets.append((srv.submit(scenes[si], cam, p), si, cam, p))
+        if i % 6 == 5:
+            time.sleep(0.01)   # arrivals while ticks run
+    results = []
+    for t, si, cam, p in tickets:
+        r = srv.wait(t, 60000)
+        assert r.status == 0 and r.spp_done == p.spp and r.latency_ns >= r.queue_ns
+        results.append(srv.read(t, r))
+    st = srv.stats()
+    assert st.completed == 24 and st.ticks > 1 and st.queue_depth == 0 and st.active == 0
+    srv.close()
+    # alone, on a fresh context
+    ctx2 = solrt.Context(0)
+    scenes2 = _scenes(solrt, ctx2)
+    r = solrt.Renderer(ctx2)
+    for (t, si, cam, p), (a32, a8) in zip(tickets, results):
+        img = solrt.Image(ctx2, p.width, p.height, p.accum_mode)
+        r.cmd_trace_rays(scenes2[si], cam, p, img)
+        b32, b8 = img.read()
+        assert np.array_equal(a32.view(np.uint32), b32.view(np.uint32)), t
+        assert np.array_equal(a8, b8)
+        img.close()
+
+
+def test_budget_admission_and_eviction(solrt):
+    ctx = solrt.Context(0)
+    sc = solrt.SceneDescription(ctx, S.cornell())
+    cam = camera_of(S.cornell(), 1.0)
+    scene_bytes = sc.device_bytes()
+    img_bytes = 32 * 32 * 40
+    # room for the scene and two 32x32 images: later jobs wait or evict old results
+    srv = solrt.Server(ctx, memory_budget=scene_bytes + 2 * img_bytes + 100)
+    p = solrt.render_params(32, 32, spp=4, max_bounces=3, material_mode=solrt.MATERIAL_LAMBERT,
+                            rng_mode=solrt.RNG_PER_SAMPLE, seed=1)
+    tickets = [srv.submit(sc, cam, p) for _ in range(6)]
+    r = srv.wait(tickets[-1], 60000)   # results of earlier jobs may already be evicted
+    assert r.status == 0
+    st = srv.stats()
+    assert st.completed == 6 and st.evicted >= 3
+    assert st.bytes_in_use <= scene_bytes + 2 * img_bytes + 100
+    # the oldest results were evicted
+    s, _ = srv.poll(tickets[0])
+    assert s == 7   # SOLRT_ERR_NOT_FOUND
+    # a job bigger than the whole budget fails instead of waiting forever
+    big = solrt.render_params(256, 256, spp=1)
+    t = srv.submit(sc, cam, big)
+    with pytest.raises(solrt.SolrtError) as e:
+        srv.wait(t, 20000)
+    assert e.value.status == 8   # SOLRT_ERR_BUDGET
+    srv.close()
+
+
+def test_wait_is_bounded(solrt):
+    ctx = solrt.Context(0)
+    sc = solrt.SceneDescription(ctx, S.soup(20000, seed=3))
+    cam = camera_of(S.soup(20000, seed=3), 1.0)
+    srv = solrt.Server(ctx, tick_paths=1000)
+    p = solrt.render_params(64, 64, spp=64, max_bounces=4, material_mode=solrt.MATERIAL_LAMBERT,
+                            rng_mode=solrt.RNG_PER_SAMPLE, seed=3)
+    t = srv.submit(sc, cam, p)
+    with pytest.raises(solrt.SolrtError) as e:
+        srv.wait(t, 0)
+    assert e.value.status == 4   # SOLRT_ERR_TIMEOUT
+    r = srv.wait(t, 60000)
+    assert r.status == 0
+    srv.close()
