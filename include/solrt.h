@@ -425,6 +425,29 @@ solrt_status solrt_debug_unit(solrt_context* ctx, uint32_t op, uint32_t n, const
                               float* out_f32);
 
 /* ------------------------------------------------------------------------ */
+/* glTF 2.0 scene input                                                     */
+/* ------------------------------------------------------------------------ */
+
+typedef struct solrt_gltf solrt_gltf;
+
+/* Reads a .gltf (JSON with external .bin or base64 data URIs) or .glb file
+ * into host arrays, as load_scene does (src/scene/mod.rs:138-295): one
+ * section per mesh primitive with its material; POSITION, NORMAL (default
+ * 0,1,0), COLOR_0 (default 1,1,1,1), TEXCOORD_0 (default 0); u8/u16/u32
+ * indices; every primitive of a mesh gets the mesh's global transform
+ * (calc_mesh_global_transform, src/scene/mod.rs:124-136) and its
+ * inverse-transpose. Primitives without a material use a default one
+ * (base colour 1, metallic 1, roughness 1, as glTF specifies). */
+solrt_status solrt_gltf_load(const char* path, solrt_gltf** out);
+/* Scene description over the loaded arrays (valid until solrt_gltf_destroy). */
+solrt_status solrt_gltf_scene_desc(const solrt_gltf* g, solrt_scene_desc* out);
+/* The first perspective camera: its node matrix taken as the view matrix and
+ * yfov taken in degrees, as Camera::from_view and update_persp do
+ * (src/scene/camera.rs:73-106). SOLRT_ERR_NOT_FOUND when there is none. */
+solrt_status solrt_gltf_camera(const solrt_gltf* g, float aspect, solrt_camera* out);
+solrt_status solrt_gltf_destroy(solrt_gltf* g);
+
+/* ------------------------------------------------------------------------ */
 /* Allocation-free BVH build (no counterpart in the reference)              */
 /* ------------------------------------------------------------------------ */
 

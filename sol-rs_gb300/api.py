@@ -175,6 +175,10 @@ _PROTOS = {
     "solrt_trace_rays": (ctypes.c_int, [_P, _P, _P, _U32, _P]),
     "solrt_trace_rays_device": (ctypes.c_int, [_P, _P, _P, _U32, _P]),
     "solrt_debug_unit": (ctypes.c_int, [_P, _U32, _U32, _P, _P, _P, _P, _P]),
+    "solrt_gltf_load": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_P)]),
+    "solrt_gltf_scene_desc": (ctypes.c_int, [_P, ctypes.POINTER(SceneDesc)]),
+    "solrt_gltf_camera": (ctypes.c_int, [_P, ctypes.c_float, ctypes.POINTER(Camera)]),
+    "solrt_gltf_destroy": (ctypes.c_int, [_P]),
 }
 
 _lib = None
@@ -492,3 +496,60 @@ class Renderer:
                                  image.handle))
 
     render = cmd_trace_rays
+
+
+# ---------------------------------------------------------------------------
+# glTF input
+# ---------------------------------------------------------------------------
+
+def _copy(ptr, n, dtype):
+    if n == 0 or not ptr:
+        return np.zeros(0, dtype)
+    return np.frombuffer(ctypes.string_at(ptr, n * dtype.itemsize), dtype=dtype).copy()
+
+
+class GltfScene:
+    """A .gltf / .glb file read on the host by solrt_gltf_load; the
+    counterpart of scene::load_scene (src/scene/mod.rs:138-295).
+
+    `data` is a scenes.SceneData (one section and one instance per glTF
+    primitive, the instance carrying its mesh's global node transform);
+    `camera(aspect)` is the file's first perspective camera as
+    Camera::from_view + set_window_size builds it (src/scene/camera.rs:73-106),
+    or None when the file has none.
+    """
+
+    def __init__(self, path):
+        from . import scenes
+        h = ctypes.c_void_p()
+        check(lib().solrt_gltf_load(os.fsencode(path), ctypes.byref(h)))
+        self.handle = h
+        d = SceneDesc()
+        check(lib().solrt_gltf_scene_desc(h, ctypes.byref(d)))
+        self.data = scenes.SceneData(
+            _copy(d.vertices, d.vertex_count, scenes.VERTEX_DTYPE),
+            _copy(d.indices, d.index_count, np.dtype("<u4")),
+            _copy(d.sections, d.section_count, scenes.SECTION_DTYPE),
+            _copy(d.materials, d.material_count, scenes.MATERIAL_DTYPE),
+            _copy(d.instances, d.section_count, scenes.INSTANCE_DTYPE),
+            name=os.path.basename(path))
+
+    def camera(self, aspect):
+        c = Camera()
+        st = lib().solrt_gltf_camera(self.handle, float(aspect), ctypes.byref(c))
+        if st == ERR_NOT_FOUND:
+            return None
+        check(st)
+        return c
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().solrt_gltf_destroy(self.handle)
+            self.handle = None
+
+    __del__ = close
+
+
+def load_scene(path):
+    """scene::load_scene: reads a glTF file into a GltfScene."""
+    return GltfScene(path)

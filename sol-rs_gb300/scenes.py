@@ -248,3 +248,102 @@ def mixed_scene(i, seed_base=4, min_tris=1000, max_tris=500000):
     spp = int(rng.integers(4, 65))
     data = b.build(dict(CORNELL_CAMERA), "mixed%d" % i)
     return data, dict(width=res, height=res, spp=spp, max_bounces=5, seed=seed_base + i)
+
+
+def write_gltf(data, path, view=None, yfov=None, znear=0.01, zfar=100.0, node_transforms=None,
+               index_type="u32", external_bin=False):
+    """Writes a SceneData as glTF 2.0 that load_scene reads back
+    (src/scene/mod.rs:138-295 / solrt_gltf_load): one mesh and one node per
+    section, positions / normals / COLOR_0 / TEXCOORD_0 as float accessors,
+    indices as u16 or u32, the materials' factors, and optionally a
+    perspective camera node whose matrix is `view` (column-major) with
+    `yfov` in the reference's unit (degrees, passed through Camera::from_view).
+
+    node_transforms: optional per-section dict of glTF node properties
+    ("matrix" or "translation"/"rotation"/"scale"); the vertices are written
+    as stored, so the loaded instance transform is the node's.
+    Path suffix .glb writes a binary container; external_bin writes the
+    buffer beside a .gltf instead of a base64 data URI.
+    """
+    import base64
+    import json
+    import os
+    import struct
+
+    blob = bytearray()
+    views, accessors = [], []
+
+    def add(arr, ctype, atype, target=None, minmax=False):
+        arr = np.ascontiguousarray(arr)
+        while len(blob) % 4:
+            blob.append(0)
+        off = len(blob)
+        blob.extend(arr.tobytes())
+        bv = {"buffer": 0, "byteOffset": off, "byteLength": arr.nbytes}
+        if target:
+            bv["target"] = target
+        views.append(bv)
+        acc = {"bufferView": len(views) - 1, "componentType": ctype, "count": int(arr.shape[0]), "type": atype}
+        if minmax and arr.shape[0]:
+            acc["min"] = [float(x) for x in arr.min(axis=0)]
+            acc["max"] = [float(x) for x in arr.max(axis=0)]
+        accessors.append(acc)
+        return len(accessors) - 1
+
+    meshes, nodes = [], []
+    for si, s in enumerate(data.sections):
+        v = data.vertices[int(s["vertex_offset"]):int(s["vertex_offset"] + s["vertex_count"])]
+        idx = data.indices[int(s["index_offset"]):int(s["index_offset"] + s["index_count"])]
+        attrs = {
+            "POSITION": add(v["pos"][:, :3].astype("<f4"), 5126, "VEC3", 34962, minmax=True),
+            "NORMAL": add(v["normal"][:, :3].astype("<f4"), 5126, "VEC3", 34962),
+            "COLOR_0": add(v["color"].astype("<f4"), 5126, "VEC4", 34962),
+            "TEXCOORD_0": add(v["uv"][:, :2].astype("<f4"), 5126, "VEC2", 34962),
+        }
+        if index_type == "u16":
+            ia = add(idx.astype("<u2"), 5123, "SCALAR", 34963)
+        else:
+            ia = add(idx.astype("<u4"), 5125, "SCALAR", 34963)
+        meshes.append({"primitives": [{"attributes": attrs, "indices": ia, "material": int(s["material_index"]),
+                                       "mode": 4}]})
+        node = {"mesh": si}
+        if node_transforms is not None and node_transforms[si]:
+            node.update(node_transforms[si])
+        nodes.append(node)
+    mats = []
+    for m in data.materials:
+        mats.append({"pbrMetallicRoughness": {"baseColorFactor": [float(x) for x in m["base_color"]],
+                                              "metallicFactor": float(m["metallic"]),
+                                              "roughnessFactor": float(m["roughness"])},
+                     "emissiveFactor": [float(x) for x in m["emissive"]]})
+    doc = {"asset": {"version": "2.0", "generator": "sol-rs_gb300 scenes.write_gltf"},
+           "scene": 0, "scenes": [{"nodes": list(range(len(nodes)))}],
+           "nodes": nodes, "meshes": meshes, "materials": mats, "accessors": accessors, "bufferViews": views}
+    if view is not None:
+        doc["cameras"] = [{"type": "perspective",
+                           "perspective": {"yfov": float(yfov), "znear": float(znear), "zfar": float(zfar),
+                                           "aspectRatio": 1.0}}]
+        nodes.append({"camera": 0, "matrix": [float(x) for x in np.asarray(view, np.float64).reshape(16)]})
+        doc["scenes"][0]["nodes"].append(len(nodes) - 1)
+    while len(blob) % 4:
+        blob.append(0)
+    if str(path).endswith(".glb"):
+        doc["buffers"] = [{"byteLength": len(blob)}]
+        js = json.dumps(doc).encode()
+        js += b" " * ((4 - len(js) % 4) % 4)
+        total = 12 + 8 + len(js) + 8 + len(blob)
+        with open(path, "wb") as f:
+            f.write(struct.pack("<4sII", b"glTF", 2, total))
+            f.write(struct.pack("<II", len(js), 0x4E4F534A) + js)
+            f.write(struct.pack("<II", len(blob), 0x004E4942) + bytes(blob))
+        return
+    if external_bin:
+        bin_name = os.path.splitext(os.path.basename(str(path)))[0] + ".bin"
+        with open(os.path.join(os.path.dirname(str(path)), bin_name), "wb") as f:
+            f.write(bytes(blob))
+        doc["buffers"] = [{"byteLength": len(blob), "uri": bin_name}]
+    else:
+        doc["buffers"] = [{"byteLength": len(blob),
+                           "uri": "data:application/octet-stream;base64," + base64.b64encode(bytes(blob)).decode()}]
+    with open(path, "w") as f:
+        json.dump(doc, f)
