@@ -115,10 +115,16 @@ typedef enum solrt_bvh_kind {
     SOLRT_BVH8_Q8 = 1   /* 8-wide, 8-bit quantised child boxes, 80 B nodes */
 } solrt_bvh_kind;
 
+/* solrt_bvh_desc.flags */
+#define SOLRT_BVH_DYNAMIC 1u  /* keep object-space geometry and the BVH topology on
+                                 the device so solrt_scene_set_instances +
+                                 solrt_scene_regenerate can move sections */
+
 typedef struct solrt_bvh_desc {
     uint32_t kind;       /* solrt_bvh_kind */
     uint32_t leaf_max;   /* BVH8: max triangles per leaf child (1..3), 0 = 3 */
-    uint32_t reserved[2];
+    uint32_t flags;      /* SOLRT_BVH_DYNAMIC (honoured by solrt_scene_create) */
+    uint32_t reserved;
 } solrt_bvh_desc;
 
 typedef struct solrt_bvh_info {
@@ -185,8 +191,31 @@ typedef struct solrt_render_params {
     uint32_t rng_mode;          /* solrt_rng_mode */
     float tmax;                 /* 0 = reference 1e4 */
     uint32_t kernel;            /* solrt_kernel */
-    uint32_t reserved[2];
+    uint32_t integrator;        /* solrt_integrator */
+    uint32_t reserved;
 } solrt_render_params;
+
+/* What one launch computes per pixel. DEBUG and AO are the reference's
+ * sibling ray-tracing pipelines over the same acceleration structure; they
+ * run one thread per pixel (their shaders' structure), ignore `kernel`, and
+ * are not accepted by batches or the server. */
+typedef enum solrt_integrator {
+    /* pathtrace.rgen / .rchit / .rmiss */
+    SOLRT_INTEGRATOR_PATH = 0,
+    /* debug.rgen / .rchit / .rmiss: one ray through each pixel centre
+     * (tmin 0.001, tmax 1000); the image gets (1-u-v, u, v, 0) of the hit, or
+     * the ray direction (x, y, z, 0) on a miss. No accumulation: the RGBA32F
+     * image holds that value, the RGBA8 image its UNORM conversion. */
+    SOLRT_INTEGRATOR_DEBUG = 1,
+    /* ao.rgen / .rchit / .rmiss: `spp` jittered samples (reference 4), each
+     * a chain of cosine-weighted rays along which every hit after the first
+     * counts one occlusion, until a miss or `max_bounces` + 1 hits
+     * (reference max_samples 4); directions from the blue-noise texture
+     * set by solrt_context_set_blue_noise; colour = 1 - mean occlusion /
+     * max_bounces, mixed into the image with 1 / (frame + 1 -
+     * accum_start_frame) (ao.rgen:57-80). RGBA8 = UNORM of the colour. */
+    SOLRT_INTEGRATOR_AO = 2
+} solrt_integrator;
 
 typedef enum solrt_kernel {
     /* generate / extend / shade stages over queues shared by all paths */
@@ -280,6 +309,11 @@ solrt_status solrt_reset_stats(solrt_context* ctx);
 /* The CUDA stream (cudaStream_t) of the context, for callers that enqueue
  * their own work around the library's. */
 void* solrt_context_stream(solrt_context* ctx);
+/* Blue-noise texture of SOLRT_INTEGRATOR_AO: width x height RGBA8 UNORM
+ * texels, row-major (the sampler2D of ao.rchit:39, loaded from
+ * textures/HDR_RGBA_0.png by examples/4-ray-ao.rs:198-201). Copied. */
+solrt_status solrt_context_set_blue_noise(solrt_context* ctx, const uint8_t* rgba8, uint32_t width,
+                                          uint32_t height);
 
 /* Scene: flattens sections to world space (transform, transform_it as in
  * pathtrace.rchit:80-86), uploads and builds the BVH. Synchronises.
@@ -297,6 +331,33 @@ solrt_status solrt_scene_bvh_export(solrt_scene* scene, void* nodes, size_t node
                                     void* tris, size_t tris_bytes);
 /* Device memory held by the scene, in bytes. */
 solrt_status solrt_scene_bytes(solrt_scene* scene, uint64_t* out);
+
+/* ---- per-frame instance transforms --------------------------------------
+ * Replaces SceneDescription::blas_transform / blas_transforms (which set a
+ * BLAS instance's transform and the SceneInstance transform + inverse
+ * transpose, src/ray/mod.rs:162-176, SceneInstance::update_transform
+ * src/ray/mod.rs:26-35) and tlas_regenerate (src/ray/mod.rs:178-181, called
+ * every frame by examples/5-pathtrace.rs:316).
+ *
+ * The scene keeps its sections' object-space vertices on the device (scene
+ * created with SOLRT_BVH_DYNAMIC). set_instances stores one instance per
+ * section; regenerate transforms every vertex on the device with its
+ * section's instance (the same arithmetic as solrt_scene_create's
+ * flattening, so results equal a scene created with those instances) and
+ * then rebuilds the BVH (REBUILD: identical to a fresh build) or refits the
+ * boxes of the existing topology (REFIT: cheaper, same hits, BVH quality
+ * degrades as sections move). Stream-ordered on the context stream. */
+typedef enum solrt_regen_mode {
+    SOLRT_REGEN_REBUILD = 0,
+    SOLRT_REGEN_REFIT = 1
+} solrt_regen_mode;
+
+/* transform (column-major) -> instance with transform_it = inverse(T)^T
+ * computed in FP64 and rounded; ERR_INVALID for a singular transform. */
+solrt_status solrt_instance_from_transform(const float transform[16], uint32_t id, solrt_instance* out);
+/* count must equal the scene's section count. */
+solrt_status solrt_scene_set_instances(solrt_scene* scene, const solrt_instance* instances, uint32_t count);
+solrt_status solrt_scene_regenerate(solrt_scene* scene, uint32_t mode);
 
 /* Camera matrices (src/scene/camera.rs:98-106: look_at_rh, perspective_rh),
  * computed in FP64 and rounded to FP32. vfov in degrees. */

@@ -59,6 +59,7 @@ def lib():
         L.oracle_render.argtypes = [_P, ctypes.POINTER(_api.Camera), ctypes.POINTER(_api.RenderParams), _P, _P, _P,
                                     _P, ctypes.c_int, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32,
                                     ctypes.POINTER(RenderStats)]
+        L.oracle_render_ex.argtypes = L.oracle_render.argtypes + [_P, ctypes.c_uint32, ctypes.c_uint32]
         L.oracle_render_samples.argtypes = [_P, ctypes.POINTER(_api.Camera), ctypes.POINTER(_api.RenderParams), _P,
                                             ctypes.c_int, ctypes.c_int]
         L.oracle_tea.restype = ctypes.c_uint32
@@ -131,9 +132,11 @@ class OracleScene:
                            ctypes.byref(fb))
         return hits, fb.value
 
-    def render(self, camera, params, accum=None, ksum=None, kcomp=None, precision=32, threads=0, rows=None):
+    def render(self, camera, params, accum=None, ksum=None, kcomp=None, precision=32, threads=0, rows=None,
+               blue_noise=None):
         """One launch. Returns (accum, rgba8, stats); accum/ksum/kcomp are
-        updated in place when given (running accumulation across frames)."""
+        updated in place when given (running accumulation across frames).
+        blue_noise: (h, w, 4) uint8 texture of the AO integrator."""
         h, w = params.height, params.width
         if accum is None:
             accum = np.zeros((h, w, 4), np.float32)
@@ -145,8 +148,11 @@ class OracleScene:
         rgba8 = np.zeros((h, w, 4), np.uint8)
         st = RenderStats()
         r0, r1 = (0, 0) if rows is None else rows
-        rc = lib().oracle_render(self.handle, ctypes.byref(camera), ctypes.byref(params), _ptr(accum), _ptr(ksum),
-                                 _ptr(kcomp), _ptr(rgba8), precision, threads, r0, r1, ctypes.byref(st))
+        nz = None if blue_noise is None else np.ascontiguousarray(blue_noise, np.uint8)
+        nh, nw = (0, 0) if nz is None else nz.shape[:2]
+        rc = lib().oracle_render_ex(self.handle, ctypes.byref(camera), ctypes.byref(params), _ptr(accum), _ptr(ksum),
+                                    _ptr(kcomp), _ptr(rgba8), precision, threads, r0, r1, ctypes.byref(st),
+                                    _ptr(nz), nw, nh)
         if rc != 0:
             raise ValueError("oracle_render failed")
         return accum, rgba8, st

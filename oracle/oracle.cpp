@@ -692,6 +692,107 @@ void render_pixel(const oracle_scene* s, const solrt_camera* cam, const solrt_re
     rgba8[4 * pix + 3] = 255;
 }
 
+// debug.rgen:18-36 + debug.rchit:9-13 + debug.rmiss: one ray through the
+// pixel centre; barycentrics of the hit or the ray direction, stored as is.
+template <class R>
+void render_pixel_debug(const oracle_scene* s, const solrt_camera* cam, const solrt_render_params* p, uint32_t x,
+                        uint32_t y, float* accum, uint8_t* rgba8, Counters& cn) {
+    const uint32_t W = p->width, H = p->height, pix = x + y * W;
+    const R px = R(x) + R(0.5f), py = R(y) + R(0.5f);
+    const R ux = px / R(W), uy = py / R(H);
+    const R dx = ux * R(2) - R(1), dy = uy * R(2) - R(1);
+    R org[4], tgt[4], dir[4];
+    mat4_mul<R>(cam->view_inverse, R(0), R(0), R(0), R(1), org);
+    mat4_mul<R>(cam->projection_inverse, dx, dy, R(1), R(1), tgt);
+    const V3<R> tn = normalize(V3<R>{tgt[0], tgt[1], tgt[2]});
+    mat4_mul<R>(cam->view_inverse, tn.x, tn.y, tn.z, R(0), dir);
+    const HitR<R> h = closest_hit<R>(s, V3<R>{org[0], org[1], org[2]}, V3<R>{dir[0], dir[1], dir[2]}, R(0.001f),
+                                     R(1000.0f), 1, cn.fb, cn.nv, cn.nt);
+    ++cn.seg;
+    ++cn.paths;
+    float v[3] = {(float)dir[0], (float)dir[1], (float)dir[2]};
+    if (h.prim != SOLRT_NO_HIT) {
+        v[0] = (float)((R(1) - h.u) - h.v);
+        v[1] = (float)h.u;
+        v[2] = (float)h.v;
+    }
+    for (int c = 0; c < 3; ++c) {
+        accum[4 * pix + c] = v[c];
+        rgba8[4 * pix + c] = to_unorm8(v[c]);
+    }
+    accum[4 * pix + 3] = 0.0f;
+    rgba8[4 * pix + 3] = 0;
+}
+
+// ao.rgen:37-83 + ao.rchit:53-88 + ao.rmiss. `spp` samples of at most
+// `max_bounces` + 1 hits; every hit after the first is one occlusion.
+template <class R>
+void render_pixel_ao(const oracle_scene* s, const solrt_camera* cam, const solrt_render_params* p, uint32_t x,
+                     uint32_t y, float* accum, uint8_t* rgba8, const uint8_t* noise, uint32_t nw, uint32_t nh,
+                     Counters& cn) {
+    const uint32_t W = p->width, H = p->height, pix = x + y * W;
+    uint32_t rng = tea(pix, p->frame);                              // ao.rgen:49
+    const R max_samples = R(p->max_bounces);
+    V3<R> ao{R(0), R(0), R(0)};
+    for (uint32_t i = 0; i < p->spp; ++i) {
+        V3<R> o, d;
+        R tmin;
+        camera_ray<R>(cam, x, y, W, H, rng, o, d, tmin);           // ao.rgen:52-61 + preparePayload
+        R tmax = R(10000.0f);
+        ++cn.paths;
+        R hv = R(0);
+        uint32_t depth = 0;
+        for (;;) {
+            const HitR<R> h = closest_hit<R>(s, o, d, tmin, tmax, 1, cn.fb, cn.nv, cn.nt);
+            ++cn.seg;
+            if (h.prim == SOLRT_NO_HIT) break;                      // ao.rmiss: done
+            const TriW& tri = s->tris[h.prim];
+            const R b1 = h.u, b2 = h.v;
+            const R b0 = (R(1) - b1) - b2;
+            auto cv = [](V3<float> a) { return V3<R>{R(a.x), R(a.y), R(a.z)}; };
+            const V3<R> normal = normalize(cv(tri.n[0]) * b0 + cv(tri.n[1]) * b1 + cv(tri.n[2]) * b2);
+            const V3<R> pos = cv(tri.p[0]) * b0 + cv(tri.p[1]) * b1 + cv(tri.p[2]) * b2;
+            const V3<R> no = pos + R(0.00001f) * d;                 // ao.rchit:78
+            // getBlueRand2(depth + depth * sampleId) (ao.rchit:43-49)
+            const uint32_t bi = depth + depth * i;
+            const R r0 = next_rand<R>(rng);
+            const R r1 = next_rand<R>(rng);
+            const R tw = R(nw), th = R(nh);
+            R cx = R(x) + r0 * tw, cy = R(y) + r1 * th;
+            cx = cx - tw * std::floor(cx / tw);                     // GLSL mod
+            cy = cy - th * std::floor(cy / th);
+            int ix = (int)cx, iy = (int)cy;
+            ix = std::min(std::max(ix, 0), (int)nw - 1);
+            iy = std::min(std::max(iy, 0), (int)nh - 1);
+            const uint8_t* t = noise + 4 * ((size_t)iy * nw + ix);
+            const R blue[4] = {R((float)t[0] / 255.0f), R((float)t[1] / 255.0f), R((float)t[2] / 255.0f),
+                               R((float)t[3] / 255.0f)};
+            const R xi0 = blue[bi % 4], xi1 = blue[(bi + 1) % 4];
+            const V3<R> hit_n = normal * glsl_sign(dot(-d, normal));
+            d = sample_cosine(hit_n, xi0, xi1);
+            o = no;
+            tmin = R(0.001f);
+            tmax = R(10.0f);
+            if (depth > 0) hv = hv + R(1);
+            ++depth;
+            if (depth > p->max_bounces) break;                      // ao.rgen:75
+        }
+        ao = ao + (R(1) / max_samples) * V3<R>{hv, hv, hv};        // ao.rgen:77
+    }
+    const R n = R(p->spp);
+    V3<R> color = V3<R>{R(1) - ao.x / n, R(1) - ao.y / n, R(1) - ao.z / n};
+    const R a = R(1) / R((uint32_t)(p->frame - p->accum_start_frame + 1u));
+    const V3<R> old{R(accum[4 * pix]), R(accum[4 * pix + 1]), R(accum[4 * pix + 2])};
+    color = mix(old, color, a);                                     // ao.rgen:79-82
+    const float of[3] = {(float)color.x, (float)color.y, (float)color.z};
+    for (int c = 0; c < 3; ++c) {
+        accum[4 * pix + c] = of[c];
+        rgba8[4 * pix + c] = to_unorm8(of[c]);
+    }
+    accum[4 * pix + 3] = 1.0f;
+    rgba8[4 * pix + 3] = 255;
+}
+
 template <class F> void parallel_for(uint32_t n, int threads, F&& f) {
     if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
     if (threads == 1 || n < 2) {
@@ -802,9 +903,13 @@ int oracle_trace(const oracle_scene* s, const solrt_ray* rays, uint32_t n, solrt
 
 static int render_impl(const oracle_scene* s, const solrt_camera* cam, const solrt_render_params* p, float* accum,
                        float* ksum, float* kcomp, uint8_t* rgba8, float* samples_out, int precision,
-                       int threads, uint32_t row_begin, uint32_t row_end, oracle_render_stats* stats) {
+                       int threads, uint32_t row_begin, uint32_t row_end, oracle_render_stats* stats,
+                       const uint8_t* noise = nullptr, uint32_t nw = 0, uint32_t nh = 0) {
     if (!s || !cam || !p || p->width == 0 || p->height == 0 || p->spp == 0) return 1;
     if (!samples_out && (!accum || !rgba8)) return 1;
+    if (p->integrator > SOLRT_INTEGRATOR_AO) return 1;
+    if (p->integrator != SOLRT_INTEGRATOR_PATH && samples_out) return 1;
+    if (p->integrator == SOLRT_INTEGRATOR_AO && (!noise || nw == 0 || nh == 0 || p->max_bounces == 0)) return 1;
     if (!samples_out && p->accum_mode == SOLRT_ACCUM_KAHAN && (!ksum || !kcomp)) return 1;
     if (row_end <= row_begin) { row_begin = 0; row_end = p->height; }
     row_end = std::min(row_end, p->height);
@@ -814,10 +919,17 @@ static int render_impl(const oracle_scene* s, const solrt_camera* cam, const sol
     parallel_for(rows, threads, [&](uint32_t r, int t) {
         const uint32_t y = row_begin + r;
         for (uint32_t x = 0; x < p->width; ++x) {
-            if (precision == 64)
+            if (p->integrator == SOLRT_INTEGRATOR_DEBUG) {
+                if (precision == 64) render_pixel_debug<double>(s, cam, p, x, y, accum, rgba8, cn[t]);
+                else render_pixel_debug<float>(s, cam, p, x, y, accum, rgba8, cn[t]);
+            } else if (p->integrator == SOLRT_INTEGRATOR_AO) {
+                if (precision == 64) render_pixel_ao<double>(s, cam, p, x, y, accum, rgba8, noise, nw, nh, cn[t]);
+                else render_pixel_ao<float>(s, cam, p, x, y, accum, rgba8, noise, nw, nh, cn[t]);
+            } else if (precision == 64) {
                 render_pixel<double>(s, cam, p, x, y, accum, ksum, kcomp, rgba8, samples_out, cn[t]);
-            else
+            } else {
                 render_pixel<float>(s, cam, p, x, y, accum, ksum, kcomp, rgba8, samples_out, cn[t]);
+            }
         }
     });
     if (stats) {
@@ -838,6 +950,14 @@ int oracle_render(const oracle_scene* s, const solrt_camera* cam, const solrt_re
                   uint32_t row_begin, uint32_t row_end, oracle_render_stats* stats) {
     return render_impl(s, cam, p, accum, kahan_sum, kahan_comp, rgba8, nullptr, precision, threads, row_begin,
                        row_end, stats);
+}
+
+int oracle_render_ex(const oracle_scene* s, const solrt_camera* cam, const solrt_render_params* p, float* accum,
+                     float* kahan_sum, float* kahan_comp, uint8_t* rgba8, int precision, int threads,
+                     uint32_t row_begin, uint32_t row_end, oracle_render_stats* stats, const uint8_t* blue_noise,
+                     uint32_t noise_w, uint32_t noise_h) {
+    return render_impl(s, cam, p, accum, kahan_sum, kahan_comp, rgba8, nullptr, precision, threads, row_begin,
+                       row_end, stats, blue_noise, noise_w, noise_h);
 }
 
 int oracle_render_samples(const oracle_scene* s, const solrt_camera* cam, const solrt_render_params* p,

@@ -79,6 +79,15 @@ int oracle_render(const oracle_scene* s, const solrt_camera* cam, const solrt_re
                   int precision, int threads, uint32_t row_begin, uint32_t row_end,
                   oracle_render_stats* stats);
 
+/* oracle_render for every integrator (p->integrator): DEBUG and AO write
+ * accum and rgba8 as the library does; AO needs the blue-noise texture
+ * (noise_w x noise_h RGBA8 texels). */
+int oracle_render_ex(const oracle_scene* s, const solrt_camera* cam, const solrt_render_params* p,
+                     float* accum, float* kahan_sum, float* kahan_comp, uint8_t* rgba8,
+                     int precision, int threads, uint32_t row_begin, uint32_t row_end,
+                     oracle_render_stats* stats, const uint8_t* blue_noise, uint32_t noise_w,
+                     uint32_t noise_h);
+
 /* Per-path radiance of one launch, no accumulation: out[(pix*spp + s)*4]. */
 int oracle_render_samples(const oracle_scene* s, const solrt_camera* cam,
                           const solrt_render_params* p, float* out, int precision, int threads);

@@ -26,6 +26,9 @@ MATERIAL_REF, MATERIAL_LAMBERT = 0, 1
 ACCUM_REF_MIX, ACCUM_KAHAN = 0, 1
 RNG_REF_STREAM, RNG_PER_SAMPLE = 0, 1
 KERNEL_WAVEFRONT, KERNEL_MEGA = 0, 1
+INTEGRATOR_PATH, INTEGRATOR_DEBUG, INTEGRATOR_AO = 0, 1, 2
+BVH_DYNAMIC = 1
+REGEN_REBUILD, REGEN_REFIT = 0, 1
 EFLAG_STACK, EFLAG_QUEUE, EFLAG_INDEX, EFLAG_TIMEOUT = 1, 2, 4, 8
 
 
@@ -67,7 +70,8 @@ class SceneDesc(ctypes.Structure):
 
 
 class BvhDesc(ctypes.Structure):
-    _fields_ = [("kind", ctypes.c_uint32), ("leaf_max", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 2)]
+    _fields_ = [("kind", ctypes.c_uint32), ("leaf_max", ctypes.c_uint32), ("flags", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
 
 
 class BvhInfo(ctypes.Structure):
@@ -85,7 +89,8 @@ class RenderParams(ctypes.Structure):
                 ("max_bounces", ctypes.c_uint32), ("frame", ctypes.c_uint32), ("accum_start_frame", ctypes.c_uint32),
                 ("seed", ctypes.c_uint32), ("job_id", ctypes.c_uint32), ("miss_mode", ctypes.c_uint32),
                 ("material_mode", ctypes.c_uint32), ("accum_mode", ctypes.c_uint32), ("rng_mode", ctypes.c_uint32),
-                ("tmax", ctypes.c_float), ("kernel", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 2)]
+                ("tmax", ctypes.c_float), ("kernel", ctypes.c_uint32), ("integrator", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
 
 
 class Job(ctypes.Structure):
@@ -143,6 +148,7 @@ _PROTOS = {
     "solrt_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(Stats)]),
     "solrt_reset_stats": (ctypes.c_int, [_P]),
     "solrt_context_stream": (_P, [_P]),
+    "solrt_context_set_blue_noise": (ctypes.c_int, [_P, _P, _U32, _U32]),
     "solrt_scene_create": (ctypes.c_int, [_P, ctypes.POINTER(SceneDesc), ctypes.POINTER(BvhDesc), ctypes.POINTER(_P)]),
     "solrt_scene_destroy": (ctypes.c_int, [_P]),
     "solrt_scene_build_bvh": (ctypes.c_int, [_P, ctypes.POINTER(BvhDesc)]),
@@ -175,6 +181,9 @@ _PROTOS = {
     "solrt_trace_rays": (ctypes.c_int, [_P, _P, _P, _U32, _P]),
     "solrt_trace_rays_device": (ctypes.c_int, [_P, _P, _P, _U32, _P]),
     "solrt_debug_unit": (ctypes.c_int, [_P, _U32, _U32, _P, _P, _P, _P, _P]),
+    "solrt_instance_from_transform": (ctypes.c_int, [ctypes.POINTER(F16), _U32, ctypes.POINTER(Instance)]),
+    "solrt_scene_set_instances": (ctypes.c_int, [_P, _P, _U32]),
+    "solrt_scene_regenerate": (ctypes.c_int, [_P, _U32]),
     "solrt_gltf_load": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(_P)]),
     "solrt_gltf_scene_desc": (ctypes.c_int, [_P, ctypes.POINTER(SceneDesc)]),
     "solrt_gltf_camera": (ctypes.c_int, [_P, ctypes.c_float, ctypes.POINTER(Camera)]),
@@ -250,6 +259,13 @@ class Context:
     def stream(self):
         return lib().solrt_context_stream(self.handle)
 
+    def set_blue_noise(self, rgba8):
+        """(h, w, 4) uint8 texture of the AO integrator (the reference loads
+        textures/HDR_RGBA_0.png)."""
+        t = np.ascontiguousarray(rgba8, np.uint8)
+        assert t.ndim == 3 and t.shape[2] == 4
+        check(lib().solrt_context_set_blue_noise(self.handle, _ptr(t), t.shape[1], t.shape[0]))
+
     def debug_unit(self, op, n, a=None, b=None, fin=None, out_u=None, out_f=None):
         check(lib().solrt_debug_unit(self.handle, op, n, _ptr(a), _ptr(b), _ptr(fin), _ptr(out_u), _ptr(out_f)))
 
@@ -270,20 +286,50 @@ def scene_desc(data):
 
 
 class SceneDescription:
-    """Device scene + BVH (solrt_scene). Mirrors ray::SceneDescription."""
+    """Device scene + BVH (solrt_scene). Mirrors ray::SceneDescription.
 
-    def __init__(self, context, data, bvh=BVH2, leaf_max=0, keep_data=True):
+    dynamic=True keeps object-space geometry on the device so that
+    blas_transform(s) + tlas_regenerate move sections per frame
+    (src/ray/mod.rs:162-181)."""
+
+    def __init__(self, context, data, bvh=BVH2, leaf_max=0, keep_data=True, dynamic=False):
         self.context = context
         self.data = data if keep_data else None
+        self.dynamic = dynamic
         d = scene_desc(data)
-        bd = BvhDesc(kind=bvh, leaf_max=leaf_max)
+        bd = BvhDesc(kind=bvh, leaf_max=leaf_max, flags=BVH_DYNAMIC if dynamic else 0)
         h = ctypes.c_void_p()
         check(lib().solrt_scene_create(context.handle, ctypes.byref(d), ctypes.byref(bd), ctypes.byref(h)))
         self.handle = h
+        if dynamic:
+            from . import scenes
+            if data.instances is not None:
+                self.instances = data.instances.copy()
+            else:
+                self.instances = np.zeros(len(data.sections), scenes.INSTANCE_DTYPE)
+                self.instances["id"] = np.arange(len(data.sections))
+                self.instances["transform"] = np.eye(4, dtype=np.float32).reshape(-1)
+                self.instances["transform_it"] = np.eye(4, dtype=np.float32).reshape(-1)
 
     @classmethod
-    def from_scene(cls, context, scene, bvh=BVH2):
-        return cls(context, scene, bvh=bvh)
+    def from_scene(cls, context, scene, bvh=BVH2, dynamic=False):
+        return cls(context, scene, bvh=bvh, dynamic=dynamic)
+
+    def blas_transform(self, transform, index):
+        """Section `index` gets `transform` (4x4, row-major numpy
+        convention: M @ p) and its inverse transpose; applied by the next
+        tlas_regenerate."""
+        self.instances[index] = instance_from_transform(transform, int(self.instances["id"][index]))
+        check(lib().solrt_scene_set_instances(self.handle, self.instances.ctypes.data, len(self.instances)))
+
+    def blas_transforms(self, transforms):
+        for i, t in enumerate(transforms):
+            self.instances[i] = instance_from_transform(t, int(self.instances["id"][i]))
+        check(lib().solrt_scene_set_instances(self.handle, self.instances.ctypes.data, len(self.instances)))
+
+    def set_instances(self, instances):
+        self.instances = np.ascontiguousarray(instances).copy()
+        check(lib().solrt_scene_set_instances(self.handle, self.instances.ctypes.data, len(self.instances)))
 
     def close(self):
         if getattr(self, "handle", None):
@@ -295,9 +341,14 @@ class SceneDescription:
     def build_bvh(self, bvh=BVH2, leaf_max=0):
         check(lib().solrt_scene_build_bvh(self.handle, ctypes.byref(BvhDesc(kind=bvh, leaf_max=leaf_max))))
 
-    def tlas_regenerate(self):
-        """Rebuilds the acceleration structure with its current kind."""
-        self.build_bvh(self.bvh_info().kind)
+    def tlas_regenerate(self, mode=REGEN_REBUILD):
+        """Dynamic scene: applies the staged instance transforms on the
+        device and rebuilds (or refits) the BVH. Static scene: rebuilds the
+        BVH with its current kind."""
+        if self.dynamic:
+            check(lib().solrt_scene_regenerate(self.handle, mode))
+        else:
+            self.build_bvh(self.bvh_info().kind)
 
     def bvh_info(self):
         i = BvhInfo()
@@ -363,6 +414,18 @@ class Image:
         return a.value, b.value
 
 
+def instance_from_transform(transform, id=0):
+    """SceneInstance::update_transform (src/ray/mod.rs:27-30) as a
+    scenes.INSTANCE_DTYPE record; `transform` is a 4x4 array acting as
+    M @ [x, y, z, 1]."""
+    from . import scenes
+    m = np.asarray(transform, np.float32).reshape(4, 4)
+    inst = Instance()
+    check(lib().solrt_instance_from_transform(F16(*[float(x) for x in m.T.reshape(-1)]), int(id),
+                                              ctypes.byref(inst)))
+    return np.frombuffer(bytes(inst), scenes.INSTANCE_DTYPE)[0]
+
+
 def camera_look_at(eye, center, up, vfov_deg, aspect, znear=0.1, zfar=1000.0):
     f3 = ctypes.c_float * 3
     c = Camera()
@@ -379,14 +442,16 @@ def camera_from_view(view16, vfov_deg, aspect, znear=0.1, zfar=1000.0):
 
 def render_params(width, height, spp=8, max_bounces=32, frame=0, accum_start_frame=0, seed=0, job_id=0,
                   miss_mode=MISS_BLACK, material_mode=MATERIAL_REF, accum_mode=ACCUM_REF_MIX,
-                  rng_mode=RNG_REF_STREAM, tmax=0.0, kernel=0):
+                  rng_mode=RNG_REF_STREAM, tmax=0.0, kernel=0, integrator=0):
     """Defaults are the reference's: 8 spp per launch, 32 bounces, black miss,
     pathtrace.rchit materials, running mix, one RNG stream per pixel.
-    kernel: KERNEL_WAVEFRONT (0) or KERNEL_MEGA (1, per-pixel loop)."""
+    kernel: KERNEL_WAVEFRONT (0) or KERNEL_MEGA (1, per-pixel loop).
+    integrator: INTEGRATOR_PATH, INTEGRATOR_DEBUG or INTEGRATOR_AO (the
+    reference's AO pipeline uses spp=4, max_bounces=4)."""
     return RenderParams(width=width, height=height, spp=spp, max_bounces=max_bounces, frame=frame,
                         accum_start_frame=accum_start_frame, seed=seed, job_id=job_id, miss_mode=miss_mode,
                         material_mode=material_mode, accum_mode=accum_mode, rng_mode=rng_mode, tmax=tmax,
-                        kernel=kernel)
+                        kernel=kernel, integrator=integrator)
 
 
 def make_jobs(jobs):

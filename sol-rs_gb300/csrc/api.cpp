@@ -244,6 +244,21 @@ solrt_status solrt_context_destroy(solrt_context* ctx) {
 
 void* solrt_context_stream(solrt_context* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
 
+solrt_status solrt_context_set_blue_noise(solrt_context* ctx, const uint8_t* rgba8, uint32_t width,
+                                          uint32_t height) {
+    CHECK_ARG(ctx && rgba8, "null argument");
+    CHECK_ARG(width > 0 && height > 0 && (uint64_t)width * height <= (1ull << 26), "bad texture size");
+    SOLRT_CUDA(cudaSetDevice(ctx->device));
+    SOLRT_CUDA(cudaStreamSynchronize(ctx->stream));  // launches in flight may read the old texture
+    SOLRT_TRY(ctx->blue_noise.alloc(4ull * width * height));
+    SOLRT_CUDA(cudaMemcpyAsync(ctx->blue_noise.ptr, rgba8, 4ull * width * height, cudaMemcpyHostToDevice,
+                               ctx->stream));
+    SOLRT_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->noise_w = width;
+    ctx->noise_h = height;
+    return SOLRT_OK;
+}
+
 solrt_status solrt_synchronize(solrt_context* ctx) {
     CHECK_ARG(ctx, "null context");
     SOLRT_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -307,15 +322,34 @@ solrt_status solrt_scene_create(solrt_context* ctx, const solrt_scene_desc* d, c
         nt += sec.index_count / 3;
     }
     CHECK_ARG(nv < (1ull << 31) && nt < (1ull << 31), "scene too large");
+    const bool dynamic = bvh && (bvh->flags & SOLRT_BVH_DYNAMIC);
     std::vector<float4> pos(nv), nrm(nv), col(nv);
+    std::vector<float4> opos(dynamic ? nv : 0), onrm(dynamic ? nv : 0);
+    std::vector<uint32_t> vsec_start(dynamic ? d->section_count : 0);
+    std::vector<solrt_instance> inst(dynamic ? d->section_count : 0);
     std::vector<uint4> tri(nt);
     uint64_t vb = 0, tb = 0;
     for (uint32_t s = 0; s < d->section_count; ++s) {
         const solrt_section& sec = d->sections[s];
         const float* T = d->instances ? d->instances[s].transform : ident;
         const float* Tit = d->instances ? d->instances[s].transform_it : ident;
+        if (dynamic) {
+            vsec_start[s] = (uint32_t)vb;
+            if (d->instances) {
+                inst[s] = d->instances[s];
+            } else {
+                inst[s] = solrt_instance{};
+                inst[s].id = s;
+                std::memcpy(inst[s].transform, ident, sizeof(ident));
+                std::memcpy(inst[s].transform_it, ident, sizeof(ident));
+            }
+        }
         for (uint32_t v = 0; v < sec.vertex_count; ++v) {
             const solrt_vertex& in = d->vertices[sec.vertex_offset + v];
+            if (dynamic) {
+                opos[vb + v] = make_float4(in.pos[0], in.pos[1], in.pos[2], 0.0f);
+                onrm[vb + v] = make_float4(in.normal[0], in.normal[1], in.normal[2], 0.0f);
+            }
             float o[4];
             mat4_mul(T, in.pos[0], in.pos[1], in.pos[2], 1.0f, o);       // pathtrace.rchit:88-90
             pos[vb + v] = make_float4(o[0], o[1], o[2], 0.0f);
@@ -370,6 +404,23 @@ solrt_status solrt_scene_create(solrt_context* ctx, const solrt_scene_desc* d, c
                         st) != cudaSuccess) {
         set_error("scene upload failed");
         return fail(SOLRT_ERR_DEVICE);
+    }
+    sc->section_count = d->section_count;
+    if (dynamic) {
+        sc->dynamic = true;
+        const size_t ns = d->section_count;
+        if ((s = sc->opos.alloc(16 * nv)) || (s = sc->onrm.alloc(16 * nv)) ||
+            (s = sc->vsec_start.alloc(4 * ns)) || (s = sc->instances.alloc(sizeof(solrt_instance) * ns)))
+            return fail(s);
+        if ((nv && (cudaMemcpyAsync(sc->opos.ptr, opos.data(), 16 * nv, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+                    cudaMemcpyAsync(sc->onrm.ptr, onrm.data(), 16 * nv, cudaMemcpyHostToDevice, st) != cudaSuccess)) ||
+            (ns && (cudaMemcpyAsync(sc->vsec_start.ptr, vsec_start.data(), 4 * ns, cudaMemcpyHostToDevice, st) !=
+                        cudaSuccess ||
+                    cudaMemcpyAsync(sc->instances.ptr, inst.data(), sizeof(solrt_instance) * ns,
+                                    cudaMemcpyHostToDevice, st) != cudaSuccess))) {
+            set_error("scene upload failed");
+            return fail(SOLRT_ERR_DEVICE);
+        }
     }
     if (cudaStreamSynchronize(st) != cudaSuccess) {
         set_error("scene upload failed");
@@ -427,8 +478,50 @@ solrt_status solrt_scene_bvh_export(solrt_scene* scene, void* nodes, size_t node
 solrt_status solrt_scene_bytes(solrt_scene* scene, uint64_t* out) {
     CHECK_ARG(scene && out, "null argument");
     *out = scene->vpos.bytes + scene->vnrm.bytes + scene->vcol.bytes + scene->tri_idx.bytes +
-           scene->materials.bytes + scene->nodes.bytes + scene->tri_wt.bytes;
+           scene->materials.bytes + scene->nodes.bytes + scene->tri_wt.bytes + scene->opos.bytes +
+           scene->onrm.bytes + scene->vsec_start.bytes + scene->instances.bytes + scene->topo_order.bytes +
+           scene->topo_child.bytes + scene->topo_par_int.bytes + scene->topo_par_leaf.bytes +
+           scene->topo_range.bytes;
     return SOLRT_OK;
+}
+
+solrt_status solrt_instance_from_transform(const float transform[16], uint32_t id, solrt_instance* out) {
+    CHECK_ARG(transform && out, "null argument");
+    // SceneInstance::update_transform: transform_it = inverse(T)^T
+    // (src/ray/mod.rs:27-30), in FP64 and rounded once
+    double m[16], inv[16];
+    for (int i = 0; i < 16; ++i) m[i] = transform[i];
+    bool ok = false;
+    inverse4(m, inv, &ok);
+    CHECK_ARG(ok, "singular instance transform");
+    *out = solrt_instance{};
+    out->id = id;
+    for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < 4; ++r) {
+            out->transform[c * 4 + r] = transform[c * 4 + r];
+            out->transform_it[c * 4 + r] = (float)inv[r * 4 + c];
+        }
+    return SOLRT_OK;
+}
+
+solrt_status solrt_scene_set_instances(solrt_scene* scene, const solrt_instance* instances, uint32_t count) {
+    CHECK_ARG(scene && instances, "null argument");
+    CHECK_ARG(scene->dynamic, "scene was not created with SOLRT_BVH_DYNAMIC");
+    CHECK_ARG(count == scene->section_count, "instance count must equal the section count");
+    if (count == 0) return SOLRT_OK;
+    SOLRT_CUDA(cudaSetDevice(scene->ctx->device));
+    // pageable source: the call returns once the host array has been staged
+    SOLRT_CUDA(cudaMemcpyAsync(scene->instances.ptr, instances, sizeof(solrt_instance) * count,
+                               cudaMemcpyHostToDevice, scene->ctx->stream));
+    return SOLRT_OK;
+}
+
+solrt_status solrt_scene_regenerate(solrt_scene* scene, uint32_t mode) {
+    CHECK_ARG(scene, "null scene");
+    CHECK_ARG(scene->dynamic, "scene was not created with SOLRT_BVH_DYNAMIC");
+    CHECK_ARG(mode == SOLRT_REGEN_REBUILD || mode == SOLRT_REGEN_REFIT, "unknown regenerate mode");
+    SOLRT_CUDA(cudaSetDevice(scene->ctx->device));
+    return regenerate_scene(*scene->ctx, *scene, mode);
 }
 
 solrt_status solrt_camera_look_at(const float eye[3], const float center[3], const float up[3], float vfov_deg,

@@ -430,6 +430,14 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
         SOLRT_CUDA(cudaStreamSynchronize(st));
         sc.info.depth = n > 1 ? dh : 1;
     }
+    sc.desc = desc;
+    if (sc.dynamic) {  // the topology stays for solrt_scene_regenerate(REFIT)
+        sc.topo_order.adopt(vals[cur]);
+        sc.topo_child.adopt(child);
+        sc.topo_par_int.adopt(par_int);
+        sc.topo_par_leaf.adopt(par_leaf);
+        sc.topo_range.adopt(range);
+    }
     sc.info.tri_bytes = sc.tri_wt.bytes;
     sc.info.shade_bytes = sc.vpos.bytes + sc.vnrm.bytes + sc.vcol.bytes + sc.tri_idx.bytes + sc.materials.bytes;
     SOLRT_CUDA(cudaEventRecord(ctx.ev1, st));
@@ -442,6 +450,115 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
         return SOLRT_ERR_CAPACITY;
     }
     return SOLRT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Dynamic scenes (solrt_scene_set_instances + solrt_scene_regenerate): the
+// per-frame instance transforms of SceneDescription::blas_transforms and
+// tlas_regenerate (src/ray/mod.rs:162-181).
+// ---------------------------------------------------------------------------
+
+namespace {
+
+// World-space vertex v from its object-space copy and the instance of its
+// section: the flattening of solrt_scene_create (pathtrace.rchit:84-90
+// applied once per vertex), with the same operation order (mat4_mul), so a
+// regenerated scene equals one created with these instances bit for bit.
+__global__ void k_apply_instances(const float4* __restrict__ opos, const float4* __restrict__ onrm,
+                                  const uint32_t* __restrict__ vsec_start, uint32_t nsec,
+                                  const solrt_instance* __restrict__ inst, uint32_t nv, float4* __restrict__ vpos,
+                                  float4* __restrict__ vnrm) {
+    const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    // last section whose first vertex is <= v (empty sections share starts
+    // with their successor and are skipped by taking the last)
+    uint32_t lo = 0, hi = nsec - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (vsec_start[mid] <= v) lo = mid;
+        else hi = mid - 1;
+    }
+    const solrt_instance& in = inst[lo];
+    float o[4];
+    const float4 p = opos[v];
+    mat4_mul(in.transform, p.x, p.y, p.z, 1.0f, o);
+    vpos[v] = make_float4(o[0], o[1], o[2], 0.0f);
+    const float4 n = onrm[v];
+    mat4_mul(in.transform_it, n.x, n.y, n.z, 0.0f, o);
+    vnrm[v] = make_float4(o[0], o[1], o[2], 0.0f);
+}
+
+// New boxes for the kept topology: the refit pass of build_bvh over the
+// moved triangles, then (BVH8) a fresh collapse of the refitted tree.
+solrt_status refit_bvh(Context& ctx, Scene& sc) {
+    const uint32_t n = sc.tri_count;
+    const uint32_t ni = n > 1 ? n - 1 : 1;
+    cudaStream_t st = ctx.stream;
+    SOLRT_CUDA(cudaEventRecord(ctx.ev0, st));
+    const bool b8 = sc.info.kind == SOLRT_BVH8_Q8;
+    DeviceBuffer flags, nbox, nodes2, tri2;
+    SOLRT_TRY(flags.alloc(sizeof(unsigned int) * (size_t)ni));
+    SOLRT_TRY(nbox.alloc(2 * sizeof(float4) * (size_t)ni));
+    float4* nodes_out = sc.nodes.as<float4>();
+    float4* tri_out = sc.tri_wt.as<float4>();
+    if (b8) {
+        SOLRT_TRY(nodes2.alloc(4 * sizeof(float4) * (size_t)ni));
+        SOLRT_TRY(tri2.alloc(3 * sizeof(float4) * (size_t)n));
+        nodes_out = nodes2.as<float4>();
+        tri_out = tri2.as<float4>();
+    }
+    SOLRT_CUDA(cudaMemsetAsync(flags.ptr, 0, flags.bytes, st));
+    k_refit<<<blocks_for(n, 256), 256, 0, st>>>(sc.vpos.as<float4>(), sc.tri_idx.as<uint4>(),
+                                                sc.topo_order.as<uint32_t>(), sc.topo_child.as<uint32_t>(),
+                                                sc.topo_par_int.as<uint32_t>(), sc.topo_par_leaf.as<uint32_t>(), n,
+                                                flags.as<unsigned int>(), nbox.as<float4>(), nodes_out, tri_out);
+    ++ctx.launches;
+    SOLRT_CUDA(cudaGetLastError());
+    if (b8) {
+        Bvh8BuildInput in;
+        in.n = n;
+        in.child = sc.topo_child.as<uint32_t>();
+        in.nbox = nbox.as<float4>();
+        in.range = sc.topo_range.as<uint2>();
+        in.tri_wt_leaf = tri2.as<float4>();
+        in.leaf_max = sc.desc.leaf_max == 0 ? 3u : std::min(3u, sc.desc.leaf_max);
+        DeviceBuffer nodes8, tri8;
+        uint32_t node_count = 0, depth8 = 0;
+        SOLRT_TRY(build_bvh8(ctx, in, nodes8, tri8, &node_count, &depth8));
+        if (depth8 > SOLRT_BVH8_STACK) {
+            set_error("BVH8 depth %u exceeds the traversal stack (%d)", depth8, SOLRT_BVH8_STACK);
+            return SOLRT_ERR_CAPACITY;
+        }
+        sc.nodes.adopt(nodes8);
+        sc.tri_wt.adopt(tri8);
+        sc.info.node_count = node_count;
+        sc.info.depth = depth8;
+        sc.info.node_bytes = (uint64_t)node_count * 80u;
+        sc.info.tri_bytes = sc.tri_wt.bytes;
+    }
+    SOLRT_CUDA(cudaEventRecord(ctx.ev1, st));
+    SOLRT_CUDA(cudaEventSynchronize(ctx.ev1));
+    float ms = 0.0f;
+    SOLRT_CUDA(cudaEventElapsedTime(&ms, ctx.ev0, ctx.ev1));
+    sc.info.build_ms = ms;
+    return SOLRT_OK;
+}
+
+}  // namespace
+
+solrt_status regenerate_scene(Context& ctx, Scene& sc, uint32_t mode) {
+    cudaGetLastError();  // launch errors below must be this call's own
+    cudaStream_t st = ctx.stream;
+    if (sc.vertex_count) {
+        k_apply_instances<<<blocks_for(sc.vertex_count, 256), 256, 0, st>>>(
+            sc.opos.as<float4>(), sc.onrm.as<float4>(), sc.vsec_start.as<uint32_t>(), sc.section_count,
+            sc.instances.as<solrt_instance>(), sc.vertex_count, sc.vpos.as<float4>(), sc.vnrm.as<float4>());
+        ++ctx.launches;
+        SOLRT_CUDA(cudaGetLastError());
+    }
+    if (mode == SOLRT_REGEN_REFIT && sc.tri_count > 0 && sc.topo_order.ptr && sc.nodes.ptr)
+        return refit_bvh(ctx, sc);
+    return build_bvh(ctx, sc, sc.desc);
 }
 
 // ---------------------------------------------------------------------------

@@ -59,6 +59,15 @@ struct DeviceBuffer {
         return SOLRT_OK;
     }
     template <class T> T* as() const { return reinterpret_cast<T*>(ptr); }
+    // Takes over `o`'s allocation (releasing this one's).
+    void adopt(DeviceBuffer& o) {
+        if (&o == this) return;
+        release();
+        ptr = o.ptr;
+        bytes = o.bytes;
+        o.ptr = nullptr;
+        o.bytes = 0;
+    }
 };
 
 // Statistics and error word kept on the device.
@@ -95,7 +104,8 @@ struct DevJob {
     uint32_t width, height, spp, frame, start, seed, job_id, rng_mode;
     uint32_t miss_mode, material_mode, max_bounces, accum_mode;
     float tmax;
-    uint32_t pad[3];
+    uint32_t integrator, noise_w, noise_h;
+    const uchar4* noise;
     float4* accum;
     uchar4* rgba8;
     float4* fsum;
@@ -161,6 +171,9 @@ struct Context {
     uint32_t block_size = 0;
     DeviceBuffer q_o[2], q_d[2], q_thr[2], q_meta[2];
     DeviceBuffer hits, rad, ctl, stats, trace_work;
+    DeviceBuffer blue_noise;  // RGBA8 texels of SOLRT_INTEGRATOR_AO
+    DeviceBuffer sibling_job;  // one-job table of DEBUG / AO launches
+    uint32_t noise_w = 0, noise_h = 0;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     uint64_t launches = 0;
     double last_render_ms = 0.0;
@@ -214,6 +227,15 @@ struct Scene {
     DeviceBuffer vpos, vnrm, vcol, tri_idx, materials;
     DeviceBuffer nodes, tri_wt;
     solrt_bvh_info info{};
+    solrt_bvh_desc desc{};
+    // SOLRT_BVH_DYNAMIC: object-space positions / normals (float4 per
+    // vertex), the first vertex of each section (section_count + 1 entries),
+    // the staged instances, and the BVH2 topology of the last build (leaf
+    // order, children, parents, key ranges) for refits.
+    bool dynamic = false;
+    uint32_t section_count = 0;
+    DeviceBuffer opos, onrm, vsec_start, instances;
+    DeviceBuffer topo_order, topo_child, topo_par_int, topo_par_leaf, topo_range;
     DevScene view() const {
         DevScene d;
         d.tri_count = tri_count;
@@ -238,6 +260,9 @@ struct Image {
 
 // bvh_build.cu
 solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc);
+// Dynamic scenes: world-space vertices from object space and the staged
+// instances, then a rebuild or a refit of the kept topology.
+solrt_status regenerate_scene(Context& ctx, Scene& sc, uint32_t mode);
 
 // trace.cu
 solrt_status launch_trace_rays(Context& ctx, const Scene& sc, const solrt_ray* rays, uint32_t n, solrt_hit* hits);

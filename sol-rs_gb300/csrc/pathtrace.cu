@@ -227,6 +227,150 @@ __device__ __forceinline__ unsigned char to_unorm8(float c) {
     return (unsigned char)(cl * 255.0f + 0.5f);
 }
 
+// ---------------------------------------------------------------------------
+// Sibling integrators over the same traversal (one thread per pixel, the
+// structure of their ray-generation shaders).
+// ---------------------------------------------------------------------------
+
+// Primary direction of debug.rgen:20-27 / ao.rgen:56-61 for pixel position
+// (px, py): origin and direction through the inverse matrices.
+__device__ __forceinline__ void pixel_ray(const DevJob& J, float px, float py, float org[4], float dir[4]) {
+    const float ux = px / __uint2float_rn(J.width), uy = py / __uint2float_rn(J.height);
+    const float dx = ux * 2.0f - 1.0f, dy = uy * 2.0f - 1.0f;
+    float tgt[4];
+    mat4_mul(J.vinv, 0.0f, 0.0f, 0.0f, 1.0f, org);
+    mat4_mul(J.pinv, dx, dy, 1.0f, 1.0f, tgt);
+    const f3 tn = normalize(f3{tgt[0], tgt[1], tgt[2]});
+    mat4_mul(J.vinv, tn.x, tn.y, tn.z, 0.0f, dir);
+}
+
+template <int KIND>
+__device__ __forceinline__ void trace_one(const TravScene& ts, float ox, float oy, float oz, float dx, float dy,
+                                          float dz, float tmin, float tmax, HitRec& h, TraceCounters& cnt,
+                                          uint32_t& ef) {
+    if (KIND == SOLRT_BVH8_Q8) trace_bvh8<false>(ts, ox, oy, oz, dx, dy, dz, tmin, tmax, h, cnt, ef);
+    else trace_bvh2_ray(ts, ox, oy, oz, dx, dy, dz, tmin, tmax, h, cnt, ef);
+}
+
+__device__ __forceinline__ void flush_stats(DevStats* stats, uint32_t segs, uint32_t paths, uint32_t fb,
+                                            uint32_t ef) {
+    const uint32_t wsegs = __reduce_add_sync(0xffffffffu, segs);
+    const uint32_t wpaths = __reduce_add_sync(0xffffffffu, paths);
+    const uint32_t wfb = __reduce_add_sync(0xffffffffu, fb);
+    const uint32_t wef = __reduce_or_sync(0xffffffffu, ef);
+    if ((threadIdx.x & 31) == 0) {
+        if (wsegs) atomicAdd(&stats->segments, (unsigned long long)wsegs);
+        if (wpaths) atomicAdd(&stats->paths, (unsigned long long)wpaths);
+        if (wfb) atomicAdd(&stats->fp64_fallbacks, (unsigned long long)wfb);
+        if (wef) atomicOr(&stats->eflags, wef);
+    }
+}
+
+// debug.rgen:18-36, debug.rchit:9-13, debug.rmiss: barycentrics of the
+// primary hit through the pixel centre, else the ray direction; stored
+// without accumulation (imageStore of vec4(hitValue, 0)).
+template <int KIND>
+__global__ void __launch_bounds__(128) k_debug(const DevJob* __restrict__ job, DevStats* stats) {
+    const DevJob& J = *job;
+    const uint32_t npix = J.width * J.height;
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t segs = 0, ef = 0;
+    TraceCounters cnt{0, 0, 0};
+    if (pix < npix) {
+        const TravScene ts = trav_scene(J.sc);
+        const uint32_t x = pix % J.width, y = pix / J.width;
+        float org[4], dir[4];
+        pixel_ray(J, __uint2float_rn(x) + 0.5f, __uint2float_rn(y) + 0.5f, org, dir);
+        HitRec h;
+        trace_one<KIND>(ts, org[0], org[1], org[2], dir[0], dir[1], dir[2], 0.001f, 1000.0f, h, cnt, ef);
+        ++segs;
+        float4 v = make_float4(dir[0], dir[1], dir[2], 0.0f);
+        if (h.prim != SOLRT_NO_HIT) v = make_float4((1.0f - h.u) - h.v, h.u, h.v, 0.0f);
+        J.accum[pix] = v;
+        J.rgba8[pix] = make_uchar4(to_unorm8(v.x), to_unorm8(v.y), to_unorm8(v.z), 0);
+    }
+    flush_stats(stats, segs, pix < npix ? 1u : 0u, cnt.fallbacks, ef);
+}
+
+// ao.rgen:37-83, ao.rchit:53-88, ao.rmiss: `spp` jittered samples; each
+// follows cosine-weighted rays (directions from the blue-noise texture)
+// until a miss or max_bounces + 1 hits, counting every hit after the first.
+template <int KIND>
+__global__ void __launch_bounds__(128) k_ao(const DevJob* __restrict__ job, DevStats* stats) {
+    const DevJob& J = *job;
+    const uint32_t npix = J.width * J.height;
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t segs = 0, ef = 0;
+    TraceCounters cnt{0, 0, 0};
+    if (pix < npix) {
+        const DevScene& sc = J.sc;
+        const TravScene ts = trav_scene(sc);
+        const uint32_t x = pix % J.width, y = pix / J.width;
+        uint32_t rng = tea(pix, J.frame);                                     // ao.rgen:49
+        const float max_samples = __uint2float_rn(J.max_bounces);
+        const float tw = __uint2float_rn(J.noise_w), th = __uint2float_rn(J.noise_h);
+        f3 ao{0.0f, 0.0f, 0.0f};
+        for (uint32_t i = 0; i < J.spp; ++i) {
+            const float j0 = next_rand(rng);                                  // nextRand2 (ao.rgen:53)
+            const float j1 = next_rand(rng);
+            float org[4], dir[4];
+            pixel_ray(J, __uint2float_rn(x) + j0, __uint2float_rn(y) + j1, org, dir);
+            f3 o{org[0], org[1], org[2]}, d{dir[0], dir[1], dir[2]};
+            float tmin = glsl_max(1.0f, length(o)) * 1e-3f, tmax = 10000.0f;  // preparePayload
+            float hv = 0.0f;
+            uint32_t depth = 0;
+            for (;;) {
+                HitRec h;
+                trace_one<KIND>(ts, o.x, o.y, o.z, d.x, d.y, d.z, tmin, tmax, h, cnt, ef);
+                ++segs;
+                if (h.prim == SOLRT_NO_HIT) break;                            // ao.rmiss
+                if (h.prim >= sc.tri_count) {
+                    ef |= SOLRT_EFLAG_INDEX;
+                    break;
+                }
+                const uint4 ti = __ldg(sc.tri_idx + h.prim);
+                const float b1 = h.u, b2 = h.v;
+                const float b0 = (1.0f - b1) - b2;
+                const float4 n0 = __ldg(sc.vnrm + ti.x), n1 = __ldg(sc.vnrm + ti.y), n2 = __ldg(sc.vnrm + ti.z);
+                const float4 p0 = __ldg(sc.vpos + ti.x), p1 = __ldg(sc.vpos + ti.y), p2 = __ldg(sc.vpos + ti.z);
+                const f3 normal =
+                    normalize(f3{n0.x, n0.y, n0.z} * b0 + f3{n1.x, n1.y, n1.z} * b1 + f3{n2.x, n2.y, n2.z} * b2);
+                const f3 pos = f3{p0.x, p0.y, p0.z} * b0 + f3{p1.x, p1.y, p1.z} * b1 + f3{p2.x, p2.y, p2.z} * b2;
+                const f3 no = pos + 0.00001f * d;                             // ao.rchit:78
+                // getBlueRand2(depth + depth * sampleId) (ao.rchit:43-49)
+                const uint32_t bi = depth + depth * i;
+                const float r0 = next_rand(rng);
+                const float r1 = next_rand(rng);
+                float cx = __uint2float_rn(x) + r0 * tw, cy = __uint2float_rn(y) + r1 * th;
+                cx = cx - tw * floorf(cx / tw);                               // GLSL mod
+                cy = cy - th * floorf(cy / th);
+                const int ix = min(max((int)cx, 0), (int)J.noise_w - 1);
+                const int iy = min(max((int)cy, 0), (int)J.noise_h - 1);
+                const uchar4 t = __ldg(J.noise + (size_t)iy * J.noise_w + ix);
+                const float blue[4] = {__uint2float_rn(t.x) / 255.0f, __uint2float_rn(t.y) / 255.0f,
+                                       __uint2float_rn(t.z) / 255.0f, __uint2float_rn(t.w) / 255.0f};
+                const f3 hit_n = normal * glsl_sign(dot(-d, normal));
+                d = sample_cosine(hit_n, blue[bi % 4], blue[(bi + 1) % 4]);
+                o = no;
+                tmin = 0.001f;
+                tmax = 10.0f;
+                if (depth > 0) hv = hv + 1.0f;
+                ++depth;
+                if (depth > J.max_bounces) break;                             // ao.rgen:75
+            }
+            ao = ao + (1.0f / max_samples) * f3{hv, hv, hv};                  // ao.rgen:77
+        }
+        const float n = __uint2float_rn(J.spp);
+        f3 color{1.0f - ao.x / n, 1.0f - ao.y / n, 1.0f - ao.z / n};
+        const float a = 1.0f / __uint2float_rn(J.frame - J.start + 1u);      // ao.rgen:79-82
+        const float4 old = J.accum[pix];
+        color = mix(f3{old.x, old.y, old.z}, color, a);
+        J.accum[pix] = make_float4(color.x, color.y, color.z, 1.0f);
+        J.rgba8[pix] = make_uchar4(to_unorm8(color.x), to_unorm8(color.y), to_unorm8(color.z), 255);
+    }
+    flush_stats(stats, segs, pix < npix ? J.spp : 0u, cnt.fallbacks, ef);
+}
+
 // rgen:88-103 (REF_MIX) or the Kahan mean, for every pixel of every job.
 __global__ void k_finalize(const DevJob* __restrict__ jobs, const uint32_t* __restrict__ job_pix, uint32_t njobs,
                            uint32_t pixels) {
@@ -309,6 +453,12 @@ solrt_status check_params(const Context& ctx, const Scene& sc, const Image& img,
     }
     if (!(p.tmax >= 0.0f)) { set_error("tmax must be >= 0"); return SOLRT_ERR_INVALID; }
     if (p.kernel > SOLRT_KERNEL_MEGA) { set_error("unknown kernel"); return SOLRT_ERR_INVALID; }
+    if (p.integrator > SOLRT_INTEGRATOR_AO) { set_error("unknown integrator"); return SOLRT_ERR_INVALID; }
+    if (p.integrator == SOLRT_INTEGRATOR_AO) {
+        if (!ctx.blue_noise.ptr) { set_error("the AO integrator needs solrt_context_set_blue_noise"); return SOLRT_ERR_INVALID; }
+        if (p.max_bounces < 1) { set_error("the AO integrator needs max_bounces >= 1"); return SOLRT_ERR_INVALID; }
+        if (p.frame + 1u - p.accum_start_frame == 0u) { set_error("frame + 1 - accum_start_frame is zero"); return SOLRT_ERR_INVALID; }
+    }
     return SOLRT_OK;
 }
 
@@ -406,6 +556,7 @@ solrt_status batch_plan(Context& ctx, const solrt_job* jobs, uint32_t n, uint32_
         const Image& img = *static_cast<const Image*>(reinterpret_cast<const void*>(jb.image));
         SOLRT_TRY(check_params(ctx, sc, img, jb.params));
         if (jb.params.kernel != SOLRT_KERNEL_WAVEFRONT) { set_error("job %u: batches run the wavefront kernel", j); return SOLRT_ERR_INVALID; }
+        if (jb.params.integrator != SOLRT_INTEGRATOR_PATH) { set_error("job %u: batches run the path integrator", j); return SOLRT_ERR_INVALID; }
         if (j == 0) b.kind = sc.info.kind;
         if (sc.info.kind != b.kind) { set_error("job %u: all scenes of a batch need the same BVH kind", j); return SOLRT_ERR_INVALID; }
         b.jobs.push_back(make_job(sc, img, jb.camera, jb.params));
@@ -551,11 +702,46 @@ DevJob job_for(const Scene& sc, const Image& img, const solrt_camera& cam, const
 }
 
 solrt_status check_job(const Context& ctx, const Scene& sc, const Image& img, const solrt_render_params& p) {
+    if (p.integrator != SOLRT_INTEGRATOR_PATH) {
+        set_error("the server runs the path integrator");
+        return SOLRT_ERR_INVALID;
+    }
     return check_params(ctx, sc, img, p);
+}
+
+// DEBUG / AO: one per-pixel launch over a one-job table.
+static solrt_status render_sibling(Context& ctx, const Scene& sc, const solrt_camera& cam,
+                                   const solrt_render_params& p, Image& img) {
+    SOLRT_TRY(check_params(ctx, sc, img, p));
+    DevJob J = make_job(sc, img, cam, p);
+    J.integrator = p.integrator;
+    J.noise = ctx.blue_noise.as<uchar4>();
+    J.noise_w = ctx.noise_w;
+    J.noise_h = ctx.noise_h;
+    cudaGetLastError();
+    SOLRT_TRY(ctx.sibling_job.alloc(sizeof(DevJob)));
+    SOLRT_CUDA(cudaMemcpyAsync(ctx.sibling_job.ptr, &J, sizeof(DevJob), cudaMemcpyHostToDevice, ctx.stream));
+    const uint32_t npix = p.width * p.height;
+    const DevJob* dj = ctx.sibling_job.as<DevJob>();
+    DevStats* stats = ctx.stats.as<DevStats>();
+    SOLRT_CUDA(cudaEventRecord(ctx.ev0, ctx.stream));
+    const bool b8 = sc.info.kind == SOLRT_BVH8_Q8;
+    if (p.integrator == SOLRT_INTEGRATOR_DEBUG) {
+        if (b8) k_debug<SOLRT_BVH8_Q8><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
+        else k_debug<SOLRT_BVH2><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
+    } else {
+        if (b8) k_ao<SOLRT_BVH8_Q8><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
+        else k_ao<SOLRT_BVH2><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
+    }
+    ++ctx.launches;
+    SOLRT_CUDA(cudaGetLastError());
+    SOLRT_CUDA(cudaEventRecord(ctx.ev1, ctx.stream));
+    return SOLRT_OK;
 }
 
 solrt_status render_frame(Context& ctx, const Scene& sc, const solrt_camera& cam, const solrt_render_params& p,
                           Image& img) {
+    if (p.integrator != SOLRT_INTEGRATOR_PATH) return render_sibling(ctx, sc, cam, p, img);
     solrt_job jb;
     jb.scene = reinterpret_cast<solrt_scene*>(const_cast<Scene*>(&sc));
     jb.image = reinterpret_cast<solrt_image*>(&img);

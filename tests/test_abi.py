@@ -58,6 +58,21 @@ def test_camera_is_host_math(solrt):
         solrt.camera_look_at((0, 0, 1), (0, 0, 0), (0, 1, 0), 0.0, 1.0)
 
 
+def test_instance_from_transform_is_host_math(solrt):
+    """SceneInstance::update_transform: transform_it = inverse(T)^T, FP64
+    then rounded; a singular transform is an error."""
+    a = np.radians(33.0)
+    M = np.array([[np.cos(a), 0, np.sin(a), 0.3], [0, 2.0, 0, -1.0], [-np.sin(a), 0, np.cos(a), 4.0], [0, 0, 0, 1]])
+    inst = solrt.instance_from_transform(M, 7)
+    assert inst["id"] == 7
+    assert np.array_equal(inst["transform"], M.astype(np.float32).T.reshape(-1))
+    want = np.linalg.inv(M.astype(np.float32).astype(np.float64)).T
+    assert np.array_equal(inst["transform_it"], want.astype(np.float32).T.reshape(-1)) or \
+        np.allclose(inst["transform_it"], want.astype(np.float32).T.reshape(-1), rtol=2e-7, atol=1e-7)
+    with pytest.raises(solrt.SolrtError, match="singular"):
+        solrt.instance_from_transform(np.zeros((4, 4)))
+
+
 def test_context_without_gpu_fails_cleanly(solrt):
     try:
         import torch

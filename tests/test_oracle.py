@@ -193,3 +193,47 @@ def test_ref_stream_matches_sequential_samples(oracle, solrt):
         s = s + samples[:, k, :3]
     mean = np.float32(1.0 / 4) * s
     assert np.array_equal(mean.reshape(16, 16, 3), acc[..., :3])
+
+
+def test_debug_integrator_properties(oracle, solrt):
+    """debug.rgen/.rchit/.rmiss: hits give barycentrics that sum to 1 and
+    agree with the ray-file trace of the same pixel-centre rays; misses give
+    the ray direction."""
+    d = S.cornell()
+    sc = oracle.OracleScene(d)
+    cam = oracle.camera_look_at(d.camera["eye"], d.camera["center"], d.camera["up"], d.camera["vfov"], 1.0)
+    p = _params(24, 24, 1, integrator=solrt.INTEGRATOR_DEBUG)
+    acc, rgba8, st = sc.render(cam, p)
+    assert st.segments == 24 * 24
+    assert (acc[..., 3] == 0).all() and (rgba8[..., 3] == 0).all()
+    bary = acc[..., :3]
+    hit = np.abs(bary.sum(-1) - 1.0) < 1e-6
+    assert hit.mean() > 0.9                       # the box fills the view
+    assert (bary[hit] >= -1e-6).all()
+    e = oracle.OracleScene(empty_scene())
+    acc_e, _, _ = e.render(cam, p)
+    dirs = acc_e[..., :3]
+    assert np.allclose(np.linalg.norm(dirs, axis=-1), 1.0, atol=1e-5)
+
+
+def test_ao_integrator_properties(oracle, solrt):
+    """ao.rgen: an empty scene is fully open (1.0); inside the closed-top
+    Cornell box occlusion darkens every pixel that sees a wall; the running
+    mix of two frames equals their mean."""
+    noise = np.random.default_rng(3).integers(0, 256, (32, 32, 4), dtype=np.uint8)
+    d = S.cornell()
+    cam = oracle.camera_look_at(d.camera["eye"], d.camera["center"], d.camera["up"], d.camera["vfov"], 1.0)
+    p0 = _params(16, 16, 4, max_bounces=4, integrator=solrt.INTEGRATOR_AO)
+    e, _, _ = oracle.OracleScene(empty_scene()).render(cam, p0, blue_noise=noise)
+    assert (e[..., :3] == 1.0).all()
+    sc = oracle.OracleScene(d)
+    a0, _, st = sc.render(cam, p0, blue_noise=noise)
+    assert 0.0 < a0[..., :3].mean() < 1.0 and st.paths == 16 * 16 * 4
+    acc = a0.copy()
+    sc.render(cam, _params(16, 16, 4, max_bounces=4, frame=1, integrator=solrt.INTEGRATOR_AO), accum=acc,
+              blue_noise=noise)
+    a1, _, _ = sc.render(cam, _params(16, 16, 4, max_bounces=4, frame=1, accum_start_frame=1,
+                                      integrator=solrt.INTEGRATOR_AO), blue_noise=noise)
+    assert np.allclose(acc[..., :3], 0.5 * (a0[..., :3] + a1[..., :3]), rtol=1e-5, atol=1e-6)
+    with pytest.raises(ValueError):
+        sc.render(cam, p0)                        # no texture
