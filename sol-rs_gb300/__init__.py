@@ -12,4 +12,4 @@ from .api import (  # noqa: F401
     INTEGRATOR_AO, INTEGRATOR_DEBUG, INTEGRATOR_PATH, Job, KERNEL_MEGA, KERNEL_WAVEFRONT, RenderParams, Renderer, SceneDescription, Server, SolrtError,
     GltfScene, camera_from_view, camera_look_at, check, lib, load_scene, make_jobs, render_params, scene_desc,
 )
-from . import scenes  # noqa: F401
+from . import imageio, scenes  # noqa: F401

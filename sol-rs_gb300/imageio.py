@@ -68,3 +68,75 @@ def to_rgba8(rgb, tonemap=None):
     out[..., :3] = (np.clip(x, 0, 1) * 255.0 + 0.5).astype(np.uint8)
     out[..., 3] = 255
     return out
+
+
+def read_png(path):
+    """Non-interlaced 8- or 16-bit PNG (grey, grey+alpha, RGB, RGBA) ->
+    (h, w, 4) uint8 RGBA, rows in file order; e.g. the blue-noise texture
+    the AO example loads (examples/4-ray-ao.rs:198-201; src/texture.rs:489-492
+    converts it with to_rgba8). 16-bit samples v become round(v * 255 /
+    65535) = (v + 128) // 257."""
+    data = open(path, "rb").read()
+    if data[:8] != b"\x89PNG\r\n\x1a\n":
+        raise ValueError("not a PNG file")
+    pos, idat, hdr = 8, [], None
+    while pos + 8 <= len(data):
+        n, kind = struct.unpack(">I4s", data[pos:pos + 8])
+        body = data[pos + 8:pos + 8 + n]
+        if kind == b"IHDR":
+            hdr = struct.unpack(">IIBBBBB", body)
+        elif kind == b"IDAT":
+            idat.append(body)
+        elif kind == b"IEND":
+            break
+        pos += 12 + n
+    if hdr is None:
+        raise ValueError("PNG without IHDR")
+    w, h, depth, ctype, _, _, interlace = hdr
+    chans = {0: 1, 2: 3, 4: 2, 6: 4}.get(ctype)
+    if depth not in (8, 16) or chans is None or interlace != 0:
+        raise ValueError("unsupported PNG (need 8/16-bit non-interlaced grey/RGB/RGBA)")
+    bpp = chans * depth // 8                     # bytes per pixel (filter unit)
+    stride = w * bpp
+    raw = np.frombuffer(zlib.decompress(b"".join(idat)), np.uint8).reshape(h, 1 + stride)
+    out = np.zeros((h, stride), np.uint8)
+    prev = np.zeros(stride, np.uint8)
+    for y in range(h):
+        f, line = raw[y, 0], raw[y, 1:]
+        if f == 0:
+            cur = line.copy()
+        elif f == 2:
+            cur = (line.astype(np.uint16) + prev).astype(np.uint8)
+        else:
+            cur = np.zeros_like(line)
+            for x in range(stride):        # sub / average / paeth depend on the left neighbour
+                a = int(cur[x - bpp]) if x >= bpp else 0
+                c = int(prev[x - bpp]) if x >= bpp else 0
+                b = int(prev[x])
+                if f == 1:
+                    pred = a
+                elif f == 3:
+                    pred = (a + b) // 2
+                elif f == 4:
+                    p = a + b - c
+                    pa, pb, pc = abs(p - a), abs(p - b), abs(p - c)
+                    pred = a if (pa <= pb and pa <= pc) else (b if pb <= pc else c)
+                else:
+                    raise ValueError("bad PNG filter %d" % f)
+                cur[x] = (int(line[x]) + pred) & 0xFF
+        out[y] = cur
+        prev = cur
+    if depth == 16:
+        v = out.reshape(h, w * chans, 2).astype(np.uint32)
+        px = (((v[..., 0] << 8) | v[..., 1]) + 128) // 257
+        px = px.astype(np.uint8).reshape(h, w, chans)
+    else:
+        px = out.reshape(h, w, chans)
+    rgba = np.zeros((h, w, 4), np.uint8)
+    if chans in (1, 2):
+        rgba[..., :3] = px[..., :1]
+        rgba[..., 3] = px[..., 1] if chans == 2 else 255
+    else:
+        rgba[..., :3] = px[..., :3]
+        rgba[..., 3] = px[..., 3] if chans == 4 else 255
+    return rgba

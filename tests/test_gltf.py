@@ -235,3 +235,66 @@ def test_reference_models(solrt, name):
     assert np.array_equal(np.array(c.projection), np.array(ref.projection))
     if name == "cornell.gltf":
         assert d.tri_count == 32 and len(d.materials) == 8
+
+
+def _png16(path, px16, filters):
+    """Writes a 16-bit RGBA PNG with the given per-row filter types."""
+    import zlib
+    h, w, _ = px16.shape
+    raw = px16.astype(">u2").tobytes()
+    stride = w * 8
+    rows = []
+    prev = bytes(stride)
+    for y in range(h):
+        line = raw[y * stride:(y + 1) * stride]
+        f = filters[y % len(filters)]
+        out = bytearray(stride)
+        for x in range(stride):
+            a = line[x - 8] if x >= 8 else 0
+            b = prev[x]
+            c = prev[x - 8] if x >= 8 else 0
+            if f == 0:
+                pred = 0
+            elif f == 1:
+                pred = a
+            elif f == 2:
+                pred = b
+            elif f == 3:
+                pred = (a + b) // 2
+            else:
+                p = a + b - c
+                pa, pb, pc = abs(p - a), abs(p - b), abs(p - c)
+                pred = a if (pa <= pb and pa <= pc) else (b if pb <= pc else c)
+            out[x] = (line[x] - pred) & 0xFF
+        rows.append(bytes([f]) + bytes(out))
+        prev = line
+
+    def chunk(kind, body):
+        return struct.pack(">I", len(body)) + kind + body + struct.pack(">I", zlib.crc32(kind + body) & 0xFFFFFFFF)
+    with open(path, "wb") as fh:
+        fh.write(b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 16, 6, 0, 0, 0)) +
+                 chunk(b"IDAT", zlib.compress(b"".join(rows))) + chunk(b"IEND", b""))
+
+
+def test_read_png_8_and_16_bit(solrt, tmp_path):
+    io = solrt.imageio
+    x = np.random.default_rng(4).integers(0, 256, (9, 11, 4), dtype=np.uint8)
+    io.write_png(str(tmp_path / "a.png"), x)
+    assert np.array_equal(io.read_png(str(tmp_path / "a.png")), x)
+    px = np.random.default_rng(5).integers(0, 65536, (7, 5, 4), dtype=np.uint32)
+    _png16(str(tmp_path / "b.png"), px, filters=[0, 1, 2, 3, 4])
+    want = ((px + 128) // 257).astype(np.uint8)
+    assert np.array_equal(io.read_png(str(tmp_path / "b.png")), want)
+
+
+def test_reference_blue_noise_texture(solrt):
+    path = "/root/reference/assets/textures/HDR_RGBA_0.png"
+    if not os.path.exists(path):
+        pytest.skip("reference textures not present")
+    from importlib import import_module
+    render = import_module("sol-rs_gb300.render")
+    t = render.load_blue_noise(path)
+    assert t.shape == (256, 256, 4) and t.dtype == np.uint8
+    assert abs(float(t.mean()) - 127.5) < 2.0          # uniform blue noise
+    raw = solrt.imageio.read_png(path)
+    assert np.array_equal(t, raw[::-1])               # Texture2d::new flips rows

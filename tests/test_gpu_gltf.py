@@ -59,3 +59,37 @@ def test_gltf_equals_direct_scene(solrt, ctx, tmp_path):
         solrt.Renderer(ctx).cmd_trace_rays(sc, cam, p, img)
         out.append(img.read()[0])
     assert np.array_equal(out[0].view(np.uint32), out[1].view(np.uint32))
+
+
+@pytest.mark.parametrize("integrator", ["path", "ao", "debug"])
+def test_render_cli_on_gltf(solrt, ctx, tmp_path, integrator):
+    """The headless example command on a written .glb: its PNG equals the
+    RGBA8 image of the same launches made through the Python API."""
+    import importlib
+    render = importlib.import_module("sol-rs_gb300.render")
+    g = _transformed_glb(solrt, tmp_path / "cornell.glb")
+    out = tmp_path / "out.png"
+    args = ["--model", str(tmp_path / "cornell.glb"), "--width", "32", "--height", "24", "--frames", "2",
+            "--integrator", integrator, "--out", str(out)]
+    if integrator == "path":
+        args += ["--sky", "--bounces", "6"]
+    assert render.main(args) == 0
+    png = solrt.imageio.read_png(str(out))
+    cam = g.camera(32 / 24)
+    if integrator == "ao":
+        ctx.set_blue_noise(render.load_blue_noise(None))
+    sc = solrt.SceneDescription(ctx, g.data)
+    img = solrt.Image(ctx, 32, 24)
+    integ = {"path": solrt.INTEGRATOR_PATH, "ao": solrt.INTEGRATOR_AO, "debug": solrt.INTEGRATOR_DEBUG}[integrator]
+    spp, bounces = {"path": (8, 6), "ao": (4, 4), "debug": (1, 1)}[integrator]
+    for f in range(1 if integrator == "debug" else 2):
+        p = solrt.render_params(32, 24, spp=spp, max_bounces=bounces, frame=f, integrator=integ,
+                                miss_mode=solrt.MISS_REF_SKY if integrator == "path" else solrt.MISS_BLACK)
+        solrt.Renderer(ctx).cmd_trace_rays(sc, cam, p, img)
+    _, rgba8 = img.read()
+    if integrator == "debug":
+        rgba8 = rgba8.copy()
+        rgba8[..., 3] = 0
+        png = png.copy()
+        png[..., 3] = 0
+    assert np.array_equal(png, rgba8)
