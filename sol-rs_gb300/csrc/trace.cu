@@ -13,7 +13,15 @@ namespace solrt {
 
 namespace {
 
-constexpr int kExtendBlock = 128;
+#ifndef SOLRT_EXTEND_BLOCK
+#define SOLRT_EXTEND_BLOCK 128
+#endif
+// Minimum resident blocks per SM requested from the register allocator
+// (0 = no constraint).
+#ifndef SOLRT_EXTEND_MINB
+#define SOLRT_EXTEND_MINB 0
+#endif
+constexpr int kExtendBlock = SOLRT_EXTEND_BLOCK;
 
 SOLRT_D void flush_counters(DevStats* stats, const TraceCounters& cnt, uint32_t ef, bool count_nodes) {
     const uint32_t fb = __reduce_add_sync(0xffffffffu, cnt.fallbacks);
@@ -70,7 +78,7 @@ struct RayFileIO {
 
 // n = *count when count != nullptr (queue length on the device), else n_static.
 template <int KIND, class IO, bool kCount>
-__global__ void __launch_bounds__(kExtendBlock) k_extend(IO io, const unsigned int* __restrict__ count,
+__global__ void __launch_bounds__(kExtendBlock, SOLRT_EXTEND_MINB) k_extend(IO io, const unsigned int* __restrict__ count,
                                                          uint32_t n_static, unsigned int* __restrict__ work,
                                                          DevStats* stats) {
     const uint32_t n = count ? *count : n_static;
