@@ -21,14 +21,52 @@ namespace solrt {
 
 constexpr int kBvh2Sentinel = 0x7fffffff;
 #ifndef SOLRT_BVH2_REFILL
-#define SOLRT_BVH2_REFILL 8
+#define SOLRT_BVH2_REFILL 16
+#endif
+// Traversal stack entries kept in shared memory (slot-major, one column per
+// thread, so lanes at different depths hit different banks); deeper entries
+// go to a local-memory array. 0 = all in local memory.
+#ifndef SOLRT_SMEM_STACK
+#define SOLRT_SMEM_STACK 32
 #endif
 
-template <class IO, bool kCount>
+// The 4 float4 of BVH2 node `node` (64-byte aligned) in two 256-bit loads.
+SOLRT_D void load_bvh2_node(const float4* nodes, int node, float4& n0, float4& n1, float4& n2, int4& n3) {
+    const float4* np = nodes + 4 * (size_t)node;
+    float4 r;
+    ldg_2x4(np, n0, n1);
+    ldg_2x4(np + 2, n2, r);
+    n3 = make_int4(__float_as_int(r.x), __float_as_int(r.y), __float_as_int(r.z), __float_as_int(r.w));
+}
+
+// Per-thread traversal stack: slots [0, SOLRT_SMEM_STACK) in shared memory,
+// the rest in local memory; SOLRT_BVH2_STACK + 1 slots in all.
+template <int kBlock>
+struct Bvh2Stack {
+#if SOLRT_SMEM_STACK > 0
+    int* sh;  // slot k at sh[k * kBlock]
+    int lo[SOLRT_BVH2_STACK + 1 - SOLRT_SMEM_STACK];
+    SOLRT_D void put(int k, int v) {
+        if (k < SOLRT_SMEM_STACK) sh[k * kBlock] = v;
+        else lo[k - SOLRT_SMEM_STACK] = v;
+    }
+    SOLRT_D int get(int k) const { return k < SOLRT_SMEM_STACK ? sh[k * kBlock] : lo[k - SOLRT_SMEM_STACK]; }
+#else
+    int lo[SOLRT_BVH2_STACK + 1];
+    SOLRT_D void put(int k, int v) { lo[k] = v; }
+    SOLRT_D int get(int k) const { return lo[k]; }
+#endif
+};
+
+template <class IO, bool kCount, int kBlock>
 SOLRT_D void extend_bvh2_ww(const IO& io, uint32_t n, unsigned int* work, TraceCounters& cnt, uint32_t& ef) {
     const int lane = threadIdx.x & 31;
     const uint32_t lane_lt = (1u << lane) - 1u;
-    int stack[SOLRT_BVH2_STACK + 1];
+    Bvh2Stack<kBlock> stack;
+#if SOLRT_SMEM_STACK > 0
+    __shared__ int s_stack[SOLRT_SMEM_STACK * kBlock];
+    stack.sh = s_stack + threadIdx.x;
+#endif
     int sp = 0;
     int node = kBvh2Sentinel;  // >= 0 inner node, < 0 leaf ~k, sentinel = nothing left
     int leaf = 0;              // parked leaf (< 0) or none (>= 0)
@@ -69,7 +107,7 @@ SOLRT_D void extend_bvh2_ww(const IO& io, uint32_t n, unsigned int* work, TraceC
                     noz = -(o.z * iz);
                     best = HitRec{d.w, SOLRT_NO_HIT, 0.0f, 0.0f};
                     budget = 2u * (ts.node_count + ts.tri_count) + 64u;
-                    stack[0] = kBvh2Sentinel;
+                    stack.put(0, kBvh2Sentinel);
                     sp = 1;
                     node = ts.tri_count ? 0 : kBvh2Sentinel;
                     leaf = 0;
@@ -90,9 +128,9 @@ SOLRT_D void extend_bvh2_ww(const IO& io, uint32_t n, unsigned int* work, TraceC
                     node = kBvh2Sentinel;
                     leaf = 0;
                 } else {
-                    const float4* np = ts.nodes + 4 * (size_t)node;
-                    const float4 n0 = __ldg(np + 0), n1 = __ldg(np + 1), n2 = __ldg(np + 2);
-                    const int4 n3 = __ldg(reinterpret_cast<const int4*>(np + 3));
+                    float4 n0, n1, n2;
+                    int4 n3;
+                    load_bvh2_node(ts.nodes, node, n0, n1, n2, n3);
                     if (kCount) ++cnt.nodes;
                     float t0, t1;
                     const bool h0 = slab_fma(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, ix, iy, iz, nox, noy, noz, r.tmin,
@@ -101,7 +139,7 @@ SOLRT_D void extend_bvh2_ww(const IO& io, uint32_t n, unsigned int* work, TraceC
                                              best.t, t1);
                     if (h0 && h1) {
                         const bool swap = t1 < t0;
-                        if (sp <= SOLRT_BVH2_STACK) stack[sp++] = swap ? n3.x : n3.y;
+                        if (sp <= SOLRT_BVH2_STACK) stack.put(sp++, swap ? n3.x : n3.y);
                         else ef |= SOLRT_EFLAG_STACK;
                         node = swap ? n3.y : n3.x;
                     } else if (h0) {
@@ -109,11 +147,11 @@ SOLRT_D void extend_bvh2_ww(const IO& io, uint32_t n, unsigned int* work, TraceC
                     } else if (h1) {
                         node = n3.y;
                     } else {
-                        node = stack[--sp];
+                        node = stack.get(--sp);
                     }
                     if (node < 0 && leaf >= 0) {  // park the leaf, keep descending
                         leaf = node;
-                        node = stack[--sp];
+                        node = stack.get(--sp);
                     }
                 }
             }
@@ -131,7 +169,7 @@ SOLRT_D void extend_bvh2_ww(const IO& io, uint32_t n, unsigned int* work, TraceC
                     if (kCount) ++cnt.tris;
                     cnt.fallbacks += intersect_tri(r, __ldg(tp), __ldg(tp + 1), __ldg(tp + 2), best);
                     leaf = node;
-                    if (node < 0) node = stack[--sp];
+                    if (node < 0) node = stack.get(--sp);
                 }
             }
         }
@@ -162,9 +200,9 @@ SOLRT_D void trace_bvh2_ray(const TravScene& ts, float ox, float oy, float oz, f
                 ef |= SOLRT_EFLAG_INDEX;
                 return;
             }
-            const float4* np = ts.nodes + 4 * (size_t)node;
-            const float4 n0 = __ldg(np + 0), n1 = __ldg(np + 1), n2 = __ldg(np + 2);
-            const int4 n3 = __ldg(reinterpret_cast<const int4*>(np + 3));
+            float4 n0, n1, n2;
+            int4 n3;
+            load_bvh2_node(ts.nodes, node, n0, n1, n2, n3);
             float t0, t1;
             const bool h0 = slab_fma(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, ix, iy, iz, nox, noy, noz, tmin, best.t, t0);
             const bool h1 = slab_fma(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, ix, iy, iz, nox, noy, noz, tmin, best.t, t1);

@@ -85,8 +85,8 @@ __global__ void __launch_bounds__(kExtendBlock, SOLRT_EXTEND_MINB) k_extend(IO i
     if (count && blockIdx.x == 0 && threadIdx.x == 0 && n) atomicAdd(&stats->segments, (unsigned long long)n);
     TraceCounters cnt{0, 0, 0};
     uint32_t ef = 0;
-    if (KIND == SOLRT_BVH2) {
-        extend_bvh2_ww<IO, kCount>(io, n, work, cnt, ef);
+    if constexpr (KIND == SOLRT_BVH2) {
+        extend_bvh2_ww<IO, kCount, kExtendBlock>(io, n, work, cnt, ef);
     } else {
         const int lane = threadIdx.x & 31;
         for (;;) {

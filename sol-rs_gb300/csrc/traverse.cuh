@@ -114,6 +114,23 @@ SOLRT_D uint32_t intersect_tri(const RayWT& r, float4 q0, float4 q1, float4 q2, 
     return fb;
 }
 
+// Two consecutive float4 from a 32-byte-aligned address. With
+// SOLRT_NODE_V8 one 256-bit load (PTX ld.global.nc.v8.f32, sm_100 and
+// later): half the L1 load instructions / wavefronts of two 128-bit loads.
+#ifndef SOLRT_NODE_V8
+#define SOLRT_NODE_V8 1
+#endif
+SOLRT_D void ldg_2x4(const float4* p, float4& a, float4& b) {
+#if SOLRT_NODE_V8
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+        : "l"(p));
+#else
+    a = __ldg(p);
+    b = __ldg(p + 1);
+#endif
+}
+
 // Three-input min / max (PTX ISA min.f32 / max.f32 with three sources).
 SOLRT_D float max3(float a, float b, float c) {
     float r;
