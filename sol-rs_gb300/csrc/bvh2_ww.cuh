@@ -133,10 +133,8 @@ SOLRT_D void extend_bvh2_ww(const IO& io, uint32_t n, unsigned int* work, TraceC
                     load_bvh2_node(ts.nodes, node, n0, n1, n2, n3);
                     if (kCount) ++cnt.nodes;
                     float t0, t1;
-                    const bool h0 = slab_fma(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, ix, iy, iz, nox, noy, noz, r.tmin,
-                                             best.t, t0);
-                    const bool h1 = slab_fma(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, ix, iy, iz, nox, noy, noz, r.tmin,
-                                             best.t, t1);
+                    bool h0, h1;
+                    slab2_fma(n0, n1, n2, ix, iy, iz, nox, noy, noz, r.tmin, best.t, h0, t0, h1, t1);
                     if (h0 && h1) {
                         const bool swap = t1 < t0;
                         if (sp <= SOLRT_BVH2_STACK) stack.put(sp++, swap ? n3.x : n3.y);
@@ -204,8 +202,8 @@ SOLRT_D void trace_bvh2_ray(const TravScene& ts, float ox, float oy, float oz, f
             int4 n3;
             load_bvh2_node(ts.nodes, node, n0, n1, n2, n3);
             float t0, t1;
-            const bool h0 = slab_fma(n0.x, n0.y, n0.z, n0.w, n2.x, n2.y, ix, iy, iz, nox, noy, noz, tmin, best.t, t0);
-            const bool h1 = slab_fma(n1.x, n1.y, n1.z, n1.w, n2.z, n2.w, ix, iy, iz, nox, noy, noz, tmin, best.t, t1);
+            bool h0, h1;
+            slab2_fma(n0, n1, n2, ix, iy, iz, nox, noy, noz, tmin, best.t, h0, t0, h1, t1);
             if (h0 && h1) {
                 const bool swap = t1 < t0;
                 if (sp <= SOLRT_BVH2_STACK) stack[sp++] = swap ? n3.x : n3.y;

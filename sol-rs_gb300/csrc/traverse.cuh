@@ -165,6 +165,48 @@ SOLRT_D bool slab_fma(float lox, float hix, float loy, float hiy, float loz, flo
     return tn <= tf * 1.0000153f;
 }
 
+// Both child boxes of a BVH2 node (n0: child 0 x/y planes, n1: child 1 x/y
+// planes, n2: z planes of both) against one ray: the same arithmetic as two
+// slab_fma calls. With SOLRT_SLAB_F32X2 the 12 plane distances are six
+// packed two-lane FMAs (PTX fma.rn.f32x2, sm_100 and later; each lane is an
+// ordinary correctly rounded fma).
+#ifndef SOLRT_SLAB_F32X2
+#define SOLRT_SLAB_F32X2 1
+#endif
+SOLRT_D float2 fma_x2(float a0, float a1, float b, float c) {
+    float2 r;
+#if SOLRT_SLAB_F32X2
+    asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\t"
+        "mov.b64 rb, {%4, %4};\n\t"
+        "mov.b64 rc, {%5, %5};\n\t"
+        "fma.rn.f32x2 rd, ra, rb, rc;\n\t"
+        "mov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a0), "f"(a1), "f"(b), "f"(c));
+#else
+    r.x = fmaf(a0, b, c);
+    r.y = fmaf(a1, b, c);
+#endif
+    return r;
+}
+SOLRT_D void slab2_fma(const float4& n0, const float4& n1, const float4& n2, float ix, float iy, float iz,
+                       float nox, float noy, float noz, float tmin, float tmax, bool& h0, float& t0, bool& h1,
+                       float& t1) {
+    const float2 x0 = fma_x2(n0.x, n0.y, ix, nox), y0 = fma_x2(n0.z, n0.w, iy, noy);
+    const float2 z0 = fma_x2(n2.x, n2.y, iz, noz);
+    const float2 x1 = fma_x2(n1.x, n1.y, ix, nox), y1 = fma_x2(n1.z, n1.w, iy, noy);
+    const float2 z1 = fma_x2(n2.z, n2.w, iz, noz);
+    const float tn0 = fmaxf(max3(fminf(x0.x, x0.y), fminf(y0.x, y0.y), fminf(z0.x, z0.y)), tmin);
+    const float tf0 = fminf(min3(fmaxf(x0.x, x0.y), fmaxf(y0.x, y0.y), fmaxf(z0.x, z0.y)), tmax);
+    const float tn1 = fmaxf(max3(fminf(x1.x, x1.y), fminf(y1.x, y1.y), fminf(z1.x, z1.y)), tmin);
+    const float tf1 = fminf(min3(fmaxf(x1.x, x1.y), fmaxf(y1.x, y1.y), fmaxf(z1.x, z1.y)), tmax);
+    t0 = tn0;
+    t1 = tn1;
+    h0 = tn0 <= tf0 * 1.0000153f;
+    h1 = tn1 <= tf1 * 1.0000153f;
+}
+
 // Outward widening of a box face by a relative 2^-21 (about 4 ulp) plus an
 // absolute 2^-80 (which matters only near 0).
 SOLRT_HD float widen_lo(float v) { return (v - fabsf(v) * 0x1p-21f) - 0x1p-80f; }
