@@ -315,12 +315,12 @@ void build_lbvh(oracle_scene* s) {
             cmax[a] = std::max(cmax[a], cen[i][a]);
         }
     }
-    const float ext[3] = {cmax[0] - cmin[0], cmax[1] - cmin[1], cmax[2] - cmin[2]};
+    const float ext = std::max(std::max(cmax[0] - cmin[0], cmax[1] - cmin[1]), cmax[2] - cmin[2]);  // cubic cells
     std::vector<uint32_t> code(n);
     for (uint32_t i = 0; i < n; ++i) {
-        const uint32_t qx = quantise10(cen[i].x, cmin[0], ext[0]);
-        const uint32_t qy = quantise10(cen[i].y, cmin[1], ext[1]);
-        const uint32_t qz = quantise10(cen[i].z, cmin[2], ext[2]);
+        const uint32_t qx = quantise10(cen[i].x, cmin[0], ext);
+        const uint32_t qy = quantise10(cen[i].y, cmin[1], ext);
+        const uint32_t qz = quantise10(cen[i].z, cmin[2], ext);
         code[i] = (expand_bits10(qx) << 2) | (expand_bits10(qy) << 1) | expand_bits10(qz);
     }
     s->order.resize(n);

@@ -23,6 +23,12 @@ constexpr int kBvh2Sentinel = 0x7fffffff;
 #ifndef SOLRT_BVH2_REFILL
 #define SOLRT_BVH2_REFILL 16
 #endif
+// The node phase ends early when fewer than this many lanes have inner
+// nodes to visit and some lane holds a leaf (0 = only when no lane without
+// a parked leaf has inner nodes left).
+#ifndef SOLRT_WW_NODE_MIN
+#define SOLRT_WW_NODE_MIN 12
+#endif
 // Traversal stack entries kept in shared memory (slot-major, one column per
 // thread, so lanes at different depths hit different banks); deeper entries
 // go to a local-memory array. 0 = all in local memory.
@@ -122,6 +128,13 @@ SOLRT_D void extend_bvh2_ww(const IO& io, uint32_t n, unsigned int* work, TraceC
         for (;;) {
             const bool inner = (unsigned)node < (unsigned)kBvh2Sentinel;
             if (!__any_sync(0xffffffffu, inner && leaf >= 0)) break;
+#if SOLRT_WW_NODE_MIN > 0
+            // few lanes left with inner nodes while others hold leaves: test
+            // the leaves first (the leaf phase then has work, so this ends)
+            if (__popc(__ballot_sync(0xffffffffu, inner)) < SOLRT_WW_NODE_MIN &&
+                __any_sync(0xffffffffu, leaf < 0))
+                break;
+#endif
             if (inner) {
                 if (--budget == 0u || (uint32_t)node >= ts.node_count) {
                     ef |= SOLRT_EFLAG_INDEX;

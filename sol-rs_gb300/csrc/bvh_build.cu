@@ -5,7 +5,8 @@
 //
 // Pipeline (all on the context stream):
 //   1. centroids + centroid bounds (block reduction, ordered-int atomics)
-//   2. 30-bit Morton codes of centroids normalised to the centroid bounds
+//   2. 30-bit Morton codes of centroids in cubic cells over the centroid
+//      bounds (all axes scaled by the largest extent)
 //   3. stable LSD radix sort of (code, triangle) with 8-bit digits
 //   4. Karras 2012 radix-tree hierarchy over the sorted codes, equal codes
 //      split by index (delta = 32 + clz(i ^ j))
@@ -92,9 +93,12 @@ __global__ void k_morton(const float4* __restrict__ cen, const unsigned int* __r
     const float lo[3] = {ordered_to_float(cb[0]), ordered_to_float(cb[1]), ordered_to_float(cb[2])};
     const float hi[3] = {ordered_to_float(cb[3]), ordered_to_float(cb[4]), ordered_to_float(cb[5])};
     const float4 c = cen[i];
-    const uint32_t qx = quantise10(c.x, lo[0], hi[0] - lo[0]);
-    const uint32_t qy = quantise10(c.y, lo[1], hi[1] - lo[1]);
-    const uint32_t qz = quantise10(c.z, lo[2], hi[2] - lo[2]);
+    // cubic cells: every axis is scaled by the largest extent, so a long
+    // thin scene does not get cells stretched along its long axis
+    const float ext = fmaxf(fmaxf(hi[0] - lo[0], hi[1] - lo[1]), hi[2] - lo[2]);
+    const uint32_t qx = quantise10(c.x, lo[0], ext);
+    const uint32_t qy = quantise10(c.y, lo[1], ext);
+    const uint32_t qz = quantise10(c.z, lo[2], ext);
     keys[i] = (expand_bits10(qx) << 2) | (expand_bits10(qy) << 1) | expand_bits10(qz);
     vals[i] = i;
 }
