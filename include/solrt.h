@@ -419,6 +419,38 @@ solrt_status solrt_batch_destroy(solrt_batch* batch);
 /* Passes, work items and bounce launches of the plan. */
 solrt_status solrt_batch_info(solrt_batch* batch, uint32_t* passes, uint32_t* items, uint64_t* paths);
 
+/* ---- launch tuning ---------------------------------------------------------
+ * No counterpart in the reference (its launch shape is the driver's). The
+ * extend kernel's block size and the number of BVH2 traversal-stack slots
+ * kept in shared memory, and the number of paths per batch pass, change
+ * speed only: images are identical for every setting. */
+typedef struct solrt_tune_config {
+    uint32_t block_size;   /* extend threads per block: 64, 128 or 256 */
+    uint32_t smem_stack;   /* BVH2 stack slots per thread in shared memory: 16 or 32 */
+    uint32_t pass_paths;   /* paths per batch pass, <= the path capacity; 0 = the capacity */
+    uint32_t reserved;
+} solrt_tune_config;
+
+typedef struct solrt_tune_result {
+    solrt_tune_config best;
+    float best_ms;         /* one launch of the batch with `best` */
+    float initial_ms;      /* one launch with the configuration the call started from */
+    uint32_t candidates;   /* configurations timed */
+    uint32_t reserved;
+} solrt_tune_result;
+
+solrt_status solrt_context_get_tune(solrt_context* ctx, solrt_tune_config* out);
+/* Applies to later launches and plans (a batch already captured into a CUDA
+ * graph keeps its launch shape until it is re-planned). */
+solrt_status solrt_context_set_tune(solrt_context* ctx, const solrt_tune_config* cfg);
+/* Times the batch under each extend block size x shared stack depth, then
+ * under pass sizes of 1/4, 1/2 and all of the path capacity with the best of
+ * those, keeps the fastest on the context and re-plans the batch with it.
+ * Each candidate is launched three times (one warm-up): REF_MIX images hold
+ * the last launch's frame afterwards, KAHAN images the sum of all of them
+ * (clear them before rendering for real). */
+solrt_status solrt_batch_autotune(solrt_batch* batch, solrt_tune_result* out);
+
 /* ------------------------------------------------------------------------ */
 /* Serving: continuous batching of render jobs                              */
 /* ------------------------------------------------------------------------ */

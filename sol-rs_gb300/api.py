@@ -117,6 +117,16 @@ class ServerStats(ctypes.Structure):
                 ("busy_ms", ctypes.c_double)]
 
 
+class TuneConfig(ctypes.Structure):
+    _fields_ = [("block_size", ctypes.c_uint32), ("smem_stack", ctypes.c_uint32), ("pass_paths", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
+
+
+class TuneResult(ctypes.Structure):
+    _fields_ = [("best", TuneConfig), ("best_ms", ctypes.c_float), ("initial_ms", ctypes.c_float),
+                ("candidates", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
 class Stats(ctypes.Structure):
     _fields_ = [("segments", ctypes.c_uint64), ("paths", ctypes.c_uint64), ("node_visits", ctypes.c_uint64),
                 ("tri_tests", ctypes.c_uint64), ("fp64_fallbacks", ctypes.c_uint64), ("launches", ctypes.c_uint64),
@@ -170,6 +180,9 @@ _PROTOS = {
     "solrt_batch_destroy": (ctypes.c_int, [_P]),
     "solrt_batch_info": (ctypes.c_int, [_P, ctypes.POINTER(_U32), ctypes.POINTER(_U32),
                                         ctypes.POINTER(ctypes.c_uint64)]),
+    "solrt_context_get_tune": (ctypes.c_int, [_P, ctypes.POINTER(TuneConfig)]),
+    "solrt_context_set_tune": (ctypes.c_int, [_P, ctypes.POINTER(TuneConfig)]),
+    "solrt_batch_autotune": (ctypes.c_int, [_P, ctypes.POINTER(TuneResult)]),
     "solrt_server_create": (ctypes.c_int, [_P, ctypes.POINTER(ServerDesc), ctypes.POINTER(_P)]),
     "solrt_server_submit": (ctypes.c_int, [_P, _P, ctypes.POINTER(Camera), ctypes.POINTER(RenderParams),
                                            ctypes.POINTER(ctypes.c_uint64)]),
@@ -258,6 +271,15 @@ class Context:
 
     def stream(self):
         return lib().solrt_context_stream(self.handle)
+
+    def get_tune(self):
+        c = TuneConfig()
+        check(lib().solrt_context_get_tune(self.handle, ctypes.byref(c)))
+        return dict(block_size=c.block_size, smem_stack=c.smem_stack, pass_paths=c.pass_paths)
+
+    def set_tune(self, block_size=128, smem_stack=32, pass_paths=0):
+        check(lib().solrt_context_set_tune(self.handle, ctypes.byref(
+            TuneConfig(block_size=block_size, smem_stack=smem_stack, pass_paths=pass_paths))))
 
     def set_blue_noise(self, rgba8):
         """(h, w, 4) uint8 texture of the AO integrator (the reference loads
@@ -495,6 +517,14 @@ class Batch:
         p, i, n = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint64()
         check(lib().solrt_batch_info(self.handle, ctypes.byref(p), ctypes.byref(i), ctypes.byref(n)))
         return dict(passes=p.value, items=i.value, paths=n.value)
+
+    def autotune(self):
+        """solrt_batch_autotune: times block size x shared stack depth, then
+        the pass size; keeps the fastest on the context."""
+        r = TuneResult()
+        check(lib().solrt_batch_autotune(self.handle, ctypes.byref(r)))
+        return dict(block_size=r.best.block_size, smem_stack=r.best.smem_stack, pass_paths=r.best.pass_paths,
+                    best_ms=r.best_ms, initial_ms=r.initial_ms, candidates=r.candidates)
 
 
 class Server:

@@ -199,6 +199,14 @@ solrt_status solrt_context_create(const solrt_context_desc* desc, solrt_context*
     c->capacity = d.path_capacity ? d.path_capacity : (8u << 20);
     c->counters = d.enable_counters != 0;
     c->block_size = d.block_size;
+    if (d.block_size) {
+        if (!extend_variant_ok(d.block_size, c->tune.smem)) {
+            set_error("block_size must be 64, 128 or 256");
+            delete c;
+            return SOLRT_ERR_INVALID;
+        }
+        c->tune.block = d.block_size;
+    }
     c->timing = d.enable_timing != 0;
     auto fail = [&](solrt_status s) {
         solrt_context_destroy(c);
@@ -674,6 +682,32 @@ solrt_status solrt_batch_destroy(solrt_batch* batch) {
     delete batch;
     context_release(c);
     return SOLRT_OK;
+}
+
+solrt_status solrt_context_get_tune(solrt_context* ctx, solrt_tune_config* out) {
+    CHECK_ARG(ctx && out, "null argument");
+    out->block_size = ctx->tune.block;
+    out->smem_stack = ctx->tune.smem;
+    out->pass_paths = ctx->tune.pass_paths;
+    out->reserved = 0;
+    return SOLRT_OK;
+}
+
+solrt_status solrt_context_set_tune(solrt_context* ctx, const solrt_tune_config* cfg) {
+    CHECK_ARG(ctx && cfg, "null argument");
+    CHECK_ARG(extend_variant_ok(cfg->block_size, cfg->smem_stack),
+              "block_size must be 64, 128 or 256 and smem_stack 16 or 32");
+    CHECK_ARG(cfg->pass_paths <= ctx->capacity, "pass_paths exceeds the path capacity");
+    ctx->tune.block = cfg->block_size;
+    ctx->tune.smem = cfg->smem_stack;
+    ctx->tune.pass_paths = cfg->pass_paths;
+    return SOLRT_OK;
+}
+
+solrt_status solrt_batch_autotune(solrt_batch* batch, solrt_tune_result* out) {
+    CHECK_ARG(batch, "null batch");
+    SOLRT_CUDA(cudaSetDevice(batch->ctx->device));
+    return batch_autotune(*batch, out);
 }
 
 solrt_status solrt_batch_info(solrt_batch* batch, uint32_t* passes, uint32_t* items, uint64_t* paths) {

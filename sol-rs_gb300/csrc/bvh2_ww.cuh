@@ -29,9 +29,10 @@ constexpr int kBvh2Sentinel = 0x7fffffff;
 #ifndef SOLRT_WW_NODE_MIN
 #define SOLRT_WW_NODE_MIN 12
 #endif
-// Traversal stack entries kept in shared memory (slot-major, one column per
-// thread, so lanes at different depths hit different banks); deeper entries
-// go to a local-memory array. 0 = all in local memory.
+// Default traversal stack entries kept in shared memory (slot-major, one
+// column per thread, so lanes at different depths hit different banks);
+// deeper entries go to a local-memory array. The launch may pick 16 or 32
+// (solrt_context_set_tune / solrt_batch_autotune).
 #ifndef SOLRT_SMEM_STACK
 #define SOLRT_SMEM_STACK 32
 #endif
@@ -45,34 +46,33 @@ SOLRT_D void load_bvh2_node(const float4* nodes, int node, float4& n0, float4& n
     n3 = make_int4(__float_as_int(r.x), __float_as_int(r.y), __float_as_int(r.z), __float_as_int(r.w));
 }
 
-// Per-thread traversal stack: slots [0, SOLRT_SMEM_STACK) in shared memory,
-// the rest in local memory; SOLRT_BVH2_STACK + 1 slots in all.
-template <int kBlock>
+// Per-thread traversal stack: slots [0, kSmem) in shared memory, the rest
+// in local memory; SOLRT_BVH2_STACK + 1 slots in all.
+template <int kBlock, int kSmem>
 struct Bvh2Stack {
-#if SOLRT_SMEM_STACK > 0
     int* sh;  // slot k at sh[k * kBlock]
-    int lo[SOLRT_BVH2_STACK + 1 - SOLRT_SMEM_STACK];
+    int lo[SOLRT_BVH2_STACK + 1 - kSmem];
     SOLRT_D void put(int k, int v) {
-        if (k < SOLRT_SMEM_STACK) sh[k * kBlock] = v;
-        else lo[k - SOLRT_SMEM_STACK] = v;
+        if (k < kSmem) sh[k * kBlock] = v;
+        else lo[k - kSmem] = v;
     }
-    SOLRT_D int get(int k) const { return k < SOLRT_SMEM_STACK ? sh[k * kBlock] : lo[k - SOLRT_SMEM_STACK]; }
-#else
+    SOLRT_D int get(int k) const { return k < kSmem ? sh[k * kBlock] : lo[k - kSmem]; }
+};
+template <int kBlock>
+struct Bvh2Stack<kBlock, 0> {
+    int* sh;
     int lo[SOLRT_BVH2_STACK + 1];
     SOLRT_D void put(int k, int v) { lo[k] = v; }
     SOLRT_D int get(int k) const { return lo[k]; }
-#endif
 };
 
-template <class IO, bool kCount, int kBlock>
+template <class IO, bool kCount, int kBlock, int kSmem>
 SOLRT_D void extend_bvh2_ww(const IO& io, uint32_t n, unsigned int* work, TraceCounters& cnt, uint32_t& ef) {
     const int lane = threadIdx.x & 31;
     const uint32_t lane_lt = (1u << lane) - 1u;
-    Bvh2Stack<kBlock> stack;
-#if SOLRT_SMEM_STACK > 0
-    __shared__ int s_stack[SOLRT_SMEM_STACK * kBlock];
+    Bvh2Stack<kBlock, kSmem> stack;
+    __shared__ int s_stack[(kSmem > 0 ? kSmem : 1) * kBlock];
     stack.sh = s_stack + threadIdx.x;
-#endif
     int sp = 0;
     int node = kBvh2Sentinel;  // >= 0 inner node, < 0 leaf ~k, sentinel = nothing left
     int leaf = 0;              // parked leaf (< 0) or none (>= 0)

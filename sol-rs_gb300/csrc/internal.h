@@ -148,6 +148,7 @@ struct Batch {
     DeviceBuffer d_jobs, d_items, d_job_pix;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    std::vector<solrt_job> src;  // the jobs as given (re-planned by the autotuner)
     Batch() = default;
     Batch(const Batch&) = delete;
     Batch& operator=(const Batch&) = delete;
@@ -157,12 +158,21 @@ struct Batch {
     }
 };
 
+// Launch shape of the extend kernel and pass size of batches, chosen by
+// solrt_context_set_tune or solrt_batch_autotune.
+struct TuneConfig {
+    uint32_t block = 128;      // threads per extend block: 64, 128 or 256
+    uint32_t smem = 32;        // BVH2 traversal-stack slots in shared memory: 16 or 32
+    uint32_t pass_paths = 0;   // paths per batch pass (0 = the path capacity)
+};
+
 struct Context {
     // The handle and every scene, image and batch created on the context hold
     // a reference; the context is freed when the last one goes, so objects
     // destroyed after solrt_context_destroy stay valid until then.
     int refs = 1;
     Batch single;  // plan of the last solrt_render call
+    TuneConfig tune;
     int device = 0;
     int sm_count = 0;
     cudaStream_t stream = nullptr;
@@ -269,9 +279,12 @@ solrt_status launch_trace_rays(Context& ctx, const Scene& sc, const solrt_ray* r
 // Extend for a batched queue: the scene of ray i is jobs[meta[i].y >> kDepthBits].sc.
 solrt_status launch_extend(Context& ctx, uint32_t kind, const DevJob* jobs, const PathQueue& q, float4* hits,
                            const unsigned int* count, unsigned int* work);
+// Whether an extend kernel exists for this block size / shared stack slots.
+bool extend_variant_ok(uint32_t block, uint32_t smem);
 
 // pathtrace.cu
 solrt_status batch_plan(Context& ctx, const solrt_job* jobs, uint32_t n, uint32_t flags, Batch& b);
+solrt_status batch_autotune(Batch& b, solrt_tune_result* out);
 solrt_status batch_set_jobs(Batch& b, const solrt_job* jobs);
 solrt_status batch_launch(Batch& b);
 solrt_status render_frame(Context& ctx, const Scene& sc, const solrt_camera& cam, const solrt_render_params& p,

@@ -544,11 +544,13 @@ solrt_status batch_plan(Context& ctx, const solrt_job* jobs, uint32_t n, uint32_
     if (n > (1u << (32 - kDepthBits))) { set_error("too many jobs in one batch"); return SOLRT_ERR_CAPACITY; }
     b.ctx = &ctx;
     b.flags = flags;
+    if (jobs != b.src.data()) b.src.assign(jobs, jobs + n);
+    b.total_paths = 0;
     b.jobs.clear();
     b.items.clear();
     b.passes.clear();
     b.job_pix_base.assign(1, 0u);
-    const uint32_t cap = ctx.capacity;
+    const uint32_t cap = ctx.tune.pass_paths ? std::min(ctx.tune.pass_paths, ctx.capacity) : ctx.capacity;
     for (uint32_t j = 0; j < n; ++j) {
         const solrt_job& jb = jobs[j];
         if (!jb.scene || !jb.image) { set_error("job %u: null scene or image", j); return SOLRT_ERR_INVALID; }
@@ -632,6 +634,7 @@ solrt_status batch_set_jobs(Batch& b, const solrt_job* jobs) {
             return SOLRT_ERR_INVALID;
         }
         b.jobs[j] = nj;
+        b.src[j] = jb;
     }
     SOLRT_CUDA(cudaMemcpyAsync(b.d_jobs.ptr, b.jobs.data(), sizeof(DevJob) * b.jobs.size(), cudaMemcpyHostToDevice,
                                b.ctx->stream));
@@ -668,6 +671,85 @@ solrt_status batch_launch(Batch& b) {
     SOLRT_CUDA(cudaEventRecord(ctx.ev1, ctx.stream));
     ctx.launches += b.graph_launches;
     return SOLRT_OK;
+}
+
+// Coordinate search over the extend launch shape, then the pass size; each
+// candidate re-plans the batch (a new CUDA graph) and is timed on its best of
+// two launches after a warm-up.
+solrt_status batch_autotune(Batch& b, solrt_tune_result* out) {
+    Context& ctx = *b.ctx;
+    const TuneConfig initial = ctx.tune;
+    const std::vector<solrt_job> src = b.src;
+    uint32_t candidates = 0;
+    auto measure = [&](const TuneConfig& cfg, float* ms) -> solrt_status {
+        ctx.tune = cfg;
+        if (b.exec) { cudaGraphExecDestroy(b.exec); b.exec = nullptr; }
+        if (b.graph) { cudaGraphDestroy(b.graph); b.graph = nullptr; }
+        SOLRT_TRY(batch_plan(ctx, src.data(), (uint32_t)src.size(), b.flags, b));
+        float best = 0.0f;
+        for (int r = 0; r < 3; ++r) {
+            SOLRT_TRY(batch_launch(b));
+            SOLRT_CUDA(cudaEventSynchronize(ctx.ev1));
+            float t = 0.0f;
+            SOLRT_CUDA(cudaEventElapsedTime(&t, ctx.ev0, ctx.ev1));
+            if (r == 1 || (r > 1 && t < best)) best = t;
+        }
+        ++candidates;
+        *ms = best;
+        return SOLRT_OK;
+    };
+    auto run = [&]() -> solrt_status {
+        float initial_ms = 0.0f;
+        SOLRT_TRY(measure(initial, &initial_ms));
+        TuneConfig best = initial;
+        float best_ms = initial_ms;
+        const uint32_t smems[2] = {16u, 32u};
+        const uint32_t blocks[3] = {64u, 128u, 256u};
+        for (uint32_t bl : blocks) {
+            for (uint32_t sm : smems) {
+                if (b.kind != SOLRT_BVH2 && sm != initial.smem) continue;  // no shared stack
+                TuneConfig c = initial;
+                c.block = bl;
+                c.smem = sm;
+                if (c.block == initial.block && c.smem == initial.smem) continue;
+                float ms = 0.0f;
+                SOLRT_TRY(measure(c, &ms));
+                if (ms < best_ms) { best_ms = ms; best = c; }
+            }
+        }
+        const uint32_t cap = ctx.capacity;
+        const uint32_t passes[3] = {std::max(1u, cap / 4u), std::max(1u, cap / 2u), 0u};
+        const TuneConfig shape = best;
+        for (uint32_t pp : passes) {
+            TuneConfig c = shape;
+            c.pass_paths = pp;
+            if (c.pass_paths == shape.pass_paths) continue;
+            float ms = 0.0f;
+            SOLRT_TRY(measure(c, &ms));
+            if (ms < best_ms) { best_ms = ms; best = c; }
+        }
+        float final_ms = 0.0f;
+        SOLRT_TRY(measure(best, &final_ms));  // leaves the batch planned with `best`
+        if (out) {
+            out->best.block_size = best.block;
+            out->best.smem_stack = best.smem;
+            out->best.pass_paths = best.pass_paths;
+            out->best.reserved = 0;
+            out->best_ms = best_ms;
+            out->initial_ms = initial_ms;
+            out->candidates = candidates;
+            out->reserved = 0;
+        }
+        return SOLRT_OK;
+    };
+    const solrt_status s = run();
+    if (s != SOLRT_OK) {  // back to the configuration the call started from
+        ctx.tune = initial;
+        if (b.exec) { cudaGraphExecDestroy(b.exec); b.exec = nullptr; }
+        if (b.graph) { cudaGraphDestroy(b.graph); b.graph = nullptr; }
+        batch_plan(ctx, src.data(), (uint32_t)src.size(), b.flags, b);
+    }
+    return s;
 }
 
 // One serving tick: uploads the active jobs and this tick's items, runs one

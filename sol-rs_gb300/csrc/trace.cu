@@ -5,6 +5,8 @@
 // so the queue length can stay on the device (no host round trip).
 //   BVH2: while-while traversal with per-lane refill (bvh2_ww.cuh).
 //   BVH8: one ray per lane, 32 rays per fetch (bvh8_traverse.cuh).
+#include <algorithm>
+
 #include "bvh2_ww.cuh"
 #include "bvh8_traverse.cuh"
 #include "internal.h"
@@ -77,16 +79,18 @@ struct RayFileIO {
 };
 
 // n = *count when count != nullptr (queue length on the device), else n_static.
-template <int KIND, class IO, bool kCount>
-__global__ void __launch_bounds__(kExtendBlock, SOLRT_EXTEND_MINB) k_extend(IO io, const unsigned int* __restrict__ count,
-                                                         uint32_t n_static, unsigned int* __restrict__ work,
-                                                         DevStats* stats) {
+// kBlock threads per block; kSmem traversal-stack slots per thread in
+// shared memory (BVH2).
+template <int KIND, class IO, bool kCount, int kBlock, int kSmem>
+__global__ void __launch_bounds__(kBlock, SOLRT_EXTEND_MINB) k_extend(IO io, const unsigned int* __restrict__ count,
+                                                                      uint32_t n_static, unsigned int* __restrict__ work,
+                                                                      DevStats* stats) {
     const uint32_t n = count ? *count : n_static;
     if (count && blockIdx.x == 0 && threadIdx.x == 0 && n) atomicAdd(&stats->segments, (unsigned long long)n);
     TraceCounters cnt{0, 0, 0};
     uint32_t ef = 0;
     if constexpr (KIND == SOLRT_BVH2) {
-        extend_bvh2_ww<IO, kCount, kExtendBlock>(io, n, work, cnt, ef);
+        extend_bvh2_ww<IO, kCount, kBlock, kSmem>(io, n, work, cnt, ef);
     } else {
         const int lane = threadIdx.x & 31;
         for (;;) {
@@ -108,38 +112,58 @@ __global__ void __launch_bounds__(kExtendBlock, SOLRT_EXTEND_MINB) k_extend(IO i
     flush_counters(stats, cnt, ef, kCount);
 }
 
-template <int KIND, class IO>
-void launch_kind(const Context& ctx, uint32_t grid, const IO& io, const unsigned int* count, uint32_t n_static,
-                 unsigned int* work, DevStats* st) {
-    if (ctx.counters)
-        k_extend<KIND, IO, true><<<grid, kExtendBlock, 0, ctx.stream>>>(io, count, n_static, work, st);
-    else
-        k_extend<KIND, IO, false><<<grid, kExtendBlock, 0, ctx.stream>>>(io, count, n_static, work, st);
+// One extend launch of a kernel variant: a persistent grid of (SMs x
+// resident blocks), or fewer blocks when `n_cap` (> 0) rays need fewer.
+template <int KIND, class IO, bool kCount, int kBlock, int kSmem>
+void launch_variant(const Context& ctx, const IO& io, const unsigned int* count, uint32_t n_static, uint32_t n_cap,
+                    unsigned int* work, DevStats* st) {
+    auto kern = k_extend<KIND, IO, kCount, kBlock, kSmem>;
+    int b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kBlock, 0);
+    uint32_t grid = (uint32_t)ctx.sm_count * (uint32_t)(b > 0 ? b : 1);
+    if (n_cap) grid = std::min(grid, (n_cap + kBlock - 1) / kBlock);
+    kern<<<grid, kBlock, 0, ctx.stream>>>(io, count, n_static, work, st);
 }
 
-template <class IO>
-int blocks_per_sm(uint32_t kind, bool counters) {
-    int b = 0;
-    if (kind == SOLRT_BVH8_Q8)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &b, counters ? k_extend<SOLRT_BVH8_Q8, IO, true> : k_extend<SOLRT_BVH8_Q8, IO, false>, kExtendBlock, 0);
-    else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &b, counters ? k_extend<SOLRT_BVH2, IO, true> : k_extend<SOLRT_BVH2, IO, false>, kExtendBlock, 0);
-    return b > 0 ? b : 1;
+// The variant of the context's tuning (solrt_context_set_tune /
+// solrt_batch_autotune); counting launches use the default shape.
+template <int KIND, class IO>
+solrt_status launch_tuned(const Context& ctx, const IO& io, const unsigned int* count, uint32_t n_static,
+                          uint32_t n_cap, unsigned int* work, DevStats* st) {
+    constexpr int S = KIND == SOLRT_BVH2 ? 1 : 0;  // BVH8 keeps its stack in registers / local memory
+    if (ctx.counters) {
+        launch_variant<KIND, IO, true, kExtendBlock, S * SOLRT_SMEM_STACK>(ctx, io, count, n_static, n_cap, work, st);
+        return SOLRT_OK;
+    }
+    const uint32_t blk = ctx.tune.block, sm = S ? ctx.tune.smem : 0u;
+#define SOLRT_VARIANT(B, M)                                                                              \
+    if (blk == B && sm == S * M) {                                                                       \
+        launch_variant<KIND, IO, false, B, S * M>(ctx, io, count, n_static, n_cap, work, st);            \
+        return SOLRT_OK;                                                                                 \
+    }
+    SOLRT_VARIANT(64, 16)
+    SOLRT_VARIANT(64, 32)
+    SOLRT_VARIANT(128, 16)
+    SOLRT_VARIANT(128, 32)
+    SOLRT_VARIANT(256, 16)
+    SOLRT_VARIANT(256, 32)
+#undef SOLRT_VARIANT
+    set_error("no extend kernel for block %u, stack %u", blk, sm);
+    return SOLRT_ERR_INVALID;
 }
 
 }  // namespace
 
-int extend_blocks_per_sm(uint32_t kind, bool counters) { return blocks_per_sm<QueueIO>(kind, counters); }
+bool extend_variant_ok(uint32_t block, uint32_t smem) {
+    return (block == 64 || block == 128 || block == 256) && (smem == 16 || smem == 32);
+}
 
 solrt_status launch_extend(Context& ctx, uint32_t kind, const DevJob* jobs, const PathQueue& q, float4* hits,
                            const unsigned int* count, unsigned int* work) {
-    const uint32_t grid = (uint32_t)(ctx.sm_count * blocks_per_sm<QueueIO>(kind, ctx.counters));
     const QueueIO io{q.o_tmin, q.d_tmax, q.meta, jobs, hits};
     DevStats* st = ctx.stats.as<DevStats>();
-    if (kind == SOLRT_BVH8_Q8) launch_kind<SOLRT_BVH8_Q8>(ctx, grid, io, count, 0, work, st);
-    else launch_kind<SOLRT_BVH2>(ctx, grid, io, count, 0, work, st);
+    if (kind == SOLRT_BVH8_Q8) SOLRT_TRY((launch_tuned<SOLRT_BVH8_Q8>(ctx, io, count, 0, 0, work, st)));
+    else SOLRT_TRY((launch_tuned<SOLRT_BVH2>(ctx, io, count, 0, 0, work, st)));
     ++ctx.launches;
     SOLRT_CUDA(cudaGetLastError());
     return SOLRT_OK;
@@ -148,16 +172,12 @@ solrt_status launch_extend(Context& ctx, uint32_t kind, const DevJob* jobs, cons
 solrt_status launch_trace_rays(Context& ctx, const Scene& sc, const solrt_ray* rays, uint32_t n, solrt_hit* hits) {
     if (n == 0) return SOLRT_OK;
     const DevScene d = sc.view();
-    const uint32_t per_sm = (uint32_t)blocks_per_sm<RayFileIO>(d.bvh_kind, ctx.counters);
-    const uint32_t want = (n + kExtendBlock - 1) / kExtendBlock;
-    const uint32_t cap = (uint32_t)ctx.sm_count * per_sm;
-    const uint32_t grid = want < cap ? want : cap;
     const RayFileIO io{reinterpret_cast<const float4*>(rays), reinterpret_cast<float4*>(hits), trav_scene(d)};
     unsigned int* work = ctx.trace_work.as<unsigned int>();
     SOLRT_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned int), ctx.stream));
     DevStats* st = ctx.stats.as<DevStats>();
-    if (d.bvh_kind == SOLRT_BVH8_Q8) launch_kind<SOLRT_BVH8_Q8>(ctx, grid, io, nullptr, n, work, st);
-    else launch_kind<SOLRT_BVH2>(ctx, grid, io, nullptr, n, work, st);
+    if (d.bvh_kind == SOLRT_BVH8_Q8) SOLRT_TRY((launch_tuned<SOLRT_BVH8_Q8>(ctx, io, nullptr, n, n, work, st)));
+    else SOLRT_TRY((launch_tuned<SOLRT_BVH2>(ctx, io, nullptr, n, n, work, st)));
     ++ctx.launches;
     SOLRT_CUDA(cudaGetLastError());
     return SOLRT_OK;

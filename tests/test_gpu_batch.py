@@ -122,3 +122,56 @@ def test_batch_rejects_mixed_bvh_kinds(solrt, ctx):
     p = solrt.render_params(8, 8)
     with pytest.raises(solrt.SolrtError):
         solrt.Batch(ctx, [(a, ia, cam, p), (b, ib, cam, p)])
+
+
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh8"])
+def test_autotune_keeps_images(solrt, bvh):
+    """solrt_batch_autotune times every extend block size x shared stack
+    depth and three pass sizes; the batch re-planned with the winner renders
+    the same images as the default configuration, and the winner stays on
+    the context."""
+    kind = solrt.BVH2 if bvh == "bvh2" else solrt.BVH8_Q8
+    c = solrt.Context(0, path_capacity=1 << 18)
+    jobs = _make(solrt, c, kind)
+    b = solrt.Batch(c, jobs, graph=True)
+    b.launch()
+    c.synchronize()
+    want = [img.read()[0].copy() for _, img, _, _ in jobs]
+    r = b.autotune()
+    assert r["candidates"] >= (8 if bvh == "bvh2" else 5)
+    assert r["block_size"] in (64, 128, 256) and r["smem_stack"] in (16, 32)
+    assert r["best_ms"] > 0 and r["best_ms"] <= r["initial_ms"] * 1.05
+    assert c.get_tune() == {k: r[k] for k in ("block_size", "smem_stack", "pass_paths")}
+    b.launch()
+    c.synchronize()
+    for (_, img, _, _), w in zip(jobs, want):
+        assert np.array_equal(img.read()[0].view(np.uint32), w.view(np.uint32))
+    assert c.stats().error_flags == 0
+    b.close()
+    c.close()
+
+
+def test_every_tune_config_renders_the_same(solrt):
+    c = solrt.Context(0, path_capacity=1 << 18)
+    jobs = _make(solrt, c, solrt.BVH2)
+    ref = None
+    for blk in (64, 128, 256):
+        for sm in (16, 32):
+            for pp in (0, 5000):
+                c.set_tune(blk, sm, pp)
+                b = solrt.Batch(c, jobs)
+                b.launch()
+                c.synchronize()
+                got = [img.read()[0].copy() for _, img, _, _ in jobs]
+                if ref is None:
+                    ref = got
+                for x, y in zip(ref, got):
+                    assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), (blk, sm, pp)
+                b.close()
+    with pytest.raises(solrt.SolrtError):
+        c.set_tune(96, 32, 0)
+    with pytest.raises(solrt.SolrtError):
+        c.set_tune(128, 8, 0)
+    with pytest.raises(solrt.SolrtError):
+        c.set_tune(128, 32, 1 << 20)
+    c.close()
