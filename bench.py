@@ -201,6 +201,87 @@ def cpu_baseline(data, kw, cam, budget_s=12.0, threads=0):
             "segments": int(total_seg), "seconds": round(total_t, 3)}
 
 
+def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, main_tris, n_rays=1 << 22):
+    """8-bit quantised 8-wide BVH vs the FP32 binary BVH on the same scene:
+    hit records of 4M rays (every camera ray of the frame's first sample
+    positions plus seeded rays from inside the scene) compared bit for bit on
+    the device, node bytes, visits per segment, Mrays/s of one 64-spp frame
+    and the FP64 fallback count of each."""
+    import torch
+    solrt = importlib.import_module("sol-rs_gb300")
+    W, H = kw["width"], kw["height"]
+    g = torch.Generator(device="cpu").manual_seed(7)
+    n_cam = W * H
+    n_in = n_rays - n_cam
+    rays = torch.zeros((n_rays, 8), dtype=torch.float32)
+    # camera rays through pixel centres (origin, tmin, direction, tmax)
+    V = np.array(cam.view_inverse, np.float64).reshape(4, 4).T
+    P = np.array(cam.projection_inverse, np.float64).reshape(4, 4).T
+    ys, xs = np.mgrid[0:H, 0:W]
+    d = np.stack([(xs + 0.5) / W * 2 - 1, (ys + 0.5) / H * 2 - 1, np.ones_like(xs, float), np.ones_like(xs, float)], -1)
+    t = d.reshape(-1, 4) @ P.T
+    t = t[:, :3] / np.linalg.norm(t[:, :3], axis=1, keepdims=True)
+    dirs = t @ V[:3, :3].T
+    org = V[:3, 3]
+    rays[:n_cam, 0:3] = torch.from_numpy(np.tile(org, (n_cam, 1)).astype(np.float32))
+    rays[:n_cam, 4:7] = torch.from_numpy(dirs.astype(np.float32))
+    rays[n_cam:, 0:3] = torch.rand((n_in, 3), generator=g)
+    dd = torch.randn((n_in, 3), generator=g)
+    rays[n_cam:, 4:7] = dd / dd.norm(dim=1, keepdim=True)
+    rays[:, 3] = 1e-3
+    rays[:, 7] = 1e4
+    dev = torch.device("cuda", local)
+    rays_d = rays.to(dev)
+    out = {"rays_compared": n_rays, "leaf_max": 1}
+    hits = {}
+    with solrt.Context(local, enable_timing=True) as ctx, solrt.Context(local, enable_counters=True) as cctx:
+        for name, kind in (("bvh2_fp32", solrt.BVH2), ("bvh8_q8", solrt.BVH8_Q8)):
+            sc = solrt.SceneDescription(ctx, data, bvh=kind, leaf_max=1 if kind == solrt.BVH8_Q8 else 0)
+            info = sc.bvh_info()
+            h = torch.zeros((n_rays, 4), dtype=torch.float32, device=dev)
+            ctx.reset_stats()
+            sc.trace_rays_device(rays_d.data_ptr(), n_rays, h.data_ptr())
+            ctx.synchronize()
+            fb_trace = ctx.stats().fp64_fallbacks
+            hits[name] = h
+            if kind == solrt.BVH2:
+                mr, nodes, tris = main_mrays, main_nodes, main_tris
+            else:
+                img = solrt.Image(ctx, W, H, kw["accum_mode"])
+                r = solrt.Renderer(ctx)
+                r.cmd_trace_rays(sc, cam, solrt.render_params(**kw), img)
+                ctx.synchronize()
+                ctx.reset_stats()
+                r.cmd_trace_rays(sc, cam, solrt.render_params(**dict(kw, frame=1)), img)
+                ctx.synchronize()
+                st = ctx.stats()
+                mr = st.segments / (st.render_ms / 1000.0) / 1e6 if st.render_ms > 0 else None
+                img.close()
+                csc = solrt.SceneDescription(cctx, data, bvh=kind, leaf_max=1)
+                cimg = solrt.Image(cctx, W, H, kw["accum_mode"])
+                cctx.reset_stats()
+                solrt.Renderer(cctx).cmd_trace_rays(csc, cam, solrt.render_params(**dict(kw, spp=min(4, kw["spp"]))),
+                                                    cimg)
+                cctx.synchronize()
+                cs = cctx.stats()
+                nodes = cs.node_visits / max(cs.segments, 1)
+                tris = cs.tri_tests / max(cs.segments, 1)
+                cimg.close()
+                csc.close()
+            nb = NODE_BYTES[info.kind]
+            out[name] = {"mrays_per_s": round(mr, 1) if mr else None, "node_bytes": int(info.node_bytes),
+                         "node_count": int(info.node_count), "bytes_per_node": nb,
+                         "nodes_per_segment": round(nodes, 2), "tris_per_segment": round(tris, 2),
+                         "node_bytes_per_segment": round(nb * nodes, 1),
+                         "fp64_fallbacks_in_compared_rays": int(fb_trace), "build_ms": round(info.build_ms, 3)}
+            sc.close()
+    a = hits["bvh2_fp32"].view(torch.int32)
+    b8 = hits["bvh8_q8"].view(torch.int32)
+    out["hit_mismatches"] = int((a != b8).any(dim=1).sum().item())
+    out["hits"] = int((a[:, 1] != -1).sum().item())
+    return out
+
+
 def run_batch(args, world, rank, local, pg, njobs=None, steps=None, emit=True):
     """Batched mixed scenes (256 randomised Cornell boxes with log-uniform
     1k-500k-triangle soups, 128^2..1024^2, 4-64 spp, depth 5): one CUDA-graph
@@ -232,6 +313,11 @@ def run_batch(args, world, rank, local, pg, njobs=None, steps=None, emit=True):
         samples += w * h * jp["spp"]
     setup_s = time.perf_counter() - t0
     batch = solrt.Batch(ctx, jobs, graph=True)
+    # launch shape and pass size chosen by the autotuner (outside the timed
+    # region; it leaves the batch re-planned with its choice)
+    t1 = time.perf_counter()
+    tune = batch.autotune()
+    tune["tune_s"] = round(time.perf_counter() - t1, 2)
     info = batch.info()
     ext = torch.cuda.ExternalStream(ctx.stream())
 
@@ -284,7 +370,8 @@ def run_batch(args, world, rank, local, pg, njobs=None, steps=None, emit=True):
            "ratio": round(value / plain_v, 3) if plain_v > 0 else None,
            "wavefront_scene_by_scene": round(wave_v, 3),
            "ratio_vs_wavefront": round(value / wave_v, 3) if wave_v > 0 else None,
-           "batch_ms": round(ms_b_max / steps, 3), "passes": info["passes"]}
+           "batch_ms": round(ms_b_max / steps, 3), "passes": info["passes"],
+           "autotune": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in tune.items()}}
     if rank == 0 and emit:
         out = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": steps,
                "warmup": args.warmup, "ms_per_step": round(ms_b_max / steps, 3), "higher_is_better": True,
@@ -427,6 +514,10 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="skip the short serving run of the default line")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-precision", action="store_true", help="skip the BVH8-q8 vs FP32 BVH2 comparison")
+    ap.add_argument("--width", type=int, default=0, help="override the workload's image width (profiling runs)")
+    ap.add_argument("--height", type=int, default=0, help="override the workload's image height")
+    ap.add_argument("--spp", type=int, default=0, help="override the workload's samples per pixel")
     args = ap.parse_args()
     world, rank, local, pg = dist_setup(args)
     if args.impl == "reference":
@@ -448,6 +539,10 @@ def main():
     b.build_lib()
     solrt = importlib.import_module("sol-rs_gb300")
     data, kw, cfg = workload(args.workload)
+    for key in ("width", "height", "spp"):   # reduced sizes for profiler captures
+        if getattr(args, key):
+            kw[key] = getattr(args, key)
+            cfg = dict(cfg, **{key: getattr(args, key)}, reduced=True)
     bvh = solrt.BVH8_Q8 if args.bvh == "bvh8" else solrt.BVH2
     c = data.camera
     cam = solrt.camera_look_at(c["eye"], c["center"], c["up"], c["vfov"], kw["width"] / kw["height"])
@@ -560,6 +655,12 @@ def main():
     img.close()
     sc.close()
     ctx.close()
+    precision = None
+    if rank == 0 and args.workload == "soup" and not args.no_precision:
+        try:
+            precision = precision_study(local, data, kw, cam, value / max(world, 1), info, nodes_per_seg, tris_per_seg)
+        except Exception as ex:
+            precision = {"error": str(ex)}
     # the other two parts of the headline metric, measured on smaller runs:
     # batched vs plain (first 32 jobs of the mixed-scene workload) and the
     # p99 latency of served jobs
@@ -587,7 +688,8 @@ def main():
                               bvh_build_ms=round(info.build_ms, 3), bvh_node_count=info.node_count),
                "segments_per_step": int(st.segments // args.steps), "fp64_fallbacks_per_segment": fb_per_seg,
                "gpu_launches": int(st.launches), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-               "clocks": clk, "rmse_vs_fp64": rmse, "batched_vs_plain": batched, "serving": serving}
+               "clocks": clk, "rmse_vs_fp64": rmse, "precision_study": precision, "batched_vs_plain": batched,
+               "serving": serving}
         print(json.dumps(out), flush=True)
     if pg is not None:
         pg.destroy_process_group()
