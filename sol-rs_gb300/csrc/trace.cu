@@ -4,11 +4,11 @@
 // (SMs x resident blocks) whose warps take rays from an atomic work counter,
 // so the queue length can stay on the device (no host round trip).
 //   BVH2: while-while traversal with per-lane refill (bvh2_ww.cuh).
-//   BVH8: one ray per lane, 32 rays per fetch (bvh8_traverse.cuh).
+//   BVH8: the same warp-uniform organisation over 8-wide nodes (bvh8_ww.cuh).
 #include <algorithm>
 
 #include "bvh2_ww.cuh"
-#include "bvh8_traverse.cuh"
+#include "bvh8_ww.cuh"
 #include "internal.h"
 
 namespace solrt {
@@ -92,22 +92,7 @@ __global__ void __launch_bounds__(kBlock, SOLRT_EXTEND_MINB) k_extend(IO io, con
     if constexpr (KIND == SOLRT_BVH2) {
         extend_bvh2_ww<IO, kCount, kBlock, kSmem>(io, n, work, cnt, ef);
     } else {
-        const int lane = threadIdx.x & 31;
-        for (;;) {
-            unsigned int base = 0;
-            if (lane == 0) base = atomicAdd(work, 32u);
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (base >= n) break;
-            const unsigned int i = base + lane;
-            if (i < n) {
-                float4 o, d;
-                TravScene ts;
-                io.load(i, o, d, ts);
-                HitRec h;
-                trace_bvh8<kCount>(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, ef);
-                io.store(i, h);
-            }
-        }
+        extend_bvh8_ww<IO, kCount>(io, n, work, cnt, ef);
     }
     flush_counters(stats, cnt, ef, kCount);
 }
