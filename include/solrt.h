@@ -122,7 +122,7 @@ typedef enum solrt_bvh_kind {
 
 typedef struct solrt_bvh_desc {
     uint32_t kind;       /* solrt_bvh_kind */
-    uint32_t leaf_max;   /* BVH8: max triangles per leaf child (1..3), 0 = 3 */
+    uint32_t leaf_max;   /* BVH8: max triangles per leaf child (1..3), 0 = 1 */
     uint32_t flags;      /* SOLRT_BVH_DYNAMIC (honoured by solrt_scene_create) */
     uint32_t reserved;
 } solrt_bvh_desc;
@@ -433,8 +433,8 @@ typedef struct solrt_tune_config {
 
 typedef struct solrt_tune_result {
     solrt_tune_config best;
-    float best_ms;         /* one launch of the batch with `best` */
-    float initial_ms;      /* one launch with the configuration the call started from */
+    float best_ms;         /* one launch of the timed jobs with `best` */
+    float initial_ms;      /* the same with the configuration the call started from */
     uint32_t candidates;   /* configurations timed */
     uint32_t reserved;
 } solrt_tune_result;
@@ -443,12 +443,13 @@ solrt_status solrt_context_get_tune(solrt_context* ctx, solrt_tune_config* out);
 /* Applies to later launches and plans (a batch already captured into a CUDA
  * graph keeps its launch shape until it is re-planned). */
 solrt_status solrt_context_set_tune(solrt_context* ctx, const solrt_tune_config* cfg);
-/* Times the batch under each extend block size x shared stack depth, then
- * under pass sizes of 1/4, 1/2 and all of the path capacity with the best of
- * those, keeps the fastest on the context and re-plans the batch with it.
- * Each candidate is launched three times (one warm-up): REF_MIX images hold
- * the last launch's frame afterwards, KAHAN images the sum of all of them
- * (clear them before rendering for real). */
+/* Times the batch (at most 32 of its jobs, spread over it) under each extend
+ * block size x shared stack depth, then under pass sizes of 1/4, 1/2 and all
+ * of the path capacity with the best of those, keeps the fastest on the
+ * context and re-plans the batch with it. Each candidate is launched three
+ * times (one warm-up): REF_MIX images of the timed jobs hold the last
+ * launch's frame afterwards, KAHAN images the sum of all of them (clear
+ * them before rendering for real). */
 solrt_status solrt_batch_autotune(solrt_batch* batch, solrt_tune_result* out);
 
 /* ------------------------------------------------------------------------ */

@@ -116,16 +116,33 @@ __global__ void k_gather(const uint32_t* __restrict__ tasks, uint32_t ntasks, co
     n_tris[t] = ntri;
 }
 
-// Smallest e with ext / 2^e <= 254, clamped to [-126, 127].
-__device__ __forceinline__ int grid_exponent(double ext) {
-    const double x = ext / 254.0;
+// Smallest e with ext / 2^e <= limit, clamped to [-126, 127].
+__device__ __forceinline__ int grid_exponent(double ext, double limit) {
+    const double x = ext / limit;
     if (!(x > 0.0)) return -126;
     int k = 0;
     const double m = frexp(x, &k);  // x = m * 2^k, m in [0.5, 1)
     int e = (m == 0.5) ? k - 1 : k;
     // x was rounded: make sure the grid really spans ext (scaling is exact)
-    while (e < 127 && ext * ldexp(1.0, -e) > 254.0) ++e;
+    while (e < 127 && ext * ldexp(1.0, -e) > limit) ++e;
     return e < -126 ? -126 : (e > 127 ? 127 : e);
+}
+
+// Anchor of a node's grid on one axis: one grid step below widen_lo(lo),
+// rounded down to a float, with the exponent raised until hi is within 253
+// steps. Every decoded face, q = 0 included, then lies at least one step
+// outside the child it bounds (q ranges over 0..255 with the +-1 margins).
+__device__ __forceinline__ void grid_anchor(float lo, float hi, float& p, int& e) {
+    const float p0 = widen_lo(lo);
+    e = grid_exponent((double)hi - (double)p0, 252.0);
+    for (;;) {
+        const double pd = (double)p0 - ldexp(1.0, e);
+        float pf = (float)pd;
+        if ((double)pf > pd) pf = nextafterf(pf, -INFINITY);
+        p = pf;
+        if (e >= 127 || ((double)hi - (double)pf) * ldexp(1.0, -e) <= 253.0) break;
+        ++e;
+    }
 }
 
 // Pass 2: slots, quantisation, node + next tasks + leaf triangles.
@@ -187,10 +204,7 @@ __global__ void k_emit(const uint32_t* __restrict__ tasks, uint32_t ntasks, uint
     // grid
     int e[3];
     float p[3];
-    for (int a = 0; a < 3; ++a) {
-        p[a] = widen_lo(nb.lo[a]);  // anchor just below the box (see widen_lo)
-        e[a] = grid_exponent((double)nb.hi[a] - (double)p[a]);
-    }
+    for (int a = 0; a < 3; ++a) grid_anchor(nb.lo[a], nb.hi[a], p[a], e[a]);
     uint32_t qlo[3][2] = {{0, 0}, {0, 0}, {0, 0}}, qhi[3][2] = {{0, 0}, {0, 0}, {0, 0}};
     uint32_t meta[2] = {0, 0};
     uint32_t imask = 0;
@@ -202,11 +216,10 @@ __global__ void k_emit(const uint32_t* __restrict__ tasks, uint32_t ntasks, uint
         if (i < 0) continue;
         for (int a = 0; a < 3; ++a) {
             const double inv_step = ldexp(1.0, -e[a]);
-            // Outward rounding plus one grid step of margin on every face off
-            // the anchor plane: a decoded face never lies within one step of
-            // the child's triangles unless it is the anchor plane itself
-            // (q = 0), whose distance the traversal computes without
-            // cancellation.
+            // Outward rounding plus one grid step of margin on every face:
+            // a decoded face never lies within one step of the child's
+            // triangles (the anchor sits one step below the node's box, so
+            // the low clamp below does not bind).
             const double lr = ((double)cb[i].lo[a] - (double)p[a]) * inv_step;
             const double hr = ((double)cb[i].hi[a] - (double)p[a]) * inv_step;
             double ql = floor(lr) - 1.0;

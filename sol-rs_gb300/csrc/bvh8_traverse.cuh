@@ -8,11 +8,11 @@
 // tested right away so that the closest distance shrinks early.
 //
 // Child box planes are decoded as p + q * 2^e from 8-bit q. The distance to
-// a plane is fma(q, 2^e / d, (p - o) / d): the build keeps every face other
-// than the anchor plane (q = 0) at least one grid step away from the child's
-// triangles, which bounds the rounding error of that form well inside the
-// margin, and the relative 2^-16 widening of the far distance covers the
-// rest. The anchor plane itself sits below the node's box by widen_lo. Zero
+// a plane is fma(q, 2^e / d, (p - o) / d): the build keeps every face (the
+// anchor plane q = 0 included: it sits one step below the node's box) at
+// least one grid step away from the child's triangles, which bounds the
+// rounding error of that form well inside the margin, and the relative 2^-16
+// widening of the far distance covers the rest. Zero
 // direction components are replaced by box_dir for these tests only (the
 // triangle test uses the exact direction).
 #pragma once
@@ -29,6 +29,11 @@ namespace solrt {
 // 2^23 and 2^23 is subtracted.
 SOLRT_D float byte_as_float(uint32_t word, uint32_t k) {
     return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7440u | k)) - 8388608.0f;
+}
+
+// byte k of `word` as the float 2^23 + byte, exactly.
+SOLRT_D float byte_biased(uint32_t word, uint32_t k) {
+    return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7440u | k));
 }
 
 template <bool kCount>

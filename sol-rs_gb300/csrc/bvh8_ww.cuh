@@ -38,9 +38,13 @@ SOLRT_D void bvh8_node_test(const uint4& w0, const uint4& w1, const uint4& w2, c
     const float sx = __uint_as_float((uint32_t)(ex + 127) << 23) * ix;
     const float sy = __uint_as_float((uint32_t)(ey + 127) << 23) * iy;
     const float sz = __uint_as_float((uint32_t)(ez + 127) << 23) * iz;
-    const float ax = (__uint_as_float(w0.x) - ox) * ix;
-    const float ay = (__uint_as_float(w0.y) - oy) * iy;
-    const float az = (__uint_as_float(w0.z) - oz) * iz;
+    // plane q is at t = (2^23 + q) * s + (a - 2^23 s): the biased byte
+    // (byte_biased) needs no conversion. Rounding a - 2^23 s adds at most half
+    // a grid step (in t) to each face, inside the one-step margin every face
+    // has (grid_anchor); the rest is relative to |t| as in trace_bvh8.
+    const float ax = fmaf(-8388608.0f, sx, (__uint_as_float(w0.x) - ox) * ix);
+    const float ay = fmaf(-8388608.0f, sy, (__uint_as_float(w0.y) - oy) * iy);
+    const float az = fmaf(-8388608.0f, sz, (__uint_as_float(w0.z) - oz) * iz);
     // near / far plane bytes per axis: lo is near for a positive direction
     const uint32_t nx0 = negx ? w3.z : w2.x, nx1 = negx ? w3.w : w2.y;
     const uint32_t fx0 = negx ? w2.x : w3.z, fx1 = negx ? w2.y : w3.w;
@@ -54,12 +58,12 @@ SOLRT_D void bvh8_node_test(const uint4& w0, const uint4& w1, const uint4& w2, c
     for (int s = 0; s < 8; ++s) {
         const uint32_t k = (uint32_t)(s & 3);
         const uint32_t meta = ((s < 4 ? w1.z : w1.w) >> (8u * k)) & 0xffu;
-        const float tnx = fmaf(byte_as_float(s < 4 ? nx0 : nx1, k), sx, ax);
-        const float tny = fmaf(byte_as_float(s < 4 ? ny0 : ny1, k), sy, ay);
-        const float tnz = fmaf(byte_as_float(s < 4 ? nz0 : nz1, k), sz, az);
-        const float tfx = fmaf(byte_as_float(s < 4 ? fx0 : fx1, k), sx, ax);
-        const float tfy = fmaf(byte_as_float(s < 4 ? fy0 : fy1, k), sy, ay);
-        const float tfz = fmaf(byte_as_float(s < 4 ? fz0 : fz1, k), sz, az);
+        const float tnx = fmaf(byte_biased(s < 4 ? nx0 : nx1, k), sx, ax);
+        const float tny = fmaf(byte_biased(s < 4 ? ny0 : ny1, k), sy, ay);
+        const float tnz = fmaf(byte_biased(s < 4 ? nz0 : nz1, k), sz, az);
+        const float tfx = fmaf(byte_biased(s < 4 ? fx0 : fx1, k), sx, ax);
+        const float tfy = fmaf(byte_biased(s < 4 ? fy0 : fy1, k), sy, ay);
+        const float tfz = fmaf(byte_biased(s < 4 ? fz0 : fz1, k), sz, az);
         const float tn = max3(tnx, tny, fmaxf(tnz, tmin));
         const float tf = min3(tfx, tfy, fminf(tfz, tmax));
         if (meta != 0u && tn <= tf * 1.0000153f) {

@@ -62,11 +62,26 @@ __global__ void k_centroids(const float4* __restrict__ vpos, const uint4* __rest
             mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], off));
         }
     }
+    // one atomic per block and bound (per-warp atomics on six addresses
+    // serialise at millions of triangles)
+    __shared__ float s_mn[3][32], s_mx[3][32];
+    const int warp = threadIdx.x >> 5, nwarps = (blockDim.x + 31) >> 5;
     if ((threadIdx.x & 31) == 0) {
         for (int k = 0; k < 3; ++k) {
-            atomicMin(cb + k, float_to_ordered(mn[k]));
-            atomicMax(cb + 3 + k, float_to_ordered(mx[k]));
+            s_mn[k][warp] = mn[k];
+            s_mx[k][warp] = mx[k];
         }
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        const int k = threadIdx.x;
+        float a = s_mn[k][0], b = s_mx[k][0];
+        for (int w = 1; w < nwarps; ++w) {
+            a = fminf(a, s_mn[k][w]);
+            b = fmaxf(b, s_mx[k][w]);
+        }
+        atomicMin(cb + k, float_to_ordered(a));
+        atomicMax(cb + 3 + k, float_to_ordered(b));
     }
 }
 
@@ -152,6 +167,62 @@ __global__ void __launch_bounds__(1024) k_scan_exclusive(uint32_t* __restrict__ 
         __syncthreads();
         if (threadIdx.x == 1023) carry = incl;
         __syncthreads();
+    }
+}
+
+// Exclusive scan of a long array in three launches: per-tile sums (tiles of
+// kScanTile counts, 4 per thread), one-block scan of the tile sums, then each
+// tile's scan offset by its tile's sum.
+constexpr int kScanTile = 4096;
+
+__device__ __forceinline__ uint32_t block_exclusive_1024(uint32_t x, uint32_t* warp_sums, uint32_t* total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = x;
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += y;
+    }
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = warp_sums[lane];
+        for (int off = 1; off < 32; off <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, w, off);
+            if (lane >= off) w += y;
+        }
+        warp_sums[lane] = w;
+    }
+    __syncthreads();
+    if (total) *total = warp_sums[31];
+    return incl - x + (warp > 0 ? warp_sums[warp - 1] : 0u);
+}
+
+__global__ void __launch_bounds__(1024) k_scan_reduce(const uint32_t* __restrict__ data, uint32_t len,
+                                                      uint32_t* __restrict__ sums) {
+    __shared__ uint32_t warp_sums[32];
+    const uint32_t base = blockIdx.x * kScanTile + 4u * threadIdx.x;
+    uint32_t x = 0;
+    for (uint32_t i = 0; i < 4; ++i)
+        if (base + i < len) x += data[base + i];
+    uint32_t total = 0;
+    block_exclusive_1024(x, warp_sums, &total);
+    if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_apply(uint32_t* __restrict__ data, uint32_t len,
+                                                     const uint32_t* __restrict__ sums) {
+    __shared__ uint32_t warp_sums[32];
+    const uint32_t base = blockIdx.x * kScanTile + 4u * threadIdx.x;
+    uint32_t v[4];
+    uint32_t x = 0;
+    for (uint32_t i = 0; i < 4; ++i) {
+        v[i] = base + i < len ? data[base + i] : 0u;
+        x += v[i];
+    }
+    uint32_t run = block_exclusive_1024(x, warp_sums, nullptr) + sums[blockIdx.x];
+    for (uint32_t i = 0; i < 4; ++i) {
+        if (base + i < len) data[base + i] = run;
+        run += v[i];
     }
 }
 
@@ -329,6 +400,21 @@ void launch_scan_exclusive(uint32_t* data, uint32_t len, cudaStream_t stream) {
     k_scan_exclusive<<<1, 1024, 0, stream>>>(data, len);
 }
 
+// Tile sums needed by scan_exclusive_tiled for `len` counts.
+static uint32_t scan_tiles(uint32_t len) { return blocks_for(len, kScanTile); }
+
+// Exclusive scan of `len` counts; `sums` holds scan_tiles(len) entries.
+static void scan_exclusive_tiled(uint32_t* data, uint32_t len, uint32_t* sums, cudaStream_t stream) {
+    const uint32_t tiles = scan_tiles(len);
+    if (tiles <= 1) {
+        k_scan_exclusive<<<1, 1024, 0, stream>>>(data, len);
+        return;
+    }
+    k_scan_reduce<<<tiles, 1024, 0, stream>>>(data, len, sums);
+    k_scan_exclusive<<<1, 1024, 0, stream>>>(sums, tiles);
+    k_scan_apply<<<tiles, 1024, 0, stream>>>(data, len, sums);
+}
+
 // Builds the LBVH of `sc` (and the 8-wide collapse when asked). Scratch is
 // allocated for the duration of the build. Synchronises.
 solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
@@ -353,6 +439,8 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
     }
     const uint32_t nblocks = blocks_for(n, kSortTile);
     SOLRT_TRY(hist.alloc(sizeof(uint32_t) * 256 * (size_t)nblocks));
+    DeviceBuffer scan_sums;
+    SOLRT_TRY(scan_sums.alloc(sizeof(uint32_t) * scan_tiles(256 * nblocks)));
     SOLRT_TRY(child.alloc(sizeof(uint32_t) * 2 * (size_t)ni));
     SOLRT_TRY(par_int.alloc(sizeof(uint32_t) * (size_t)ni));
     SOLRT_TRY(par_leaf.alloc(sizeof(uint32_t) * (size_t)n));
@@ -377,7 +465,7 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
     for (int shift = 0; shift < 30; shift += 8) {
         k_radix_hist<<<nblocks, kSortThreads, 0, st>>>(keys[cur].as<uint32_t>(), n, shift, nblocks,
                                                        hist.as<uint32_t>());
-        k_scan_exclusive<<<1, 1024, 0, st>>>(hist.as<uint32_t>(), 256 * nblocks);
+        scan_exclusive_tiled(hist.as<uint32_t>(), 256 * nblocks, scan_sums.as<uint32_t>(), st);
         k_radix_scatter<<<nblocks, kSortThreads, 0, st>>>(keys[cur].as<uint32_t>(), vals[cur].as<uint32_t>(),
                                                           keys[cur ^ 1].as<uint32_t>(), vals[cur ^ 1].as<uint32_t>(),
                                                           hist.as<uint32_t>(), n, shift, nblocks);
@@ -406,7 +494,7 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
         in.nbox = nbox.as<float4>();
         in.range = range.as<uint2>();
         in.tri_wt_leaf = sc.tri_wt.as<float4>();
-        in.leaf_max = desc.leaf_max == 0 ? 3u : std::min(3u, desc.leaf_max);
+        in.leaf_max = desc.leaf_max == 0 ? 1u : std::min(3u, desc.leaf_max);
         DeviceBuffer tri8;
         uint32_t node_count = 0, depth8 = 0;
         SOLRT_TRY(build_bvh8(ctx, in, sc.nodes, tri8, &node_count, &depth8));
@@ -525,7 +613,7 @@ solrt_status refit_bvh(Context& ctx, Scene& sc) {
         in.nbox = nbox.as<float4>();
         in.range = sc.topo_range.as<uint2>();
         in.tri_wt_leaf = tri2.as<float4>();
-        in.leaf_max = sc.desc.leaf_max == 0 ? 3u : std::min(3u, sc.desc.leaf_max);
+        in.leaf_max = sc.desc.leaf_max == 0 ? 1u : std::min(3u, sc.desc.leaf_max);
         DeviceBuffer nodes8, tri8;
         uint32_t node_count = 0, depth8 = 0;
         SOLRT_TRY(build_bvh8(ctx, in, nodes8, tri8, &node_count, &depth8));

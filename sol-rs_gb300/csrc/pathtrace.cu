@@ -680,15 +680,24 @@ solrt_status batch_autotune(Batch& b, solrt_tune_result* out) {
     Context& ctx = *b.ctx;
     const TuneConfig initial = ctx.tune;
     const std::vector<solrt_job> src = b.src;
+    // candidates are timed on at most kTuneJobs jobs spread over the batch
+    constexpr size_t kTuneJobs = 32;
+    std::vector<solrt_job> sample;
+    if (src.size() <= kTuneJobs) {
+        sample = src;
+    } else {
+        for (size_t i = 0; i < kTuneJobs; ++i) sample.push_back(src[i * src.size() / kTuneJobs]);
+    }
+    Batch tb;
     uint32_t candidates = 0;
     auto measure = [&](const TuneConfig& cfg, float* ms) -> solrt_status {
         ctx.tune = cfg;
-        if (b.exec) { cudaGraphExecDestroy(b.exec); b.exec = nullptr; }
-        if (b.graph) { cudaGraphDestroy(b.graph); b.graph = nullptr; }
-        SOLRT_TRY(batch_plan(ctx, src.data(), (uint32_t)src.size(), b.flags, b));
+        if (tb.exec) { cudaGraphExecDestroy(tb.exec); tb.exec = nullptr; }
+        if (tb.graph) { cudaGraphDestroy(tb.graph); tb.graph = nullptr; }
+        SOLRT_TRY(batch_plan(ctx, sample.data(), (uint32_t)sample.size(), b.flags, tb));
         float best = 0.0f;
         for (int r = 0; r < 3; ++r) {
-            SOLRT_TRY(batch_launch(b));
+            SOLRT_TRY(batch_launch(tb));
             SOLRT_CUDA(cudaEventSynchronize(ctx.ev1));
             float t = 0.0f;
             SOLRT_CUDA(cudaEventElapsedTime(&t, ctx.ev0, ctx.ev1));
@@ -728,8 +737,10 @@ solrt_status batch_autotune(Batch& b, solrt_tune_result* out) {
             SOLRT_TRY(measure(c, &ms));
             if (ms < best_ms) { best_ms = ms; best = c; }
         }
-        float final_ms = 0.0f;
-        SOLRT_TRY(measure(best, &final_ms));  // leaves the batch planned with `best`
+        ctx.tune = best;  // the whole batch, re-planned with the winner
+        if (b.exec) { cudaGraphExecDestroy(b.exec); b.exec = nullptr; }
+        if (b.graph) { cudaGraphDestroy(b.graph); b.graph = nullptr; }
+        SOLRT_TRY(batch_plan(ctx, src.data(), (uint32_t)src.size(), b.flags, b));
         if (out) {
             out->best.block_size = best.block;
             out->best.smem_stack = best.smem;
