@@ -283,7 +283,7 @@ typedef struct solrt_server solrt_server;
 
 typedef struct solrt_context_desc {
     int device;                  /* CUDA ordinal */
-    uint32_t path_capacity;      /* paths in flight per pass; 0 = default (8M) */
+    uint32_t path_capacity;      /* paths in flight per pass; 0 = default (32M, 4.8 GB of queues) */
     uint32_t enable_counters;    /* 1 = count node visits / triangle tests */
     uint32_t block_size;         /* extend kernel block size; 0 = default */
     uint32_t enable_timing;      /* 1 = CUDA-event timing of every extend / shade launch */
@@ -458,7 +458,7 @@ solrt_status solrt_batch_autotune(solrt_batch* batch, solrt_tune_result* out);
 
 typedef struct solrt_server_desc {
     uint64_t memory_budget;   /* bytes of job images + scenes in use; 0 = 150 GB */
-    uint32_t tick_paths;      /* paths per tick; 0 = the context's path capacity */
+    uint32_t tick_paths;      /* paths per tick; 0 = min(8M, the context's path capacity) */
     uint32_t reserved[5];
 } solrt_server_desc;
 

@@ -196,7 +196,7 @@ solrt_status solrt_context_create(const solrt_context_desc* desc, solrt_context*
     if (!c) return SOLRT_ERR_OOM;
     c->device = d.device;
     c->sm_count = prop.multiProcessorCount;
-    c->capacity = d.path_capacity ? d.path_capacity : (8u << 20);
+    c->capacity = d.path_capacity ? d.path_capacity : (32u << 20);
     c->counters = d.enable_counters != 0;
     c->block_size = d.block_size;
     if (d.block_size) {

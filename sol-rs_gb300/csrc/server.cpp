@@ -266,7 +266,9 @@ solrt_status solrt_server_create(solrt_context* ctx, const solrt_server_desc* de
     if (!srv) return SOLRT_ERR_OOM;
     srv->ctx = ctx;
     srv->budget = desc && desc->memory_budget ? desc->memory_budget : 150ull * 1000 * 1000 * 1000;
-    srv->tick_paths = desc && desc->tick_paths ? std::min(desc->tick_paths, ctx->capacity) : ctx->capacity;
+    // default tick: 8M paths (tens of ms), so that short jobs finish within a few ticks
+    srv->tick_paths = desc && desc->tick_paths ? std::min(desc->tick_paths, ctx->capacity)
+                                               : std::min(8u << 20, ctx->capacity);
     try {
         srv->th = std::thread(serve_loop, srv);
     } catch (...) {
