@@ -174,31 +174,28 @@ def sum_over_ranks(pg, v):
     return float(t.item())
 
 
-def cpu_baseline(data, kw, cam, budget_s=12.0, threads=0):
-    """Oracle FP32 render (its LBVH, all host cores) on a band of rows at
-    1 spp: Mrays/s over the band. Grows the band until ~budget_s."""
+def cpu_baseline(data, kw, cam, budget_s=10.0, threads=0):
+    """Oracle FP32 render (its LBVH, all host cores) of the full image at as
+    many samples per pixel as fit in about budget_s (at most the workload's
+    spp), sized from a timed band of rows at 1 spp: Mrays/s of that render."""
     import oracle
     solrt = importlib.import_module("sol-rs_gb300")
     o = oracle.OracleScene(data)
-    p = solrt.render_params(**dict(kw, spp=1))
     h = kw["height"]
-    rows = max(1, h // 64)
-    total_seg, total_t, total_rows = 0, 0.0, 0
-    while True:
-        r0 = (h // 2 - rows // 2)
-        t0 = time.perf_counter()
-        _, _, st = o.render(cam, p, rows=(r0, r0 + rows), threads=threads)
-        dt = time.perf_counter() - t0
-        total_seg += st.segments
-        total_t += dt
-        total_rows += rows
-        if total_t > budget_s * 0.3 or rows >= h:
-            break
-        rows = min(h, int(rows * max(2.0, budget_s * 0.6 / max(dt, 1e-3))))
+    rows = max(1, h // 16)
+    r0 = h // 2 - rows // 2
+    t0 = time.perf_counter()
+    o.render(cam, solrt.render_params(**dict(kw, spp=1)), rows=(r0, r0 + rows), threads=threads)
+    est = (time.perf_counter() - t0) * h / rows          # seconds for the full image at 1 spp
+    spp = max(1, min(kw["spp"], int(budget_s / max(est, 1e-6))))
+    t0 = time.perf_counter()
+    _, _, st = o.render(cam, solrt.render_params(**dict(kw, spp=spp)), threads=threads)
+    dt = time.perf_counter() - t0
     cores = threads if threads > 0 else (os.cpu_count() or 1)
-    sample = "%d rows x %d px x 1 spp (central band), FP32 oracle with its LBVH" % (total_rows, kw["width"])
-    return {"value": total_seg / total_t / 1e6, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
-            "segments": int(total_seg), "seconds": round(total_t, 3)}
+    sample = "full %dx%d image at %d of the workload's %d spp, FP32 oracle with its LBVH" % (
+        kw["width"], h, spp, kw["spp"])
+    return {"value": st.segments / dt / 1e6, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample,
+            "segments": int(st.segments), "seconds": round(dt, 3)}
 
 
 def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, main_tris, n_rays=1 << 22):
