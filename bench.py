@@ -390,7 +390,7 @@ def run_batch(args, world, rank, local, pg, njobs=None, steps=None, emit=True):
     return cmp
 
 
-def run_serve(local, rate, duration, n_scenes=16, seed=5):
+def run_serve(local, rate, duration, n_scenes=16, seed=5, policy=0):
     """Served render jobs: Poisson arrivals at `rate` jobs/s for `duration`
     seconds; each job draws a scene from a resident pool of config-4 scenes
     (randomised Cornell box + log-uniform soup), a resolution from
@@ -403,7 +403,7 @@ def run_serve(local, rate, duration, n_scenes=16, seed=5):
     c = S.CORNELL_CAMERA
     cam = solrt.camera_look_at(c["eye"], c["center"], c["up"], c["vfov"], 1.0)
     rng = np.random.default_rng(seed)
-    srv = solrt.Server(ctx)
+    srv = solrt.Server(ctx, policy=policy)
     arrivals = []
     t = 0.0
     while True:
@@ -447,7 +447,8 @@ def run_serve(local, rate, duration, n_scenes=16, seed=5):
     seg = ctx.stats().segments
     ctx.close()
     lat = np.array(lat) if lat else np.zeros(1)
-    return {"rate_jobs_per_s": rate, "duration_s": duration, "jobs": len(arrivals), "completed": int(st.completed),
+    return {"rate_jobs_per_s": rate, "duration_s": duration, "policy": ["fair", "shortest_first"][policy],
+            "jobs": len(arrivals), "completed": int(st.completed),
             "p50_latency_ms": round(float(np.percentile(lat, 50)), 2),
             "p99_latency_ms": round(float(np.percentile(lat, 99)), 2),
             "sustained_mrays_s": round(seg / wall / 1e6, 2), "wall_s": round(wall, 2),
@@ -508,6 +509,7 @@ def main():
     ap.add_argument("--jobs", type=int, default=256)
     ap.add_argument("--rate", type=float, default=6.0, help="serve: Poisson arrival rate, jobs/s")
     ap.add_argument("--duration", type=float, default=8.0, help="serve: arrival window, s")
+    ap.add_argument("--policy", default="fair", choices=["fair", "shortest"], help="serve: scheduling policy")
     ap.add_argument("--no-serve", action="store_true", help="skip the short serving run of the default line")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -525,7 +527,7 @@ def main():
         return 0
     if args.workload == "serve":
         importlib.import_module("sol-rs_gb300.build").build_lib()
-        out = run_serve(local, args.rate, args.duration)
+        out = run_serve(local, args.rate, args.duration, policy=1 if args.policy == "shortest" else 0)
         if rank == 0:
             print(json.dumps({"metric": "p99 job latency (served render jobs)", "value": out["p99_latency_ms"],
                               "unit": "ms", "higher_is_better": False, "n_gpus": world, "serving": out}), flush=True)

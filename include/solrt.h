@@ -456,10 +456,20 @@ solrt_status solrt_batch_autotune(solrt_batch* batch, solrt_tune_result* out);
 /* Serving: continuous batching of render jobs                              */
 /* ------------------------------------------------------------------------ */
 
+typedef enum solrt_serve_policy {
+    /* every active job gets an equal share of each tick's paths */
+    SOLRT_SERVE_FAIR = 0,
+    /* jobs with the least remaining work (pixels x samples left) first, each
+     * taking as many of its remaining samples as the tick has room for:
+     * short jobs finish in one tick while long ones wait */
+    SOLRT_SERVE_SHORTEST_FIRST = 1
+} solrt_serve_policy;
+
 typedef struct solrt_server_desc {
     uint64_t memory_budget;   /* bytes of job images + scenes in use; 0 = 150 GB */
     uint32_t tick_paths;      /* paths per tick; 0 = min(8M, the context's path capacity) */
-    uint32_t reserved[5];
+    uint32_t policy;          /* solrt_serve_policy */
+    uint32_t reserved[4];
 } solrt_server_desc;
 
 typedef struct solrt_job_result {

@@ -98,11 +98,12 @@ class Job(ctypes.Structure):
 
 
 BATCH_GRAPH = 1
+SERVE_FAIR, SERVE_SHORTEST_FIRST = 0, 1
 
 
 class ServerDesc(ctypes.Structure):
-    _fields_ = [("memory_budget", ctypes.c_uint64), ("tick_paths", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32 * 5)]
+    _fields_ = [("memory_budget", ctypes.c_uint64), ("tick_paths", ctypes.c_uint32), ("policy", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32 * 4)]
 
 
 class JobResult(ctypes.Structure):
@@ -531,10 +532,12 @@ class Server:
     """Continuous-batching render server (solrt_server): a serving thread
     admits jobs by memory budget and advances all active jobs each tick."""
 
-    def __init__(self, context, memory_budget=0, tick_paths=0):
+    def __init__(self, context, memory_budget=0, tick_paths=0, policy=0):
+        """policy: SERVE_FAIR (0) or SERVE_SHORTEST_FIRST (1)."""
         self.context = context
         h = ctypes.c_void_p()
-        check(lib().solrt_server_create(context.handle, ctypes.byref(ServerDesc(memory_budget, tick_paths)),
+        check(lib().solrt_server_create(context.handle,
+                                        ctypes.byref(ServerDesc(memory_budget, tick_paths, policy)),
                                         ctypes.byref(h)))
         self.handle = h
         self._scenes = {}

@@ -65,6 +65,7 @@ struct solrt_server {
     solrt_context* ctx = nullptr;
     uint64_t budget = 0;
     uint32_t tick_paths = 0;
+    uint32_t policy = SOLRT_SERVE_FAIR;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::thread th;
@@ -177,12 +178,26 @@ void serve_loop(solrt_server* srv) {
             tick_tickets.clear();
             fin_tickets.clear();
             tick_k.clear();
+            const bool shortest = srv->policy == SOLRT_SERVE_SHORTEST_FIRST;
+            if (shortest) {  // least remaining work first (ticket order breaks ties)
+                std::sort(srv->active.begin(), srv->active.end(), [&](uint64_t a, uint64_t b) {
+                    const ServerJob& x = srv->jobs[a];
+                    const ServerJob& y = srv->jobs[b];
+                    const uint64_t wx = (uint64_t)x.p.width * x.p.height * (x.p.spp - x.spp_done);
+                    const uint64_t wy = (uint64_t)y.p.width * y.p.height * (y.p.spp - y.spp_done);
+                    return wx != wy ? wx < wy : a < b;
+                });
+            }
             const uint32_t share = std::max<uint32_t>(1u, srv->tick_paths / (uint32_t)srv->active.size());
             for (uint64_t t : srv->active) {
                 ServerJob& j = srv->jobs[t];
                 const uint32_t np = j.p.width * j.p.height;
                 const uint32_t left = j.p.spp - j.spp_done;
-                uint32_t k = j.p.rng_mode == SOLRT_RNG_REF_STREAM ? 1u : std::max(1u, std::min(left, share / np));
+                // fair: an equal share; shortest first: what is left of the tick
+                const uint32_t room = shortest ? (srv->tick_paths > pp.paths ? srv->tick_paths - pp.paths : 0u)
+                                               : share;
+                if (shortest && room < np) continue;
+                uint32_t k = j.p.rng_mode == SOLRT_RNG_REF_STREAM ? 1u : std::max(1u, std::min(left, room / np));
                 if ((uint64_t)pp.paths + (uint64_t)np * k > ctx.capacity) {
                     if (pp.paths + np > ctx.capacity) continue;  // next tick
                     k = 1;
@@ -262,6 +277,10 @@ solrt_status solrt_server_create(solrt_context* ctx, const solrt_server_desc* de
         return SOLRT_ERR_INVALID;
     }
     *out = nullptr;
+    if (desc && desc->policy > SOLRT_SERVE_SHORTEST_FIRST) {
+        set_error("unknown serving policy %u", desc->policy);
+        return SOLRT_ERR_INVALID;
+    }
     solrt_server* srv = new (std::nothrow) solrt_server();
     if (!srv) return SOLRT_ERR_OOM;
     srv->ctx = ctx;
@@ -269,6 +288,7 @@ solrt_status solrt_server_create(solrt_context* ctx, const solrt_server_desc* de
     // default tick: 8M paths (tens of ms), so that short jobs finish within a few ticks
     srv->tick_paths = desc && desc->tick_paths ? std::min(desc->tick_paths, ctx->capacity)
                                                : std::min(8u << 20, ctx->capacity);
+    srv->policy = desc ? desc->policy : (uint32_t)SOLRT_SERVE_FAIR;
     try {
         srv->th = std::thread(serve_loop, srv);
     } catch (...) {

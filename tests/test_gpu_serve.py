@@ -29,11 +29,13 @@ def _job(solrt, i):
     return int(rng.integers(0, 3)), solrt.render_params(w, h, **kw)
 
 
-def test_served_results_equal_alone(solrt):
+@pytest.mark.parametrize("policy", [0, 1])
+def test_served_results_equal_alone(solrt, policy):
     ctx = solrt.Context(0)
     scenes = _scenes(solrt, ctx)
     datas = [S.cornell(), S.soup(20000, seed=2), S.tunnel(n_ang=128, n_ax=64, length=20.0)]
-    srv = solrt.Server(ctx, tick_paths=3000)   # small ticks: jobs span many ticks and overlap
+    # small ticks: jobs span many ticks and overlap
+    srv = solrt.Server(ctx, tick_paths=3000, policy=policy)
     tickets = []
     for i in range(24):
         si, p = _job(solrt, i)
@@ -104,3 +106,26 @@ def test_wait_is_bounded(solrt):
     r = srv.wait(t, 60000)
     assert r.status == 0
     srv.close()
+
+
+def test_shortest_first_finishes_small_jobs_first(solrt):
+    """Under SERVE_SHORTEST_FIRST a small job submitted after a large one,
+    while the large one is running, completes first."""
+    ctx = solrt.Context(0)
+    scenes = _scenes(solrt, ctx)
+    d = S.cornell()
+    srv = solrt.Server(ctx, tick_paths=20000, policy=solrt.api.SERVE_SHORTEST_FIRST)
+    big = solrt.render_params(128, 128, spp=64, max_bounces=4, material_mode=solrt.MATERIAL_LAMBERT,
+                              rng_mode=solrt.RNG_PER_SAMPLE, seed=1)
+    small = solrt.render_params(16, 16, spp=2, max_bounces=4, material_mode=solrt.MATERIAL_LAMBERT,
+                                rng_mode=solrt.RNG_PER_SAMPLE, seed=2, job_id=1)
+    tb = srv.submit(scenes[0], camera_of(d, 1.0), big)
+    time.sleep(0.002)
+    ts = srv.submit(scenes[0], camera_of(d, 1.0), small)
+    rs = srv.wait(ts, 60000)
+    rb = srv.wait(tb, 60000)
+    assert rs.status == 0 and rb.status == 0
+    assert rs.latency_ns < rb.latency_ns
+    srv.close()
+    with pytest.raises(solrt.SolrtError):
+        solrt.Server(ctx, policy=7)
