@@ -509,7 +509,7 @@ def main():
     ap.add_argument("--jobs", type=int, default=256)
     ap.add_argument("--rate", type=float, default=6.0, help="serve: Poisson arrival rate, jobs/s")
     ap.add_argument("--duration", type=float, default=8.0, help="serve: arrival window, s")
-    ap.add_argument("--policy", default="fair", choices=["fair", "shortest"], help="serve: scheduling policy")
+    ap.add_argument("--policy", default="shortest", choices=["fair", "shortest"], help="serve: scheduling policy")
     ap.add_argument("--no-serve", action="store_true", help="skip the short serving run of the default line")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -678,7 +678,7 @@ def main():
     if args.workload == "soup" and not args.no_serve:
         try:
             batched = run_batch(args, world, rank, local, pg, njobs=32, steps=2, emit=False)
-            serving = run_serve(local, args.rate, args.duration)
+            serving = run_serve(local, args.rate, args.duration, policy=1 if args.policy == "shortest" else 0)
         except Exception as ex:
             batched = batched or {"error": str(ex)}
             serving = serving or {"error": str(ex)}
