@@ -40,7 +40,7 @@ sys.path.insert(0, ROOT)
 METRIC = "Mrays/s at RMSE≤1e-3 vs FP64 oracle, batched vs plain on 1 GB300; p99 job latency"
 UNIT = "Mrays/s"
 
-NODE_BYTES = {0: 64, 1: 80}
+NODE_BYTES = {0: 64, 1: 80, 2: 64}
 
 
 def workload(name):
@@ -199,7 +199,7 @@ def cpu_baseline(data, kw, cam, budget_s=10.0, threads=0):
 
 
 def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, main_tris, n_rays=1 << 22):
-    """8-bit quantised 8-wide BVH vs the FP32 binary BVH on the same scene:
+    """8-bit quantised 4- and 8-wide BVHs vs the FP32 binary BVH on the same scene:
     hit records of 4M rays (every camera ray of the frame's first sample
     positions plus seeded rays from inside the scene) compared bit for bit on
     the device, node bytes, visits per segment, Mrays/s of one 64-spp frame
@@ -232,8 +232,8 @@ def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, mai
     out = {"rays_compared": n_rays, "leaf_max": 1}
     hits = {}
     with solrt.Context(local, enable_timing=True) as ctx, solrt.Context(local, enable_counters=True) as cctx:
-        for name, kind in (("bvh2_fp32", solrt.BVH2), ("bvh8_q8", solrt.BVH8_Q8)):
-            sc = solrt.SceneDescription(ctx, data, bvh=kind, leaf_max=1 if kind == solrt.BVH8_Q8 else 0)
+        for name, kind in (("bvh2_fp32", solrt.BVH2), ("bvh4_q8", solrt.BVH4_Q8), ("bvh8_q8", solrt.BVH8_Q8)):
+            sc = solrt.SceneDescription(ctx, data, bvh=kind, leaf_max=0 if kind == solrt.BVH2 else 1)
             info = sc.bvh_info()
             h = torch.zeros((n_rays, 4), dtype=torch.float32, device=dev)
             ctx.reset_stats()
@@ -273,8 +273,8 @@ def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, mai
                          "fp64_fallbacks_in_compared_rays": int(fb_trace), "build_ms": round(info.build_ms, 3)}
             sc.close()
     a = hits["bvh2_fp32"].view(torch.int32)
-    b8 = hits["bvh8_q8"].view(torch.int32)
-    out["hit_mismatches"] = int((a != b8).any(dim=1).sum().item())
+    out["hit_mismatches"] = {k: int((a != hits[k].view(torch.int32)).any(dim=1).sum().item())
+                             for k in ("bvh4_q8", "bvh8_q8")}
     out["hits"] = int((a[:, 1] != -1).sum().item())
     return out
 
@@ -287,7 +287,7 @@ def run_batch(args, world, rank, local, pg, njobs=None, steps=None, emit=True):
     import torch
     solrt = importlib.import_module("sol-rs_gb300")
     S = solrt.scenes
-    bvh = solrt.BVH8_Q8 if args.bvh == "bvh8" else solrt.BVH2
+    bvh = {"bvh2": solrt.BVH2, "bvh4": solrt.BVH4_Q8, "bvh8": solrt.BVH8_Q8}[args.bvh]
     njobs = args.jobs if njobs is None else njobs
     steps = args.steps if steps is None else steps
     ctx = solrt.Context(local)
@@ -505,7 +505,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="solrt", choices=["solrt", "reference"])
     ap.add_argument("--workload", default="soup", choices=["soup", "cornell", "tunnel", "batch", "serve"])
-    ap.add_argument("--bvh", default="bvh2", choices=["bvh2", "bvh8"])
+    ap.add_argument("--bvh", default="bvh2", choices=["bvh2", "bvh4", "bvh8"])
     ap.add_argument("--jobs", type=int, default=256)
     ap.add_argument("--rate", type=float, default=6.0, help="serve: Poisson arrival rate, jobs/s")
     ap.add_argument("--duration", type=float, default=8.0, help="serve: arrival window, s")
@@ -542,7 +542,7 @@ def main():
         if getattr(args, key):
             kw[key] = getattr(args, key)
             cfg = dict(cfg, **{key: getattr(args, key)}, reduced=True)
-    bvh = solrt.BVH8_Q8 if args.bvh == "bvh8" else solrt.BVH2
+    bvh = {"bvh2": solrt.BVH2, "bvh4": solrt.BVH4_Q8, "bvh8": solrt.BVH8_Q8}[args.bvh]
     c = data.camera
     cam = solrt.camera_look_at(c["eye"], c["center"], c["up"], c["vfov"], kw["width"] / kw["height"])
     params = solrt.render_params(**kw)

@@ -112,7 +112,8 @@ typedef struct solrt_scene_desc {
 
 typedef enum solrt_bvh_kind {
     SOLRT_BVH2 = 0,     /* binary LBVH, FP32 child boxes, 64 B nodes */
-    SOLRT_BVH8_Q8 = 1   /* 8-wide, 8-bit quantised child boxes, 80 B nodes */
+    SOLRT_BVH8_Q8 = 1,  /* 8-wide, 8-bit quantised child boxes, 80 B nodes */
+    SOLRT_BVH4_Q8 = 2   /* 4-wide, 8-bit quantised child boxes, 64 B nodes */
 } solrt_bvh_kind;
 
 /* solrt_bvh_desc.flags */
@@ -122,7 +123,7 @@ typedef enum solrt_bvh_kind {
 
 typedef struct solrt_bvh_desc {
     uint32_t kind;       /* solrt_bvh_kind */
-    uint32_t leaf_max;   /* BVH8: max triangles per leaf child (1..3), 0 = 1 */
+    uint32_t leaf_max;   /* BVH8 / BVH4: max triangles per leaf child (1..3), 0 = 1 */
     uint32_t flags;      /* SOLRT_BVH_DYNAMIC (honoured by solrt_scene_create) */
     uint32_t reserved;
 } solrt_bvh_desc;

@@ -30,9 +30,9 @@ struct Bvh8BuildInput {
 // In-place exclusive scan of `len` u32 counts (bvh_build.cu).
 void launch_scan_exclusive(uint32_t* data, uint32_t len, cudaStream_t stream);
 
-// Writes the 8-wide nodes into `nodes` and the triangles in 8-wide leaf order
-// into `tris`. Synchronises.
-solrt_status build_bvh8(Context& ctx, const Bvh8BuildInput& in, DeviceBuffer& nodes, DeviceBuffer& tris,
-                        uint32_t* node_count, uint32_t* depth);
+// Writes the `width`-wide nodes (8: 80 B, 4: 64 B) into `nodes` and the
+// triangles in leaf order into `tris`. Synchronises.
+solrt_status build_wide(Context& ctx, const Bvh8BuildInput& in, uint32_t width, DeviceBuffer& nodes,
+                        DeviceBuffer& tris, uint32_t* node_count, uint32_t* depth);
 
 }  // namespace solrt

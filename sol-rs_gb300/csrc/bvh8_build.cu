@@ -1,5 +1,5 @@
-// bvh8_build.cu — collapse of the binary LBVH into the 8-wide BVH with 8-bit
-// quantised child boxes (layout in bvh8.cuh).
+// bvh8_build.cu — collapse of the binary LBVH into the 8-wide or 4-wide BVH
+// with 8-bit quantised child boxes (layouts in bvh8.cuh and k_emit4).
 //
 // Level-synchronous and deterministic: each level is a list of tasks (one
 // binary node -> one 8-wide node). Per task, one thread
@@ -69,8 +69,9 @@ __device__ __forceinline__ float half_area(const Box3& b) {
 // Pass 1: gather children, count internal children and leaf triangles.
 __global__ void k_gather(const uint32_t* __restrict__ tasks, uint32_t ntasks, const uint32_t* __restrict__ child,
                          const uint2* __restrict__ range, const float4* __restrict__ nbox,
-                         const float4* __restrict__ tris, uint32_t leaf_max, uint32_t* __restrict__ gathered,
-                         uint32_t* __restrict__ n_inner, uint32_t* __restrict__ n_tris) {
+                         const float4* __restrict__ tris, uint32_t leaf_max, uint32_t width,
+                         uint32_t* __restrict__ gathered, uint32_t* __restrict__ n_inner,
+                         uint32_t* __restrict__ n_tris) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t > ntasks) return;
     if (t == ntasks) {  // trailing zero so the exclusive scans end with the totals
@@ -88,7 +89,7 @@ __global__ void k_gather(const uint32_t* __restrict__ tasks, uint32_t ntasks, co
         c[0] = child[2 * (size_t)b];
         c[1] = child[2 * (size_t)b + 1];
         m = 2;
-        while (m < 8) {
+        while (m < (int)width) {
             int best = -1;
             float best_a = -1.0f;
             for (int i = 0; i < m; ++i) {
@@ -261,16 +262,97 @@ __global__ void k_emit(const uint32_t* __restrict__ tasks, uint32_t ntasks, uint
     out[4] = make_uint4(qhi[1][0], qhi[1][1], qhi[2][0], qhi[2][1]);
 }
 
+// Pass 2 of the 4-wide collapse: quantisation as k_emit, slots in gathered
+// order (the traversal orders hit children by distance), 64-byte nodes:
+//   w0: origin p.xyz (float) | e.xyz (int8), imask (low 4 bits of the top byte)
+//   w1: child_base, tri_base, meta[0..3] (u8), qlo.x[0..3] (u8)
+//   w2: qlo.y[0..3], qlo.z[0..3], qhi.x[0..3], qhi.y[0..3]
+//   w3: qhi.z[0..3], 0, 0, 0
+__global__ void k_emit4(const uint32_t* __restrict__ tasks, uint32_t ntasks, uint32_t node_base,
+                        uint32_t next_base, uint32_t tri_level_base, const uint32_t* __restrict__ gathered,
+                        const uint32_t* __restrict__ inner_scan, const uint32_t* __restrict__ tri_scan,
+                        const uint2* __restrict__ range, const float4* __restrict__ nbox,
+                        const float4* __restrict__ tris_in, uint32_t leaf_max, uint4* __restrict__ nodes,
+                        uint32_t* __restrict__ next_tasks, float4* __restrict__ tris_out) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntasks) return;
+    Box3 cb[4];
+    uint32_t cr[4];
+    int m = 0;
+    for (int i = 0; i < 4; ++i) {
+        const uint32_t r = gathered[8 * (size_t)t + i];
+        if (r == 0xffffffffu) break;
+        cr[m] = r;
+        cb[m] = ref_box(r, nbox, tris_in);
+        ++m;
+    }
+    Box3 nb = cb[0];
+    for (int i = 1; i < m; ++i)
+        for (int a = 0; a < 3; ++a) {
+            nb.lo[a] = fminf(nb.lo[a], cb[i].lo[a]);
+            nb.hi[a] = fmaxf(nb.hi[a], cb[i].hi[a]);
+        }
+    int e[3];
+    float p[3];
+    for (int a = 0; a < 3; ++a) grid_anchor(nb.lo[a], nb.hi[a], p[a], e[a]);
+    uint32_t qlo[3] = {0, 0, 0}, qhi[3] = {0, 0, 0};
+    uint32_t meta = 0, imask = 0;
+    const uint32_t child_base = next_base + inner_scan[t];
+    const uint32_t tri_base = tri_level_base + tri_scan[t];
+    uint32_t inner_rank = 0, tri_off = 0;
+    for (int s = 0; s < m; ++s) {
+        for (int a = 0; a < 3; ++a) {
+            const double inv_step = ldexp(1.0, -e[a]);
+            // outward rounding + one grid step of margin (see k_emit)
+            const double lr = ((double)cb[s].lo[a] - (double)p[a]) * inv_step;
+            const double hr = ((double)cb[s].hi[a] - (double)p[a]) * inv_step;
+            double ql = floor(lr) - 1.0;
+            double qh = ceil(hr) + 1.0;
+            ql = ql < 0.0 ? 0.0 : ql;
+            qh = qh > 255.0 ? 255.0 : qh;
+            qlo[a] |= (uint32_t)ql << (8u * (uint32_t)s);
+            qhi[a] |= (uint32_t)qh << (8u * (uint32_t)s);
+        }
+        const uint32_t r = cr[s];
+        const uint32_t k = ref_count(r, range);
+        uint32_t mb;
+        if (k > leaf_max) {
+            imask |= 1u << s;
+            mb = 1u << 5;
+            next_tasks[inner_scan[t] + inner_rank] = r;
+            ++inner_rank;
+        } else {
+            mb = (((1u << k) - 1u) << 5) | tri_off;
+            const uint32_t first = ref_first(r, range);
+            for (uint32_t j = 0; j < k; ++j) {
+                const size_t src = 3 * (size_t)(first + j), dst = 3 * (size_t)(tri_base + tri_off + j);
+                tris_out[dst] = tris_in[src];
+                tris_out[dst + 1] = tris_in[src + 1];
+                tris_out[dst + 2] = tris_in[src + 2];
+            }
+            tri_off += k;
+        }
+        meta |= mb << (8u * (uint32_t)s);
+    }
+    const uint32_t packed = ((uint32_t)(uint8_t)(int8_t)e[0]) | ((uint32_t)(uint8_t)(int8_t)e[1] << 8) |
+                            ((uint32_t)(uint8_t)(int8_t)e[2] << 16) | (imask << 24);
+    uint4* out = nodes + 4 * (size_t)(node_base + t);
+    out[0] = make_uint4(__float_as_uint(p[0]), __float_as_uint(p[1]), __float_as_uint(p[2]), packed);
+    out[1] = make_uint4(child_base, tri_base, meta, qlo[0]);
+    out[2] = make_uint4(qlo[1], qlo[2], qhi[0], qhi[1]);
+    out[3] = make_uint4(qhi[2], 0u, 0u, 0u);
+}
+
 inline uint32_t blocks_of(uint64_t n, uint32_t b) { return (uint32_t)((n + b - 1) / b); }
 
 }  // namespace
 
-solrt_status build_bvh8(Context& ctx, const Bvh8BuildInput& in, DeviceBuffer& nodes, DeviceBuffer& tris,
-                        uint32_t* node_count, uint32_t* depth) {
+solrt_status build_wide(Context& ctx, const Bvh8BuildInput& in, uint32_t width, DeviceBuffer& nodes,
+                        DeviceBuffer& tris, uint32_t* node_count, uint32_t* depth) {
     const uint32_t n = in.n;
     cudaStream_t st = ctx.stream;
     const uint32_t max_nodes = std::max(1u, n);
-    SOLRT_TRY(nodes.alloc(80ull * max_nodes));
+    SOLRT_TRY(nodes.alloc((width == 4 ? 64ull : 80ull) * max_nodes));
     SOLRT_TRY(tris.alloc(48ull * n));
     DeviceBuffer task[2], gathered, inner, ntri;
     SOLRT_TRY(task[0].alloc(4ull * max_nodes));
@@ -284,11 +366,11 @@ solrt_status build_bvh8(Context& ctx, const Bvh8BuildInput& in, DeviceBuffer& no
     int cur = 0;
     while (ntasks > 0) {
         if (node_base + ntasks > max_nodes) {
-            set_error("BVH8 collapse overflowed its node bound");
+            set_error("wide BVH collapse overflowed its node bound");
             return SOLRT_ERR_CAPACITY;
         }
         k_gather<<<blocks_of(ntasks + 1, 128), 128, 0, st>>>(task[cur].as<uint32_t>(), ntasks, in.child, in.range,
-                                                             in.nbox, in.tri_wt_leaf, in.leaf_max,
+                                                             in.nbox, in.tri_wt_leaf, in.leaf_max, width,
                                                              gathered.as<uint32_t>(), inner.as<uint32_t>(),
                                                              ntri.as<uint32_t>());
         launch_scan_exclusive(inner.as<uint32_t>(), ntasks + 1, st);
@@ -297,11 +379,18 @@ solrt_status build_bvh8(Context& ctx, const Bvh8BuildInput& in, DeviceBuffer& no
         SOLRT_CUDA(cudaMemcpyAsync(&totals[0], inner.as<uint32_t>() + ntasks, 4, cudaMemcpyDeviceToHost, st));
         SOLRT_CUDA(cudaMemcpyAsync(&totals[1], ntri.as<uint32_t>() + ntasks, 4, cudaMemcpyDeviceToHost, st));
         const uint32_t next_base = node_base + ntasks;
-        k_emit<<<blocks_of(ntasks, 128), 128, 0, st>>>(task[cur].as<uint32_t>(), ntasks, node_base, next_base,
-                                                       tri_level_base, gathered.as<uint32_t>(), inner.as<uint32_t>(),
-                                                       ntri.as<uint32_t>(), in.range, in.nbox, in.tri_wt_leaf,
-                                                       in.leaf_max, nodes.as<uint4>(), task[cur ^ 1].as<uint32_t>(),
-                                                       tris.as<float4>());
+        if (width == 4)
+            k_emit4<<<blocks_of(ntasks, 128), 128, 0, st>>>(task[cur].as<uint32_t>(), ntasks, node_base, next_base,
+                                                            tri_level_base, gathered.as<uint32_t>(),
+                                                            inner.as<uint32_t>(), ntri.as<uint32_t>(), in.range,
+                                                            in.nbox, in.tri_wt_leaf, in.leaf_max, nodes.as<uint4>(),
+                                                            task[cur ^ 1].as<uint32_t>(), tris.as<float4>());
+        else
+            k_emit<<<blocks_of(ntasks, 128), 128, 0, st>>>(task[cur].as<uint32_t>(), ntasks, node_base, next_base,
+                                                           tri_level_base, gathered.as<uint32_t>(),
+                                                           inner.as<uint32_t>(), ntri.as<uint32_t>(), in.range,
+                                                           in.nbox, in.tri_wt_leaf, in.leaf_max, nodes.as<uint4>(),
+                                                           task[cur ^ 1].as<uint32_t>(), tris.as<float4>());
         ctx.launches += 4;
         SOLRT_CUDA(cudaStreamSynchronize(st));
         SOLRT_CUDA(cudaGetLastError());
@@ -311,12 +400,12 @@ solrt_status build_bvh8(Context& ctx, const Bvh8BuildInput& in, DeviceBuffer& no
         ntasks = totals[0];
         cur ^= 1;
         if (levels > 4096) {
-            set_error("BVH8 collapse did not terminate");
+            set_error("wide BVH collapse did not terminate");
             return SOLRT_ERR_DEVICE;
         }
     }
     if (tri_level_base != n) {
-        set_error("BVH8 collapse placed %u of %u triangles", tri_level_base, n);
+        set_error("wide BVH collapse placed %u of %u triangles", tri_level_base, n);
         return SOLRT_ERR_DEVICE;
     }
     *node_count = node_base;

@@ -394,6 +394,20 @@ __global__ void k_depth(const uint32_t* __restrict__ parent_int, const uint32_t*
 
 inline uint32_t blocks_for(uint64_t n, uint32_t b) { return (uint32_t)((n + b - 1) / b); }
 
+// A wide BVH of `depth` levels must fit its traversal stack: BVH8 pushes
+// one node group per level, BVH4 up to three node indices per level.
+solrt_status check_wide_depth(uint32_t width, uint32_t depth) {
+    if (width == 8 && depth > SOLRT_BVH8_STACK) {
+        set_error("BVH8 depth %u exceeds the traversal stack (%d)", depth, SOLRT_BVH8_STACK);
+        return SOLRT_ERR_CAPACITY;
+    }
+    if (width == 4 && 3u * depth + 1u > SOLRT_BVH2_STACK) {
+        set_error("BVH4 depth %u exceeds the traversal stack (%d)", depth, SOLRT_BVH2_STACK);
+        return SOLRT_ERR_CAPACITY;
+    }
+    return SOLRT_OK;
+}
+
 }  // namespace
 
 void launch_scan_exclusive(uint32_t* data, uint32_t len, cudaStream_t stream) {
@@ -487,7 +501,8 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
     ctx.launches += 5;
     SOLRT_CUDA(cudaGetLastError());
 
-    if (desc.kind == SOLRT_BVH8_Q8) {
+    if (desc.kind == SOLRT_BVH8_Q8 || desc.kind == SOLRT_BVH4_Q8) {
+        const uint32_t width = desc.kind == SOLRT_BVH4_Q8 ? 4u : 8u;
         Bvh8BuildInput in;
         in.n = n;
         in.child = child.as<uint32_t>();
@@ -497,7 +512,7 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
         in.leaf_max = desc.leaf_max == 0 ? 1u : std::min(3u, desc.leaf_max);
         DeviceBuffer tri8;
         uint32_t node_count = 0, depth8 = 0;
-        SOLRT_TRY(build_bvh8(ctx, in, sc.nodes, tri8, &node_count, &depth8));
+        SOLRT_TRY(build_wide(ctx, in, width, sc.nodes, tri8, &node_count, &depth8));
         sc.tri_wt.release();
         sc.tri_wt.ptr = tri8.ptr;
         sc.tri_wt.bytes = tri8.bytes;
@@ -505,11 +520,8 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
         tri8.bytes = 0;
         sc.info.node_count = node_count;
         sc.info.depth = depth8;
-        sc.info.node_bytes = (uint64_t)node_count * 80u;
-        if (depth8 > SOLRT_BVH8_STACK) {
-            set_error("BVH8 depth %u exceeds the traversal stack (%d)", depth8, SOLRT_BVH8_STACK);
-            return SOLRT_ERR_CAPACITY;
-        }
+        sc.info.node_bytes = (uint64_t)node_count * (width == 4 ? 64u : 80u);
+        SOLRT_TRY(check_wide_depth(width, depth8));
     } else {
         sc.nodes.ptr = bvh2_nodes.ptr;
         sc.nodes.bytes = bvh2_nodes.bytes;
@@ -587,7 +599,8 @@ solrt_status refit_bvh(Context& ctx, Scene& sc) {
     const uint32_t ni = n > 1 ? n - 1 : 1;
     cudaStream_t st = ctx.stream;
     SOLRT_CUDA(cudaEventRecord(ctx.ev0, st));
-    const bool b8 = sc.info.kind == SOLRT_BVH8_Q8;
+    const bool b8 = sc.info.kind == SOLRT_BVH8_Q8 || sc.info.kind == SOLRT_BVH4_Q8;
+    const uint32_t width = sc.info.kind == SOLRT_BVH4_Q8 ? 4u : 8u;
     DeviceBuffer flags, nbox, nodes2, tri2;
     SOLRT_TRY(flags.alloc(sizeof(unsigned int) * (size_t)ni));
     SOLRT_TRY(nbox.alloc(2 * sizeof(float4) * (size_t)ni));
@@ -616,16 +629,13 @@ solrt_status refit_bvh(Context& ctx, Scene& sc) {
         in.leaf_max = sc.desc.leaf_max == 0 ? 1u : std::min(3u, sc.desc.leaf_max);
         DeviceBuffer nodes8, tri8;
         uint32_t node_count = 0, depth8 = 0;
-        SOLRT_TRY(build_bvh8(ctx, in, nodes8, tri8, &node_count, &depth8));
-        if (depth8 > SOLRT_BVH8_STACK) {
-            set_error("BVH8 depth %u exceeds the traversal stack (%d)", depth8, SOLRT_BVH8_STACK);
-            return SOLRT_ERR_CAPACITY;
-        }
+        SOLRT_TRY(build_wide(ctx, in, width, nodes8, tri8, &node_count, &depth8));
+        SOLRT_TRY(check_wide_depth(width, depth8));
         sc.nodes.adopt(nodes8);
         sc.tri_wt.adopt(tri8);
         sc.info.node_count = node_count;
         sc.info.depth = depth8;
-        sc.info.node_bytes = (uint64_t)node_count * 80u;
+        sc.info.node_bytes = (uint64_t)node_count * (width == 4 ? 64u : 80u);
         sc.info.tri_bytes = sc.tri_wt.bytes;
     }
     SOLRT_CUDA(cudaEventRecord(ctx.ev1, st));

@@ -24,6 +24,7 @@
 #include <algorithm>
 
 #include "bvh2_ww.cuh"
+#include "bvh4_ww.cuh"
 #include "bvh8_traverse.cuh"
 #include "internal.h"
 #include "path_ops.cuh"
@@ -180,6 +181,7 @@ __global__ void __launch_bounds__(128) k_megakernel(const DevJob* __restrict__ j
             for (;;) {
                 HitRec h;
                 if (KIND == SOLRT_BVH8_Q8) trace_bvh8<false>(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, fb_ef[1]);
+                else if (KIND == SOLRT_BVH4_Q8) trace_bvh4_ray(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, fb_ef[1]);
                 else trace_bvh2_ray(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, fb_ef[1]);
                 ++segs;
                 float4 on, dn;
@@ -249,6 +251,7 @@ __device__ __forceinline__ void trace_one(const TravScene& ts, float ox, float o
                                           float dz, float tmin, float tmax, HitRec& h, TraceCounters& cnt,
                                           uint32_t& ef) {
     if (KIND == SOLRT_BVH8_Q8) trace_bvh8<false>(ts, ox, oy, oz, dx, dy, dz, tmin, tmax, h, cnt, ef);
+    else if (KIND == SOLRT_BVH4_Q8) trace_bvh4_ray(ts, ox, oy, oz, dx, dy, dz, tmin, tmax, h, cnt, ef);
     else trace_bvh2_ray(ts, ox, oy, oz, dx, dy, dz, tmin, tmax, h, cnt, ef);
 }
 
@@ -818,12 +821,14 @@ static solrt_status render_sibling(Context& ctx, const Scene& sc, const solrt_ca
     const DevJob* dj = ctx.sibling_job.as<DevJob>();
     DevStats* stats = ctx.stats.as<DevStats>();
     SOLRT_CUDA(cudaEventRecord(ctx.ev0, ctx.stream));
-    const bool b8 = sc.info.kind == SOLRT_BVH8_Q8;
+    const uint32_t kind = sc.info.kind;
     if (p.integrator == SOLRT_INTEGRATOR_DEBUG) {
-        if (b8) k_debug<SOLRT_BVH8_Q8><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
+        if (kind == SOLRT_BVH8_Q8) k_debug<SOLRT_BVH8_Q8><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
+        else if (kind == SOLRT_BVH4_Q8) k_debug<SOLRT_BVH4_Q8><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
         else k_debug<SOLRT_BVH2><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
     } else {
-        if (b8) k_ao<SOLRT_BVH8_Q8><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
+        if (kind == SOLRT_BVH8_Q8) k_ao<SOLRT_BVH8_Q8><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
+        else if (kind == SOLRT_BVH4_Q8) k_ao<SOLRT_BVH4_Q8><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
         else k_ao<SOLRT_BVH2><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
     }
     ++ctx.launches;
@@ -850,6 +855,8 @@ solrt_status render_frame(Context& ctx, const Scene& sc, const solrt_camera& cam
     SOLRT_CUDA(cudaEventRecord(ctx.ev0, ctx.stream));
     if (b.kind == SOLRT_BVH8_Q8)
         k_megakernel<SOLRT_BVH8_Q8><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(b.d_jobs.as<DevJob>(), ctx.stats.as<DevStats>());
+    else if (b.kind == SOLRT_BVH4_Q8)
+        k_megakernel<SOLRT_BVH4_Q8><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(b.d_jobs.as<DevJob>(), ctx.stats.as<DevStats>());
     else
         k_megakernel<SOLRT_BVH2><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(b.d_jobs.as<DevJob>(), ctx.stats.as<DevStats>());
     k_finalize<<<cdiv(npix, 256), 256, 0, ctx.stream>>>(b.d_jobs.as<DevJob>(), b.d_job_pix.as<uint32_t>(), 1u, npix);

@@ -4,10 +4,12 @@
 // (SMs x resident blocks) whose warps take rays from an atomic work counter,
 // so the queue length can stay on the device (no host round trip).
 //   BVH2: while-while traversal with per-lane refill (bvh2_ww.cuh).
-//   BVH8: the same warp-uniform organisation over 8-wide nodes (bvh8_ww.cuh).
+//   BVH8 / BVH4: the same warp-uniform organisation over quantised wide
+//   nodes (bvh8_ww.cuh, bvh4_ww.cuh).
 #include <algorithm>
 
 #include "bvh2_ww.cuh"
+#include "bvh4_ww.cuh"
 #include "bvh8_ww.cuh"
 #include "internal.h"
 
@@ -91,6 +93,8 @@ __global__ void __launch_bounds__(kBlock, SOLRT_EXTEND_MINB) k_extend(IO io, con
     uint32_t ef = 0;
     if constexpr (KIND == SOLRT_BVH2) {
         extend_bvh2_ww<IO, kCount, kBlock, kSmem>(io, n, work, cnt, ef);
+    } else if constexpr (KIND == SOLRT_BVH4_Q8) {
+        extend_bvh4_ww<IO, kCount, kBlock, kSmem>(io, n, work, cnt, ef);
     } else {
         extend_bvh8_ww<IO, kCount>(io, n, work, cnt, ef);
     }
@@ -115,7 +119,7 @@ void launch_variant(const Context& ctx, const IO& io, const unsigned int* count,
 template <int KIND, class IO>
 solrt_status launch_tuned(const Context& ctx, const IO& io, const unsigned int* count, uint32_t n_static,
                           uint32_t n_cap, unsigned int* work, DevStats* st) {
-    constexpr int S = KIND == SOLRT_BVH2 ? 1 : 0;  // BVH8 keeps its stack in registers / local memory
+    constexpr int S = KIND == SOLRT_BVH8_Q8 ? 0 : 1;  // BVH8 keeps its stack in local memory
     if (ctx.counters) {
         launch_variant<KIND, IO, true, kExtendBlock, S * SOLRT_SMEM_STACK>(ctx, io, count, n_static, n_cap, work, st);
         return SOLRT_OK;
@@ -148,6 +152,7 @@ solrt_status launch_extend(Context& ctx, uint32_t kind, const DevJob* jobs, cons
     const QueueIO io{q.o_tmin, q.d_tmax, q.meta, jobs, hits};
     DevStats* st = ctx.stats.as<DevStats>();
     if (kind == SOLRT_BVH8_Q8) SOLRT_TRY((launch_tuned<SOLRT_BVH8_Q8>(ctx, io, count, 0, 0, work, st)));
+    else if (kind == SOLRT_BVH4_Q8) SOLRT_TRY((launch_tuned<SOLRT_BVH4_Q8>(ctx, io, count, 0, 0, work, st)));
     else SOLRT_TRY((launch_tuned<SOLRT_BVH2>(ctx, io, count, 0, 0, work, st)));
     ++ctx.launches;
     SOLRT_CUDA(cudaGetLastError());
@@ -162,6 +167,7 @@ solrt_status launch_trace_rays(Context& ctx, const Scene& sc, const solrt_ray* r
     SOLRT_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned int), ctx.stream));
     DevStats* st = ctx.stats.as<DevStats>();
     if (d.bvh_kind == SOLRT_BVH8_Q8) SOLRT_TRY((launch_tuned<SOLRT_BVH8_Q8>(ctx, io, nullptr, n, n, work, st)));
+    else if (d.bvh_kind == SOLRT_BVH4_Q8) SOLRT_TRY((launch_tuned<SOLRT_BVH4_Q8>(ctx, io, nullptr, n, n, work, st)));
     else SOLRT_TRY((launch_tuned<SOLRT_BVH2>(ctx, io, nullptr, n, n, work, st)));
     ++ctx.launches;
     SOLRT_CUDA(cudaGetLastError());

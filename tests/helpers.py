@@ -115,3 +115,8 @@ def transformed_cornell():
     inst["transform_it"] = Tit.T.reshape(-1).astype(np.float32)
     d.instances = inst
     return d
+
+
+def bvh_kind(solrt_mod, name):
+    """"bvh2" / "bvh4" / "bvh8" -> solrt BVH kind."""
+    return {"bvh2": solrt_mod.BVH2, "bvh4": solrt_mod.BVH4_Q8, "bvh8": solrt_mod.BVH8_Q8}[name]

@@ -7,7 +7,7 @@ batched path."""
 import numpy as np
 import pytest
 
-from helpers import S, camera_of, empty_scene, single_triangle, transformed_cornell
+from helpers import S, bvh_kind, camera_of, empty_scene, single_triangle, transformed_cornell
 
 pytestmark = pytest.mark.gpu
 
@@ -55,9 +55,9 @@ def _alone(solrt, ctx, jobs, frames=1):
 
 
 @pytest.mark.parametrize("graph", [False, True])
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh8"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh4", "bvh8"])
 def test_batch_equals_alone(solrt, ctx, bvh, graph):
-    kind = solrt.BVH2 if bvh == "bvh2" else solrt.BVH8_Q8
+    kind = bvh_kind(solrt, bvh)
     jobs = _make(solrt, ctx, kind)
     batch = solrt.Batch(ctx, jobs, graph=graph)
     ctx.reset_stats()
@@ -124,13 +124,13 @@ def test_batch_rejects_mixed_bvh_kinds(solrt, ctx):
         solrt.Batch(ctx, [(a, ia, cam, p), (b, ib, cam, p)])
 
 
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh8"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh4", "bvh8"])
 def test_autotune_keeps_images(solrt, bvh):
     """solrt_batch_autotune times every extend block size x shared stack
     depth and three pass sizes; the batch re-planned with the winner renders
     the same images as the default configuration, and the winner stays on
     the context."""
-    kind = solrt.BVH2 if bvh == "bvh2" else solrt.BVH8_Q8
+    kind = bvh_kind(solrt, bvh)
     c = solrt.Context(0, path_capacity=1 << 18)
     jobs = _make(solrt, c, kind)
     b = solrt.Batch(c, jobs, graph=True)
@@ -140,7 +140,7 @@ def test_autotune_keeps_images(solrt, bvh):
     r = b.autotune()
     for _, img, _, _ in jobs:   # KAHAN images summed every tuning launch
         img.clear()
-    assert r["candidates"] >= (8 if bvh == "bvh2" else 5)
+    assert r["candidates"] >= (5 if bvh == "bvh8" else 8)
     assert r["block_size"] in (64, 128, 256) and r["smem_stack"] in (16, 32)
     assert r["best_ms"] > 0 and r["best_ms"] <= r["initial_ms"] * 1.05
     assert c.get_tune() == {k: r[k] for k in ("block_size", "smem_stack", "pass_paths")}

@@ -79,17 +79,38 @@ def _decode_bvh8(nodes_u8):
     return dict(child_base=w[:, 4], tri_base=w[:, 5], imask=imask, meta=meta, lo=lo, hi=hi)
 
 
+def _decode_bvh4(nodes_u8):
+    """64-byte 4-wide nodes: p.xyz | e.xyz, imask; child_base, tri_base,
+    meta[4], qlo.x[4]; qlo.y, qlo.z, qhi.x, qhi.y; qhi.z."""
+    w = nodes_u8.view(np.uint32).reshape(-1, 16)
+    p = w[:, 0:3].copy().view(np.float32).astype(np.float64)
+    e = np.stack([((w[:, 3] >> (8 * a)) & 0xFF).astype(np.uint8).view(np.int8) for a in range(3)], 1)
+    imask = w[:, 3] >> 24
+    scale = np.ldexp(1.0, e.astype(np.int64))
+
+    def bytes4(c):
+        return w[:, c].copy().view(np.uint8).reshape(-1, 4).astype(np.float64)
+
+    qlo = np.stack([bytes4(7), bytes4(8), bytes4(9)], 2)
+    qhi = np.stack([bytes4(10), bytes4(11), bytes4(12)], 2)
+    lo = p[:, None, :] + qlo * scale[:, None, :]
+    hi = p[:, None, :] + qhi * scale[:, None, :]
+    meta = w[:, 6].copy().view(np.uint8).reshape(-1, 4)
+    return dict(child_base=w[:, 4], tri_base=w[:, 5], imask=imask, meta=meta, lo=lo, hi=hi)
+
+
+@pytest.mark.parametrize("width", [8, 4])
 @pytest.mark.parametrize("maker", [lambda: S.cornell(), lambda: S.soup(40000, seed=3),
                                    lambda: S.tunnel(n_ang=128, n_ax=64, length=20.0), lambda: single_triangle()])
-def test_bvh8_conservative_and_complete(solrt, ctx, maker):
+def test_wide_bvh_conservative_and_complete(solrt, ctx, maker, width):
     """Every triangle is referenced by exactly one leaf slot and lies inside
     the decoded (quantised) box of that slot and of every ancestor slot."""
     d = maker()
-    sc = solrt.SceneDescription(ctx, d, bvh=solrt.BVH8_Q8)
+    sc = solrt.SceneDescription(ctx, d, bvh=solrt.BVH8_Q8 if width == 8 else solrt.BVH4_Q8)
     nodes, tris = sc.bvh_export()
     info = sc.bvh_info()
     n = info.tri_count
-    dec = _decode_bvh8(nodes)
+    dec = _decode_bvh8(nodes) if width == 8 else _decode_bvh4(nodes)
     tv = tris.view(np.float32).reshape(-1, 3, 4)[:, :, :3].astype(np.float64)
     prim = tris.view(np.uint32).reshape(-1, 12)[:, 3]
     assert np.array_equal(np.sort(prim), np.arange(n))
@@ -99,7 +120,7 @@ def test_bvh8_conservative_and_complete(solrt, ctx, maker):
     while stack:
         node, alo, ahi = stack.pop()
         visited += 1
-        for s in range(8):
+        for s in range(width):
             m = int(dec["meta"][node, s])
             if m == 0:
                 continue

@@ -6,7 +6,7 @@ same closest hits), and like the oracle."""
 import numpy as np
 import pytest
 
-from helpers import S, camera_of, hits_equal, random_rays
+from helpers import S, bvh_kind, camera_of, hits_equal, random_rays
 
 pytestmark = pytest.mark.gpu
 
@@ -41,9 +41,9 @@ def _render(solrt, ctx, sc, cam, w, h, p):
 
 
 @pytest.mark.parametrize("mode", ["rebuild", "refit"])
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh8"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh4", "bvh8"])
 def test_regenerate_matches_fresh_scene(solrt, oracle, ctx, bvh, mode):
-    kind = solrt.BVH2 if bvh == "bvh2" else solrt.BVH8_Q8
+    kind = bvh_kind(solrt, bvh)
     regen = solrt.REGEN_REBUILD if mode == "rebuild" else solrt.REGEN_REFIT
     base = S.cornell()
     w, h = 32, 32

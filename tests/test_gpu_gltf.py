@@ -5,7 +5,7 @@ Cornell box renders exactly like the directly built scene."""
 import numpy as np
 import pytest
 
-from helpers import S, camera_of
+from helpers import S, bvh_kind, camera_of
 
 pytestmark = pytest.mark.gpu
 
@@ -25,12 +25,12 @@ def _transformed_glb(solrt, path):
     return solrt.load_scene(str(path))
 
 
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh8"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh4", "bvh8"])
 def test_gltf_render_matches_oracle(solrt, oracle, ctx, tmp_path, bvh):
     g = _transformed_glb(solrt, tmp_path / "cornell.glb")
     w, h = 40, 32
     cam = g.camera(w / h)
-    kind = solrt.BVH2 if bvh == "bvh2" else solrt.BVH8_Q8
+    kind = bvh_kind(solrt, bvh)
     sc = solrt.SceneDescription(ctx, g.data, bvh=kind)
     img = solrt.Image(ctx, w, h)
     p = solrt.render_params(w, h, spp=3, max_bounces=6, material_mode=solrt.MATERIAL_REF,

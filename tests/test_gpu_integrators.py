@@ -5,7 +5,7 @@ texture). Both must equal the oracle bit for bit, on both BVH kinds."""
 import numpy as np
 import pytest
 
-from helpers import S, camera_of, transformed_cornell
+from helpers import S, bvh_kind, camera_of, transformed_cornell
 
 pytestmark = pytest.mark.gpu
 
@@ -15,12 +15,12 @@ def blue_noise(h=64, w=48, seed=17):
     return np.random.default_rng(seed).integers(0, 256, (h, w, 4), dtype=np.uint8)
 
 
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh8"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh4", "bvh8"])
 @pytest.mark.parametrize("scene", ["cornell", "transformed", "soup"])
 def test_debug_matches_oracle(solrt, oracle, ctx, bvh, scene):
     data = {"cornell": S.cornell, "transformed": transformed_cornell, "soup": lambda: S.soup(20000, seed=3)}[scene]()
     w, h = 48, 40
-    kind = solrt.BVH2 if bvh == "bvh2" else solrt.BVH8_Q8
+    kind = bvh_kind(solrt, bvh)
     cam = camera_of(data, w / h)
     sc = solrt.SceneDescription(ctx, data, bvh=kind)
     img = solrt.Image(ctx, w, h)
@@ -37,11 +37,11 @@ def test_debug_matches_oracle(solrt, oracle, ctx, bvh, scene):
     assert hit.any()
 
 
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh8"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh4", "bvh8"])
 def test_ao_matches_oracle(solrt, oracle, ctx, bvh):
     data = S.cornell()
     w, h = 40, 32
-    kind = solrt.BVH2 if bvh == "bvh2" else solrt.BVH8_Q8
+    kind = bvh_kind(solrt, bvh)
     cam = camera_of(data, w / h)
     noise = blue_noise()
     ctx.set_blue_noise(noise)

@@ -6,7 +6,7 @@ the host); the count of traced segments must be equal."""
 import numpy as np
 import pytest
 
-from helpers import S, camera_of, transformed_cornell
+from helpers import S, bvh_kind, camera_of, transformed_cornell
 
 pytestmark = pytest.mark.gpu
 
@@ -78,12 +78,12 @@ def _render_both(solrt, oracle, ctx, data, w, h, kw, frames=2, bvh=None):
     return ga, g8, acc, rgba_o, stats, seg_o
 
 
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh8"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh4", "bvh8"])
 @pytest.mark.parametrize("name", ["cornell_lambert", "cornell_ref_stream", "cornell_ref_sky", "transformed",
                                   "soup_gradient", "tunnel_kahan"])
 def test_render_bit_exact(solrt, oracle, ctx, name, bvh):
     data, w, h, kw = _case(name)
-    kind = solrt.BVH2 if bvh == "bvh2" else solrt.BVH8_Q8
+    kind = bvh_kind(solrt, bvh)
     ga, g8, oa, o8, stats, seg_o = _render_both(solrt, oracle, ctx, data, w, h, kw, bvh=kind)
     diff = np.nonzero(np.any(ga.view(np.uint32) != oa.view(np.uint32), axis=-1))
     assert len(diff[0]) == 0, (len(diff[0]), list(zip(diff[0][:5], diff[1][:5])), ga[diff][:3], oa[diff][:3])
@@ -93,13 +93,13 @@ def test_render_bit_exact(solrt, oracle, ctx, name, bvh):
     assert np.isfinite(ga).all() and ga[..., :3].mean() > 0
 
 
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh8"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh4", "bvh8"])
 @pytest.mark.parametrize("name", ["cornell_lambert", "cornell_ref_stream", "soup_gradient", "tunnel_kahan"])
 def test_megakernel_equals_wavefront(solrt, oracle, ctx, name, bvh):
     """The per-pixel megakernel (the reference's loop structure) renders the
     same image as the wavefront and as the oracle."""
     data, w, h, kw = _case(name)
-    kind = solrt.BVH2 if bvh == "bvh2" else solrt.BVH8_Q8
+    kind = bvh_kind(solrt, bvh)
     ga, g8, oa, o8, stats, seg_o = _render_both(solrt, oracle, ctx, data, w, h, dict(kw, kernel=solrt.api.KERNEL_MEGA),
                                                 bvh=kind)
     assert np.array_equal(ga.view(np.uint32), oa.view(np.uint32))

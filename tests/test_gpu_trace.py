@@ -4,8 +4,8 @@ bit (watertight test with the same arithmetic, deterministic tie-break)."""
 import numpy as np
 import pytest
 
-from helpers import (S, axis_rays, edge_rays, empty_scene, hit_mismatch, hits_equal, random_rays, single_triangle,
-                     transformed_cornell)
+from helpers import (S, axis_rays, bvh_kind, edge_rays, empty_scene, hit_mismatch, hits_equal, random_rays,
+                     single_triangle, transformed_cornell)
 
 pytestmark = pytest.mark.gpu
 
@@ -18,11 +18,11 @@ def _both(solrt, oracle, ctx, data, rays, bvh):
     return g, ref
 
 
-BVHS = ["bvh2", "bvh8"]
+BVHS = ["bvh2", "bvh4", "bvh8"]
 
 
 def _kind(solrt, name):
-    return solrt.BVH2 if name == "bvh2" else solrt.BVH8_Q8
+    return bvh_kind(solrt, name)
 
 
 @pytest.mark.parametrize("bvh", BVHS)
