@@ -719,7 +719,7 @@ solrt_status batch_autotune(Batch& b, solrt_tune_result* out) {
         const uint32_t blocks[3] = {64u, 128u, 256u};
         for (uint32_t bl : blocks) {
             for (uint32_t sm : smems) {
-                if (b.kind != SOLRT_BVH2 && sm != initial.smem) continue;  // no shared stack
+                if (b.kind == SOLRT_BVH8_Q8 && sm != initial.smem) continue;  // no shared stack
                 TuneConfig c = initial;
                 c.block = bl;
                 c.smem = sm;
