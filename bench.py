@@ -41,6 +41,11 @@ METRIC = "Mrays/s at RMSE≤1e-3 vs FP64 oracle, batched vs plain on 1 GB300; p9
 UNIT = "Mrays/s"
 
 NODE_BYTES = {0: 64, 1: 80, 2: 64}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per traced segment
+# of the BVH2 extend kernel on the default soup workload, from one ncu
+# capture of the last 15 k_extend launches of a timed frame (3 of its 4
+# passes, 15.24 GB for ~242.7M segments; one-pass metrics, full size).
+EXTEND_DRAM_BYTES_PER_SEGMENT_SOUP = 62.8
 
 
 def workload(name):
@@ -624,8 +629,15 @@ def main():
     b_seg = 32 + 16 + NODE_BYTES[info.kind] * nodes_per_seg + 48 * tris_per_seg
     ext_s = st.extend_ms / 1000.0
     achieved = (st.segments * b_seg) / ext_s / 1e9 if ext_s > 0 else 0.0
+    traffic = None
+    if args.workload == "soup" and info.kind == solrt.BVH2 and not (args.width or args.height or args.spp):
+        seg_per_launch = st.segments / max(st.extend_launches, 1)
+        traffic = round(EXTEND_DRAM_BYTES_PER_SEGMENT_SOUP * seg_per_launch)
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_kind + " (MEASURED_PEAKS hbm_gbs)",
+                "frac": round(achieved / peak, 4), "traffic": traffic,
+                "traffic_note": "DRAM bytes per launch from an ncu capture of this workload (62.8 B per segment); "
+                                "the algorithmic bytes are mostly served by L1 / L2" if traffic else None,
+                "peak_source": peak_kind + " (MEASURED_PEAKS hbm_gbs)",
                 "kernel": "k_extend (BVH traversal)", "bytes_per_segment": round(b_seg, 1),
                 "nodes_per_segment": round(nodes_per_seg, 2), "tris_per_segment": round(tris_per_seg, 2),
                 "extend_ms_per_launch": round(st.extend_ms / max(st.extend_launches, 1), 4),

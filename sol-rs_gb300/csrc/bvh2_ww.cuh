@@ -6,9 +6,11 @@
 //           (one atomic per warp), once at least SOLRT_BVH2_REFILL lanes are
 //           free;
 //   nodes   lanes visit inner nodes until every lane has parked a leaf or has
-//           no inner node left; a lane that already parked a leaf keeps
-//           descending until it reaches a second one ("while-while" with
-//           speculative traversal, after Aila & Laine, HPG 2009);
+//           no inner node left, or until fewer than SOLRT_WW_NODE_MIN lanes
+//           still have inner nodes while others hold leaves; a lane that
+//           already parked a leaf keeps descending until it reaches a second
+//           one ("while-while" with speculative traversal, after Aila &
+//           Laine, HPG 2009);
 //   leaves  lanes test their parked leaves together.
 // Each lane carries its own scene (IO::load), so one launch can serve rays of
 // many scenes. The closest hit does not depend on visiting order, so results
