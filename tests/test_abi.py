@@ -83,3 +83,38 @@ def test_context_without_gpu_fails_cleanly(solrt):
     with pytest.raises(solrt.SolrtError) as e:
         solrt.Context(0)
     assert e.value.status == 3   # SOLRT_ERR_DEVICE
+
+
+def test_ctypes_mirror_matches_header(solrt, tmp_path):
+    """Every ctypes struct of the Python binding has the size and field
+    offsets of its C struct in include/solrt.h (a C program compiled from
+    the header prints them)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    api = solrt.api
+    pairs = [("solrt_vertex", api.Vertex), ("solrt_material", api.Material), ("solrt_instance", api.Instance),
+             ("solrt_section", api.Section), ("solrt_scene_desc", api.SceneDesc), ("solrt_bvh_desc", api.BvhDesc),
+             ("solrt_bvh_info", api.BvhInfo), ("solrt_camera", api.Camera), ("solrt_render_params", api.RenderParams),
+             ("solrt_context_desc", api.ContextDesc), ("solrt_stats", api.Stats), ("solrt_job", api.Job),
+             ("solrt_server_desc", api.ServerDesc), ("solrt_job_result", api.JobResult),
+             ("solrt_server_stats", api.ServerStats), ("solrt_tune_config", api.TuneConfig),
+             ("solrt_tune_result", api.TuneResult)]
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "solrt.h"', "int main(void) {"]
+    for cname, cls in pairs:
+        lines.append('printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
+        for f in cls._fields_:
+            lines.append('printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (cname, f[0], cname, f[0]))
+    lines.append("return 0; }")
+    src = tmp_path / "sizes.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "sizes"
+    subprocess.run([cc, "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(l.split() for l in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                  text=True).stdout.splitlines())
+    for cname, cls in pairs:
+        assert int(got[cname]) == ctypes.sizeof(cls), cname
+        for f in cls._fields_:
+            assert int(got["%s.%s" % (cname, f[0])]) == getattr(cls, f[0]).offset, (cname, f[0])
