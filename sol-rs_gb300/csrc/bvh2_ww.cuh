@@ -31,6 +31,11 @@ constexpr int kBvh2Sentinel = 0x7fffffff;
 #ifndef SOLRT_WW_NODE_MIN
 #define SOLRT_WW_NODE_MIN 12
 #endif
+// 1: a lane that has parked a leaf keeps visiting inner nodes until it
+// reaches a second leaf; 0: it waits for the leaf phase.
+#ifndef SOLRT_WW_SPECULATE
+#define SOLRT_WW_SPECULATE 1
+#endif
 // Default traversal stack entries kept in shared memory (slot-major, one
 // column per thread, so lanes at different depths hit different banks);
 // deeper entries go to a local-memory array. The launch may pick 16 or 32
@@ -133,11 +138,11 @@ SOLRT_D void extend_bvh2_ww(const IO& io, uint32_t n, unsigned int* work, TraceC
 #if SOLRT_WW_NODE_MIN > 0
             // few lanes left with inner nodes while others hold leaves: test
             // the leaves first (the leaf phase then has work, so this ends)
-            if (__popc(__ballot_sync(0xffffffffu, inner)) < SOLRT_WW_NODE_MIN &&
+            if (__popc(__ballot_sync(0xffffffffu, inner && (SOLRT_WW_SPECULATE || leaf >= 0))) < SOLRT_WW_NODE_MIN &&
                 __any_sync(0xffffffffu, leaf < 0))
                 break;
 #endif
-            if (inner) {
+            if (inner && (SOLRT_WW_SPECULATE || leaf >= 0)) {
                 if (--budget == 0u || (uint32_t)node >= ts.node_count) {
                     ef |= SOLRT_EFLAG_INDEX;
                     node = kBvh2Sentinel;
