@@ -47,7 +47,8 @@ typedef enum solrt_status {
     SOLRT_ERR_CAPACITY = 5,      /* a fixed-capacity queue or stack overflowed */
     SOLRT_ERR_NOT_READY = 6,     /* job still running (server poll) */
     SOLRT_ERR_NOT_FOUND = 7,     /* unknown job / object */
-    SOLRT_ERR_BUDGET = 8         /* request larger than the memory budget */
+    SOLRT_ERR_BUDGET = 8,        /* request larger than the memory budget */
+    SOLRT_ERR_CANCELLED = 9      /* served job cancelled (solrt_server_cancel) */
 } solrt_status;
 
 /* ------------------------------------------------------------------------ */
@@ -470,7 +471,10 @@ typedef struct solrt_server_desc {
     uint64_t memory_budget;   /* bytes of job images + scenes in use; 0 = 150 GB */
     uint32_t tick_paths;      /* paths per tick; 0 = min(8M, the context's path capacity) */
     uint32_t policy;          /* solrt_serve_policy */
-    uint32_t reserved[4];
+    /* host-side fault injection for tests: the next this-many admissions
+     * fail as if their image allocation had failed (SOLRT_ERR_OOM) */
+    uint32_t inject_alloc_failures;
+    uint32_t reserved[3];
 } solrt_server_desc;
 
 typedef struct solrt_job_result {
@@ -509,6 +513,12 @@ solrt_status solrt_server_poll(solrt_server* srv, uint64_t ticket, solrt_job_res
 solrt_status solrt_server_wait(solrt_server* srv, uint64_t ticket, uint32_t timeout_ms, solrt_job_result* out);
 /* Frees a completed job's image. */
 solrt_status solrt_server_release(solrt_server* srv, uint64_t ticket);
+/* Cancels a queued or running job: a queued job leaves the queue at once, a
+ * running one after the tick in flight (a job whose last samples are in that
+ * tick completes normally); its memory is freed and poll / wait then return
+ * SOLRT_ERR_CANCELLED until it is released. SOLRT_ERR_INVALID for a job that
+ * has already finished. */
+solrt_status solrt_server_cancel(solrt_server* srv, uint64_t ticket);
 solrt_status solrt_server_get_stats(solrt_server* srv, solrt_server_stats* out);
 /* Stops the serving thread (unfinished jobs are dropped) and frees images. */
 solrt_status solrt_server_destroy(solrt_server* srv);

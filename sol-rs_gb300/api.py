@@ -19,7 +19,8 @@ LIB_PATH = os.path.join(PKG, "_build", "libsolrt.so")
 NO_HIT = 0xFFFFFFFF
 
 # enums (solrt.h)
-OK, ERR_INVALID, ERR_OOM, ERR_DEVICE, ERR_TIMEOUT, ERR_CAPACITY, ERR_NOT_READY, ERR_NOT_FOUND, ERR_BUDGET = range(9)
+(OK, ERR_INVALID, ERR_OOM, ERR_DEVICE, ERR_TIMEOUT, ERR_CAPACITY, ERR_NOT_READY, ERR_NOT_FOUND, ERR_BUDGET,
+ ERR_CANCELLED) = range(10)
 BVH2, BVH8_Q8, BVH4_Q8 = 0, 1, 2
 MISS_BLACK, MISS_REF_SKY, MISS_GRADIENT = 0, 1, 2
 MATERIAL_REF, MATERIAL_LAMBERT = 0, 1
@@ -103,7 +104,7 @@ SERVE_FAIR, SERVE_SHORTEST_FIRST = 0, 1
 
 class ServerDesc(ctypes.Structure):
     _fields_ = [("memory_budget", ctypes.c_uint64), ("tick_paths", ctypes.c_uint32), ("policy", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32 * 4)]
+                ("inject_alloc_failures", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 3)]
 
 
 class JobResult(ctypes.Structure):
@@ -190,6 +191,7 @@ _PROTOS = {
     "solrt_server_poll": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.POINTER(JobResult)]),
     "solrt_server_wait": (ctypes.c_int, [_P, ctypes.c_uint64, _U32, ctypes.POINTER(JobResult)]),
     "solrt_server_release": (ctypes.c_int, [_P, ctypes.c_uint64]),
+    "solrt_server_cancel": (ctypes.c_int, [_P, ctypes.c_uint64]),
     "solrt_server_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(ServerStats)]),
     "solrt_server_destroy": (ctypes.c_int, [_P]),
     "solrt_trace_rays": (ctypes.c_int, [_P, _P, _P, _U32, _P]),
@@ -532,13 +534,13 @@ class Server:
     """Continuous-batching render server (solrt_server): a serving thread
     admits jobs by memory budget and advances all active jobs each tick."""
 
-    def __init__(self, context, memory_budget=0, tick_paths=0, policy=0):
-        """policy: SERVE_FAIR (0) or SERVE_SHORTEST_FIRST (1)."""
+    def __init__(self, context, memory_budget=0, tick_paths=0, policy=0, inject_alloc_failures=0):
+        """policy: SERVE_FAIR (0) or SERVE_SHORTEST_FIRST (1);
+        inject_alloc_failures: host-side fault injection for tests."""
         self.context = context
         h = ctypes.c_void_p()
-        check(lib().solrt_server_create(context.handle,
-                                        ctypes.byref(ServerDesc(memory_budget, tick_paths, policy)),
-                                        ctypes.byref(h)))
+        desc = ServerDesc(memory_budget, tick_paths, policy, inject_alloc_failures)
+        check(lib().solrt_server_create(context.handle, ctypes.byref(desc), ctypes.byref(h)))
         self.handle = h
         self._scenes = {}
 
@@ -576,6 +578,10 @@ class Server:
     def release(self, ticket):
         self._scenes.pop(ticket, None)
         return lib().solrt_server_release(self.handle, ticket)
+
+    def cancel(self, ticket):
+        """solrt_server_cancel: returns the status code."""
+        return lib().solrt_server_cancel(self.handle, ticket)
 
     def stats(self):
         s = ServerStats()

@@ -167,6 +167,7 @@ const char* solrt_status_string(solrt_status s) {
         case SOLRT_ERR_NOT_READY: return "not ready";
         case SOLRT_ERR_NOT_FOUND: return "not found";
         case SOLRT_ERR_BUDGET: return "over memory budget";
+        case SOLRT_ERR_CANCELLED: return "cancelled";
     }
     return "unknown status";
 }

@@ -52,6 +52,7 @@ struct ServerJob {
     uint64_t t_submit = 0, t_admit = 0, t_done = 0, last_use = 0;
     uint64_t image_bytes = 0;
     bool counted = false;  // image and scene counted against the budget
+    bool cancel = false;   // cancelled while running: leaves after the tick in flight
 };
 
 uint64_t image_bytes_of(const solrt_render_params& p) {
@@ -66,6 +67,7 @@ struct solrt_server {
     uint64_t budget = 0;
     uint32_t tick_paths = 0;
     uint32_t policy = SOLRT_SERVE_FAIR;
+    uint32_t inject_alloc_failures = 0;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::thread th;
@@ -131,7 +133,14 @@ void admit(solrt_server* srv) {
             return;  // wait for active jobs to finish
         }
         solrt_image* img = nullptr;
-        const solrt_status s = solrt_image_create(srv->ctx, j.p.width, j.p.height, j.p.accum_mode, &img);
+        solrt_status s;
+        if (srv->inject_alloc_failures) {  // host-side fault injection (tests)
+            --srv->inject_alloc_failures;
+            solrt::set_error("injected allocation failure");
+            s = SOLRT_ERR_OOM;
+        } else {
+            s = solrt_image_create(srv->ctx, j.p.width, j.p.height, j.p.accum_mode, &img);
+        }
         srv->queue.pop_front();
         if (s != SOLRT_OK) {
             j.state = kFailed;
@@ -169,6 +178,21 @@ void serve_loop(solrt_server* srv) {
             srv->cv_work.wait_for(lock, std::chrono::milliseconds(20),
                                   [&] { return srv->stop || !srv->queue.empty() || !srv->active.empty(); });
             if (srv->stop) break;
+            // running jobs cancelled since the last tick leave now (no tick
+            // in flight uses their images)
+            for (uint64_t t : srv->active) {
+                ServerJob& j = srv->jobs[t];
+                if (j.cancel) {
+                    drop_job_memory(srv, j);
+                    j.state = kFailed;
+                    j.status = SOLRT_ERR_CANCELLED;
+                    j.t_done = now_ns();
+                }
+            }
+            srv->active.erase(std::remove_if(srv->active.begin(), srv->active.end(),
+                                             [&](uint64_t t) { return srv->jobs[t].state != kActive; }),
+                              srv->active.end());
+            srv->cv_done.notify_all();
             admit(srv);
             if (srv->active.empty()) continue;
             // plan the tick: a fair share of tick_paths per active job
@@ -289,6 +313,7 @@ solrt_status solrt_server_create(solrt_context* ctx, const solrt_server_desc* de
     srv->tick_paths = desc && desc->tick_paths ? std::min(desc->tick_paths, ctx->capacity)
                                                : std::min(8u << 20, ctx->capacity);
     srv->policy = desc ? desc->policy : (uint32_t)SOLRT_SERVE_FAIR;
+    srv->inject_alloc_failures = desc ? desc->inject_alloc_failures : 0u;
     try {
         srv->th = std::thread(serve_loop, srv);
     } catch (...) {
@@ -407,6 +432,35 @@ solrt_status solrt_server_release(solrt_server* srv, uint64_t ticket) {
     drop_job_memory(srv, j);
     srv->jobs.erase(it);
     return SOLRT_OK;
+}
+
+solrt_status solrt_server_cancel(solrt_server* srv, uint64_t ticket) {
+    if (!srv) {
+        set_error("null server");
+        return SOLRT_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lock(srv->mu);
+    auto it = srv->jobs.find(ticket);
+    if (it == srv->jobs.end()) {
+        set_error("unknown, released or evicted ticket");
+        return SOLRT_ERR_NOT_FOUND;
+    }
+    ServerJob& j = it->second;
+    if (j.state == kQueued) {
+        srv->queue.erase(std::find(srv->queue.begin(), srv->queue.end(), ticket));
+        j.state = kFailed;
+        j.status = SOLRT_ERR_CANCELLED;
+        j.t_done = now_ns();
+        srv->cv_done.notify_all();
+        return SOLRT_OK;
+    }
+    if (j.state == kActive) {
+        j.cancel = true;
+        srv->cv_work.notify_all();
+        return SOLRT_OK;
+    }
+    set_error("job already finished");
+    return SOLRT_ERR_INVALID;
 }
 
 solrt_status solrt_server_get_stats(solrt_server* srv, solrt_server_stats* out) {

@@ -129,3 +129,79 @@ def test_shortest_first_finishes_small_jobs_first(solrt):
     srv.close()
     with pytest.raises(solrt.SolrtError):
         solrt.Server(ctx, policy=7)
+
+
+def _wait_status(srv, ticket, timeout_s=60.0):
+    """Polls until the job leaves the queued / running states; returns the status."""
+    t0 = time.time()
+    while time.time() - t0 < timeout_s:
+        s, _ = srv.poll(ticket)
+        if s != solrt_mod().ERR_NOT_READY:
+            return s
+        time.sleep(0.002)
+    return None
+
+
+def solrt_mod():
+    import importlib
+    return importlib.import_module("sol-rs_gb300").api
+
+
+def test_cancel_queued_and_running(solrt):
+    """A cancelled running job leaves after its tick and a cancelled queued
+    job at once; both report SOLRT_ERR_CANCELLED; the other jobs finish with
+    the images they have alone."""
+    ctx = solrt.Context(0)
+    scenes = _scenes(solrt, ctx)
+    d = S.cornell()
+    # tiny ticks: the long job is still running when it is cancelled
+    srv = solrt.Server(ctx, tick_paths=2000, memory_budget=16 << 20)
+    long_p = solrt.render_params(512, 512, spp=256, max_bounces=4, material_mode=solrt.MATERIAL_LAMBERT,
+                                 rng_mode=solrt.RNG_PER_SAMPLE, seed=3)
+    keep = [solrt.render_params(24, 24, spp=4, max_bounces=3, material_mode=solrt.MATERIAL_LAMBERT,
+                                rng_mode=solrt.RNG_PER_SAMPLE, seed=10 + i, job_id=i) for i in range(3)]
+    cam = camera_of(d, 1.0)
+    t_long = srv.submit(scenes[0], cam, long_p)
+    t_keep = [srv.submit(scenes[0], cam, p) for p in keep]
+    t_queued = srv.submit(scenes[0], cam, long_p)      # does not fit the budget next to the first
+    t0 = time.time()
+    while srv.poll(t_long)[1].spp_done == 0 and time.time() - t0 < 30:   # running: one sample per tick
+        time.sleep(0.001)
+    assert srv.poll(t_long)[0] == solrt.api.ERR_NOT_READY
+    assert srv.cancel(t_queued) == 0
+    assert srv.poll(t_queued)[0] == solrt.api.ERR_CANCELLED
+    assert srv.cancel(t_long) == 0
+    st = _wait_status(srv, t_long)
+    assert st == solrt.api.ERR_CANCELLED
+    results = [srv.read(t, srv.wait(t, 60000)) for t in t_keep]
+    done = srv.submit(scenes[0], cam, keep[0])
+    srv.wait(done, 60000)
+    assert srv.cancel(done) == solrt.api.ERR_INVALID      # already finished
+    assert srv.release(t_long) == 0
+    srv.close()
+    r = solrt.Renderer(ctx)
+    for p, (a32, _) in zip(keep, results):
+        img = solrt.Image(ctx, p.width, p.height)
+        r.cmd_trace_rays(scenes[0], cam, p, img)
+        assert np.array_equal(img.read()[0].view(np.uint32), a32.view(np.uint32))
+        img.close()
+
+
+def test_injected_allocation_failure(solrt):
+    """Host-side fault injection: the first admission fails as an image
+    allocation failure would; the job reports SOLRT_ERR_OOM and the server
+    goes on serving the others."""
+    ctx = solrt.Context(0)
+    scenes = _scenes(solrt, ctx)
+    d = S.cornell()
+    srv = solrt.Server(ctx, inject_alloc_failures=1)
+    cam = camera_of(d, 1.0)
+    ps = [solrt.render_params(16, 16, spp=2, max_bounces=3, material_mode=solrt.MATERIAL_LAMBERT,
+                              rng_mode=solrt.RNG_PER_SAMPLE, seed=20 + i, job_id=i) for i in range(3)]
+    tickets = [srv.submit(scenes[0], cam, p) for p in ps]
+    assert _wait_status(srv, tickets[0]) == solrt.api.ERR_OOM
+    for t in tickets[1:]:
+        r = srv.wait(t, 60000)
+        assert r.status == 0
+    assert srv.stats().completed == 2
+    srv.close()
