@@ -641,6 +641,10 @@ def main():
                 "kernel": "k_extend (BVH traversal)", "bytes_per_segment": round(b_seg, 1),
                 "nodes_per_segment": round(nodes_per_seg, 2), "tris_per_segment": round(tris_per_seg, 2),
                 "extend_ms_per_launch": round(st.extend_ms / max(st.extend_launches, 1), 4),
+                "stage_ms_per_step": {"generate": round(st.generate_ms / args.steps, 3),
+                                      "extend": round(st.extend_ms / args.steps, 3),
+                                      "shade": round(st.shade_ms / args.steps, 3),
+                                      "accumulate_finalize": round(st.accumulate_ms / args.steps, 3)},
                 "extend_share_of_step": round(st.extend_ms / ms, 4) if ms > 0 else None}
 
     # RMSE of the device image (one fresh frame) against the FP64 oracle on the

@@ -265,6 +265,8 @@ typedef struct solrt_stats {
     double shade_ms;          /* summed device time of shade launches (enable_timing) */
     uint64_t extend_launches; /* launches timed into extend_ms */
     uint64_t shade_launches;  /* launches timed into shade_ms */
+    double generate_ms;       /* camera-ray generation (enable_timing) */
+    double accumulate_ms;     /* per-pixel sums, frame begin / finalize (enable_timing) */
 } solrt_stats;
 
 typedef enum solrt_error_bits {

@@ -134,7 +134,7 @@ class Stats(ctypes.Structure):
                 ("tri_tests", ctypes.c_uint64), ("fp64_fallbacks", ctypes.c_uint64), ("launches", ctypes.c_uint64),
                 ("error_flags", ctypes.c_uint32), ("reserved", ctypes.c_uint32), ("render_ms", ctypes.c_double),
                 ("extend_ms", ctypes.c_double), ("shade_ms", ctypes.c_double), ("extend_launches", ctypes.c_uint64),
-                ("shade_launches", ctypes.c_uint64)]
+                ("shade_launches", ctypes.c_uint64), ("generate_ms", ctypes.c_double), ("accumulate_ms", ctypes.c_double)]
 
 
 class ContextDesc(ctypes.Structure):

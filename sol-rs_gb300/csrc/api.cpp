@@ -285,6 +285,8 @@ solrt_status solrt_get_stats(solrt_context* ctx, solrt_stats* out) {
     out->shade_ms = ctx->shade_ms;
     out->extend_launches = ctx->extend_launches;
     out->shade_launches = ctx->shade_launches;
+    out->generate_ms = ctx->generate_ms;
+    out->accumulate_ms = ctx->accumulate_ms;
     out->segments = d.segments;
     out->paths = d.paths;
     out->node_visits = d.node_visits;
@@ -304,7 +306,7 @@ solrt_status solrt_reset_stats(solrt_context* ctx) {
     SOLRT_CUDA(cudaStreamSynchronize(ctx->stream));
     ctx->timing_collect();
     ctx->launches = 0;
-    ctx->extend_ms = ctx->shade_ms = 0.0;
+    ctx->extend_ms = ctx->shade_ms = ctx->generate_ms = ctx->accumulate_ms = 0.0;
     ctx->extend_launches = ctx->shade_launches = 0;
     return SOLRT_OK;
 }

@@ -192,11 +192,11 @@ struct Context {
     bool timing = false;
     struct TimedLaunch {
         cudaEvent_t start, end;
-        int stage;  // 0 extend, 1 shade
+        int stage;  // 0 extend, 1 shade, 2 generate, 3 begin / accumulate / finalize
     };
     std::vector<TimedLaunch> timed;
     size_t timed_used = 0;
-    double extend_ms = 0.0, shade_ms = 0.0;
+    double extend_ms = 0.0, shade_ms = 0.0, generate_ms = 0.0, accumulate_ms = 0.0;
     uint64_t extend_launches = 0, shade_launches = 0;
     // Records the start event of a timed launch of `stage`; returns its slot.
     int timing_begin(int stage) {
@@ -219,7 +219,9 @@ struct Context {
             float ms = 0.0f;
             if (cudaEventElapsedTime(&ms, timed[i].start, timed[i].end) == cudaSuccess) {
                 if (timed[i].stage == 0) { extend_ms += ms; ++extend_launches; }
-                else { shade_ms += ms; ++shade_launches; }
+                else if (timed[i].stage == 1) { shade_ms += ms; ++shade_launches; }
+                else if (timed[i].stage == 2) generate_ms += ms;
+                else accumulate_ms += ms;
             }
         }
         timed_used = 0;

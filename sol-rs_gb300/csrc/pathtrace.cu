@@ -501,8 +501,10 @@ solrt_status issue_pass(Context& ctx, uint32_t kind, const DevJob* dj, const Dev
     const size_t ctl_bytes = sizeof(unsigned int) * (pp.bounces + 1);
     SOLRT_CUDA(cudaMemsetAsync(ctl->count, 0, ctl_bytes, st));
     SOLRT_CUDA(cudaMemsetAsync(ctl->work, 0, ctl_bytes, st));
+    const int tg = record_timing ? ctx.timing_begin(2) : -1;
     k_generate<<<cdiv(pp.paths, 256), 256, 0, st>>>(dj, items, pp.item_count, pp.paths, ctx.queue(0), ctl->count,
                                                     stats);
+    ctx.timing_end(tg);
     ++ctx.launches;
     const int shade_grid = ctx.sm_count * 8;
     for (uint32_t bnc = 0; bnc < pp.bounces; ++bnc) {
@@ -516,7 +518,9 @@ solrt_status issue_pass(Context& ctx, uint32_t kind, const DevJob* dj, const Dev
         ctx.timing_end(ts);
         ++ctx.launches;
     }
+    const int ta = record_timing ? ctx.timing_begin(3) : -1;
     k_accumulate<<<cdiv(pp.pixels, 256), 256, 0, st>>>(dj, items, pp.item_count, pp.pixels, ctx.rad.as<float4>());
+    ctx.timing_end(ta);
     ++ctx.launches;
     return SOLRT_OK;
 }
@@ -530,10 +534,14 @@ solrt_status batch_issue(Batch& b, bool record_timing) {
     const uint32_t* jp = b.d_job_pix.as<uint32_t>();
     const uint32_t njobs = (uint32_t)b.jobs.size();
     const uint32_t total_pix = b.job_pix_base[njobs];
+    const int tb = record_timing ? ctx.timing_begin(3) : -1;
     k_begin<<<cdiv(total_pix, 256), 256, 0, st>>>(dj, jp, njobs, total_pix);
+    ctx.timing_end(tb);
     ++ctx.launches;
     for (const PassPlan& pp : b.passes) SOLRT_TRY(issue_pass(ctx, b.kind, dj, di + pp.item_begin, pp, record_timing));
+    const int tf = record_timing ? ctx.timing_begin(3) : -1;
     k_finalize<<<cdiv(total_pix, 256), 256, 0, st>>>(dj, jp, njobs, total_pix);
+    ctx.timing_end(tf);
     ++ctx.launches;
     SOLRT_CUDA(cudaGetLastError());
     return SOLRT_OK;
