@@ -382,6 +382,16 @@ solrt_status solrt_image_clear(solrt_image* img);
 solrt_status solrt_image_read(solrt_image* img, float* rgba32f, uint8_t* rgba8);
 /* Device pointers of the images (float4 accumulation, uchar4 render). */
 solrt_status solrt_image_device_ptrs(solrt_image* img, void** accum, void** rgba8);
+/* Checkpoint / resume of the accumulation state (no counterpart in the
+ * reference, whose images live only in VRAM): the RGBA32F accumulation
+ * (W*H*4 floats) and, for KAHAN images, the compensated sums and
+ * compensations (W*H*4 floats each; NULL for REF_MIX images). Restoring a
+ * snapshot into an image of the same size and mode and rendering the next
+ * frame index continues the accumulation bit for bit (the RGBA8 image is
+ * written by the next render). Both synchronise. */
+solrt_status solrt_image_snapshot(solrt_image* img, float* accum, float* kahan_sum, float* kahan_comp);
+solrt_status solrt_image_restore(solrt_image* img, const float* accum, const float* kahan_sum,
+                                 const float* kahan_comp);
 
 /* One launch of the path tracer: spp samples for every pixel, accumulated
  * into `img`. Asynchronous on the context stream. */

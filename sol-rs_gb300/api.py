@@ -175,6 +175,8 @@ _PROTOS = {
     "solrt_image_clear": (ctypes.c_int, [_P]),
     "solrt_image_read": (ctypes.c_int, [_P, _P, _P]),
     "solrt_image_device_ptrs": (ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.POINTER(_P)]),
+    "solrt_image_snapshot": (ctypes.c_int, [_P, _P, _P, _P]),
+    "solrt_image_restore": (ctypes.c_int, [_P, _P, _P, _P]),
     "solrt_render": (ctypes.c_int, [_P, _P, ctypes.POINTER(Camera), ctypes.POINTER(RenderParams), _P]),
     "solrt_batch_create": (ctypes.c_int, [_P, ctypes.POINTER(Job), _U32, _U32, ctypes.POINTER(_P)]),
     "solrt_batch_update": (ctypes.c_int, [_P, ctypes.POINTER(Job)]),
@@ -432,6 +434,21 @@ class Image:
 
     def read_into(self, rgba32f, rgba8=None):
         check(lib().solrt_image_read(self.handle, _ptr(rgba32f), _ptr(rgba8)))
+
+    def snapshot(self):
+        """Accumulation state for checkpoint / resume: (accum, kahan_sum,
+        kahan_comp) as (H, W, 4) float32 arrays (the last two None for
+        REF_MIX images)."""
+        shape = (self.height, self.width, 4)
+        acc = np.zeros(shape, np.float32)
+        ks = np.zeros(shape, np.float32) if self.accum_mode == ACCUM_KAHAN else None
+        kc = np.zeros(shape, np.float32) if self.accum_mode == ACCUM_KAHAN else None
+        check(lib().solrt_image_snapshot(self.handle, _ptr(acc), _ptr(ks), _ptr(kc)))
+        return acc, ks, kc
+
+    def restore(self, snapshot):
+        acc, ks, kc = (None if a is None else np.ascontiguousarray(a, np.float32) for a in snapshot)
+        check(lib().solrt_image_restore(self.handle, _ptr(acc), _ptr(ks), _ptr(kc)))
 
     def device_ptrs(self):
         a, b = ctypes.c_void_p(), ctypes.c_void_p()

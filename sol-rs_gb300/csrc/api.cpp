@@ -623,6 +623,37 @@ solrt_status solrt_image_read(solrt_image* img, float* rgba32f, uint8_t* rgba8) 
     return check_device_flags(*img->ctx);
 }
 
+solrt_status solrt_image_snapshot(solrt_image* img, float* accum, float* kahan_sum, float* kahan_comp) {
+    CHECK_ARG(img && accum, "null argument");
+    const bool kahan = img->accum_mode == SOLRT_ACCUM_KAHAN;
+    CHECK_ARG(!kahan || (kahan_sum && kahan_comp), "a KAHAN image needs its sums and compensations");
+    cudaStream_t st = img->ctx->stream;
+    const size_t bytes = 16 * (size_t)img->width * img->height;
+    SOLRT_CUDA(cudaMemcpyAsync(accum, img->accum.ptr, bytes, cudaMemcpyDeviceToHost, st));
+    if (kahan) {
+        SOLRT_CUDA(cudaMemcpyAsync(kahan_sum, img->ksum.ptr, bytes, cudaMemcpyDeviceToHost, st));
+        SOLRT_CUDA(cudaMemcpyAsync(kahan_comp, img->kcomp.ptr, bytes, cudaMemcpyDeviceToHost, st));
+    }
+    SOLRT_CUDA(cudaStreamSynchronize(st));
+    return check_device_flags(*img->ctx);
+}
+
+solrt_status solrt_image_restore(solrt_image* img, const float* accum, const float* kahan_sum,
+                                 const float* kahan_comp) {
+    CHECK_ARG(img && accum, "null argument");
+    const bool kahan = img->accum_mode == SOLRT_ACCUM_KAHAN;
+    CHECK_ARG(!kahan || (kahan_sum && kahan_comp), "a KAHAN image needs its sums and compensations");
+    cudaStream_t st = img->ctx->stream;
+    const size_t bytes = 16 * (size_t)img->width * img->height;
+    SOLRT_CUDA(cudaMemcpyAsync(img->accum.ptr, accum, bytes, cudaMemcpyHostToDevice, st));
+    if (kahan) {
+        SOLRT_CUDA(cudaMemcpyAsync(img->ksum.ptr, kahan_sum, bytes, cudaMemcpyHostToDevice, st));
+        SOLRT_CUDA(cudaMemcpyAsync(img->kcomp.ptr, kahan_comp, bytes, cudaMemcpyHostToDevice, st));
+    }
+    SOLRT_CUDA(cudaStreamSynchronize(st));
+    return SOLRT_OK;
+}
+
 solrt_status solrt_image_device_ptrs(solrt_image* img, void** accum, void** rgba8) {
     CHECK_ARG(img, "null image");
     if (accum) *accum = img->accum.ptr;

@@ -158,3 +158,35 @@ def test_full_size_soup_properties(solrt, ctx):
         assert 1920 * 1080 <= st.segments <= 5 * 1920 * 1080
     assert np.array_equal(imgs[0], imgs[1])
     assert np.isfinite(imgs[0]).all()
+
+
+@pytest.mark.parametrize("accum", ["mix", "kahan"])
+def test_checkpoint_resume(solrt, ctx, accum):
+    """Four frames rendered straight through equal two frames, a snapshot of
+    the accumulation state restored into a fresh image, then frames 2 and 3
+    (bit for bit, both accumulation modes)."""
+    data = S.cornell()
+    w, h = 32, 24
+    mode = solrt.ACCUM_KAHAN if accum == "kahan" else solrt.ACCUM_REF_MIX
+    cam = camera_of(data, w / h)
+    sc = solrt.SceneDescription(ctx, data)
+    r = solrt.Renderer(ctx)
+
+    def params(f):
+        return solrt.render_params(w, h, spp=2, max_bounces=4, frame=f, material_mode=solrt.MATERIAL_LAMBERT,
+                                   rng_mode=solrt.RNG_PER_SAMPLE, seed=4, accum_mode=mode)
+    straight = solrt.Image(ctx, w, h, mode)
+    for f in range(4):
+        r.cmd_trace_rays(sc, cam, params(f), straight)
+    a_ref, b_ref = straight.read()
+    first = solrt.Image(ctx, w, h, mode)
+    for f in range(2):
+        r.cmd_trace_rays(sc, cam, params(f), first)
+    snap = first.snapshot()
+    resumed = solrt.Image(ctx, w, h, mode)
+    resumed.restore(snap)
+    for f in range(2, 4):
+        r.cmd_trace_rays(sc, cam, params(f), resumed)
+    a, b = resumed.read()
+    assert np.array_equal(a.view(np.uint32), a_ref.view(np.uint32))
+    assert np.array_equal(b, b_ref)
