@@ -280,6 +280,16 @@ def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, mai
     a = hits["bvh2_fp32"].view(torch.int32)
     out["hit_mismatches"] = {k: int((a != hits[k].view(torch.int32)).any(dim=1).sum().item())
                              for k in ("bvh4_q8", "bvh8_q8")}
+    # hits within about one float ulp of a triangle edge (a barycentric below
+    # 2^-23), counted separately: the watertight test and the lower-index tie
+    # rule make even these agree across BVHs
+    h = hits["bvh2_fp32"]
+    hit = a[:, 1] != -1
+    u, v = h[:, 2], h[:, 3]
+    edge = hit & (torch.minimum(torch.minimum(u, v), 1.0 - u - v) < 2.0 ** -23)
+    out["near_edge_hits"] = int(edge.sum().item())
+    out["near_edge_mismatches"] = {k: int(((a != hits[k].view(torch.int32)).any(dim=1) & edge).sum().item())
+                                   for k in ("bvh4_q8", "bvh8_q8")}
     out["hits"] = int((a[:, 1] != -1).sum().item())
     return out
 
