@@ -6,6 +6,11 @@
 //   w2: qlo.x[0..7], qlo.y[0..7]        (u8)
 //   w3: qlo.z[0..7], qhi.x[0..7]        (u8)
 //   w4: qhi.y[0..7], qhi.z[0..7]        (u8)
+// The full-precision variant (SOLRT_BVH8_F32, 224 B = 7 x 32 B) keeps the
+// same slots, meta bytes and child / triangle bases:
+//   w0: child_base, tri_base, meta[0..3], meta[4..7]    w1: imask, 0, 0, 0
+//   then lo.x[8], hi.x[8], lo.y[8], hi.y[8], lo.z[8], hi.z[8] (float), each
+//   child box widened outward by widen_lo / widen_hi.
 // Child slot s decodes to lo = p + qlo * 2^e, hi = p + qhi * 2^e per axis;
 // the build rounds outward so the decoded box contains the child exactly.
 // meta[s]: 0 = empty; internal child = 0b001_xxxxx with xxxxx = 24 + s;
@@ -30,9 +35,10 @@ struct Bvh8BuildInput {
 // In-place exclusive scan of `len` u32 counts (bvh_build.cu).
 void launch_scan_exclusive(uint32_t* data, uint32_t len, cudaStream_t stream);
 
-// Writes the `width`-wide nodes (8: 80 B, 4: 64 B) into `nodes` and the
-// triangles in leaf order into `tris`. Synchronises.
-solrt_status build_wide(Context& ctx, const Bvh8BuildInput& in, uint32_t width, DeviceBuffer& nodes,
+// Writes the `width`-wide nodes (8: 80 B quantised or, with f32, 224 B full
+// precision; 4: 64 B quantised) into `nodes` and the triangles in leaf order
+// into `tris`. Synchronises.
+solrt_status build_wide(Context& ctx, const Bvh8BuildInput& in, uint32_t width, bool f32, DeviceBuffer& nodes,
                         DeviceBuffer& tris, uint32_t* node_count, uint32_t* depth);
 
 }  // namespace solrt

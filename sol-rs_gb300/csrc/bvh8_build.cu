@@ -147,12 +147,15 @@ __device__ __forceinline__ void grid_anchor(float lo, float hi, float& p, int& e
 }
 
 // Pass 2: slots, quantisation, node + next tasks + leaf triangles.
+// f32: write the full-precision 224-byte node (header + 6 x 8 FP32 planes,
+// each child box widened outward by widen_lo / widen_hi) instead of the
+// quantised 80-byte one.
 __global__ void k_emit(const uint32_t* __restrict__ tasks, uint32_t ntasks, uint32_t node_base,
                        uint32_t next_base, uint32_t tri_level_base, const uint32_t* __restrict__ gathered,
                        const uint32_t* __restrict__ inner_scan, const uint32_t* __restrict__ tri_scan,
                        const uint2* __restrict__ range, const float4* __restrict__ nbox,
                        const float4* __restrict__ tris_in, uint32_t leaf_max, uint4* __restrict__ nodes,
-                       uint32_t* __restrict__ next_tasks, float4* __restrict__ tris_out) {
+                       uint32_t* __restrict__ next_tasks, float4* __restrict__ tris_out, bool f32) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ntasks) return;
     const uint32_t b = tasks[t];
@@ -252,6 +255,20 @@ __global__ void k_emit(const uint32_t* __restrict__ tasks, uint32_t ntasks, uint
         }
         meta[s >> 2] |= mb << (8u * (uint32_t)(s & 3));
     }
+    if (f32) {
+        uint4* out = nodes + 14 * (size_t)(node_base + t);
+        out[0] = make_uint4(child_base, tri_base, meta[0], meta[1]);
+        out[1] = make_uint4(imask, 0u, 0u, 0u);
+        float* planes = reinterpret_cast<float*>(out + 2);  // [axis][lo / hi][slot]
+        for (int s = 0; s < 8; ++s) {
+            const int i = child_in_slot[s];
+            for (int a = 0; a < 3; ++a) {
+                planes[(2 * a) * 8 + s] = i < 0 ? 0.0f : widen_lo(cb[i].lo[a]);
+                planes[(2 * a + 1) * 8 + s] = i < 0 ? 0.0f : widen_hi(cb[i].hi[a]);
+            }
+        }
+        return;
+    }
     const uint32_t packed = ((uint32_t)(uint8_t)(int8_t)e[0]) | ((uint32_t)(uint8_t)(int8_t)e[1] << 8) |
                             ((uint32_t)(uint8_t)(int8_t)e[2] << 16) | (imask << 24);
     uint4* out = nodes + 5 * (size_t)(node_base + t);
@@ -347,12 +364,12 @@ inline uint32_t blocks_of(uint64_t n, uint32_t b) { return (uint32_t)((n + b - 1
 
 }  // namespace
 
-solrt_status build_wide(Context& ctx, const Bvh8BuildInput& in, uint32_t width, DeviceBuffer& nodes,
+solrt_status build_wide(Context& ctx, const Bvh8BuildInput& in, uint32_t width, bool f32, DeviceBuffer& nodes,
                         DeviceBuffer& tris, uint32_t* node_count, uint32_t* depth) {
     const uint32_t n = in.n;
     cudaStream_t st = ctx.stream;
     const uint32_t max_nodes = std::max(1u, n);
-    SOLRT_TRY(nodes.alloc((width == 4 ? 64ull : 80ull) * max_nodes));
+    SOLRT_TRY(nodes.alloc((width == 4 ? 64ull : (f32 ? 224ull : 80ull)) * max_nodes));
     SOLRT_TRY(tris.alloc(48ull * n));
     DeviceBuffer task[2], gathered, inner, ntri;
     SOLRT_TRY(task[0].alloc(4ull * max_nodes));
@@ -390,7 +407,7 @@ solrt_status build_wide(Context& ctx, const Bvh8BuildInput& in, uint32_t width, 
                                                            tri_level_base, gathered.as<uint32_t>(),
                                                            inner.as<uint32_t>(), ntri.as<uint32_t>(), in.range,
                                                            in.nbox, in.tri_wt_leaf, in.leaf_max, nodes.as<uint4>(),
-                                                           task[cur ^ 1].as<uint32_t>(), tris.as<float4>());
+                                                           task[cur ^ 1].as<uint32_t>(), tris.as<float4>(), f32);
         ctx.launches += 4;
         SOLRT_CUDA(cudaStreamSynchronize(st));
         SOLRT_CUDA(cudaGetLastError());

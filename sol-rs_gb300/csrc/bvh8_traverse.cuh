@@ -8,13 +8,14 @@
 // tested right away so that the closest distance shrinks early.
 //
 // Child box planes are decoded as p + q * 2^e from 8-bit q. The distance to
-// a plane is fma(q, 2^e / d, (p - o) / d): the build keeps every face (the
-// anchor plane q = 0 included: it sits one step below the node's box) at
-// least one grid step away from the child's triangles, which bounds the
-// rounding error of that form well inside the margin, and the relative 2^-16
-// widening of the far distance covers the rest. Zero
+// a plane is fma(2^23 + q, 2^e / d, (p - o) / d - 2^23 * 2^e / d): the build
+// keeps every face (the anchor plane q = 0 included: it sits one step below
+// the node's box) at least one grid step away from the child's triangles,
+// which bounds the rounding error of that form well inside the margin, and
+// the relative 2^-16 widening of the far distance covers the rest. Zero
 // direction components are replaced by box_dir for these tests only (the
-// triangle test uses the exact direction).
+// triangle test uses the exact direction). SOLRT_BVH8_F32 nodes hold the
+// child boxes in FP32 and use the binary BVH's slab test instead.
 #pragma once
 
 #include "traverse.cuh"
@@ -25,18 +26,106 @@ namespace solrt {
 #define SOLRT_BVH8_STACK 32
 #endif
 
-// byte k of `word` as a float, exactly: the byte is placed in the mantissa of
-// 2^23 and 2^23 is subtracted.
-SOLRT_D float byte_as_float(uint32_t word, uint32_t k) {
-    return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7440u | k)) - 8388608.0f;
-}
-
 // byte k of `word` as the float 2^23 + byte, exactly.
 SOLRT_D float byte_biased(uint32_t word, uint32_t k) {
     return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7440u | k));
 }
 
-template <bool kCount>
+// Tests the 8 children of one node. Returns the hit internal children in
+// visiting order (bit s ^ oct for slot s) and the hit leaf triangles
+// (bit o of the node's triangle range).
+SOLRT_D void bvh8_node_test(const uint4& w0, const uint4& w1, const uint4& w2, const uint4& w3, const uint4& w4,
+                            float ox, float oy, float oz, float ix, float iy, float iz, bool negx, bool negy,
+                            bool negz, uint32_t oct, float tmin, float tmax, uint32_t& hit_inner,
+                            uint32_t& hit_tri) {
+    const int ex = (int)(int8_t)(w0.w & 0xffu), ey = (int)(int8_t)((w0.w >> 8) & 0xffu),
+              ez = (int)(int8_t)((w0.w >> 16) & 0xffu);
+    const uint32_t imask = w0.w >> 24;
+    const float sx = __uint_as_float((uint32_t)(ex + 127) << 23) * ix;
+    const float sy = __uint_as_float((uint32_t)(ey + 127) << 23) * iy;
+    const float sz = __uint_as_float((uint32_t)(ez + 127) << 23) * iz;
+    // plane q is at t = (2^23 + q) * s + (a - 2^23 s): the biased byte
+    // (byte_biased) needs no conversion. Rounding a - 2^23 s adds at most half
+    // a grid step (in t) to each face, inside the one-step margin every face
+    // has (grid_anchor); the rest is relative to |t| as in trace_bvh8.
+    const float ax = fmaf(-8388608.0f, sx, (__uint_as_float(w0.x) - ox) * ix);
+    const float ay = fmaf(-8388608.0f, sy, (__uint_as_float(w0.y) - oy) * iy);
+    const float az = fmaf(-8388608.0f, sz, (__uint_as_float(w0.z) - oz) * iz);
+    // near / far plane bytes per axis: lo is near for a positive direction
+    const uint32_t nx0 = negx ? w3.z : w2.x, nx1 = negx ? w3.w : w2.y;
+    const uint32_t fx0 = negx ? w2.x : w3.z, fx1 = negx ? w2.y : w3.w;
+    const uint32_t ny0 = negy ? w4.x : w2.z, ny1 = negy ? w4.y : w2.w;
+    const uint32_t fy0 = negy ? w2.z : w4.x, fy1 = negy ? w2.w : w4.y;
+    const uint32_t nz0 = negz ? w4.z : w3.x, nz1 = negz ? w4.w : w3.y;
+    const uint32_t fz0 = negz ? w3.x : w4.z, fz1 = negz ? w3.y : w4.w;
+    hit_inner = 0;
+    hit_tri = 0;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const uint32_t k = (uint32_t)(s & 3);
+        const uint32_t meta = ((s < 4 ? w1.z : w1.w) >> (8u * k)) & 0xffu;
+        const float tnx = fmaf(byte_biased(s < 4 ? nx0 : nx1, k), sx, ax);
+        const float tny = fmaf(byte_biased(s < 4 ? ny0 : ny1, k), sy, ay);
+        const float tnz = fmaf(byte_biased(s < 4 ? nz0 : nz1, k), sz, az);
+        const float tfx = fmaf(byte_biased(s < 4 ? fx0 : fx1, k), sx, ax);
+        const float tfy = fmaf(byte_biased(s < 4 ? fy0 : fy1, k), sy, ay);
+        const float tfz = fmaf(byte_biased(s < 4 ? fz0 : fz1, k), sz, az);
+        const float tn = max3(tnx, tny, fmaxf(tnz, tmin));
+        const float tf = min3(tfx, tfy, fminf(tfz, tmax));
+        if (meta != 0u && tn <= tf * 1.0000153f) {
+            if (imask & (1u << s)) hit_inner |= 1u << ((uint32_t)s ^ oct);
+            else hit_tri |= (meta >> 5) << (meta & 31u);
+        }
+    }
+}
+
+// The same outputs for a full-precision node (SOLRT_BVH8_F32, 224 B at np):
+// the slab test of the binary BVH (fma(plane, 1/d, -o/d) against child boxes
+// widened at build time) on 8 children, one axis at a time.
+SOLRT_D void bvh8f_node_test(const float4* np, float ix, float iy, float iz, float nox, float noy, float noz,
+                             uint32_t oct, float tmin, float tmax, uint32_t& hit_inner, uint32_t& hit_tri,
+                             uint32_t& child_base, uint32_t& tri_base, uint32_t& imask) {
+    float4 h0, h1;
+    ldg_2x4(np, h0, h1);
+    child_base = __float_as_uint(h0.x);
+    tri_base = __float_as_uint(h0.y);
+    const uint32_t meta0 = __float_as_uint(h0.z), meta1 = __float_as_uint(h0.w);
+    imask = __float_as_uint(h1.x);
+    float tn[8], tf[8];
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        tn[s] = tmin;
+        tf[s] = tmax;
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float4 l0, l1, u0, u1;
+        ldg_2x4(np + 2 + 4 * a, l0, l1);
+        ldg_2x4(np + 4 + 4 * a, u0, u1);
+        const float inv = a == 0 ? ix : (a == 1 ? iy : iz);
+        const float no = a == 0 ? nox : (a == 1 ? noy : noz);
+        const float lo[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
+        const float hi[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
+#pragma unroll
+        for (int s = 0; s < 8; ++s) {
+            const float t0 = fmaf(lo[s], inv, no), t1 = fmaf(hi[s], inv, no);
+            tn[s] = fmaxf(tn[s], fminf(t0, t1));
+            tf[s] = fminf(tf[s], fmaxf(t0, t1));
+        }
+    }
+    hit_inner = 0;
+    hit_tri = 0;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const uint32_t meta = ((s < 4 ? meta0 : meta1) >> (8u * (uint32_t)(s & 3))) & 0xffu;
+        if (meta != 0u && tn[s] <= tf[s] * 1.0000153f) {
+            if (imask & (1u << s)) hit_inner |= 1u << ((uint32_t)s ^ oct);
+            else hit_tri |= (meta >> 5) << (meta & 31u);
+        }
+    }
+}
+
+template <bool kCount, bool kF32 = false>
 SOLRT_D void trace_bvh8(const TravScene& sc, float ox, float oy, float oz, float dx, float dy, float dz, float tmin,
                         float tmax, HitRec& best, TraceCounters& cnt, uint32_t& eflags) {
     best.t = tmax;
@@ -47,6 +136,7 @@ SOLRT_D void trace_bvh8(const TravScene& sc, float ox, float oy, float oz, float
     const RayWT r = setup_ray(ox, oy, oz, dx, dy, dz, tmin);
     const float bx = box_dir(dx), by = box_dir(dy), bz = box_dir(dz);
     const float ix = 1.0f / bx, iy = 1.0f / by, iz = 1.0f / bz;
+    const float nox = -(ox * ix), noy = -(oy * iy), noz = -(oz * iz);
     const bool negx = signbit(bx), negy = signbit(by), negz = signbit(bz);
     const uint32_t oct = (negx ? 1u : 0u) | (negy ? 2u : 0u) | (negz ? 4u : 0u);
     const uint4* nodes = reinterpret_cast<const uint4*>(sc.nodes);
@@ -61,44 +151,21 @@ SOLRT_D void trace_bvh8(const TravScene& sc, float ox, float oy, float oz, float
             eflags |= SOLRT_EFLAG_INDEX;
             break;
         }
-        const uint4* np = nodes + 5 * (size_t)node;
-        const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3), w4 = __ldg(np + 4);
         if (kCount) ++cnt.nodes;
-        const int ex = (int)(int8_t)(w0.w & 0xffu), ey = (int)(int8_t)((w0.w >> 8) & 0xffu),
-                  ez = (int)(int8_t)((w0.w >> 16) & 0xffu);
-        const uint32_t imask = w0.w >> 24;
-        const float sx = __uint_as_float((uint32_t)(ex + 127) << 23) * ix;
-        const float sy = __uint_as_float((uint32_t)(ey + 127) << 23) * iy;
-        const float sz = __uint_as_float((uint32_t)(ez + 127) << 23) * iz;
-        const float ax = (__uint_as_float(w0.x) - ox) * ix;
-        const float ay = (__uint_as_float(w0.y) - oy) * iy;
-        const float az = (__uint_as_float(w0.z) - oz) * iz;
-        // near / far plane bytes per axis: lo is near for a positive direction
-        const uint32_t nx0 = negx ? w3.z : w2.x, nx1 = negx ? w3.w : w2.y;
-        const uint32_t fx0 = negx ? w2.x : w3.z, fx1 = negx ? w2.y : w3.w;
-        const uint32_t ny0 = negy ? w4.x : w2.z, ny1 = negy ? w4.y : w2.w;
-        const uint32_t fy0 = negy ? w2.z : w4.x, fy1 = negy ? w2.w : w4.y;
-        const uint32_t nz0 = negz ? w4.z : w3.x, nz1 = negz ? w4.w : w3.y;
-        const uint32_t fz0 = negz ? w3.x : w4.z, fz1 = negz ? w3.y : w4.w;
-        uint32_t hit_inner = 0, hit_tri = 0;
-#pragma unroll
-        for (int s = 0; s < 8; ++s) {
-            const uint32_t k = (uint32_t)(s & 3);
-            const uint32_t meta = ((s < 4 ? w1.z : w1.w) >> (8u * k)) & 0xffu;
-            const float tnx = fmaf(byte_as_float(s < 4 ? nx0 : nx1, k), sx, ax);
-            const float tny = fmaf(byte_as_float(s < 4 ? ny0 : ny1, k), sy, ay);
-            const float tnz = fmaf(byte_as_float(s < 4 ? nz0 : nz1, k), sz, az);
-            const float tfx = fmaf(byte_as_float(s < 4 ? fx0 : fx1, k), sx, ax);
-            const float tfy = fmaf(byte_as_float(s < 4 ? fy0 : fy1, k), sy, ay);
-            const float tfz = fmaf(byte_as_float(s < 4 ? fz0 : fz1, k), sz, az);
-            const float tn = fmaxf(fmaxf(fmaxf(tnx, tny), tnz), tmin);
-            const float tf = fminf(fminf(fminf(tfx, tfy), tfz), best.t);
-            if (meta != 0u && tn <= tf * 1.0000153f) {
-                if (imask & (1u << s)) hit_inner |= 1u << ((uint32_t)s ^ oct);
-                else hit_tri |= (meta >> 5) << (meta & 31u);
-            }
+        uint32_t hit_inner = 0, hit_tri = 0, child_base = 0, tri_base = 0, imask = 0;
+        if (kF32) {
+            bvh8f_node_test(sc.nodes + 14 * (size_t)node, ix, iy, iz, nox, noy, noz, oct, tmin, best.t, hit_inner,
+                            hit_tri, child_base, tri_base, imask);
+        } else {
+            const uint4* np = nodes + 5 * (size_t)node;
+            const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3),
+                        w4 = __ldg(np + 4);
+            bvh8_node_test(w0, w1, w2, w3, w4, ox, oy, oz, ix, iy, iz, negx, negy, negz, oct, tmin, best.t,
+                           hit_inner, hit_tri);
+            child_base = w1.x;
+            tri_base = w1.y;
+            imask = w0.w >> 24;
         }
-        const uint32_t tri_base = w1.y;
         while (hit_tri) {
             const uint32_t k = (uint32_t)(__ffs(hit_tri) - 1);
             hit_tri &= hit_tri - 1u;
@@ -116,7 +183,7 @@ SOLRT_D void trace_bvh8(const TravScene& sc, float ox, float oy, float oz, float
                 if (sp < SOLRT_BVH8_STACK) stack[sp++] = group;
                 else eflags |= SOLRT_EFLAG_STACK;
             }
-            group = make_uint2(w1.x, (hit_inner << 24) | imask);
+            group = make_uint2(child_base, (hit_inner << 24) | imask);
         }
         if ((group.y >> 24) == 0u) {
             if (sp == 0) break;

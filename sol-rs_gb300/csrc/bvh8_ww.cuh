@@ -10,8 +10,9 @@
 //           parked. The phase ends when no lane can step, or when fewer than
 //           SOLRT_BVH8_NODE_MIN lanes can while others hold triangles;
 //   leaves  lanes test their parked triangles, one per step.
-// The child-box test is the one of trace_bvh8 (bvh8_traverse.cuh), so the
-// closest hit equals that of the per-ray loop.
+// The child-box tests are those of trace_bvh8 (bvh8_traverse.cuh: quantised
+// or, for SOLRT_BVH8_F32, full-precision nodes), so the closest hit equals
+// that of the per-ray loop.
 #pragma once
 
 #include "bvh8_traverse.cuh"
@@ -25,55 +26,7 @@ namespace solrt {
 #define SOLRT_BVH8_NODE_MIN 12
 #endif
 
-// Tests the 8 children of one node. Returns the hit internal children in
-// visiting order (bit s ^ oct for slot s) and the hit leaf triangles
-// (bit o of the node's triangle range).
-SOLRT_D void bvh8_node_test(const uint4& w0, const uint4& w1, const uint4& w2, const uint4& w3, const uint4& w4,
-                            float ox, float oy, float oz, float ix, float iy, float iz, bool negx, bool negy,
-                            bool negz, uint32_t oct, float tmin, float tmax, uint32_t& hit_inner,
-                            uint32_t& hit_tri) {
-    const int ex = (int)(int8_t)(w0.w & 0xffu), ey = (int)(int8_t)((w0.w >> 8) & 0xffu),
-              ez = (int)(int8_t)((w0.w >> 16) & 0xffu);
-    const uint32_t imask = w0.w >> 24;
-    const float sx = __uint_as_float((uint32_t)(ex + 127) << 23) * ix;
-    const float sy = __uint_as_float((uint32_t)(ey + 127) << 23) * iy;
-    const float sz = __uint_as_float((uint32_t)(ez + 127) << 23) * iz;
-    // plane q is at t = (2^23 + q) * s + (a - 2^23 s): the biased byte
-    // (byte_biased) needs no conversion. Rounding a - 2^23 s adds at most half
-    // a grid step (in t) to each face, inside the one-step margin every face
-    // has (grid_anchor); the rest is relative to |t| as in trace_bvh8.
-    const float ax = fmaf(-8388608.0f, sx, (__uint_as_float(w0.x) - ox) * ix);
-    const float ay = fmaf(-8388608.0f, sy, (__uint_as_float(w0.y) - oy) * iy);
-    const float az = fmaf(-8388608.0f, sz, (__uint_as_float(w0.z) - oz) * iz);
-    // near / far plane bytes per axis: lo is near for a positive direction
-    const uint32_t nx0 = negx ? w3.z : w2.x, nx1 = negx ? w3.w : w2.y;
-    const uint32_t fx0 = negx ? w2.x : w3.z, fx1 = negx ? w2.y : w3.w;
-    const uint32_t ny0 = negy ? w4.x : w2.z, ny1 = negy ? w4.y : w2.w;
-    const uint32_t fy0 = negy ? w2.z : w4.x, fy1 = negy ? w2.w : w4.y;
-    const uint32_t nz0 = negz ? w4.z : w3.x, nz1 = negz ? w4.w : w3.y;
-    const uint32_t fz0 = negz ? w3.x : w4.z, fz1 = negz ? w3.y : w4.w;
-    hit_inner = 0;
-    hit_tri = 0;
-#pragma unroll
-    for (int s = 0; s < 8; ++s) {
-        const uint32_t k = (uint32_t)(s & 3);
-        const uint32_t meta = ((s < 4 ? w1.z : w1.w) >> (8u * k)) & 0xffu;
-        const float tnx = fmaf(byte_biased(s < 4 ? nx0 : nx1, k), sx, ax);
-        const float tny = fmaf(byte_biased(s < 4 ? ny0 : ny1, k), sy, ay);
-        const float tnz = fmaf(byte_biased(s < 4 ? nz0 : nz1, k), sz, az);
-        const float tfx = fmaf(byte_biased(s < 4 ? fx0 : fx1, k), sx, ax);
-        const float tfy = fmaf(byte_biased(s < 4 ? fy0 : fy1, k), sy, ay);
-        const float tfz = fmaf(byte_biased(s < 4 ? fz0 : fz1, k), sz, az);
-        const float tn = max3(tnx, tny, fmaxf(tnz, tmin));
-        const float tf = min3(tfx, tfy, fminf(tfz, tmax));
-        if (meta != 0u && tn <= tf * 1.0000153f) {
-            if (imask & (1u << s)) hit_inner |= 1u << ((uint32_t)s ^ oct);
-            else hit_tri |= (meta >> 5) << (meta & 31u);
-        }
-    }
-}
-
-template <class IO, bool kCount>
+template <class IO, bool kCount, bool kF32 = false>
 SOLRT_D void extend_bvh8_ww(const IO& io, uint32_t n, unsigned int* work, TraceCounters& cnt, uint32_t& ef) {
     const int lane = threadIdx.x & 31;
     const uint32_t lane_lt = (1u << lane) - 1u;
@@ -88,6 +41,7 @@ SOLRT_D void extend_bvh8_ww(const IO& io, uint32_t n, unsigned int* work, TraceC
     RayWT r;
     TravScene ts{nullptr, nullptr, 0u, 0u};
     float ix = 0.0f, iy = 0.0f, iz = 0.0f;
+    float nox = 0.0f, noy = 0.0f, noz = 0.0f;  // -o / box_dir(d) (FP32 nodes)
     HitRec best{0.0f, SOLRT_NO_HIT, 0.0f, 0.0f};
     const uint4* nodes = nullptr;
     for (;;) {
@@ -118,6 +72,9 @@ SOLRT_D void extend_bvh8_ww(const IO& io, uint32_t n, unsigned int* work, TraceC
                     negx = signbit(bx);
                     negy = signbit(by);
                     negz = signbit(bz);
+                    nox = -(o.x * ix);
+                    noy = -(o.y * iy);
+                    noz = -(o.z * iz);
                     oct = (negx ? 1u : 0u) | (negy ? 2u : 0u) | (negz ? 4u : 0u);
                     best = HitRec{d.w, SOLRT_NO_HIT, 0.0f, 0.0f};
                     budget = 2u * (ts.node_count + ts.tri_count) + 64u;
@@ -154,15 +111,23 @@ SOLRT_D void extend_bvh8_ww(const IO& io, uint32_t n, unsigned int* work, TraceC
                     ef |= SOLRT_EFLAG_INDEX;
                     sp = 0;
                 } else {
-                    const uint4* np = nodes + 5 * (size_t)node;
-                    const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3),
-                                w4 = __ldg(np + 4);
                     if (kCount) ++cnt.nodes;
                     uint32_t hi = 0, ht = 0;
-                    bvh8_node_test(w0, w1, w2, w3, w4, r.ox, r.oy, r.oz, ix, iy, iz, negx, negy, negz, oct, r.tmin,
-                                   best.t, hi, ht);
-                    if (hi) grp = make_uint2(w1.x, (hi << 24) | (w0.w >> 24));
-                    tgrp = make_uint2(w1.y, ht);
+                    if constexpr (kF32) {
+                        uint32_t cbase = 0, tbase = 0, imask = 0;
+                        bvh8f_node_test(ts.nodes + 14 * (size_t)node, ix, iy, iz, nox, noy, noz, oct, r.tmin, best.t,
+                                        hi, ht, cbase, tbase, imask);
+                        if (hi) grp = make_uint2(cbase, (hi << 24) | imask);
+                        tgrp = make_uint2(tbase, ht);
+                    } else {
+                        const uint4* np = nodes + 5 * (size_t)node;
+                        const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3),
+                                    w4 = __ldg(np + 4);
+                        bvh8_node_test(w0, w1, w2, w3, w4, r.ox, r.oy, r.oz, ix, iy, iz, negx, negy, negz, oct,
+                                       r.tmin, best.t, hi, ht);
+                        if (hi) grp = make_uint2(w1.x, (hi << 24) | (w0.w >> 24));
+                        tgrp = make_uint2(w1.y, ht);
+                    }
                 }
             }
         }

@@ -501,8 +501,9 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
     ctx.launches += 5;
     SOLRT_CUDA(cudaGetLastError());
 
-    if (desc.kind == SOLRT_BVH8_Q8 || desc.kind == SOLRT_BVH4_Q8) {
+    if (desc.kind == SOLRT_BVH8_Q8 || desc.kind == SOLRT_BVH4_Q8 || desc.kind == SOLRT_BVH8_F32) {
         const uint32_t width = desc.kind == SOLRT_BVH4_Q8 ? 4u : 8u;
+        const bool f32 = desc.kind == SOLRT_BVH8_F32;
         Bvh8BuildInput in;
         in.n = n;
         in.child = child.as<uint32_t>();
@@ -512,7 +513,7 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
         in.leaf_max = desc.leaf_max == 0 ? 1u : std::min(3u, desc.leaf_max);
         DeviceBuffer tri8;
         uint32_t node_count = 0, depth8 = 0;
-        SOLRT_TRY(build_wide(ctx, in, width, sc.nodes, tri8, &node_count, &depth8));
+        SOLRT_TRY(build_wide(ctx, in, width, f32, sc.nodes, tri8, &node_count, &depth8));
         sc.tri_wt.release();
         sc.tri_wt.ptr = tri8.ptr;
         sc.tri_wt.bytes = tri8.bytes;
@@ -520,7 +521,7 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
         tri8.bytes = 0;
         sc.info.node_count = node_count;
         sc.info.depth = depth8;
-        sc.info.node_bytes = (uint64_t)node_count * (width == 4 ? 64u : 80u);
+        sc.info.node_bytes = (uint64_t)node_count * (width == 4 ? 64u : (f32 ? 224u : 80u));
         SOLRT_TRY(check_wide_depth(width, depth8));
     } else {
         sc.nodes.ptr = bvh2_nodes.ptr;
@@ -599,8 +600,9 @@ solrt_status refit_bvh(Context& ctx, Scene& sc) {
     const uint32_t ni = n > 1 ? n - 1 : 1;
     cudaStream_t st = ctx.stream;
     SOLRT_CUDA(cudaEventRecord(ctx.ev0, st));
-    const bool b8 = sc.info.kind == SOLRT_BVH8_Q8 || sc.info.kind == SOLRT_BVH4_Q8;
+    const bool b8 = sc.info.kind == SOLRT_BVH8_Q8 || sc.info.kind == SOLRT_BVH4_Q8 || sc.info.kind == SOLRT_BVH8_F32;
     const uint32_t width = sc.info.kind == SOLRT_BVH4_Q8 ? 4u : 8u;
+    const bool f32 = sc.info.kind == SOLRT_BVH8_F32;
     DeviceBuffer flags, nbox, nodes2, tri2;
     SOLRT_TRY(flags.alloc(sizeof(unsigned int) * (size_t)ni));
     SOLRT_TRY(nbox.alloc(2 * sizeof(float4) * (size_t)ni));
@@ -629,13 +631,13 @@ solrt_status refit_bvh(Context& ctx, Scene& sc) {
         in.leaf_max = sc.desc.leaf_max == 0 ? 1u : std::min(3u, sc.desc.leaf_max);
         DeviceBuffer nodes8, tri8;
         uint32_t node_count = 0, depth8 = 0;
-        SOLRT_TRY(build_wide(ctx, in, width, nodes8, tri8, &node_count, &depth8));
+        SOLRT_TRY(build_wide(ctx, in, width, f32, nodes8, tri8, &node_count, &depth8));
         SOLRT_TRY(check_wide_depth(width, depth8));
         sc.nodes.adopt(nodes8);
         sc.tri_wt.adopt(tri8);
         sc.info.node_count = node_count;
         sc.info.depth = depth8;
-        sc.info.node_bytes = (uint64_t)node_count * (width == 4 ? 64u : 80u);
+        sc.info.node_bytes = (uint64_t)node_count * (width == 4 ? 64u : (f32 ? 224u : 80u));
         sc.info.tri_bytes = sc.tri_wt.bytes;
     }
     SOLRT_CUDA(cudaEventRecord(ctx.ev1, st));

@@ -181,6 +181,7 @@ __global__ void __launch_bounds__(128) k_megakernel(const DevJob* __restrict__ j
             for (;;) {
                 HitRec h;
                 if (KIND == SOLRT_BVH8_Q8) trace_bvh8<false>(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, fb_ef[1]);
+                else if (KIND == SOLRT_BVH8_F32) trace_bvh8<false, true>(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, fb_ef[1]);
                 else if (KIND == SOLRT_BVH4_Q8) trace_bvh4_ray(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, fb_ef[1]);
                 else trace_bvh2_ray(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, fb_ef[1]);
                 ++segs;
@@ -251,6 +252,7 @@ __device__ __forceinline__ void trace_one(const TravScene& ts, float ox, float o
                                           float dz, float tmin, float tmax, HitRec& h, TraceCounters& cnt,
                                           uint32_t& ef) {
     if (KIND == SOLRT_BVH8_Q8) trace_bvh8<false>(ts, ox, oy, oz, dx, dy, dz, tmin, tmax, h, cnt, ef);
+    else if (KIND == SOLRT_BVH8_F32) trace_bvh8<false, true>(ts, ox, oy, oz, dx, dy, dz, tmin, tmax, h, cnt, ef);
     else if (KIND == SOLRT_BVH4_Q8) trace_bvh4_ray(ts, ox, oy, oz, dx, dy, dz, tmin, tmax, h, cnt, ef);
     else trace_bvh2_ray(ts, ox, oy, oz, dx, dy, dz, tmin, tmax, h, cnt, ef);
 }
@@ -727,7 +729,7 @@ solrt_status batch_autotune(Batch& b, solrt_tune_result* out) {
         const uint32_t blocks[3] = {64u, 128u, 256u};
         for (uint32_t bl : blocks) {
             for (uint32_t sm : smems) {
-                if (b.kind == SOLRT_BVH8_Q8 && sm != initial.smem) continue;  // no shared stack
+                if ((b.kind == SOLRT_BVH8_Q8 || b.kind == SOLRT_BVH8_F32) && sm != initial.smem) continue;  // no shared stack
                 TuneConfig c = initial;
                 c.block = bl;
                 c.smem = sm;
@@ -833,10 +835,12 @@ static solrt_status render_sibling(Context& ctx, const Scene& sc, const solrt_ca
     if (p.integrator == SOLRT_INTEGRATOR_DEBUG) {
         if (kind == SOLRT_BVH8_Q8) k_debug<SOLRT_BVH8_Q8><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
         else if (kind == SOLRT_BVH4_Q8) k_debug<SOLRT_BVH4_Q8><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
+        else if (kind == SOLRT_BVH8_F32) k_debug<SOLRT_BVH8_F32><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
         else k_debug<SOLRT_BVH2><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
     } else {
         if (kind == SOLRT_BVH8_Q8) k_ao<SOLRT_BVH8_Q8><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
         else if (kind == SOLRT_BVH4_Q8) k_ao<SOLRT_BVH4_Q8><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
+        else if (kind == SOLRT_BVH8_F32) k_ao<SOLRT_BVH8_F32><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
         else k_ao<SOLRT_BVH2><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
     }
     ++ctx.launches;
@@ -865,6 +869,8 @@ solrt_status render_frame(Context& ctx, const Scene& sc, const solrt_camera& cam
         k_megakernel<SOLRT_BVH8_Q8><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(b.d_jobs.as<DevJob>(), ctx.stats.as<DevStats>());
     else if (b.kind == SOLRT_BVH4_Q8)
         k_megakernel<SOLRT_BVH4_Q8><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(b.d_jobs.as<DevJob>(), ctx.stats.as<DevStats>());
+    else if (b.kind == SOLRT_BVH8_F32)
+        k_megakernel<SOLRT_BVH8_F32><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(b.d_jobs.as<DevJob>(), ctx.stats.as<DevStats>());
     else
         k_megakernel<SOLRT_BVH2><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(b.d_jobs.as<DevJob>(), ctx.stats.as<DevStats>());
     k_finalize<<<cdiv(npix, 256), 256, 0, ctx.stream>>>(b.d_jobs.as<DevJob>(), b.d_job_pix.as<uint32_t>(), 1u, npix);

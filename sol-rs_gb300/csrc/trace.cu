@@ -95,8 +95,10 @@ __global__ void __launch_bounds__(kBlock, SOLRT_EXTEND_MINB) k_extend(IO io, con
         extend_bvh2_ww<IO, kCount, kBlock, kSmem>(io, n, work, cnt, ef);
     } else if constexpr (KIND == SOLRT_BVH4_Q8) {
         extend_bvh4_ww<IO, kCount, kBlock, kSmem>(io, n, work, cnt, ef);
+    } else if constexpr (KIND == SOLRT_BVH8_F32) {
+        extend_bvh8_ww<IO, kCount, true>(io, n, work, cnt, ef);
     } else {
-        extend_bvh8_ww<IO, kCount>(io, n, work, cnt, ef);
+        extend_bvh8_ww<IO, kCount, false>(io, n, work, cnt, ef);
     }
     flush_counters(stats, cnt, ef, kCount);
 }
@@ -119,7 +121,7 @@ void launch_variant(const Context& ctx, const IO& io, const unsigned int* count,
 template <int KIND, class IO>
 solrt_status launch_tuned(const Context& ctx, const IO& io, const unsigned int* count, uint32_t n_static,
                           uint32_t n_cap, unsigned int* work, DevStats* st) {
-    constexpr int S = KIND == SOLRT_BVH8_Q8 ? 0 : 1;  // BVH8 keeps its stack in local memory
+    constexpr int S = (KIND == SOLRT_BVH8_Q8 || KIND == SOLRT_BVH8_F32) ? 0 : 1;  // BVH8: local-memory stack
     if (ctx.counters) {
         launch_variant<KIND, IO, true, kExtendBlock, S * SOLRT_SMEM_STACK>(ctx, io, count, n_static, n_cap, work, st);
         return SOLRT_OK;
@@ -153,6 +155,7 @@ solrt_status launch_extend(Context& ctx, uint32_t kind, const DevJob* jobs, cons
     DevStats* st = ctx.stats.as<DevStats>();
     if (kind == SOLRT_BVH8_Q8) SOLRT_TRY((launch_tuned<SOLRT_BVH8_Q8>(ctx, io, count, 0, 0, work, st)));
     else if (kind == SOLRT_BVH4_Q8) SOLRT_TRY((launch_tuned<SOLRT_BVH4_Q8>(ctx, io, count, 0, 0, work, st)));
+    else if (kind == SOLRT_BVH8_F32) SOLRT_TRY((launch_tuned<SOLRT_BVH8_F32>(ctx, io, count, 0, 0, work, st)));
     else SOLRT_TRY((launch_tuned<SOLRT_BVH2>(ctx, io, count, 0, 0, work, st)));
     ++ctx.launches;
     SOLRT_CUDA(cudaGetLastError());
@@ -168,6 +171,7 @@ solrt_status launch_trace_rays(Context& ctx, const Scene& sc, const solrt_ray* r
     DevStats* st = ctx.stats.as<DevStats>();
     if (d.bvh_kind == SOLRT_BVH8_Q8) SOLRT_TRY((launch_tuned<SOLRT_BVH8_Q8>(ctx, io, nullptr, n, n, work, st)));
     else if (d.bvh_kind == SOLRT_BVH4_Q8) SOLRT_TRY((launch_tuned<SOLRT_BVH4_Q8>(ctx, io, nullptr, n, n, work, st)));
+    else if (d.bvh_kind == SOLRT_BVH8_F32) SOLRT_TRY((launch_tuned<SOLRT_BVH8_F32>(ctx, io, nullptr, n, n, work, st)));
     else SOLRT_TRY((launch_tuned<SOLRT_BVH2>(ctx, io, nullptr, n, n, work, st)));
     ++ctx.launches;
     SOLRT_CUDA(cudaGetLastError());

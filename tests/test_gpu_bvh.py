@@ -99,18 +99,31 @@ def _decode_bvh4(nodes_u8):
     return dict(child_base=w[:, 4], tri_base=w[:, 5], imask=imask, meta=meta, lo=lo, hi=hi)
 
 
-@pytest.mark.parametrize("width", [8, 4])
+def _decode_bvh8f(nodes_u8):
+    """224-byte full-precision 8-wide nodes: child_base, tri_base, meta[8],
+    imask, 3 pad words; then per axis lo[8], hi[8] (float32)."""
+    w = nodes_u8.view(np.uint32).reshape(-1, 56)
+    f = nodes_u8.view(np.float32).reshape(-1, 56).astype(np.float64)
+    planes = f[:, 8:].reshape(-1, 3, 2, 8)                              # node, axis, lo/hi, slot
+    meta = np.stack([w[:, 2], w[:, 3]], 1).copy().view(np.uint8).reshape(-1, 8)
+    return dict(child_base=w[:, 0], tri_base=w[:, 1], imask=w[:, 4], meta=meta,
+                lo=planes[:, :, 0, :].transpose(0, 2, 1), hi=planes[:, :, 1, :].transpose(0, 2, 1))
+
+
+@pytest.mark.parametrize("width", [8, 4, "8f"])
 @pytest.mark.parametrize("maker", [lambda: S.cornell(), lambda: S.soup(40000, seed=3),
                                    lambda: S.tunnel(n_ang=128, n_ax=64, length=20.0), lambda: single_triangle()])
 def test_wide_bvh_conservative_and_complete(solrt, ctx, maker, width):
     """Every triangle is referenced by exactly one leaf slot and lies inside
     the decoded (quantised) box of that slot and of every ancestor slot."""
     d = maker()
-    sc = solrt.SceneDescription(ctx, d, bvh=solrt.BVH8_Q8 if width == 8 else solrt.BVH4_Q8)
+    kind = {8: solrt.BVH8_Q8, 4: solrt.BVH4_Q8, "8f": solrt.BVH8_F32}[width]
+    sc = solrt.SceneDescription(ctx, d, bvh=kind)
     nodes, tris = sc.bvh_export()
     info = sc.bvh_info()
     n = info.tri_count
-    dec = _decode_bvh8(nodes) if width == 8 else _decode_bvh4(nodes)
+    dec = {8: _decode_bvh8, 4: _decode_bvh4, "8f": _decode_bvh8f}[width](nodes)
+    width = 4 if width == 4 else 8
     tv = tris.view(np.float32).reshape(-1, 3, 4)[:, :, :3].astype(np.float64)
     prim = tris.view(np.uint32).reshape(-1, 12)[:, 3]
     assert np.array_equal(np.sort(prim), np.arange(n))

@@ -78,7 +78,7 @@ def _render_both(solrt, oracle, ctx, data, w, h, kw, frames=2, bvh=None):
     return ga, g8, acc, rgba_o, stats, seg_o
 
 
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh4", "bvh8"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh4", "bvh8", "bvh8f"])
 @pytest.mark.parametrize("name", ["cornell_lambert", "cornell_ref_stream", "cornell_ref_sky", "transformed",
                                   "soup_gradient", "tunnel_kahan"])
 def test_render_bit_exact(solrt, oracle, ctx, name, bvh):
@@ -93,7 +93,7 @@ def test_render_bit_exact(solrt, oracle, ctx, name, bvh):
     assert np.isfinite(ga).all() and ga[..., :3].mean() > 0
 
 
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh4", "bvh8"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh4", "bvh8", "bvh8f"])
 @pytest.mark.parametrize("name", ["cornell_lambert", "cornell_ref_stream", "soup_gradient", "tunnel_kahan"])
 def test_megakernel_equals_wavefront(solrt, oracle, ctx, name, bvh):
     """The per-pixel megakernel (the reference's loop structure) renders the
