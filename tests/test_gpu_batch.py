@@ -140,7 +140,7 @@ def test_autotune_keeps_images(solrt, bvh):
     r = b.autotune()
     for _, img, _, _ in jobs:   # KAHAN images summed every tuning launch
         img.clear()
-    assert r["candidates"] >= (5 if bvh == "bvh8" else 8)
+    assert r["candidates"] >= (5 if bvh in ("bvh8", "bvh8f") else 8)   # 8-wide: no shared stack
     assert r["block_size"] in (64, 128, 256) and r["smem_stack"] in (16, 32)
     assert r["best_ms"] > 0 and r["best_ms"] <= r["initial_ms"] * 1.05
     assert c.get_tune() == {k: r[k] for k in ("block_size", "smem_stack", "pass_paths")}
