@@ -40,7 +40,7 @@ sys.path.insert(0, ROOT)
 METRIC = "Mrays/s at RMSE≤1e-3 vs FP64 oracle, batched vs plain on 1 GB300; p99 job latency"
 UNIT = "Mrays/s"
 
-NODE_BYTES = {0: 64, 1: 80, 2: 64, 3: 224}
+NODE_BYTES = {0: 64, 1: 80, 2: 64, 3: 224, 4: 32}
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per traced segment
 # of the BVH2 extend kernel on the default soup workload, from one ncu
 # capture of the last 15 k_extend launches of a timed frame (3 of its 4
@@ -204,7 +204,8 @@ def cpu_baseline(data, kw, cam, budget_s=10.0, threads=0):
 
 
 def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, main_tris, n_rays=1 << 22):
-    """8-bit quantised 4- and 8-wide BVHs vs the FP32 binary BVH on the same scene:
+    """The 16-bit quantised binary BVH, the 8-bit quantised 4- and 8-wide BVHs
+    and the FP32 8-wide BVH vs the FP32 binary BVH on the same scene:
     hit records of 4M rays (every camera ray of the frame's first sample
     positions plus seeded rays from inside the scene) compared bit for bit on
     the device, node bytes, visits per segment, Mrays/s of one 64-spp frame
@@ -237,9 +238,9 @@ def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, mai
     out = {"rays_compared": n_rays, "leaf_max": 1}
     hits = {}
     with solrt.Context(local, enable_timing=True) as ctx, solrt.Context(local, enable_counters=True) as cctx:
-        for name, kind in (("bvh2_fp32", solrt.BVH2), ("bvh4_q8", solrt.BVH4_Q8), ("bvh8_q8", solrt.BVH8_Q8),
-                           ("bvh8_fp32", solrt.BVH8_F32)):
-            sc = solrt.SceneDescription(ctx, data, bvh=kind, leaf_max=0 if kind == solrt.BVH2 else 1)
+        for name, kind in (("bvh2_fp32", solrt.BVH2), ("bvh2_q16", solrt.BVH2_Q16), ("bvh4_q8", solrt.BVH4_Q8),
+                           ("bvh8_q8", solrt.BVH8_Q8), ("bvh8_fp32", solrt.BVH8_F32)):
+            sc = solrt.SceneDescription(ctx, data, bvh=kind, leaf_max=0 if kind in (solrt.BVH2, solrt.BVH2_Q16) else 1)
             info = sc.bvh_info()
             h = torch.zeros((n_rays, 4), dtype=torch.float32, device=dev)
             ctx.reset_stats()
@@ -247,7 +248,7 @@ def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, mai
             ctx.synchronize()
             fb_trace = ctx.stats().fp64_fallbacks
             hits[name] = h
-            if kind == solrt.BVH2:
+            if kind == main_info.kind:
                 mr, nodes, tris = main_mrays, main_nodes, main_tris
             else:
                 img = solrt.Image(ctx, W, H, kw["accum_mode"])
@@ -260,7 +261,7 @@ def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, mai
                 st = ctx.stats()
                 mr = st.segments / (st.render_ms / 1000.0) / 1e6 if st.render_ms > 0 else None
                 img.close()
-                csc = solrt.SceneDescription(cctx, data, bvh=kind, leaf_max=1)
+                csc = solrt.SceneDescription(cctx, data, bvh=kind, leaf_max=0 if kind in (solrt.BVH2, solrt.BVH2_Q16) else 1)
                 cimg = solrt.Image(cctx, W, H, kw["accum_mode"])
                 cctx.reset_stats()
                 solrt.Renderer(cctx).cmd_trace_rays(csc, cam, solrt.render_params(**dict(kw, spp=min(4, kw["spp"]))),
@@ -280,7 +281,7 @@ def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, mai
             sc.close()
     a = hits["bvh2_fp32"].view(torch.int32)
     out["hit_mismatches"] = {k: int((a != hits[k].view(torch.int32)).any(dim=1).sum().item())
-                             for k in ("bvh4_q8", "bvh8_q8", "bvh8_fp32")}
+                             for k in ("bvh2_q16", "bvh4_q8", "bvh8_q8", "bvh8_fp32")}
     # hits within about one float ulp of a triangle edge (a barycentric below
     # 2^-23), counted separately: the watertight test and the lower-index tie
     # rule make even these agree across BVHs
@@ -290,7 +291,7 @@ def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, mai
     edge = hit & (torch.minimum(torch.minimum(u, v), 1.0 - u - v) < 2.0 ** -23)
     out["near_edge_hits"] = int(edge.sum().item())
     out["near_edge_mismatches"] = {k: int(((a != hits[k].view(torch.int32)).any(dim=1) & edge).sum().item())
-                                   for k in ("bvh4_q8", "bvh8_q8", "bvh8_fp32")}
+                                   for k in ("bvh2_q16", "bvh4_q8", "bvh8_q8", "bvh8_fp32")}
     out["hits"] = int((a[:, 1] != -1).sum().item())
     return out
 
@@ -303,7 +304,8 @@ def run_batch(args, world, rank, local, pg, njobs=None, steps=None, emit=True):
     import torch
     solrt = importlib.import_module("sol-rs_gb300")
     S = solrt.scenes
-    bvh = {"bvh2": solrt.BVH2, "bvh4": solrt.BVH4_Q8, "bvh8": solrt.BVH8_Q8, "bvh8f": solrt.BVH8_F32}[args.bvh]
+    bvh = {"bvh2": solrt.BVH2, "bvh2q": solrt.BVH2_Q16, "bvh4": solrt.BVH4_Q8, "bvh8": solrt.BVH8_Q8,
+           "bvh8f": solrt.BVH8_F32}[args.bvh]
     njobs = args.jobs if njobs is None else njobs
     steps = args.steps if steps is None else steps
     ctx = solrt.Context(local)
@@ -521,7 +523,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="solrt", choices=["solrt", "reference"])
     ap.add_argument("--workload", default="soup", choices=["soup", "cornell", "tunnel", "batch", "serve"])
-    ap.add_argument("--bvh", default="bvh2", choices=["bvh2", "bvh4", "bvh8", "bvh8f"])
+    ap.add_argument("--bvh", default="bvh2", choices=["bvh2", "bvh2q", "bvh4", "bvh8", "bvh8f"])
     ap.add_argument("--jobs", type=int, default=256)
     ap.add_argument("--rate", type=float, default=6.0, help="serve: Poisson arrival rate, jobs/s")
     ap.add_argument("--duration", type=float, default=8.0, help="serve: arrival window, s")
@@ -558,7 +560,8 @@ def main():
         if getattr(args, key):
             kw[key] = getattr(args, key)
             cfg = dict(cfg, **{key: getattr(args, key)}, reduced=True)
-    bvh = {"bvh2": solrt.BVH2, "bvh4": solrt.BVH4_Q8, "bvh8": solrt.BVH8_Q8, "bvh8f": solrt.BVH8_F32}[args.bvh]
+    bvh = {"bvh2": solrt.BVH2, "bvh2q": solrt.BVH2_Q16, "bvh4": solrt.BVH4_Q8, "bvh8": solrt.BVH8_Q8,
+           "bvh8f": solrt.BVH8_F32}[args.bvh]
     c = data.camera
     cam = solrt.camera_look_at(c["eye"], c["center"], c["up"], c["vfov"], kw["width"] / kw["height"])
     params = solrt.render_params(**kw)

@@ -115,8 +115,10 @@ typedef enum solrt_bvh_kind {
     SOLRT_BVH2 = 0,     /* binary LBVH, FP32 child boxes, 64 B nodes */
     SOLRT_BVH8_Q8 = 1,  /* 8-wide, 8-bit quantised child boxes, 80 B nodes */
     SOLRT_BVH4_Q8 = 2,  /* 4-wide, 8-bit quantised child boxes, 64 B nodes */
-    SOLRT_BVH8_F32 = 3  /* 8-wide, FP32 child boxes, 224 B nodes (the unquantised
+    SOLRT_BVH8_F32 = 3, /* 8-wide, FP32 child boxes, 224 B nodes (the unquantised
                            reference point of SOLRT_BVH8_Q8) */
+    SOLRT_BVH2_Q16 = 4  /* binary LBVH, child boxes as 16-bit planes of one
+                           per-scene grid, 32 B nodes (same hits as SOLRT_BVH2) */
 } solrt_bvh_kind;
 
 /* solrt_bvh_desc.flags */

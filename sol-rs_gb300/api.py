@@ -21,7 +21,7 @@ NO_HIT = 0xFFFFFFFF
 # enums (solrt.h)
 (OK, ERR_INVALID, ERR_OOM, ERR_DEVICE, ERR_TIMEOUT, ERR_CAPACITY, ERR_NOT_READY, ERR_NOT_FOUND, ERR_BUDGET,
  ERR_CANCELLED) = range(10)
-BVH2, BVH8_Q8, BVH4_Q8, BVH8_F32 = 0, 1, 2, 3
+BVH2, BVH8_Q8, BVH4_Q8, BVH8_F32, BVH2_Q16 = 0, 1, 2, 3, 4
 MISS_BLACK, MISS_REF_SKY, MISS_GRADIENT = 0, 1, 2
 MATERIAL_REF, MATERIAL_LAMBERT = 0, 1
 ACCUM_REF_MIX, ACCUM_KAHAN = 0, 1

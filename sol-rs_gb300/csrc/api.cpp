@@ -456,7 +456,7 @@ solrt_status solrt_scene_destroy(solrt_scene* scene) {
 
 solrt_status solrt_scene_build_bvh(solrt_scene* scene, const solrt_bvh_desc* bvh) {
     CHECK_ARG(scene && bvh, "null argument");
-    CHECK_ARG(bvh->kind <= SOLRT_BVH8_F32, "unknown BVH kind");
+    CHECK_ARG(bvh->kind <= SOLRT_BVH2_Q16, "unknown BVH kind");
     CHECK_ARG(bvh->leaf_max <= 3, "leaf_max must be 0..3");
     SOLRT_CUDA(cudaSetDevice(scene->ctx->device));
     return build_bvh(*scene->ctx, *scene, *bvh);

@@ -73,7 +73,46 @@ struct Bvh2Stack<kBlock, 0> {
     SOLRT_D int get(int k) const { return lo[k]; }
 };
 
-template <class IO, bool kCount, int kBlock, int kSmem>
+// One node test in either node format (kQ16: 32-byte
+// BVH2-q16 nodes, one 256-bit load; else 64-byte FP32 nodes, two).
+template <bool kQ16>
+SOLRT_D void bvh2_node_step(const float4* nodes, int node, float ix, float iy, float iz, float nox, float noy,
+                            float noz, float tmin, float tmax, bool& h0, float& t0, bool& h1, float& t1, int& ref0,
+                            int& ref1) {
+    if constexpr (kQ16) {
+        float4 a, b;
+        ldg_2x4(nodes + 2 + 2 * (size_t)node, a, b);
+        slab2_q16(a, b, ix, iy, iz, nox, noy, noz, tmin, tmax, h0, t0, h1, t1);
+        ref0 = __float_as_int(a.x);
+        ref1 = __float_as_int(a.y);
+    } else {
+        float4 n0, n1, n2;
+        int4 n3;
+        load_bvh2_node(nodes, node, n0, n1, n2, n3);
+        slab2_fma(n0, n1, n2, ix, iy, iz, nox, noy, noz, tmin, tmax, h0, t0, h1, t1);
+        ref0 = n3.x;
+        ref1 = n3.y;
+    }
+}
+
+// Per-ray constants of the slab test: (1/d, -o/d) per axis for FP32 nodes,
+// (c/d, (G - o)/d - 2^23 c/d) for BVH2-q16 nodes (q16_ray).
+template <bool kQ16>
+SOLRT_D void bvh2_ray_consts(const float4* nodes, float ox, float oy, float oz, float dx, float dy, float dz,
+                             float& ix, float& iy, float& iz, float& nox, float& noy, float& noz) {
+    if constexpr (kQ16) {
+        q16_ray(nodes, ox, oy, oz, dx, dy, dz, ix, iy, iz, nox, noy, noz);
+    } else {
+        ix = 1.0f / box_dir(dx);
+        iy = 1.0f / box_dir(dy);
+        iz = 1.0f / box_dir(dz);
+        nox = -(ox * ix);
+        noy = -(oy * iy);
+        noz = -(oz * iz);
+    }
+}
+
+template <class IO, bool kCount, int kBlock, int kSmem, bool kQ16 = false>
 SOLRT_D void extend_bvh2_ww(const IO& io, uint32_t n, unsigned int* work, TraceCounters& cnt, uint32_t& ef) {
     const int lane = threadIdx.x & 31;
     const uint32_t lane_lt = (1u << lane) - 1u;
@@ -112,12 +151,8 @@ SOLRT_D void extend_bvh2_ww(const IO& io, uint32_t n, unsigned int* work, TraceC
                     idx = i;
                     has = true;
                     r = setup_ray(o.x, o.y, o.z, d.x, d.y, d.z, o.w);
-                    ix = 1.0f / box_dir(d.x);
-                    iy = 1.0f / box_dir(d.y);
-                    iz = 1.0f / box_dir(d.z);
-                    nox = -(o.x * ix);
-                    noy = -(o.y * iy);
-                    noz = -(o.z * iz);
+                    if (ts.tri_count)
+                        bvh2_ray_consts<kQ16>(ts.nodes, o.x, o.y, o.z, d.x, d.y, d.z, ix, iy, iz, nox, noy, noz);
                     best = HitRec{d.w, SOLRT_NO_HIT, 0.0f, 0.0f};
                     budget = 2u * (ts.node_count + ts.tri_count) + 64u;
                     stack.put(0, kBvh2Sentinel);
@@ -148,22 +183,21 @@ SOLRT_D void extend_bvh2_ww(const IO& io, uint32_t n, unsigned int* work, TraceC
                     node = kBvh2Sentinel;
                     leaf = 0;
                 } else {
-                    float4 n0, n1, n2;
-                    int4 n3;
-                    load_bvh2_node(ts.nodes, node, n0, n1, n2, n3);
                     if (kCount) ++cnt.nodes;
                     float t0, t1;
                     bool h0, h1;
-                    slab2_fma(n0, n1, n2, ix, iy, iz, nox, noy, noz, r.tmin, best.t, h0, t0, h1, t1);
+                    int c0, c1;
+                    bvh2_node_step<kQ16>(ts.nodes, node, ix, iy, iz, nox, noy, noz, r.tmin, best.t, h0, t0, h1, t1,
+                                         c0, c1);
                     if (h0 && h1) {
                         const bool swap = t1 < t0;
-                        if (sp <= SOLRT_BVH2_STACK) stack.put(sp++, swap ? n3.x : n3.y);
+                        if (sp <= SOLRT_BVH2_STACK) stack.put(sp++, swap ? c0 : c1);
                         else ef |= SOLRT_EFLAG_STACK;
-                        node = swap ? n3.y : n3.x;
+                        node = swap ? c1 : c0;
                     } else if (h0) {
-                        node = n3.x;
+                        node = c0;
                     } else if (h1) {
-                        node = n3.y;
+                        node = c1;
                     } else {
                         node = stack.get(--sp);
                     }
@@ -196,13 +230,14 @@ SOLRT_D void extend_bvh2_ww(const IO& io, uint32_t n, unsigned int* work, TraceC
 
 // One ray, plain depth-first loop (nearer child first): the traversal of the
 // per-pixel megakernel.
+template <bool kQ16 = false>
 SOLRT_D void trace_bvh2_ray(const TravScene& ts, float ox, float oy, float oz, float dx, float dy, float dz,
                             float tmin, float tmax, HitRec& best, TraceCounters& cnt, uint32_t& ef) {
     best = HitRec{tmax, SOLRT_NO_HIT, 0.0f, 0.0f};
     if (ts.tri_count == 0) return;
     const RayWT r = setup_ray(ox, oy, oz, dx, dy, dz, tmin);
-    const float ix = 1.0f / box_dir(dx), iy = 1.0f / box_dir(dy), iz = 1.0f / box_dir(dz);
-    const float nox = -(ox * ix), noy = -(oy * iy), noz = -(oz * iz);
+    float ix, iy, iz, nox, noy, noz;
+    bvh2_ray_consts<kQ16>(ts.nodes, ox, oy, oz, dx, dy, dz, ix, iy, iz, nox, noy, noz);
     int stack[SOLRT_BVH2_STACK + 1];
     stack[0] = kBvh2Sentinel;
     int sp = 1;
@@ -218,21 +253,19 @@ SOLRT_D void trace_bvh2_ray(const TravScene& ts, float ox, float oy, float oz, f
                 ef |= SOLRT_EFLAG_INDEX;
                 return;
             }
-            float4 n0, n1, n2;
-            int4 n3;
-            load_bvh2_node(ts.nodes, node, n0, n1, n2, n3);
             float t0, t1;
             bool h0, h1;
-            slab2_fma(n0, n1, n2, ix, iy, iz, nox, noy, noz, tmin, best.t, h0, t0, h1, t1);
+            int c0, c1;
+            bvh2_node_step<kQ16>(ts.nodes, node, ix, iy, iz, nox, noy, noz, tmin, best.t, h0, t0, h1, t1, c0, c1);
             if (h0 && h1) {
                 const bool swap = t1 < t0;
-                if (sp <= SOLRT_BVH2_STACK) stack[sp++] = swap ? n3.x : n3.y;
+                if (sp <= SOLRT_BVH2_STACK) stack[sp++] = swap ? c0 : c1;
                 else ef |= SOLRT_EFLAG_STACK;
-                node = swap ? n3.y : n3.x;
+                node = swap ? c1 : c0;
                 continue;
             }
-            if (h0) { node = n3.x; continue; }
-            if (h1) { node = n3.y; continue; }
+            if (h0) { node = c0; continue; }
+            if (h1) { node = c1; continue; }
         } else {
             const uint32_t k = (uint32_t)(~node);
             if (k >= ts.tri_count) {

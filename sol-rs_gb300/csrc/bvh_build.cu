@@ -408,6 +408,98 @@ solrt_status check_wide_depth(uint32_t width, uint32_t depth) {
     return SOLRT_OK;
 }
 
+// BVH2-q16 (SOLRT_BVH2_Q16): the BVH2 with every child box stored as 16-bit
+// planes of one grid per scene, a 32-byte node (one 256-bit load) instead of
+// 64 bytes. Layout: a 32-byte header (grid origin G.xyz, cell c.x | c.y,
+// c.z, ok flag, 0) followed by node i at byte 32 (i + 1):
+//   (ref0, ref1, c0.x, c0.y, c0.z, c1.x, c1.y, c1.z)
+// where each axis word packs the low plane in bits 0-15 and the high plane
+// in bits 16-31; plane q of axis a lies at G.a + q c.a.
+//
+// Per axis the cell is the smallest power of two with extent / c <= 60000
+// and c >= 2^-20 max|coordinate| (and 2^-60 <= c <= 2^23); G = floor(lo / c) c
+// - 4 c. Planes are quantised outward from the (already widened) FP32 child
+// boxes with two extra cells: the traversal's t = fma(2^23 + q, c / d,
+// (G - o) / d - 2^23 c / d) differs from the exact plane distance by at most
+// half a cell plus 3 * 2^-24 (|o| + |G|) / |d| plus 2^-24 |t|; the margin covers
+// the first two for ray origins within twice the scene's coordinate range,
+// and the relative 2^-16 widening of the far distance covers the rest (and
+// the case of farther origins, where |t| ~ |o| / |d|).
+__global__ void k_q16_grid(const float4* __restrict__ nbox, float4* __restrict__ header) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    const float4 blo = nbox[0], bhi = nbox[1];
+    const float lo[3] = {blo.x, blo.y, blo.z}, hi[3] = {bhi.x, bhi.y, bhi.z};
+    float g[3], c[3];
+    uint32_t ok = 1u;
+    for (int a = 0; a < 3; ++a) {
+        if (!isfinite(lo[a]) || !isfinite(hi[a]) || lo[a] > hi[a]) {
+            ok = 0u;
+            g[a] = 0.0f;
+            c[a] = 1.0f;
+            continue;
+        }
+        const double ext = (double)hi[a] - (double)lo[a];
+        const double m = fmax(fabs((double)lo[a]), fabs((double)hi[a]));
+        const double need = fmax(fmax(ext / 60000.0, m * 0x1p-20), 0x1p-60);
+        int e = ilogb(need);
+        if (ldexp(1.0, e) < need) ++e;
+        if (e > 23) ok = 0u;
+        const double cd = ldexp(1.0, e);
+        c[a] = (float)cd;
+        g[a] = (float)(floor((double)lo[a] / cd) * cd - 4.0 * cd);
+    }
+    header[0] = make_float4(g[0], g[1], g[2], c[0]);
+    header[1] = make_float4(c[1], c[2], __uint_as_float(ok), 0.0f);
+}
+
+// Grid planes of one child axis: the low plane at least two cells below
+// `lo`, the high plane two cells above `hi` (differences rounded outward,
+// division by the power-of-two cell exact).
+__device__ __forceinline__ uint32_t q16_pair(float lo, float hi, float g, float c) {
+    const double dc = (double)c;
+    const double ql = floor(__dsub_rd((double)lo, (double)g) / dc) - 2.0;
+    const double qh = ceil(__dsub_ru((double)hi, (double)g) / dc) + 2.0;
+    const uint32_t a = (uint32_t)fmin(fmax(ql, 0.0), 65535.0), b = (uint32_t)fmin(fmax(qh, 0.0), 65535.0);
+    return a | (b << 16);
+}
+
+__global__ void k_q16_nodes(const float4* __restrict__ nodes, uint32_t ni, float4* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ni) return;
+    const float4 h0 = out[0], h1 = out[1];
+    const float g[3] = {h0.x, h0.y, h0.z}, c[3] = {h0.w, h1.x, h1.y};
+    const float4 n0 = nodes[4 * (size_t)i], n1 = nodes[4 * (size_t)i + 1], n2 = nodes[4 * (size_t)i + 2],
+                 n3 = nodes[4 * (size_t)i + 3];
+    uint4* o = reinterpret_cast<uint4*>(out + 2 + 2 * (size_t)i);
+    o[0] = make_uint4(__float_as_uint(n3.x), __float_as_uint(n3.y), q16_pair(n0.x, n0.y, g[0], c[0]),
+                      q16_pair(n0.z, n0.w, g[1], c[1]));
+    o[1] = make_uint4(q16_pair(n2.x, n2.y, g[2], c[2]), q16_pair(n1.x, n1.y, g[0], c[0]),
+                      q16_pair(n1.z, n1.w, g[1], c[1]), q16_pair(n2.z, n2.w, g[2], c[2]));
+}
+
+// Replaces the 64-byte BVH2 nodes in `nodes` by the 32-byte BVH2-q16 nodes
+// (header + ni nodes); `nbox` holds the exact internal-node boxes (root
+// first). Fails when a coordinate is not finite or the scene is too large
+// for the grid (synchronises to read the grid's flag).
+solrt_status quantize_bvh2(Context& ctx, DeviceBuffer& nodes, const float4* nbox, uint32_t ni) {
+    cudaStream_t st = ctx.stream;
+    DeviceBuffer q;
+    SOLRT_TRY(q.alloc(32ull * ((size_t)ni + 1)));
+    k_q16_grid<<<1, 32, 0, st>>>(nbox, q.as<float4>());
+    k_q16_nodes<<<blocks_for(ni, 256), 256, 0, st>>>(nodes.as<float4>(), ni, q.as<float4>());
+    ctx.launches += 2;
+    SOLRT_CUDA(cudaGetLastError());
+    uint32_t ok = 0;
+    SOLRT_CUDA(cudaMemcpyAsync(&ok, (const char*)q.ptr + 24, sizeof(ok), cudaMemcpyDeviceToHost, st));
+    SOLRT_CUDA(cudaStreamSynchronize(st));
+    if (ok != 1u) {
+        set_error("BVH2_Q16: scene bounds are not finite or too large for a 16-bit grid (use SOLRT_BVH2)");
+        return SOLRT_ERR_INVALID;
+    }
+    nodes.adopt(q);
+    return SOLRT_OK;
+}
+
 }  // namespace
 
 void launch_scan_exclusive(uint32_t* data, uint32_t len, cudaStream_t stream) {
@@ -530,6 +622,10 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
         bvh2_nodes.bytes = 0;
         sc.info.node_count = ni;
         sc.info.node_bytes = (uint64_t)ni * 64u;
+        if (desc.kind == SOLRT_BVH2_Q16) {
+            SOLRT_TRY(quantize_bvh2(ctx, sc.nodes, nbox.as<float4>(), ni));
+            sc.info.node_bytes = 32ull * ((uint64_t)ni + 1);
+        }
         unsigned int dh = 0;
         SOLRT_CUDA(cudaMemcpyAsync(&dh, depth.ptr, sizeof(dh), cudaMemcpyDeviceToHost, st));
         SOLRT_CUDA(cudaStreamSynchronize(st));
@@ -550,7 +646,7 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
     float ms = 0.0f;
     SOLRT_CUDA(cudaEventElapsedTime(&ms, ctx.ev0, ctx.ev1));
     sc.info.build_ms = ms;
-    if (sc.info.kind == SOLRT_BVH2 && sc.info.depth > SOLRT_BVH2_STACK) {
+    if ((sc.info.kind == SOLRT_BVH2 || sc.info.kind == SOLRT_BVH2_Q16) && sc.info.depth > SOLRT_BVH2_STACK) {
         set_error("BVH2 depth %u exceeds the traversal stack (%d)", sc.info.depth, SOLRT_BVH2_STACK);
         return SOLRT_ERR_CAPACITY;
     }
@@ -603,6 +699,7 @@ solrt_status refit_bvh(Context& ctx, Scene& sc) {
     const bool b8 = sc.info.kind == SOLRT_BVH8_Q8 || sc.info.kind == SOLRT_BVH4_Q8 || sc.info.kind == SOLRT_BVH8_F32;
     const uint32_t width = sc.info.kind == SOLRT_BVH4_Q8 ? 4u : 8u;
     const bool f32 = sc.info.kind == SOLRT_BVH8_F32;
+    const bool q16 = sc.info.kind == SOLRT_BVH2_Q16;
     DeviceBuffer flags, nbox, nodes2, tri2;
     SOLRT_TRY(flags.alloc(sizeof(unsigned int) * (size_t)ni));
     SOLRT_TRY(nbox.alloc(2 * sizeof(float4) * (size_t)ni));
@@ -613,6 +710,9 @@ solrt_status refit_bvh(Context& ctx, Scene& sc) {
         SOLRT_TRY(tri2.alloc(3 * sizeof(float4) * (size_t)n));
         nodes_out = nodes2.as<float4>();
         tri_out = tri2.as<float4>();
+    } else if (q16) {  // FP32 nodes first, quantised below
+        SOLRT_TRY(nodes2.alloc(4 * sizeof(float4) * (size_t)ni));
+        nodes_out = nodes2.as<float4>();
     }
     SOLRT_CUDA(cudaMemsetAsync(flags.ptr, 0, flags.bytes, st));
     k_refit<<<blocks_for(n, 256), 256, 0, st>>>(sc.vpos.as<float4>(), sc.tri_idx.as<uint4>(),
@@ -639,6 +739,9 @@ solrt_status refit_bvh(Context& ctx, Scene& sc) {
         sc.info.depth = depth8;
         sc.info.node_bytes = (uint64_t)node_count * (width == 4 ? 64u : (f32 ? 224u : 80u));
         sc.info.tri_bytes = sc.tri_wt.bytes;
+    } else if (q16) {
+        SOLRT_TRY(quantize_bvh2(ctx, nodes2, nbox.as<float4>(), ni));
+        sc.nodes.adopt(nodes2);
     }
     SOLRT_CUDA(cudaEventRecord(ctx.ev1, st));
     SOLRT_CUDA(cudaEventSynchronize(ctx.ev1));

@@ -92,7 +92,9 @@ __global__ void __launch_bounds__(kBlock, SOLRT_EXTEND_MINB) k_extend(IO io, con
     TraceCounters cnt{0, 0, 0};
     uint32_t ef = 0;
     if constexpr (KIND == SOLRT_BVH2) {
-        extend_bvh2_ww<IO, kCount, kBlock, kSmem>(io, n, work, cnt, ef);
+        extend_bvh2_ww<IO, kCount, kBlock, kSmem, false>(io, n, work, cnt, ef);
+    } else if constexpr (KIND == SOLRT_BVH2_Q16) {
+        extend_bvh2_ww<IO, kCount, kBlock, kSmem, true>(io, n, work, cnt, ef);
     } else if constexpr (KIND == SOLRT_BVH4_Q8) {
         extend_bvh4_ww<IO, kCount, kBlock, kSmem>(io, n, work, cnt, ef);
     } else if constexpr (KIND == SOLRT_BVH8_F32) {
@@ -156,6 +158,7 @@ solrt_status launch_extend(Context& ctx, uint32_t kind, const DevJob* jobs, cons
     if (kind == SOLRT_BVH8_Q8) SOLRT_TRY((launch_tuned<SOLRT_BVH8_Q8>(ctx, io, count, 0, 0, work, st)));
     else if (kind == SOLRT_BVH4_Q8) SOLRT_TRY((launch_tuned<SOLRT_BVH4_Q8>(ctx, io, count, 0, 0, work, st)));
     else if (kind == SOLRT_BVH8_F32) SOLRT_TRY((launch_tuned<SOLRT_BVH8_F32>(ctx, io, count, 0, 0, work, st)));
+    else if (kind == SOLRT_BVH2_Q16) SOLRT_TRY((launch_tuned<SOLRT_BVH2_Q16>(ctx, io, count, 0, 0, work, st)));
     else SOLRT_TRY((launch_tuned<SOLRT_BVH2>(ctx, io, count, 0, 0, work, st)));
     ++ctx.launches;
     SOLRT_CUDA(cudaGetLastError());
@@ -172,6 +175,7 @@ solrt_status launch_trace_rays(Context& ctx, const Scene& sc, const solrt_ray* r
     if (d.bvh_kind == SOLRT_BVH8_Q8) SOLRT_TRY((launch_tuned<SOLRT_BVH8_Q8>(ctx, io, nullptr, n, n, work, st)));
     else if (d.bvh_kind == SOLRT_BVH4_Q8) SOLRT_TRY((launch_tuned<SOLRT_BVH4_Q8>(ctx, io, nullptr, n, n, work, st)));
     else if (d.bvh_kind == SOLRT_BVH8_F32) SOLRT_TRY((launch_tuned<SOLRT_BVH8_F32>(ctx, io, nullptr, n, n, work, st)));
+    else if (d.bvh_kind == SOLRT_BVH2_Q16) SOLRT_TRY((launch_tuned<SOLRT_BVH2_Q16>(ctx, io, nullptr, n, n, work, st)));
     else SOLRT_TRY((launch_tuned<SOLRT_BVH2>(ctx, io, nullptr, n, n, work, st)));
     ++ctx.launches;
     SOLRT_CUDA(cudaGetLastError());

@@ -207,6 +207,53 @@ SOLRT_D void slab2_fma(const float4& n0, const float4& n1, const float4& n2, flo
     h1 = tn1 <= tf1 * 1.0000153f;
 }
 
+// BVH2-q16 nodes (32 B): (ref0, ref1, c0.x, c0.y, c0.z, c1.x, c1.y, c1.z),
+// each axis word holding the child's low plane in bits 0-15 and its high
+// plane in bits 16-31, in units of the scene grid's cell from its origin G
+// (a 32-byte header before node 0: G.xyz, c.x, c.y, c.z). The plane
+// distance is t = fma(2^23 + q, s, a) with per-ray s = c / d and
+// a = (G - o) / d - 2^23 s; 2^23 + q is q placed in the mantissa of 2^23
+// (exact, one byte permute). The build quantises outward with two cells of
+// margin, which covers the rounding of a and s (see the grid rules there).
+// Direction components below 2^-80 are replaced by +-2^-80 for these tests
+// (2^23 s stays finite for cells up to 2^23).
+SOLRT_D float box_dir_q16(float v) { return fabsf(v) < 0x1p-80f ? copysignf(0x1p-80f, v) : v; }
+SOLRT_D float q16_lo(uint32_t w) { return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7410u)); }
+SOLRT_D float q16_hi(uint32_t w) { return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7432u)); }
+
+SOLRT_D void q16_ray(const float4* header, float ox, float oy, float oz, float dx, float dy, float dz, float& sx,
+                     float& sy, float& sz, float& ax, float& ay, float& az) {
+    float4 g0, g1;
+    ldg_2x4(header, g0, g1);
+    const float jx = 1.0f / box_dir_q16(dx), jy = 1.0f / box_dir_q16(dy), jz = 1.0f / box_dir_q16(dz);
+    sx = g0.w * jx;
+    sy = g1.x * jy;
+    sz = g1.y * jz;
+    ax = fmaf(-8388608.0f, sx, fmaf(g0.x, jx, -(ox * jx)));
+    ay = fmaf(-8388608.0f, sy, fmaf(g0.y, jy, -(oy * jy)));
+    az = fmaf(-8388608.0f, sz, fmaf(g0.z, jz, -(oz * jz)));
+}
+
+// Both child boxes of a BVH2-q16 node (a, b: its two halves) against one
+// ray; the outputs of slab2_fma.
+SOLRT_D void slab2_q16(const float4& a, const float4& b, float sx, float sy, float sz, float ax, float ay, float az,
+                       float tmin, float tmax, bool& h0, float& t0, bool& h1, float& t1) {
+    const uint32_t c0x = __float_as_uint(a.z), c0y = __float_as_uint(a.w), c0z = __float_as_uint(b.x);
+    const uint32_t c1x = __float_as_uint(b.y), c1y = __float_as_uint(b.z), c1z = __float_as_uint(b.w);
+    const float2 x0 = fma_x2(q16_lo(c0x), q16_hi(c0x), sx, ax), y0 = fma_x2(q16_lo(c0y), q16_hi(c0y), sy, ay);
+    const float2 z0 = fma_x2(q16_lo(c0z), q16_hi(c0z), sz, az);
+    const float2 x1 = fma_x2(q16_lo(c1x), q16_hi(c1x), sx, ax), y1 = fma_x2(q16_lo(c1y), q16_hi(c1y), sy, ay);
+    const float2 z1 = fma_x2(q16_lo(c1z), q16_hi(c1z), sz, az);
+    const float tn0 = fmaxf(max3(fminf(x0.x, x0.y), fminf(y0.x, y0.y), fminf(z0.x, z0.y)), tmin);
+    const float tf0 = fminf(min3(fmaxf(x0.x, x0.y), fmaxf(y0.x, y0.y), fmaxf(z0.x, z0.y)), tmax);
+    const float tn1 = fmaxf(max3(fminf(x1.x, x1.y), fminf(y1.x, y1.y), fminf(z1.x, z1.y)), tmin);
+    const float tf1 = fminf(min3(fmaxf(x1.x, x1.y), fmaxf(y1.x, y1.y), fmaxf(z1.x, z1.y)), tmax);
+    t0 = tn0;
+    t1 = tn1;
+    h0 = tn0 <= tf0 * 1.0000153f;
+    h1 = tn1 <= tf1 * 1.0000153f;
+}
+
 // Outward widening of a box face by a relative 2^-21 (about 4 ulp) plus an
 // absolute 2^-80 (which matters only near 0).
 SOLRT_HD float widen_lo(float v) { return (v - fabsf(v) * 0x1p-21f) - 0x1p-80f; }

@@ -60,6 +60,52 @@ def test_bvh2_topology_bit_exact(solrt, oracle, ctx, maker):
     assert info.tri_count == n and info.node_count == n - 1 and info.depth >= np.log2(n)
 
 
+def _decode_bvh2_q16(nodes_u8):
+    """Header (G.xyz, c.xyz) + 32-byte nodes: refs, then per child x, y, z
+    words of (low | high << 16) grid planes. Boxes as lo xyz, hi xyz (FP64)."""
+    hdr = nodes_u8[:32].view(np.float32).astype(np.float64)
+    g, c = hdr[0:3], hdr[3:6]
+    w = nodes_u8[32:].view(np.uint32).reshape(-1, 8)
+    refs = w[:, 0:2].view(np.int32)
+
+    def box(words):
+        lo = (words & 0xFFFF).astype(np.float64)
+        hi = (words >> 16).astype(np.float64)
+        return np.concatenate([g + lo * c, g + hi * c], 1)
+
+    return g, c, refs, box(w[:, 2:5]), box(w[:, 5:8])
+
+
+@pytest.mark.parametrize("maker", [lambda: S.cornell(), lambda: S.soup(50000, seed=2),
+                                   lambda: S.tunnel(n_ang=128, n_ax=64, length=20.0), lambda: single_triangle()])
+def test_bvh2_q16_conservative(solrt, ctx, maker):
+    """BVH2-q16 nodes hold the FP32 BVH2's topology, and every quantised child
+    box contains the FP32 (widened) child box with two to three cells of
+    margin per face; the grid cell is a power of two with the scene's extent
+    within 60000 cells."""
+    d = maker()
+    f = solrt.SceneDescription(ctx, d, bvh=solrt.BVH2)
+    q = solrt.SceneDescription(ctx, d, bvh=solrt.BVH2_Q16)
+    nf, tf = f.bvh_export()
+    nq, tq = q.bvh_export()
+    assert np.array_equal(tf, tq)
+    assert q.bvh_info().node_count == f.bvh_info().node_count
+    assert len(nq) == 32 * (q.bvh_info().node_count + 1)
+    refs, c0, c1 = _decode_bvh2(nf)
+    g, c, qrefs, q0, q1 = _decode_bvh2_q16(nq)
+    assert np.array_equal(qrefs, refs)
+    assert np.all(np.log2(c) == np.round(np.log2(c)))
+    assert np.all(np.mod(g, c) == 0)
+    for fb, qb in ((c0, q0), (c1, q1)):
+        fb = fb.astype(np.float64)
+        assert np.all(qb[:, :3] <= fb[:, :3] - 2 * c) and np.all(qb[:, 3:] >= fb[:, 3:] + 2 * c)
+        slack = 3.0001 * c   # three cells, plus the outward rounding of lo - G / hi - G
+        assert np.all(qb[:, :3] >= fb[:, :3] - slack) and np.all(qb[:, 3:] <= fb[:, 3:] + slack)
+    lo = np.minimum(c0[:, :3].min(0), c1[:, :3].min(0)).astype(np.float64)
+    hi = np.maximum(c0[:, 3:].max(0), c1[:, 3:].max(0)).astype(np.float64)
+    assert np.all((hi - lo) / c <= 60001)
+
+
 def _decode_bvh8(nodes_u8):
     w = nodes_u8.view(np.uint32).reshape(-1, 20)
     p = w[:, 0:3].copy().view(np.float32).astype(np.float64)

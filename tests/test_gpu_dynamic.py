@@ -41,7 +41,7 @@ def _render(solrt, ctx, sc, cam, w, h, p):
 
 
 @pytest.mark.parametrize("mode", ["rebuild", "refit"])
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh4", "bvh8", "bvh8f"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh4", "bvh8", "bvh8f"])
 def test_regenerate_matches_fresh_scene(solrt, oracle, ctx, bvh, mode):
     kind = bvh_kind(solrt, bvh)
     regen = solrt.REGEN_REBUILD if mode == "rebuild" else solrt.REGEN_REFIT

@@ -25,7 +25,7 @@ def _transformed_glb(solrt, path):
     return solrt.load_scene(str(path))
 
 
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh4", "bvh8", "bvh8f"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh4", "bvh8", "bvh8f"])
 def test_gltf_render_matches_oracle(solrt, oracle, ctx, tmp_path, bvh):
     g = _transformed_glb(solrt, tmp_path / "cornell.glb")
     w, h = 40, 32

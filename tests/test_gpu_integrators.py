@@ -15,7 +15,7 @@ def blue_noise(h=64, w=48, seed=17):
     return np.random.default_rng(seed).integers(0, 256, (h, w, 4), dtype=np.uint8)
 
 
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh4", "bvh8", "bvh8f"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh4", "bvh8", "bvh8f"])
 @pytest.mark.parametrize("scene", ["cornell", "transformed", "soup"])
 def test_debug_matches_oracle(solrt, oracle, ctx, bvh, scene):
     data = {"cornell": S.cornell, "transformed": transformed_cornell, "soup": lambda: S.soup(20000, seed=3)}[scene]()
@@ -37,7 +37,7 @@ def test_debug_matches_oracle(solrt, oracle, ctx, bvh, scene):
     assert hit.any()
 
 
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh4", "bvh8", "bvh8f"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh4", "bvh8", "bvh8f"])
 def test_ao_matches_oracle(solrt, oracle, ctx, bvh):
     data = S.cornell()
     w, h = 40, 32

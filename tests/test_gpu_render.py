@@ -78,7 +78,7 @@ def _render_both(solrt, oracle, ctx, data, w, h, kw, frames=2, bvh=None):
     return ga, g8, acc, rgba_o, stats, seg_o
 
 
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh4", "bvh8", "bvh8f"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh4", "bvh8", "bvh8f"])
 @pytest.mark.parametrize("name", ["cornell_lambert", "cornell_ref_stream", "cornell_ref_sky", "transformed",
                                   "soup_gradient", "tunnel_kahan"])
 def test_render_bit_exact(solrt, oracle, ctx, name, bvh):
@@ -93,7 +93,7 @@ def test_render_bit_exact(solrt, oracle, ctx, name, bvh):
     assert np.isfinite(ga).all() and ga[..., :3].mean() > 0
 
 
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh4", "bvh8", "bvh8f"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh4", "bvh8", "bvh8f"])
 @pytest.mark.parametrize("name", ["cornell_lambert", "cornell_ref_stream", "soup_gradient", "tunnel_kahan"])
 def test_megakernel_equals_wavefront(solrt, oracle, ctx, name, bvh):
     """The per-pixel megakernel (the reference's loop structure) renders the
@@ -104,6 +104,43 @@ def test_megakernel_equals_wavefront(solrt, oracle, ctx, name, bvh):
                                                 bvh=kind)
     assert np.array_equal(ga.view(np.uint32), oa.view(np.uint32))
     assert stats.segments == seg_o and stats.error_flags == 0
+
+
+@pytest.mark.parametrize("name", ["cornell_lambert", "soup_gradient", "tunnel_kahan"])
+def test_visit_counters_vs_oracle(solrt, oracle, name):
+    """The device counters of node visits and triangle tests (the N_node and
+    N_tri of the roofline's algorithmic bytes) against the oracle's CPU
+    traversal of the same binary LBVH on the same paths: the warp-organised
+    kernel visits what the per-ray loop visits, plus the speculative visits
+    of lanes that hold a leaf (and widened boxes), within a few percent."""
+    data, w, h, kw = _case(name)
+    c = solrt.Context(0, enable_counters=True)
+    sc = solrt.SceneDescription(c, data, bvh=solrt.BVH2)
+    cam = camera_of(data, w / h)
+    mode = kw.get("accum_mode", solrt.ACCUM_REF_MIX)
+    img = solrt.Image(c, w, h, mode)
+    o = oracle.OracleScene(data)
+    acc = np.zeros((h, w, 4), np.float32)
+    ks = np.zeros((h, w, 4), np.float32) if mode == solrt.ACCUM_KAHAN else None
+    kc = np.zeros((h, w, 4), np.float32) if mode == solrt.ACCUM_KAHAN else None
+    seg = nv = nt = 0
+    c.reset_stats()
+    for f in range(2):
+        p = solrt.render_params(w, h, frame=f, **kw)
+        solrt.Renderer(c).cmd_trace_rays(sc, cam, p, img)
+        acc, _, st = o.render(cam, p, accum=acc, ksum=ks, kcomp=kc)
+        seg += st.segments
+        nv += st.node_visits
+        nt += st.tri_tests
+    c.synchronize()
+    g = c.stats()
+    assert g.segments == seg and g.error_flags == 0
+    assert nv > 0 and nt > 0
+    assert 0.999 * nv <= g.node_visits <= 1.10 * nv, (g.node_visits, nv)
+    assert 0.999 * nt <= g.tri_tests <= 1.10 * nt, (g.tri_tests, nt)
+    img.close()
+    sc.close()
+    c.close()
 
 
 def test_pass_splitting_invariance(solrt, oracle):

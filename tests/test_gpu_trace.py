@@ -18,7 +18,7 @@ def _both(solrt, oracle, ctx, data, rays, bvh):
     return g, ref
 
 
-BVHS = ["bvh2", "bvh4", "bvh8", "bvh8f"]
+BVHS = ["bvh2", "bvh2q", "bvh4", "bvh8", "bvh8f"]
 
 
 def _kind(solrt, name):
