@@ -238,9 +238,11 @@ def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, mai
     out = {"rays_compared": n_rays, "leaf_max": 1}
     hits = {}
     with solrt.Context(local, enable_timing=True) as ctx, solrt.Context(local, enable_counters=True) as cctx:
-        for name, kind in (("bvh2_fp32", solrt.BVH2), ("bvh2_q16", solrt.BVH2_Q16), ("bvh4_q8", solrt.BVH4_Q8),
-                           ("bvh8_q8", solrt.BVH8_Q8), ("bvh8_fp32", solrt.BVH8_F32)):
-            sc = solrt.SceneDescription(ctx, data, bvh=kind, leaf_max=0 if kind in (solrt.BVH2, solrt.BVH2_Q16) else 1)
+        for name, kind, sah in (("bvh2_fp32", solrt.BVH2, False), ("bvh2_q16", solrt.BVH2_Q16, False),
+                                ("bvh4_q8", solrt.BVH4_Q8, False), ("bvh8_q8", solrt.BVH8_Q8, False),
+                                ("bvh8_q8_sah", solrt.BVH8_Q8, True), ("bvh8_fp32", solrt.BVH8_F32, False)):
+            sc = solrt.SceneDescription(ctx, data, bvh=kind, leaf_max=0 if kind in (solrt.BVH2, solrt.BVH2_Q16) else 1,
+                                        sah=sah)
             info = sc.bvh_info()
             h = torch.zeros((n_rays, 4), dtype=torch.float32, device=dev)
             ctx.reset_stats()
@@ -248,7 +250,7 @@ def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, mai
             ctx.synchronize()
             fb_trace = ctx.stats().fp64_fallbacks
             hits[name] = h
-            if kind == main_info.kind:
+            if kind == main_info.kind and not sah:
                 mr, nodes, tris = main_mrays, main_nodes, main_tris
             else:
                 img = solrt.Image(ctx, W, H, kw["accum_mode"])
@@ -261,7 +263,8 @@ def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, mai
                 st = ctx.stats()
                 mr = st.segments / (st.render_ms / 1000.0) / 1e6 if st.render_ms > 0 else None
                 img.close()
-                csc = solrt.SceneDescription(cctx, data, bvh=kind, leaf_max=0 if kind in (solrt.BVH2, solrt.BVH2_Q16) else 1)
+                csc = solrt.SceneDescription(cctx, data, bvh=kind, leaf_max=0 if kind in (solrt.BVH2, solrt.BVH2_Q16) else 1,
+                                             sah=sah)
                 cimg = solrt.Image(cctx, W, H, kw["accum_mode"])
                 cctx.reset_stats()
                 solrt.Renderer(cctx).cmd_trace_rays(csc, cam, solrt.render_params(**dict(kw, spp=min(4, kw["spp"]))),
@@ -281,7 +284,7 @@ def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, mai
             sc.close()
     a = hits["bvh2_fp32"].view(torch.int32)
     out["hit_mismatches"] = {k: int((a != hits[k].view(torch.int32)).any(dim=1).sum().item())
-                             for k in ("bvh2_q16", "bvh4_q8", "bvh8_q8", "bvh8_fp32")}
+                             for k in ("bvh2_q16", "bvh4_q8", "bvh8_q8", "bvh8_q8_sah", "bvh8_fp32")}
     # hits within about one float ulp of a triangle edge (a barycentric below
     # 2^-23), counted separately: the watertight test and the lower-index tie
     # rule make even these agree across BVHs
@@ -291,7 +294,7 @@ def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, mai
     edge = hit & (torch.minimum(torch.minimum(u, v), 1.0 - u - v) < 2.0 ** -23)
     out["near_edge_hits"] = int(edge.sum().item())
     out["near_edge_mismatches"] = {k: int(((a != hits[k].view(torch.int32)).any(dim=1) & edge).sum().item())
-                                   for k in ("bvh2_q16", "bvh4_q8", "bvh8_q8", "bvh8_fp32")}
+                                   for k in ("bvh2_q16", "bvh4_q8", "bvh8_q8", "bvh8_q8_sah", "bvh8_fp32")}
     out["hits"] = int((a[:, 1] != -1).sum().item())
     return out
 
@@ -313,7 +316,7 @@ def run_batch(args, world, rank, local, pg, njobs=None, steps=None, emit=True):
     t0 = time.perf_counter()
     for i in range(njobs):
         data, jp = S.mixed_scene(i)
-        sc = solrt.SceneDescription(ctx, data, bvh=bvh, keep_data=False)
+        sc = solrt.SceneDescription(ctx, data, bvh=bvh, keep_data=False, sah=args.sah)
         tris += data.tri_count
         del data
         w, h = jp["width"], jp["height"]
@@ -524,6 +527,7 @@ def main():
     ap.add_argument("--impl", default="solrt", choices=["solrt", "reference"])
     ap.add_argument("--workload", default="soup", choices=["soup", "cornell", "tunnel", "batch", "serve"])
     ap.add_argument("--bvh", default="bvh2", choices=["bvh2", "bvh2q", "bvh4", "bvh8", "bvh8f"])
+    ap.add_argument("--sah", action="store_true", help="wide BVH kinds: SAH-optimal collapse")
     ap.add_argument("--jobs", type=int, default=256)
     ap.add_argument("--rate", type=float, default=6.0, help="serve: Poisson arrival rate, jobs/s")
     ap.add_argument("--duration", type=float, default=8.0, help="serve: arrival window, s")
@@ -569,7 +573,7 @@ def main():
 
     # visit counts per segment (one counting launch at reduced spp)
     with solrt.Context(local, enable_counters=True) as cctx:
-        csc = solrt.SceneDescription(cctx, data, bvh=bvh)
+        csc = solrt.SceneDescription(cctx, data, bvh=bvh, sah=args.sah)
         cimg = solrt.Image(cctx, W, H, kw["accum_mode"])
         cctx.reset_stats()
         solrt.Renderer(cctx).cmd_trace_rays(csc, cam, solrt.render_params(**dict(kw, spp=min(4, kw["spp"]))), cimg)
@@ -582,7 +586,7 @@ def main():
         csc.close()
 
     ctx = solrt.Context(local, enable_timing=True)
-    sc = solrt.SceneDescription(ctx, data, bvh=bvh)
+    sc = solrt.SceneDescription(ctx, data, bvh=bvh, sah=args.sah)
     info = sc.bvh_info()
     img = solrt.Image(ctx, W, H, kw["accum_mode"])
     r = solrt.Renderer(ctx)

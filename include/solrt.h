@@ -125,11 +125,15 @@ typedef enum solrt_bvh_kind {
 #define SOLRT_BVH_DYNAMIC 1u  /* keep object-space geometry and the BVH topology on
                                  the device so solrt_scene_set_instances +
                                  solrt_scene_regenerate can move sections */
+#define SOLRT_BVH_SAH 2u      /* BVH8 / BVH4 kinds: choose each wide node's children
+                                 by the SAH-optimal collapse of the binary tree
+                                 (dynamic program over the binary nodes) instead of
+                                 opening the largest child first; same hits */
 
 typedef struct solrt_bvh_desc {
     uint32_t kind;       /* solrt_bvh_kind */
     uint32_t leaf_max;   /* BVH8 / BVH4: max triangles per leaf child (1..3), 0 = 1 */
-    uint32_t flags;      /* SOLRT_BVH_DYNAMIC (honoured by solrt_scene_create) */
+    uint32_t flags;      /* SOLRT_BVH_DYNAMIC (honoured by solrt_scene_create), SOLRT_BVH_SAH */
     uint32_t reserved;
 } solrt_bvh_desc;
 

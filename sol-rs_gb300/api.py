@@ -28,7 +28,7 @@ ACCUM_REF_MIX, ACCUM_KAHAN = 0, 1
 RNG_REF_STREAM, RNG_PER_SAMPLE = 0, 1
 KERNEL_WAVEFRONT, KERNEL_MEGA = 0, 1
 INTEGRATOR_PATH, INTEGRATOR_DEBUG, INTEGRATOR_AO = 0, 1, 2
-BVH_DYNAMIC = 1
+BVH_DYNAMIC, BVH_SAH = 1, 2
 REGEN_REBUILD, REGEN_REFIT = 0, 1
 EFLAG_STACK, EFLAG_QUEUE, EFLAG_INDEX, EFLAG_TIMEOUT = 1, 2, 4, 8
 
@@ -317,14 +317,15 @@ class SceneDescription:
 
     dynamic=True keeps object-space geometry on the device so that
     blas_transform(s) + tlas_regenerate move sections per frame
-    (src/ray/mod.rs:162-181)."""
+    (src/ray/mod.rs:162-181). sah=True chooses the children of wide (BVH8 /
+    BVH4) nodes by the SAH-optimal collapse."""
 
-    def __init__(self, context, data, bvh=BVH2, leaf_max=0, keep_data=True, dynamic=False):
+    def __init__(self, context, data, bvh=BVH2, leaf_max=0, keep_data=True, dynamic=False, sah=False):
         self.context = context
         self.data = data if keep_data else None
         self.dynamic = dynamic
         d = scene_desc(data)
-        bd = BvhDesc(kind=bvh, leaf_max=leaf_max, flags=BVH_DYNAMIC if dynamic else 0)
+        bd = BvhDesc(kind=bvh, leaf_max=leaf_max, flags=(BVH_DYNAMIC if dynamic else 0) | (BVH_SAH if sah else 0))
         h = ctypes.c_void_p()
         check(lib().solrt_scene_create(context.handle, ctypes.byref(d), ctypes.byref(bd), ctypes.byref(h)))
         self.handle = h
@@ -365,8 +366,9 @@ class SceneDescription:
 
     __del__ = close
 
-    def build_bvh(self, bvh=BVH2, leaf_max=0):
-        check(lib().solrt_scene_build_bvh(self.handle, ctypes.byref(BvhDesc(kind=bvh, leaf_max=leaf_max))))
+    def build_bvh(self, bvh=BVH2, leaf_max=0, sah=False):
+        check(lib().solrt_scene_build_bvh(self.handle, ctypes.byref(
+            BvhDesc(kind=bvh, leaf_max=leaf_max, flags=BVH_SAH if sah else 0))))
 
     def tlas_regenerate(self, mode=REGEN_REBUILD):
         """Dynamic scene: applies the staged instance transforms on the

@@ -458,6 +458,7 @@ solrt_status solrt_scene_build_bvh(solrt_scene* scene, const solrt_bvh_desc* bvh
     CHECK_ARG(scene && bvh, "null argument");
     CHECK_ARG(bvh->kind <= SOLRT_BVH2_Q16, "unknown BVH kind");
     CHECK_ARG(bvh->leaf_max <= 3, "leaf_max must be 0..3");
+    CHECK_ARG((bvh->flags & ~(SOLRT_BVH_DYNAMIC | SOLRT_BVH_SAH)) == 0, "unknown BVH flags");
     SOLRT_CUDA(cudaSetDevice(scene->ctx->device));
     return build_bvh(*scene->ctx, *scene, *bvh);
 }

@@ -30,6 +30,9 @@ struct Bvh8BuildInput {
     const uint2* range;        // binary LBVH internal nodes: first, last leaf position
     const float4* tri_wt_leaf; // triangles in LBVH leaf order (3 float4 each)
     uint32_t leaf_max;         // max triangles per leaf child (1..3)
+    const uint32_t* par_int;   // binary LBVH: parent of each internal node (SAH collapse)
+    const uint32_t* par_leaf;  // binary LBVH: parent of each leaf (SAH collapse)
+    bool sah;                  // SAH-optimal collapse instead of largest-child-first
 };
 
 // In-place exclusive scan of `len` u32 counts (bvh_build.cu).

@@ -5,7 +5,8 @@
 // binary node -> one 8-wide node). Per task, one thread
 //   1. gathers up to 8 children by repeatedly opening the child with the
 //      largest surface area among those holding more than `leaf_max`
-//      triangles (those cannot be leaves);
+//      triangles (those cannot be leaves), or, with the SAH collapse, by
+//      decoding the choices of a bottom-up dynamic program (k_sah_costs);
 //   2. (after an exclusive scan of the internal-child and triangle counts of
 //      all tasks of the level) assigns children to slots so that slot s
 //      holds the child whose centre lies most in direction
@@ -66,12 +67,126 @@ __device__ __forceinline__ float half_area(const Box3& b) {
     return dx * dy + dy * dz + dz * dx;
 }
 
+// SAH-optimal collapse (after Ylitie, Karras and Laine, HPG 2017, section
+// 4.1). For every binary node n and i = 1..W, cost(n, i) is the least SAH
+// cost of representing n's subtree by at most i children of the wide node
+// above it:
+//   a subtree of <= leaf_max triangles is one leaf child:
+//       cost(n, i) = A(n) * kSahTri * count(n)
+//   otherwise (cost(n, 1): n becomes a wide node itself)
+//       cost(n, 1) = A(n) * kSahNode + D(n, W)
+//       cost(n, i) = min(cost(n, i - 1), D(n, i))
+//   D(n, j) = min over k = 1..j-1 of cost(left, k) + cost(right, j - k)
+// with A the half surface area. Nodes are finished bottom-up as in the refit
+// (the second thread to arrive computes the node). Per internal node the
+// table keeps cost(n, 1..W), the split k of each i (0: same as i - 1) in
+// nibbles, and the split of D(n, W).
+constexpr float kSahNode = 1.0f;
+constexpr float kSahTri = 0.3f;
+
+__device__ __forceinline__ float sah_leaf_cost(uint32_t ref, const uint2* __restrict__ range,
+                                               const float4* __restrict__ nbox, const float4* __restrict__ tris) {
+    return half_area(ref_box(ref, nbox, tris)) * kSahTri * (float)ref_count(ref, range);
+}
+
+__global__ void k_sah_costs(uint32_t n, const uint32_t* __restrict__ child, const uint32_t* __restrict__ par_int,
+                            const uint32_t* __restrict__ par_leaf, const uint2* __restrict__ range,
+                            const float4* __restrict__ nbox, const float4* __restrict__ tris, uint32_t leaf_max,
+                            uint32_t width, unsigned int* __restrict__ flags, float* __restrict__ cost,
+                            uint2* __restrict__ dec) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n || n < 2) return;
+    const int W = (int)width;
+    uint32_t p = par_leaf[k];
+    for (uint32_t steps = 0; steps < n; ++steps) {
+        if (p >= n - 1) return;  // malformed parent link: stop
+        __threadfence();
+        if (atomicAdd(flags + p, 1u) == 0u) return;
+        __threadfence();
+        float c[8];
+        uint32_t decs = 0, dw = 0;
+        const float area = half_area(ref_box(p, nbox, tris));
+        if (ref_count(p, range) <= leaf_max) {
+            const float lc = area * kSahTri * (float)ref_count(p, range);
+            for (int i = 0; i < 8; ++i) c[i] = lc;
+        } else {
+            float cl[8], cr[8];
+            for (int side = 0; side < 2; ++side) {
+                const uint32_t r = child[2 * (size_t)p + side];
+                float* t = side ? cr : cl;
+                if ((r & kLeafFlag) || ref_count(r, range) <= leaf_max) {
+                    const float lc = sah_leaf_cost(r, range, nbox, tris);
+                    for (int i = 0; i < 8; ++i) t[i] = lc;
+                } else {
+                    for (int i = 0; i < 8; ++i) t[i] = __ldcg(cost + 8 * (size_t)r + i);
+                }
+            }
+            float D[9];
+            uint32_t K[9];
+            for (int j = 2; j <= W; ++j) {
+                D[j] = INFINITY;
+                K[j] = 1;
+                for (int s = 1; s < j; ++s) {
+                    const float v = cl[s - 1] + cr[j - s - 1];
+                    if (v < D[j]) { D[j] = v; K[j] = (uint32_t)s; }
+                }
+            }
+            c[0] = area * kSahNode + D[W];
+            dw = K[W];
+            for (int i = 2; i <= W; ++i) {
+                if (D[i] < c[i - 2]) {
+                    c[i - 1] = D[i];
+                    decs |= K[i] << (4 * (i - 1));
+                } else {
+                    c[i - 1] = c[i - 2];
+                }
+            }
+            for (int i = W; i < 8; ++i) c[i] = c[W - 1];
+        }
+        for (int i = 0; i < 8; ++i) __stcg(cost + 8 * (size_t)p + i, c[i]);
+        __stcg(dec + p, make_uint2(decs, dw));
+        if (p == 0) return;
+        p = par_int[p];
+    }
+}
+
+// The children of wide node `b` chosen by the SAH collapse: D(b, W)'s split,
+// each side resolved to the roots of its cost(r, i) choice.
+__device__ int sah_children(uint32_t b, uint32_t width, const uint32_t* __restrict__ child,
+                            const uint2* __restrict__ range, uint32_t leaf_max, const uint2* __restrict__ dec,
+                            uint32_t* c) {
+    uint32_t sr[16];
+    uint32_t si[16];
+    int sp = 0, m = 0;
+    const uint32_t k = dec[b].y;
+    sr[sp] = child[2 * (size_t)b + 1]; si[sp++] = width - k;
+    sr[sp] = child[2 * (size_t)b]; si[sp++] = k;
+    while (sp > 0 && m < 8) {
+        const uint32_t r = sr[--sp];
+        uint32_t i = si[sp];
+        if ((r & kLeafFlag) || ref_count(r, range) <= leaf_max) {
+            c[m++] = r;
+            continue;
+        }
+        const uint32_t decs = dec[r].x;
+        while (i > 1 && ((decs >> (4 * (i - 1))) & 15u) == 0u) --i;
+        if (i <= 1 || sp + 2 > 16) {
+            c[m++] = r;
+            continue;
+        }
+        const uint32_t s = (decs >> (4 * (i - 1))) & 15u;
+        sr[sp] = child[2 * (size_t)r + 1]; si[sp++] = i - s;
+        sr[sp] = child[2 * (size_t)r]; si[sp++] = s;
+    }
+    return m;
+}
+
 // Pass 1: gather children, count internal children and leaf triangles.
 __global__ void k_gather(const uint32_t* __restrict__ tasks, uint32_t ntasks, const uint32_t* __restrict__ child,
                          const uint2* __restrict__ range, const float4* __restrict__ nbox,
                          const float4* __restrict__ tris, uint32_t leaf_max, uint32_t width,
-                         uint32_t* __restrict__ gathered, uint32_t* __restrict__ n_inner,
-                         uint32_t* __restrict__ n_tris) {
+                         const uint2* __restrict__ sah_dec, uint32_t* __restrict__ gathered,
+                         uint32_t* __restrict__ n_inner, uint32_t* __restrict__ n_tris) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t > ntasks) return;
     if (t == ntasks) {  // trailing zero so the exclusive scans end with the totals
@@ -85,6 +200,8 @@ __global__ void k_gather(const uint32_t* __restrict__ tasks, uint32_t ntasks, co
     if (b & kLeafFlag) {  // single-triangle scene: the root holds one leaf
         c[0] = b;
         m = 1;
+    } else if (sah_dec) {
+        m = sah_children(b, width, child, range, leaf_max, sah_dec, c);
     } else {
         c[0] = child[2 * (size_t)b];
         c[1] = child[2 * (size_t)b + 1];
@@ -379,6 +496,19 @@ solrt_status build_wide(Context& ctx, const Bvh8BuildInput& in, uint32_t width, 
     SOLRT_TRY(ntri.alloc(4ull * (max_nodes + 1)));
     const uint32_t root = n > 1 ? 0u : kLeafFlag;  // binary root, or the single leaf
     SOLRT_CUDA(cudaMemcpyAsync(task[0].ptr, &root, 4, cudaMemcpyHostToDevice, st));
+    DeviceBuffer sah_cost, sah_dec, sah_flags;
+    const bool sah = in.sah && n > 1 && in.par_int && in.par_leaf;
+    if (sah) {
+        SOLRT_TRY(sah_cost.alloc(32ull * (n - 1)));
+        SOLRT_TRY(sah_dec.alloc(8ull * (n - 1)));
+        SOLRT_TRY(sah_flags.alloc(4ull * (n - 1)));
+        SOLRT_CUDA(cudaMemsetAsync(sah_flags.ptr, 0, sah_flags.bytes, st));
+        k_sah_costs<<<blocks_of(n, 256), 256, 0, st>>>(n, in.child, in.par_int, in.par_leaf, in.range, in.nbox,
+                                                       in.tri_wt_leaf, in.leaf_max, width,
+                                                       sah_flags.as<unsigned int>(), sah_cost.as<float>(),
+                                                       sah_dec.as<uint2>());
+        ++ctx.launches;
+    }
     uint32_t ntasks = 1, node_base = 0, tri_level_base = 0, levels = 0;
     int cur = 0;
     while (ntasks > 0) {
@@ -388,6 +518,7 @@ solrt_status build_wide(Context& ctx, const Bvh8BuildInput& in, uint32_t width, 
         }
         k_gather<<<blocks_of(ntasks + 1, 128), 128, 0, st>>>(task[cur].as<uint32_t>(), ntasks, in.child, in.range,
                                                              in.nbox, in.tri_wt_leaf, in.leaf_max, width,
+                                                             sah ? sah_dec.as<uint2>() : nullptr,
                                                              gathered.as<uint32_t>(), inner.as<uint32_t>(),
                                                              ntri.as<uint32_t>());
         launch_scan_exclusive(inner.as<uint32_t>(), ntasks + 1, st);

@@ -603,6 +603,9 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
         in.range = range.as<uint2>();
         in.tri_wt_leaf = sc.tri_wt.as<float4>();
         in.leaf_max = desc.leaf_max == 0 ? 1u : std::min(3u, desc.leaf_max);
+        in.par_int = par_int.as<uint32_t>();
+        in.par_leaf = par_leaf.as<uint32_t>();
+        in.sah = (desc.flags & SOLRT_BVH_SAH) != 0;
         DeviceBuffer tri8;
         uint32_t node_count = 0, depth8 = 0;
         SOLRT_TRY(build_wide(ctx, in, width, f32, sc.nodes, tri8, &node_count, &depth8));
@@ -729,6 +732,9 @@ solrt_status refit_bvh(Context& ctx, Scene& sc) {
         in.range = sc.topo_range.as<uint2>();
         in.tri_wt_leaf = tri2.as<float4>();
         in.leaf_max = sc.desc.leaf_max == 0 ? 1u : std::min(3u, sc.desc.leaf_max);
+        in.par_int = sc.topo_par_int.as<uint32_t>();
+        in.par_leaf = sc.topo_par_leaf.as<uint32_t>();
+        in.sah = (sc.desc.flags & SOLRT_BVH_SAH) != 0;
         DeviceBuffer nodes8, tri8;
         uint32_t node_count = 0, depth8 = 0;
         SOLRT_TRY(build_wide(ctx, in, width, f32, nodes8, tri8, &node_count, &depth8));

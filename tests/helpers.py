@@ -117,6 +117,14 @@ def transformed_cornell():
     return d
 
 
+def bvh_args(solrt_mod, name):
+    """SceneDescription keyword arguments of a BVH name: bvh_kind's names,
+    plus "bvh8s" / "bvh4s" for the wide kinds with the SAH collapse."""
+    if name in ("bvh8s", "bvh4s"):
+        return dict(bvh=bvh_kind(solrt_mod, name[:-1]), sah=True)
+    return dict(bvh=bvh_kind(solrt_mod, name))
+
+
 def bvh_kind(solrt_mod, name):
     """"bvh2" / "bvh2q" / "bvh4" / "bvh8" / "bvh8f" -> solrt BVH kind."""
     return {"bvh2": solrt_mod.BVH2, "bvh2q": solrt_mod.BVH2_Q16, "bvh4": solrt_mod.BVH4_Q8,

@@ -156,15 +156,16 @@ def _decode_bvh8f(nodes_u8):
                 lo=planes[:, :, 0, :].transpose(0, 2, 1), hi=planes[:, :, 1, :].transpose(0, 2, 1))
 
 
+@pytest.mark.parametrize("sah", [False, True])
 @pytest.mark.parametrize("width", [8, 4, "8f"])
 @pytest.mark.parametrize("maker", [lambda: S.cornell(), lambda: S.soup(40000, seed=3),
                                    lambda: S.tunnel(n_ang=128, n_ax=64, length=20.0), lambda: single_triangle()])
-def test_wide_bvh_conservative_and_complete(solrt, ctx, maker, width):
+def test_wide_bvh_conservative_and_complete(solrt, ctx, maker, width, sah):
     """Every triangle is referenced by exactly one leaf slot and lies inside
     the decoded (quantised) box of that slot and of every ancestor slot."""
     d = maker()
     kind = {8: solrt.BVH8_Q8, 4: solrt.BVH4_Q8, "8f": solrt.BVH8_F32}[width]
-    sc = solrt.SceneDescription(ctx, d, bvh=kind)
+    sc = solrt.SceneDescription(ctx, d, bvh=kind, sah=sah)
     nodes, tris = sc.bvh_export()
     info = sc.bvh_info()
     n = info.tri_count
@@ -212,3 +213,52 @@ def test_rebuild_is_deterministic(solrt, ctx):
     sc.tlas_regenerate()
     b, tb = sc.bvh_export()
     assert np.array_equal(a, b) and np.array_equal(ta, tb)
+
+
+def _wide_sah_cost(dec, tv, width, c_node=1.0, c_tri=0.3):
+    """SAH cost of a decoded wide BVH with exact boxes (union of the
+    triangles below each slot): A(node) c_node per node plus
+    A(leaf) c_tri k per leaf slot of k triangles."""
+    def half_area(lo, hi):
+        e = hi - lo
+        return e[0] * e[1] + e[1] * e[2] + e[2] * e[0]
+
+    def walk(node):
+        lo, hi, cost = np.full(3, np.inf), np.full(3, -np.inf), 0.0
+        for s in range(width):
+            m = int(dec["meta"][node, s])
+            if m == 0:
+                continue
+            if (int(dec["imask"][node]) >> s) & 1:
+                rank = bin(int(dec["imask"][node]) & ((1 << s) - 1)).count("1")
+                clo, chi, cc = walk(int(dec["child_base"][node]) + rank)
+                cost += cc
+            else:
+                k = bin(m >> 5).count("1")
+                t0 = int(dec["tri_base"][node]) + (m & 31)
+                v = tv[t0:t0 + k].reshape(-1, 3)
+                clo, chi = v.min(0), v.max(0)
+                cost += half_area(clo, chi) * c_tri * k
+            lo, hi = np.minimum(lo, clo), np.maximum(hi, chi)
+        return lo, hi, cost + half_area(lo, hi) * c_node
+
+    return walk(0)[2]
+
+
+@pytest.mark.parametrize("width", [8, 4])
+@pytest.mark.parametrize("maker", [lambda: S.cornell(), lambda: S.soup(20000, seed=4),
+                                   lambda: S.tunnel(n_ang=96, n_ax=48, length=20.0)])
+def test_sah_collapse_not_worse_than_greedy(solrt, ctx, maker, width):
+    """The SAH collapse minimises the SAH cost over all collapses of the
+    binary tree (with leaves of <= leaf_max triangles), so its tree costs no
+    more than the largest-child-first tree; both give the oracle's hits."""
+    d = maker()
+    kind = solrt.BVH8_Q8 if width == 8 else solrt.BVH4_Q8
+    costs = {}
+    for sah in (False, True):
+        sc = solrt.SceneDescription(ctx, d, bvh=kind, sah=sah)
+        nodes, tris = sc.bvh_export()
+        dec = _decode_bvh8(nodes) if width == 8 else _decode_bvh4(nodes)
+        tv = tris.view(np.float32).reshape(-1, 3, 4)[:, :, :3].astype(np.float64)
+        costs[sah] = _wide_sah_cost(dec, tv, width)
+    assert costs[True] <= costs[False] * (1 + 1e-5), costs

@@ -54,10 +54,10 @@ def importlib_solrt():
     return importlib.import_module("sol-rs_gb300")
 
 
-def _render_both(solrt, oracle, ctx, data, w, h, kw, frames=2, bvh=None):
+def _render_both(solrt, oracle, ctx, data, w, h, kw, frames=2, bvh=None, sah=False):
     bvh = solrt.BVH2 if bvh is None else bvh
     cam = camera_of(data, w / h)
-    sc = solrt.SceneDescription(ctx, data, bvh=bvh)
+    sc = solrt.SceneDescription(ctx, data, bvh=bvh, sah=sah)
     mode = kw.get("accum_mode", solrt.ACCUM_REF_MIX)
     img = solrt.Image(ctx, w, h, mode)
     r = solrt.Renderer(ctx)
@@ -91,6 +91,16 @@ def test_render_bit_exact(solrt, oracle, ctx, name, bvh):
     assert stats.segments == seg_o
     assert stats.error_flags == 0
     assert np.isfinite(ga).all() and ga[..., :3].mean() > 0
+
+
+@pytest.mark.parametrize("bvh", ["bvh4", "bvh8"])
+@pytest.mark.parametrize("name", ["cornell_ref_sky", "soup_gradient", "tunnel_kahan"])
+def test_render_bit_exact_sah_collapse(solrt, oracle, ctx, name, bvh):
+    """Wide BVHs collapsed by SAH render the oracle's image too."""
+    data, w, h, kw = _case(name)
+    ga, g8, oa, o8, stats, seg_o = _render_both(solrt, oracle, ctx, data, w, h, kw, bvh=bvh_kind(solrt, bvh), sah=True)
+    assert np.array_equal(ga.view(np.uint32), oa.view(np.uint32))
+    assert stats.segments == seg_o and stats.error_flags == 0
 
 
 @pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh4", "bvh8", "bvh8f"])

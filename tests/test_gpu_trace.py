@@ -4,25 +4,25 @@ bit (watertight test with the same arithmetic, deterministic tie-break)."""
 import numpy as np
 import pytest
 
-from helpers import (S, axis_rays, bvh_kind, edge_rays, empty_scene, hit_mismatch, hits_equal, random_rays,
+from helpers import (S, axis_rays, bvh_args, edge_rays, empty_scene, hit_mismatch, hits_equal, random_rays,
                      single_triangle, transformed_cornell)
 
 pytestmark = pytest.mark.gpu
 
 
 def _both(solrt, oracle, ctx, data, rays, bvh):
-    sc = solrt.SceneDescription(ctx, data, bvh=bvh)
+    sc = solrt.SceneDescription(ctx, data, **bvh)
     g = sc.trace_rays(rays)
     o = oracle.OracleScene(data)
     ref, _ = o.trace(rays, brute=True)
     return g, ref
 
 
-BVHS = ["bvh2", "bvh2q", "bvh4", "bvh8", "bvh8f"]
+BVHS = ["bvh2", "bvh2q", "bvh4", "bvh8", "bvh8f", "bvh4s", "bvh8s"]
 
 
 def _kind(solrt, name):
-    return bvh_kind(solrt, name)
+    return bvh_args(solrt, name)
 
 
 @pytest.mark.parametrize("bvh", BVHS)
