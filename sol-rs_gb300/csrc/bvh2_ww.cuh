@@ -169,13 +169,16 @@ SOLRT_D void extend_bvh2_ww(const IO& io, uint32_t n, unsigned int* work, TraceC
         // node phase
         for (;;) {
             const bool inner = (unsigned)node < (unsigned)kBvh2Sentinel;
-            if (!__any_sync(0xffffffffu, inner && leaf >= 0)) break;
+            // two ballots decide the phase: stop when no lane without a
+            // parked leaf has inner nodes, or when few lanes still have inner
+            // nodes while others hold leaves (test the leaves first; the leaf
+            // phase then has work, so this ends)
+            const uint32_t b_inner = __ballot_sync(0xffffffffu, inner);
+            const uint32_t b_leaf = __ballot_sync(0xffffffffu, leaf < 0);
+            const uint32_t b_free = b_inner & ~b_leaf;  // inner nodes, no parked leaf
+            if (b_free == 0u) break;
 #if SOLRT_WW_NODE_MIN > 0
-            // few lanes left with inner nodes while others hold leaves: test
-            // the leaves first (the leaf phase then has work, so this ends)
-            if (__popc(__ballot_sync(0xffffffffu, inner && (SOLRT_WW_SPECULATE || leaf >= 0))) < SOLRT_WW_NODE_MIN &&
-                __any_sync(0xffffffffu, leaf < 0))
-                break;
+            if (__popc(SOLRT_WW_SPECULATE ? b_inner : b_free) < SOLRT_WW_NODE_MIN && b_leaf) break;
 #endif
             if (inner && (SOLRT_WW_SPECULATE || leaf >= 0)) {
                 if (--budget == 0u || (uint32_t)node >= ts.node_count) {
