@@ -515,13 +515,15 @@ typedef struct solrt_server_stats {
     double busy_ms;           /* device time of all ticks */
 } solrt_server_stats;
 
-/* A serving thread owns the context's stream until solrt_server_destroy.
- * Each tick it admits waiting jobs in arrival order while their image (and
- * scene, when not already counted) fits the memory budget, evicting the
- * least recently completed unreleased results first; then it runs one
- * wavefront pass in which every active job advances by its share of
- * tick_paths (at least one sample), and finalizes the jobs that reached
- * their spp. A job's image equals solrt_render of the same job alone. */
+/* A serving thread owns the context's stream until solrt_server_destroy:
+ * meanwhile no other render, trace or batch call may use that context (use
+ * a second context). Each tick it admits waiting jobs in arrival order
+ * while their image (and scene, when not already counted) fits the memory
+ * budget, evicting the least recently completed unreleased results first;
+ * then it runs one wavefront pass in which every active job advances by its
+ * share of tick_paths (at least one sample; a job with more pixels than a
+ * tick runs one sample per tick), and finalizes the jobs that reached their
+ * spp. A job's image equals solrt_render of the same job alone. */
 solrt_status solrt_server_create(solrt_context* ctx, const solrt_server_desc* desc, solrt_server** out);
 /* Queues a job: the server allocates its image (params.width x height). */
 solrt_status solrt_server_submit(solrt_server* srv, solrt_scene* scene, const solrt_camera* camera,

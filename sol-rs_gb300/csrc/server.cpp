@@ -220,7 +220,10 @@ void serve_loop(solrt_server* srv) {
                 // fair: an equal share; shortest first: what is left of the tick
                 const uint32_t room = shortest ? (srv->tick_paths > pp.paths ? srv->tick_paths - pp.paths : 0u)
                                                : share;
-                if (shortest && room < np) continue;
+                // a job larger than what is left waits for the next tick,
+                // unless the tick is still empty (it then runs one sample, so
+                // jobs larger than a whole tick are not starved)
+                if (shortest && room < np && pp.paths > 0) continue;
                 uint32_t k = j.p.rng_mode == SOLRT_RNG_REF_STREAM ? 1u : std::max(1u, std::min(left, room / np));
                 if ((uint64_t)pp.paths + (uint64_t)np * k > ctx.capacity) {
                     if (pp.paths + np > ctx.capacity) continue;  // next tick

@@ -131,6 +131,31 @@ def test_shortest_first_finishes_small_jobs_first(solrt):
         solrt.Server(ctx, policy=7)
 
 
+@pytest.mark.parametrize("policy", [0, 1])
+def test_job_larger_than_a_tick_completes(solrt, policy):
+    """A job with more pixels than one tick holds still runs (one sample per
+    tick) under both policies, next to small jobs, and renders as alone."""
+    ctx = solrt.Context(0)
+    d = S.cornell()
+    sc = solrt.SceneDescription(ctx, d)
+    srv = solrt.Server(ctx, tick_paths=256, policy=policy)
+    big = solrt.render_params(32, 32, spp=3, max_bounces=3, material_mode=solrt.MATERIAL_LAMBERT,
+                              rng_mode=solrt.RNG_PER_SAMPLE, seed=5)
+    small = solrt.render_params(8, 8, spp=2, max_bounces=3, material_mode=solrt.MATERIAL_LAMBERT,
+                                rng_mode=solrt.RNG_PER_SAMPLE, seed=6, job_id=1)
+    cam = camera_of(d, 1.0)
+    tb = srv.submit(sc, cam, big)
+    ts = srv.submit(sc, cam, small)
+    rb = srv.wait(tb, 60000)
+    rs = srv.wait(ts, 60000)
+    assert rb.status == 0 and rb.spp_done == 3 and rs.status == 0
+    got = srv.read(tb, rb)[0]
+    srv.close()
+    img = solrt.Image(ctx, 32, 32)
+    solrt.Renderer(ctx).cmd_trace_rays(sc, cam, big, img)
+    assert np.array_equal(img.read()[0].view(np.uint32), got.view(np.uint32))
+
+
 def _wait_status(srv, ticket, timeout_s=60.0):
     """Polls until the job leaves the queued / running states; returns the status."""
     t0 = time.time()
