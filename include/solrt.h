@@ -117,8 +117,14 @@ typedef enum solrt_bvh_kind {
     SOLRT_BVH4_Q8 = 2,  /* 4-wide, 8-bit quantised child boxes, 64 B nodes */
     SOLRT_BVH8_F32 = 3, /* 8-wide, FP32 child boxes, 224 B nodes (the unquantised
                            reference point of SOLRT_BVH8_Q8) */
-    SOLRT_BVH2_Q16 = 4  /* binary LBVH, child boxes as 16-bit planes of one
+    SOLRT_BVH2_Q16 = 4, /* binary LBVH, child boxes as 16-bit planes of one
                            per-scene grid, 32 B nodes (same hits as SOLRT_BVH2) */
+    SOLRT_BVH2_TWO_LEVEL = 5 /* one binary BLAS per section over its object-space
+                           triangles, built once, and a binary TLAS over the
+                           instances, rebuilt by solrt_scene_regenerate; rays
+                           enter an instance through its inverse transform
+                           (transform_it transposed), as the reference's
+                           TLAS / BLAS pair does. Implies SOLRT_BVH_DYNAMIC */
 } solrt_bvh_kind;
 
 /* solrt_bvh_desc.flags */

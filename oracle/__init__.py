@@ -49,6 +49,7 @@ def lib():
         L.oracle_scene_create.restype = _P
         L.oracle_scene_create.argtypes = [ctypes.POINTER(_api.SceneDesc)]
         L.oracle_scene_destroy.argtypes = [_P]
+        L.oracle_scene_set_two_level.argtypes = [_P, ctypes.c_int]
         L.oracle_scene_tri_count.restype = ctypes.c_uint32
         L.oracle_scene_tri_count.argtypes = [_P]
         L.oracle_scene_export_world.argtypes = [_P, _P, _P]
@@ -86,15 +87,19 @@ def _ptr(a):
 
 
 class OracleScene:
-    """World-space flattening + CPU LBVH of a scenes.SceneData."""
+    """World-space flattening + CPU LBVH of a scenes.SceneData.
+    two_level=True: closest hits as a two-level scene (object-space sections
+    entered through their inverse transforms, brute force)."""
 
-    def __init__(self, data):
+    def __init__(self, data, two_level=False):
         self.data = data
         self._desc = _api.scene_desc(data)
         h = lib().oracle_scene_create(ctypes.byref(self._desc))
         if not h:
             raise ValueError("oracle rejected the scene")
         self.handle = h
+        if two_level:
+            lib().oracle_scene_set_two_level(h, 1)
 
     def close(self):
         if getattr(self, "handle", None):

@@ -12,6 +12,7 @@
 #include "oracle.h"
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstdint>
@@ -231,6 +232,13 @@ struct Box {
 struct oracle_scene {
     std::vector<TriW> tris;
     std::vector<solrt_material> mats;
+    // two-level mode (SOLRT_BVH2_TWO_LEVEL): object-space triangles, each
+    // section's triangle range and the rows 0-2 of its inverse transform
+    // (transform_it transposed)
+    bool two_level = false;
+    std::vector<TriW> obj;
+    std::vector<uint32_t> sec_first, sec_count;
+    std::vector<std::array<float, 12>> minv;
     // LBVH
     std::vector<uint32_t> order;         // sorted position -> triangle
     std::vector<uint32_t> morton;        // sorted codes
@@ -256,8 +264,13 @@ bool flatten(const solrt_scene_desc* d, oracle_scene* s) {
         if (sec.material_index >= d->material_count) return false;
         const float* T = d->instances ? d->instances[si].transform : ident;
         const float* Tit = d->instances ? d->instances[si].transform_it : ident;
+        s->sec_first.push_back((uint32_t)s->tris.size());
+        s->sec_count.push_back(sec.index_count / 3);
+        std::array<float, 12> mi;
+        for (int k = 0; k < 12; ++k) mi[k] = Tit[k];  // row r of the transpose = Tit[4r .. 4r + 3]
+        s->minv.push_back(mi);
         for (uint32_t t = 0; t < sec.index_count / 3; ++t) {
-            TriW tw;
+            TriW tw, to;
             for (int k = 0; k < 3; ++k) {
                 const uint32_t li = d->indices[sec.index_offset + 3 * t + k];
                 if (li >= sec.vertex_count) return false;
@@ -265,12 +278,15 @@ bool flatten(const solrt_scene_desc* d, oracle_scene* s) {
                 float o[4];
                 mat4_mul<float>(T, v.pos[0], v.pos[1], v.pos[2], 1.0f, o);
                 tw.p[k] = V3<float>{o[0], o[1], o[2]};
+                to.p[k] = V3<float>{v.pos[0], v.pos[1], v.pos[2]};
                 mat4_mul<float>(Tit, v.normal[0], v.normal[1], v.normal[2], 0.0f, o);
                 tw.n[k] = V3<float>{o[0], o[1], o[2]};
                 tw.c[k] = V3<float>{v.color[0], v.color[1], v.color[2]};
             }
             tw.mat = sec.material_index;
             s->tris.push_back(tw);
+            to.mat = sec.material_index;
+            s->obj.push_back(to);
         }
     }
     return true;
@@ -481,8 +497,33 @@ template <class R> inline bool box_hit(const Box& b, V3<R> o, V3<R> inv, R tmin,
     return tn <= tf * R(1.0000153);
 }
 
+// Two-level scenes: every section's triangles in its object space, the ray
+// entering through the section's inverse transform with the device's
+// arithmetic (((m0 x + m1 y) + m2 z) + m3 per component, no contraction).
+template <class R> HitR<R> closest_hit_two_level(const oracle_scene* s, V3<R> o, V3<R> d, R tmin, R tmax,
+                                                 uint64_t& fb, uint64_t& nt) {
+    HitR<R> best{tmax, SOLRT_NO_HIT, R(0), R(0)};
+    for (size_t si = 0; si < s->sec_first.size(); ++si) {
+        const uint32_t first = s->sec_first[si], cnt = s->sec_count[si];
+        if (cnt == 0) continue;
+        const float* m = s->minv[si].data();
+        const V3<R> p{R(m[0]) * o.x + R(m[1]) * o.y + R(m[2]) * o.z + R(m[3]),
+                      R(m[4]) * o.x + R(m[5]) * o.y + R(m[6]) * o.z + R(m[7]),
+                      R(m[8]) * o.x + R(m[9]) * o.y + R(m[10]) * o.z + R(m[11])};
+        const V3<R> q{R(m[0]) * d.x + R(m[1]) * d.y + R(m[2]) * d.z, R(m[4]) * d.x + R(m[5]) * d.y + R(m[6]) * d.z,
+                      R(m[8]) * d.x + R(m[9]) * d.y + R(m[10]) * d.z};
+        const RayWT<R> r = setup_ray(p, q, tmin);
+        for (uint32_t i = 0; i < cnt; ++i) {
+            ++nt;
+            intersect_tri(r, s->obj[first + i], first + i, best, fb);
+        }
+    }
+    return best;
+}
+
 template <class R> HitR<R> closest_hit(const oracle_scene* s, V3<R> o, V3<R> d, R tmin, R tmax,
                                        int mode, uint64_t& fb, uint64_t& nv, uint64_t& nt) {
+    if (s->two_level) return closest_hit_two_level<R>(s, o, d, tmin, tmax, fb, nt);
     HitR<R> best{tmax, SOLRT_NO_HIT, R(0), R(0)};
     const RayWT<R> r = setup_ray(o, d, tmin);
     const uint32_t n = (uint32_t)s->tris.size();
@@ -837,6 +878,10 @@ oracle_scene* oracle_scene_create(const solrt_scene_desc* desc) {
 }
 
 void oracle_scene_destroy(oracle_scene* s) { delete s; }
+
+void oracle_scene_set_two_level(oracle_scene* s, int on) {
+    if (s) s->two_level = on != 0;
+}
 
 uint32_t oracle_scene_tri_count(const oracle_scene* s) { return (uint32_t)s->tris.size(); }
 

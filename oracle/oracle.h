@@ -51,6 +51,10 @@ typedef struct oracle_render_stats {
 /* Flattens to world space and builds the CPU LBVH. NULL on error. */
 oracle_scene* oracle_scene_create(const solrt_scene_desc* desc);
 void oracle_scene_destroy(oracle_scene* s);
+/* on != 0: closest hits as a two-level scene (SOLRT_BVH2_TWO_LEVEL): each
+ * section's triangles in object space, the ray entering through the
+ * section's inverse transform (brute force over sections and triangles). */
+void oracle_scene_set_two_level(oracle_scene* s, int on);
 uint32_t oracle_scene_tri_count(const oracle_scene* s);
 
 /* World-space flattened geometry: per triangle 3 vertices x (pos, normal,

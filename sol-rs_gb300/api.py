@@ -21,7 +21,7 @@ NO_HIT = 0xFFFFFFFF
 # enums (solrt.h)
 (OK, ERR_INVALID, ERR_OOM, ERR_DEVICE, ERR_TIMEOUT, ERR_CAPACITY, ERR_NOT_READY, ERR_NOT_FOUND, ERR_BUDGET,
  ERR_CANCELLED) = range(10)
-BVH2, BVH8_Q8, BVH4_Q8, BVH8_F32, BVH2_Q16 = 0, 1, 2, 3, 4
+BVH2, BVH8_Q8, BVH4_Q8, BVH8_F32, BVH2_Q16, BVH2_TWO_LEVEL = 0, 1, 2, 3, 4, 5
 MISS_BLACK, MISS_REF_SKY, MISS_GRADIENT = 0, 1, 2
 MATERIAL_REF, MATERIAL_LAMBERT = 0, 1
 ACCUM_REF_MIX, ACCUM_KAHAN = 0, 1
@@ -323,13 +323,13 @@ class SceneDescription:
     def __init__(self, context, data, bvh=BVH2, leaf_max=0, keep_data=True, dynamic=False, sah=False):
         self.context = context
         self.data = data if keep_data else None
-        self.dynamic = dynamic
+        self.dynamic = dynamic or bvh == BVH2_TWO_LEVEL   # two-level scenes take instances too
         d = scene_desc(data)
         bd = BvhDesc(kind=bvh, leaf_max=leaf_max, flags=(BVH_DYNAMIC if dynamic else 0) | (BVH_SAH if sah else 0))
         h = ctypes.c_void_p()
         check(lib().solrt_scene_create(context.handle, ctypes.byref(d), ctypes.byref(bd), ctypes.byref(h)))
         self.handle = h
-        if dynamic:
+        if self.dynamic:
             from . import scenes
             if data.instances is not None:
                 self.instances = data.instances.copy()

@@ -333,28 +333,30 @@ solrt_status solrt_scene_create(solrt_context* ctx, const solrt_scene_desc* d, c
         nt += sec.index_count / 3;
     }
     CHECK_ARG(nv < (1ull << 31) && nt < (1ull << 31), "scene too large");
-    const bool dynamic = bvh && (bvh->flags & SOLRT_BVH_DYNAMIC);
+    // two-level scenes keep the object-space geometry, as dynamic ones do
+    const bool dynamic = bvh && ((bvh->flags & SOLRT_BVH_DYNAMIC) || bvh->kind == SOLRT_BVH2_TWO_LEVEL);
     std::vector<float4> pos(nv), nrm(nv), col(nv);
     std::vector<float4> opos(dynamic ? nv : 0), onrm(dynamic ? nv : 0);
     std::vector<uint32_t> vsec_start(dynamic ? d->section_count : 0);
-    std::vector<solrt_instance> inst(dynamic ? d->section_count : 0);
+    std::vector<solrt_instance> inst(d->section_count);
+    std::vector<uint32_t> sec_first(d->section_count), sec_count(d->section_count);
     std::vector<uint4> tri(nt);
     uint64_t vb = 0, tb = 0;
     for (uint32_t s = 0; s < d->section_count; ++s) {
         const solrt_section& sec = d->sections[s];
         const float* T = d->instances ? d->instances[s].transform : ident;
         const float* Tit = d->instances ? d->instances[s].transform_it : ident;
-        if (dynamic) {
-            vsec_start[s] = (uint32_t)vb;
-            if (d->instances) {
-                inst[s] = d->instances[s];
-            } else {
-                inst[s] = solrt_instance{};
-                inst[s].id = s;
-                std::memcpy(inst[s].transform, ident, sizeof(ident));
-                std::memcpy(inst[s].transform_it, ident, sizeof(ident));
-            }
+        if (d->instances) {
+            inst[s] = d->instances[s];
+        } else {
+            inst[s] = solrt_instance{};
+            inst[s].id = s;
+            std::memcpy(inst[s].transform, ident, sizeof(ident));
+            std::memcpy(inst[s].transform_it, ident, sizeof(ident));
         }
+        sec_first[s] = (uint32_t)tb;
+        sec_count[s] = sec.index_count / 3;
+        if (dynamic) vsec_start[s] = (uint32_t)vb;
         for (uint32_t v = 0; v < sec.vertex_count; ++v) {
             const solrt_vertex& in = d->vertices[sec.vertex_offset + v];
             if (dynamic) {
@@ -417,6 +419,9 @@ solrt_status solrt_scene_create(solrt_context* ctx, const solrt_scene_desc* d, c
         return fail(SOLRT_ERR_DEVICE);
     }
     sc->section_count = d->section_count;
+    sc->sec_tri_first = std::move(sec_first);
+    sc->sec_tri_count = std::move(sec_count);
+    sc->inst_host = inst;
     if (dynamic) {
         sc->dynamic = true;
         const size_t ns = d->section_count;
@@ -456,7 +461,7 @@ solrt_status solrt_scene_destroy(solrt_scene* scene) {
 
 solrt_status solrt_scene_build_bvh(solrt_scene* scene, const solrt_bvh_desc* bvh) {
     CHECK_ARG(scene && bvh, "null argument");
-    CHECK_ARG(bvh->kind <= SOLRT_BVH2_Q16, "unknown BVH kind");
+    CHECK_ARG(bvh->kind <= SOLRT_BVH2_TWO_LEVEL, "unknown BVH kind");
     CHECK_ARG(bvh->leaf_max <= 3, "leaf_max must be 0..3");
     CHECK_ARG((bvh->flags & ~(SOLRT_BVH_DYNAMIC | SOLRT_BVH_SAH)) == 0, "unknown BVH flags");
     SOLRT_CUDA(cudaSetDevice(scene->ctx->device));
@@ -525,6 +530,7 @@ solrt_status solrt_scene_set_instances(solrt_scene* scene, const solrt_instance*
     // pageable source: the call returns once the host array has been staged
     SOLRT_CUDA(cudaMemcpyAsync(scene->instances.ptr, instances, sizeof(solrt_instance) * count,
                                cudaMemcpyHostToDevice, scene->ctx->stream));
+    scene->inst_host.assign(instances, instances + count);  // the two-level TLAS is built from these
     return SOLRT_OK;
 }
 

@@ -17,7 +17,10 @@
 // every box are a pure function of the input: they equal the CPU LBVH of the
 // oracle bit for bit.
 #include <algorithm>
+#include <cmath>
+#include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "bvh8.cuh"
 #include "bvh8_traverse.cuh"
@@ -320,13 +323,13 @@ __global__ void k_refit(const float4* __restrict__ vpos, const uint4* __restrict
                         const uint32_t* __restrict__ order, const uint32_t* __restrict__ child,
                         const uint32_t* __restrict__ parent_int, const uint32_t* __restrict__ parent_leaf,
                         uint32_t n, unsigned int* __restrict__ flags, float4* __restrict__ nbox,
-                        float4* __restrict__ nodes, float4* __restrict__ tri_wt) {
+                        float4* __restrict__ nodes, float4* __restrict__ tri_wt, uint32_t prim_base = 0) {
     const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const uint32_t prim = order[k];
     const uint4 ti = tri_idx[prim];
     const float4 a = vpos[ti.x], b = vpos[ti.y], c = vpos[ti.z];
-    tri_wt[3 * (size_t)k + 0] = make_float4(a.x, a.y, a.z, __uint_as_float(prim));
+    tri_wt[3 * (size_t)k + 0] = make_float4(a.x, a.y, a.z, __uint_as_float(prim_base + prim));
     tri_wt[3 * (size_t)k + 1] = make_float4(b.x, b.y, b.z, 0.0f);
     tri_wt[3 * (size_t)k + 2] = make_float4(c.x, c.y, c.z, 0.0f);
     float lo[3] = {fminf(fminf(a.x, b.x), c.x), fminf(fminf(a.y, b.y), c.y), fminf(fminf(a.z, b.z), c.z)};
@@ -521,22 +524,40 @@ static void scan_exclusive_tiled(uint32_t* data, uint32_t len, uint32_t* sums, c
     k_scan_apply<<<tiles, 1024, 0, stream>>>(data, len, sums);
 }
 
-// Builds the LBVH of `sc` (and the 8-wide collapse when asked). Scratch is
-// allocated for the duration of the build. Synchronises.
-solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
-    const uint32_t n = sc.tri_count;
-    cudaStream_t st = ctx.stream;
-    sc.info = solrt_bvh_info{};
-    sc.info.kind = desc.kind;
-    sc.info.tri_count = n;
-    sc.nodes.release();
-    sc.tri_wt.release();
-    if (n == 0) return SOLRT_OK;
-    cudaGetLastError();  // launch errors below must be this call's own
+// ---------------------------------------------------------------------------
+// Two-level scenes (SOLRT_BVH2_TWO_LEVEL)
+// ---------------------------------------------------------------------------
 
-    SOLRT_CUDA(cudaEventRecord(ctx.ev0, st));
-    const uint32_t ni = n > 1 ? n - 1 : 1;  // internal nodes (one for a single triangle)
-    DeviceBuffer cen, cb, keys[2], vals[2], hist, child, par_int, par_leaf, flags, nbox, depth, bvh2_nodes, range;
+// Moves the references of `ni` BVH2 nodes built alone into the concatenated
+// arrays: internal nodes by `node_off`, leaves by `tri_off`.
+__global__ void k_offset_refs(float4* __restrict__ nodes, uint32_t ni, uint32_t node_off, uint32_t tri_off) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ni) return;
+    float4 r = nodes[4 * (size_t)i + 3];
+    int a = __float_as_int(r.x), b = __float_as_int(r.y);
+    a = a >= 0 ? a + (int)node_off : ~((~a) + (int)tri_off);
+    b = b >= 0 ? b + (int)node_off : ~((~b) + (int)tri_off);
+    r.x = __int_as_float(a);
+    r.y = __int_as_float(b);
+    nodes[4 * (size_t)i + 3] = r;
+}
+
+// One binary LBVH over triangles tri_idx[0, n) of positions vpos: the
+// 64-byte BVH2 nodes, the triangles in leaf order (prim = prim_base + index
+// into tri_idx), and the topology and exact boxes the wide collapse and the
+// refit reuse. Synchronises (reads the depth back).
+struct Lbvh {
+    uint32_t n = 0, ni = 0, depth = 0;
+    DeviceBuffer nodes, tri_wt, child, par_int, par_leaf, range, nbox, order;
+};
+
+static solrt_status lbvh_build(Context& ctx, const float4* vpos, const uint4* tri_idx, uint32_t n, uint32_t prim_base,
+                               Lbvh& L) {
+    cudaStream_t st = ctx.stream;
+    L.n = n;
+    L.ni = n > 1 ? n - 1 : 1;  // internal nodes (one for a single triangle)
+    const uint32_t ni = L.ni;
+    DeviceBuffer cen, cb, keys[2], vals[2], hist, flags, depth;
     SOLRT_TRY(cen.alloc(sizeof(float4) * (size_t)n));
     SOLRT_TRY(cb.alloc(6 * sizeof(unsigned int)));
     for (int i = 0; i < 2; ++i) {
@@ -547,24 +568,23 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
     SOLRT_TRY(hist.alloc(sizeof(uint32_t) * 256 * (size_t)nblocks));
     DeviceBuffer scan_sums;
     SOLRT_TRY(scan_sums.alloc(sizeof(uint32_t) * scan_tiles(256 * nblocks)));
-    SOLRT_TRY(child.alloc(sizeof(uint32_t) * 2 * (size_t)ni));
-    SOLRT_TRY(par_int.alloc(sizeof(uint32_t) * (size_t)ni));
-    SOLRT_TRY(par_leaf.alloc(sizeof(uint32_t) * (size_t)n));
+    SOLRT_TRY(L.child.alloc(sizeof(uint32_t) * 2 * (size_t)ni));
+    SOLRT_TRY(L.par_int.alloc(sizeof(uint32_t) * (size_t)ni));
+    SOLRT_TRY(L.par_leaf.alloc(sizeof(uint32_t) * (size_t)n));
     SOLRT_TRY(flags.alloc(sizeof(unsigned int) * (size_t)ni));
-    SOLRT_TRY(nbox.alloc(2 * sizeof(float4) * (size_t)ni));
+    SOLRT_TRY(L.nbox.alloc(2 * sizeof(float4) * (size_t)ni));
     SOLRT_TRY(depth.alloc(sizeof(unsigned int)));
-    SOLRT_TRY(range.alloc(sizeof(uint2) * (size_t)ni));
-    SOLRT_TRY(bvh2_nodes.alloc(4 * sizeof(float4) * (size_t)ni));
-    SOLRT_TRY(sc.tri_wt.alloc(3 * sizeof(float4) * (size_t)n));
+    SOLRT_TRY(L.range.alloc(sizeof(uint2) * (size_t)ni));
+    SOLRT_TRY(L.nodes.alloc(4 * sizeof(float4) * (size_t)ni));
+    SOLRT_TRY(L.tri_wt.alloc(3 * sizeof(float4) * (size_t)n));
 
     const unsigned int cb_init[6] = {0xffffffffu, 0xffffffffu, 0xffffffffu, 0u, 0u, 0u};
     SOLRT_CUDA(cudaMemcpyAsync(cb.ptr, cb_init, sizeof(cb_init), cudaMemcpyHostToDevice, st));
     SOLRT_CUDA(cudaMemsetAsync(flags.ptr, 0, flags.bytes, st));
     SOLRT_CUDA(cudaMemsetAsync(depth.ptr, 0, depth.bytes, st));
-    SOLRT_CUDA(cudaMemsetAsync(par_int.ptr, 0xff, par_int.bytes, st));
+    SOLRT_CUDA(cudaMemsetAsync(L.par_int.ptr, 0xff, L.par_int.bytes, st));
 
-    k_centroids<<<blocks_for(n, 256), 256, 0, st>>>(sc.vpos.as<float4>(), sc.tri_idx.as<uint4>(), n,
-                                                    cen.as<float4>(), cb.as<unsigned int>());
+    k_centroids<<<blocks_for(n, 256), 256, 0, st>>>(vpos, tri_idx, n, cen.as<float4>(), cb.as<unsigned int>());
     k_morton<<<blocks_for(n, 256), 256, 0, st>>>(cen.as<float4>(), cb.as<unsigned int>(), n, keys[0].as<uint32_t>(),
                                                  vals[0].as<uint32_t>());
     int cur = 0;
@@ -579,69 +599,293 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
         ctx.launches += 3;
     }
     if (n > 1) {
-        k_karras<<<blocks_for(n - 1, 256), 256, 0, st>>>(keys[cur].as<uint32_t>(), n, child.as<uint32_t>(),
-                                                         par_int.as<uint32_t>(), par_leaf.as<uint32_t>(),
-                                                         range.as<uint2>());
+        k_karras<<<blocks_for(n - 1, 256), 256, 0, st>>>(keys[cur].as<uint32_t>(), n, L.child.as<uint32_t>(),
+                                                         L.par_int.as<uint32_t>(), L.par_leaf.as<uint32_t>(),
+                                                         L.range.as<uint2>());
         ++ctx.launches;
     }
-    k_refit<<<blocks_for(n, 256), 256, 0, st>>>(sc.vpos.as<float4>(), sc.tri_idx.as<uint4>(), vals[cur].as<uint32_t>(),
-                                                child.as<uint32_t>(), par_int.as<uint32_t>(), par_leaf.as<uint32_t>(),
-                                                n, flags.as<unsigned int>(), nbox.as<float4>(),
-                                                bvh2_nodes.as<float4>(), sc.tri_wt.as<float4>());
-    k_depth<<<blocks_for(n, 256), 256, 0, st>>>(par_int.as<uint32_t>(), par_leaf.as<uint32_t>(), n,
+    k_refit<<<blocks_for(n, 256), 256, 0, st>>>(vpos, tri_idx, vals[cur].as<uint32_t>(), L.child.as<uint32_t>(),
+                                                L.par_int.as<uint32_t>(), L.par_leaf.as<uint32_t>(), n,
+                                                flags.as<unsigned int>(), L.nbox.as<float4>(), L.nodes.as<float4>(),
+                                                L.tri_wt.as<float4>(), prim_base);
+    k_depth<<<blocks_for(n, 256), 256, 0, st>>>(L.par_int.as<uint32_t>(), L.par_leaf.as<uint32_t>(), n,
                                                 depth.as<unsigned int>());
     ctx.launches += 5;
     SOLRT_CUDA(cudaGetLastError());
+    L.order.adopt(vals[cur]);
+    unsigned int dh = 0;
+    SOLRT_CUDA(cudaMemcpyAsync(&dh, depth.ptr, sizeof(dh), cudaMemcpyDeviceToHost, st));
+    SOLRT_CUDA(cudaStreamSynchronize(st));
+    L.depth = n > 1 ? dh : 1;
+    return SOLRT_OK;
+}
 
+// TLAS of a two-level scene, built on the host from the staged instances:
+// each non-empty section's object-space root box is transformed (8 corners,
+// FP64), rounded outward to float and widened like every BVH2 child box,
+// then the instance boxes are split at the median centroid of their widest
+// axis. Node 0 is the root; leaves are ~section. Uploads the TLAS nodes and
+// the instance table (inverse-transform rows = transform_it transposed, and
+// the section's BLAS root).
+static float host_int_as_float(int v) {
+    float f;
+    std::memcpy(&f, &v, sizeof(f));
+    return f;
+}
+
+static solrt_status build_tlas(Context& ctx, Scene& sc) {
+    struct IBox {
+        float lo[3], hi[3], c[3];
+        int32_t sec;
+    };
+    const uint32_t S = sc.section_count;
+    std::vector<IBox> items;
+    for (uint32_t s = 0; s < S; ++s) {
+        if (sc.blas_root.size() <= s || sc.blas_root[s] < 0) continue;
+        const float* T = sc.inst_host[s].transform;  // column-major
+        double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int k = 0; k < 8; ++k) {
+            const double v[3] = {sc.blas_box[6 * s + ((k & 1) ? 3 : 0)], sc.blas_box[6 * s + 1 + ((k & 2) ? 3 : 0)],
+                                 sc.blas_box[6 * s + 2 + ((k & 4) ? 3 : 0)]};
+            for (int r = 0; r < 3; ++r) {
+                const double w = (double)T[r] * v[0] + (double)T[4 + r] * v[1] + (double)T[8 + r] * v[2] +
+                                 (double)T[12 + r];
+                lo[r] = std::min(lo[r], w);
+                hi[r] = std::max(hi[r], w);
+            }
+        }
+        IBox b;
+        for (int r = 0; r < 3; ++r) {
+            if (!std::isfinite(lo[r]) || !std::isfinite(hi[r]) || std::fabs(lo[r]) > 1e37 || std::fabs(hi[r]) > 1e37) {
+                set_error("instance %u: transformed bounds are not finite", s);
+                return SOLRT_ERR_INVALID;
+            }
+            float fl = (float)lo[r], fh = (float)hi[r];
+            if ((double)fl > lo[r]) fl = std::nextafter(fl, -INFINITY);
+            if ((double)fh < hi[r]) fh = std::nextafter(fh, INFINITY);
+            b.lo[r] = widen_lo(fl);
+            b.hi[r] = widen_hi(fh);
+            b.c[r] = 0.5f * (b.lo[r] + b.hi[r]);
+        }
+        b.sec = (int32_t)s;
+        items.push_back(b);
+    }
+    std::vector<float4> nodes;
+    uint32_t depth = 0;
+    auto box_of = [&](size_t a, size_t e, float* lo, float* hi) {
+        for (int r = 0; r < 3; ++r) {
+            lo[r] = INFINITY;
+            hi[r] = -INFINITY;
+        }
+        for (size_t i = a; i < e; ++i)
+            for (int r = 0; r < 3; ++r) {
+                lo[r] = std::min(lo[r], items[i].lo[r]);
+                hi[r] = std::max(hi[r], items[i].hi[r]);
+            }
+    };
+    auto put_node = [&](size_t id, const float* l0, const float* h0, const float* l1, const float* h1, int r0,
+                        int r1) {
+        nodes[4 * id + 0] = make_float4(l0[0], h0[0], l0[1], h0[1]);
+        nodes[4 * id + 1] = make_float4(l1[0], h1[0], l1[1], h1[1]);
+        nodes[4 * id + 2] = make_float4(l0[2], h0[2], l1[2], h1[2]);
+        nodes[4 * id + 3] = make_float4(host_int_as_float(r0), host_int_as_float(r1), 0.0f, 0.0f);
+    };
+    // explicit stack of (first, end, node slot, depth); children are built
+    // after their parent so node 0 is the root
+    struct Task {
+        size_t a, e, id;
+        uint32_t d;
+    };
+    if (items.size() == 1) {  // one instance: both children are that leaf
+        nodes.resize(4);
+        put_node(0, items[0].lo, items[0].hi, items[0].lo, items[0].hi, ~items[0].sec, ~items[0].sec);
+        depth = 1;
+    } else if (items.size() > 1) {
+        nodes.resize(4);
+        std::vector<Task> todo{{0, items.size(), 0, 1}};
+        while (!todo.empty()) {
+            const Task t = todo.back();
+            todo.pop_back();
+            depth = std::max(depth, t.d);
+            float clo[3], chi[3];
+            for (int r = 0; r < 3; ++r) {
+                clo[r] = INFINITY;
+                chi[r] = -INFINITY;
+            }
+            for (size_t i = t.a; i < t.e; ++i)
+                for (int r = 0; r < 3; ++r) {
+                    clo[r] = std::min(clo[r], items[i].c[r]);
+                    chi[r] = std::max(chi[r], items[i].c[r]);
+                }
+            int axis = 0;
+            for (int r = 1; r < 3; ++r)
+                if (chi[r] - clo[r] > chi[axis] - clo[axis]) axis = r;
+            std::sort(items.begin() + (long)t.a, items.begin() + (long)t.e, [&](const IBox& x, const IBox& y) {
+                return x.c[axis] != y.c[axis] ? x.c[axis] < y.c[axis] : x.sec < y.sec;
+            });
+            const size_t mid = t.a + (t.e - t.a) / 2;
+            float l0[3], h0[3], l1[3], h1[3];
+            box_of(t.a, mid, l0, h0);
+            box_of(mid, t.e, l1, h1);
+            int refs[2];
+            const size_t ranges[2][2] = {{t.a, mid}, {mid, t.e}};
+            for (int side = 0; side < 2; ++side) {
+                const size_t a = ranges[side][0], e = ranges[side][1];
+                if (e - a == 1) {
+                    refs[side] = ~items[a].sec;
+                } else {
+                    const size_t id = nodes.size() / 4;
+                    nodes.resize(nodes.size() + 4);
+                    refs[side] = (int)id;
+                    todo.push_back({a, e, id, t.d + 1});
+                }
+            }
+            put_node(t.id, l0, h0, l1, h1, refs[0], refs[1]);
+        }
+    }
+    sc.tlas_count = (uint32_t)(nodes.size() / 4);
+    sc.tlas_depth = depth;
+    if (sc.blas_depth + sc.tlas_depth + 2 > SOLRT_BVH2_STACK) {
+        set_error("two-level depth %u + %u exceeds the traversal stack (%d)", sc.tlas_depth, sc.blas_depth,
+                  SOLRT_BVH2_STACK);
+        return SOLRT_ERR_CAPACITY;
+    }
+    std::vector<float4> table(4 * (size_t)S);
+    for (uint32_t s = 0; s < S; ++s) {
+        const float* Ti = sc.inst_host[s].transform_it;  // column-major; row r of its transpose = Ti[4r..4r+3]
+        for (int r = 0; r < 3; ++r) table[4 * s + r] = make_float4(Ti[4 * r], Ti[4 * r + 1], Ti[4 * r + 2], Ti[4 * r + 3]);
+        table[4 * s + 3] = make_float4(host_int_as_float(sc.blas_root.size() > s ? sc.blas_root[s] : -1), 0.0f,
+                                       0.0f, 0.0f);
+    }
+    cudaStream_t st = ctx.stream;
+    if (sc.tlas_count) {
+        SOLRT_TRY(sc.tlas.alloc(sizeof(float4) * nodes.size()));
+        SOLRT_CUDA(cudaMemcpyAsync(sc.tlas.ptr, nodes.data(), sizeof(float4) * nodes.size(), cudaMemcpyHostToDevice, st));
+    }
+    if (S) {
+        SOLRT_TRY(sc.inst_table.alloc(sizeof(float4) * table.size()));
+        SOLRT_CUDA(cudaMemcpyAsync(sc.inst_table.ptr, table.data(), sizeof(float4) * table.size(),
+                                   cudaMemcpyHostToDevice, st));
+    }
+    SOLRT_CUDA(cudaStreamSynchronize(st));  // the host arrays go out of scope
+    return SOLRT_OK;
+}
+
+// The BLASes of a two-level scene: one LBVH per non-empty section over its
+// object-space triangles, concatenated (nodes, then triangles in the
+// sections' order), then the TLAS.
+static solrt_status build_two_level(Context& ctx, Scene& sc) {
+    cudaStream_t st = ctx.stream;
+    const uint32_t S = sc.section_count;
+    if (!sc.opos.ptr || sc.sec_tri_first.size() != S || sc.inst_host.size() != S) {
+        set_error("a two-level BVH needs a scene created with SOLRT_BVH2_TWO_LEVEL (object-space geometry)");
+        return SOLRT_ERR_INVALID;
+    }
+    uint64_t total = 0;
+    for (uint32_t s = 0; s < S; ++s)
+        if (sc.sec_tri_count[s]) total += sc.sec_tri_count[s] > 1 ? sc.sec_tri_count[s] - 1 : 1;
+    SOLRT_TRY(sc.nodes.alloc(4 * sizeof(float4) * std::max<uint64_t>(total, 1)));
+    SOLRT_TRY(sc.tri_wt.alloc(3 * sizeof(float4) * (size_t)sc.tri_count));
+    sc.blas_box.assign(6 * (size_t)S, 0.0f);
+    sc.blas_root.assign(S, -1);
+    sc.blas_depth = 0;
+    uint32_t node_off = 0;
+    for (uint32_t s = 0; s < S; ++s) {
+        const uint32_t cnt = sc.sec_tri_count[s], first = sc.sec_tri_first[s];
+        if (cnt == 0) continue;
+        Lbvh L;
+        SOLRT_TRY(lbvh_build(ctx, sc.opos.as<float4>(), sc.tri_idx.as<uint4>() + first, cnt, first, L));
+        SOLRT_CUDA(cudaMemcpyAsync(sc.nodes.as<float4>() + 4 * (size_t)node_off, L.nodes.ptr,
+                                   4 * sizeof(float4) * (size_t)L.ni, cudaMemcpyDeviceToDevice, st));
+        SOLRT_CUDA(cudaMemcpyAsync(sc.tri_wt.as<float4>() + 3 * (size_t)first, L.tri_wt.ptr,
+                                   3 * sizeof(float4) * (size_t)cnt, cudaMemcpyDeviceToDevice, st));
+        k_offset_refs<<<blocks_for(L.ni, 256), 256, 0, st>>>(sc.nodes.as<float4>() + 4 * (size_t)node_off, L.ni,
+                                                            node_off, first);
+        ++ctx.launches;
+        SOLRT_CUDA(cudaGetLastError());
+        float4 box[2];
+        SOLRT_CUDA(cudaMemcpyAsync(box, L.nbox.ptr, sizeof(box), cudaMemcpyDeviceToHost, st));
+        SOLRT_CUDA(cudaStreamSynchronize(st));
+        const float b[6] = {box[0].x, box[0].y, box[0].z, box[1].x, box[1].y, box[1].z};
+        for (int i = 0; i < 6; ++i) sc.blas_box[6 * s + i] = b[i];
+        sc.blas_root[s] = (int32_t)node_off;
+        node_off += L.ni;
+        sc.blas_depth = std::max(sc.blas_depth, L.depth);
+    }
+    sc.info.node_count = node_off;
+    sc.info.node_bytes = 64ull * node_off;
+    SOLRT_TRY(build_tlas(ctx, sc));
+    sc.info.depth = sc.blas_depth + sc.tlas_depth;
+    return SOLRT_OK;
+}
+
+// The single-level kinds: one LBVH over the world-space triangles, then the
+// wide collapse or the 16-bit quantisation when asked.
+static solrt_status build_single_level(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
+    const uint32_t n = sc.tri_count;
+    Lbvh L;
+    SOLRT_TRY(lbvh_build(ctx, sc.vpos.as<float4>(), sc.tri_idx.as<uint4>(), n, 0u, L));
+    const uint32_t ni = L.ni;
     if (desc.kind == SOLRT_BVH8_Q8 || desc.kind == SOLRT_BVH4_Q8 || desc.kind == SOLRT_BVH8_F32) {
         const uint32_t width = desc.kind == SOLRT_BVH4_Q8 ? 4u : 8u;
         const bool f32 = desc.kind == SOLRT_BVH8_F32;
         Bvh8BuildInput in;
         in.n = n;
-        in.child = child.as<uint32_t>();
-        in.nbox = nbox.as<float4>();
-        in.range = range.as<uint2>();
-        in.tri_wt_leaf = sc.tri_wt.as<float4>();
+        in.child = L.child.as<uint32_t>();
+        in.nbox = L.nbox.as<float4>();
+        in.range = L.range.as<uint2>();
+        in.tri_wt_leaf = L.tri_wt.as<float4>();
         in.leaf_max = desc.leaf_max == 0 ? 1u : std::min(3u, desc.leaf_max);
-        in.par_int = par_int.as<uint32_t>();
-        in.par_leaf = par_leaf.as<uint32_t>();
+        in.par_int = L.par_int.as<uint32_t>();
+        in.par_leaf = L.par_leaf.as<uint32_t>();
         in.sah = (desc.flags & SOLRT_BVH_SAH) != 0;
         DeviceBuffer tri8;
         uint32_t node_count = 0, depth8 = 0;
         SOLRT_TRY(build_wide(ctx, in, width, f32, sc.nodes, tri8, &node_count, &depth8));
-        sc.tri_wt.release();
-        sc.tri_wt.ptr = tri8.ptr;
-        sc.tri_wt.bytes = tri8.bytes;
-        tri8.ptr = nullptr;
-        tri8.bytes = 0;
+        sc.tri_wt.adopt(tri8);
         sc.info.node_count = node_count;
         sc.info.depth = depth8;
         sc.info.node_bytes = (uint64_t)node_count * (width == 4 ? 64u : (f32 ? 224u : 80u));
         SOLRT_TRY(check_wide_depth(width, depth8));
     } else {
-        sc.nodes.ptr = bvh2_nodes.ptr;
-        sc.nodes.bytes = bvh2_nodes.bytes;
-        bvh2_nodes.ptr = nullptr;
-        bvh2_nodes.bytes = 0;
+        sc.nodes.adopt(L.nodes);
+        sc.tri_wt.adopt(L.tri_wt);
         sc.info.node_count = ni;
         sc.info.node_bytes = (uint64_t)ni * 64u;
         if (desc.kind == SOLRT_BVH2_Q16) {
-            SOLRT_TRY(quantize_bvh2(ctx, sc.nodes, nbox.as<float4>(), ni));
+            SOLRT_TRY(quantize_bvh2(ctx, sc.nodes, L.nbox.as<float4>(), ni));
             sc.info.node_bytes = 32ull * ((uint64_t)ni + 1);
         }
-        unsigned int dh = 0;
-        SOLRT_CUDA(cudaMemcpyAsync(&dh, depth.ptr, sizeof(dh), cudaMemcpyDeviceToHost, st));
-        SOLRT_CUDA(cudaStreamSynchronize(st));
-        sc.info.depth = n > 1 ? dh : 1;
+        sc.info.depth = L.depth;
     }
-    sc.desc = desc;
     if (sc.dynamic) {  // the topology stays for solrt_scene_regenerate(REFIT)
-        sc.topo_order.adopt(vals[cur]);
-        sc.topo_child.adopt(child);
-        sc.topo_par_int.adopt(par_int);
-        sc.topo_par_leaf.adopt(par_leaf);
-        sc.topo_range.adopt(range);
+        sc.topo_order.adopt(L.order);
+        sc.topo_child.adopt(L.child);
+        sc.topo_par_int.adopt(L.par_int);
+        sc.topo_par_leaf.adopt(L.par_leaf);
+        sc.topo_range.adopt(L.range);
     }
+    return SOLRT_OK;
+}
+
+// Builds the LBVH of `sc` (and the wide collapse or the 16-bit quantisation
+// when asked). Scratch is allocated for the duration of the build.
+// Synchronises.
+solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
+    const uint32_t n = sc.tri_count;
+    cudaStream_t st = ctx.stream;
+    sc.info = solrt_bvh_info{};
+    sc.info.kind = desc.kind;
+    sc.info.tri_count = n;
+    sc.nodes.release();
+    sc.tri_wt.release();
+    sc.desc = desc;
+    if (n == 0) return SOLRT_OK;
+    cudaGetLastError();  // launch errors below must be this call's own
+
+    SOLRT_CUDA(cudaEventRecord(ctx.ev0, st));
+    if (desc.kind == SOLRT_BVH2_TWO_LEVEL) SOLRT_TRY(build_two_level(ctx, sc));
+    else SOLRT_TRY(build_single_level(ctx, sc, desc));
     sc.info.tri_bytes = sc.tri_wt.bytes;
     sc.info.shade_bytes = sc.vpos.bytes + sc.vnrm.bytes + sc.vcol.bytes + sc.tri_idx.bytes + sc.materials.bytes;
     SOLRT_CUDA(cudaEventRecord(ctx.ev1, st));
@@ -768,6 +1012,18 @@ solrt_status regenerate_scene(Context& ctx, Scene& sc, uint32_t mode) {
             sc.instances.as<solrt_instance>(), sc.vertex_count, sc.vpos.as<float4>(), sc.vnrm.as<float4>());
         ++ctx.launches;
         SOLRT_CUDA(cudaGetLastError());
+    }
+    if (sc.info.kind == SOLRT_BVH2_TWO_LEVEL) {  // BLASes stay; a new TLAS for the instances
+        if (sc.tri_count == 0) return SOLRT_OK;
+        SOLRT_CUDA(cudaEventRecord(ctx.ev0, st));
+        SOLRT_TRY(build_tlas(ctx, sc));
+        SOLRT_CUDA(cudaEventRecord(ctx.ev1, st));
+        SOLRT_CUDA(cudaEventSynchronize(ctx.ev1));
+        float ms = 0.0f;
+        SOLRT_CUDA(cudaEventElapsedTime(&ms, ctx.ev0, ctx.ev1));
+        sc.info.build_ms = ms;
+        sc.info.depth = sc.blas_depth + sc.tlas_depth;
+        return SOLRT_OK;
     }
     if (mode == SOLRT_REGEN_REFIT && sc.tri_count > 0 && sc.topo_order.ptr && sc.nodes.ptr)
         return refit_bvh(ctx, sc);

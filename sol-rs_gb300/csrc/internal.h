@@ -248,11 +248,28 @@ struct Scene {
     uint32_t section_count = 0;
     DeviceBuffer opos, onrm, vsec_start, instances;
     DeviceBuffer topo_order, topo_child, topo_par_int, topo_par_leaf, topo_range;
+    // Host copies: each section's first triangle and triangle count, and the
+    // staged instances (one per section).
+    std::vector<uint32_t> sec_tri_first, sec_tri_count;
+    std::vector<solrt_instance> inst_host;
+    // SOLRT_BVH2_TWO_LEVEL: one BLAS per section over its object-space
+    // triangles (concatenated in `nodes` / `tri_wt`), their object-space
+    // root boxes (6 floats per section) and root nodes (-1: empty section),
+    // and the TLAS over the instances with the instance table.
+    std::vector<float> blas_box;
+    std::vector<int32_t> blas_root;
+    uint32_t blas_depth = 0, tlas_count = 0, tlas_depth = 0;
+    DeviceBuffer tlas, inst_table;
     DevScene view() const {
         DevScene d;
         d.tri_count = tri_count;
         d.bvh_kind = info.kind;
         d.node_count = info.node_count;
+        const bool two = info.kind == SOLRT_BVH2_TWO_LEVEL;
+        d.tlas_count = two ? tlas_count : 0u;
+        d.inst_count = two ? section_count : 0u;
+        d.tlas = two ? tlas.as<float4>() : nullptr;
+        d.inst = two ? inst_table.as<float4>() : nullptr;
         d.vpos = vpos.as<float4>();
         d.vnrm = vnrm.as<float4>();
         d.vcol = vcol.as<float4>();

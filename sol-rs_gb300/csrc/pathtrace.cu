@@ -23,6 +23,7 @@
 // bit.
 #include <algorithm>
 
+#include "bvh2_2l.cuh"
 #include "bvh2_ww.cuh"
 #include "bvh4_ww.cuh"
 #include "bvh8_traverse.cuh"
@@ -184,6 +185,7 @@ __global__ void __launch_bounds__(128) k_megakernel(const DevJob* __restrict__ j
                 else if (KIND == SOLRT_BVH8_F32) trace_bvh8<false, true>(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, fb_ef[1]);
                 else if (KIND == SOLRT_BVH4_Q8) trace_bvh4_ray(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, fb_ef[1]);
                 else if (KIND == SOLRT_BVH2_Q16) trace_bvh2_ray<true>(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, fb_ef[1]);
+                else if (KIND == SOLRT_BVH2_TWO_LEVEL) trace_bvh2_2l_ray(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, fb_ef[1]);
                 else trace_bvh2_ray(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, fb_ef[1]);
                 ++segs;
                 float4 on, dn;
@@ -256,6 +258,7 @@ __device__ __forceinline__ void trace_one(const TravScene& ts, float ox, float o
     else if (KIND == SOLRT_BVH8_F32) trace_bvh8<false, true>(ts, ox, oy, oz, dx, dy, dz, tmin, tmax, h, cnt, ef);
     else if (KIND == SOLRT_BVH4_Q8) trace_bvh4_ray(ts, ox, oy, oz, dx, dy, dz, tmin, tmax, h, cnt, ef);
     else if (KIND == SOLRT_BVH2_Q16) trace_bvh2_ray<true>(ts, ox, oy, oz, dx, dy, dz, tmin, tmax, h, cnt, ef);
+    else if (KIND == SOLRT_BVH2_TWO_LEVEL) trace_bvh2_2l_ray(ts, ox, oy, oz, dx, dy, dz, tmin, tmax, h, cnt, ef);
     else trace_bvh2_ray(ts, ox, oy, oz, dx, dy, dz, tmin, tmax, h, cnt, ef);
 }
 
@@ -839,12 +842,14 @@ static solrt_status render_sibling(Context& ctx, const Scene& sc, const solrt_ca
         else if (kind == SOLRT_BVH4_Q8) k_debug<SOLRT_BVH4_Q8><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
         else if (kind == SOLRT_BVH8_F32) k_debug<SOLRT_BVH8_F32><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
         else if (kind == SOLRT_BVH2_Q16) k_debug<SOLRT_BVH2_Q16><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
+        else if (kind == SOLRT_BVH2_TWO_LEVEL) k_debug<SOLRT_BVH2_TWO_LEVEL><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
         else k_debug<SOLRT_BVH2><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
     } else {
         if (kind == SOLRT_BVH8_Q8) k_ao<SOLRT_BVH8_Q8><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
         else if (kind == SOLRT_BVH4_Q8) k_ao<SOLRT_BVH4_Q8><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
         else if (kind == SOLRT_BVH8_F32) k_ao<SOLRT_BVH8_F32><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
         else if (kind == SOLRT_BVH2_Q16) k_ao<SOLRT_BVH2_Q16><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
+        else if (kind == SOLRT_BVH2_TWO_LEVEL) k_ao<SOLRT_BVH2_TWO_LEVEL><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
         else k_ao<SOLRT_BVH2><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(dj, stats);
     }
     ++ctx.launches;
@@ -877,6 +882,8 @@ solrt_status render_frame(Context& ctx, const Scene& sc, const solrt_camera& cam
         k_megakernel<SOLRT_BVH8_F32><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(b.d_jobs.as<DevJob>(), ctx.stats.as<DevStats>());
     else if (b.kind == SOLRT_BVH2_Q16)
         k_megakernel<SOLRT_BVH2_Q16><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(b.d_jobs.as<DevJob>(), ctx.stats.as<DevStats>());
+    else if (b.kind == SOLRT_BVH2_TWO_LEVEL)
+        k_megakernel<SOLRT_BVH2_TWO_LEVEL><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(b.d_jobs.as<DevJob>(), ctx.stats.as<DevStats>());
     else
         k_megakernel<SOLRT_BVH2><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(b.d_jobs.as<DevJob>(), ctx.stats.as<DevStats>());
     k_finalize<<<cdiv(npix, 256), 256, 0, ctx.stream>>>(b.d_jobs.as<DevJob>(), b.d_job_pix.as<uint32_t>(), 1u, npix);

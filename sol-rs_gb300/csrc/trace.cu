@@ -3,11 +3,13 @@
 // (assets/glsl/pathtrace.rgen:65-76). Persistent kernels: one grid of
 // (SMs x resident blocks) whose warps take rays from an atomic work counter,
 // so the queue length can stay on the device (no host round trip).
-//   BVH2: while-while traversal with per-lane refill (bvh2_ww.cuh).
+//   BVH2: while-while traversal with per-lane refill (bvh2_ww.cuh); two-level
+//   scenes: the same loop over a TLAS and object-space BLASes (bvh2_2l.cuh).
 //   BVH8 / BVH4: the same warp-uniform organisation over quantised wide
 //   nodes (bvh8_ww.cuh, bvh4_ww.cuh).
 #include <algorithm>
 
+#include "bvh2_2l.cuh"
 #include "bvh2_ww.cuh"
 #include "bvh4_ww.cuh"
 #include "bvh8_ww.cuh"
@@ -59,6 +61,10 @@ struct QueueIO {
         ts.tris = s->tri_wt;
         ts.node_count = s->node_count;
         ts.tri_count = s->tri_count;
+        ts.tlas = s->tlas;
+        ts.inst = s->inst;
+        ts.tlas_count = s->tlas_count;
+        ts.inst_count = s->inst_count;
     }
     SOLRT_D void store(uint32_t i, const HitRec& h) const {
         hits[i] = make_float4(h.t, __uint_as_float(h.prim), h.u, h.v);
@@ -95,6 +101,8 @@ __global__ void __launch_bounds__(kBlock, SOLRT_EXTEND_MINB) k_extend(IO io, con
         extend_bvh2_ww<IO, kCount, kBlock, kSmem, false>(io, n, work, cnt, ef);
     } else if constexpr (KIND == SOLRT_BVH2_Q16) {
         extend_bvh2_ww<IO, kCount, kBlock, kSmem, true>(io, n, work, cnt, ef);
+    } else if constexpr (KIND == SOLRT_BVH2_TWO_LEVEL) {
+        extend_bvh2_2l_ww<IO, kCount, kBlock, kSmem>(io, n, work, cnt, ef);
     } else if constexpr (KIND == SOLRT_BVH4_Q8) {
         extend_bvh4_ww<IO, kCount, kBlock, kSmem>(io, n, work, cnt, ef);
     } else if constexpr (KIND == SOLRT_BVH8_F32) {
@@ -159,6 +167,8 @@ solrt_status launch_extend(Context& ctx, uint32_t kind, const DevJob* jobs, cons
     else if (kind == SOLRT_BVH4_Q8) SOLRT_TRY((launch_tuned<SOLRT_BVH4_Q8>(ctx, io, count, 0, 0, work, st)));
     else if (kind == SOLRT_BVH8_F32) SOLRT_TRY((launch_tuned<SOLRT_BVH8_F32>(ctx, io, count, 0, 0, work, st)));
     else if (kind == SOLRT_BVH2_Q16) SOLRT_TRY((launch_tuned<SOLRT_BVH2_Q16>(ctx, io, count, 0, 0, work, st)));
+    else if (kind == SOLRT_BVH2_TWO_LEVEL)
+        SOLRT_TRY((launch_tuned<SOLRT_BVH2_TWO_LEVEL>(ctx, io, count, 0, 0, work, st)));
     else SOLRT_TRY((launch_tuned<SOLRT_BVH2>(ctx, io, count, 0, 0, work, st)));
     ++ctx.launches;
     SOLRT_CUDA(cudaGetLastError());
@@ -176,6 +186,8 @@ solrt_status launch_trace_rays(Context& ctx, const Scene& sc, const solrt_ray* r
     else if (d.bvh_kind == SOLRT_BVH4_Q8) SOLRT_TRY((launch_tuned<SOLRT_BVH4_Q8>(ctx, io, nullptr, n, n, work, st)));
     else if (d.bvh_kind == SOLRT_BVH8_F32) SOLRT_TRY((launch_tuned<SOLRT_BVH8_F32>(ctx, io, nullptr, n, n, work, st)));
     else if (d.bvh_kind == SOLRT_BVH2_Q16) SOLRT_TRY((launch_tuned<SOLRT_BVH2_Q16>(ctx, io, nullptr, n, n, work, st)));
+    else if (d.bvh_kind == SOLRT_BVH2_TWO_LEVEL)
+        SOLRT_TRY((launch_tuned<SOLRT_BVH2_TWO_LEVEL>(ctx, io, nullptr, n, n, work, st)));
     else SOLRT_TRY((launch_tuned<SOLRT_BVH2>(ctx, io, nullptr, n, n, work, st)));
     ++ctx.launches;
     SOLRT_CUDA(cudaGetLastError());

@@ -23,6 +23,10 @@ struct DevScene {
     uint32_t tri_count;
     uint32_t bvh_kind;
     uint32_t node_count;
+    uint32_t tlas_count;      // SOLRT_BVH2_TWO_LEVEL: TLAS nodes (0: nothing to hit)
+    uint32_t inst_count;      // SOLRT_BVH2_TWO_LEVEL: entries of `inst` (one per section)
+    const float4* tlas;       // SOLRT_BVH2_TWO_LEVEL: BVH2 nodes over instances (leaf ~section)
+    const float4* inst;       // SOLRT_BVH2_TWO_LEVEL: per section inverse-transform rows 0-2, BLAS root
     const float4* vpos;       // world position per vertex (.w unused)
     const float4* vnrm;       // world normal (transform_it applied, unnormalised)
     const float4* vcol;       // vertex colour
@@ -39,9 +43,15 @@ struct TravScene {
     const float4* tris;
     uint32_t node_count;
     uint32_t tri_count;
+    const float4* tlas;   // two-level scenes only (see DevScene)
+    const float4* inst;
+    uint32_t tlas_count;
+    uint32_t inst_count;
 };
 
-SOLRT_HD TravScene trav_scene(const DevScene& s) { return TravScene{s.nodes, s.tri_wt, s.node_count, s.tri_count}; }
+SOLRT_HD TravScene trav_scene(const DevScene& s) {
+    return TravScene{s.nodes, s.tri_wt, s.node_count, s.tri_count, s.tlas, s.inst, s.tlas_count, s.inst_count};
+}
 
 struct HitRec {
     float t;

@@ -126,6 +126,6 @@ def bvh_args(solrt_mod, name):
 
 
 def bvh_kind(solrt_mod, name):
-    """"bvh2" / "bvh2q" / "bvh4" / "bvh8" / "bvh8f" -> solrt BVH kind."""
-    return {"bvh2": solrt_mod.BVH2, "bvh2q": solrt_mod.BVH2_Q16, "bvh4": solrt_mod.BVH4_Q8,
-            "bvh8": solrt_mod.BVH8_Q8, "bvh8f": solrt_mod.BVH8_F32}[name]
+    """"bvh2" / "bvh2q" / "bvh2t" / "bvh4" / "bvh8" / "bvh8f" -> solrt BVH kind."""
+    return {"bvh2": solrt_mod.BVH2, "bvh2q": solrt_mod.BVH2_Q16, "bvh2t": solrt_mod.BVH2_TWO_LEVEL,
+            "bvh4": solrt_mod.BVH4_Q8, "bvh8": solrt_mod.BVH8_Q8, "bvh8f": solrt_mod.BVH8_F32}[name]

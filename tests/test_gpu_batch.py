@@ -55,7 +55,7 @@ def _alone(solrt, ctx, jobs, frames=1):
 
 
 @pytest.mark.parametrize("graph", [False, True])
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh4", "bvh8", "bvh8f"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh2t", "bvh4", "bvh8", "bvh8f"])
 def test_batch_equals_alone(solrt, ctx, bvh, graph):
     kind = bvh_kind(solrt, bvh)
     jobs = _make(solrt, ctx, kind)
@@ -124,7 +124,7 @@ def test_batch_rejects_mixed_bvh_kinds(solrt, ctx):
         solrt.Batch(ctx, [(a, ia, cam, p), (b, ib, cam, p)])
 
 
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh4", "bvh8", "bvh8f"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh2t", "bvh4", "bvh8", "bvh8f"])
 def test_autotune_keeps_images(solrt, bvh):
     """solrt_batch_autotune times every extend block size x shared stack
     depth and three pass sizes; the batch re-planned with the winner renders

@@ -41,7 +41,7 @@ def _render(solrt, ctx, sc, cam, w, h, p):
 
 
 @pytest.mark.parametrize("mode", ["rebuild", "refit"])
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh4", "bvh8", "bvh8f"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh2t", "bvh4", "bvh8", "bvh8f"])
 def test_regenerate_matches_fresh_scene(solrt, oracle, ctx, bvh, mode):
     kind = bvh_kind(solrt, bvh)
     regen = solrt.REGEN_REBUILD if mode == "rebuild" else solrt.REGEN_REFIT
@@ -66,7 +66,7 @@ def test_regenerate_matches_fresh_scene(solrt, oracle, ctx, bvh, mode):
             nb, tb = fresh.bvh_export()
             assert np.array_equal(na, nb) and np.array_equal(ta, tb)
         if f == 2:
-            oa, _, _ = oracle.OracleScene(moved).render(cam, p)
+            oa, _, _ = oracle.OracleScene(moved, two_level=kind == solrt.BVH2_TWO_LEVEL).render(cam, p)
             assert np.array_equal(a.view(np.uint32), oa.view(np.uint32))
         fresh.close()
     assert ctx.stats().error_flags == 0

@@ -25,7 +25,7 @@ def _transformed_glb(solrt, path):
     return solrt.load_scene(str(path))
 
 
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh4", "bvh8", "bvh8f"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh2t", "bvh4", "bvh8", "bvh8f"])
 def test_gltf_render_matches_oracle(solrt, oracle, ctx, tmp_path, bvh):
     g = _transformed_glb(solrt, tmp_path / "cornell.glb")
     w, h = 40, 32
@@ -38,7 +38,7 @@ def test_gltf_render_matches_oracle(solrt, oracle, ctx, tmp_path, bvh):
     ctx.reset_stats()
     solrt.Renderer(ctx).cmd_trace_rays(sc, cam, p, img)
     ga, _ = img.read()
-    oa, _, st = oracle.OracleScene(g.data).render(cam, p)
+    oa, _, st = oracle.OracleScene(g.data, two_level=kind == solrt.BVH2_TWO_LEVEL).render(cam, p)
     assert np.array_equal(ga.view(np.uint32), oa.view(np.uint32))
     assert ctx.stats().segments == st.segments and ctx.stats().error_flags == 0
     assert ga[..., :3].mean() > 0

@@ -15,7 +15,7 @@ def blue_noise(h=64, w=48, seed=17):
     return np.random.default_rng(seed).integers(0, 256, (h, w, 4), dtype=np.uint8)
 
 
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh4", "bvh8", "bvh8f"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh2t", "bvh4", "bvh8", "bvh8f"])
 @pytest.mark.parametrize("scene", ["cornell", "transformed", "soup"])
 def test_debug_matches_oracle(solrt, oracle, ctx, bvh, scene):
     data = {"cornell": S.cornell, "transformed": transformed_cornell, "soup": lambda: S.soup(20000, seed=3)}[scene]()
@@ -28,7 +28,7 @@ def test_debug_matches_oracle(solrt, oracle, ctx, bvh, scene):
     ctx.reset_stats()
     solrt.Renderer(ctx).cmd_trace_rays(sc, cam, p, img)
     ga, g8 = img.read()
-    oa, o8, st = oracle.OracleScene(data).render(cam, p)
+    oa, o8, st = oracle.OracleScene(data, two_level=kind == solrt.BVH2_TWO_LEVEL).render(cam, p)
     assert np.array_equal(ga.view(np.uint32), oa.view(np.uint32))
     assert np.array_equal(g8, o8)
     s = ctx.stats()
@@ -37,7 +37,7 @@ def test_debug_matches_oracle(solrt, oracle, ctx, bvh, scene):
     assert hit.any()
 
 
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh4", "bvh8", "bvh8f"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh2t", "bvh4", "bvh8", "bvh8f"])
 def test_ao_matches_oracle(solrt, oracle, ctx, bvh):
     data = S.cornell()
     w, h = 40, 32
@@ -47,7 +47,7 @@ def test_ao_matches_oracle(solrt, oracle, ctx, bvh):
     ctx.set_blue_noise(noise)
     sc = solrt.SceneDescription(ctx, data, bvh=kind)
     img = solrt.Image(ctx, w, h)
-    o = oracle.OracleScene(data)
+    o = oracle.OracleScene(data, two_level=kind == solrt.BVH2_TWO_LEVEL)
     acc = np.zeros((h, w, 4), np.float32)
     seg = 0
     ctx.reset_stats()

@@ -61,7 +61,7 @@ def _render_both(solrt, oracle, ctx, data, w, h, kw, frames=2, bvh=None, sah=Fal
     mode = kw.get("accum_mode", solrt.ACCUM_REF_MIX)
     img = solrt.Image(ctx, w, h, mode)
     r = solrt.Renderer(ctx)
-    o = oracle.OracleScene(data)
+    o = oracle.OracleScene(data, two_level=bvh == solrt.BVH2_TWO_LEVEL)
     acc = np.zeros((h, w, 4), np.float32)
     ks = np.zeros((h, w, 4), np.float32) if mode == solrt.ACCUM_KAHAN else None
     kc = np.zeros((h, w, 4), np.float32) if mode == solrt.ACCUM_KAHAN else None
@@ -78,7 +78,7 @@ def _render_both(solrt, oracle, ctx, data, w, h, kw, frames=2, bvh=None, sah=Fal
     return ga, g8, acc, rgba_o, stats, seg_o
 
 
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh4", "bvh8", "bvh8f"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh2t", "bvh4", "bvh8", "bvh8f"])
 @pytest.mark.parametrize("name", ["cornell_lambert", "cornell_ref_stream", "cornell_ref_sky", "transformed",
                                   "soup_gradient", "tunnel_kahan"])
 def test_render_bit_exact(solrt, oracle, ctx, name, bvh):
@@ -103,7 +103,7 @@ def test_render_bit_exact_sah_collapse(solrt, oracle, ctx, name, bvh):
     assert stats.segments == seg_o and stats.error_flags == 0
 
 
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh4", "bvh8", "bvh8f"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh2t", "bvh4", "bvh8", "bvh8f"])
 @pytest.mark.parametrize("name", ["cornell_lambert", "cornell_ref_stream", "soup_gradient", "tunnel_kahan"])
 def test_megakernel_equals_wavefront(solrt, oracle, ctx, name, bvh):
     """The per-pixel megakernel (the reference's loop structure) renders the

@@ -13,12 +13,12 @@ pytestmark = pytest.mark.gpu
 def _both(solrt, oracle, ctx, data, rays, bvh):
     sc = solrt.SceneDescription(ctx, data, **bvh)
     g = sc.trace_rays(rays)
-    o = oracle.OracleScene(data)
+    o = oracle.OracleScene(data, two_level=bvh["bvh"] == solrt.BVH2_TWO_LEVEL)
     ref, _ = o.trace(rays, brute=True)
     return g, ref
 
 
-BVHS = ["bvh2", "bvh2q", "bvh4", "bvh8", "bvh8f", "bvh4s", "bvh8s"]
+BVHS = ["bvh2", "bvh2q", "bvh2t", "bvh4", "bvh8", "bvh8f", "bvh4s", "bvh8s"]
 
 
 def _kind(solrt, name):

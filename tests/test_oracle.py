@@ -237,3 +237,28 @@ def test_ao_integrator_properties(oracle, solrt):
     assert np.allclose(acc[..., :3], 0.5 * (a0[..., :3] + a1[..., :3]), rtol=1e-5, atol=1e-6)
     with pytest.raises(ValueError):
         sc.render(cam, p0)                        # no texture
+
+
+def test_two_level_oracle(oracle):
+    """Two-level mode: with identity instances every ray meets the same
+    triangle at the same t as in the flattened scene (object space = world
+    space); with transformed sections the same triangles are hit, at t
+    within rounding of the flattened ones."""
+    from helpers import transformed_cornell
+    d = S.cornell()
+    rays = np.concatenate([random_rays(20000, 0.01, 0.99, seed=81), edge_rays(d, 5000, seed=82)])
+    flat, _ = oracle.OracleScene(d).trace(rays, brute=True)
+    two, _ = oracle.OracleScene(d, two_level=True).trace(rays, brute=True)
+    assert hits_equal(flat, two)
+    d = transformed_cornell()
+    o = oracle.OracleScene(d)
+    tw, _ = o.world()
+    lo, hi = tw[..., 0, :3].reshape(-1, 3).min(0), tw[..., 0, :3].reshape(-1, 3).max(0)
+    rays = random_rays(20000, 0.0, 1.0, seed=83)
+    rays["origin"] = (lo + (hi - lo) * rays["origin"]).astype(np.float32)
+    flat, _ = o.trace(rays, brute=True)
+    two, _ = oracle.OracleScene(d, two_level=True).trace(rays, brute=True)
+    same = flat["prim"] == two["prim"]
+    assert same.mean() > 0.995
+    hit = same & (flat["prim"] != solrt.NO_HIT)
+    assert np.allclose(flat["t"][hit], two["t"][hit], rtol=1e-4, atol=1e-5)
