@@ -73,6 +73,14 @@ def workload(name):
         cfg = {"workload": "procedural tunnel 2048x1024 segments (4.19M tris), 2560x1440, 128 spp, max depth 8, "
                            "Kahan accumulation, sky", "tris": data.tri_count, "width": 2560, "height": 1440,
                "spp": 128, "max_depth": 8}
+    elif name == "instances":
+        data = S.instanced_soups(4, 16384, seed=5)
+        kw = dict(width=1920, height=1080, spp=64, max_bounces=4, miss_mode=solrt.MISS_GRADIENT,
+                  material_mode=solrt.MATERIAL_LAMBERT, rng_mode=solrt.RNG_PER_SAMPLE, seed=5,
+                  accum_mode=solrt.ACCUM_REF_MIX)
+        cfg = {"workload": "64 instanced sections of 16384-triangle soups (1.05M tris) in a 4^3 grid, 1920x1080, "
+                           "64 spp, max depth 4, gradient sky, Lambert", "tris": data.tri_count, "width": 1920,
+               "height": 1080, "spp": 64, "max_depth": 4}
     else:
         raise SystemExit("unknown workload %s" % name)
     return data, kw, cfg
@@ -307,8 +315,8 @@ def run_batch(args, world, rank, local, pg, njobs=None, steps=None, emit=True):
     import torch
     solrt = importlib.import_module("sol-rs_gb300")
     S = solrt.scenes
-    bvh = {"bvh2": solrt.BVH2, "bvh2q": solrt.BVH2_Q16, "bvh4": solrt.BVH4_Q8, "bvh8": solrt.BVH8_Q8,
-           "bvh8f": solrt.BVH8_F32}[args.bvh]
+    bvh = {"bvh2": solrt.BVH2, "bvh2q": solrt.BVH2_Q16, "bvh2t": solrt.BVH2_TWO_LEVEL, "bvh4": solrt.BVH4_Q8,
+           "bvh8": solrt.BVH8_Q8, "bvh8f": solrt.BVH8_F32}[args.bvh]
     njobs = args.jobs if njobs is None else njobs
     steps = args.steps if steps is None else steps
     ctx = solrt.Context(local)
@@ -525,8 +533,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="solrt", choices=["solrt", "reference"])
-    ap.add_argument("--workload", default="soup", choices=["soup", "cornell", "tunnel", "batch", "serve"])
-    ap.add_argument("--bvh", default="bvh2", choices=["bvh2", "bvh2q", "bvh4", "bvh8", "bvh8f"])
+    ap.add_argument("--workload", default="soup", choices=["soup", "cornell", "tunnel", "instances", "batch", "serve"])
+    ap.add_argument("--bvh", default="bvh2", choices=["bvh2", "bvh2q", "bvh2t", "bvh4", "bvh8", "bvh8f"])
     ap.add_argument("--sah", action="store_true", help="wide BVH kinds: SAH-optimal collapse")
     ap.add_argument("--jobs", type=int, default=256)
     ap.add_argument("--rate", type=float, default=6.0, help="serve: Poisson arrival rate, jobs/s")
@@ -564,8 +572,8 @@ def main():
         if getattr(args, key):
             kw[key] = getattr(args, key)
             cfg = dict(cfg, **{key: getattr(args, key)}, reduced=True)
-    bvh = {"bvh2": solrt.BVH2, "bvh2q": solrt.BVH2_Q16, "bvh4": solrt.BVH4_Q8, "bvh8": solrt.BVH8_Q8,
-           "bvh8f": solrt.BVH8_F32}[args.bvh]
+    bvh = {"bvh2": solrt.BVH2, "bvh2q": solrt.BVH2_Q16, "bvh2t": solrt.BVH2_TWO_LEVEL, "bvh4": solrt.BVH4_Q8,
+           "bvh8": solrt.BVH8_Q8, "bvh8f": solrt.BVH8_F32}[args.bvh]
     c = data.camera
     cam = solrt.camera_look_at(c["eye"], c["center"], c["up"], c["vfov"], kw["width"] / kw["height"])
     params = solrt.render_params(**kw)

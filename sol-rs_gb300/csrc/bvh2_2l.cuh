@@ -155,6 +155,7 @@ SOLRT_D void extend_bvh2_2l_ww(const IO& io, uint32_t n, unsigned int* work, Tra
             bool h0, h1;
             int c0, c1;
             bvh2_node_step<false>(arr, node, ix, iy, iz, nox, noy, noz, tmin, best.t, h0, t0, h1, t1, c0, c1);
+            h1 = h1 && c1 != c0;  // a node whose two children are the same (one instance, one triangle)
             if (h0 && h1) {
                 const bool swap = t1 < t0;
                 if (sp <= SOLRT_BVH2_STACK) stack.put(sp++, swap ? c0 : c1);
@@ -254,6 +255,7 @@ SOLRT_D void trace_bvh2_2l_ray(const TravScene& ts, float ox, float oy, float oz
             bool h0, h1;
             int c0, c1;
             bvh2_node_step<false>(arr, node, ix, iy, iz, nox, noy, noz, tmin, best.t, h0, t0, h1, t1, c0, c1);
+            h1 = h1 && c1 != c0;
             if (h0 && h1) {
                 const bool swap = t1 < t0;
                 if (sp <= SOLRT_BVH2_STACK) stack[sp++] = swap ? c0 : c1;

@@ -89,8 +89,15 @@ struct RayFileIO {
 // n = *count when count != nullptr (queue length on the device), else n_static.
 // kBlock threads per block; kSmem traversal-stack slots per thread in
 // shared memory (BVH2).
+// Two-level scenes: registers capped at 64 so that 1024 threads fit an SM
+// (as the single-level BVH2 kernel does by itself).
+template <int KIND, int kBlock>
+constexpr int extend_min_blocks() {
+    return KIND == SOLRT_BVH2_TWO_LEVEL ? 1024 / kBlock : SOLRT_EXTEND_MINB;
+}
+
 template <int KIND, class IO, bool kCount, int kBlock, int kSmem>
-__global__ void __launch_bounds__(kBlock, SOLRT_EXTEND_MINB) k_extend(IO io, const unsigned int* __restrict__ count,
+__global__ void __launch_bounds__(kBlock, (extend_min_blocks<KIND, kBlock>())) k_extend(IO io, const unsigned int* __restrict__ count,
                                                                       uint32_t n_static, unsigned int* __restrict__ work,
                                                                       DevStats* stats) {
     const uint32_t n = count ? *count : n_static;

@@ -171,6 +171,52 @@ def soup(n_tris, seed=2, lo=0.0, hi=1.0, sigma=0.005, builder=None):
     return b
 
 
+def rotation(axis, deg):
+    """3x3 rotation about a unit axis (Rodrigues), FP64."""
+    a = np.asarray(axis, np.float64)
+    a = a / np.linalg.norm(a)
+    t = np.radians(deg)
+    K = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+    return np.eye(3) + np.sin(t) * K + (1 - np.cos(t)) * (K @ K)
+
+
+def instance_of(M, ident):
+    """SceneInstance of a 4x4 row-major FP64 transform: transform and
+    inverse-transpose rounded to FP32, stored column-major (glam layout)."""
+    inst = np.zeros((), INSTANCE_DTYPE)
+    inst["id"] = ident
+    inst["transform"] = M.astype(np.float32).T.reshape(-1)
+    inst["transform_it"] = np.linalg.inv(M.astype(np.float32).astype(np.float64)).T.astype(np.float32).T.reshape(-1)
+    return inst
+
+
+def instanced_soups(n_side=4, tris_each=16384, seed=5, angle=0.0):
+    """n_side^3 sections, each a triangle soup of `tris_each` triangles in the
+    unit cube of its own object space, placed by its instance in one cell of
+    an n_side^3 grid over [0, 1]^3 (scaled by 1 / n_side, turned by a random
+    rotation about its centre plus `angle` degrees about y): the per-section
+    instances of SceneDescription::from_meshes (src/ray/mod.rs:59-156)."""
+    rng = np.random.default_rng(seed)
+    b = _Builder()
+    insts = []
+    k = 0
+    for ix in range(n_side):
+        for iy in range(n_side):
+            for iz in range(n_side):
+                soup(tris_each, seed=seed * 1000 + k, builder=b)
+                R = rotation(rng.normal(size=3), rng.uniform(0, 360)) @ rotation((0, 1, 0), angle)
+                c = (np.array([ix, iy, iz], np.float64) + 0.5) / n_side
+                M = np.eye(4)
+                M[:3, :3] = R / n_side
+                M[:3, 3] = c - (R / n_side) @ np.full(3, 0.5)
+                insts.append(instance_of(M, k))
+                k += 1
+    cam = dict(eye=(0.5, 0.5, -1.2), center=(0.5, 0.5, 0.5), up=(0.0, -1.0, 0.0), vfov=45.0)
+    d = b.build(cam, "instances%dx%d" % (n_side ** 3, tris_each))
+    d.instances = np.array(insts, INSTANCE_DTYPE)
+    return d
+
+
 def _value_noise(u, v, nu, nv, rng):
     """Smooth value noise on a periodic-in-u lattice of nu x nv cells,
     values uniform in [-1, 1], smoothstep interpolation. u, v in cell units."""
