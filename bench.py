@@ -40,7 +40,7 @@ sys.path.insert(0, ROOT)
 METRIC = "Mrays/s at RMSE≤1e-3 vs FP64 oracle, batched vs plain on 1 GB300; p99 job latency"
 UNIT = "Mrays/s"
 
-NODE_BYTES = {0: 64, 1: 80, 2: 64, 3: 224, 4: 32}
+NODE_BYTES = {0: 64, 1: 80, 2: 64, 3: 224, 4: 32, 5: 64}
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per traced segment
 # of the BVH2 extend kernel on the default soup workload, from one ncu
 # capture of the last 15 k_extend launches of a timed frame (3 of its 4
@@ -650,6 +650,26 @@ def main():
                "h2d_bytes_per_step": 256 + 64, "d2h_bytes_per_step": W * H * 20,
                "path": "solrt_render (camera + params from host) + solrt_image_read into pinned host buffers"}
 
+    # instanced workload: the per-frame cost of moving every instance
+    # (solrt_scene_set_instances + solrt_scene_regenerate, host-timed)
+    regen = None
+    if args.workload == "instances":
+        S = solrt.scenes
+        moved = S.instanced_soups(4, 16384, seed=5, angle=10.0).instances
+        dyn = solrt.SceneDescription(ctx, data, bvh=bvh, keep_data=False, dynamic=True)
+        regen = {}
+        for name, mode in (("rebuild", solrt.REGEN_REBUILD), ("refit", solrt.REGEN_REFIT)):
+            ts = []
+            for i in range(7):
+                dyn.set_instances(moved if i % 2 == 0 else data.instances)
+                ctx.synchronize()
+                t0 = time.perf_counter()
+                dyn.tlas_regenerate(mode)
+                ctx.synchronize()
+                ts.append((time.perf_counter() - t0) * 1e3)
+            regen[name + "_ms"] = round(float(np.median(ts[1:])), 3)
+        dyn.close()
+
     # roofline of the extend kernel
     peak, peak_kind = peaks()
     b_seg = 32 + 16 + NODE_BYTES[info.kind] * nodes_per_seg + 48 * tris_per_seg
@@ -689,6 +709,8 @@ def main():
             fresh.close()
             band = (H // 2 - 2, H // 2 + 2)
             t0 = time.perf_counter()
+            # flattened FP64 scene for every kind (the two-level oracle mode is
+            # a brute force, too slow for a million triangles)
             o64 = oracle.OracleScene(data)
             a64 = np.zeros((H, W, 4), np.float32)
             kahan = kw["accum_mode"] == solrt.ACCUM_KAHAN
@@ -742,6 +764,8 @@ def main():
                "gpu_launches": int(st.launches), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                "clocks": clk, "rmse_vs_fp64": rmse, "precision_study": precision, "batched_vs_plain": batched,
                "serving": serving}
+        if regen is not None:
+            out["regenerate_ms"] = regen
         print(json.dumps(out), flush=True)
     if pg is not None:
         pg.destroy_process_group()
