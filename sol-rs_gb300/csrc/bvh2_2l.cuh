@@ -114,7 +114,7 @@ SOLRT_D void extend_bvh2_2l_ww(const IO& io, uint32_t n, unsigned int* work, Tra
             }
             if (leave) {  // back to the TLAS: world ray again
                 float4 o, d;
-                io.load(idx, o, d, ts);
+                io.load_ray(idx, o, d);
                 bvh2_ray_consts<false>(ts.nodes, o.x, o.y, o.z, d.x, d.y, d.z, ix, iy, iz, nox, noy, noz);
                 inst = -1;
                 node = stack.get(--sp);
@@ -125,7 +125,7 @@ SOLRT_D void extend_bvh2_2l_ww(const IO& io, uint32_t n, unsigned int* work, Tra
                 int root = -1;
                 if (k < ts.inst_count) {
                     float4 o, d;
-                    io.load(idx, o, d, ts);
+                    io.load_ray(idx, o, d);
                     float px, py, pz, qx, qy, qz;
                     instance_ray(ts.inst, k, o.x, o.y, o.z, d.x, d.y, d.z, px, py, pz, qx, qy, qz, root);
                     if (root >= 0 && (uint32_t)root < ts.node_count && sp <= SOLRT_BVH2_STACK) {

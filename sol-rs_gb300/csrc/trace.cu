@@ -66,6 +66,10 @@ struct QueueIO {
         ts.tlas_count = s->tlas_count;
         ts.inst_count = s->inst_count;
     }
+    SOLRT_D void load_ray(uint32_t i, float4& o, float4& d) const {
+        o = o_tmin[i];
+        d = d_tmax[i];
+    }
     SOLRT_D void store(uint32_t i, const HitRec& h) const {
         hits[i] = make_float4(h.t, __uint_as_float(h.prim), h.u, h.v);
     }
@@ -80,6 +84,10 @@ struct RayFileIO {
         o = rays[2 * (size_t)i];
         d = rays[2 * (size_t)i + 1];
         ts = scene;
+    }
+    SOLRT_D void load_ray(uint32_t i, float4& o, float4& d) const {
+        o = rays[2 * (size_t)i];
+        d = rays[2 * (size_t)i + 1];
     }
     SOLRT_D void store(uint32_t i, const HitRec& h) const {
         hits[i] = make_float4(h.t, __uint_as_float(h.prim), h.u, h.v);
