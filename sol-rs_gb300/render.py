@@ -68,7 +68,7 @@ def main(argv=None):
     ap.add_argument("--frames", type=int, default=16)
     ap.add_argument("--spp", type=int, default=None, help="samples per launch (path 8, ao 4)")
     ap.add_argument("--bounces", type=int, default=None, help="maxBounces (path 32) / max_samples (ao 4)")
-    ap.add_argument("--bvh", choices=["bvh2", "bvh8"], default="bvh2")
+    ap.add_argument("--bvh", choices=["bvh2", "bvh2q", "bvh2t", "bvh4", "bvh8", "bvh8f"], default="bvh2")
     ap.add_argument("--lambert", action="store_true", help="cosine-diffuse materials only")
     ap.add_argument("--blue-noise", help="PNG texture of the AO integrator")
     ap.add_argument("--out", default="render.png")
@@ -83,7 +83,8 @@ def main(argv=None):
     ctx = _pkg.Context(0)
     if args.integrator == "ao":
         ctx.set_blue_noise(load_blue_noise(args.blue_noise))
-    kind = _pkg.BVH2 if args.bvh == "bvh2" else _pkg.BVH8_Q8
+    kind = {"bvh2": _pkg.BVH2, "bvh2q": _pkg.BVH2_Q16, "bvh2t": _pkg.BVH2_TWO_LEVEL, "bvh4": _pkg.BVH4_Q8,
+            "bvh8": _pkg.BVH8_Q8, "bvh8f": _pkg.BVH8_F32}[args.bvh]
     sc = _pkg.SceneDescription(ctx, data, bvh=kind)
     img = _pkg.Image(ctx, w, h)
     r = _pkg.Renderer(ctx)
