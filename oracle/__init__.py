@@ -1,9 +1,11 @@
 """ctypes binding of the CPU oracle (oracle.cpp). TEST INFRASTRUCTURE ONLY.
 
 Imported by the tests, the smoke check and the CPU-baseline leg of bench.py
-as the checker; never by the product. Parity status: see oracle.h (sampling
-and postprocess functions pinned against the reference's GLSL compiled as
-C++; the rest of the path parity unpinned, no runnable reference).
+as the checker; never by the product. Parity status: the sampling and
+postprocess functions and the whole path (pathtrace.rgen / .rchit / .rmiss)
+are pinned against the reference's own shaders compiled as C++
+(oracle/ref_glsl, ref_path_render below); unpinned only where the reference
+has no source (the driver's intersection and its sin / cos).
 """
 import ctypes
 import importlib
@@ -223,3 +225,68 @@ def camera_look_at(eye, center, up, vfov, aspect, znear=0.1, zfar=1000.0):
     c = _api.Camera()
     lib().oracle_camera_look_at(_F3(*eye), _F3(*center), _F3(*up), vfov, aspect, znear, zfar, ctypes.byref(c))
     return c
+
+
+# --- the reference's own path shaders compiled as C++ (oracle/_ref) --------
+
+REF_LIB_PATH = os.path.join(HERE, "_ref", "libref_glsl.so")
+_ref = None
+
+
+def ref_lib():
+    """libref_glsl.so (pathtrace.rgen / .rchit / .rmiss of the reference,
+    rewritten to C++ by oracle/ref_glsl/build_ref.py), or None when it was
+    not built. Built from the reference checkout when present, else from the
+    generated sources left in oracle/_ref."""
+    global _ref
+    if _ref is not None:
+        return _ref
+    if not os.path.exists(REF_LIB_PATH):
+        import sys
+        sys.path.insert(0, os.path.join(HERE, "ref_glsl"))
+        try:
+            import build_ref
+            ref = build_ref.reference_root()
+            if os.path.isdir(os.path.join(ref, "assets", "glsl")):
+                build_ref.build()
+            else:
+                build_ref.build_from_generated()
+        except Exception:
+            return None
+    L = ctypes.CDLL(REF_LIB_PATH)
+    L.ref_path_render.restype = ctypes.c_int
+    L.ref_path_render.argtypes = [ctypes.POINTER(_api.SceneDesc), _P, _P, ctypes.c_uint32, ctypes.c_uint32,
+                                  ctypes.c_uint32, ctypes.c_int32, ctypes.c_int, _P, _P, _P, _P, ctypes.c_int,
+                                  ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint64)]
+    _ref = L
+    return L
+
+
+def ref_path_render(scene, camera, width, height, frame=0, accum_start=0, sky=False, accum=None, threads=0,
+                    rows=None, stats=None):
+    """One launch of the reference's pathtrace.rgen (8 samples per pixel, at
+    most 32 bounces, its TEA / PCG stream per pixel and frame, mix
+    accumulation, gamma 2.2) with its closest-hit and miss shaders, on CPU
+    threads; traceRayEXT is answered by the oracle's closest hit on `scene`
+    (an OracleScene). rows = (first, end) limits the launch to a band of the
+    W x H image; stats (a dict) receives "rays", the traceRayEXT count.
+    Returns (accum RGBA32F, rgba8)."""
+    L = ref_lib()
+    if L is None:
+        raise FileNotFoundError("reference shaders not built (oracle/_ref)")
+    if accum is None:
+        accum = np.zeros((height, width, 4), np.float32)
+    rgba8 = np.zeros((height, width, 4), np.uint8)
+    vi = (ctypes.c_float * 16)(*camera.view_inverse)
+    pi = (ctypes.c_float * 16)(*camera.projection_inverse)
+    hit = ctypes.cast(lib().oracle_closest_hit, _P)
+    r0, r1 = (0, 0) if rows is None else rows
+    nrays = ctypes.c_uint64(0)
+    rc = L.ref_path_render(ctypes.byref(scene._desc), ctypes.cast(vi, _P), ctypes.cast(pi, _P), width, height, frame,
+                           accum_start, 1 if sky else 0, _ptr(accum), _ptr(rgba8), hit, scene.handle, threads, r0, r1,
+                           ctypes.byref(nrays))
+    if rc != 0:
+        raise ValueError("ref_path_render failed")
+    if stats is not None:
+        stats["rays"] = nrays.value
+    return accum, rgba8

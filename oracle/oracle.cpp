@@ -879,6 +879,19 @@ oracle_scene* oracle_scene_create(const solrt_scene_desc* desc) {
 
 void oracle_scene_destroy(oracle_scene* s) { delete s; }
 
+int oracle_closest_hit(const void* scene, const float* o, const float* d, float tmin, float tmax, uint32_t* prim,
+                       float* u, float* v) {
+    const oracle_scene* s = static_cast<const oracle_scene*>(scene);
+    uint64_t fb = 0, nv = 0, nt = 0;
+    const HitR<float> h = closest_hit<float>(s, V3<float>{o[0], o[1], o[2]}, V3<float>{d[0], d[1], d[2]}, tmin,
+                                             tmax, 1, fb, nv, nt);
+    if (h.prim == SOLRT_NO_HIT) return 0;
+    *prim = h.prim;
+    *u = h.u;
+    *v = h.v;
+    return 1;
+}
+
 void oracle_scene_set_two_level(oracle_scene* s, int on) {
     if (s) s->two_level = on != 0;
 }

@@ -55,6 +55,12 @@ void oracle_scene_destroy(oracle_scene* s);
  * section's triangles in object space, the ray entering through the
  * section's inverse transform (brute force over sections and triangles). */
 void oracle_scene_set_two_level(oracle_scene* s, int on);
+/* Closest hit of one ray (the oracle's watertight traversal, FP32): 1 and
+ * the triangle index (sections' order) with the barycentrics u, v of
+ * vertices 1 and 2, or 0 for a miss. `scene` is an oracle_scene; the
+ * signature is the one the reference-shader pipeline (oracle/ref_glsl) calls. */
+int oracle_closest_hit(const void* scene, const float* o, const float* d, float tmin, float tmax, uint32_t* prim,
+                       float* u, float* v);
 uint32_t oracle_scene_tri_count(const oracle_scene* s);
 
 /* World-space flattened geometry: per triangle 3 vertices x (pos, normal,

@@ -1,4 +1,5 @@
-"""Generates tests/golden/glsl_sampling.json from the reference's own shaders.
+"""Generates tests/golden/glsl_sampling.json and ref_pathtrace_cornell.npz
+from the reference's own shaders.
 
 Builds oracle/_ref/libref_glsl.so (the reference's assets/glsl/sampling.glsl
 and postprocess.glsl compiled as C++ by oracle/ref_glsl/build_ref.py) and
@@ -110,6 +111,33 @@ def main():
     path = os.path.join(HERE, "glsl_sampling.json")
     with open(path, "w") as f:
         json.dump(out, f, separators=(",", ":"))
+    print("wrote", path)
+    pathtrace_fixture()
+
+
+def pathtrace_fixture():
+    """tests/golden/ref_pathtrace_cornell.npz: the reference's pathtrace.rgen /
+    .rchit / .rmiss (compiled as C++, traceRayEXT answered by the oracle's
+    watertight closest hit) on the procedural Cornell box, 32 x 24 pixels,
+    sky on, two launches (frames 0 and 1) accumulated: the RGBA32F
+    accumulation image and the RGBA8 image after each launch."""
+    sys.path.insert(0, ROOT)
+    import importlib
+    import oracle
+    solrt = importlib.import_module("sol-rs_gb300")
+    d = solrt.scenes.cornell()
+    w, h = 32, 24
+    c = d.camera
+    cam = solrt.camera_look_at(c["eye"], c["center"], c["up"], c["vfov"], w / h)
+    o = oracle.OracleScene(d)
+    acc = None
+    out = {}
+    for f in range(2):
+        acc, rgba8 = oracle.ref_path_render(o, cam, w, h, frame=f, sky=True, accum=acc)
+        out["accum%d" % f] = acc.copy()
+        out["rgba8_%d" % f] = rgba8.copy()
+    path = os.path.join(HERE, "ref_pathtrace_cornell.npz")
+    np.savez_compressed(path, **out)
     print("wrote", path)
 
 

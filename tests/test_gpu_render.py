@@ -237,3 +237,27 @@ def test_checkpoint_resume(solrt, ctx, accum):
     a, b = resumed.read()
     assert np.array_equal(a.view(np.uint32), a_ref.view(np.uint32))
     assert np.array_equal(b, b_ref)
+
+
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh2t", "bvh8"])
+def test_gpu_equals_reference_pipeline_fixture(solrt, ctx, bvh):
+    """The device against the committed image of the reference's own
+    pathtrace.rgen / .rchit / .rmiss compiled as C++ (tests/golden/
+    ref_pathtrace_cornell.npz): Cornell box, 32 x 24, sky, REF materials,
+    the reference's per-pixel stream, 8 spp, 32 bounces, two launches
+    accumulated; bit for bit."""
+    import os
+    fx = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_pathtrace_cornell.npz"))
+    d = S.cornell()
+    w, h = 32, 24
+    cam = camera_of(d, w / h)
+    sc = solrt.SceneDescription(ctx, d, bvh=bvh_kind(solrt, bvh))
+    img = solrt.Image(ctx, w, h)
+    r = solrt.Renderer(ctx)
+    for f in range(2):
+        p = solrt.render_params(w, h, spp=8, max_bounces=32, frame=f, material_mode=solrt.MATERIAL_REF,
+                                rng_mode=solrt.RNG_REF_STREAM, miss_mode=solrt.MISS_REF_SKY)
+        r.cmd_trace_rays(sc, cam, p, img)
+        a32, a8 = img.read()
+        assert np.array_equal(a32.view(np.uint32), fx["accum%d" % f].view(np.uint32)), f
+        assert np.max(np.abs(a8.astype(int) - fx["rgba8_%d" % f].astype(int))) <= 1, f
