@@ -22,9 +22,11 @@
  *
  * Parity: sampling.glsl and postprocess.glsl are pinned against the
  * reference's own GLSL source compiled as C++ (golden vectors under
- * tests/golden). The rest of the path (raygen / closest-hit / miss control
- * flow, BVH, intersection) has no reference implementation that runs here
- * (Rust + Vulkan RT, closed driver): parity unpinned for those parts.
+ * tests/golden), and the whole path against the reference's
+ * pathtrace.rgen / .rchit / .rmiss compiled as C++ and run as a CPU
+ * pipeline (oracle/ref_glsl; traceRayEXT answered by oracle_closest_hit):
+ * equal images bit for bit. Unpinned only where the reference has no source
+ * (the Vulkan driver's BVH and intersection, and its sin / cos).
  */
 #ifndef SOLRT_ORACLE_H
 #define SOLRT_ORACLE_H
