@@ -217,10 +217,13 @@ template <class R> V3<R> miss_color(V3<R> dir, uint32_t mode) {
 // ---------------------------------------------------------------------------
 
 struct TriW {
-    V3<float> p[3];  // world-space positions
-    V3<float> n[3];  // world-space (unnormalised) normals
-    V3<float> c[3];  // vertex colours
+    V3<float> p[3];   // world-space positions (intersection)
+    V3<float> n[3];   // world-space (unnormalised) normals (export)
+    V3<float> c[3];   // vertex colours
+    V3<float> op[3];  // object-space positions and normals (shading)
+    V3<float> on[3];
     uint32_t mat;
+    uint32_t sec;     // section
 };
 
 struct Box {
@@ -239,6 +242,8 @@ struct oracle_scene {
     std::vector<TriW> obj;
     std::vector<uint32_t> sec_first, sec_count;
     std::vector<std::array<float, 12>> minv;
+    // per section its instance's transform and transform_it (column-major)
+    std::vector<std::array<float, 16>> sec_t, sec_tit;
     // LBVH
     std::vector<uint32_t> order;         // sorted position -> triangle
     std::vector<uint32_t> morton;        // sorted codes
@@ -269,6 +274,13 @@ bool flatten(const solrt_scene_desc* d, oracle_scene* s) {
         std::array<float, 12> mi;
         for (int k = 0; k < 12; ++k) mi[k] = Tit[k];  // row r of the transpose = Tit[4r .. 4r + 3]
         s->minv.push_back(mi);
+        std::array<float, 16> t16, ti16;
+        for (int k = 0; k < 16; ++k) {
+            t16[k] = T[k];
+            ti16[k] = Tit[k];
+        }
+        s->sec_t.push_back(t16);
+        s->sec_tit.push_back(ti16);
         for (uint32_t t = 0; t < sec.index_count / 3; ++t) {
             TriW tw, to;
             for (int k = 0; k < 3; ++k) {
@@ -281,9 +293,12 @@ bool flatten(const solrt_scene_desc* d, oracle_scene* s) {
                 to.p[k] = V3<float>{v.pos[0], v.pos[1], v.pos[2]};
                 mat4_mul<float>(Tit, v.normal[0], v.normal[1], v.normal[2], 0.0f, o);
                 tw.n[k] = V3<float>{o[0], o[1], o[2]};
+                tw.op[k] = V3<float>{v.pos[0], v.pos[1], v.pos[2]};
+                tw.on[k] = V3<float>{v.normal[0], v.normal[1], v.normal[2]};
                 tw.c[k] = V3<float>{v.color[0], v.color[1], v.color[2]};
             }
             tw.mat = sec.material_index;
+            tw.sec = si;
             s->tris.push_back(tw);
             to.mat = sec.material_index;
             s->obj.push_back(to);
@@ -574,6 +589,22 @@ struct Counters {
     uint64_t seg = 0, paths = 0, fb = 0, nv = 0, nt = 0;
 };
 
+// Shading normal and position of a hit (pathtrace.rchit:82-90,
+// ao.rchit:66-75): object-space vertex normals and positions interpolated,
+// then the section instance's transform_it (w = 0, normalised) and
+// transform (w = 1).
+template <class R> void hit_frame(const oracle_scene* s, const TriW& tri, R b0, R b1, R b2, V3<R>& normal,
+                                  V3<R>& pos) {
+    auto cv = [](V3<float> a) { return V3<R>{R(a.x), R(a.y), R(a.z)}; };
+    const V3<R> n = cv(tri.on[0]) * b0 + cv(tri.on[1]) * b1 + cv(tri.on[2]) * b2;
+    const V3<R> p = cv(tri.op[0]) * b0 + cv(tri.op[1]) * b1 + cv(tri.op[2]) * b2;
+    R o[4];
+    mat4_mul<R>(s->sec_tit[tri.sec].data(), n.x, n.y, n.z, R(0), o);
+    normal = normalize(V3<R>{o[0], o[1], o[2]});
+    mat4_mul<R>(s->sec_t[tri.sec].data(), p.x, p.y, p.z, R(1), o);
+    pos = V3<R>{o[0], o[1], o[2]};
+}
+
 template <class R> V3<R> trace_path(const oracle_scene* s, const solrt_render_params* p, V3<R> o,
                                     V3<R> d, R tmin, R tmax, uint32_t& rng, Counters& cn) {
     V3<R> acc{R(1), R(1), R(1)};
@@ -594,9 +625,8 @@ template <class R> V3<R> trace_path(const oracle_scene* s, const solrt_render_pa
         const R b1 = h.u, b2 = h.v;
         const R b0 = (R(1) - b1) - b2;
         auto cv = [](V3<float> a) { return V3<R>{R(a.x), R(a.y), R(a.z)}; };
-        V3<R> normal = cv(tri.n[0]) * b0 + cv(tri.n[1]) * b1 + cv(tri.n[2]) * b2;
-        normal = normalize(normal);
-        const V3<R> pos = cv(tri.p[0]) * b0 + cv(tri.p[1]) * b1 + cv(tri.p[2]) * b2;
+        V3<R> normal, pos;
+        hit_frame<R>(s, tri, b0, b1, b2, normal, pos);
         const V3<R> vcol = cv(tri.c[0]) * b0 + cv(tri.c[1]) * b1 + cv(tri.c[2]) * b2;
         const V3<R> wi = normalize(d);
         const V3<R> n_o = normal * glsl_sign(dot(normal, -wi));
@@ -790,9 +820,8 @@ void render_pixel_ao(const oracle_scene* s, const solrt_camera* cam, const solrt
             const TriW& tri = s->tris[h.prim];
             const R b1 = h.u, b2 = h.v;
             const R b0 = (R(1) - b1) - b2;
-            auto cv = [](V3<float> a) { return V3<R>{R(a.x), R(a.y), R(a.z)}; };
-            const V3<R> normal = normalize(cv(tri.n[0]) * b0 + cv(tri.n[1]) * b1 + cv(tri.n[2]) * b2);
-            const V3<R> pos = cv(tri.p[0]) * b0 + cv(tri.p[1]) * b1 + cv(tri.p[2]) * b2;
+            V3<R> normal, pos;
+            hit_frame<R>(s, tri, b0, b1, b2, normal, pos);
             const V3<R> no = pos + R(0.00001f) * d;                 // ao.rchit:78
             // getBlueRand2(depth + depth * sampleId) (ao.rchit:43-49)
             const uint32_t bi = depth + depth * i;

@@ -333,11 +333,13 @@ solrt_status solrt_scene_create(solrt_context* ctx, const solrt_scene_desc* d, c
         nt += sec.index_count / 3;
     }
     CHECK_ARG(nv < (1ull << 31) && nt < (1ull << 31), "scene too large");
-    // two-level scenes keep the object-space geometry, as dynamic ones do
+    // two-level scenes take instances, as dynamic ones do
     const bool dynamic = bvh && ((bvh->flags & SOLRT_BVH_DYNAMIC) || bvh->kind == SOLRT_BVH2_TWO_LEVEL);
-    std::vector<float4> pos(nv), nrm(nv), col(nv);
-    std::vector<float4> opos(dynamic ? nv : 0), onrm(dynamic ? nv : 0);
-    std::vector<uint32_t> vsec_start(dynamic ? d->section_count : 0);
+    // world positions for the BVH; object-space positions and normals for
+    // shading, which interpolates them and then applies the section's
+    // transform / transform_it (pathtrace.rchit:80-90)
+    std::vector<float4> pos(nv), col(nv), opos(nv), onrm(nv);
+    std::vector<uint32_t> vsec_start(d->section_count), sec_mat(d->section_count);
     std::vector<solrt_instance> inst(d->section_count);
     std::vector<uint32_t> sec_first(d->section_count), sec_count(d->section_count);
     std::vector<uint4> tri(nt);
@@ -356,18 +358,16 @@ solrt_status solrt_scene_create(solrt_context* ctx, const solrt_scene_desc* d, c
         }
         sec_first[s] = (uint32_t)tb;
         sec_count[s] = sec.index_count / 3;
-        if (dynamic) vsec_start[s] = (uint32_t)vb;
+        sec_mat[s] = sec.material_index;
+        vsec_start[s] = (uint32_t)vb;
+        (void)Tit;
         for (uint32_t v = 0; v < sec.vertex_count; ++v) {
             const solrt_vertex& in = d->vertices[sec.vertex_offset + v];
-            if (dynamic) {
-                opos[vb + v] = make_float4(in.pos[0], in.pos[1], in.pos[2], 0.0f);
-                onrm[vb + v] = make_float4(in.normal[0], in.normal[1], in.normal[2], 0.0f);
-            }
+            opos[vb + v] = make_float4(in.pos[0], in.pos[1], in.pos[2], 0.0f);
+            onrm[vb + v] = make_float4(in.normal[0], in.normal[1], in.normal[2], 0.0f);
             float o[4];
-            mat4_mul(T, in.pos[0], in.pos[1], in.pos[2], 1.0f, o);       // pathtrace.rchit:88-90
+            mat4_mul(T, in.pos[0], in.pos[1], in.pos[2], 1.0f, o);       // the BVH's world positions
             pos[vb + v] = make_float4(o[0], o[1], o[2], 0.0f);
-            mat4_mul(Tit, in.normal[0], in.normal[1], in.normal[2], 0.0f, o);  // rchit:84-86
-            nrm[vb + v] = make_float4(o[0], o[1], o[2], 0.0f);
             col[vb + v] = make_float4(in.color[0], in.color[1], in.color[2], 0.0f);
         }
         for (uint32_t t = 0; t < sec.index_count / 3; ++t) {
@@ -379,8 +379,7 @@ solrt_status solrt_scene_create(solrt_context* ctx, const solrt_scene_desc* d, c
                     return SOLRT_ERR_INVALID;
                 }
             }
-            tri[tb + t] = make_uint4((uint32_t)(vb + id[0]), (uint32_t)(vb + id[1]), (uint32_t)(vb + id[2]),
-                                     sec.material_index);
+            tri[tb + t] = make_uint4((uint32_t)(vb + id[0]), (uint32_t)(vb + id[1]), (uint32_t)(vb + id[2]), s);
         }
         vb += sec.vertex_count;
         tb += sec.index_count / 3;
@@ -397,16 +396,28 @@ solrt_status solrt_scene_create(solrt_context* ctx, const solrt_scene_desc* d, c
     };
     cudaStream_t st = ctx->stream;
     solrt_status s;
-    if ((s = sc->vpos.alloc(16 * nv)) || (s = sc->vnrm.alloc(16 * nv)) || (s = sc->vcol.alloc(16 * nv)) ||
-        (s = sc->tri_idx.alloc(16 * nt)) || (s = sc->materials.alloc(48 * (size_t)d->material_count)))
+    const size_t ns = d->section_count;
+    if ((s = sc->vpos.alloc(16 * nv)) || (s = sc->vcol.alloc(16 * nv)) || (s = sc->opos.alloc(16 * nv)) ||
+        (s = sc->onrm.alloc(16 * nv)) || (s = sc->tri_idx.alloc(16 * nt)) ||
+        (s = sc->materials.alloc(48 * (size_t)d->material_count)) || (s = sc->sec_mat.alloc(4 * ns)) ||
+        (s = sc->vsec_start.alloc(4 * ns)) || (s = sc->instances.alloc(sizeof(solrt_instance) * ns)))
         return fail(s);
     if (nv) {
         if (cudaMemcpyAsync(sc->vpos.ptr, pos.data(), 16 * nv, cudaMemcpyHostToDevice, st) != cudaSuccess ||
-            cudaMemcpyAsync(sc->vnrm.ptr, nrm.data(), 16 * nv, cudaMemcpyHostToDevice, st) != cudaSuccess ||
-            cudaMemcpyAsync(sc->vcol.ptr, col.data(), 16 * nv, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+            cudaMemcpyAsync(sc->vcol.ptr, col.data(), 16 * nv, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+            cudaMemcpyAsync(sc->opos.ptr, opos.data(), 16 * nv, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+            cudaMemcpyAsync(sc->onrm.ptr, onrm.data(), 16 * nv, cudaMemcpyHostToDevice, st) != cudaSuccess) {
             set_error("scene upload failed");
             return fail(SOLRT_ERR_DEVICE);
         }
+    }
+    if (ns && (cudaMemcpyAsync(sc->sec_mat.ptr, sec_mat.data(), 4 * ns, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+               cudaMemcpyAsync(sc->vsec_start.ptr, vsec_start.data(), 4 * ns, cudaMemcpyHostToDevice, st) !=
+                   cudaSuccess ||
+               cudaMemcpyAsync(sc->instances.ptr, inst.data(), sizeof(solrt_instance) * ns, cudaMemcpyHostToDevice,
+                               st) != cudaSuccess)) {
+        set_error("scene upload failed");
+        return fail(SOLRT_ERR_DEVICE);
     }
     if (nt && cudaMemcpyAsync(sc->tri_idx.ptr, tri.data(), 16 * nt, cudaMemcpyHostToDevice, st) != cudaSuccess) {
         set_error("scene upload failed");
@@ -422,22 +433,7 @@ solrt_status solrt_scene_create(solrt_context* ctx, const solrt_scene_desc* d, c
     sc->sec_tri_first = std::move(sec_first);
     sc->sec_tri_count = std::move(sec_count);
     sc->inst_host = inst;
-    if (dynamic) {
-        sc->dynamic = true;
-        const size_t ns = d->section_count;
-        if ((s = sc->opos.alloc(16 * nv)) || (s = sc->onrm.alloc(16 * nv)) ||
-            (s = sc->vsec_start.alloc(4 * ns)) || (s = sc->instances.alloc(sizeof(solrt_instance) * ns)))
-            return fail(s);
-        if ((nv && (cudaMemcpyAsync(sc->opos.ptr, opos.data(), 16 * nv, cudaMemcpyHostToDevice, st) != cudaSuccess ||
-                    cudaMemcpyAsync(sc->onrm.ptr, onrm.data(), 16 * nv, cudaMemcpyHostToDevice, st) != cudaSuccess)) ||
-            (ns && (cudaMemcpyAsync(sc->vsec_start.ptr, vsec_start.data(), 4 * ns, cudaMemcpyHostToDevice, st) !=
-                        cudaSuccess ||
-                    cudaMemcpyAsync(sc->instances.ptr, inst.data(), sizeof(solrt_instance) * ns,
-                                    cudaMemcpyHostToDevice, st) != cudaSuccess))) {
-            set_error("scene upload failed");
-            return fail(SOLRT_ERR_DEVICE);
-        }
-    }
+    sc->dynamic = dynamic;
     if (cudaStreamSynchronize(st) != cudaSuccess) {
         set_error("scene upload failed");
         return fail(SOLRT_ERR_DEVICE);
@@ -494,11 +490,11 @@ solrt_status solrt_scene_bvh_export(solrt_scene* scene, void* nodes, size_t node
 
 solrt_status solrt_scene_bytes(solrt_scene* scene, uint64_t* out) {
     CHECK_ARG(scene && out, "null argument");
-    *out = scene->vpos.bytes + scene->vnrm.bytes + scene->vcol.bytes + scene->tri_idx.bytes +
-           scene->materials.bytes + scene->nodes.bytes + scene->tri_wt.bytes + scene->opos.bytes +
-           scene->onrm.bytes + scene->vsec_start.bytes + scene->instances.bytes + scene->topo_order.bytes +
-           scene->topo_child.bytes + scene->topo_par_int.bytes + scene->topo_par_leaf.bytes +
-           scene->topo_range.bytes;
+    *out = scene->vpos.bytes + scene->opos.bytes + scene->onrm.bytes + scene->vcol.bytes + scene->tri_idx.bytes +
+           scene->materials.bytes + scene->sec_mat.bytes + scene->nodes.bytes + scene->tri_wt.bytes +
+           scene->vsec_start.bytes + scene->instances.bytes + scene->topo_order.bytes + scene->topo_child.bytes +
+           scene->topo_par_int.bytes + scene->topo_par_leaf.bytes + scene->topo_range.bytes + scene->tlas.bytes +
+           scene->inst_table.bytes;
     return SOLRT_OK;
 }
 

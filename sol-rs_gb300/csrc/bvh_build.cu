@@ -887,7 +887,8 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
     if (desc.kind == SOLRT_BVH2_TWO_LEVEL) SOLRT_TRY(build_two_level(ctx, sc));
     else SOLRT_TRY(build_single_level(ctx, sc, desc));
     sc.info.tri_bytes = sc.tri_wt.bytes;
-    sc.info.shade_bytes = sc.vpos.bytes + sc.vnrm.bytes + sc.vcol.bytes + sc.tri_idx.bytes + sc.materials.bytes;
+    sc.info.shade_bytes = sc.opos.bytes + sc.onrm.bytes + sc.vcol.bytes + sc.tri_idx.bytes + sc.materials.bytes +
+                          sc.instances.bytes + sc.sec_mat.bytes;
     SOLRT_CUDA(cudaEventRecord(ctx.ev1, st));
     SOLRT_CUDA(cudaEventSynchronize(ctx.ev1));
     float ms = 0.0f;
@@ -908,14 +909,13 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
 
 namespace {
 
-// World-space vertex v from its object-space copy and the instance of its
-// section: the flattening of solrt_scene_create (pathtrace.rchit:84-90
-// applied once per vertex), with the same operation order (mat4_mul), so a
-// regenerated scene equals one created with these instances bit for bit.
-__global__ void k_apply_instances(const float4* __restrict__ opos, const float4* __restrict__ onrm,
-                                  const uint32_t* __restrict__ vsec_start, uint32_t nsec,
-                                  const solrt_instance* __restrict__ inst, uint32_t nv, float4* __restrict__ vpos,
-                                  float4* __restrict__ vnrm) {
+// World-space position of vertex v (for the BVH) from its object-space copy
+// and the instance of its section, with the operation order of
+// solrt_scene_create (mat4_mul), so a regenerated scene equals one created
+// with these instances bit for bit. Shading reads the instances directly.
+__global__ void k_apply_instances(const float4* __restrict__ opos, const uint32_t* __restrict__ vsec_start,
+                                  uint32_t nsec, const solrt_instance* __restrict__ inst, uint32_t nv,
+                                  float4* __restrict__ vpos) {
     const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nv) return;
     // last section whose first vertex is <= v (empty sections share starts
@@ -931,9 +931,6 @@ __global__ void k_apply_instances(const float4* __restrict__ opos, const float4*
     const float4 p = opos[v];
     mat4_mul(in.transform, p.x, p.y, p.z, 1.0f, o);
     vpos[v] = make_float4(o[0], o[1], o[2], 0.0f);
-    const float4 n = onrm[v];
-    mat4_mul(in.transform_it, n.x, n.y, n.z, 0.0f, o);
-    vnrm[v] = make_float4(o[0], o[1], o[2], 0.0f);
 }
 
 // New boxes for the kept topology: the refit pass of build_bvh over the
@@ -1008,8 +1005,8 @@ solrt_status regenerate_scene(Context& ctx, Scene& sc, uint32_t mode) {
     cudaStream_t st = ctx.stream;
     if (sc.vertex_count) {
         k_apply_instances<<<blocks_for(sc.vertex_count, 256), 256, 0, st>>>(
-            sc.opos.as<float4>(), sc.onrm.as<float4>(), sc.vsec_start.as<uint32_t>(), sc.section_count,
-            sc.instances.as<solrt_instance>(), sc.vertex_count, sc.vpos.as<float4>(), sc.vnrm.as<float4>());
+            sc.opos.as<float4>(), sc.vsec_start.as<uint32_t>(), sc.section_count, sc.instances.as<solrt_instance>(),
+            sc.vertex_count, sc.vpos.as<float4>());
         ++ctx.launches;
         SOLRT_CUDA(cudaGetLastError());
     }

@@ -236,14 +236,18 @@ struct Scene {
     uint32_t tri_count = 0;
     uint32_t vertex_count = 0;
     uint32_t material_count = 0;
-    DeviceBuffer vpos, vnrm, vcol, tri_idx, materials;
+    // world positions (BVH builds), object-space positions and normals and
+    // colours (shading), triangles (v0, v1, v2, section), materials, and per
+    // section its material index
+    DeviceBuffer vpos, vcol, tri_idx, materials, sec_mat;
     DeviceBuffer nodes, tri_wt;
     solrt_bvh_info info{};
     solrt_bvh_desc desc{};
-    // SOLRT_BVH_DYNAMIC: object-space positions / normals (float4 per
-    // vertex), the first vertex of each section (section_count + 1 entries),
-    // the staged instances, and the BVH2 topology of the last build (leaf
-    // order, children, parents, key ranges) for refits.
+    // Object-space positions / normals (float4 per vertex; shading reads
+    // them and transforms by the section's instance, as pathtrace.rchit
+    // does), the first vertex of each section, the instances (one per
+    // section); SOLRT_BVH_DYNAMIC also keeps the BVH2 topology of the last
+    // build (leaf order, children, parents, key ranges) for refits.
     bool dynamic = false;
     uint32_t section_count = 0;
     DeviceBuffer opos, onrm, vsec_start, instances;
@@ -271,9 +275,12 @@ struct Scene {
         d.tlas = two ? tlas.as<float4>() : nullptr;
         d.inst = two ? inst_table.as<float4>() : nullptr;
         d.vpos = vpos.as<float4>();
-        d.vnrm = vnrm.as<float4>();
+        d.opos = opos.as<float4>();
+        d.onrm = onrm.as<float4>();
         d.vcol = vcol.as<float4>();
         d.tri_idx = tri_idx.as<uint4>();
+        d.sections = instances.as<float4>();
+        d.sec_mat = sec_mat.as<uint32_t>();
         d.materials = materials.as<float4>();
         d.nodes = nodes.as<float4>();
         d.tri_wt = tri_wt.as<float4>();

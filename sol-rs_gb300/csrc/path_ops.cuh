@@ -37,6 +37,29 @@ SOLRT_D void camera_ray(const DevJob& J, uint32_t pix, uint32_t& rng, float4& o_
     d_tmax = make_float4(dir[0], dir[1], dir[2], J.tmax);
 }
 
+// Column-major mat4 (4 float4 columns at m) times (x, y, z, w), per row
+// ((c0 x + c1 y) + c2 z) + c3 w: GLSL's mat4 * vec4 in the order the oracle
+// and the reference's shaders compiled as C++ use.
+SOLRT_D f3 mat4_xyz(const float4* m, float x, float y, float z, float w) {
+    const float4 c0 = __ldg(m), c1 = __ldg(m + 1), c2 = __ldg(m + 2), c3 = __ldg(m + 3);
+    return f3{((c0.x * x + c1.x * y) + c2.x * z) + c3.x * w, ((c0.y * x + c1.y * y) + c2.y * z) + c3.y * w,
+              ((c0.z * x + c1.z * y) + c2.z * z) + c3.z * w};
+}
+
+// Shading normal and position of a hit as pathtrace.rchit:82-90 (and
+// ao.rchit:66-75) compute them: object-space vertex normals and positions
+// interpolated with the barycentrics, then the section instance's
+// transform_it (normal, w = 0, normalised) and transform (position, w = 1).
+SOLRT_D void hit_frame(const DevScene& sc, uint4 ti, float b0, float b1, float b2, f3& normal, f3& pos) {
+    const float4 n0 = __ldg(sc.onrm + ti.x), n1 = __ldg(sc.onrm + ti.y), n2 = __ldg(sc.onrm + ti.z);
+    const float4 p0 = __ldg(sc.opos + ti.x), p1 = __ldg(sc.opos + ti.y), p2 = __ldg(sc.opos + ti.z);
+    const f3 n = f3{n0.x, n0.y, n0.z} * b0 + f3{n1.x, n1.y, n1.z} * b1 + f3{n2.x, n2.y, n2.z} * b2;
+    const f3 p = f3{p0.x, p0.y, p0.z} * b0 + f3{p1.x, p1.y, p1.z} * b1 + f3{p2.x, p2.y, p2.z} * b2;
+    const float4* inst = sc.sections + 9 * (size_t)ti.w;  // (id, ..), transform, transform_it
+    normal = normalize(mat4_xyz(inst + 5, n.x, n.y, n.z, 0.0f));
+    pos = mat4_xyz(inst + 1, p.x, p.y, p.z, 1.0f);
+}
+
 // One closest-hit or miss step (pathtrace.rchit:56-113, pathtrace.rmiss:8-21
 // and pathtrace.rgen:77-84). h = (t, prim bits, u, v). Updates the path
 // throughput `acc`, the rng state and the depth; returns true when the path
@@ -52,21 +75,19 @@ SOLRT_D bool shade_step(const DevJob& J, float4 o, float4 d, float4 h, f3& acc, 
         return false;
     }
     const uint4 ti = __ldg(sc.tri_idx + prim);                               // rchit:63-73
-    const float4 m0 = __ldg(sc.materials + 3 * ti.w);
-    const float4 m1 = __ldg(sc.materials + 3 * ti.w + 1);
-    const float4 m2 = __ldg(sc.materials + 3 * ti.w + 2);
+    const uint32_t mat = __ldg(sc.sec_mat + ti.w);                           // rchit:71
+    const float4 m0 = __ldg(sc.materials + 3 * mat);
+    const float4 m1 = __ldg(sc.materials + 3 * mat + 1);
+    const float4 m2 = __ldg(sc.materials + 3 * mat + 2);
     if (m1.x >= 1.0f || m1.y >= 1.0f || m1.z >= 1.0f) {                      // rchit:75-80
         acc = acc * f3{m1.x, m1.y, m1.z};
         return false;
     }
     const float b1 = h.z, b2 = h.w;
     const float b0 = (1.0f - b1) - b2;                                       // rchit:82
-    const float4 n0 = __ldg(sc.vnrm + ti.x), n1 = __ldg(sc.vnrm + ti.y), n2 = __ldg(sc.vnrm + ti.z);
-    const float4 p0 = __ldg(sc.vpos + ti.x), p1 = __ldg(sc.vpos + ti.y), p2 = __ldg(sc.vpos + ti.z);
+    f3 normal, pos;
+    hit_frame(sc, ti, b0, b1, b2, normal, pos);                              // rchit:82-90
     const float4 c0 = __ldg(sc.vcol + ti.x), c1 = __ldg(sc.vcol + ti.y), c2 = __ldg(sc.vcol + ti.z);
-    f3 normal = f3{n0.x, n0.y, n0.z} * b0 + f3{n1.x, n1.y, n1.z} * b1 + f3{n2.x, n2.y, n2.z} * b2;
-    normal = normalize(normal);                                              // rchit:84-86
-    const f3 pos = f3{p0.x, p0.y, p0.z} * b0 + f3{p1.x, p1.y, p1.z} * b1 + f3{p2.x, p2.y, p2.z} * b2;
     const f3 vcol = f3{c0.x, c0.y, c0.z} * b0 + f3{c1.x, c1.y, c1.z} * b1 + f3{c2.x, c2.y, c2.z} * b2;
     const f3 wi = normalize(dir);                                            // rchit:94-95
     const f3 n_o = normal * glsl_sign(dot(normal, -wi));

@@ -341,11 +341,8 @@ __global__ void __launch_bounds__(128) k_ao(const DevJob* __restrict__ job, DevS
                 const uint4 ti = __ldg(sc.tri_idx + h.prim);
                 const float b1 = h.u, b2 = h.v;
                 const float b0 = (1.0f - b1) - b2;
-                const float4 n0 = __ldg(sc.vnrm + ti.x), n1 = __ldg(sc.vnrm + ti.y), n2 = __ldg(sc.vnrm + ti.z);
-                const float4 p0 = __ldg(sc.vpos + ti.x), p1 = __ldg(sc.vpos + ti.y), p2 = __ldg(sc.vpos + ti.z);
-                const f3 normal =
-                    normalize(f3{n0.x, n0.y, n0.z} * b0 + f3{n1.x, n1.y, n1.z} * b1 + f3{n2.x, n2.y, n2.z} * b2);
-                const f3 pos = f3{p0.x, p0.y, p0.z} * b0 + f3{p1.x, p1.y, p1.z} * b1 + f3{p2.x, p2.y, p2.z} * b2;
+                f3 normal, pos;
+                hit_frame(sc, ti, b0, b1, b2, normal, pos);                   // ao.rchit:66-75
                 const f3 no = pos + 0.00001f * d;                             // ao.rchit:78
                 // getBlueRand2(depth + depth * sampleId) (ao.rchit:43-49)
                 const uint32_t bi = depth + depth * i;

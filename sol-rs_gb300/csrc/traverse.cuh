@@ -27,10 +27,14 @@ struct DevScene {
     uint32_t inst_count;      // SOLRT_BVH2_TWO_LEVEL: entries of `inst` (one per section)
     const float4* tlas;       // SOLRT_BVH2_TWO_LEVEL: BVH2 nodes over instances (leaf ~section)
     const float4* inst;       // SOLRT_BVH2_TWO_LEVEL: per section inverse-transform rows 0-2, BLAS root
-    const float4* vpos;       // world position per vertex (.w unused)
-    const float4* vnrm;       // world normal (transform_it applied, unnormalised)
+    const float4* vpos;       // world position per vertex (.w unused): the BVH builds
+    const float4* opos;       // object-space position per vertex: shading
+    const float4* onrm;       // object-space normal per vertex: shading
     const float4* vcol;       // vertex colour
-    const uint4* tri_idx;     // (v0, v1, v2, material) per original triangle
+    const uint4* tri_idx;     // (v0, v1, v2, section) per original triangle
+    const float4* sections;   // per section its solrt_instance as 9 float4: (id, ..), transform
+                              // columns, transform_it columns (column-major)
+    const uint32_t* sec_mat;  // material index per section
     const float4* materials;  // solrt_material as 3 float4
     const float4* nodes;      // BVH2: 4 float4 per node; BVH8: 5 float4 per node
     const float4* tri_wt;     // 3 float4 per triangle in leaf order; p0.w = prim bits

@@ -54,22 +54,46 @@ def test_reference_shaders_equal_oracle(ref, name, sky):
 
 
 def test_reference_shaders_transformed_sections(ref):
-    """Sections with transforms: the reference interpolates object-space
-    vertex data and transforms the result (pathtrace.rchit:80-90), the
-    oracle and the device transform the vertices first; equal in exact
-    arithmetic, so the images agree up to paths that rounding sends another
-    way."""
+    """Sections with transforms: like the reference, shading interpolates
+    object-space vertex data and then applies the section's transform_it /
+    transform (pathtrace.rchit:80-90), so the images are equal too."""
     d = transformed_cornell()
     w, h = 48, 40
     cam = camera_of(d, w / h)
     o = ref.OracleScene(d)
+    for sky in (False, True):
+        acc = None
+        for f in range(2):
+            acc, r8 = ref.ref_path_render(o, cam, w, h, frame=f, sky=sky, accum=acc)
+        oa, o8 = _oracle_frames(ref, o, cam, w, h, sky, 2)
+        assert np.array_equal(acc.view(np.uint32), oa.view(np.uint32)), sky
+        assert np.array_equal(r8, o8), sky
+
+
+REF_MODELS = "/root/reference/assets/models"
+
+
+@pytest.mark.parametrize("model,sky", [("cornell.gltf", False), ("tunnel.gltf", True)])
+def test_reference_shaders_on_reference_models(ref, model, sky):
+    """The reference's own scenes (node transforms, u16 / u32 indices,
+    COLOR_0) read by the glTF loader, rendered by the reference's shaders and
+    by the oracle: equal bit for bit."""
+    path = os.path.join(REF_MODELS, model)
+    if not os.path.exists(path):
+        pytest.skip("reference models not present")
+    g = solrt.load_scene(path)
+    w, h = 40, 30
+    cam = g.camera(w / h)
+    if cam is None:  # the tunnel has none: the example's default camera (5-pathtrace.rs:128-135)
+        cam = solrt.camera_look_at((0.0, 0.0, -2.0), (0.0, 0.0, 0.0), (0.0, -1.0, 0.0), 45.0, w / h)
+    o = ref.OracleScene(g.data)
     acc = None
-    for f in range(4):
-        acc, _ = ref.ref_path_render(o, cam, w, h, frame=f, accum=acc)
-    oa, _ = _oracle_frames(ref, o, cam, w, h, False, 4)
-    close = np.all(np.abs(acc - oa) <= 1e-5 + 1e-4 * np.abs(oa), axis=-1)
-    assert close.mean() > 0.9
-    assert abs(acc[..., :3].mean() - oa[..., :3].mean()) < 0.02 * oa[..., :3].mean()
+    for f in range(2):
+        acc, r8 = ref.ref_path_render(o, cam, w, h, frame=f, sky=sky, accum=acc)
+    oa, o8 = _oracle_frames(ref, o, cam, w, h, sky, 2)
+    assert np.array_equal(acc.view(np.uint32), oa.view(np.uint32))
+    assert np.array_equal(r8, o8)
+    assert acc[..., :3].mean() > 0
 
 
 def test_oracle_equals_reference_pipeline_fixture(oracle):
