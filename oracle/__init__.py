@@ -290,3 +290,57 @@ def ref_path_render(scene, camera, width, height, frame=0, accum_start=0, sky=Fa
     if stats is not None:
         stats["rays"] = nrays.value
     return accum, rgba8
+
+
+def _ref_sibling_setup(L):
+    if getattr(L, "_sibling_ready", False):
+        return
+    L.ref_ao_render.restype = ctypes.c_int
+    L.ref_ao_render.argtypes = [ctypes.POINTER(_api.SceneDesc), _P, _P, ctypes.c_uint32, ctypes.c_uint32,
+                                ctypes.c_uint32, ctypes.c_int32, _P, ctypes.c_uint32, ctypes.c_uint32, _P, _P, _P,
+                                ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint64)]
+    L.ref_debug_render.restype = ctypes.c_int
+    L.ref_debug_render.argtypes = [ctypes.POINTER(_api.SceneDesc), _P, _P, ctypes.c_uint32, ctypes.c_uint32, _P, _P,
+                                   _P, ctypes.c_int]
+    L._sibling_ready = True
+
+
+def ref_ao_render(scene, camera, width, height, noise, frame=0, accum_start=0, accum=None, threads=0):
+    """One launch of the reference's ao.rgen / ao.rchit / ao.rmiss (4 samples,
+    4 hits, as the shaders fix) into an RGBA32F target, on CPU threads, with
+    the oracle's closest hit on `scene`; noise: (h, w, 4) uint8 blue-noise
+    texture. Returns the accumulation image."""
+    L = ref_lib()
+    if L is None:
+        raise FileNotFoundError("reference shaders not built (oracle/_ref)")
+    _ref_sibling_setup(L)
+    if accum is None:
+        accum = np.zeros((height, width, 4), np.float32)
+    nz = np.ascontiguousarray(noise, np.uint8)
+    vi = (ctypes.c_float * 16)(*camera.view_inverse)
+    pi = (ctypes.c_float * 16)(*camera.projection_inverse)
+    hit = ctypes.cast(lib().oracle_closest_hit, _P)
+    rc = L.ref_ao_render(ctypes.byref(scene._desc), ctypes.cast(vi, _P), ctypes.cast(pi, _P), width, height, frame,
+                         accum_start, _ptr(nz), nz.shape[1], nz.shape[0], _ptr(accum), hit, scene.handle, threads, 0,
+                         0, None)
+    if rc != 0:
+        raise ValueError("ref_ao_render failed")
+    return accum
+
+
+def ref_debug_render(scene, camera, width, height, threads=0):
+    """One launch of the reference's debug.rgen / .rchit / .rmiss into an RGBA8
+    target, with the oracle's closest hit on `scene`."""
+    L = ref_lib()
+    if L is None:
+        raise FileNotFoundError("reference shaders not built (oracle/_ref)")
+    _ref_sibling_setup(L)
+    rgba8 = np.zeros((height, width, 4), np.uint8)
+    vi = (ctypes.c_float * 16)(*camera.view_inverse)
+    pi = (ctypes.c_float * 16)(*camera.projection_inverse)
+    hit = ctypes.cast(lib().oracle_closest_hit, _P)
+    rc = L.ref_debug_render(ctypes.byref(scene._desc), ctypes.cast(vi, _P), ctypes.cast(pi, _P), width, height,
+                            _ptr(rgba8), hit, scene.handle, threads)
+    if rc != 0:
+        raise ValueError("ref_debug_render failed")
+    return rgba8

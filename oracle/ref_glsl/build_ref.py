@@ -1,8 +1,9 @@
 """Builds oracle/_ref/libref_glsl.so from the reference's own GLSL sources.
 
 TEST INFRASTRUCTURE ONLY. Reads assets/glsl/sampling.glsl,
-postprocess.glsl, payload.glsl and the path's shaders pathtrace.rgen,
-pathtrace.rchit and pathtrace.rmiss from the reference checkout (default
+postprocess.glsl, payload.glsl and the ray-tracing shaders of the path
+(pathtrace.rgen / .rchit / .rmiss) and of its sibling pipelines (ao.* and
+debug.*) from the reference checkout (default
 /root/reference, or $SOLRT_REFERENCE), applies a mechanical GLSL -> C++
 rewrite and compiles them with glsl_shim.h; ref_glsl.cpp runs the three
 shaders as a ray-tracing pipeline on CPU threads, with traceRayEXT answered
@@ -42,7 +43,7 @@ OUT = os.path.join(ORACLE, "_ref")
 
 
 SHADERS = ("sampling.glsl", "postprocess.glsl", "payload.glsl", "pathtrace.rgen", "pathtrace.rchit",
-           "pathtrace.rmiss")
+           "pathtrace.rmiss", "ao.rgen", "ao.rchit", "ao.rmiss", "debug.rgen", "debug.rchit", "debug.rmiss")
 
 
 def reference_root():

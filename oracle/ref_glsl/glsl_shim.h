@@ -25,10 +25,14 @@ struct uvec3 {
     uint x, y, z;
     uvec2 xy() const { return uvec2{x, y}; }
 };
+struct vec2;
 struct ivec2 {
     int x, y;
     ivec2() : x(0), y(0) {}
+    ivec2(int a, int b) : x(a), y(b) {}
     ivec2(uvec2 v) : x((int)v.x), y((int)v.y) {}
+    explicit ivec2(const vec2& v);
+    ivec2 xy() const { return *this; }
 };
 struct ivec3 {
     int x, y, z;
@@ -42,7 +46,9 @@ struct vec2 {
     vec2(float s) : x(s), y(s) {}
     vec2(float a, float b) : x(a), y(b) {}
     vec2(uvec2 v) : x((float)v.x), y((float)v.y) {}
+    vec2(ivec2 v) : x((float)v.x), y((float)v.y) {}
 };
+inline ivec2::ivec2(const vec2& v) : x((int)v.x), y((int)v.y) {}
 
 struct vec4;
 struct vec3 {
@@ -62,6 +68,7 @@ struct vec4 {
     vec4(float a, float b, float c, float d) : x(a), y(b), z(c), w(d) {}
     vec4(vec3 v, float d) : x(v.x), y(v.y), z(v.z), w(d) {}
     vec3 xyz() const { return vec3{x, y, z}; }
+    float operator[](uint i) const { return i == 0 ? x : (i == 1 ? y : (i == 2 ? z : w)); }
 };
 inline vec3::vec3(const vec4& v) : x(v.x), y(v.y), z(v.z) {}
 
@@ -81,6 +88,15 @@ inline vec2 operator+(vec2 a, vec2 b) { return vec2{a.x + b.x, a.y + b.y}; }
 inline vec2 operator/(vec2 a, vec2 b) { return vec2{a.x / b.x, a.y / b.y}; }
 inline vec2 operator*(vec2 a, float s) { return vec2{a.x * s, a.y * s}; }
 inline vec2 operator-(vec2 a, float s) { return vec2{a.x - s, a.y - s}; }
+inline vec2 operator-(vec2 a, vec2 b) { return vec2{a.x - b.x, a.y - b.y}; }
+inline vec2 operator*(vec2 a, vec2 b) { return vec2{a.x * b.x, a.y * b.y}; }
+// mixed integer / float operands convert to float, as GLSL does implicitly
+inline vec2 operator*(vec2 a, ivec2 b) { return a * vec2{b}; }
+inline vec2 operator+(uvec2 a, vec2 b) { return vec2{a} + b; }
+// GLSL mod(x, y) = x - y * floor(x / y)
+inline vec2 mod(vec2 x, vec2 y) {
+    return vec2{x.x - y.x * std::floor(x.x / y.x), x.y - y.y * std::floor(x.y / y.y)};
+}
 
 inline vec3 operator+(vec3 a, vec3 b) { return vec3{a.x + b.x, a.y + b.y, a.z + b.z}; }
 inline vec3 operator-(vec3 a, vec3 b) { return vec3{a.x - b.x, a.y - b.y, a.z - b.z}; }
@@ -199,8 +215,20 @@ struct image2D {
     int width = 0;
 };
 inline vec4 imageLoad(const image2D& im, ivec2 p) {
-    const float* q = im.f32 + 4 * ((size_t)p.y * im.width + p.x);
-    return vec4{q[0], q[1], q[2], q[3]};
+    const size_t i = 4 * ((size_t)p.y * im.width + p.x);
+    if (im.f32) return vec4{im.f32[i], im.f32[i + 1], im.f32[i + 2], im.f32[i + 3]};
+    return vec4{im.u8[i] / 255.0f, im.u8[i + 1] / 255.0f, im.u8[i + 2] / 255.0f, im.u8[i + 3] / 255.0f};
+}
+
+// sampler2D of an RGBA8 UNORM texture: texelFetch returns c / 255
+struct sampler2D {
+    const unsigned char* texels = nullptr;
+    int width = 0, height = 0;
+};
+inline ivec2 textureSize(const sampler2D& s, int) { return ivec2{s.width, s.height}; }
+inline vec4 texelFetch(const sampler2D& s, ivec2 p, int) {
+    const unsigned char* t = s.texels + 4 * ((size_t)p.y * s.width + p.x);
+    return vec4{t[0] / 255.0f, t[1] / 255.0f, t[2] / 255.0f, t[3] / 255.0f};
 }
 inline void imageStore(image2D& im, ivec2 p, vec4 v) {
     const size_t i = 4 * ((size_t)p.y * im.width + p.x);

@@ -59,6 +59,31 @@ namespace ref_rmiss {
 REF_PIPELINE_TRIG
 #include "pathtrace.rmiss.inc"
 }
+// the AO pipeline (examples/4-ray-ao.rs)
+#undef SAMPLING_GLSL
+namespace ref_ao_rgen {
+REF_PIPELINE_TRIG
+#include "ao.rgen.inc"
+}
+#undef SAMPLING_GLSL
+namespace ref_ao_rchit {
+REF_PIPELINE_TRIG
+#include "ao.rchit.inc"
+}
+namespace ref_ao_rmiss {
+#include "ao.rmiss.inc"
+}
+// the debug pipeline (examples/3-ray-debug.rs): its payload is one vec3
+thread_local vec3 hitValue;
+namespace ref_dbg_rgen {
+#include "debug.rgen.inc"
+}
+namespace ref_dbg_rchit {
+#include "debug.rchit.inc"
+}
+namespace ref_dbg_rmiss {
+#include "debug.rmiss.inc"
+}
 }  // namespace glsl
 
 #undef in
@@ -77,7 +102,10 @@ typedef int (*ref_hit_fn)(const void* ctx, const float* o, const float* d, float
 
 namespace {
 
+enum Pipeline { kPath, kAo, kDebug };
+
 struct PathState {
+    Pipeline pipeline = kPath;
     ref_hit_fn hit = nullptr;
     const void* hit_ctx = nullptr;
     std::vector<uint32_t> sec_first;  // first triangle of each section (+ total)
@@ -98,10 +126,74 @@ void trace_ray(glsl::vec3 o, float tmin, glsl::vec3 d, float tmax) {
         glsl::gl_InstanceID = (int)s;
         glsl::gl_PrimitiveID = (int)(prim - f[s]);
         glsl::attribs = glsl::vec3{u, v, 0.0f};
-        glsl::ref_rchit::main();
+        if (g_path->pipeline == kPath) glsl::ref_rchit::main();
+        else if (g_path->pipeline == kAo) glsl::ref_ao_rchit::main();
+        else glsl::ref_dbg_rchit::main();
     } else {
-        glsl::ref_rmiss::main();
+        if (g_path->pipeline == kPath) glsl::ref_rmiss::main();
+        else if (g_path->pipeline == kAo) glsl::ref_ao_rmiss::main();
+        else glsl::ref_dbg_rmiss::main();
     }
+}
+
+// The closest-hit shaders' buffers (pathtrace.rchit / ao.rchit bindings 3-6)
+// from a scene description: instances (identity when absent, id = section),
+// each section's vertices and u64 indices (src/scene/mod.rs:228-233), and
+// each instance's material.
+struct SceneBufs {
+    std::vector<solrt_instance> inst;
+    std::vector<const solrt_vertex*> verts;
+    std::vector<std::vector<uint64_t>> idx64;
+    std::vector<solrt_material> mats;
+};
+
+bool scene_bufs(const solrt_scene_desc* desc, SceneBufs& b, PathState& st) {
+    static const float ident[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    const uint32_t S = desc->section_count;
+    b.inst.resize(S);
+    b.verts.resize(S);
+    b.idx64.resize(S);
+    b.mats.resize(S);
+    uint32_t first = 0;
+    for (uint32_t s = 0; s < S; ++s) {
+        const solrt_section& sec = desc->sections[s];
+        if (sec.material_index >= desc->material_count) return false;
+        if (desc->instances) {
+            b.inst[s] = desc->instances[s];
+        } else {
+            b.inst[s] = solrt_instance{};
+            b.inst[s].id = s;
+            std::memcpy(b.inst[s].transform, ident, sizeof(ident));
+            std::memcpy(b.inst[s].transform_it, ident, sizeof(ident));
+        }
+        b.verts[s] = desc->vertices + sec.vertex_offset;
+        b.idx64[s].assign(desc->indices + sec.index_offset, desc->indices + sec.index_offset + sec.index_count);
+        b.mats[s] = desc->materials[sec.material_index];
+        st.sec_first.push_back(first);
+        first += sec.index_count / 3;
+    }
+    st.sec_first.push_back(first);
+    return true;
+}
+
+// rgen main over rows [r0, r1) of a W x H launch on `threads` threads
+template <class F>
+void launch_rows(uint32_t width, uint32_t height, uint32_t r0, uint32_t r1, int threads, F rgen) {
+    if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    threads = std::min<int>(threads, (int)(r1 - r0));
+    auto rows = [&](int t) {
+        for (uint32_t y = r0 + (uint32_t)t; y < r1; y += (uint32_t)threads) {
+            for (uint32_t x = 0; x < width; ++x) {
+                glsl::gl_LaunchIDEXT = glsl::uvec3{x, y, 0u};
+                glsl::gl_LaunchSizeEXT = glsl::uvec3{width, height, 1u};
+                rgen();
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < threads; ++t) pool.emplace_back(rows, t);
+    rows(0);
+    for (auto& th : pool) th.join();
 }
 
 glsl::mat4 to_mat4(const float* m) {
@@ -229,6 +321,78 @@ int ref_path_render(const solrt_scene_desc* desc, const float* view_inverse, con
     for (auto& th : pool) th.join();
     g_path = nullptr;
     if (rays) *rays = st.rays.load();
+    return 0;
+}
+
+// One launch of examples/4-ray-ao.rs: ao.rgen (4 samples, at most 4 hits per
+// sample, as the shader fixes) with ao.rchit / ao.rmiss over rows [row_begin,
+// row_end) of a W x H launch (all rows when row_end is 0). `accum` is the
+// RGBA32F render target the example allocates (4-ray-ao.rs:58), read and
+// written; `noise` the RGBA8 blue-noise texture (nw x nh texels, rows as the
+// loader uploads them).
+int ref_ao_render(const solrt_scene_desc* desc, const float* view_inverse, const float* projection_inverse,
+                  uint32_t width, uint32_t height, uint32_t frame, int32_t accum_start, const uint8_t* noise,
+                  uint32_t nw, uint32_t nh, float* accum, ref_hit_fn hit, const void* hit_ctx, int threads,
+                  uint32_t row_begin, uint32_t row_end, uint64_t* rays) {
+    using namespace glsl;
+    if (!desc || !view_inverse || !projection_inverse || !accum || !noise || !hit || width == 0 || height == 0 ||
+        nw == 0 || nh == 0)
+        return 1;
+    PathState st;
+    st.pipeline = kAo;
+    st.hit = hit;
+    st.hit_ctx = hit_ctx;
+    SceneBufs b;
+    if (!scene_bufs(desc, b, st)) return 1;
+    const uint32_t S = desc->section_count;
+    std::vector<ref_ao_rchit::SceneInstance> inst(S);
+    std::vector<ref_ao_rchit::Vertices> verts(S);
+    std::vector<ref_ao_rchit::Indices> idx(S);
+    for (uint32_t s = 0; s < S; ++s) {
+        std::memcpy(&inst[s], &b.inst[s], sizeof(solrt_instance));
+        verts[s].v = reinterpret_cast<const ref_ao_rchit::ModelVertex*>(b.verts[s]);
+        idx[s].i = b.idx64[s].data();
+    }
+    ref_ao_rchit::scnDesc.i = inst.data();
+    ref_ao_rchit::vertices = verts.data();
+    ref_ao_rchit::indices = idx.data();
+    ref_ao_rchit::blueNoise = sampler2D{noise, (int)nw, (int)nh};
+    ref_ao_rgen::scene.view_inverse = to_mat4(view_inverse);
+    ref_ao_rgen::scene.projection_inverse = to_mat4(projection_inverse);
+    ref_ao_rgen::scene.frame = uvec3{width, height, frame};
+    ref_ao_rgen::push.accum_start_frame = accum_start;
+    ref_ao_rgen::image = image2D{accum, nullptr, (int)width};
+    if (row_end == 0 || row_end > height) row_end = height;
+    if (row_begin >= row_end) return 1;
+    g_path = &st;
+    g_trace = trace_ray;
+    launch_rows(width, height, row_begin, row_end, threads, [] { ref_ao_rgen::main(); });
+    g_path = nullptr;
+    if (rays) *rays = st.rays.load();
+    return 0;
+}
+
+// One launch of examples/3-ray-debug.rs: debug.rgen / .rchit / .rmiss into
+// the RGBA8 render target the example allocates (3-ray-debug.rs:54).
+int ref_debug_render(const solrt_scene_desc* desc, const float* view_inverse, const float* projection_inverse,
+                     uint32_t width, uint32_t height, uint8_t* rgba8, ref_hit_fn hit, const void* hit_ctx,
+                     int threads) {
+    using namespace glsl;
+    if (!desc || !view_inverse || !projection_inverse || !rgba8 || !hit || width == 0 || height == 0) return 1;
+    PathState st;
+    st.pipeline = kDebug;
+    st.hit = hit;
+    st.hit_ctx = hit_ctx;
+    SceneBufs b;
+    if (!scene_bufs(desc, b, st)) return 1;
+    ref_dbg_rgen::scene.view_inverse = to_mat4(view_inverse);
+    ref_dbg_rgen::scene.projection_inverse = to_mat4(projection_inverse);
+    ref_dbg_rgen::scene.frame = uvec3{width, height, 0u};
+    ref_dbg_rgen::image = image2D{nullptr, rgba8, (int)width};
+    g_path = &st;
+    g_trace = trace_ray;
+    launch_rows(width, height, 0, height, threads, [] { ref_dbg_rgen::main(); });
+    g_path = nullptr;
     return 0;
 }
 

@@ -1,5 +1,5 @@
-"""Generates tests/golden/glsl_sampling.json and ref_pathtrace_cornell.npz
-from the reference's own shaders.
+"""Generates tests/golden/glsl_sampling.json, ref_pathtrace_cornell.npz and
+ref_ao_debug_cornell.npz from the reference's own shaders.
 
 Builds oracle/_ref/libref_glsl.so (the reference's assets/glsl/sampling.glsl
 and postprocess.glsl compiled as C++ by oracle/ref_glsl/build_ref.py) and
@@ -137,6 +137,18 @@ def pathtrace_fixture():
         out["accum%d" % f] = acc.copy()
         out["rgba8_%d" % f] = rgba8.copy()
     path = os.path.join(HERE, "ref_pathtrace_cornell.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path)
+    # the sibling pipelines: ao.rgen / .rchit / .rmiss (frames 0 and 1, a seeded
+    # stand-in for the blue-noise texture) and debug.rgen / .rchit / .rmiss
+    noise = np.random.default_rng(20261204).integers(0, 256, (64, 64, 4), dtype=np.uint8)
+    out = {"noise": noise}
+    acc = None
+    for f in range(2):
+        acc = oracle.ref_ao_render(o, cam, w, h, noise, frame=f, accum=acc)
+        out["ao%d" % f] = acc.copy()
+    out["debug_rgba8"] = oracle.ref_debug_render(o, cam, w, h)
+    path = os.path.join(HERE, "ref_ao_debug_cornell.npz")
     np.savez_compressed(path, **out)
     print("wrote", path)
 

@@ -80,3 +80,28 @@ def test_integrator_errors(solrt, ctx):
     sc.close()
     img.close()
     c2.close()
+
+
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh2t", "bvh8"])
+def test_gpu_equals_reference_ao_debug_fixture(solrt, ctx, bvh):
+    """The device against the committed images of the reference's own
+    ao.rgen / .rchit / .rmiss and debug.rgen / .rchit / .rmiss compiled as
+    C++ (tests/golden/ref_ao_debug_cornell.npz): bit for bit."""
+    import os
+    fx = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_ao_debug_cornell.npz"))
+    d = S.cornell()
+    w, h = 32, 24
+    cam = camera_of(d, w / h)
+    ctx.set_blue_noise(fx["noise"])
+    sc = solrt.SceneDescription(ctx, d, bvh=bvh_kind(solrt, bvh))
+    img = solrt.Image(ctx, w, h)
+    r = solrt.Renderer(ctx)
+    for f in range(2):
+        r.cmd_trace_rays(sc, cam, solrt.render_params(w, h, spp=4, max_bounces=4, frame=f,
+                                                      integrator=solrt.INTEGRATOR_AO), img)
+        a32, _ = img.read()
+        assert np.array_equal(a32.view(np.uint32), fx["ao%d" % f].view(np.uint32)), f
+    dbg = solrt.Image(ctx, w, h)
+    r.cmd_trace_rays(sc, cam, solrt.render_params(w, h, spp=1, max_bounces=1, integrator=solrt.INTEGRATOR_DEBUG), dbg)
+    _, d8 = dbg.read()
+    assert np.array_equal(d8[..., :3], fx["debug_rgba8"][..., :3])

@@ -1,16 +1,18 @@
-"""The oracle's path against the reference's own shaders: pathtrace.rgen,
-pathtrace.rchit and pathtrace.rmiss (with sampling.glsl, postprocess.glsl
-and payload.glsl), rewritten to C++ by oracle/ref_glsl/build_ref.py and run
-as a ray-tracing pipeline on CPU threads, traceRayEXT answered by the
-oracle's watertight closest hit and sin / cos by the evaluation the oracle
-and the device share (GLSL leaves both to the implementation).
+"""The oracle's pipelines against the reference's own shaders:
+pathtrace.rgen / .rchit / .rmiss, ao.* and debug.* (with sampling.glsl,
+postprocess.glsl and payload.glsl), rewritten to C++ by
+oracle/ref_glsl/build_ref.py and run as ray-tracing pipelines on CPU
+threads, traceRayEXT answered by the oracle's watertight closest hit and
+sin / cos by the evaluation the oracle and the device share (GLSL leaves
+both to the implementation).
 
 The reference material model, its per-pixel TEA / PCG stream, 8 samples, 32
 bounces and mix accumulation map to MATERIAL_REF, RNG_REF_STREAM, spp 8,
 max_bounces 32 and ACCUM_REF_MIX: the images must be equal bit for bit.
-The pipeline is built when the reference checkout (or sources generated from
-it) is present; the committed fixture ref_pathtrace_cornell.npz, made by the
-same pipeline (tests/golden/make_golden.py), is checked everywhere."""
+The pipelines are built when the reference checkout (or sources generated
+from it) is present; the committed fixtures ref_pathtrace_cornell.npz and
+ref_ao_debug_cornell.npz, made by the same pipelines
+(tests/golden/make_golden.py), are checked everywhere."""
 import os
 
 import numpy as np
@@ -111,3 +113,45 @@ def test_oracle_equals_reference_pipeline_fixture(oracle):
         acc, rgba8, _ = o.render(cam, p, accum=acc)
         assert np.array_equal(acc.view(np.uint32), fx["accum%d" % f].view(np.uint32)), f
         assert np.array_equal(rgba8, fx["rgba8_%d" % f]), f
+
+
+def blue_noise_fixture():
+    """The seeded 64 x 64 RGBA8 stand-in of textures/HDR_RGBA_0.png that
+    tests/golden/make_golden.py used."""
+    return np.random.default_rng(20261204).integers(0, 256, (64, 64, 4), dtype=np.uint8)
+
+
+@pytest.mark.parametrize("name", ["cornell", "transformed", "soup"])
+def test_reference_ao_and_debug_shaders_equal_oracle(ref, name):
+    """ao.rgen / .rchit / .rmiss (4 samples, 4 hits, blue-noise directions,
+    RGBA32F target of 4-ray-ao.rs) and debug.rgen / .rchit / .rmiss (RGBA8
+    target of 3-ray-debug.rs) against the oracle's AO and debug integrators."""
+    d = {"cornell": S.cornell, "transformed": transformed_cornell, "soup": lambda: S.soup(20000, seed=3)}[name]()
+    w, h = 48, 40
+    cam = camera_of(d, w / h)
+    o = ref.OracleScene(d)
+    noise = blue_noise_fixture()
+    ra = oa = None
+    for f in range(3):
+        ra = ref.ref_ao_render(o, cam, w, h, noise, frame=f, accum=ra)
+        p = solrt.render_params(w, h, spp=4, max_bounces=4, frame=f, integrator=solrt.INTEGRATOR_AO)
+        oa, _, _ = o.render(cam, p, accum=oa, blue_noise=noise)
+        assert np.array_equal(ra.view(np.uint32), oa.view(np.uint32)), f
+    r8 = ref.ref_debug_render(o, cam, w, h)
+    _, d8, _ = o.render(cam, solrt.render_params(w, h, spp=1, max_bounces=1, integrator=solrt.INTEGRATOR_DEBUG))
+    assert np.array_equal(r8[..., :3], d8[..., :3])
+
+
+def test_oracle_equals_reference_ao_debug_fixture(oracle):
+    fx = np.load(os.path.join(HERE, "golden", "ref_ao_debug_cornell.npz"))
+    d = S.cornell()
+    w, h = 32, 24
+    cam = camera_of(d, w / h)
+    o = oracle.OracleScene(d)
+    acc = None
+    for f in range(2):
+        p = solrt.render_params(w, h, spp=4, max_bounces=4, frame=f, integrator=solrt.INTEGRATOR_AO)
+        acc, _, _ = o.render(cam, p, accum=acc, blue_noise=fx["noise"])
+        assert np.array_equal(acc.view(np.uint32), fx["ao%d" % f].view(np.uint32)), f
+    _, d8, _ = o.render(cam, solrt.render_params(w, h, spp=1, max_bounces=1, integrator=solrt.INTEGRATOR_DEBUG))
+    assert np.array_equal(d8[..., :3], fx["debug_rgba8"][..., :3])
