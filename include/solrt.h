@@ -230,7 +230,23 @@ typedef enum solrt_integrator {
      * set by solrt_context_set_blue_noise; colour = 1 - mean occlusion /
      * max_bounces, mixed into the image with 1 / (frame + 1 -
      * accum_start_frame) (ao.rgen:57-80). RGBA8 = UNORM of the colour. */
-    SOLRT_INTEGRATOR_AO = 2
+    SOLRT_INTEGRATOR_AO = 2,
+    /* Path tracing with next-event estimation, an estimator the reference
+     * does not have (it finds emitters only by hitting them). At every
+     * diffuse vertex that continues the path, after the vertex's three
+     * pathtrace.rchit draws, three more draws pick an emissive triangle
+     * (probability proportional to its world area when the scene was
+     * created) and a uniform point on it; one shadow ray per vertex goes
+     * through a second wavefront queue, and an unoccluded one adds
+     * throughput * albedo * Le * cos_x * cos_y * area / (pi * r^2 * p_pick)
+     * to the sample. Emitters hit after a bounce then add nothing (their
+     * light came through the shadow rays); camera rays that hit an emitter
+     * and misses keep the reference's terms. Same expected image as
+     * SOLRT_INTEGRATOR_PATH with material_mode SOLRT_MATERIAL_LAMBERT, less
+     * noise under small lights. Needs material_mode SOLRT_MATERIAL_LAMBERT
+     * and the wavefront kernel; runs in batches and the server. Shadow
+     * segments are counted in solrt_stats.shadow_segments, not segments. */
+    SOLRT_INTEGRATOR_PATH_NEE = 3
 } solrt_integrator;
 
 typedef enum solrt_kernel {
@@ -281,6 +297,8 @@ typedef struct solrt_stats {
     uint64_t shade_launches;  /* launches timed into shade_ms */
     double generate_ms;       /* camera-ray generation (enable_timing) */
     double accumulate_ms;     /* per-pixel sums, frame begin / finalize (enable_timing) */
+    uint64_t shadow_segments; /* shadow rays traced (SOLRT_INTEGRATOR_PATH_NEE) */
+    uint64_t shadow_unoccluded; /* of them, those that reached their light */
 } solrt_stats;
 
 typedef enum solrt_error_bits {

@@ -23,7 +23,8 @@ _api = importlib.import_module("sol-rs_gb300.api")
 
 class RenderStats(ctypes.Structure):
     _fields_ = [("segments", ctypes.c_uint64), ("paths", ctypes.c_uint64), ("fp64_fallbacks", ctypes.c_uint64),
-                ("node_visits", ctypes.c_uint64), ("tri_tests", ctypes.c_uint64)]
+                ("node_visits", ctypes.c_uint64), ("tri_tests", ctypes.c_uint64),
+                ("shadow_segments", ctypes.c_uint64), ("shadow_unoccluded", ctypes.c_uint64)]
 
 
 _P = ctypes.c_void_p

@@ -250,6 +250,14 @@ struct oracle_scene {
     std::vector<uint32_t> child;         // 2 per internal node
     std::vector<Box> node_box;           // per internal node
     std::vector<Box> leaf_box;           // per sorted position
+    // next-event estimation: emissive triangles with their inclusive float
+    // prefix of world areas (triangle order) and pick probability
+    struct Light {
+        float cdf, pick;
+        uint32_t prim;
+    };
+    std::vector<Light> lights;
+    float light_total = 0.0f;
 };
 
 namespace {
@@ -587,6 +595,7 @@ template <class R> HitR<R> closest_hit(const oracle_scene* s, V3<R> o, V3<R> d, 
 
 struct Counters {
     uint64_t seg = 0, paths = 0, fb = 0, nv = 0, nt = 0;
+    uint64_t shadow = 0, unoccluded = 0;  // next-event estimation
 };
 
 // Shading normal and position of a hit (pathtrace.rchit:82-90,
@@ -605,10 +614,64 @@ template <class R> void hit_frame(const oracle_scene* s, const TriW& tri, R b0, 
     pos = V3<R>{o[0], o[1], o[2]};
 }
 
+// Next-event estimation at a diffuse vertex (SOLRT_INTEGRATOR_PATH_NEE, an
+// estimator the reference does not have). Three draws: l0 picks an emissive
+// triangle by its area prefix, l1 and l2 a uniform point on it
+// (b0 = 1 - sqrt(l1), b1 = l2 sqrt(l1)); the shadow ray leaves from the
+// continuation origin `no` towards it with tmax 0.9999 of the distance. An
+// unoccluded one returns thr * Le * cos_x * cos_y * area / (pi r^2 p_pick):
+// Lambert albedo / pi (thr already holds the albedo) times Le times the
+// geometry term over the area pdf p_pick / area. Emitters are two-sided.
+template <class R> bool nee_term(const oracle_scene* s, V3<R> no, V3<R> n_o, V3<R> thr, R tmin, uint32_t& rng,
+                                 Counters& cn, V3<R>& contrib) {
+    const R l0 = next_rand<R>(rng);
+    const R l1 = next_rand<R>(rng);
+    const R l2 = next_rand<R>(rng);
+    if (s->lights.empty()) return false;
+    const R target = l0 * R(s->light_total);
+    size_t lo = 0, hi = s->lights.size() - 1;  // first light whose prefix exceeds the target
+    while (lo < hi) {
+        const size_t mid = (lo + hi) / 2;
+        if (R(s->lights[mid].cdf) > target) hi = mid;
+        else lo = mid + 1;
+    }
+    const oracle_scene::Light& L = s->lights[lo];
+    const TriW& tri = s->tris[L.prim];
+    auto cv = [](V3<float> a) { return V3<R>{R(a.x), R(a.y), R(a.z)}; };
+    const V3<R> p0 = cv(tri.p[0]), p1 = cv(tri.p[1]), p2 = cv(tri.p[2]);
+    const R su = std::sqrt(l1);
+    const R b0 = R(1) - su, b1 = l2 * su;
+    const R b2 = (R(1) - b0) - b1;
+    const V3<R> y = p0 * b0 + p1 * b1 + p2 * b2;
+    const V3<R> e1 = p1 - p0, e2 = p2 - p0;
+    const V3<R> ng{e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x};
+    const R a2 = length(ng);
+    const V3<R> w = y - no;
+    const R d2 = dot(w, w);
+    if (!(a2 > R(0)) || !(d2 > R(0))) return false;
+    const R dist = std::sqrt(d2);
+    const V3<R> wl{w.x / dist, w.y / dist, w.z / dist};
+    const R cx = dot(n_o, wl);
+    const R cy = std::abs(dot(ng, wl)) / a2;
+    const R tmax = dist * R(0.9999f);
+    if (!(cx > R(0)) || !(cy > R(0)) || !(tmax > tmin)) return false;
+    const float* le = s->mats[tri.mat].emissive;
+    const R wgt = ((cx * cy) * (R(0.5f) * a2)) / ((R(3.14159265f) * d2) * R(L.pick));
+    ++cn.shadow;
+    uint64_t nv = 0, nt = 0, fb = 0;
+    const HitR<R> h = closest_hit<R>(s, no, wl, tmin, tmax, 1, fb, nv, nt);
+    if (h.prim != SOLRT_NO_HIT) return false;
+    ++cn.unoccluded;
+    contrib = (thr * V3<R>{R(le[0]), R(le[1]), R(le[2])}) * wgt;
+    return true;
+}
+
 template <class R> V3<R> trace_path(const oracle_scene* s, const solrt_render_params* p, V3<R> o,
                                     V3<R> d, R tmin, R tmax, uint32_t& rng, Counters& cn) {
     V3<R> acc{R(1), R(1), R(1)};
     uint32_t depth = 0;
+    const bool nee = p->integrator == SOLRT_INTEGRATOR_PATH_NEE;
+    V3<R> nee_sum{R(0), R(0), R(0)};  // shadow terms in bounce order, then the path's end
     for (;;) {
         const HitR<R> h = closest_hit<R>(s, o, d, tmin, tmax, 1, cn.fb, cn.nv, cn.nt);
         ++cn.seg;
@@ -619,7 +682,8 @@ template <class R> V3<R> trace_path(const oracle_scene* s, const solrt_render_pa
         const TriW& tri = s->tris[h.prim];                  // pathtrace.rchit
         const solrt_material& m = s->mats[tri.mat];
         if (m.emissive[0] >= 1.0f || m.emissive[1] >= 1.0f || m.emissive[2] >= 1.0f) {
-            acc = acc * V3<R>{R(m.emissive[0]), R(m.emissive[1]), R(m.emissive[2])};
+            if (nee && depth > 0) acc = V3<R>{R(0), R(0), R(0)};  // its light came through shadow rays
+            else acc = acc * V3<R>{R(m.emissive[0]), R(m.emissive[1]), R(m.emissive[2])};
             break;
         }
         const R b1 = h.u, b2 = h.v;
@@ -659,8 +723,10 @@ template <class R> V3<R> trace_path(const oracle_scene* s, const solrt_render_pa
             acc = V3<R>{R(0), R(0), R(0)};
             break;
         }
+        V3<R> c;
+        if (nee && nee_term<R>(s, o, n_o, acc, tmin, rng, cn, c)) nee_sum = nee_sum + c;
     }
-    return acc;
+    return nee ? nee_sum + acc : acc;
 }
 
 template <class R> struct Cam {
@@ -903,6 +969,23 @@ oracle_scene* oracle_scene_create(const solrt_scene_desc* desc) {
         return nullptr;
     }
     build_lbvh(s);
+    // emissive as pathtrace.rchit:75-80 decides it; areas of the world
+    // triangles in float, summed in triangle order
+    float total = 0.0f;
+    for (uint32_t t = 0; t < (uint32_t)s->tris.size(); ++t) {
+        const TriW& tr = s->tris[t];
+        const solrt_material& m = s->mats[tr.mat];
+        if (!(m.emissive[0] >= 1.0f || m.emissive[1] >= 1.0f || m.emissive[2] >= 1.0f)) continue;
+        const V3<float> e1 = tr.p[1] - tr.p[0], e2 = tr.p[2] - tr.p[0];
+        const float nx = e1.y * e2.z - e1.z * e2.y, ny = e1.z * e2.x - e1.x * e2.z, nz = e1.x * e2.y - e1.y * e2.x;
+        const float area = 0.5f * std::sqrt((nx * nx + ny * ny) + nz * nz);
+        if (!(area > 0.0f)) continue;
+        total = total + area;
+        s->lights.push_back(oracle_scene::Light{total, area, t});
+    }
+    if (!(total > 0.0f) || !std::isfinite(total)) s->lights.clear();
+    for (oracle_scene::Light& L : s->lights) L.pick = L.pick / total;
+    s->light_total = s->lights.empty() ? 0.0f : total;
     return s;
 }
 
@@ -994,8 +1077,10 @@ static int render_impl(const oracle_scene* s, const solrt_camera* cam, const sol
                        const uint8_t* noise = nullptr, uint32_t nw = 0, uint32_t nh = 0) {
     if (!s || !cam || !p || p->width == 0 || p->height == 0 || p->spp == 0) return 1;
     if (!samples_out && (!accum || !rgba8)) return 1;
-    if (p->integrator > SOLRT_INTEGRATOR_AO) return 1;
-    if (p->integrator != SOLRT_INTEGRATOR_PATH && samples_out) return 1;
+    if (p->integrator > SOLRT_INTEGRATOR_PATH_NEE) return 1;
+    if (p->integrator == SOLRT_INTEGRATOR_PATH_NEE && p->material_mode != SOLRT_MATERIAL_LAMBERT) return 1;
+    const bool path = p->integrator == SOLRT_INTEGRATOR_PATH || p->integrator == SOLRT_INTEGRATOR_PATH_NEE;
+    if (!path && samples_out) return 1;
     if (p->integrator == SOLRT_INTEGRATOR_AO && (!noise || nw == 0 || nh == 0 || p->max_bounces == 0)) return 1;
     if (!samples_out && p->accum_mode == SOLRT_ACCUM_KAHAN && (!ksum || !kcomp)) return 1;
     if (row_end <= row_begin) { row_begin = 0; row_end = p->height; }
@@ -1027,6 +1112,8 @@ static int render_impl(const oracle_scene* s, const solrt_camera* cam, const sol
             stats->fp64_fallbacks += c.fb;
             stats->node_visits += c.nv;
             stats->tri_tests += c.nt;
+            stats->shadow_segments += c.shadow;
+            stats->shadow_unoccluded += c.unoccluded;
         }
     }
     return 0;

@@ -48,6 +48,8 @@ typedef struct oracle_render_stats {
     uint64_t fp64_fallbacks;
     uint64_t node_visits;
     uint64_t tri_tests;
+    uint64_t shadow_segments;    /* SOLRT_INTEGRATOR_PATH_NEE shadow rays */
+    uint64_t shadow_unoccluded;  /* of them, those that reached their light */
 } oracle_render_stats;
 
 /* Flattens to world space and builds the CPU LBVH. NULL on error. */

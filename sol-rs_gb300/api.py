@@ -27,7 +27,7 @@ MATERIAL_REF, MATERIAL_LAMBERT = 0, 1
 ACCUM_REF_MIX, ACCUM_KAHAN = 0, 1
 RNG_REF_STREAM, RNG_PER_SAMPLE = 0, 1
 KERNEL_WAVEFRONT, KERNEL_MEGA = 0, 1
-INTEGRATOR_PATH, INTEGRATOR_DEBUG, INTEGRATOR_AO = 0, 1, 2
+INTEGRATOR_PATH, INTEGRATOR_DEBUG, INTEGRATOR_AO, INTEGRATOR_PATH_NEE = 0, 1, 2, 3
 BVH_DYNAMIC, BVH_SAH = 1, 2
 REGEN_REBUILD, REGEN_REFIT = 0, 1
 EFLAG_STACK, EFLAG_QUEUE, EFLAG_INDEX, EFLAG_TIMEOUT = 1, 2, 4, 8
@@ -134,7 +134,8 @@ class Stats(ctypes.Structure):
                 ("tri_tests", ctypes.c_uint64), ("fp64_fallbacks", ctypes.c_uint64), ("launches", ctypes.c_uint64),
                 ("error_flags", ctypes.c_uint32), ("reserved", ctypes.c_uint32), ("render_ms", ctypes.c_double),
                 ("extend_ms", ctypes.c_double), ("shade_ms", ctypes.c_double), ("extend_launches", ctypes.c_uint64),
-                ("shade_launches", ctypes.c_uint64), ("generate_ms", ctypes.c_double), ("accumulate_ms", ctypes.c_double)]
+                ("shade_launches", ctypes.c_uint64), ("generate_ms", ctypes.c_double), ("accumulate_ms", ctypes.c_double),
+                ("shadow_segments", ctypes.c_uint64), ("shadow_unoccluded", ctypes.c_uint64)]
 
 
 class ContextDesc(ctypes.Structure):
@@ -490,8 +491,9 @@ def render_params(width, height, spp=8, max_bounces=32, frame=0, accum_start_fra
     """Defaults are the reference's: 8 spp per launch, 32 bounces, black miss,
     pathtrace.rchit materials, running mix, one RNG stream per pixel.
     kernel: KERNEL_WAVEFRONT (0) or KERNEL_MEGA (1, per-pixel loop).
-    integrator: INTEGRATOR_PATH, INTEGRATOR_DEBUG or INTEGRATOR_AO (the
-    reference's AO pipeline uses spp=4, max_bounces=4)."""
+    integrator: INTEGRATOR_PATH, INTEGRATOR_DEBUG, INTEGRATOR_AO (the
+    reference's AO pipeline uses spp=4, max_bounces=4) or INTEGRATOR_PATH_NEE
+    (next-event estimation through a shadow-ray queue; MATERIAL_LAMBERT)."""
     return RenderParams(width=width, height=height, spp=spp, max_bounces=max_bounces, frame=frame,
                         accum_start_frame=accum_start_frame, seed=seed, job_id=job_id, miss_mode=miss_mode,
                         material_mode=material_mode, accum_mode=accum_mode, rng_mode=rng_mode, tmax=tmax,

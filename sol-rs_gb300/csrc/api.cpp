@@ -59,12 +59,15 @@ namespace {
     } while (0)
 
 solrt_status check_device_flags(Context& ctx) {
-    unsigned int flags = 0;
+    // block 0: path segments; block 1: shadow rays
+    unsigned int fl[2] = {0u, 0u};
     DevStats* st = ctx.stats.as<DevStats>();
-    SOLRT_CUDA(cudaMemcpyAsync(&flags, &st->eflags, sizeof(flags), cudaMemcpyDeviceToHost, ctx.stream));
+    for (int k = 0; k < 2; ++k)
+        SOLRT_CUDA(cudaMemcpyAsync(&fl[k], &st[k].eflags, sizeof(unsigned int), cudaMemcpyDeviceToHost, ctx.stream));
     SOLRT_CUDA(cudaStreamSynchronize(ctx.stream));
+    const unsigned int flags = fl[0] | fl[1];
     if (flags == 0) return SOLRT_OK;
-    SOLRT_CUDA(cudaMemsetAsync(&st->eflags, 0, sizeof(unsigned int), ctx.stream));
+    for (int k = 0; k < 2; ++k) SOLRT_CUDA(cudaMemsetAsync(&st[k].eflags, 0, sizeof(unsigned int), ctx.stream));
     SOLRT_CUDA(cudaStreamSynchronize(ctx.stream));
     set_error("device error flags 0x%x (1 stack overflow, 2 queue overflow, 4 bad index, 8 timeout)", flags);
     if (flags & SOLRT_EFLAG_TIMEOUT) return SOLRT_ERR_TIMEOUT;
@@ -233,10 +236,10 @@ solrt_status solrt_context_create(const solrt_context_desc* desc, solrt_context*
     if ((s = c->hits.alloc(16 * C)) != SOLRT_OK) return fail(s);
     if ((s = c->rad.alloc(16 * C)) != SOLRT_OK) return fail(s);
     if ((s = c->ctl.alloc(sizeof(PassCtl))) != SOLRT_OK) return fail(s);
-    if ((s = c->stats.alloc(sizeof(DevStats))) != SOLRT_OK) return fail(s);
+    if ((s = c->stats.alloc(2 * sizeof(DevStats))) != SOLRT_OK) return fail(s);
     if ((s = c->trace_work.alloc(sizeof(unsigned int))) != SOLRT_OK) return fail(s);
     if (cudaMemset(c->ctl.ptr, 0, sizeof(PassCtl)) != cudaSuccess ||
-        cudaMemset(c->stats.ptr, 0, sizeof(DevStats)) != cudaSuccess ||
+        cudaMemset(c->stats.ptr, 0, 2 * sizeof(DevStats)) != cudaSuccess ||
         cudaDeviceSynchronize() != cudaSuccess) {
         set_error("device initialisation failed");
         return fail(SOLRT_ERR_DEVICE);
@@ -276,8 +279,9 @@ solrt_status solrt_synchronize(solrt_context* ctx) {
 
 solrt_status solrt_get_stats(solrt_context* ctx, solrt_stats* out) {
     CHECK_ARG(ctx && out, "null argument");
-    DevStats d;
-    SOLRT_CUDA(cudaMemcpyAsync(&d, ctx->stats.ptr, sizeof(d), cudaMemcpyDeviceToHost, ctx->stream));
+    DevStats d2[2];
+    SOLRT_CUDA(cudaMemcpyAsync(d2, ctx->stats.ptr, sizeof(d2), cudaMemcpyDeviceToHost, ctx->stream));
+    const DevStats& d = d2[0];
     SOLRT_CUDA(cudaStreamSynchronize(ctx->stream));
     ctx->timing_collect();
     std::memset(out, 0, sizeof(*out));
@@ -293,7 +297,9 @@ solrt_status solrt_get_stats(solrt_context* ctx, solrt_stats* out) {
     out->tri_tests = d.tri_tests;
     out->fp64_fallbacks = d.fp64_fallbacks;
     out->launches = ctx->launches;
-    out->error_flags = d.eflags;
+    out->error_flags = d.eflags | d2[1].eflags;
+    out->shadow_segments = d2[1].segments;
+    out->shadow_unoccluded = d2[1].unoccluded;
     float ms = 0.0f;
     if (cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1) == cudaSuccess) out->render_ms = ms;
     cudaGetLastError();
@@ -302,7 +308,7 @@ solrt_status solrt_get_stats(solrt_context* ctx, solrt_stats* out) {
 
 solrt_status solrt_reset_stats(solrt_context* ctx) {
     CHECK_ARG(ctx, "null context");
-    SOLRT_CUDA(cudaMemsetAsync(ctx->stats.ptr, 0, sizeof(DevStats), ctx->stream));
+    SOLRT_CUDA(cudaMemsetAsync(ctx->stats.ptr, 0, 2 * sizeof(DevStats), ctx->stream));
     SOLRT_CUDA(cudaStreamSynchronize(ctx->stream));
     ctx->timing_collect();
     ctx->launches = 0;
@@ -429,6 +435,39 @@ solrt_status solrt_scene_create(solrt_context* ctx, const solrt_scene_desc* d, c
         set_error("scene upload failed");
         return fail(SOLRT_ERR_DEVICE);
     }
+    // Emissive triangles for next-event estimation, emissive as the closest-hit
+    // shader decides it (any emissive channel >= 1, pathtrace.rchit:75-80):
+    // per light its inclusive float prefix of world areas in triangle order,
+    // its pick probability area / total and its triangle.
+    std::vector<float4> lights;
+    float total = 0.0f;
+    for (uint64_t t = 0; t < nt; ++t) {
+        const solrt_material& m = d->materials[sec_mat[tri[t].w]];
+        if (!(m.emissive[0] >= 1.0f || m.emissive[1] >= 1.0f || m.emissive[2] >= 1.0f)) continue;
+        const float4 a = pos[tri[t].x], b = pos[tri[t].y], c = pos[tri[t].z];
+        const float e1x = b.x - a.x, e1y = b.y - a.y, e1z = b.z - a.z;
+        const float e2x = c.x - a.x, e2y = c.y - a.y, e2z = c.z - a.z;
+        const float nx = e1y * e2z - e1z * e2y, ny = e1z * e2x - e1x * e2z, nz = e1x * e2y - e1y * e2x;
+        const float area = 0.5f * std::sqrt((nx * nx + ny * ny) + nz * nz);
+        if (!(area > 0.0f)) continue;  // cannot be hit, never picked
+        total = total + area;
+        const uint32_t prim = (uint32_t)t;
+        float pf;
+        std::memcpy(&pf, &prim, sizeof(pf));
+        lights.push_back(make_float4(total, area, pf, 0.0f));
+    }
+    if (!(total > 0.0f) || !std::isfinite(total)) lights.clear();
+    for (float4& L : lights) L.y = L.y / total;
+    if (!lights.empty()) {
+        if ((s = sc->lights.alloc(sizeof(float4) * lights.size())) != SOLRT_OK) return fail(s);
+        if (cudaMemcpyAsync(sc->lights.ptr, lights.data(), sizeof(float4) * lights.size(), cudaMemcpyHostToDevice,
+                            st) != cudaSuccess) {
+            set_error("scene upload failed");
+            return fail(SOLRT_ERR_DEVICE);
+        }
+    }
+    sc->light_count = (uint32_t)lights.size();
+    sc->light_total = lights.empty() ? 0.0f : total;
     sc->section_count = d->section_count;
     sc->sec_tri_first = std::move(sec_first);
     sc->sec_tri_count = std::move(sec_count);
@@ -494,7 +533,7 @@ solrt_status solrt_scene_bytes(solrt_scene* scene, uint64_t* out) {
            scene->materials.bytes + scene->sec_mat.bytes + scene->nodes.bytes + scene->tri_wt.bytes +
            scene->vsec_start.bytes + scene->instances.bytes + scene->topo_order.bytes + scene->topo_child.bytes +
            scene->topo_par_int.bytes + scene->topo_par_leaf.bytes + scene->topo_range.bytes + scene->tlas.bytes +
-           scene->inst_table.bytes;
+           scene->inst_table.bytes + scene->lights.bytes;
     return SOLRT_OK;
 }
 

@@ -77,6 +77,7 @@ struct DevStats {
     unsigned long long node_visits;
     unsigned long long tri_tests;
     unsigned long long fp64_fallbacks;
+    unsigned long long unoccluded;  // shadow rays that reached their light
     unsigned int eflags;
     unsigned int pad;
 };
@@ -86,6 +87,8 @@ struct DevStats {
 struct PassCtl {
     unsigned int count[SOLRT_MAX_BOUNCES + 2];
     unsigned int work[SOLRT_MAX_BOUNCES + 2];
+    unsigned int scount[SOLRT_MAX_BOUNCES + 2];  // shadow queue per bounce
+    unsigned int swork[SOLRT_MAX_BOUNCES + 2];
 };
 
 // Structure-of-arrays path queue (one wavefront).
@@ -130,6 +133,7 @@ struct PassPlan {
     uint32_t item_begin, item_count;
     uint32_t paths, pixels;
     uint32_t bounces;  // extend/shade launches of the pass
+    uint32_t nee = 0;  // a job of the pass uses SOLRT_INTEGRATOR_PATH_NEE
 };
 
 struct Context;
@@ -179,7 +183,9 @@ struct Context {
     uint32_t capacity = 0;
     bool counters = false;
     uint32_t block_size = 0;
-    DeviceBuffer q_o[2], q_d[2], q_thr[2], q_meta[2];
+    // queues 0 and 1: paths of alternate bounces; queue 2: shadow rays of
+    // SOLRT_INTEGRATOR_PATH_NEE (allocated when a render first needs it)
+    DeviceBuffer q_o[3], q_d[3], q_thr[3], q_meta[3];
     DeviceBuffer hits, rad, ctl, stats, trace_work;
     DeviceBuffer blue_noise;  // RGBA8 texels of SOLRT_INTEGRATOR_AO
     DeviceBuffer sibling_job;  // one-job table of DEBUG / AO launches
@@ -264,6 +270,10 @@ struct Scene {
     std::vector<int32_t> blas_root;
     uint32_t blas_depth = 0, tlas_count = 0, tlas_depth = 0;
     DeviceBuffer tlas, inst_table;
+    // emissive triangles (see DevScene::lights), fixed at creation
+    DeviceBuffer lights;
+    uint32_t light_count = 0;
+    float light_total = 0.0f;
     DevScene view() const {
         DevScene d;
         d.tri_count = tri_count;
@@ -284,6 +294,9 @@ struct Scene {
         d.materials = materials.as<float4>();
         d.nodes = nodes.as<float4>();
         d.tri_wt = tri_wt.as<float4>();
+        d.lights = lights.as<float4>();
+        d.light_count = light_count;
+        d.light_total = light_total;
         return d;
     }
 };
@@ -303,8 +316,10 @@ solrt_status regenerate_scene(Context& ctx, Scene& sc, uint32_t mode);
 // trace.cu
 solrt_status launch_trace_rays(Context& ctx, const Scene& sc, const solrt_ray* rays, uint32_t n, solrt_hit* hits);
 // Extend for a batched queue: the scene of ray i is jobs[meta[i].y >> kDepthBits].sc.
+// Closest hits of the `*count` rays of queue `q`; `st` (default: the
+// context's first stats block) receives their segment and visit counts.
 solrt_status launch_extend(Context& ctx, uint32_t kind, const DevJob* jobs, const PathQueue& q, float4* hits,
-                           const unsigned int* count, unsigned int* work);
+                           const unsigned int* count, unsigned int* work, DevStats* st = nullptr);
 // Whether an extend kernel exists for this block size / shared stack slots.
 bool extend_variant_ok(uint32_t block, uint32_t smem);
 
@@ -322,6 +337,8 @@ solrt_status serve_tick(Context& ctx, TickBuffers& tb, uint32_t kind, const std:
                         const std::vector<DevItem>& items, const PassPlan& pp, const std::vector<DevJob>& fin);
 DevJob job_for(const Scene& sc, const Image& img, const solrt_camera& cam, const solrt_render_params& p);
 solrt_status check_job(const Context& ctx, const Scene& sc, const Image& img, const solrt_render_params& p);
+// Allocates the shadow-ray queue of SOLRT_INTEGRATOR_PATH_NEE (no-op once done).
+solrt_status ensure_shadow_queue(Context& ctx);
 solrt_status debug_unit(Context& ctx, uint32_t op, uint32_t n, const uint32_t* a, const uint32_t* b,
                         const float* in_f32, uint32_t* out_u32, float* out_f32);
 

@@ -64,8 +64,11 @@ SOLRT_D void hit_frame(const DevScene& sc, uint4 ti, float b0, float b1, float b
 // and pathtrace.rgen:77-84). h = (t, prim bits, u, v). Updates the path
 // throughput `acc`, the rng state and the depth; returns true when the path
 // continues with the ray (o_next, d_next).
+// With SOLRT_INTEGRATOR_PATH_NEE an emitter hit after a bounce adds nothing
+// (next-event estimation carried that light), and `n_out`, when given,
+// receives the oriented shading normal of a continuing path.
 SOLRT_D bool shade_step(const DevJob& J, float4 o, float4 d, float4 h, f3& acc, uint32_t& rng, uint32_t& depth,
-                        float4& o_next, float4& d_next, uint32_t& ef) {
+                        float4& o_next, float4& d_next, uint32_t& ef, f3* n_out = nullptr) {
     const DevScene& sc = J.sc;
     const f3 dir{d.x, d.y, d.z};
     const uint32_t prim = __float_as_uint(h.y);
@@ -80,7 +83,8 @@ SOLRT_D bool shade_step(const DevJob& J, float4 o, float4 d, float4 h, f3& acc, 
     const float4 m1 = __ldg(sc.materials + 3 * mat + 1);
     const float4 m2 = __ldg(sc.materials + 3 * mat + 2);
     if (m1.x >= 1.0f || m1.y >= 1.0f || m1.z >= 1.0f) {                      // rchit:75-80
-        acc = acc * f3{m1.x, m1.y, m1.z};
+        if (J.integrator == SOLRT_INTEGRATOR_PATH_NEE && depth > 0u) acc = f3{0.0f, 0.0f, 0.0f};
+        else acc = acc * f3{m1.x, m1.y, m1.z};
         return false;
     }
     const float b1 = h.z, b2 = h.w;
@@ -122,6 +126,58 @@ SOLRT_D bool shade_step(const DevJob& J, float4 o, float4 d, float4 h, f3& acc, 
     }
     o_next = make_float4(no.x, no.y, no.z, o.w);
     d_next = make_float4(nd.x, nd.y, nd.z, d.w);
+    if (n_out) *n_out = n_o;
+    return true;
+}
+
+// Next-event estimation at a diffuse vertex of SOLRT_INTEGRATOR_PATH_NEE (an
+// estimator the reference does not have). Three draws: l0 picks an emissive
+// triangle by its area prefix, l1 and l2 a uniform point on it
+// (b0 = 1 - sqrt(l1), b1 = l2 sqrt(l1)). `no` is the continuation origin
+// (hit + 1e-4 n_o), `thr` the throughput after the vertex's albedo. Returns
+// true with the shadow ray (so, sd: unit direction, tmax 0.9999 of the
+// distance) and the radiance it adds when unoccluded:
+// thr * Le * cos_x * cos_y * area / (pi * r^2 * p_pick), i.e. the Lambert
+// BRDF albedo / pi times Le times the geometry term over the area pdf
+// p_pick / area. Emitters are two-sided, as hits on them are (rchit:75-80).
+SOLRT_D bool nee_sample(const DevScene& sc, f3 no, f3 n_o, f3 thr, float tmin, uint32_t& rng, float4& so,
+                        float4& sd, f3& contrib) {
+    const float l0 = next_rand(rng);
+    const float l1 = next_rand(rng);
+    const float l2 = next_rand(rng);
+    if (sc.light_count == 0u) return false;
+    const float target = l0 * sc.light_total;
+    uint32_t lo = 0, hi = sc.light_count - 1u;  // first light whose prefix exceeds the target
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&sc.lights[mid].x) > target) hi = mid;
+        else lo = mid + 1u;
+    }
+    const float4 L = __ldg(sc.lights + lo);
+    const uint4 ti = __ldg(sc.tri_idx + __float_as_uint(L.z));
+    const float4 a = __ldg(sc.vpos + ti.x), b = __ldg(sc.vpos + ti.y), c = __ldg(sc.vpos + ti.z);
+    const f3 p0{a.x, a.y, a.z}, p1{b.x, b.y, b.z}, p2{c.x, c.y, c.z};
+    const float su = sqrtf(l1);
+    const float b0 = 1.0f - su, b1 = l2 * su;
+    const float b2 = (1.0f - b0) - b1;
+    const f3 y = p0 * b0 + p1 * b1 + p2 * b2;
+    const f3 e1 = p1 - p0, e2 = p2 - p0;
+    const f3 ng{e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x};
+    const float a2 = length(ng);  // twice the area
+    const f3 w = y - no;
+    const float d2 = dot(w, w);
+    if (!(a2 > 0.0f) || !(d2 > 0.0f)) return false;
+    const float dist = sqrtf(d2);
+    const f3 wl{w.x / dist, w.y / dist, w.z / dist};
+    const float cx = dot(n_o, wl);
+    const float cy = fabsf(dot(ng, wl)) / a2;
+    const float tmax = dist * 0.9999f;
+    if (!(cx > 0.0f) || !(cy > 0.0f) || !(tmax > tmin)) return false;
+    const float4 le = __ldg(sc.materials + 3 * __ldg(sc.sec_mat + ti.w) + 1);
+    const float wgt = ((cx * cy) * (0.5f * a2)) / ((3.14159265f * d2) * L.y);
+    contrib = (thr * f3{le.x, le.y, le.z}) * wgt;
+    so = make_float4(no.x, no.y, no.z, tmin);
+    sd = make_float4(wl.x, wl.y, wl.z, tmax);
     return true;
 }
 

@@ -47,7 +47,8 @@ SOLRT_D uint32_t find_last_le(uint32_t n, uint32_t v, F key) {
 }
 
 __global__ void k_generate(const DevJob* __restrict__ jobs, const DevItem* __restrict__ items, uint32_t nitems,
-                           uint32_t P, PathQueue q, unsigned int* __restrict__ count0, DevStats* stats) {
+                           uint32_t P, PathQueue q, unsigned int* __restrict__ count0, DevStats* stats,
+                           float4* __restrict__ rad) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) {
         *count0 = P;
@@ -66,13 +67,15 @@ __global__ void k_generate(const DevJob* __restrict__ jobs, const DevItem* __res
     q.d_tmax[i] = d;
     q.thr_rng[i] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(rng));
     q.meta[i] = make_uint2(i, it.job << kDepthBits);
+    if (J.integrator == SOLRT_INTEGRATOR_PATH_NEE) rad[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // sums shadow terms
 }
 
 __global__ void __launch_bounds__(256) k_shade(const DevJob* __restrict__ jobs, const DevItem* __restrict__ items,
                                                uint32_t nitems, PathQueue qin, const float4* __restrict__ hits,
                                                const unsigned int* __restrict__ count_in, PathQueue qout,
                                                unsigned int* __restrict__ count_out, uint32_t capacity,
-                                               float4* __restrict__ rad, DevStats* stats) {
+                                               float4* __restrict__ rad, DevStats* stats, PathQueue qs,
+                                               unsigned int* __restrict__ count_s) {
     const unsigned int n = *count_in;
     const int lane = threadIdx.x & 31;
     const uint32_t lane_lt = (1u << lane) - 1u;
@@ -81,23 +84,36 @@ __global__ void __launch_bounds__(256) k_shade(const DevJob* __restrict__ jobs, 
     uint32_t ef = 0;
     for (uint32_t base = warp_global * 32u; base < n; base += warps * 32u) {
         const uint32_t i = base + lane;
-        bool alive = false;
+        bool alive = false, shadow = false;
         float4 out_o = make_float4(0, 0, 0, 0), out_d = make_float4(0, 0, 0, 0), out_t = make_float4(0, 0, 0, 0);
+        float4 s_o = make_float4(0, 0, 0, 0), s_d = make_float4(0, 0, 0, 0), s_c = make_float4(0, 0, 0, 0);
         uint2 m = make_uint2(0, 0);
         if (i < n) {
             const float4 o = qin.o_tmin[i], d = qin.d_tmax[i], tr = qin.thr_rng[i];
             m = qin.meta[i];
             const uint32_t job = m.y >> kDepthBits;
             const DevJob& J = jobs[job];
+            const bool nee = J.integrator == SOLRT_INTEGRATOR_PATH_NEE && qs.o_tmin != nullptr;
             uint32_t rng = __float_as_uint(tr.w);
             uint32_t depth = m.y & kDepthMask;
             f3 acc{tr.x, tr.y, tr.z};
-            if (shade_step(J, o, d, hits[i], acc, rng, depth, out_o, out_d, ef)) {
+            f3 n_o{0.0f, 0.0f, 0.0f};
+            if (shade_step(J, o, d, hits[i], acc, rng, depth, out_o, out_d, ef, &n_o)) {
                 alive = true;
+                if (nee) {
+                    f3 cn;
+                    shadow = nee_sample(J.sc, f3{out_o.x, out_o.y, out_o.z}, n_o, acc, o.w, rng, s_o, s_d, cn);
+                    s_c = make_float4(cn.x, cn.y, cn.z, 0.0f);
+                }
                 out_t = make_float4(acc.x, acc.y, acc.z, __uint_as_float(rng));
                 m.y = (job << kDepthBits) | depth;
             } else {
-                rad[m.x] = make_float4(acc.x, acc.y, acc.z, 0.0f);
+                if (nee) {  // after this path's earlier shadow terms (resolved in bounce order)
+                    const float4 r = rad[m.x];
+                    rad[m.x] = make_float4(r.x + acc.x, r.y + acc.y, r.z + acc.z, 0.0f);
+                } else {
+                    rad[m.x] = make_float4(acc.x, acc.y, acc.z, 0.0f);
+                }
                 if (J.rng_mode == SOLRT_RNG_REF_STREAM) {
                     const DevItem it = items[find_last_le(nitems, m.x, [&](uint32_t t) { return items[t].path_base; })];
                     J.rng_state[it.pix0 + (m.x - it.path_base) / it.k] = rng;
@@ -122,8 +138,46 @@ __global__ void __launch_bounds__(256) k_shade(const DevJob* __restrict__ jobs, 
                 }
             }
         }
+        const uint32_t smask = __ballot_sync(0xffffffffu, shadow);
+        if (smask) {
+            const int leader = __ffs(smask) - 1;
+            uint32_t pos0 = 0;
+            if (lane == leader) pos0 = atomicAdd(count_s, (unsigned int)__popc(smask));
+            pos0 = __shfl_sync(0xffffffffu, pos0, leader);
+            if (shadow) {
+                const uint32_t pos = pos0 + __popc(smask & lane_lt);
+                if (pos < capacity) {
+                    qs.o_tmin[pos] = s_o;
+                    qs.d_tmax[pos] = s_d;
+                    qs.thr_rng[pos] = s_c;
+                    qs.meta[pos] = m;
+                } else {
+                    ef |= SOLRT_EFLAG_QUEUE;
+                }
+            }
+        }
     }
     if (ef) atomicOr(&stats->eflags, ef);
+}
+
+// Adds the contribution of every shadow ray that reached its light to its
+// path's slot (one shadow ray per path and bounce, so no two threads share a
+// slot). Counts them into the shadow stats block.
+__global__ void __launch_bounds__(256) k_shadow_resolve(PathQueue qs, const float4* __restrict__ hits,
+                                                        const unsigned int* __restrict__ count_s,
+                                                        float4* __restrict__ rad, DevStats* sstats) {
+    const unsigned int n = *count_s;
+    uint32_t reached = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (__float_as_uint(hits[i].y) != SOLRT_NO_HIT) continue;
+        const float4 c = qs.thr_rng[i];
+        const uint32_t slot = qs.meta[i].x;
+        const float4 r = rad[slot];
+        rad[slot] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, 0.0f);
+        ++reached;
+    }
+    const uint32_t w = __reduce_add_sync(0xffffffffu, reached);
+    if ((threadIdx.x & 31) == 0 && w) atomicAdd(&sstats->unoccluded, (unsigned long long)w);
 }
 
 // Per-pixel sums of one pass, samples in order (rgen:86).
@@ -460,7 +514,11 @@ solrt_status check_params(const Context& ctx, const Scene& sc, const Image& img,
     }
     if (!(p.tmax >= 0.0f)) { set_error("tmax must be >= 0"); return SOLRT_ERR_INVALID; }
     if (p.kernel > SOLRT_KERNEL_MEGA) { set_error("unknown kernel"); return SOLRT_ERR_INVALID; }
-    if (p.integrator > SOLRT_INTEGRATOR_AO) { set_error("unknown integrator"); return SOLRT_ERR_INVALID; }
+    if (p.integrator > SOLRT_INTEGRATOR_PATH_NEE) { set_error("unknown integrator"); return SOLRT_ERR_INVALID; }
+    if (p.integrator == SOLRT_INTEGRATOR_PATH_NEE && p.material_mode != SOLRT_MATERIAL_LAMBERT) {
+        set_error("next-event estimation needs material_mode SOLRT_MATERIAL_LAMBERT");
+        return SOLRT_ERR_INVALID;
+    }
     if (p.integrator == SOLRT_INTEGRATOR_AO) {
         if (!ctx.blue_noise.ptr) { set_error("the AO integrator needs solrt_context_set_blue_noise"); return SOLRT_ERR_INVALID; }
         if (p.max_bounces < 1) { set_error("the AO integrator needs max_bounces >= 1"); return SOLRT_ERR_INVALID; }
@@ -486,6 +544,7 @@ DevJob make_job(const Scene& sc, const Image& img, const solrt_camera& cam, cons
     J.material_mode = p.material_mode;
     J.max_bounces = p.max_bounces;
     J.accum_mode = p.accum_mode;
+    J.integrator = p.integrator;
     J.tmax = p.tmax > 0.0f ? p.tmax : 10000.0f;
     J.accum = img.accum.as<float4>();
     J.rgba8 = img.rgba8.as<uchar4>();
@@ -505,9 +564,14 @@ solrt_status issue_pass(Context& ctx, uint32_t kind, const DevJob* dj, const Dev
     const size_t ctl_bytes = sizeof(unsigned int) * (pp.bounces + 1);
     SOLRT_CUDA(cudaMemsetAsync(ctl->count, 0, ctl_bytes, st));
     SOLRT_CUDA(cudaMemsetAsync(ctl->work, 0, ctl_bytes, st));
+    if (pp.nee) {
+        if (!ctx.q_o[2].ptr) { set_error("shadow queue not allocated"); return SOLRT_ERR_INVALID; }
+        SOLRT_CUDA(cudaMemsetAsync(ctl->scount, 0, ctl_bytes, st));
+        SOLRT_CUDA(cudaMemsetAsync(ctl->swork, 0, ctl_bytes, st));
+    }
     const int tg = record_timing ? ctx.timing_begin(2) : -1;
     k_generate<<<cdiv(pp.paths, 256), 256, 0, st>>>(dj, items, pp.item_count, pp.paths, ctx.queue(0), ctl->count,
-                                                    stats);
+                                                    stats, ctx.rad.as<float4>());
     ctx.timing_end(tg);
     ++ctx.launches;
     const int shade_grid = ctx.sm_count * 8;
@@ -518,9 +582,21 @@ solrt_status issue_pass(Context& ctx, uint32_t kind, const DevJob* dj, const Dev
         ctx.timing_end(te);
         const int ts = record_timing ? ctx.timing_begin(1) : -1;
         k_shade<<<shade_grid, 256, 0, st>>>(dj, items, pp.item_count, qin, ctx.hits.as<float4>(), ctl->count + bnc,
-                                            qout, ctl->count + bnc + 1, ctx.capacity, ctx.rad.as<float4>(), stats);
+                                            qout, ctl->count + bnc + 1, ctx.capacity, ctx.rad.as<float4>(), stats,
+                                            pp.nee ? ctx.queue(2) : PathQueue{}, ctl->scount + bnc);
         ctx.timing_end(ts);
         ++ctx.launches;
+        if (pp.nee && bnc + 1 < pp.bounces) {  // shadow rays of this bounce (none at the last: depth > max)
+            const int tx = record_timing ? ctx.timing_begin(0) : -1;
+            SOLRT_TRY(launch_extend(ctx, kind, dj, ctx.queue(2), ctx.hits.as<float4>(), ctl->scount + bnc,
+                                    ctl->swork + bnc, stats + 1));
+            ctx.timing_end(tx);
+            const int tr = record_timing ? ctx.timing_begin(1) : -1;
+            k_shadow_resolve<<<shade_grid, 256, 0, st>>>(ctx.queue(2), ctx.hits.as<float4>(), ctl->scount + bnc,
+                                                         ctx.rad.as<float4>(), stats + 1);
+            ctx.timing_end(tr);
+            ++ctx.launches;
+        }
     }
     const int ta = record_timing ? ctx.timing_begin(3) : -1;
     k_accumulate<<<cdiv(pp.pixels, 256), 256, 0, st>>>(dj, items, pp.item_count, pp.pixels, ctx.rad.as<float4>());
@@ -573,7 +649,11 @@ solrt_status batch_plan(Context& ctx, const solrt_job* jobs, uint32_t n, uint32_
         const Image& img = *static_cast<const Image*>(reinterpret_cast<const void*>(jb.image));
         SOLRT_TRY(check_params(ctx, sc, img, jb.params));
         if (jb.params.kernel != SOLRT_KERNEL_WAVEFRONT) { set_error("job %u: batches run the wavefront kernel", j); return SOLRT_ERR_INVALID; }
-        if (jb.params.integrator != SOLRT_INTEGRATOR_PATH) { set_error("job %u: batches run the path integrator", j); return SOLRT_ERR_INVALID; }
+        if (jb.params.integrator != SOLRT_INTEGRATOR_PATH && jb.params.integrator != SOLRT_INTEGRATOR_PATH_NEE) {
+            set_error("job %u: batches run the path integrators", j);
+            return SOLRT_ERR_INVALID;
+        }
+        if (jb.params.integrator == SOLRT_INTEGRATOR_PATH_NEE) SOLRT_TRY(ensure_shadow_queue(ctx));
         if (j == 0) b.kind = sc.info.kind;
         if (sc.info.kind != b.kind) { set_error("job %u: all scenes of a batch need the same BVH kind", j); return SOLRT_ERR_INVALID; }
         b.jobs.push_back(make_job(sc, img, jb.camera, jb.params));
@@ -620,6 +700,7 @@ solrt_status batch_plan(Context& ctx, const solrt_job* jobs, uint32_t n, uint32_
         cur.paths += (uint32_t)paths;
         cur.pixels += it.npix;
         cur.bounces = std::max(cur.bounces, b.jobs[it.job].max_bounces + 1u);
+        if (b.jobs[it.job].integrator == SOLRT_INTEGRATOR_PATH_NEE) cur.nee = 1u;
         b.total_paths += paths;
     }
     close_pass();
@@ -810,11 +891,20 @@ DevJob job_for(const Scene& sc, const Image& img, const solrt_camera& cam, const
 }
 
 solrt_status check_job(const Context& ctx, const Scene& sc, const Image& img, const solrt_render_params& p) {
-    if (p.integrator != SOLRT_INTEGRATOR_PATH) {
-        set_error("the server runs the path integrator");
+    if (p.integrator != SOLRT_INTEGRATOR_PATH && p.integrator != SOLRT_INTEGRATOR_PATH_NEE) {
+        set_error("the server runs the path integrators");
         return SOLRT_ERR_INVALID;
     }
     return check_params(ctx, sc, img, p);
+}
+
+solrt_status ensure_shadow_queue(Context& ctx) {
+    const size_t C = ctx.capacity;
+    SOLRT_TRY(ctx.q_o[2].alloc(16 * C));
+    SOLRT_TRY(ctx.q_d[2].alloc(16 * C));
+    SOLRT_TRY(ctx.q_thr[2].alloc(16 * C));
+    SOLRT_TRY(ctx.q_meta[2].alloc(8 * C));
+    return SOLRT_OK;
 }
 
 // DEBUG / AO: one per-pixel launch over a one-job table.
@@ -857,7 +947,12 @@ static solrt_status render_sibling(Context& ctx, const Scene& sc, const solrt_ca
 
 solrt_status render_frame(Context& ctx, const Scene& sc, const solrt_camera& cam, const solrt_render_params& p,
                           Image& img) {
-    if (p.integrator != SOLRT_INTEGRATOR_PATH) return render_sibling(ctx, sc, cam, p, img);
+    if (p.integrator == SOLRT_INTEGRATOR_PATH_NEE && p.kernel != SOLRT_KERNEL_WAVEFRONT) {
+        set_error("next-event estimation runs in the wavefront kernel");
+        return SOLRT_ERR_INVALID;
+    }
+    if (p.integrator != SOLRT_INTEGRATOR_PATH && p.integrator != SOLRT_INTEGRATOR_PATH_NEE)
+        return render_sibling(ctx, sc, cam, p, img);
     solrt_job jb;
     jb.scene = reinterpret_cast<solrt_scene*>(const_cast<Scene*>(&sc));
     jb.image = reinterpret_cast<solrt_image*>(&img);

@@ -238,6 +238,7 @@ void serve_loop(solrt_server* srv) {
                 pp.paths += np * k;
                 pp.pixels += np;
                 pp.bounces = std::max(pp.bounces, j.p.max_bounces + 1u);
+                if (j.p.integrator == SOLRT_INTEGRATOR_PATH_NEE) pp.nee = 1u;
                 tick_tickets.push_back(t);
                 tick_k.push_back(k);
                 if (j.spp_done + k == j.p.spp) {
@@ -348,6 +349,11 @@ solrt_status solrt_server_submit(solrt_server* srv, solrt_scene* scene, const so
         set_error("invalid render parameters");
         return SOLRT_ERR_INVALID;
     }
+    if ((p.integrator != SOLRT_INTEGRATOR_PATH && p.integrator != SOLRT_INTEGRATOR_PATH_NEE) ||
+        (p.integrator == SOLRT_INTEGRATOR_PATH_NEE && p.material_mode != SOLRT_MATERIAL_LAMBERT)) {
+        set_error("the server runs the path integrators (next-event estimation with Lambert materials)");
+        return SOLRT_ERR_INVALID;
+    }
     if ((uint64_t)p.width * p.height > srv->ctx->capacity) {
         set_error("job of %u x %u pixels exceeds the path capacity", p.width, p.height);
         return SOLRT_ERR_CAPACITY;
@@ -359,6 +365,10 @@ solrt_status solrt_server_submit(solrt_server* srv, solrt_scene* scene, const so
     } else if (sc.info.kind != srv->kind) {
         set_error("all scenes of a server need the same BVH kind");
         return SOLRT_ERR_INVALID;
+    }
+    if (p.integrator == SOLRT_INTEGRATOR_PATH_NEE) {  // before the serving thread can see the job
+        const solrt_status s = solrt::ensure_shadow_queue(*srv->ctx);
+        if (s != SOLRT_OK) return s;
     }
     ServerJob j;
     j.ticket = srv->next_ticket++;

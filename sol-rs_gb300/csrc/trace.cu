@@ -175,9 +175,9 @@ bool extend_variant_ok(uint32_t block, uint32_t smem) {
 }
 
 solrt_status launch_extend(Context& ctx, uint32_t kind, const DevJob* jobs, const PathQueue& q, float4* hits,
-                           const unsigned int* count, unsigned int* work) {
+                           const unsigned int* count, unsigned int* work, DevStats* st) {
     const QueueIO io{q.o_tmin, q.d_tmax, q.meta, jobs, hits};
-    DevStats* st = ctx.stats.as<DevStats>();
+    if (!st) st = ctx.stats.as<DevStats>();
     if (kind == SOLRT_BVH8_Q8) SOLRT_TRY((launch_tuned<SOLRT_BVH8_Q8>(ctx, io, count, 0, 0, work, st)));
     else if (kind == SOLRT_BVH4_Q8) SOLRT_TRY((launch_tuned<SOLRT_BVH4_Q8>(ctx, io, count, 0, 0, work, st)));
     else if (kind == SOLRT_BVH8_F32) SOLRT_TRY((launch_tuned<SOLRT_BVH8_F32>(ctx, io, count, 0, 0, work, st)));

@@ -28,6 +28,13 @@ def _specs(solrt):
         (single_triangle(), 16, 16, dict(spp=1, max_bounces=2, material_mode=L, rng_mode=PS, seed=6, job_id=5)),
         (empty_scene(), 8, 8, dict(spp=2, max_bounces=1, material_mode=L, rng_mode=PS, seed=7, job_id=6,
                                    miss_mode=solrt.MISS_GRADIENT)),
+        # next-event estimation jobs share passes (and shadow queues) with the rest
+        (S.cornell(), 32, 24, dict(spp=3, max_bounces=4, material_mode=L, rng_mode=PS, seed=8, job_id=7,
+                                   integrator=solrt.INTEGRATOR_PATH_NEE)),
+        (S.tunnel(n_ang=128, n_ax=64, length=20.0), 24, 16, dict(spp=2, max_bounces=6, material_mode=L,
+                                                                 rng_mode=RS, miss_mode=solrt.MISS_REF_SKY,
+                                                                 accum_mode=solrt.ACCUM_KAHAN,
+                                                                 integrator=solrt.INTEGRATOR_PATH_NEE)),
     ]
 
 
@@ -107,7 +114,7 @@ def test_batch_matches_oracle(solrt, oracle, ctx):
     b = solrt.Batch(ctx, jobs)
     b.launch()
     ctx.synchronize()
-    for (data, w, h, kw), (sc, img, cam, p) in list(zip(_specs(solrt), jobs))[:3]:
+    for (data, w, h, kw), (sc, img, cam, p) in [x for i, x in enumerate(zip(_specs(solrt), jobs)) if i in (0, 1, 2, 7)]:
         want, _, _ = oracle.OracleScene(data).render(cam, p)
         got, _ = img.read()
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32))

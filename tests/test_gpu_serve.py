@@ -25,7 +25,8 @@ def _job(solrt, i):
     kw = dict(spp=int(rng.integers(1, 9)), max_bounces=int(rng.integers(1, 6)), seed=7 + i, job_id=i,
               material_mode=solrt.MATERIAL_LAMBERT if i % 2 else solrt.MATERIAL_REF,
               rng_mode=solrt.RNG_PER_SAMPLE if i % 3 else solrt.RNG_REF_STREAM,
-              miss_mode=int(i % 3), accum_mode=solrt.ACCUM_KAHAN if i % 4 == 1 else solrt.ACCUM_REF_MIX)
+              miss_mode=int(i % 3), accum_mode=solrt.ACCUM_KAHAN if i % 4 == 1 else solrt.ACCUM_REF_MIX,
+              integrator=solrt.INTEGRATOR_PATH_NEE if i % 4 == 3 else solrt.INTEGRATOR_PATH)
     return int(rng.integers(0, 3)), solrt.render_params(w, h, **kw)
 
 
