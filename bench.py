@@ -598,6 +598,8 @@ def main():
     ap.add_argument("--workload", default="soup", choices=["soup", "cornell", "tunnel", "instances", "batch", "serve"])
     ap.add_argument("--bvh", default="bvh2", choices=["bvh2", "bvh2q", "bvh2t", "bvh4", "bvh8", "bvh8f"])
     ap.add_argument("--sah", action="store_true", help="wide BVH kinds: SAH-optimal collapse")
+    ap.add_argument("--nee", action="store_true",
+                    help="next-event estimation (shadow-ray queue); shadow rays are reported apart from the metric")
     ap.add_argument("--jobs", type=int, default=256)
     ap.add_argument("--rate", type=float, default=6.0, help="serve: Poisson arrival rate, jobs/s")
     ap.add_argument("--duration", type=float, default=8.0, help="serve: arrival window, s")
@@ -630,6 +632,9 @@ def main():
     b.build_lib()
     solrt = importlib.import_module("sol-rs_gb300")
     data, kw, cfg = workload(args.workload)
+    if args.nee:
+        kw["integrator"] = solrt.INTEGRATOR_PATH_NEE
+        cfg = dict(cfg, integrator="path tracing + next-event estimation (shadow-ray queue)")
     for key in ("width", "height", "spp"):   # reduced sizes for profiler captures
         if getattr(args, key):
             kw[key] = getattr(args, key)
@@ -688,6 +693,7 @@ def main():
     clk = clocks.stop()
     ms_max = max_over_ranks(pg, ms)
     seg_total = sum_over_ranks(pg, float(st.segments))
+    shadow_total = sum_over_ranks(pg, float(st.shadow_segments))
     value = seg_total / (ms_max / 1000.0) / 1e6
 
     # end to end: render + read back the accumulation and RGBA8 images into pinned host memory
@@ -736,7 +742,8 @@ def main():
     peak, peak_kind = peaks()
     b_seg = 32 + 16 + NODE_BYTES[info.kind] * nodes_per_seg + 48 * tris_per_seg
     ext_s = st.extend_ms / 1000.0
-    achieved = (st.segments * b_seg) / ext_s / 1e9 if ext_s > 0 else 0.0
+    # extend launches also trace the shadow rays of --nee (same bytes per ray assumed)
+    achieved = ((st.segments + st.shadow_segments) * b_seg) / ext_s / 1e9 if ext_s > 0 else 0.0
     traffic = None
     if args.workload == "soup" and info.kind == solrt.BVH2 and not (args.width or args.height or args.spp):
         seg_per_launch = st.segments / max(st.extend_launches, 1)
@@ -834,6 +841,11 @@ def main():
                "serving": serving}
         if regen is not None:
             out["regenerate_ms"] = regen
+        if args.nee:
+            out["shadow_rays"] = {"per_step": int(st.shadow_segments // args.steps),
+                                  "mrays_s": round(shadow_total / (ms_max / 1000.0) / 1e6, 3),
+                                  "unoccluded_frac": round(st.shadow_unoccluded / max(st.shadow_segments, 1), 4),
+                                  "note": "not in value: the metric counts primary + bounce segments"}
         print(json.dumps(out), flush=True)
     if pg is not None:
         pg.destroy_process_group()

@@ -223,8 +223,13 @@ SOLRT_D void extend_bvh2_ww(const IO& io, uint32_t n, unsigned int* work, TraceC
                     const float4* tp = ts.tris + 3 * (size_t)k;
                     if (kCount) ++cnt.tris;
                     cnt.fallbacks += intersect_tri(r, __ldg(tp), __ldg(tp + 1), __ldg(tp + 2), best);
-                    leaf = node;
-                    if (node < 0) node = stack.get(--sp);
+                    if (io.any_hit && best.prim != SOLRT_NO_HIT) {  // occlusion query: done at the first hit
+                        node = kBvh2Sentinel;
+                        leaf = 0;
+                    } else {
+                        leaf = node;
+                        if (node < 0) node = stack.get(--sp);
+                    }
                 }
             }
         }

@@ -146,6 +146,11 @@ SOLRT_D void extend_bvh8_ww(const IO& io, uint32_t n, unsigned int* work, TraceC
                     const float4* tp = ts.tris + 3 * (size_t)ti;
                     if (kCount) ++cnt.tris;
                     cnt.fallbacks += intersect_tri(r, __ldg(tp), __ldg(tp + 1), __ldg(tp + 2), best);
+                    if (io.any_hit && best.prim != SOLRT_NO_HIT) {  // occlusion query: done at the first hit
+                        tgrp.y = 0u;
+                        grp = make_uint2(0u, 0u);
+                        sp = 0;
+                    }
                 }
             }
         }

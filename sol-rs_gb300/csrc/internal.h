@@ -316,10 +316,12 @@ solrt_status regenerate_scene(Context& ctx, Scene& sc, uint32_t mode);
 // trace.cu
 solrt_status launch_trace_rays(Context& ctx, const Scene& sc, const solrt_ray* rays, uint32_t n, solrt_hit* hits);
 // Extend for a batched queue: the scene of ray i is jobs[meta[i].y >> kDepthBits].sc.
-// Closest hits of the `*count` rays of queue `q`; `st` (default: the
-// context's first stats block) receives their segment and visit counts.
+// Closest hits of the `*count` rays of queue `q` (any_hit: some hit in
+// (tmin, tmax), for occlusion queries); `st` (default: the context's first
+// stats block) receives their segment and visit counts.
 solrt_status launch_extend(Context& ctx, uint32_t kind, const DevJob* jobs, const PathQueue& q, float4* hits,
-                           const unsigned int* count, unsigned int* work, DevStats* st = nullptr);
+                           const unsigned int* count, unsigned int* work, DevStats* st = nullptr,
+                           bool any_hit = false);
 // Whether an extend kernel exists for this block size / shared stack slots.
 bool extend_variant_ok(uint32_t block, uint32_t smem);
 

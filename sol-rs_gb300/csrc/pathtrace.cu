@@ -589,7 +589,7 @@ solrt_status issue_pass(Context& ctx, uint32_t kind, const DevJob* dj, const Dev
         if (pp.nee && bnc + 1 < pp.bounces) {  // shadow rays of this bounce (none at the last: depth > max)
             const int tx = record_timing ? ctx.timing_begin(0) : -1;
             SOLRT_TRY(launch_extend(ctx, kind, dj, ctx.queue(2), ctx.hits.as<float4>(), ctl->scount + bnc,
-                                    ctl->swork + bnc, stats + 1));
+                                    ctl->swork + bnc, stats + 1, true));
             ctx.timing_end(tx);
             const int tr = record_timing ? ctx.timing_begin(1) : -1;
             k_shadow_resolve<<<shade_grid, 256, 0, st>>>(ctx.queue(2), ctx.hits.as<float4>(), ctl->scount + bnc,

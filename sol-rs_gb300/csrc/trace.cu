@@ -53,6 +53,7 @@ struct QueueIO {
     const uint2* __restrict__ meta;
     const DevJob* __restrict__ jobs;
     float4* __restrict__ hits;
+    bool any_hit;  // occlusion queries (shadow rays): any hit in (tmin, tmax), not the closest
     SOLRT_D void load(uint32_t i, float4& o, float4& d, TravScene& ts) const {
         o = o_tmin[i];
         d = d_tmax[i];
@@ -80,6 +81,7 @@ struct RayFileIO {
     const float4* __restrict__ rays;
     float4* __restrict__ hits;
     TravScene scene;
+    static constexpr bool any_hit = false;
     SOLRT_D void load(uint32_t i, float4& o, float4& d, TravScene& ts) const {
         o = rays[2 * (size_t)i];
         d = rays[2 * (size_t)i + 1];
@@ -175,8 +177,8 @@ bool extend_variant_ok(uint32_t block, uint32_t smem) {
 }
 
 solrt_status launch_extend(Context& ctx, uint32_t kind, const DevJob* jobs, const PathQueue& q, float4* hits,
-                           const unsigned int* count, unsigned int* work, DevStats* st) {
-    const QueueIO io{q.o_tmin, q.d_tmax, q.meta, jobs, hits};
+                           const unsigned int* count, unsigned int* work, DevStats* st, bool any_hit) {
+    const QueueIO io{q.o_tmin, q.d_tmax, q.meta, jobs, hits, any_hit};
     if (!st) st = ctx.stats.as<DevStats>();
     if (kind == SOLRT_BVH8_Q8) SOLRT_TRY((launch_tuned<SOLRT_BVH8_Q8>(ctx, io, count, 0, 0, work, st)));
     else if (kind == SOLRT_BVH4_Q8) SOLRT_TRY((launch_tuned<SOLRT_BVH4_Q8>(ctx, io, count, 0, 0, work, st)));
