@@ -250,14 +250,13 @@ struct oracle_scene {
     std::vector<uint32_t> child;         // 2 per internal node
     std::vector<Box> node_box;           // per internal node
     std::vector<Box> leaf_box;           // per sorted position
-    // next-event estimation: emissive triangles with their inclusive float
-    // prefix of world areas (triangle order) and pick probability
-    struct Light {
-        float cdf, pick;
-        uint32_t prim;
+    // next-event estimation: light tree over the emissive triangles
+    struct LightNode {
+        float c[3], r2;            // box centre, squared half-diagonal
+        float power;
+        uint32_t left, right, prim;  // children, or the triangle of a leaf (else ~0u)
     };
-    std::vector<Light> lights;
-    float light_total = 0.0f;
+    std::vector<LightNode> light_tree;
 };
 
 namespace {
@@ -614,10 +613,20 @@ template <class R> void hit_frame(const oracle_scene* s, const TriW& tri, R b0, 
     pos = V3<R>{o[0], o[1], o[2]};
 }
 
+// Importance of light-tree node k seen from x: power / max(d^2, r^2), d the
+// distance to the box centre, r the half-diagonal.
+template <class R> R light_importance(const oracle_scene* s, uint32_t k, V3<R> x) {
+    const oracle_scene::LightNode& nd = s->light_tree[k];
+    const V3<R> dv{R(nd.c[0]) - x.x, R(nd.c[1]) - x.y, R(nd.c[2]) - x.z};
+    return R(nd.power) / std::max(dot(dv, dv), R(nd.r2));
+}
+
 // Next-event estimation at a diffuse vertex (SOLRT_INTEGRATOR_PATH_NEE, an
-// estimator the reference does not have). Three draws: l0 picks an emissive
-// triangle by its area prefix, l1 and l2 a uniform point on it
-// (b0 = 1 - sqrt(l1), b1 = l2 sqrt(l1)); the shadow ray leaves from the
+// estimator the reference does not have). Three draws: l0 walks the light
+// tree, taking each child with probability proportional to its importance
+// (l0 rescaled into the chosen interval, kept below 1; p_pick the product
+// of the choices); l1 and l2 pick a uniform point on the triangle
+// (b0 = 1 - sqrt(l1), b1 = l2 sqrt(l1)). The shadow ray leaves from the
 // continuation origin `no` towards it with tmax 0.9999 of the distance. An
 // unoccluded one returns thr * Le * cos_x * cos_y * area / (pi r^2 p_pick):
 // Lambert albedo / pi (thr already holds the albedo) times Le times the
@@ -627,16 +636,31 @@ template <class R> bool nee_term(const oracle_scene* s, V3<R> no, V3<R> n_o, V3<
     const R l0 = next_rand<R>(rng);
     const R l1 = next_rand<R>(rng);
     const R l2 = next_rand<R>(rng);
-    if (s->lights.empty()) return false;
-    const R target = l0 * R(s->light_total);
-    size_t lo = 0, hi = s->lights.size() - 1;  // first light whose prefix exceeds the target
-    while (lo < hi) {
-        const size_t mid = (lo + hi) / 2;
-        if (R(s->lights[mid].cdf) > target) hi = mid;
-        else lo = mid + 1;
+    if (s->light_tree.empty()) return false;
+    uint32_t k = 0, prim = ~0u;
+    R pick = R(1), u = l0;
+    for (int level = 0; level < 64; ++level) {
+        const oracle_scene::LightNode& nd = s->light_tree[k];
+        if (nd.prim != ~0u) {
+            prim = nd.prim;
+            break;
+        }
+        const R wl = light_importance<R>(s, nd.left, no), wr = light_importance<R>(s, nd.right, no);
+        const R pl = wl / (wl + wr);
+        if (!(pl >= R(0) && pl <= R(1))) return false;
+        if (u < pl) {
+            k = nd.left;
+            pick = pick * pl;
+            u = u / pl;
+        } else {
+            k = nd.right;
+            pick = pick * (R(1) - pl);
+            u = (u - pl) / (R(1) - pl);
+        }
+        u = std::min(u, R(0.99999994f));
     }
-    const oracle_scene::Light& L = s->lights[lo];
-    const TriW& tri = s->tris[L.prim];
+    if (prim == ~0u || !(pick > R(0))) return false;
+    const TriW& tri = s->tris[prim];
     auto cv = [](V3<float> a) { return V3<R>{R(a.x), R(a.y), R(a.z)}; };
     const V3<R> p0 = cv(tri.p[0]), p1 = cv(tri.p[1]), p2 = cv(tri.p[2]);
     const R su = std::sqrt(l1);
@@ -656,7 +680,7 @@ template <class R> bool nee_term(const oracle_scene* s, V3<R> no, V3<R> n_o, V3<
     const R tmax = dist * R(0.9999f);
     if (!(cx > R(0)) || !(cy > R(0)) || !(tmax > tmin)) return false;
     const float* le = s->mats[tri.mat].emissive;
-    const R wgt = ((cx * cy) * (R(0.5f) * a2)) / ((R(3.14159265f) * d2) * R(L.pick));
+    const R wgt = ((cx * cy) * (R(0.5f) * a2)) / ((R(3.14159265f) * d2) * pick);
     ++cn.shadow;
     uint64_t nv = 0, nt = 0, fb = 0;
     const HitR<R> h = closest_hit<R>(s, no, wl, tmin, tmax, 1, fb, nv, nt);
@@ -959,6 +983,100 @@ int resolve_threads(int threads) {
 // C API
 // ---------------------------------------------------------------------------
 
+// Light tree of next-event estimation: the emissive triangles (any emissive
+// channel >= 1, pathtrace.rchit:75-80; zero-area ones left out) sorted by
+// the 30-bit Morton code of their centroid ((p0 + p1) + p2) / 3 in the
+// centroids' bounds (ties by triangle index), ranges split at their middle;
+// a node's box is the union of its children's (a leaf's: its triangle's),
+// its power left + right (a leaf's: area * ((Le.r + Le.g) + Le.b)).
+uint32_t light_node(oracle_scene* s, const std::vector<uint32_t>& order, const std::vector<float>& box,
+                    const std::vector<float>& power, const std::vector<uint32_t>& prim, uint32_t b, uint32_t e,
+                    float mn[3], float mx[3], float& pw) {
+    const uint32_t idx = (uint32_t)s->light_tree.size();
+    s->light_tree.push_back(oracle_scene::LightNode{});
+    oracle_scene::LightNode nd{};
+    nd.left = nd.right = nd.prim = ~0u;
+    if (e - b == 1) {
+        const uint32_t k = order[b];
+        for (int c = 0; c < 3; ++c) {
+            mn[c] = box[6 * k + c];
+            mx[c] = box[6 * k + 3 + c];
+        }
+        pw = power[k];
+        nd.prim = prim[k];
+    } else {
+        const uint32_t m = b + (e - b) / 2;
+        float amn[3], amx[3], bmn[3], bmx[3], pa = 0.0f, pb = 0.0f;
+        nd.left = light_node(s, order, box, power, prim, b, m, amn, amx, pa);
+        nd.right = light_node(s, order, box, power, prim, m, e, bmn, bmx, pb);
+        for (int c = 0; c < 3; ++c) {
+            mn[c] = std::min(amn[c], bmn[c]);
+            mx[c] = std::max(amx[c], bmx[c]);
+        }
+        pw = pa + pb;
+    }
+    float h[3];
+    for (int c = 0; c < 3; ++c) {
+        nd.c[c] = (mn[c] + mx[c]) * 0.5f;
+        h[c] = (mx[c] - mn[c]) * 0.5f;
+    }
+    nd.r2 = (h[0] * h[0] + h[1] * h[1]) + h[2] * h[2];
+    nd.power = pw;
+    s->light_tree[idx] = nd;
+    return idx;
+}
+
+void build_light_tree(oracle_scene* s) {
+    std::vector<uint32_t> prim;
+    std::vector<float> box, power, cen;
+    for (uint32_t t = 0; t < (uint32_t)s->tris.size(); ++t) {
+        const TriW& tr = s->tris[t];
+        const solrt_material& m = s->mats[tr.mat];
+        if (!(m.emissive[0] >= 1.0f || m.emissive[1] >= 1.0f || m.emissive[2] >= 1.0f)) continue;
+        const V3<float> e1 = tr.p[1] - tr.p[0], e2 = tr.p[2] - tr.p[0];
+        const float nx = e1.y * e2.z - e1.z * e2.y, ny = e1.z * e2.x - e1.x * e2.z, nz = e1.x * e2.y - e1.y * e2.x;
+        const float area = 0.5f * std::sqrt((nx * nx + ny * ny) + nz * nz);
+        const float pw = area * ((m.emissive[0] + m.emissive[1]) + m.emissive[2]);
+        if (!(area > 0.0f) || !(pw > 0.0f) || !std::isfinite(pw)) continue;
+        prim.push_back(t);
+        const float v[3][3] = {{tr.p[0].x, tr.p[0].y, tr.p[0].z}, {tr.p[1].x, tr.p[1].y, tr.p[1].z},
+                               {tr.p[2].x, tr.p[2].y, tr.p[2].z}};
+        float lo[3], hi[3];
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::min(std::min(v[0][k], v[1][k]), v[2][k]);
+            hi[k] = std::max(std::max(v[0][k], v[1][k]), v[2][k]);
+            cen.push_back(((v[0][k] + v[1][k]) + v[2][k]) / 3.0f);
+        }
+        box.insert(box.end(), lo, lo + 3);
+        box.insert(box.end(), hi, hi + 3);
+        power.push_back(pw);
+    }
+    const uint32_t n = (uint32_t)prim.size();
+    if (n == 0) return;
+    float cmin[3] = {cen[0], cen[1], cen[2]}, cmax[3] = {cen[0], cen[1], cen[2]};
+    for (uint32_t i = 1; i < n; ++i)
+        for (int k = 0; k < 3; ++k) {
+            cmin[k] = std::min(cmin[k], cen[3 * i + k]);
+            cmax[k] = std::max(cmax[k], cen[3 * i + k]);
+        }
+    std::vector<std::pair<uint32_t, uint32_t>> key(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        uint32_t code = 0;
+        for (int k = 0; k < 3; ++k) {
+            const float ext = cmax[k] - cmin[k];
+            const float f = ext > 0.0f ? (cen[3 * i + k] - cmin[k]) / ext : 0.0f;
+            code |= expand_bits10((uint32_t)std::min(std::max(f * 1023.0f, 0.0f), 1023.0f)) << (2 - k);
+        }
+        key[i] = {code, i};
+    }
+    std::sort(key.begin(), key.end());
+    std::vector<uint32_t> order(n);
+    for (uint32_t i = 0; i < n; ++i) order[i] = key[i].second;
+    float mn[3], mx[3], pw = 0.0f;
+    s->light_tree.reserve(2 * (size_t)n);
+    light_node(s, order, box, power, prim, 0, n, mn, mx, pw);
+}
+
 extern "C" {
 
 oracle_scene* oracle_scene_create(const solrt_scene_desc* desc) {
@@ -969,23 +1087,7 @@ oracle_scene* oracle_scene_create(const solrt_scene_desc* desc) {
         return nullptr;
     }
     build_lbvh(s);
-    // emissive as pathtrace.rchit:75-80 decides it; areas of the world
-    // triangles in float, summed in triangle order
-    float total = 0.0f;
-    for (uint32_t t = 0; t < (uint32_t)s->tris.size(); ++t) {
-        const TriW& tr = s->tris[t];
-        const solrt_material& m = s->mats[tr.mat];
-        if (!(m.emissive[0] >= 1.0f || m.emissive[1] >= 1.0f || m.emissive[2] >= 1.0f)) continue;
-        const V3<float> e1 = tr.p[1] - tr.p[0], e2 = tr.p[2] - tr.p[0];
-        const float nx = e1.y * e2.z - e1.z * e2.y, ny = e1.z * e2.x - e1.x * e2.z, nz = e1.x * e2.y - e1.y * e2.x;
-        const float area = 0.5f * std::sqrt((nx * nx + ny * ny) + nz * nz);
-        if (!(area > 0.0f)) continue;
-        total = total + area;
-        s->lights.push_back(oracle_scene::Light{total, area, t});
-    }
-    if (!(total > 0.0f) || !std::isfinite(total)) s->lights.clear();
-    for (oracle_scene::Light& L : s->lights) L.pick = L.pick / total;
-    s->light_total = s->lights.empty() ? 0.0f : total;
+    build_light_tree(s);
     return s;
 }
 

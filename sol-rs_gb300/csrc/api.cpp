@@ -11,6 +11,7 @@
 //   solrt_render   ~ one `render` frame of examples/5-pathtrace.rs:294-369
 // Errors are status codes with a per-thread message instead of the
 // reference's panics (unwrap/expect).
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstring>
@@ -125,6 +126,116 @@ solrt_status fill_camera(const double view[16], float vfov_deg, float aspect, fl
 }
 
 std::mutex g_refs_mutex;
+
+// Light tree of next-event estimation over the emissive triangles (emissive
+// as pathtrace.rchit:75-80 decides it: any emissive channel >= 1; zero-area
+// triangles cannot be hit and are left out). Lights sorted by the 30-bit
+// Morton code of their centroid in the centroids' bounds (ties by triangle
+// index), split at the middle of each range, so the tree is balanced.
+// Per node two float4: (box centre, squared half-diagonal) and (power,
+// left, right, triangle of a leaf or ~0u); power = area * (Le.r + Le.g +
+// Le.b), summed left + right. All in float with a fixed order of operations.
+struct LightBuild {
+    std::vector<uint32_t> prim;
+    std::vector<float> lo, hi, power;  // per light: box (3 + 3), power
+    std::vector<float4> nodes;
+    uint32_t build(const std::vector<uint32_t>& order, uint32_t b, uint32_t e, float bmin[3], float bmax[3],
+                   float& pw) {
+        const uint32_t idx = (uint32_t)(nodes.size() / 2);
+        nodes.push_back(float4{});
+        nodes.push_back(float4{});
+        uint32_t l = ~0u, r = ~0u, leaf = ~0u;
+        if (e - b == 1) {
+            const uint32_t k = order[b];
+            for (int c = 0; c < 3; ++c) {
+                bmin[c] = lo[3 * k + c];
+                bmax[c] = hi[3 * k + c];
+            }
+            pw = power[k];
+            leaf = prim[k];
+        } else {
+            const uint32_t m = b + (e - b) / 2;
+            float amin[3], amax[3], cmin[3], cmax[3], pa = 0.0f, pc = 0.0f;
+            l = build(order, b, m, amin, amax, pa);
+            r = build(order, m, e, cmin, cmax, pc);
+            for (int c = 0; c < 3; ++c) {
+                bmin[c] = std::min(amin[c], cmin[c]);
+                bmax[c] = std::max(amax[c], cmax[c]);
+            }
+            pw = pa + pc;
+        }
+        const float hx = (bmax[0] - bmin[0]) * 0.5f, hy = (bmax[1] - bmin[1]) * 0.5f, hz = (bmax[2] - bmin[2]) * 0.5f;
+        nodes[2 * idx] = make_float4((bmin[0] + bmax[0]) * 0.5f, (bmin[1] + bmax[1]) * 0.5f,
+                                     (bmin[2] + bmax[2]) * 0.5f, (hx * hx + hy * hy) + hz * hz);
+        float fl, fr, ft;
+        std::memcpy(&fl, &l, 4);
+        std::memcpy(&fr, &r, 4);
+        std::memcpy(&ft, &leaf, 4);
+        nodes[2 * idx + 1] = make_float4(pw, fl, fr, ft);
+        return idx;
+    }
+};
+
+uint32_t expand10(uint32_t v) {
+    v = (v * 0x00010001u) & 0xFF0000FFu;
+    v = (v * 0x00000101u) & 0x0F00F00Fu;
+    v = (v * 0x00000011u) & 0xC30C30C3u;
+    v = (v * 0x00000005u) & 0x49249249u;
+    return v;
+}
+
+std::vector<float4> build_light_tree(const std::vector<float4>& pos, const std::vector<uint4>& tri,
+                                     const std::vector<uint32_t>& sec_mat, const solrt_material* mats,
+                                     uint32_t& count) {
+    LightBuild lb;
+    std::vector<float> cen;
+    for (size_t t = 0; t < tri.size(); ++t) {
+        const solrt_material& m = mats[sec_mat[tri[t].w]];
+        if (!(m.emissive[0] >= 1.0f || m.emissive[1] >= 1.0f || m.emissive[2] >= 1.0f)) continue;
+        const float4 a = pos[tri[t].x], b = pos[tri[t].y], c = pos[tri[t].z];
+        const float e1x = b.x - a.x, e1y = b.y - a.y, e1z = b.z - a.z;
+        const float e2x = c.x - a.x, e2y = c.y - a.y, e2z = c.z - a.z;
+        const float nx = e1y * e2z - e1z * e2y, ny = e1z * e2x - e1x * e2z, nz = e1x * e2y - e1y * e2x;
+        const float area = 0.5f * std::sqrt((nx * nx + ny * ny) + nz * nz);
+        const float pw = area * ((m.emissive[0] + m.emissive[1]) + m.emissive[2]);
+        if (!(area > 0.0f) || !(pw > 0.0f) || !std::isfinite(pw)) continue;
+        lb.prim.push_back((uint32_t)t);
+        const float v[3][3] = {{a.x, a.y, a.z}, {b.x, b.y, b.z}, {c.x, c.y, c.z}};
+        for (int k = 0; k < 3; ++k) {
+            lb.lo.push_back(std::min(std::min(v[0][k], v[1][k]), v[2][k]));
+            lb.hi.push_back(std::max(std::max(v[0][k], v[1][k]), v[2][k]));
+            cen.push_back(((v[0][k] + v[1][k]) + v[2][k]) / 3.0f);
+        }
+        lb.power.push_back(pw);
+    }
+    const uint32_t n = (uint32_t)lb.prim.size();
+    count = n;
+    if (n == 0) return {};
+    float cmin[3] = {cen[0], cen[1], cen[2]}, cmax[3] = {cen[0], cen[1], cen[2]};
+    for (uint32_t i = 1; i < n; ++i)
+        for (int k = 0; k < 3; ++k) {
+            cmin[k] = std::min(cmin[k], cen[3 * i + k]);
+            cmax[k] = std::max(cmax[k], cen[3 * i + k]);
+        }
+    std::vector<std::pair<uint32_t, uint32_t>> key(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        uint32_t code = 0;
+        for (int k = 0; k < 3; ++k) {
+            const float ext = cmax[k] - cmin[k];
+            const float f = ext > 0.0f ? (cen[3 * i + k] - cmin[k]) / ext : 0.0f;
+            const uint32_t q = (uint32_t)std::min(std::max(f * 1023.0f, 0.0f), 1023.0f);
+            code |= expand10(q) << (2 - k);
+        }
+        key[i] = {code, i};
+    }
+    std::sort(key.begin(), key.end());
+    std::vector<uint32_t> order(n);
+    for (uint32_t i = 0; i < n; ++i) order[i] = key[i].second;
+    float bmin[3], bmax[3], pw = 0.0f;
+    lb.nodes.reserve(4 * (size_t)n);
+    lb.build(order, 0, n, bmin, bmax, pw);
+    return lb.nodes;
+}
 
 }  // namespace
 }  // namespace solrt
@@ -435,29 +546,9 @@ solrt_status solrt_scene_create(solrt_context* ctx, const solrt_scene_desc* d, c
         set_error("scene upload failed");
         return fail(SOLRT_ERR_DEVICE);
     }
-    // Emissive triangles for next-event estimation, emissive as the closest-hit
-    // shader decides it (any emissive channel >= 1, pathtrace.rchit:75-80):
-    // per light its inclusive float prefix of world areas in triangle order,
-    // its pick probability area / total and its triangle.
-    std::vector<float4> lights;
-    float total = 0.0f;
-    for (uint64_t t = 0; t < nt; ++t) {
-        const solrt_material& m = d->materials[sec_mat[tri[t].w]];
-        if (!(m.emissive[0] >= 1.0f || m.emissive[1] >= 1.0f || m.emissive[2] >= 1.0f)) continue;
-        const float4 a = pos[tri[t].x], b = pos[tri[t].y], c = pos[tri[t].z];
-        const float e1x = b.x - a.x, e1y = b.y - a.y, e1z = b.z - a.z;
-        const float e2x = c.x - a.x, e2y = c.y - a.y, e2z = c.z - a.z;
-        const float nx = e1y * e2z - e1z * e2y, ny = e1z * e2x - e1x * e2z, nz = e1x * e2y - e1y * e2x;
-        const float area = 0.5f * std::sqrt((nx * nx + ny * ny) + nz * nz);
-        if (!(area > 0.0f)) continue;  // cannot be hit, never picked
-        total = total + area;
-        const uint32_t prim = (uint32_t)t;
-        float pf;
-        std::memcpy(&pf, &prim, sizeof(pf));
-        lights.push_back(make_float4(total, area, pf, 0.0f));
-    }
-    if (!(total > 0.0f) || !std::isfinite(total)) lights.clear();
-    for (float4& L : lights) L.y = L.y / total;
+    // light tree of next-event estimation (world positions at creation)
+    uint32_t light_count = 0;
+    const std::vector<float4> lights = build_light_tree(pos, tri, sec_mat, d->materials, light_count);
     if (!lights.empty()) {
         if ((s = sc->lights.alloc(sizeof(float4) * lights.size())) != SOLRT_OK) return fail(s);
         if (cudaMemcpyAsync(sc->lights.ptr, lights.data(), sizeof(float4) * lights.size(), cudaMemcpyHostToDevice,
@@ -466,8 +557,7 @@ solrt_status solrt_scene_create(solrt_context* ctx, const solrt_scene_desc* d, c
             return fail(SOLRT_ERR_DEVICE);
         }
     }
-    sc->light_count = (uint32_t)lights.size();
-    sc->light_total = lights.empty() ? 0.0f : total;
+    sc->light_count = light_count;
     sc->section_count = d->section_count;
     sc->sec_tri_first = std::move(sec_first);
     sc->sec_tri_count = std::move(sec_count);

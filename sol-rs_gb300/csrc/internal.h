@@ -270,10 +270,9 @@ struct Scene {
     std::vector<int32_t> blas_root;
     uint32_t blas_depth = 0, tlas_count = 0, tlas_depth = 0;
     DeviceBuffer tlas, inst_table;
-    // emissive triangles (see DevScene::lights), fixed at creation
+    // light tree of next-event estimation (see DevScene::lights), built at creation
     DeviceBuffer lights;
     uint32_t light_count = 0;
-    float light_total = 0.0f;
     DevScene view() const {
         DevScene d;
         d.tri_count = tri_count;
@@ -296,7 +295,6 @@ struct Scene {
         d.tri_wt = tri_wt.as<float4>();
         d.lights = lights.as<float4>();
         d.light_count = light_count;
-        d.light_total = light_total;
         return d;
     }
 };

@@ -130,31 +130,60 @@ SOLRT_D bool shade_step(const DevJob& J, float4 o, float4 d, float4 h, f3& acc, 
     return true;
 }
 
+// Importance of a light-tree node seen from x: power / max(d^2, r^2), d the
+// distance to the node's box centre, r its half-diagonal.
+SOLRT_D float light_importance(const float4* tree, uint32_t k, f3 x) {
+    const float4 a = __ldg(tree + 2 * (size_t)k);
+    const float pw = __ldg(&tree[2 * (size_t)k + 1].x);
+    const f3 dv{a.x - x.x, a.y - x.y, a.z - x.z};
+    return pw / glsl_max(dot(dv, dv), a.w);
+}
+
 // Next-event estimation at a diffuse vertex of SOLRT_INTEGRATOR_PATH_NEE (an
-// estimator the reference does not have). Three draws: l0 picks an emissive
-// triangle by its area prefix, l1 and l2 a uniform point on it
+// estimator the reference does not have). Three draws: l0 walks the light
+// tree from the root, taking each child with probability proportional to
+// its importance (l0 rescaled into the chosen interval at every level, kept
+// below 1), so near and bright lights are picked more often; p_pick is the
+// product of the choices. l1 and l2 pick a uniform point on the triangle
 // (b0 = 1 - sqrt(l1), b1 = l2 sqrt(l1)). `no` is the continuation origin
 // (hit + 1e-4 n_o), `thr` the throughput after the vertex's albedo. Returns
 // true with the shadow ray (so, sd: unit direction, tmax 0.9999 of the
 // distance) and the radiance it adds when unoccluded:
 // thr * Le * cos_x * cos_y * area / (pi * r^2 * p_pick), i.e. the Lambert
 // BRDF albedo / pi times Le times the geometry term over the area pdf
-// p_pick / area. Emitters are two-sided, as hits on them are (rchit:75-80).
+// p_pick / area (area of the triangle's current world vertices). Emitters
+// are two-sided, as hits on them are (rchit:75-80).
 SOLRT_D bool nee_sample(const DevScene& sc, f3 no, f3 n_o, f3 thr, float tmin, uint32_t& rng, float4& so,
                         float4& sd, f3& contrib) {
     const float l0 = next_rand(rng);
     const float l1 = next_rand(rng);
     const float l2 = next_rand(rng);
     if (sc.light_count == 0u) return false;
-    const float target = l0 * sc.light_total;
-    uint32_t lo = 0, hi = sc.light_count - 1u;  // first light whose prefix exceeds the target
-    while (lo < hi) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (__ldg(&sc.lights[mid].x) > target) hi = mid;
-        else lo = mid + 1u;
+    uint32_t k = 0, prim = ~0u;
+    float pick = 1.0f, u = l0;
+    for (int level = 0; level < 64; ++level) {
+        const float4 b = __ldg(sc.lights + 2 * (size_t)k + 1);
+        if (__float_as_uint(b.w) != ~0u) {
+            prim = __float_as_uint(b.w);
+            break;
+        }
+        const uint32_t kl = __float_as_uint(b.y), kr = __float_as_uint(b.z);
+        const float wl = light_importance(sc.lights, kl, no), wr = light_importance(sc.lights, kr, no);
+        const float pl = wl / (wl + wr);
+        if (!(pl >= 0.0f && pl <= 1.0f)) return false;
+        if (u < pl) {
+            k = kl;
+            pick = pick * pl;
+            u = u / pl;
+        } else {
+            k = kr;
+            pick = pick * (1.0f - pl);
+            u = (u - pl) / (1.0f - pl);
+        }
+        u = glsl_min(u, 0.99999994f);
     }
-    const float4 L = __ldg(sc.lights + lo);
-    const uint4 ti = __ldg(sc.tri_idx + __float_as_uint(L.z));
+    if (prim == ~0u || !(pick > 0.0f)) return false;
+    const uint4 ti = __ldg(sc.tri_idx + prim);
     const float4 a = __ldg(sc.vpos + ti.x), b = __ldg(sc.vpos + ti.y), c = __ldg(sc.vpos + ti.z);
     const f3 p0{a.x, a.y, a.z}, p1{b.x, b.y, b.z}, p2{c.x, c.y, c.z};
     const float su = sqrtf(l1);
@@ -174,7 +203,7 @@ SOLRT_D bool nee_sample(const DevScene& sc, f3 no, f3 n_o, f3 thr, float tmin, u
     const float tmax = dist * 0.9999f;
     if (!(cx > 0.0f) || !(cy > 0.0f) || !(tmax > tmin)) return false;
     const float4 le = __ldg(sc.materials + 3 * __ldg(sc.sec_mat + ti.w) + 1);
-    const float wgt = ((cx * cy) * (0.5f * a2)) / ((3.14159265f * d2) * L.y);
+    const float wgt = ((cx * cy) * (0.5f * a2)) / ((3.14159265f * d2) * pick);
     contrib = (thr * f3{le.x, le.y, le.z}) * wgt;
     so = make_float4(no.x, no.y, no.z, tmin);
     sd = make_float4(wl.x, wl.y, wl.z, tmax);

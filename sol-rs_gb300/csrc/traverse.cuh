@@ -38,11 +38,11 @@ struct DevScene {
     const float4* materials;  // solrt_material as 3 float4
     const float4* nodes;      // BVH2: 4 float4 per node; BVH8: 5 float4 per node
     const float4* tri_wt;     // 3 float4 per triangle in leaf order; p0.w = prim bits
-    // emissive triangles for next-event estimation: per light (inclusive
-    // area prefix, pick probability, prim bits, 0) in triangle order
+    // light tree of next-event estimation over the emissive triangles, two
+    // float4 per node: (box centre, squared half-diagonal), (power, left,
+    // right, triangle of a leaf or ~0u as bits); root = node 0
     const float4* lights;
-    uint32_t light_count;
-    float light_total;        // area sum (the last prefix)
+    uint32_t light_count;     // leaves (emissive triangles)
 };
 
 // What the traversal needs of a scene (per ray: rays of one launch may belong

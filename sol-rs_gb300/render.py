@@ -61,7 +61,8 @@ def main(argv=None):
     src.add_argument("--model", help=".gltf or .glb file")
     src.add_argument("--scene", choices=["cornell", "soup", "tunnel"])
     ap.add_argument("--tris", type=int, default=1_000_000, help="triangles of --scene soup")
-    ap.add_argument("--integrator", choices=["path", "ao", "debug"], default="path")
+    ap.add_argument("--integrator", choices=["path", "nee", "ao", "debug"], default="path",
+                    help="nee: path tracing with next-event estimation (implies --lambert)")
     ap.add_argument("--sky", action="store_true", help="pathtrace.rmiss ENABLE_SKYLIGHT")
     ap.add_argument("--width", type=int, default=1280)
     ap.add_argument("--height", type=int, default=720)
@@ -75,9 +76,11 @@ def main(argv=None):
     args = ap.parse_args(argv)
 
     w, h = args.width, args.height
-    integ = {"path": _pkg.INTEGRATOR_PATH, "ao": _pkg.INTEGRATOR_AO, "debug": _pkg.INTEGRATOR_DEBUG}[args.integrator]
-    spp = args.spp or {"path": 8, "ao": 4, "debug": 1}[args.integrator]
-    bounces = args.bounces or {"path": 32, "ao": 4, "debug": 1}[args.integrator]
+    integ = {"path": _pkg.INTEGRATOR_PATH, "nee": _pkg.INTEGRATOR_PATH_NEE, "ao": _pkg.INTEGRATOR_AO,
+             "debug": _pkg.INTEGRATOR_DEBUG}[args.integrator]
+    spp = args.spp or {"path": 8, "nee": 8, "ao": 4, "debug": 1}[args.integrator]
+    bounces = args.bounces or {"path": 32, "nee": 32, "ao": 4, "debug": 1}[args.integrator]
+    lambert = args.lambert or args.integrator == "nee"
     frames = 1 if args.integrator == "debug" else args.frames
     data, cam = _scene_and_camera(args, w / h)
     ctx = _pkg.Context(0)
@@ -93,7 +96,7 @@ def main(argv=None):
     for f in range(frames):
         p = _pkg.render_params(w, h, spp=spp, max_bounces=bounces, frame=f, integrator=integ,
                                miss_mode=_pkg.MISS_REF_SKY if args.sky else _pkg.MISS_BLACK,
-                               material_mode=_pkg.MATERIAL_LAMBERT if args.lambert else _pkg.MATERIAL_REF)
+                               material_mode=_pkg.MATERIAL_LAMBERT if lambert else _pkg.MATERIAL_REF)
         r.cmd_trace_rays(sc, cam, p, img)
     ctx.synchronize()
     dt = time.perf_counter() - t0
@@ -102,6 +105,9 @@ def main(argv=None):
     st = ctx.stats()
     print("%s: %d tris, %d frames, %d segments in %.3f s (%.1f Mrays/s) -> %s"
           % (args.model or args.scene, data.tri_count, frames, st.segments, dt, st.segments / dt / 1e6, args.out))
+    if st.shadow_segments:
+        print("shadow rays: %d (%.1f %% unoccluded)" % (st.shadow_segments,
+                                                        100.0 * st.shadow_unoccluded / st.shadow_segments))
     img.close()
     sc.close()
     ctx.close()
