@@ -250,13 +250,16 @@ struct oracle_scene {
     std::vector<uint32_t> child;         // 2 per internal node
     std::vector<Box> node_box;           // per internal node
     std::vector<Box> leaf_box;           // per sorted position
-    // next-event estimation: light tree over the emissive triangles
+    // next-event estimation: light tree over the emissive triangles; each
+    // inner node holds its two children's box centre, squared half-diagonal,
+    // power and ref (>= 0 an inner node, < 0 the triangle ~ref)
     struct LightNode {
-        float c[3], r2;            // box centre, squared half-diagonal
-        float power;
-        uint32_t left, right, prim;  // children, or the triangle of a leaf (else ~0u)
+        float c[2][3], r2[2], power[2];
+        int32_t ref[2];
     };
     std::vector<LightNode> light_tree;
+    // per triangle: (levels << 27) | branch bits of its leaf, ~0u if not a light
+    std::vector<uint32_t> tri_light;
 };
 
 namespace {
@@ -613,51 +616,80 @@ template <class R> void hit_frame(const oracle_scene* s, const TriW& tri, R b0, 
     pos = V3<R>{o[0], o[1], o[2]};
 }
 
-// Importance of light-tree node k seen from x: power / max(d^2, r^2), d the
-// distance to the box centre, r the half-diagonal.
-template <class R> R light_importance(const oracle_scene* s, uint32_t k, V3<R> x) {
-    const oracle_scene::LightNode& nd = s->light_tree[k];
-    const V3<R> dv{R(nd.c[0]) - x.x, R(nd.c[1]) - x.y, R(nd.c[2]) - x.z};
-    return R(nd.power) / std::max(dot(dv, dv), R(nd.r2));
+// Importance of child j of a light-tree node seen from x: power /
+// max(d^2, r^2), d the distance to the child's box centre, r its
+// half-diagonal.
+template <class R> R light_importance(const oracle_scene::LightNode& nd, int j, V3<R> x) {
+    const V3<R> dv{R(nd.c[j][0]) - x.x, R(nd.c[j][1]) - x.y, R(nd.c[j][2]) - x.z};
+    return R(nd.power[j]) / std::max(dot(dv, dv), R(nd.r2[j]));
+}
+
+// Probability that the light-tree walk from x picks the light of `code`
+// (the products of the sampling walk in nee_term).
+template <class R> R light_pick_prob(const oracle_scene* s, uint32_t code, V3<R> x) {
+    const uint32_t levels = code >> 27;
+    uint32_t k = 0;
+    R pick = R(1);
+    for (uint32_t lv = 0; lv < levels; ++lv) {
+        const oracle_scene::LightNode& nd = s->light_tree[k];
+        const R wl = light_importance<R>(nd, 0, x), wr = light_importance<R>(nd, 1, x);
+        const R pl = wl / (wl + wr);
+        if (!(pl >= R(0) && pl <= R(1))) return R(0);
+        const bool right = (code >> lv) & 1u;
+        pick = right ? pick * (R(1) - pl) : pick * pl;
+        const int32_t ref = nd.ref[right ? 1 : 0];
+        if (ref < 0) break;
+        k = (uint32_t)ref;
+    }
+    return pick;
+}
+
+// Power-heuristic weight of a sample whose technique has pdf p_this against
+// one with pdf p_other: 1 / (1 + (p_other / p_this)^2).
+template <class R> R mis_weight(R p_this, R p_other) {
+    if (!(p_this > R(0))) return R(0);
+    const R r = p_other / p_this;
+    return R(1) / (R(1) + r * r);
 }
 
 // Next-event estimation at a diffuse vertex (SOLRT_INTEGRATOR_PATH_NEE, an
-// estimator the reference does not have). Three draws: l0 walks the light
-// tree, taking each child with probability proportional to its importance
-// (l0 rescaled into the chosen interval, kept below 1; p_pick the product
-// of the choices); l1 and l2 pick a uniform point on the triangle
-// (b0 = 1 - sqrt(l1), b1 = l2 sqrt(l1)). The shadow ray leaves from the
-// continuation origin `no` towards it with tmax 0.9999 of the distance. An
-// unoccluded one returns thr * Le * cos_x * cos_y * area / (pi r^2 p_pick):
-// Lambert albedo / pi (thr already holds the albedo) times Le times the
-// geometry term over the area pdf p_pick / area. Emitters are two-sided.
+// estimator the reference does not have). Draws: l1 and l2 pick a uniform
+// point on the light triangle (b0 = 1 - sqrt(l1), b1 = l2 sqrt(l1)), then
+// one draw per light-tree level takes the left child with probability
+// wl / (wl + wr) of the children's importances (p_pick the product of the
+// choices). The shadow ray leaves from the continuation origin `no` towards
+// the point with tmax 0.9999 of the distance. An unoccluded one returns
+// thr * Le * (pb / pl) * w: pl = p_pick r^2 / (area cos_y) and pb = cos_x / pi
+// are the solid-angle pdfs of the light pick and of the cosine BSDF sample
+// (thr already holds the albedo), w = 1 / (1 + (pb / pl)^2) the power
+// heuristic; the BSDF sample's emitter hit gets the complementary weight in
+// trace_path. Emitters are two-sided.
 template <class R> bool nee_term(const oracle_scene* s, V3<R> no, V3<R> n_o, V3<R> thr, R tmin, uint32_t& rng,
                                  Counters& cn, V3<R>& contrib) {
-    const R l0 = next_rand<R>(rng);
     const R l1 = next_rand<R>(rng);
     const R l2 = next_rand<R>(rng);
     if (s->light_tree.empty()) return false;
     uint32_t k = 0, prim = ~0u;
-    R pick = R(1), u = l0;
+    R pick = R(1);
     for (int level = 0; level < 64; ++level) {
         const oracle_scene::LightNode& nd = s->light_tree[k];
-        if (nd.prim != ~0u) {
-            prim = nd.prim;
-            break;
-        }
-        const R wl = light_importance<R>(s, nd.left, no), wr = light_importance<R>(s, nd.right, no);
+        const R wl = light_importance<R>(nd, 0, no), wr = light_importance<R>(nd, 1, no);
         const R pl = wl / (wl + wr);
         if (!(pl >= R(0) && pl <= R(1))) return false;
-        if (u < pl) {
-            k = nd.left;
+        const R ul = next_rand<R>(rng);
+        int32_t ref;
+        if (ul < pl) {
+            ref = nd.ref[0];
             pick = pick * pl;
-            u = u / pl;
         } else {
-            k = nd.right;
+            ref = nd.ref[1];
             pick = pick * (R(1) - pl);
-            u = (u - pl) / (R(1) - pl);
         }
-        u = std::min(u, R(0.99999994f));
+        if (ref < 0) {
+            prim = (uint32_t)~ref;
+            break;
+        }
+        k = (uint32_t)ref;
     }
     if (prim == ~0u || !(pick > R(0))) return false;
     const TriW& tri = s->tris[prim];
@@ -680,7 +712,11 @@ template <class R> bool nee_term(const oracle_scene* s, V3<R> no, V3<R> n_o, V3<
     const R tmax = dist * R(0.9999f);
     if (!(cx > R(0)) || !(cy > R(0)) || !(tmax > tmin)) return false;
     const float* le = s->mats[tri.mat].emissive;
-    const R wgt = ((cx * cy) * (R(0.5f) * a2)) / ((R(3.14159265f) * d2) * pick);
+    // solid-angle pdfs of this direction: light pick, cosine BSDF sample
+    const R pl = (pick * d2) / ((R(0.5f) * a2) * cy);
+    const R pb = cx / R(3.14159265f);
+    if (!(pl > R(0))) return false;
+    const R wgt = (pb / pl) * mis_weight<R>(pl, pb);
     ++cn.shadow;
     uint64_t nv = 0, nt = 0, fb = 0;
     const HitR<R> h = closest_hit<R>(s, no, wl, tmin, tmax, 1, fb, nv, nt);
@@ -696,6 +732,7 @@ template <class R> V3<R> trace_path(const oracle_scene* s, const solrt_render_pa
     uint32_t depth = 0;
     const bool nee = p->integrator == SOLRT_INTEGRATOR_PATH_NEE;
     V3<R> nee_sum{R(0), R(0), R(0)};  // shadow terms in bounce order, then the path's end
+    R pdf_prev = R(0);                 // solid-angle pdf of the current ray's BSDF sample
     for (;;) {
         const HitR<R> h = closest_hit<R>(s, o, d, tmin, tmax, 1, cn.fb, cn.nv, cn.nt);
         ++cn.seg;
@@ -706,8 +743,21 @@ template <class R> V3<R> trace_path(const oracle_scene* s, const solrt_render_pa
         const TriW& tri = s->tris[h.prim];                  // pathtrace.rchit
         const solrt_material& m = s->mats[tri.mat];
         if (m.emissive[0] >= 1.0f || m.emissive[1] >= 1.0f || m.emissive[2] >= 1.0f) {
-            if (nee && depth > 0) acc = V3<R>{R(0), R(0), R(0)};  // its light came through shadow rays
-            else acc = acc * V3<R>{R(m.emissive[0]), R(m.emissive[1]), R(m.emissive[2])};
+            acc = acc * V3<R>{R(m.emissive[0]), R(m.emissive[1]), R(m.emissive[2])};
+            if (nee && depth > 0) {  // power heuristic against next-event estimation
+                const uint32_t code = s->tri_light.empty() ? ~0u : s->tri_light[h.prim];
+                R pl = R(0);
+                if (code != ~0u) {
+                    auto cw = [](V3<float> a) { return V3<R>{R(a.x), R(a.y), R(a.z)}; };
+                    const V3<R> e1 = cw(tri.p[1]) - cw(tri.p[0]), e2 = cw(tri.p[2]) - cw(tri.p[0]);
+                    const V3<R> ng{e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x};
+                    const R a2 = length(ng);
+                    const R cy = std::abs(dot(ng, d)) / a2;
+                    const R pick = light_pick_prob<R>(s, code, o);
+                    pl = (pick * (h.t * h.t)) / ((R(0.5f) * a2) * cy);
+                }
+                acc = acc * mis_weight<R>(pdf_prev, pl);
+            }
             break;
         }
         const R b1 = h.u, b2 = h.v;
@@ -728,6 +778,7 @@ template <class R> V3<R> trace_path(const oracle_scene* s, const solrt_render_pa
         if (p->material_mode == SOLRT_MATERIAL_LAMBERT) {
             d = sample_cosine(n_o, xi0, xi1);
             hv = base * vcol;
+            pdf_prev = dot(n_o, d) / R(3.14159265f);
         } else if (rnd < R(m.metallic)) {
             d = sample_ggx(reflect(d, n_o), xi0, xi1, alpha2);
             hv = base * vcol;
@@ -987,15 +1038,22 @@ int resolve_threads(int threads) {
 // channel >= 1, pathtrace.rchit:75-80; zero-area ones left out) sorted by
 // the 30-bit Morton code of their centroid ((p0 + p1) + p2) / 3 in the
 // centroids' bounds (ties by triangle index), ranges split at their middle;
-// a node's box is the union of its children's (a leaf's: its triangle's),
-// its power left + right (a leaf's: area * ((Le.r + Le.g) + Le.b)).
-uint32_t light_node(oracle_scene* s, const std::vector<uint32_t>& order, const std::vector<float>& box,
-                    const std::vector<float>& power, const std::vector<uint32_t>& prim, uint32_t b, uint32_t e,
-                    float mn[3], float mx[3], float& pw) {
-    const uint32_t idx = (uint32_t)s->light_tree.size();
-    s->light_tree.push_back(oracle_scene::LightNode{});
-    oracle_scene::LightNode nd{};
-    nd.left = nd.right = nd.prim = ~0u;
+// a child's box is the union of its children's (a triangle's: its own), its
+// power left + right (a triangle's: area * ((Le.r + Le.g) + Le.b)), its
+// centre (min + max) / 2 and squared half-diagonal from (max - min) / 2. One
+// light: a root whose two refs are that light and whose right power is 0.
+void light_sphere(const float mn[3], const float mx[3], float c[3], float& r2) {
+    float h[3];
+    for (int k = 0; k < 3; ++k) {
+        c[k] = (mn[k] + mx[k]) * 0.5f;
+        h[k] = (mx[k] - mn[k]) * 0.5f;
+    }
+    r2 = (h[0] * h[0] + h[1] * h[1]) + h[2] * h[2];
+}
+
+int32_t light_node(oracle_scene* s, const std::vector<uint32_t>& order, const std::vector<float>& box,
+                   const std::vector<float>& power, const std::vector<uint32_t>& prim, uint32_t b, uint32_t e,
+                   float mn[3], float mx[3], float& pw, uint32_t bits, uint32_t level) {
     if (e - b == 1) {
         const uint32_t k = order[b];
         for (int c = 0; c < 3; ++c) {
@@ -1003,27 +1061,29 @@ uint32_t light_node(oracle_scene* s, const std::vector<uint32_t>& order, const s
             mx[c] = box[6 * k + 3 + c];
         }
         pw = power[k];
-        nd.prim = prim[k];
-    } else {
-        const uint32_t m = b + (e - b) / 2;
-        float amn[3], amx[3], bmn[3], bmx[3], pa = 0.0f, pb = 0.0f;
-        nd.left = light_node(s, order, box, power, prim, b, m, amn, amx, pa);
-        nd.right = light_node(s, order, box, power, prim, m, e, bmn, bmx, pb);
-        for (int c = 0; c < 3; ++c) {
-            mn[c] = std::min(amn[c], bmn[c]);
-            mx[c] = std::max(amx[c], bmx[c]);
-        }
-        pw = pa + pb;
+        s->tri_light[prim[k]] = (level << 27) | bits;
+        return ~(int32_t)prim[k];
     }
-    float h[3];
+    const uint32_t idx = (uint32_t)s->light_tree.size();
+    s->light_tree.push_back(oracle_scene::LightNode{});
+    const uint32_t m = b + (e - b) / 2;
+    float cmn[2][3], cmx[2][3], cp[2] = {0.0f, 0.0f};
+    int32_t ref[2];
+    ref[0] = light_node(s, order, box, power, prim, b, m, cmn[0], cmx[0], cp[0], bits, level + 1);
+    ref[1] = light_node(s, order, box, power, prim, m, e, cmn[1], cmx[1], cp[1], bits | (1u << level), level + 1);
+    oracle_scene::LightNode nd{};
+    for (int j = 0; j < 2; ++j) {
+        light_sphere(cmn[j], cmx[j], nd.c[j], nd.r2[j]);
+        nd.power[j] = cp[j];
+        nd.ref[j] = ref[j];
+    }
     for (int c = 0; c < 3; ++c) {
-        nd.c[c] = (mn[c] + mx[c]) * 0.5f;
-        h[c] = (mx[c] - mn[c]) * 0.5f;
+        mn[c] = std::min(cmn[0][c], cmn[1][c]);
+        mx[c] = std::max(cmx[0][c], cmx[1][c]);
     }
-    nd.r2 = (h[0] * h[0] + h[1] * h[1]) + h[2] * h[2];
-    nd.power = pw;
+    pw = cp[0] + cp[1];
     s->light_tree[idx] = nd;
-    return idx;
+    return (int32_t)idx;
 }
 
 void build_light_tree(oracle_scene* s) {
@@ -1051,8 +1111,9 @@ void build_light_tree(oracle_scene* s) {
         box.insert(box.end(), hi, hi + 3);
         power.push_back(pw);
     }
-    const uint32_t n = (uint32_t)prim.size();
+    const uint32_t n = std::min<uint32_t>((uint32_t)prim.size(), 1u << 26);  // codes hold 27 levels
     if (n == 0) return;
+    s->tri_light.assign(s->tris.size(), ~0u);
     float cmin[3] = {cen[0], cen[1], cen[2]}, cmax[3] = {cen[0], cen[1], cen[2]};
     for (uint32_t i = 1; i < n; ++i)
         for (int k = 0; k < 3; ++k) {
@@ -1073,8 +1134,19 @@ void build_light_tree(oracle_scene* s) {
     std::vector<uint32_t> order(n);
     for (uint32_t i = 0; i < n; ++i) order[i] = key[i].second;
     float mn[3], mx[3], pw = 0.0f;
-    s->light_tree.reserve(2 * (size_t)n);
-    light_node(s, order, box, power, prim, 0, n, mn, mx, pw);
+    s->light_tree.reserve((size_t)n);
+    const int32_t root = light_node(s, order, box, power, prim, 0, n, mn, mx, pw, 0u, 0u);
+    if (root < 0) {  // one light
+        s->tri_light[prim[0]] = 1u << 27;
+        oracle_scene::LightNode nd{};
+        for (int j = 0; j < 2; ++j) {
+            light_sphere(mn, mx, nd.c[j], nd.r2[j]);
+            nd.ref[j] = root;
+        }
+        nd.power[0] = pw;
+        nd.power[1] = 0.0f;
+        s->light_tree.push_back(nd);
+    }
 }
 
 extern "C" {

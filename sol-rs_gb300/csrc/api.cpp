@@ -131,20 +131,30 @@ std::mutex g_refs_mutex;
 // as pathtrace.rchit:75-80 decides it: any emissive channel >= 1; zero-area
 // triangles cannot be hit and are left out). Lights sorted by the 30-bit
 // Morton code of their centroid in the centroids' bounds (ties by triangle
-// index), split at the middle of each range, so the tree is balanced.
-// Per node two float4: (box centre, squared half-diagonal) and (power,
-// left, right, triangle of a leaf or ~0u); power = area * (Le.r + Le.g +
-// Le.b), summed left + right. All in float with a fixed order of operations.
+// index), split at the middle of each range, so the tree is balanced. Each
+// inner node holds both children, three float4: (left box centre, left
+// squared half-diagonal), the same for the right child, (left power, right
+// power, left ref, right ref as bits); a ref >= 0 is an inner node, < 0 the
+// triangle ~ref. A leaf's power is area * ((Le.r + Le.g) + Le.b), a node's
+// the sum left + right. One light: a root whose two refs are that light and
+// whose right power is 0. Per light its code: (levels << 27) | branch bits
+// (bit l set: right child at level l).
 struct LightBuild {
-    std::vector<uint32_t> prim;
+    std::vector<uint32_t> prim, code;
     std::vector<float> lo, hi, power;  // per light: box (3 + 3), power
     std::vector<float4> nodes;
-    uint32_t build(const std::vector<uint32_t>& order, uint32_t b, uint32_t e, float bmin[3], float bmax[3],
-                   float& pw) {
-        const uint32_t idx = (uint32_t)(nodes.size() / 2);
-        nodes.push_back(float4{});
-        nodes.push_back(float4{});
-        uint32_t l = ~0u, r = ~0u, leaf = ~0u;
+    static float4 sphere(const float mn[3], const float mx[3]) {
+        const float hx = (mx[0] - mn[0]) * 0.5f, hy = (mx[1] - mn[1]) * 0.5f, hz = (mx[2] - mn[2]) * 0.5f;
+        return make_float4((mn[0] + mx[0]) * 0.5f, (mn[1] + mx[1]) * 0.5f, (mn[2] + mx[2]) * 0.5f,
+                           (hx * hx + hy * hy) + hz * hz);
+    }
+    static float as_float(int32_t v) {
+        float f;
+        std::memcpy(&f, &v, 4);
+        return f;
+    }
+    int32_t build(const std::vector<uint32_t>& order, uint32_t b, uint32_t e, float bmin[3], float bmax[3],
+                  float& pw, uint32_t bits, uint32_t level) {
         if (e - b == 1) {
             const uint32_t k = order[b];
             for (int c = 0; c < 3; ++c) {
@@ -152,27 +162,24 @@ struct LightBuild {
                 bmax[c] = hi[3 * k + c];
             }
             pw = power[k];
-            leaf = prim[k];
-        } else {
-            const uint32_t m = b + (e - b) / 2;
-            float amin[3], amax[3], cmin[3], cmax[3], pa = 0.0f, pc = 0.0f;
-            l = build(order, b, m, amin, amax, pa);
-            r = build(order, m, e, cmin, cmax, pc);
-            for (int c = 0; c < 3; ++c) {
-                bmin[c] = std::min(amin[c], cmin[c]);
-                bmax[c] = std::max(amax[c], cmax[c]);
-            }
-            pw = pa + pc;
+            code[k] = (level << 27) | bits;
+            return ~(int32_t)prim[k];
         }
-        const float hx = (bmax[0] - bmin[0]) * 0.5f, hy = (bmax[1] - bmin[1]) * 0.5f, hz = (bmax[2] - bmin[2]) * 0.5f;
-        nodes[2 * idx] = make_float4((bmin[0] + bmax[0]) * 0.5f, (bmin[1] + bmax[1]) * 0.5f,
-                                     (bmin[2] + bmax[2]) * 0.5f, (hx * hx + hy * hy) + hz * hz);
-        float fl, fr, ft;
-        std::memcpy(&fl, &l, 4);
-        std::memcpy(&fr, &r, 4);
-        std::memcpy(&ft, &leaf, 4);
-        nodes[2 * idx + 1] = make_float4(pw, fl, fr, ft);
-        return idx;
+        const uint32_t idx = (uint32_t)(nodes.size() / 3);
+        nodes.resize(nodes.size() + 3);
+        const uint32_t m = b + (e - b) / 2;
+        float amin[3], amax[3], cmin[3], cmax[3], pa = 0.0f, pc = 0.0f;
+        const int32_t l = build(order, b, m, amin, amax, pa, bits, level + 1);
+        const int32_t r = build(order, m, e, cmin, cmax, pc, bits | (1u << level), level + 1);
+        nodes[3 * idx] = sphere(amin, amax);
+        nodes[3 * idx + 1] = sphere(cmin, cmax);
+        nodes[3 * idx + 2] = make_float4(pa, pc, as_float(l), as_float(r));
+        for (int c = 0; c < 3; ++c) {
+            bmin[c] = std::min(amin[c], cmin[c]);
+            bmax[c] = std::max(amax[c], cmax[c]);
+        }
+        pw = pa + pc;
+        return (int32_t)idx;
     }
 };
 
@@ -186,7 +193,7 @@ uint32_t expand10(uint32_t v) {
 
 std::vector<float4> build_light_tree(const std::vector<float4>& pos, const std::vector<uint4>& tri,
                                      const std::vector<uint32_t>& sec_mat, const solrt_material* mats,
-                                     uint32_t& count) {
+                                     uint32_t& count, std::vector<uint32_t>& tri_code) {
     LightBuild lb;
     std::vector<float> cen;
     for (size_t t = 0; t < tri.size(); ++t) {
@@ -208,9 +215,10 @@ std::vector<float4> build_light_tree(const std::vector<float4>& pos, const std::
         }
         lb.power.push_back(pw);
     }
-    const uint32_t n = (uint32_t)lb.prim.size();
+    const uint32_t n = std::min<uint32_t>((uint32_t)lb.prim.size(), 1u << 26);  // codes hold 27 levels
     count = n;
     if (n == 0) return {};
+    lb.code.assign(n, 0u);
     float cmin[3] = {cen[0], cen[1], cen[2]}, cmax[3] = {cen[0], cen[1], cen[2]};
     for (uint32_t i = 1; i < n; ++i)
         for (int k = 0; k < 3; ++k) {
@@ -232,8 +240,15 @@ std::vector<float4> build_light_tree(const std::vector<float4>& pos, const std::
     std::vector<uint32_t> order(n);
     for (uint32_t i = 0; i < n; ++i) order[i] = key[i].second;
     float bmin[3], bmax[3], pw = 0.0f;
-    lb.nodes.reserve(4 * (size_t)n);
-    lb.build(order, 0, n, bmin, bmax, pw);
+    lb.nodes.reserve(3 * (size_t)n);
+    const int32_t root = lb.build(order, 0, n, bmin, bmax, pw, 0u, 0u);
+    if (root < 0) {  // one light
+        const float4 sp = LightBuild::sphere(bmin, bmax);
+        lb.nodes = {sp, sp, make_float4(pw, 0.0f, LightBuild::as_float(root), LightBuild::as_float(root))};
+        lb.code[0] = 1u << 27;
+    }
+    tri_code.assign(tri.size(), ~0u);
+    for (uint32_t k = 0; k < n; ++k) tri_code[lb.prim[k]] = lb.code[k];
     return lb.nodes;
 }
 
@@ -548,8 +563,15 @@ solrt_status solrt_scene_create(solrt_context* ctx, const solrt_scene_desc* d, c
     }
     // light tree of next-event estimation (world positions at creation)
     uint32_t light_count = 0;
-    const std::vector<float4> lights = build_light_tree(pos, tri, sec_mat, d->materials, light_count);
+    std::vector<uint32_t> tri_code;
+    const std::vector<float4> lights = build_light_tree(pos, tri, sec_mat, d->materials, light_count, tri_code);
     if (!lights.empty()) {
+        if ((s = sc->tri_light.alloc(4 * tri_code.size())) != SOLRT_OK) return fail(s);
+        if (cudaMemcpyAsync(sc->tri_light.ptr, tri_code.data(), 4 * tri_code.size(), cudaMemcpyHostToDevice, st) !=
+            cudaSuccess) {
+            set_error("scene upload failed");
+            return fail(SOLRT_ERR_DEVICE);
+        }
         if ((s = sc->lights.alloc(sizeof(float4) * lights.size())) != SOLRT_OK) return fail(s);
         if (cudaMemcpyAsync(sc->lights.ptr, lights.data(), sizeof(float4) * lights.size(), cudaMemcpyHostToDevice,
                             st) != cudaSuccess) {
@@ -623,7 +645,7 @@ solrt_status solrt_scene_bytes(solrt_scene* scene, uint64_t* out) {
            scene->materials.bytes + scene->sec_mat.bytes + scene->nodes.bytes + scene->tri_wt.bytes +
            scene->vsec_start.bytes + scene->instances.bytes + scene->topo_order.bytes + scene->topo_child.bytes +
            scene->topo_par_int.bytes + scene->topo_par_leaf.bytes + scene->topo_range.bytes + scene->tlas.bytes +
-           scene->inst_table.bytes + scene->lights.bytes;
+           scene->inst_table.bytes + scene->lights.bytes + scene->tri_light.bytes;
     return SOLRT_OK;
 }
 

@@ -97,6 +97,7 @@ struct PathQueue {
     float4* d_tmax;   // direction, tmax
     float4* thr_rng;  // throughput, rng state (bits)
     uint2* meta;      // slot within the pass, job << kDepthBits | depth
+    float* pdf;       // SOLRT_INTEGRATOR_PATH_NEE: solid-angle pdf of the direction's BSDF sample
 };
 
 // One job of a wavefront batch, as the device sees it.
@@ -186,6 +187,7 @@ struct Context {
     // queues 0 and 1: paths of alternate bounces; queue 2: shadow rays of
     // SOLRT_INTEGRATOR_PATH_NEE (allocated when a render first needs it)
     DeviceBuffer q_o[3], q_d[3], q_thr[3], q_meta[3];
+    DeviceBuffer q_pdf[2];  // per path of queues 0 and 1, next-event estimation only
     DeviceBuffer hits, rad, ctl, stats, trace_work;
     DeviceBuffer blue_noise;  // RGBA8 texels of SOLRT_INTEGRATOR_AO
     DeviceBuffer sibling_job;  // one-job table of DEBUG / AO launches
@@ -233,7 +235,8 @@ struct Context {
         timed_used = 0;
     }
     PathQueue queue(int i) const {
-        return PathQueue{q_o[i].as<float4>(), q_d[i].as<float4>(), q_thr[i].as<float4>(), q_meta[i].as<uint2>()};
+        return PathQueue{q_o[i].as<float4>(), q_d[i].as<float4>(), q_thr[i].as<float4>(), q_meta[i].as<uint2>(),
+                         i < 2 ? q_pdf[i].as<float>() : nullptr};
     }
 };
 
@@ -270,8 +273,9 @@ struct Scene {
     std::vector<int32_t> blas_root;
     uint32_t blas_depth = 0, tlas_count = 0, tlas_depth = 0;
     DeviceBuffer tlas, inst_table;
-    // light tree of next-event estimation (see DevScene::lights), built at creation
-    DeviceBuffer lights;
+    // light tree of next-event estimation (see DevScene::lights), built at
+    // creation, and per triangle its light-tree code (DevScene::tri_light)
+    DeviceBuffer lights, tri_light;
     uint32_t light_count = 0;
     DevScene view() const {
         DevScene d;
@@ -294,6 +298,7 @@ struct Scene {
         d.nodes = nodes.as<float4>();
         d.tri_wt = tri_wt.as<float4>();
         d.lights = lights.as<float4>();
+        d.tri_light = tri_light.as<uint32_t>();
         d.light_count = light_count;
         return d;
     }

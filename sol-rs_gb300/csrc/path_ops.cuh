@@ -64,11 +64,17 @@ SOLRT_D void hit_frame(const DevScene& sc, uint4 ti, float b0, float b1, float b
 // and pathtrace.rgen:77-84). h = (t, prim bits, u, v). Updates the path
 // throughput `acc`, the rng state and the depth; returns true when the path
 // continues with the ray (o_next, d_next).
-// With SOLRT_INTEGRATOR_PATH_NEE an emitter hit after a bounce adds nothing
-// (next-event estimation carried that light), and `n_out`, when given,
-// receives the oriented shading normal of a continuing path.
+SOLRT_D float light_pick_prob(const DevScene& sc, uint32_t code, f3 x);
+SOLRT_D float mis_weight(float p_this, float p_other);
+
+// With SOLRT_INTEGRATOR_PATH_NEE an emitter hit after a bounce is weighted
+// by the power heuristic against next-event estimation (`pdf_prev`: the
+// solid-angle pdf of this ray's BSDF sample); `n_out` and `pdf_out`, when
+// given, receive the oriented shading normal of a continuing path and the
+// pdf of its new direction.
 SOLRT_D bool shade_step(const DevJob& J, float4 o, float4 d, float4 h, f3& acc, uint32_t& rng, uint32_t& depth,
-                        float4& o_next, float4& d_next, uint32_t& ef, f3* n_out = nullptr) {
+                        float4& o_next, float4& d_next, uint32_t& ef, f3* n_out = nullptr, float pdf_prev = 0.0f,
+                        float* pdf_out = nullptr) {
     const DevScene& sc = J.sc;
     const f3 dir{d.x, d.y, d.z};
     const uint32_t prim = __float_as_uint(h.y);
@@ -83,8 +89,23 @@ SOLRT_D bool shade_step(const DevJob& J, float4 o, float4 d, float4 h, f3& acc, 
     const float4 m1 = __ldg(sc.materials + 3 * mat + 1);
     const float4 m2 = __ldg(sc.materials + 3 * mat + 2);
     if (m1.x >= 1.0f || m1.y >= 1.0f || m1.z >= 1.0f) {                      // rchit:75-80
-        if (J.integrator == SOLRT_INTEGRATOR_PATH_NEE && depth > 0u) acc = f3{0.0f, 0.0f, 0.0f};
-        else acc = acc * f3{m1.x, m1.y, m1.z};
+        acc = acc * f3{m1.x, m1.y, m1.z};
+        if (J.integrator == SOLRT_INTEGRATOR_PATH_NEE && depth > 0u) {
+            // the light pdf of this hit: pick probability from the ray's
+            // origin times distance^2 / (area cos_y)
+            const uint32_t code = sc.tri_light ? __ldg(sc.tri_light + prim) : ~0u;
+            float pl = 0.0f;
+            if (code != ~0u) {
+                const float4 a = __ldg(sc.vpos + ti.x), b = __ldg(sc.vpos + ti.y), c = __ldg(sc.vpos + ti.z);
+                const f3 e1{b.x - a.x, b.y - a.y, b.z - a.z}, e2{c.x - a.x, c.y - a.y, c.z - a.z};
+                const f3 ng{e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x};
+                const float a2 = length(ng);
+                const float cy = fabsf(dot(ng, dir)) / a2;
+                const float pick = light_pick_prob(sc, code, f3{o.x, o.y, o.z});
+                pl = (pick * (h.x * h.x)) / ((0.5f * a2) * cy);
+            }
+            acc = acc * mis_weight(pdf_prev, pl);
+        }
         return false;
     }
     const float b1 = h.z, b2 = h.w;
@@ -127,62 +148,90 @@ SOLRT_D bool shade_step(const DevJob& J, float4 o, float4 d, float4 h, f3& acc, 
     o_next = make_float4(no.x, no.y, no.z, o.w);
     d_next = make_float4(nd.x, nd.y, nd.z, d.w);
     if (n_out) *n_out = n_o;
+    if (pdf_out) *pdf_out = dot(n_o, nd) / 3.14159265f;
     return true;
 }
 
-// Importance of a light-tree node seen from x: power / max(d^2, r^2), d the
-// distance to the node's box centre, r its half-diagonal.
-SOLRT_D float light_importance(const float4* tree, uint32_t k, f3 x) {
-    const float4 a = __ldg(tree + 2 * (size_t)k);
-    const float pw = __ldg(&tree[2 * (size_t)k + 1].x);
-    const f3 dv{a.x - x.x, a.y - x.y, a.z - x.z};
-    return pw / glsl_max(dot(dv, dv), a.w);
+// Importance of a light-tree child seen from x: power / max(d^2, r^2), d the
+// distance to the child's box centre, r its half-diagonal (s = (centre, r^2)).
+SOLRT_D float light_importance(float4 s, float power, f3 x) {
+    const f3 dv{s.x - x.x, s.y - x.y, s.z - x.z};
+    return power / glsl_max(dot(dv, dv), s.w);
+}
+
+// Probability that the light-tree walk from x picks the light of `code`
+// (the same products as the sampling walk of nee_sample).
+SOLRT_D float light_pick_prob(const DevScene& sc, uint32_t code, f3 x) {
+    const uint32_t levels = code >> 27;
+    uint32_t k = 0;
+    float pick = 1.0f;
+    for (uint32_t lv = 0; lv < levels; ++lv) {
+        const float4* nd = sc.lights + 3 * (size_t)k;
+        const float4 sl = __ldg(nd), sr = __ldg(nd + 1), pc = __ldg(nd + 2);
+        const float wl = light_importance(sl, pc.x, x), wr = light_importance(sr, pc.y, x);
+        const float pl = wl / (wl + wr);
+        if (!(pl >= 0.0f && pl <= 1.0f)) return 0.0f;
+        const bool right = (code >> lv) & 1u;
+        pick = right ? pick * (1.0f - pl) : pick * pl;
+        const int ref = __float_as_int(right ? pc.w : pc.z);
+        if (ref < 0) break;
+        k = (uint32_t)ref;
+    }
+    return pick;
+}
+
+// Power-heuristic weight of a sample whose technique has pdf p_this against
+// one with pdf p_other: 1 / (1 + (p_other / p_this)^2).
+SOLRT_D float mis_weight(float p_this, float p_other) {
+    if (!(p_this > 0.0f)) return 0.0f;
+    const float r = p_other / p_this;
+    return 1.0f / (1.0f + r * r);
 }
 
 // Next-event estimation at a diffuse vertex of SOLRT_INTEGRATOR_PATH_NEE (an
-// estimator the reference does not have). Three draws: l0 walks the light
-// tree from the root, taking each child with probability proportional to
-// its importance (l0 rescaled into the chosen interval at every level, kept
-// below 1), so near and bright lights are picked more often; p_pick is the
-// product of the choices. l1 and l2 pick a uniform point on the triangle
-// (b0 = 1 - sqrt(l1), b1 = l2 sqrt(l1)). `no` is the continuation origin
-// (hit + 1e-4 n_o), `thr` the throughput after the vertex's albedo. Returns
-// true with the shadow ray (so, sd: unit direction, tmax 0.9999 of the
-// distance) and the radiance it adds when unoccluded:
-// thr * Le * cos_x * cos_y * area / (pi * r^2 * p_pick), i.e. the Lambert
-// BRDF albedo / pi times Le times the geometry term over the area pdf
-// p_pick / area (area of the triangle's current world vertices). Emitters
-// are two-sided, as hits on them are (rchit:75-80).
+// estimator the reference does not have). Draws: l1 and l2 pick a uniform
+// point on the light triangle (b0 = 1 - sqrt(l1), b1 = l2 sqrt(l1)); then
+// one draw per light-tree level takes the left child with probability
+// wl / (wl + wr) of the children's importances, so near and bright lights
+// are picked more often; p_pick is the product of the choices. `no` is the
+// continuation origin (hit + 1e-4 n_o), `thr` the throughput after the
+// vertex's albedo. Returns true with the shadow ray (so, sd: unit
+// direction, tmax 0.9999 of the distance) and the radiance it adds when
+// unoccluded: thr * Le * (pb / pl) * w, with the solid-angle pdfs
+// pl = p_pick r^2 / (area cos_y) of the light pick and pb = cos_x / pi of the
+// cosine BSDF sample, and w = 1 / (1 + (pb / pl)^2) the power heuristic
+// (the BSDF sample's emitter hit gets the complementary weight in
+// shade_step). Area of the triangle's current world vertices; emitters are
+// two-sided, as hits on them are (rchit:75-80).
 SOLRT_D bool nee_sample(const DevScene& sc, f3 no, f3 n_o, f3 thr, float tmin, uint32_t& rng, float4& so,
                         float4& sd, f3& contrib) {
-    const float l0 = next_rand(rng);
     const float l1 = next_rand(rng);
     const float l2 = next_rand(rng);
     if (sc.light_count == 0u) return false;
     uint32_t k = 0, prim = ~0u;
-    float pick = 1.0f, u = l0;
+    float pick = 1.0f;
     for (int level = 0; level < 64; ++level) {
-        const float4 b = __ldg(sc.lights + 2 * (size_t)k + 1);
-        if (__float_as_uint(b.w) != ~0u) {
-            prim = __float_as_uint(b.w);
-            break;
-        }
-        const uint32_t kl = __float_as_uint(b.y), kr = __float_as_uint(b.z);
-        const float wl = light_importance(sc.lights, kl, no), wr = light_importance(sc.lights, kr, no);
+        const float4* nd = sc.lights + 3 * (size_t)k;
+        const float4 sl = __ldg(nd), sr = __ldg(nd + 1), pc = __ldg(nd + 2);
+        const float wl = light_importance(sl, pc.x, no), wr = light_importance(sr, pc.y, no);
         const float pl = wl / (wl + wr);
         if (!(pl >= 0.0f && pl <= 1.0f)) return false;
-        if (u < pl) {
-            k = kl;
+        const float ul = next_rand(rng);
+        int ref;
+        if (ul < pl) {
+            ref = __float_as_int(pc.z);
             pick = pick * pl;
-            u = u / pl;
         } else {
-            k = kr;
+            ref = __float_as_int(pc.w);
             pick = pick * (1.0f - pl);
-            u = (u - pl) / (1.0f - pl);
         }
-        u = glsl_min(u, 0.99999994f);
+        if (ref < 0) {
+            prim = (uint32_t)~ref;
+            break;
+        }
+        k = (uint32_t)ref;
     }
-    if (prim == ~0u || !(pick > 0.0f)) return false;
+    if (prim >= sc.tri_count || !(pick > 0.0f)) return false;
     const uint4 ti = __ldg(sc.tri_idx + prim);
     const float4 a = __ldg(sc.vpos + ti.x), b = __ldg(sc.vpos + ti.y), c = __ldg(sc.vpos + ti.z);
     const f3 p0{a.x, a.y, a.z}, p1{b.x, b.y, b.z}, p2{c.x, c.y, c.z};
@@ -203,7 +252,11 @@ SOLRT_D bool nee_sample(const DevScene& sc, f3 no, f3 n_o, f3 thr, float tmin, u
     const float tmax = dist * 0.9999f;
     if (!(cx > 0.0f) || !(cy > 0.0f) || !(tmax > tmin)) return false;
     const float4 le = __ldg(sc.materials + 3 * __ldg(sc.sec_mat + ti.w) + 1);
-    const float wgt = ((cx * cy) * (0.5f * a2)) / ((3.14159265f * d2) * pick);
+    // solid-angle pdfs of this direction: light pick, cosine BSDF sample
+    const float pl = (pick * d2) / ((0.5f * a2) * cy);
+    const float pb = cx / 3.14159265f;
+    if (!(pl > 0.0f)) return false;
+    const float wgt = (pb / pl) * mis_weight(pl, pb);  // BRDF cos / pdf, MIS-weighted
     contrib = (thr * f3{le.x, le.y, le.z}) * wgt;
     so = make_float4(no.x, no.y, no.z, tmin);
     sd = make_float4(wl.x, wl.y, wl.z, tmax);

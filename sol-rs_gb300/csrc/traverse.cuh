@@ -38,11 +38,15 @@ struct DevScene {
     const float4* materials;  // solrt_material as 3 float4
     const float4* nodes;      // BVH2: 4 float4 per node; BVH8: 5 float4 per node
     const float4* tri_wt;     // 3 float4 per triangle in leaf order; p0.w = prim bits
-    // light tree of next-event estimation over the emissive triangles, two
-    // float4 per node: (box centre, squared half-diagonal), (power, left,
-    // right, triangle of a leaf or ~0u as bits); root = node 0
+    // light tree of next-event estimation over the emissive triangles, three
+    // float4 per inner node: (left box centre, squared half-diagonal), the
+    // same for the right child, (left power, right power, left ref, right
+    // ref as bits; ref >= 0 an inner node, < 0 the triangle ~ref); root 0
     const float4* lights;
     uint32_t light_count;     // leaves (emissive triangles)
+    // per triangle: (levels << 27) | branch bits (bit l set: right child at
+    // level l) of its leaf in the light tree, ~0u when it is not a light
+    const uint32_t* tri_light;
 };
 
 // What the traversal needs of a scene (per ray: rays of one launch may belong
