@@ -616,23 +616,37 @@ template <class R> void hit_frame(const oracle_scene* s, const TriW& tri, R b0, 
     pos = V3<R>{o[0], o[1], o[2]};
 }
 
-// Importance of child j of a light-tree node seen from x: power /
-// max(d^2, r^2), d the distance to the child's box centre, r its
-// half-diagonal.
-template <class R> R light_importance(const oracle_scene::LightNode& nd, int j, V3<R> x) {
+// Importance of child j of a light-tree node seen from x with normal n:
+// power * cos_bound / max(d^2, r^2), d the distance to the child's box
+// centre, r the half-diagonal, cos_bound the largest cosine between n and a
+// direction into the child's bounding sphere (1 inside the sphere's
+// half-angle beta, sin beta = r / d; else max(0, cos theta cos beta +
+// sin theta sin beta)).
+template <class R> R light_importance(const oracle_scene::LightNode& nd, int j, V3<R> x, V3<R> n) {
     const V3<R> dv{R(nd.c[j][0]) - x.x, R(nd.c[j][1]) - x.y, R(nd.c[j][2]) - x.z};
-    return R(nd.power[j]) / std::max(dot(dv, dv), R(nd.r2[j]));
+    const R d2 = dot(dv, dv), r2 = R(nd.r2[j]);
+    R cb = R(1);
+    if (d2 > r2) {
+        const R ct = dot(n, dv) / std::sqrt(d2);
+        const R sb2 = r2 / d2;
+        const R cbeta = std::sqrt(R(1) - sb2);
+        if (ct < cbeta) {
+            const R st = std::sqrt(std::max(R(1) - ct * ct, R(0)));
+            cb = std::max(ct * cbeta + st * std::sqrt(sb2), R(0));
+        }
+    }
+    return (R(nd.power[j]) * cb) / std::max(d2, r2);
 }
 
-// Probability that the light-tree walk from x picks the light of `code`
-// (the products of the sampling walk in nee_term).
-template <class R> R light_pick_prob(const oracle_scene* s, uint32_t code, V3<R> x) {
+// Probability that the light-tree walk from x (normal n) picks the light of
+// `code` (the products of the sampling walk in nee_term).
+template <class R> R light_pick_prob(const oracle_scene* s, uint32_t code, V3<R> x, V3<R> n) {
     const uint32_t levels = code >> 27;
     uint32_t k = 0;
     R pick = R(1);
     for (uint32_t lv = 0; lv < levels; ++lv) {
         const oracle_scene::LightNode& nd = s->light_tree[k];
-        const R wl = light_importance<R>(nd, 0, x), wr = light_importance<R>(nd, 1, x);
+        const R wl = light_importance<R>(nd, 0, x, n), wr = light_importance<R>(nd, 1, x, n);
         const R pl = wl / (wl + wr);
         if (!(pl >= R(0) && pl <= R(1))) return R(0);
         const bool right = (code >> lv) & 1u;
@@ -673,7 +687,7 @@ template <class R> bool nee_term(const oracle_scene* s, V3<R> no, V3<R> n_o, V3<
     R pick = R(1);
     for (int level = 0; level < 64; ++level) {
         const oracle_scene::LightNode& nd = s->light_tree[k];
-        const R wl = light_importance<R>(nd, 0, no), wr = light_importance<R>(nd, 1, no);
+        const R wl = light_importance<R>(nd, 0, no, n_o), wr = light_importance<R>(nd, 1, no, n_o);
         const R pl = wl / (wl + wr);
         if (!(pl >= R(0) && pl <= R(1))) return false;
         const R ul = next_rand<R>(rng);
@@ -733,6 +747,7 @@ template <class R> V3<R> trace_path(const oracle_scene* s, const solrt_render_pa
     const bool nee = p->integrator == SOLRT_INTEGRATOR_PATH_NEE;
     V3<R> nee_sum{R(0), R(0), R(0)};  // shadow terms in bounce order, then the path's end
     R pdf_prev = R(0);                 // solid-angle pdf of the current ray's BSDF sample
+    V3<R> n_prev{R(0), R(0), R(0)};    // oriented normal of the vertex it left
     for (;;) {
         const HitR<R> h = closest_hit<R>(s, o, d, tmin, tmax, 1, cn.fb, cn.nv, cn.nt);
         ++cn.seg;
@@ -753,7 +768,7 @@ template <class R> V3<R> trace_path(const oracle_scene* s, const solrt_render_pa
                     const V3<R> ng{e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x};
                     const R a2 = length(ng);
                     const R cy = std::abs(dot(ng, d)) / a2;
-                    const R pick = light_pick_prob<R>(s, code, o);
+                    const R pick = light_pick_prob<R>(s, code, o, n_prev);
                     pl = (pick * (h.t * h.t)) / ((R(0.5f) * a2) * cy);
                 }
                 acc = acc * mis_weight<R>(pdf_prev, pl);
@@ -779,6 +794,7 @@ template <class R> V3<R> trace_path(const oracle_scene* s, const solrt_render_pa
             d = sample_cosine(n_o, xi0, xi1);
             hv = base * vcol;
             pdf_prev = dot(n_o, d) / R(3.14159265f);
+            n_prev = n_o;
         } else if (rnd < R(m.metallic)) {
             d = sample_ggx(reflect(d, n_o), xi0, xi1, alpha2);
             hv = base * vcol;

@@ -97,7 +97,7 @@ struct PathQueue {
     float4* d_tmax;   // direction, tmax
     float4* thr_rng;  // throughput, rng state (bits)
     uint2* meta;      // slot within the pass, job << kDepthBits | depth
-    float* pdf;       // SOLRT_INTEGRATOR_PATH_NEE: solid-angle pdf of the direction's BSDF sample
+    float4* prev;     // SOLRT_INTEGRATOR_PATH_NEE: normal of the vertex the ray left, pdf of its BSDF sample
 };
 
 // One job of a wavefront batch, as the device sees it.
@@ -187,7 +187,7 @@ struct Context {
     // queues 0 and 1: paths of alternate bounces; queue 2: shadow rays of
     // SOLRT_INTEGRATOR_PATH_NEE (allocated when a render first needs it)
     DeviceBuffer q_o[3], q_d[3], q_thr[3], q_meta[3];
-    DeviceBuffer q_pdf[2];  // per path of queues 0 and 1, next-event estimation only
+    DeviceBuffer q_prev[2];  // per path of queues 0 and 1, next-event estimation only
     DeviceBuffer hits, rad, ctl, stats, trace_work;
     DeviceBuffer blue_noise;  // RGBA8 texels of SOLRT_INTEGRATOR_AO
     DeviceBuffer sibling_job;  // one-job table of DEBUG / AO launches
@@ -236,7 +236,7 @@ struct Context {
     }
     PathQueue queue(int i) const {
         return PathQueue{q_o[i].as<float4>(), q_d[i].as<float4>(), q_thr[i].as<float4>(), q_meta[i].as<uint2>(),
-                         i < 2 ? q_pdf[i].as<float>() : nullptr};
+                         i < 2 ? q_prev[i].as<float4>() : nullptr};
     }
 };
 

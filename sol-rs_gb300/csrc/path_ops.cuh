@@ -64,17 +64,18 @@ SOLRT_D void hit_frame(const DevScene& sc, uint4 ti, float b0, float b1, float b
 // and pathtrace.rgen:77-84). h = (t, prim bits, u, v). Updates the path
 // throughput `acc`, the rng state and the depth; returns true when the path
 // continues with the ray (o_next, d_next).
-SOLRT_D float light_pick_prob(const DevScene& sc, uint32_t code, f3 x);
+SOLRT_D float light_pick_prob(const DevScene& sc, uint32_t code, f3 x, f3 n);
 SOLRT_D float mis_weight(float p_this, float p_other);
 
 // With SOLRT_INTEGRATOR_PATH_NEE an emitter hit after a bounce is weighted
-// by the power heuristic against next-event estimation (`pdf_prev`: the
-// solid-angle pdf of this ray's BSDF sample); `n_out` and `pdf_out`, when
-// given, receive the oriented shading normal of a continuing path and the
-// pdf of its new direction.
+// by the power heuristic against next-event estimation (`prev`: oriented
+// normal of the vertex this ray left and the solid-angle pdf of its BSDF
+// sample); `n_out` and `prev_out`, when given, receive the oriented shading
+// normal of a continuing path and (that normal, the pdf of its new
+// direction).
 SOLRT_D bool shade_step(const DevJob& J, float4 o, float4 d, float4 h, f3& acc, uint32_t& rng, uint32_t& depth,
-                        float4& o_next, float4& d_next, uint32_t& ef, f3* n_out = nullptr, float pdf_prev = 0.0f,
-                        float* pdf_out = nullptr) {
+                        float4& o_next, float4& d_next, uint32_t& ef, f3* n_out = nullptr,
+                        float4 prev = make_float4(0.0f, 0.0f, 0.0f, 0.0f), float4* prev_out = nullptr) {
     const DevScene& sc = J.sc;
     const f3 dir{d.x, d.y, d.z};
     const uint32_t prim = __float_as_uint(h.y);
@@ -101,10 +102,10 @@ SOLRT_D bool shade_step(const DevJob& J, float4 o, float4 d, float4 h, f3& acc, 
                 const f3 ng{e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x};
                 const float a2 = length(ng);
                 const float cy = fabsf(dot(ng, dir)) / a2;
-                const float pick = light_pick_prob(sc, code, f3{o.x, o.y, o.z});
+                const float pick = light_pick_prob(sc, code, f3{o.x, o.y, o.z}, f3{prev.x, prev.y, prev.z});
                 pl = (pick * (h.x * h.x)) / ((0.5f * a2) * cy);
             }
-            acc = acc * mis_weight(pdf_prev, pl);
+            acc = acc * mis_weight(prev.w, pl);
         }
         return false;
     }
@@ -148,27 +149,44 @@ SOLRT_D bool shade_step(const DevJob& J, float4 o, float4 d, float4 h, f3& acc, 
     o_next = make_float4(no.x, no.y, no.z, o.w);
     d_next = make_float4(nd.x, nd.y, nd.z, d.w);
     if (n_out) *n_out = n_o;
-    if (pdf_out) *pdf_out = dot(n_o, nd) / 3.14159265f;
+    if (prev_out) *prev_out = make_float4(n_o.x, n_o.y, n_o.z, dot(n_o, nd) / 3.14159265f);
     return true;
 }
 
-// Importance of a light-tree child seen from x: power / max(d^2, r^2), d the
-// distance to the child's box centre, r its half-diagonal (s = (centre, r^2)).
-SOLRT_D float light_importance(float4 s, float power, f3 x) {
+// Importance of a light-tree child seen from x with normal n:
+// power * cos_bound / max(d^2, r^2), d the distance to the child's box
+// centre, r its half-diagonal (s = (centre, r^2)), cos_bound the largest
+// cosine between n and a direction into the child's bounding sphere:
+// 1 when the angle theta to the centre is within the sphere's half-angle
+// beta (sin beta = r / d), else max(0, cos(theta - beta)) =
+// max(0, cos theta cos beta + sin theta sin beta). Square roots only, so
+// the host and the device agree bit for bit.
+SOLRT_D float light_importance(float4 s, float power, f3 x, f3 n) {
     const f3 dv{s.x - x.x, s.y - x.y, s.z - x.z};
-    return power / glsl_max(dot(dv, dv), s.w);
+    const float d2 = dot(dv, dv);
+    float cb = 1.0f;
+    if (d2 > s.w) {
+        const float ct = dot(n, dv) / sqrtf(d2);
+        const float sb2 = s.w / d2;
+        const float cbeta = sqrtf(1.0f - sb2);
+        if (ct < cbeta) {
+            const float st = sqrtf(glsl_max(1.0f - ct * ct, 0.0f));
+            cb = glsl_max(ct * cbeta + st * sqrtf(sb2), 0.0f);
+        }
+    }
+    return (power * cb) / glsl_max(d2, s.w);
 }
 
-// Probability that the light-tree walk from x picks the light of `code`
-// (the same products as the sampling walk of nee_sample).
-SOLRT_D float light_pick_prob(const DevScene& sc, uint32_t code, f3 x) {
+// Probability that the light-tree walk from x (normal n) picks the light of
+// `code` (the same products as the sampling walk of nee_sample).
+SOLRT_D float light_pick_prob(const DevScene& sc, uint32_t code, f3 x, f3 n) {
     const uint32_t levels = code >> 27;
     uint32_t k = 0;
     float pick = 1.0f;
     for (uint32_t lv = 0; lv < levels; ++lv) {
         const float4* nd = sc.lights + 3 * (size_t)k;
         const float4 sl = __ldg(nd), sr = __ldg(nd + 1), pc = __ldg(nd + 2);
-        const float wl = light_importance(sl, pc.x, x), wr = light_importance(sr, pc.y, x);
+        const float wl = light_importance(sl, pc.x, x, n), wr = light_importance(sr, pc.y, x, n);
         const float pl = wl / (wl + wr);
         if (!(pl >= 0.0f && pl <= 1.0f)) return 0.0f;
         const bool right = (code >> lv) & 1u;
@@ -213,7 +231,7 @@ SOLRT_D bool nee_sample(const DevScene& sc, f3 no, f3 n_o, f3 thr, float tmin, u
     for (int level = 0; level < 64; ++level) {
         const float4* nd = sc.lights + 3 * (size_t)k;
         const float4 sl = __ldg(nd), sr = __ldg(nd + 1), pc = __ldg(nd + 2);
-        const float wl = light_importance(sl, pc.x, no), wr = light_importance(sr, pc.y, no);
+        const float wl = light_importance(sl, pc.x, no, n_o), wr = light_importance(sr, pc.y, no, n_o);
         const float pl = wl / (wl + wr);
         if (!(pl >= 0.0f && pl <= 1.0f)) return false;
         const float ul = next_rand(rng);

@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(256) k_shade(const DevJob* __restrict__ jobs, 
         bool alive = false, shadow = false;
         float4 out_o = make_float4(0, 0, 0, 0), out_d = make_float4(0, 0, 0, 0), out_t = make_float4(0, 0, 0, 0);
         float4 s_o = make_float4(0, 0, 0, 0), s_d = make_float4(0, 0, 0, 0), s_c = make_float4(0, 0, 0, 0);
-        float out_pdf = 0.0f;
+        float4 out_prev = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         bool out_nee = false;
         uint2 m = make_uint2(0, 0);
         if (i < n) {
@@ -100,8 +100,8 @@ __global__ void __launch_bounds__(256) k_shade(const DevJob* __restrict__ jobs, 
             uint32_t depth = m.y & kDepthMask;
             f3 acc{tr.x, tr.y, tr.z};
             f3 n_o{0.0f, 0.0f, 0.0f};
-            const float pdf_prev = nee && depth > 0u ? qin.pdf[i] : 0.0f;
-            if (shade_step(J, o, d, hits[i], acc, rng, depth, out_o, out_d, ef, &n_o, pdf_prev, &out_pdf)) {
+            const float4 prev = nee && depth > 0u ? qin.prev[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (shade_step(J, o, d, hits[i], acc, rng, depth, out_o, out_d, ef, &n_o, prev, &out_prev)) {
                 alive = true;
                 if (nee) {
                     out_nee = true;
@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(256) k_shade(const DevJob* __restrict__ jobs, 
                     qout.d_tmax[pos] = out_d;
                     qout.thr_rng[pos] = out_t;
                     qout.meta[pos] = m;
-                    if (out_nee) qout.pdf[pos] = out_pdf;
+                    if (out_nee) qout.prev[pos] = out_prev;
                 } else {
                     ef |= SOLRT_EFLAG_QUEUE;
                 }
@@ -909,8 +909,8 @@ solrt_status ensure_shadow_queue(Context& ctx) {
     SOLRT_TRY(ctx.q_d[2].alloc(16 * C));
     SOLRT_TRY(ctx.q_thr[2].alloc(16 * C));
     SOLRT_TRY(ctx.q_meta[2].alloc(8 * C));
-    SOLRT_TRY(ctx.q_pdf[0].alloc(4 * C));
-    SOLRT_TRY(ctx.q_pdf[1].alloc(4 * C));
+    SOLRT_TRY(ctx.q_prev[0].alloc(16 * C));
+    SOLRT_TRY(ctx.q_prev[1].alloc(16 * C));
     return SOLRT_OK;
 }
 
