@@ -67,12 +67,14 @@ SOLRT_D void hit_frame(const DevScene& sc, uint4 ti, float b0, float b1, float b
 SOLRT_D float light_pick_prob(const DevScene& sc, uint32_t code, f3 x, f3 n);
 SOLRT_D float mis_weight(float p_this, float p_other);
 
-// With SOLRT_INTEGRATOR_PATH_NEE an emitter hit after a bounce is weighted
+// kNee (jobs of SOLRT_INTEGRATOR_PATH_NEE; compiled out otherwise): an
+// emitter hit after a bounce is weighted
 // by the power heuristic against next-event estimation (`prev`: oriented
 // normal of the vertex this ray left and the solid-angle pdf of its BSDF
 // sample); `n_out` and `prev_out`, when given, receive the oriented shading
 // normal of a continuing path and (that normal, the pdf of its new
 // direction).
+template <bool kNee = false>
 SOLRT_D bool shade_step(const DevJob& J, float4 o, float4 d, float4 h, f3& acc, uint32_t& rng, uint32_t& depth,
                         float4& o_next, float4& d_next, uint32_t& ef, f3* n_out = nullptr,
                         float4 prev = make_float4(0.0f, 0.0f, 0.0f, 0.0f), float4* prev_out = nullptr) {
@@ -91,7 +93,7 @@ SOLRT_D bool shade_step(const DevJob& J, float4 o, float4 d, float4 h, f3& acc, 
     const float4 m2 = __ldg(sc.materials + 3 * mat + 2);
     if (m1.x >= 1.0f || m1.y >= 1.0f || m1.z >= 1.0f) {                      // rchit:75-80
         acc = acc * f3{m1.x, m1.y, m1.z};
-        if (J.integrator == SOLRT_INTEGRATOR_PATH_NEE && depth > 0u) {
+        if (kNee && J.integrator == SOLRT_INTEGRATOR_PATH_NEE && depth > 0u) {
             // the light pdf of this hit: pick probability from the ray's
             // origin times distance^2 / (area cos_y)
             const uint32_t code = sc.tri_light ? __ldg(sc.tri_light + prim) : ~0u;
@@ -148,8 +150,8 @@ SOLRT_D bool shade_step(const DevJob& J, float4 o, float4 d, float4 h, f3& acc, 
     }
     o_next = make_float4(no.x, no.y, no.z, o.w);
     d_next = make_float4(nd.x, nd.y, nd.z, d.w);
-    if (n_out) *n_out = n_o;
-    if (prev_out) *prev_out = make_float4(n_o.x, n_o.y, n_o.z, dot(n_o, nd) / 3.14159265f);
+    if (kNee && n_out) *n_out = n_o;
+    if (kNee && prev_out) *prev_out = make_float4(n_o.x, n_o.y, n_o.z, dot(n_o, nd) / 3.14159265f);
     return true;
 }
 

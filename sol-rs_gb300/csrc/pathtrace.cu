@@ -70,6 +70,9 @@ __global__ void k_generate(const DevJob* __restrict__ jobs, const DevItem* __res
     if (J.integrator == SOLRT_INTEGRATOR_PATH_NEE) rad[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // sums shadow terms
 }
 
+// kNee: the variant for passes with SOLRT_INTEGRATOR_PATH_NEE jobs (shadow
+// queue, MIS state); plain passes run the variant without that code.
+template <bool kNee>
 __global__ void __launch_bounds__(256) k_shade(const DevJob* __restrict__ jobs, const DevItem* __restrict__ items,
                                                uint32_t nitems, PathQueue qin, const float4* __restrict__ hits,
                                                const unsigned int* __restrict__ count_in, PathQueue qout,
@@ -95,13 +98,13 @@ __global__ void __launch_bounds__(256) k_shade(const DevJob* __restrict__ jobs, 
             m = qin.meta[i];
             const uint32_t job = m.y >> kDepthBits;
             const DevJob& J = jobs[job];
-            const bool nee = J.integrator == SOLRT_INTEGRATOR_PATH_NEE && qs.o_tmin != nullptr;
+            const bool nee = kNee && J.integrator == SOLRT_INTEGRATOR_PATH_NEE && qs.o_tmin != nullptr;
             uint32_t rng = __float_as_uint(tr.w);
             uint32_t depth = m.y & kDepthMask;
             f3 acc{tr.x, tr.y, tr.z};
             f3 n_o{0.0f, 0.0f, 0.0f};
             const float4 prev = nee && depth > 0u ? qin.prev[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            if (shade_step(J, o, d, hits[i], acc, rng, depth, out_o, out_d, ef, &n_o, prev, &out_prev)) {
+            if (shade_step<kNee>(J, o, d, hits[i], acc, rng, depth, out_o, out_d, ef, &n_o, prev, &out_prev)) {
                 alive = true;
                 if (nee) {
                     out_nee = true;
@@ -143,7 +146,7 @@ __global__ void __launch_bounds__(256) k_shade(const DevJob* __restrict__ jobs, 
                 }
             }
         }
-        const uint32_t smask = __ballot_sync(0xffffffffu, shadow);
+        const uint32_t smask = kNee ? __ballot_sync(0xffffffffu, shadow) : 0u;
         if (smask) {
             const int leader = __ffs(smask) - 1;
             uint32_t pos0 = 0;
@@ -586,9 +589,14 @@ solrt_status issue_pass(Context& ctx, uint32_t kind, const DevJob* dj, const Dev
         SOLRT_TRY(launch_extend(ctx, kind, dj, qin, ctx.hits.as<float4>(), ctl->count + bnc, ctl->work + bnc));
         ctx.timing_end(te);
         const int ts = record_timing ? ctx.timing_begin(1) : -1;
-        k_shade<<<shade_grid, 256, 0, st>>>(dj, items, pp.item_count, qin, ctx.hits.as<float4>(), ctl->count + bnc,
-                                            qout, ctl->count + bnc + 1, ctx.capacity, ctx.rad.as<float4>(), stats,
-                                            pp.nee ? ctx.queue(2) : PathQueue{}, ctl->scount + bnc);
+        if (pp.nee)
+            k_shade<true><<<shade_grid, 256, 0, st>>>(dj, items, pp.item_count, qin, ctx.hits.as<float4>(),
+                                                      ctl->count + bnc, qout, ctl->count + bnc + 1, ctx.capacity,
+                                                      ctx.rad.as<float4>(), stats, ctx.queue(2), ctl->scount + bnc);
+        else
+            k_shade<false><<<shade_grid, 256, 0, st>>>(dj, items, pp.item_count, qin, ctx.hits.as<float4>(),
+                                                       ctl->count + bnc, qout, ctl->count + bnc + 1, ctx.capacity,
+                                                       ctx.rad.as<float4>(), stats, PathQueue{}, ctl->scount + bnc);
         ctx.timing_end(ts);
         ++ctx.launches;
         if (pp.nee && bnc + 1 < pp.bounces) {  // shadow rays of this bounce (none at the last: depth > max)
