@@ -611,6 +611,8 @@ def main():
     ap.add_argument("--width", type=int, default=0, help="override the workload's image width (profiling runs)")
     ap.add_argument("--height", type=int, default=0, help="override the workload's image height")
     ap.add_argument("--spp", type=int, default=0, help="override the workload's samples per pixel")
+    ap.add_argument("--capacity", type=int, default=0,
+                    help="paths per pass of the timed context (0 = library default; small profiler captures)")
     args = ap.parse_args()
     world, rank, local, pg = dist_setup(args)
     if args.impl == "reference":
@@ -647,7 +649,7 @@ def main():
     W, H = kw["width"], kw["height"]
 
     # visit counts per segment (one counting launch at reduced spp)
-    with solrt.Context(local, enable_counters=True) as cctx:
+    with solrt.Context(local, enable_counters=True, path_capacity=args.capacity) as cctx:
         csc = solrt.SceneDescription(cctx, data, bvh=bvh, sah=args.sah)
         cimg = solrt.Image(cctx, W, H, kw["accum_mode"])
         cctx.reset_stats()
@@ -660,7 +662,7 @@ def main():
         cimg.close()
         csc.close()
 
-    ctx = solrt.Context(local, enable_timing=True)
+    ctx = solrt.Context(local, enable_timing=True, path_capacity=args.capacity)
     sc = solrt.SceneDescription(ctx, data, bvh=bvh, sah=args.sah)
     info = sc.bvh_info()
     img = solrt.Image(ctx, W, H, kw["accum_mode"])
