@@ -191,22 +191,26 @@ uint32_t expand10(uint32_t v) {
     return v;
 }
 
-std::vector<float4> build_light_tree(const std::vector<float4>& pos, const std::vector<uint4>& tri,
-                                     const std::vector<uint32_t>& sec_mat, const solrt_material* mats,
-                                     uint32_t& count, std::vector<uint32_t>& tri_code) {
+// Tree over the candidates (emissive triangles in triangle order: their
+// index and (v0, v1, v2, section)) at world positions `pos`; `tri_code`
+// gets one code per triangle of the scene (`tri_count`).
+std::vector<float4> build_light_tree(const std::vector<float4>& pos, const std::vector<uint32_t>& cand_prim,
+                                     const std::vector<uint4>& cand_tri, const std::vector<uint32_t>& sec_mat,
+                                     const std::vector<solrt_material>& mats, size_t tri_count, uint32_t& count,
+                                     std::vector<uint32_t>& tri_code) {
     LightBuild lb;
     std::vector<float> cen;
-    for (size_t t = 0; t < tri.size(); ++t) {
-        const solrt_material& m = mats[sec_mat[tri[t].w]];
-        if (!(m.emissive[0] >= 1.0f || m.emissive[1] >= 1.0f || m.emissive[2] >= 1.0f)) continue;
-        const float4 a = pos[tri[t].x], b = pos[tri[t].y], c = pos[tri[t].z];
+    for (size_t ci = 0; ci < cand_tri.size(); ++ci) {
+        const uint4 tr = cand_tri[ci];
+        const solrt_material& m = mats[sec_mat[tr.w]];
+        const float4 a = pos[tr.x], b = pos[tr.y], c = pos[tr.z];
         const float e1x = b.x - a.x, e1y = b.y - a.y, e1z = b.z - a.z;
         const float e2x = c.x - a.x, e2y = c.y - a.y, e2z = c.z - a.z;
         const float nx = e1y * e2z - e1z * e2y, ny = e1z * e2x - e1x * e2z, nz = e1x * e2y - e1y * e2x;
         const float area = 0.5f * std::sqrt((nx * nx + ny * ny) + nz * nz);
         const float pw = area * ((m.emissive[0] + m.emissive[1]) + m.emissive[2]);
         if (!(area > 0.0f) || !(pw > 0.0f) || !std::isfinite(pw)) continue;
-        lb.prim.push_back((uint32_t)t);
+        lb.prim.push_back(cand_prim[ci]);
         const float v[3][3] = {{a.x, a.y, a.z}, {b.x, b.y, b.z}, {c.x, c.y, c.z}};
         for (int k = 0; k < 3; ++k) {
             lb.lo.push_back(std::min(std::min(v[0][k], v[1][k]), v[2][k]));
@@ -217,6 +221,7 @@ std::vector<float4> build_light_tree(const std::vector<float4>& pos, const std::
     }
     const uint32_t n = std::min<uint32_t>((uint32_t)lb.prim.size(), 1u << 26);  // codes hold 27 levels
     count = n;
+    tri_code.assign(tri_count, ~0u);
     if (n == 0) return {};
     lb.code.assign(n, 0u);
     float cmin[3] = {cen[0], cen[1], cen[2]}, cmax[3] = {cen[0], cen[1], cen[2]};
@@ -247,12 +252,41 @@ std::vector<float4> build_light_tree(const std::vector<float4>& pos, const std::
         lb.nodes = {sp, sp, make_float4(pw, 0.0f, LightBuild::as_float(root), LightBuild::as_float(root))};
         lb.code[0] = 1u << 27;
     }
-    tri_code.assign(tri.size(), ~0u);
+    tri_code.assign(tri_count, ~0u);
     for (uint32_t k = 0; k < n; ++k) tri_code[lb.prim[k]] = lb.code[k];
     return lb.nodes;
 }
 
 }  // namespace
+
+solrt_status upload_light_tree(Scene& sc, const std::vector<float4>& pos, cudaStream_t st) {
+    uint32_t count = 0;
+    std::vector<uint32_t> tri_code;
+    const std::vector<float4> nodes = build_light_tree(pos, sc.light_cand_prim, sc.light_cand_tri, sc.light_sec_mat,
+                                                       sc.light_mats, sc.tri_count, count, tri_code);
+    if (cudaMemcpyAsync(sc.tri_light.ptr, tri_code.data(), 4 * tri_code.size(), cudaMemcpyHostToDevice, st) !=
+            cudaSuccess ||
+        (!nodes.empty() && cudaMemcpyAsync(sc.lights.ptr, nodes.data(), sizeof(float4) * nodes.size(),
+                                           cudaMemcpyHostToDevice, st) != cudaSuccess) ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+        set_error("light tree upload failed");
+        return SOLRT_ERR_DEVICE;
+    }
+    sc.light_count = count;
+    return SOLRT_OK;
+}
+
+// Rebuilds the light tree from the scene's current world vertices (after
+// instances moved), as a fresh scene with those positions would build it.
+solrt_status refresh_light_tree(Context& ctx, Scene& sc) {
+    if (sc.light_cand_prim.empty()) return SOLRT_OK;
+    std::vector<float4> pos(sc.vertex_count);
+    SOLRT_CUDA(cudaMemcpyAsync(pos.data(), sc.vpos.ptr, sizeof(float4) * pos.size(), cudaMemcpyDeviceToHost,
+                               ctx.stream));
+    SOLRT_CUDA(cudaStreamSynchronize(ctx.stream));
+    return upload_light_tree(sc, pos, ctx.stream);
+}
+
 }  // namespace solrt
 
 using namespace solrt;
@@ -561,25 +595,24 @@ solrt_status solrt_scene_create(solrt_context* ctx, const solrt_scene_desc* d, c
         set_error("scene upload failed");
         return fail(SOLRT_ERR_DEVICE);
     }
-    // light tree of next-event estimation (world positions at creation)
-    uint32_t light_count = 0;
-    std::vector<uint32_t> tri_code;
-    const std::vector<float4> lights = build_light_tree(pos, tri, sec_mat, d->materials, light_count, tri_code);
-    if (!lights.empty()) {
-        if ((s = sc->tri_light.alloc(4 * tri_code.size())) != SOLRT_OK) return fail(s);
-        if (cudaMemcpyAsync(sc->tri_light.ptr, tri_code.data(), 4 * tri_code.size(), cudaMemcpyHostToDevice, st) !=
-            cudaSuccess) {
-            set_error("scene upload failed");
-            return fail(SOLRT_ERR_DEVICE);
-        }
-        if ((s = sc->lights.alloc(sizeof(float4) * lights.size())) != SOLRT_OK) return fail(s);
-        if (cudaMemcpyAsync(sc->lights.ptr, lights.data(), sizeof(float4) * lights.size(), cudaMemcpyHostToDevice,
-                            st) != cudaSuccess) {
-            set_error("scene upload failed");
-            return fail(SOLRT_ERR_DEVICE);
+    // light tree of next-event estimation over the emissive triangles (world
+    // positions at creation; rebuilt by solrt_scene_regenerate), buffers
+    // sized for every candidate so that rebuilds keep their addresses
+    for (uint64_t t = 0; t < nt; ++t) {
+        const solrt_material& m = d->materials[sec_mat[tri[t].w]];
+        if (m.emissive[0] >= 1.0f || m.emissive[1] >= 1.0f || m.emissive[2] >= 1.0f) {
+            sc->light_cand_prim.push_back((uint32_t)t);
+            sc->light_cand_tri.push_back(tri[t]);
         }
     }
-    sc->light_count = light_count;
+    if (!sc->light_cand_prim.empty()) {
+        sc->light_sec_mat = sec_mat;
+        sc->light_mats.assign(d->materials, d->materials + d->material_count);
+        if ((s = sc->tri_light.alloc(4 * (size_t)nt)) != SOLRT_OK ||
+            (s = sc->lights.alloc(3 * sizeof(float4) * sc->light_cand_prim.size())) != SOLRT_OK)
+            return fail(s);
+        if ((s = upload_light_tree(*sc, pos, st)) != SOLRT_OK) return fail(s);
+    }
     sc->section_count = d->section_count;
     sc->sec_tri_first = std::move(sec_first);
     sc->sec_tri_count = std::move(sec_count);
@@ -686,7 +719,8 @@ solrt_status solrt_scene_regenerate(solrt_scene* scene, uint32_t mode) {
     CHECK_ARG(scene->dynamic, "scene was not created with SOLRT_BVH_DYNAMIC");
     CHECK_ARG(mode == SOLRT_REGEN_REBUILD || mode == SOLRT_REGEN_REFIT, "unknown regenerate mode");
     SOLRT_CUDA(cudaSetDevice(scene->ctx->device));
-    return regenerate_scene(*scene->ctx, *scene, mode);
+    SOLRT_TRY(regenerate_scene(*scene->ctx, *scene, mode));
+    return refresh_light_tree(*scene->ctx, *scene);
 }
 
 solrt_status solrt_camera_look_at(const float eye[3], const float center[3], const float up[3], float vfov_deg,

@@ -274,8 +274,14 @@ struct Scene {
     uint32_t blas_depth = 0, tlas_count = 0, tlas_depth = 0;
     DeviceBuffer tlas, inst_table;
     // light tree of next-event estimation (see DevScene::lights), built at
-    // creation, and per triangle its light-tree code (DevScene::tri_light)
+    // creation and by regenerate, and per triangle its light-tree code
+    // (DevScene::tri_light); host copies of the candidates (emissive
+    // triangles) and of what their power needs
     DeviceBuffer lights, tri_light;
+    std::vector<uint32_t> light_cand_prim;
+    std::vector<uint4> light_cand_tri;
+    std::vector<uint32_t> light_sec_mat;
+    std::vector<solrt_material> light_mats;
     uint32_t light_count = 0;
     DevScene view() const {
         DevScene d;
@@ -344,6 +350,10 @@ DevJob job_for(const Scene& sc, const Image& img, const solrt_camera& cam, const
 solrt_status check_job(const Context& ctx, const Scene& sc, const Image& img, const solrt_render_params& p);
 // Allocates the shadow-ray queue of SOLRT_INTEGRATOR_PATH_NEE (no-op once done).
 solrt_status ensure_shadow_queue(Context& ctx);
+// api.cpp: light tree of next-event estimation from world positions `pos`
+// (upload_light_tree) or from the scene's current vertices (refresh).
+solrt_status upload_light_tree(Scene& sc, const std::vector<float4>& pos, cudaStream_t st);
+solrt_status refresh_light_tree(Context& ctx, Scene& sc);
 solrt_status debug_unit(Context& ctx, uint32_t op, uint32_t n, const uint32_t* a, const uint32_t* b,
                         const float* in_f32, uint32_t* out_u32, float* out_f32);
 

@@ -40,16 +40,20 @@ def _render(solrt, ctx, sc, cam, w, h, p):
     return img.read()[0]
 
 
+@pytest.mark.parametrize("integ", ["path", "nee"])
 @pytest.mark.parametrize("mode", ["rebuild", "refit"])
 @pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh2t", "bvh4", "bvh8", "bvh8f"])
-def test_regenerate_matches_fresh_scene(solrt, oracle, ctx, bvh, mode):
+def test_regenerate_matches_fresh_scene(solrt, oracle, ctx, bvh, mode, integ):
+    """nee: the light tree of next-event estimation is rebuilt from the moved
+    vertices, as a fresh scene builds it (the light section moves too)."""
     kind = bvh_kind(solrt, bvh)
     regen = solrt.REGEN_REBUILD if mode == "rebuild" else solrt.REGEN_REFIT
     base = S.cornell()
     w, h = 32, 32
     cam = camera_of(base, 1.0)
     p = solrt.render_params(w, h, spp=2, max_bounces=4, material_mode=solrt.MATERIAL_LAMBERT,
-                            rng_mode=solrt.RNG_PER_SAMPLE, seed=9)
+                            rng_mode=solrt.RNG_PER_SAMPLE, seed=9,
+                            integrator=solrt.INTEGRATOR_PATH_NEE if integ == "nee" else solrt.INTEGRATOR_PATH)
     dyn = solrt.SceneDescription(ctx, base, bvh=kind, dynamic=True)
     rays = random_rays(4000, -0.2, 1.2, seed=21)
     for f, transforms in enumerate(_frames(len(base.sections))):
