@@ -598,6 +598,8 @@ def main():
     ap.add_argument("--workload", default="soup", choices=["soup", "cornell", "tunnel", "instances", "batch", "serve"])
     ap.add_argument("--bvh", default="bvh2", choices=["bvh2", "bvh2q", "bvh2t", "bvh4", "bvh8", "bvh8f"])
     ap.add_argument("--sah", action="store_true", help="wide BVH kinds: SAH-optimal collapse")
+    ap.add_argument("--kernel", default="wavefront", choices=["wavefront", "mega"],
+                    help="mega: the plain per-pixel kernel (the reference's loop structure) on the same workload")
     ap.add_argument("--nee", action="store_true",
                     help="next-event estimation (shadow-ray queue); shadow rays are reported apart from the metric")
     ap.add_argument("--jobs", type=int, default=256)
@@ -634,6 +636,9 @@ def main():
     b.build_lib()
     solrt = importlib.import_module("sol-rs_gb300")
     data, kw, cfg = workload(args.workload)
+    if args.kernel == "mega":
+        kw["kernel"] = solrt.KERNEL_MEGA
+        cfg = dict(cfg, kernel="plain per-pixel megakernel (one thread loops samples and bounces)")
     if args.nee:
         kw["integrator"] = solrt.INTEGRATOR_PATH_NEE
         cfg = dict(cfg, integrator="path tracing + next-event estimation (shadow-ray queue)")
@@ -653,7 +658,10 @@ def main():
         csc = solrt.SceneDescription(cctx, data, bvh=bvh, sah=args.sah)
         cimg = solrt.Image(cctx, W, H, kw["accum_mode"])
         cctx.reset_stats()
-        solrt.Renderer(cctx).cmd_trace_rays(csc, cam, solrt.render_params(**dict(kw, spp=min(4, kw["spp"]))), cimg)
+        # (the wavefront kernel counts visits; the megakernel's plain depth-first
+        # loop visits the same nodes less the speculative ones)
+        solrt.Renderer(cctx).cmd_trace_rays(csc, cam, solrt.render_params(
+            **dict(kw, spp=min(4, kw["spp"]), kernel=solrt.KERNEL_WAVEFRONT)), cimg)
         cctx.synchronize()
         cs = cctx.stats()
         nodes_per_seg = cs.node_visits / max(cs.segments, 1)
@@ -744,6 +752,8 @@ def main():
     peak, peak_kind = peaks()
     b_seg = 32 + 16 + NODE_BYTES[info.kind] * nodes_per_seg + 48 * tris_per_seg
     ext_s = st.extend_ms / 1000.0
+    if args.kernel == "mega":  # traversal and shading in one launch: the whole render time
+        ext_s = ms / 1000.0
     # extend launches also trace the shadow rays of --nee (same bytes per ray assumed)
     achieved = ((st.segments + st.shadow_segments) * b_seg) / ext_s / 1e9 if ext_s > 0 else 0.0
     traffic = None
@@ -755,7 +765,8 @@ def main():
                 "traffic_note": "DRAM bytes per launch from an ncu capture of this workload (62.8 B per segment); "
                                 "the algorithmic bytes are mostly served by L1 / L2" if traffic else None,
                 "peak_source": peak_kind + " (MEASURED_PEAKS hbm_gbs)",
-                "kernel": "k_extend (BVH traversal)", "bytes_per_segment": round(b_seg, 1),
+                "kernel": "k_megakernel (traversal + shading, whole render time)" if args.kernel == "mega"
+                          else "k_extend (BVH traversal)", "bytes_per_segment": round(b_seg, 1),
                 "nodes_per_segment": round(nodes_per_seg, 2), "tris_per_segment": round(tris_per_seg, 2),
                 "extend_ms_per_launch": round(st.extend_ms / max(st.extend_launches, 1), 4),
                 "stage_ms_per_step": {"generate": round(st.generate_ms / args.steps, 3),

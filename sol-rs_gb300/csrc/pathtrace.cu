@@ -217,8 +217,16 @@ __global__ void k_accumulate(const DevJob* __restrict__ jobs, const DevItem* __r
 // loops over its samples and their bounces, tracing each segment itself.
 // Same arithmetic as the wavefront stages, so the same image; used as the
 // plain kernel the wavefront and the batched path are measured against.
+// Minimum resident 128-thread blocks per SM asked of the register allocator
+// for the megakernel. 8 (64 registers, ~100 B of spills) against the
+// unconstrained 128 registers: 1099 vs 682 Mrays/s on the 1M-triangle soup
+// (6: 914, 10: 1106, 12: 1062, 16: 890): the per-pixel loop is latency-bound
+// and needs the warps.
+#ifndef SOLRT_MEGA_MINB
+#define SOLRT_MEGA_MINB 8
+#endif
 template <int KIND>
-__global__ void __launch_bounds__(128) k_megakernel(const DevJob* __restrict__ job, DevStats* stats) {
+__global__ void __launch_bounds__(128, SOLRT_MEGA_MINB) k_megakernel(const DevJob* __restrict__ job, DevStats* stats) {
     const DevJob& J = *job;
     const uint32_t npix = J.width * J.height;
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
