@@ -72,8 +72,15 @@ __global__ void k_generate(const DevJob* __restrict__ jobs, const DevItem* __res
 
 // kNee: the variant for passes with SOLRT_INTEGRATOR_PATH_NEE jobs (shadow
 // queue, MIS state); plain passes run the variant without that code.
+// Resident 256-thread shade blocks per SM asked of the register allocator:
+// 4 (64 registers, a few spilled) against 3 at 74 / 96 registers: soup
+// shade 12.92 -> 12.66 ms per frame, next-event-estimation shade on the
+// tunnel 1133 -> 837 ms (its light-tree walk is load-latency bound).
+#ifndef SOLRT_SHADE_MINB
+#define SOLRT_SHADE_MINB 4
+#endif
 template <bool kNee>
-__global__ void __launch_bounds__(256) k_shade(const DevJob* __restrict__ jobs, const DevItem* __restrict__ items,
+__global__ void __launch_bounds__(256, SOLRT_SHADE_MINB) k_shade(const DevJob* __restrict__ jobs, const DevItem* __restrict__ items,
                                                uint32_t nitems, PathQueue qin, const float4* __restrict__ hits,
                                                const unsigned int* __restrict__ count_in, PathQueue qout,
                                                unsigned int* __restrict__ count_out, uint32_t capacity,
