@@ -126,3 +126,20 @@ def test_nee_rejects_unsupported(solrt, ctx):
         srv.submit(sc, cam, solrt.render_params(8, 8, spp=1, integrator=solrt.INTEGRATOR_PATH_NEE,
                                                 material_mode=solrt.MATERIAL_REF))
     srv.close()
+
+
+def test_nee_pass_splitting_invariance(solrt, oracle):
+    """Tiny path capacities force many passes (each with its own shadow
+    queue per bounce); the image must not change and must equal the
+    oracle's."""
+    data, w, h, kw = _case(solrt, "cornell")
+    kw = dict(kw, spp=5)
+    out = []
+    for cap in (0, 1000, 4096 + 7):
+        c = solrt.Context(0, path_capacity=cap)
+        ga, oa, st, (seg, shadow, unocc) = _render_both(solrt, oracle, c, data, w, h, kw, frames=1)
+        assert st.shadow_segments == shadow and st.segments == seg
+        out.append(ga)
+        c.close()
+    assert np.array_equal(out[0], out[1]) and np.array_equal(out[0], out[2])
+    assert np.array_equal(out[0].view(np.uint32), oa.view(np.uint32))
