@@ -80,12 +80,11 @@ __global__ void k_generate(const DevJob* __restrict__ jobs, const DevItem* __res
 #define SOLRT_SHADE_MINB 4
 #endif
 template <bool kNee>
-__global__ void __launch_bounds__(256, SOLRT_SHADE_MINB) k_shade(const DevJob* __restrict__ jobs, const DevItem* __restrict__ items,
-                                               uint32_t nitems, PathQueue qin, const float4* __restrict__ hits,
-                                               const unsigned int* __restrict__ count_in, PathQueue qout,
-                                               unsigned int* __restrict__ count_out, uint32_t capacity,
-                                               float4* __restrict__ rad, DevStats* stats, PathQueue qs,
-                                               unsigned int* __restrict__ count_s) {
+__global__ void __launch_bounds__(256, SOLRT_SHADE_MINB)
+    k_shade(const DevJob* __restrict__ jobs, const DevItem* __restrict__ items, uint32_t nitems, PathQueue qin,
+            const float4* __restrict__ hits, const unsigned int* __restrict__ count_in, PathQueue qout,
+            unsigned int* __restrict__ count_out, uint32_t capacity, float4* __restrict__ rad, DevStats* stats,
+            PathQueue qs, unsigned int* __restrict__ count_s) {
     const unsigned int n = *count_in;
     const int lane = threadIdx.x & 31;
     const uint32_t lane_lt = (1u << lane) - 1u;
