@@ -381,8 +381,15 @@ __global__ void __launch_bounds__(128) k_debug(const DevJob* __restrict__ job, D
 // ao.rgen:37-83, ao.rchit:53-88, ao.rmiss: `spp` jittered samples; each
 // follows cosine-weighted rays (directions from the blue-noise texture)
 // until a miss or max_bounces + 1 hits, counting every hit after the first.
+// Minimum resident 128-thread AO blocks per SM asked of the register
+// allocator: 8 (64 registers) against the unconstrained 96: 1083 vs 801
+// Mrays/s for the AO pipeline on the 1M-triangle soup at 1920x1080 (same
+// image), latency-bound like the megakernel.
+#ifndef SOLRT_AO_MINB
+#define SOLRT_AO_MINB 8
+#endif
 template <int KIND>
-__global__ void __launch_bounds__(128) k_ao(const DevJob* __restrict__ job, DevStats* stats) {
+__global__ void __launch_bounds__(128, SOLRT_AO_MINB) k_ao(const DevJob* __restrict__ job, DevStats* stats) {
     const DevJob& J = *job;
     const uint32_t npix = J.width * J.height;
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
