@@ -36,7 +36,8 @@
 extern "C" {
 #endif
 
-#define SOLRT_ABI_VERSION 1u
+/* 2: solrt_stats gained shadow_segments and shadow_unoccluded. */
+#define SOLRT_ABI_VERSION 2u
 
 typedef enum solrt_status {
     SOLRT_OK = 0,

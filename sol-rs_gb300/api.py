@@ -210,6 +210,7 @@ _PROTOS = {
 }
 
 _lib = None
+ABI_VERSION = 2  # SOLRT_ABI_VERSION of the structs mirrored here
 
 
 def lib():
@@ -223,6 +224,9 @@ def lib():
             fn = getattr(L, name)
             fn.restype = res
             fn.argtypes = args
+        if L.solrt_abi_version() != ABI_VERSION:
+            raise SolrtError(ERR_DEVICE, "libsolrt.so has ABI %d, this binding %d: rebuild it (sol-rs_gb300/build.py)"
+                             % (L.solrt_abi_version(), ABI_VERSION))
         _lib = L
     return _lib
 

@@ -42,7 +42,7 @@ def test_struct_sizes(solrt):
 
 def test_abi_version_and_status_strings(solrt):
     L = solrt.lib()
-    assert L.solrt_abi_version() == 1
+    assert L.solrt_abi_version() == 2
     assert L.solrt_status_string(0) == b"ok"
     assert L.solrt_status_string(5) == b"capacity exceeded"
 
