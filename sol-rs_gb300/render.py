@@ -6,6 +6,7 @@ RGBA8 image to a PNG instead of presenting it:
     python -m sol-rs_gb300.render --model models/tunnel.gltf --sky
     python -m sol-rs_gb300.render --integrator ao --model scene.glb --blue-noise HDR_RGBA_0.png
     python -m sol-rs_gb300.render --integrator debug --scene soup
+    python -m sol-rs_gb300.render --integrator nee --scene tunnel   # next-event estimation, Lambert
 
 --model reads glTF (.gltf / .glb) with its first perspective camera, else
 the default Camera::new (eye (10,10,10), centre 0, up -Y, 35 degrees;
