@@ -628,17 +628,23 @@ solrt_status solrt_gltf_destroy(solrt_gltf* g);
  * exits.
  *
  *   vpos      float4 per vertex (world position in .xyz), 16-byte aligned
- *   tri_idx   uint4 per triangle (v0, v1, v2, material), 16-byte aligned
+ *   tri_idx   uint4 per triangle (v0, v1, v2, material), 16-byte aligned;
+ *             every vertex index must be below the number of float4 in
+ *             vpos (the call takes no vertex count and cannot check them:
+ *             an index past the end makes the build read out of bounds)
  *   nodes     output, 64 * max(tri_count - 1, 1) bytes (BVH2 node layout of
  *             solrt_scene_bvh_export)
  *   tris      output, 48 * tri_count bytes (triangles in leaf order)
  *   stream    cudaStream_t to run on (NULL = the legacy default stream)
  *
  * Work is queued on `stream` and the call returns without waiting. Up to
- * SOLRT_NOALLOC_MAX_TRIS triangles; more returns SOLRT_ERR_CAPACITY. The
- * first call on a device looks up the scratch array's device address
- * (once per device, with that device current), so make that first call
- * before any stream capture. All calls share the one scratch array: calls
+ * SOLRT_NOALLOC_MAX_TRIS triangles; more returns SOLRT_ERR_CAPACITY. Every
+ * call looks up the scratch array's device address in the CUDA context
+ * current at the call (cudaGetSymbolAddress, a host-side query; nothing is
+ * cached, so a context created again after cudaDeviceReset, or a host
+ * application's own context, gets its own address); make the first call
+ * on a device before any stream capture, since that first lookup loads the
+ * library's device code into the context. All calls share the one scratch array: calls
  * whose work overlaps on the GPU (different streams without ordering)
  * race and corrupt each other's result; order them on one stream or with
  * events. The call clears the parts of the scratch that must start at zero,

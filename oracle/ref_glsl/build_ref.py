@@ -3,8 +3,8 @@
 TEST INFRASTRUCTURE ONLY. Reads assets/glsl/sampling.glsl,
 postprocess.glsl, payload.glsl and the ray-tracing shaders of the path
 (pathtrace.rgen / .rchit / .rmiss) and of its sibling pipelines (ao.* and
-debug.*) from the reference checkout (default
-/root/reference, or $SOLRT_REFERENCE), applies a mechanical GLSL -> C++
+debug.*) from the reference checkout (reference_root(): $SOLRT_REFERENCE,
+else the checkout's location on the build machine), applies a mechanical GLSL -> C++
 rewrite and compiles them with glsl_shim.h; ref_glsl.cpp runs the three
 shaders as a ray-tracing pipeline on CPU threads, with traceRayEXT answered
 by a closest-hit function the caller passes in. Everything it writes goes to
@@ -47,6 +47,10 @@ SHADERS = ("sampling.glsl", "postprocess.glsl", "payload.glsl", "pathtrace.rgen"
 
 
 def reference_root():
+    """The reference checkout this recipe reads: $SOLRT_REFERENCE, else its
+    location on the build machine. Tests and the build step take the path
+    from here; where the checkout is absent they skip or fall back to the
+    sources already generated into oracle/_ref."""
     return os.environ.get("SOLRT_REFERENCE", "/root/reference")
 
 

@@ -19,7 +19,6 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
-#include <mutex>
 #include <vector>
 
 #include "bvh8.cuh"
@@ -1057,32 +1056,21 @@ constexpr size_t kNoAllocBytes = kOffNbox + round256(32ull * kNoAllocTris);
 }  // namespace
 
 // Scratch of the allocation-free build. Host code must not use this name as a
-// pointer (on the host it is only a stand-in): it takes the device address
-// from cudaGetSymbolAddress, once per device.
+// pointer (on the host it is only a stand-in): every call takes the device
+// address from cudaGetSymbolAddress in the context current at that call.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 namespace {
 
-constexpr int kNoAllocMaxDevices = 64;
-std::mutex g_noalloc_mutex;
-void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
-
-// Device address of the scratch array on the current device (looked up on
-// the first call for that device).
+// Device address of the scratch array in the current context. Looked up on
+// every call and never cached: an address taken in one context is not valid
+// in another (a host application's own context, or the primary context
+// created again after cudaDeviceReset). The lookup is a host-side query
+// that queues no GPU work.
 solrt_status noalloc_scratch(void** out) {
-    int dev = 0;
-    SOLRT_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kNoAllocMaxDevices) {
-        set_error("device ordinal %d out of range for the allocation-free build", dev);
-        return SOLRT_ERR_DEVICE;
-    }
-    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_ptr[dev]) {
-        void* p = nullptr;
-        SOLRT_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-        g_noalloc_ptr[dev] = p;
-    }
-    *out = g_noalloc_ptr[dev];
+    void* p = nullptr;
+    SOLRT_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    *out = p;
     return SOLRT_OK;
 }
 
@@ -1114,6 +1102,7 @@ extern "C" solrt_status solrt_bvh2_build_noalloc(const void* vpos, const void* t
         set_error("solrt_bvh2_build_noalloc: buffers must be 16-byte aligned");
         return SOLRT_ERR_INVALID;
     }
+    cudaGetLastError();  // launch errors below must be this call's own
     void* base = nullptr;
     SOLRT_TRY(noalloc_scratch(&base));
     unsigned char* s = static_cast<unsigned char*>(base);

@@ -7,6 +7,18 @@ solrt = importlib.import_module("sol-rs_gb300")
 S = solrt.scenes
 
 
+def reference_path(*parts):
+    """A file of the reference checkout (located by the recipe that reads it,
+    oracle/ref_glsl/build_ref.py); tests skip where it is absent."""
+    import os
+    import sys
+    here = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "ref_glsl")
+    if here not in sys.path:
+        sys.path.insert(0, here)
+    import build_ref
+    return os.path.join(build_ref.reference_root(), *parts)
+
+
 def random_rays(n, lo, hi, seed, tmin=1e-4, tmax=1e4):
     rng = np.random.default_rng(seed)
     r = np.zeros(n, solrt.RAY_DTYPE)

@@ -118,3 +118,27 @@ def test_ctypes_mirror_matches_header(solrt, tmp_path):
         assert int(got[cname]) == ctypes.sizeof(cls), cname
         for f in cls._fields_:
             assert int(got["%s.%s" % (cname, f[0])]) == getattr(cls, f[0]).offset, (cname, f[0])
+
+
+def test_noalloc_build_argument_checks(solrt):
+    """solrt_bvh2_build_noalloc refuses bad requests before it queues any
+    GPU work: too many triangles, output buffers one byte too small, buffers
+    that are not 16-byte aligned, null pointers. The pointers here are never
+    dereferenced (the checks come first), so this runs without a GPU."""
+    L = solrt.lib()
+    fn = L.solrt_bvh2_build_noalloc
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_size_t,
+                   ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+    a, b, c, d = 0x10000, 0x20000, 0x30000, 0x40000
+    n = 100
+    assert fn(a, b, 65537, c, 64 * 65536, d, 48 * 65537, None) == 5          # SOLRT_ERR_CAPACITY
+    assert fn(a, b, n, c, 64 * (n - 1) - 1, d, 48 * n, None) == 1           # nodes one byte short
+    assert b"too small" in L.solrt_last_error()
+    assert fn(a, b, n, c, 64 * (n - 1), d, 48 * n - 1, None) == 1           # triangles one byte short
+    assert fn(a, b, 1, c, 63, d, 48, None) == 1                              # one triangle: one node
+    assert fn(a + 8, b, n, c, 64 * (n - 1), d, 48 * n, None) == 1           # misaligned input
+    assert fn(a, b, n, c + 4, 64 * (n - 1), d, 48 * n, None) == 1           # misaligned output
+    assert b"aligned" in L.solrt_last_error()
+    assert fn(None, b, n, c, 64 * (n - 1), d, 48 * n, None) == 1            # null input
+    assert fn(a, b, 0, c, 0, d, 0, None) == 0                                # nothing to build

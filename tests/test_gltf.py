@@ -14,9 +14,9 @@ import struct
 import numpy as np
 import pytest
 
-from helpers import S
+from helpers import S, reference_path
 
-REF_MODELS = "/root/reference/assets/models"
+REF_MODELS = reference_path("assets", "models")
 
 
 def _arrays_equal(a, b):
@@ -288,7 +288,7 @@ def test_read_png_8_and_16_bit(solrt, tmp_path):
 
 
 def test_reference_blue_noise_texture(solrt):
-    path = "/root/reference/assets/textures/HDR_RGBA_0.png"
+    path = reference_path("assets", "textures", "HDR_RGBA_0.png")
     if not os.path.exists(path):
         pytest.skip("reference textures not present")
     from importlib import import_module

@@ -18,7 +18,7 @@ import os
 import numpy as np
 import pytest
 
-from helpers import S, camera_of, solrt, transformed_cornell
+from helpers import S, camera_of, reference_path, solrt, transformed_cornell
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
@@ -72,7 +72,7 @@ def test_reference_shaders_transformed_sections(ref):
         assert np.array_equal(r8, o8), sky
 
 
-REF_MODELS = "/root/reference/assets/models"
+REF_MODELS = reference_path("assets", "models")
 
 
 @pytest.mark.parametrize("model,sky", [("cornell.gltf", False), ("tunnel.gltf", True)])

@@ -78,6 +78,29 @@ def test_noalloc_build_matches_scene_build(solrt, ctx, maker):
     sc.close()
 
 
+def test_noalloc_single_triangle_on_default_stream(solrt, ctx):
+    """One triangle (the single-node layout: a root whose two children are
+    the same leaf) queued on the legacy default stream (stream = NULL)."""
+    import torch
+    data = S.soup(1, seed=9)
+    sc = solrt.SceneDescription(ctx, data, bvh=solrt.BVH2)
+    want_nodes, want_tris = sc.bvh_export()
+    vpos, tri = _world_arrays(data)
+    dv = torch.from_numpy(vpos).cuda()
+    dt = torch.from_numpy(tri.view(np.int32)).cuda()
+    nodes = torch.full((64,), 0xA5, dtype=torch.uint8, device="cuda")
+    tris = torch.full((48,), 0x5A, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    fn = _bind(solrt.lib())
+    for _ in range(2):
+        st = fn(dv.data_ptr(), dt.data_ptr(), 1, nodes.data_ptr(), 64, tris.data_ptr(), 48, None)
+        assert st == 0, solrt.lib().solrt_last_error()
+        torch.cuda.synchronize()
+        assert np.array_equal(nodes.cpu().numpy(), want_nodes)
+        assert np.array_equal(tris.cpu().numpy(), want_tris)
+    sc.close()
+
+
 def test_noalloc_rejects_too_many_triangles(solrt, ctx):
     fn = _bind(solrt.lib())
     st = fn(None, None, 65537, None, 0, None, 0, None)
