@@ -234,44 +234,44 @@ def cpu_baseline(data, kw, cam, budget_s=10.0, threads=0):
             "segments": int(st.segments), "seconds": round(dt, 3)}
 
 
-def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, main_tris, n_rays=1 << 22):
+def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, main_tris, n_rays=1 << 22,
+                    kinds=None, render=True):
     """The 16-bit quantised binary BVH, the 8-bit quantised 4- and 8-wide BVHs
-    and the FP32 8-wide BVH vs the FP32 binary BVH on the same scene:
-    hit records of 4M rays (every camera ray of the frame's first sample
-    positions plus seeded rays from inside the scene) compared bit for bit on
-    the device, node bytes, visits per segment, Mrays/s of one 64-spp frame
-    and the FP64 fallback count of each."""
+    and the FP32 8-wide BVH next to the FP32 binary BVH on the same scene:
+    hit records of 4M rays (every pixel-centre camera ray of the frame, then
+    seeded rays from inside the scene's bounds) traced on the device by each
+    kind and compared bit for bit with the oracle's CPU LBVH traversal on all
+    host cores (the checker), node bytes, visits per segment, Mrays/s of one
+    frame and the FP64 fallback count of each."""
     import torch
+    import oracle
     solrt = importlib.import_module("sol-rs_gb300")
+    S = solrt.scenes
     W, H = kw["width"], kw["height"]
-    g = torch.Generator(device="cpu").manual_seed(7)
-    n_cam = W * H
-    n_in = n_rays - n_cam
-    rays = torch.zeros((n_rays, 8), dtype=torch.float32)
-    # camera rays through pixel centres (origin, tmin, direction, tmax)
-    V = np.array(cam.view_inverse, np.float64).reshape(4, 4).T
-    P = np.array(cam.projection_inverse, np.float64).reshape(4, 4).T
-    ys, xs = np.mgrid[0:H, 0:W]
-    d = np.stack([(xs + 0.5) / W * 2 - 1, (ys + 0.5) / H * 2 - 1, np.ones_like(xs, float), np.ones_like(xs, float)], -1)
-    t = d.reshape(-1, 4) @ P.T
-    t = t[:, :3] / np.linalg.norm(t[:, :3], axis=1, keepdims=True)
-    dirs = t @ V[:3, :3].T
-    org = V[:3, 3]
-    rays[:n_cam, 0:3] = torch.from_numpy(np.tile(org, (n_cam, 1)).astype(np.float32))
-    rays[:n_cam, 4:7] = torch.from_numpy(dirs.astype(np.float32))
-    rays[n_cam:, 0:3] = torch.rand((n_in, 3), generator=g)
-    dd = torch.randn((n_in, 3), generator=g)
-    rays[n_cam:, 4:7] = dd / dd.norm(dim=1, keepdim=True)
-    rays[:, 3] = 1e-3
-    rays[:, 7] = 1e4
+    rays = S.probe_rays(data, cam, W, H, n_rays, seed=7)
+    t0 = time.perf_counter()
+    o = oracle.OracleScene(data)
+    want, want_fb = o.trace(rays)
+    o.close()
+    oracle_s = time.perf_counter() - t0
+    want_u = want.view(np.uint32).reshape(-1, 4)
+    edge = S.near_edge(want)
     dev = torch.device("cuda", local)
-    rays_d = rays.to(dev)
+    rays_d = torch.from_numpy(rays.view(np.float32).reshape(-1, 8).copy()).to(dev)
     out = {"rays_compared": n_rays, "leaf_max": 1}
-    hits = {}
+    vs = {"rays": n_rays, "hits": int((want["prim"] != 0xFFFFFFFF).sum()), "near_edge_hits": int(edge.sum()),
+          "mismatches": {}, "near_edge_mismatches": {}, "oracle_fp64_fallbacks": int(want_fb),
+          "oracle": "CPU LBVH traversal (FP32 watertight test, FP64 edge fallback, lower index wins ties) on %d "
+                    "threads, %.1f s" % (os.cpu_count() or 1, oracle_s),
+          "rays_desc": "%d pixel-centre camera rays of the %dx%d frame + %d seeded rays from inside the scene "
+                       "bounds" % (min(n_rays, W * H), W, H, max(0, n_rays - W * H))}
+    all_kinds = (("bvh2_fp32", solrt.BVH2, False), ("bvh2_q16", solrt.BVH2_Q16, False),
+                 ("bvh4_q8", solrt.BVH4_Q8, False), ("bvh8_q8", solrt.BVH8_Q8, False),
+                 ("bvh8_q8_sah", solrt.BVH8_Q8, True), ("bvh8_fp32", solrt.BVH8_F32, False))
     with solrt.Context(local, enable_timing=True) as ctx, solrt.Context(local, enable_counters=True) as cctx:
-        for name, kind, sah in (("bvh2_fp32", solrt.BVH2, False), ("bvh2_q16", solrt.BVH2_Q16, False),
-                                ("bvh4_q8", solrt.BVH4_Q8, False), ("bvh8_q8", solrt.BVH8_Q8, False),
-                                ("bvh8_q8_sah", solrt.BVH8_Q8, True), ("bvh8_fp32", solrt.BVH8_F32, False)):
+        for name, kind, sah in all_kinds:
+            if kinds is not None and name not in kinds:
+                continue
             sc = solrt.SceneDescription(ctx, data, bvh=kind, leaf_max=0 if kind in (solrt.BVH2, solrt.BVH2_Q16) else 1,
                                         sah=sah)
             info = sc.bvh_info()
@@ -280,10 +280,15 @@ def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, mai
             sc.trace_rays_device(rays_d.data_ptr(), n_rays, h.data_ptr())
             ctx.synchronize()
             fb_trace = ctx.stats().fp64_fallbacks
-            hits[name] = h
-            if kind == main_info.kind and not sah:
+            got = h.cpu().numpy().view(np.uint32)
+            bad = np.any(got != want_u, axis=1)
+            vs["mismatches"][name] = int(bad.sum())
+            vs["near_edge_mismatches"][name] = int((bad & edge).sum())
+            del h
+            mr = nodes = tris = None
+            if main_info is not None and kind == main_info.kind and not sah and main_mrays is not None:
                 mr, nodes, tris = main_mrays, main_nodes, main_tris
-            else:
+            elif render:
                 img = solrt.Image(ctx, W, H, kw["accum_mode"])
                 r = solrt.Renderer(ctx)
                 r.cmd_trace_rays(sc, cam, solrt.render_params(**kw), img)
@@ -309,25 +314,198 @@ def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, mai
             nb = NODE_BYTES[info.kind]
             out[name] = {"mrays_per_s": round(mr, 1) if mr else None, "node_bytes": int(info.node_bytes),
                          "node_count": int(info.node_count), "bytes_per_node": nb,
-                         "nodes_per_segment": round(nodes, 2), "tris_per_segment": round(tris, 2),
-                         "node_bytes_per_segment": round(nb * nodes, 1),
+                         "nodes_per_segment": round(nodes, 2) if nodes is not None else None,
+                         "tris_per_segment": round(tris, 2) if tris is not None else None,
+                         "node_bytes_per_segment": round(nb * nodes, 1) if nodes is not None else None,
                          "fp64_fallbacks_in_compared_rays": int(fb_trace), "build_ms": round(info.build_ms, 3)}
             sc.close()
-    a = hits["bvh2_fp32"].view(torch.int32)
-    out["hit_mismatches"] = {k: int((a != hits[k].view(torch.int32)).any(dim=1).sum().item())
-                             for k in ("bvh2_q16", "bvh4_q8", "bvh8_q8", "bvh8_q8_sah", "bvh8_fp32")}
-    # hits within about one float ulp of a triangle edge (a barycentric below
-    # 2^-23), counted separately: the watertight test and the lower-index tie
-    # rule make even these agree across BVHs
-    h = hits["bvh2_fp32"]
-    hit = a[:, 1] != -1
-    u, v = h[:, 2], h[:, 3]
-    edge = hit & (torch.minimum(torch.minimum(u, v), 1.0 - u - v) < 2.0 ** -23)
-    out["near_edge_hits"] = int(edge.sum().item())
-    out["near_edge_mismatches"] = {k: int(((a != hits[k].view(torch.int32)).any(dim=1) & edge).sum().item())
-                                   for k in ("bvh2_q16", "bvh4_q8", "bvh8_q8", "bvh8_q8_sah", "bvh8_fp32")}
-    out["hits"] = int((a[:, 1] != -1).sum().item())
+    out["hit_ids_vs_oracle"] = vs
     return out
+
+
+def rmse_vs_fp64(local, data, kw, cam, bvh, rows, frames=1, sah=False):
+    """RMSE of the device RGBA32F image (after `frames` accumulated frames)
+    against the FP64 oracle on identical RNG streams, over image rows
+    [rows[0], rows[1]) (the oracle is the checker). Also compares the same
+    rows with the FP32 oracle bit for bit."""
+    import oracle
+    solrt = importlib.import_module("sol-rs_gb300")
+    W, H = kw["width"], kw["height"]
+    with solrt.Context(local) as ctx:
+        sc = solrt.SceneDescription(ctx, data, bvh=bvh, sah=sah, keep_data=False)
+        img = solrt.Image(ctx, W, H, kw["accum_mode"])
+        r = solrt.Renderer(ctx)
+        for f in range(frames):
+            r.cmd_trace_rays(sc, cam, solrt.render_params(**dict(kw, frame=f)), img)
+        acc, _ = img.read()
+        img.close()
+        sc.close()
+    t0 = time.perf_counter()
+    o = oracle.OracleScene(data)
+    kahan = kw["accum_mode"] == solrt.ACCUM_KAHAN
+    out = {}
+    for prec in (64, 32):
+        a = np.zeros((H, W, 4), np.float32)
+        ks = np.zeros((H, W, 4), np.float32) if kahan else None
+        kc = np.zeros((H, W, 4), np.float32) if kahan else None
+        for f in range(frames):
+            a, _, _ = o.render(cam, solrt.render_params(**dict(kw, frame=f)), accum=a, ksum=ks, kcomp=kc, rows=rows,
+                               precision=prec)
+        out[prec] = a[rows[0]:rows[1]]
+    o.close()
+    g = acc[rows[0]:rows[1]]
+    d = g[..., :3].astype(np.float64) - out[64][..., :3].astype(np.float64)
+    v = float(np.sqrt(np.mean(d * d)))
+    return {"rmse": v, "bound": 1e-3, "within_bound": v <= 1e-3, "rows": list(rows), "width": W,
+            "spp": kw["spp"] * frames, "frames": frames,
+            "bit_exact_vs_fp32_oracle": bool(np.array_equal(g.view(np.uint32), out[32].view(np.uint32))),
+            "oracle_seconds": round(time.perf_counter() - t0, 2),
+            "how": "device RGBA32F after %d frame(s) vs FP64 oracle, identical RNG streams, rows %d-%d of %d"
+                   % (frames, rows[0], rows[1] - 1, H)}
+
+
+def parity_cornell(local):
+    """The plain small configuration at its stated size (procedural Cornell
+    box, 256x256, 16 spp, depth 5, Lambert, seed 1) rendered whole: bit for
+    bit against the FP32 oracle, equal segment counts, RMSE against the FP64
+    oracle over the whole image, device Mrays/s."""
+    import torch
+    import oracle
+    solrt = importlib.import_module("sol-rs_gb300")
+    data, kw, cfg = workload("cornell")
+    W, H = kw["width"], kw["height"]
+    c = data.camera
+    cam = solrt.camera_look_at(c["eye"], c["center"], c["up"], c["vfov"], W / H)
+    with solrt.Context(local) as ctx:
+        sc = solrt.SceneDescription(ctx, data)
+        img = solrt.Image(ctx, W, H)
+        r = solrt.Renderer(ctx)
+        p = solrt.render_params(**kw)
+        for _ in range(3):
+            r.cmd_trace_rays(sc, cam, p, img)
+        ext = torch.cuda.ExternalStream(ctx.stream())
+        ctx.synchronize()
+        ctx.reset_stats()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        for _ in range(10):
+            r.cmd_trace_rays(sc, cam, p, img)
+        e1.record(ext)
+        ctx.synchronize()
+        mrays = ctx.stats().segments / (e0.elapsed_time(e1) / 1000.0) / 1e6
+        img2 = solrt.Image(ctx, W, H)
+        ctx.reset_stats()
+        r.cmd_trace_rays(sc, cam, p, img2)
+        ctx.synchronize()
+        seg = ctx.stats().segments
+        acc, _ = img2.read()
+        img.close()
+        img2.close()
+        sc.close()
+    t0 = time.perf_counter()
+    o = oracle.OracleScene(data)
+    a32, _, st = o.render(cam, p)
+    a64, _, _ = o.render(cam, p, precision=64)
+    o.close()
+    d = acc[..., :3].astype(np.float64) - a64[..., :3].astype(np.float64)
+    v = float(np.sqrt(np.mean(d * d)))
+    return {"workload": cfg["workload"], "device_mrays_s": round(mrays, 1),
+            "bit_exact_vs_fp32_oracle": bool(np.array_equal(acc.view(np.uint32), a32.view(np.uint32))),
+            "segments": int(seg), "oracle_segments": int(st.segments),
+            "rmse_vs_fp64": {"rmse": v, "bound": 1e-3, "within_bound": v <= 1e-3, "rows": [0, H], "spp": kw["spp"],
+                             "how": "whole image, one frame, identical RNG streams"},
+            "oracle_seconds": round(time.perf_counter() - t0, 2)}
+
+
+def parity_tunnel(local, n_rays=1 << 22):
+    """The procedural tunnel at its stated size (4.19M triangles, 2560x1440,
+    128 spp, depth 8, Kahan sums): RMSE against the FP64 oracle over two
+    central rows after four frames (512 spp), and the hit records of 4M probe
+    rays of the BVH2 and the BVH8-q8 (SAH collapse) against the oracle's
+    traversal, with Mrays/s of one frame for each."""
+    solrt = importlib.import_module("sol-rs_gb300")
+    data, kw, cfg = workload("tunnel")
+    W, H = kw["width"], kw["height"]
+    c = data.camera
+    cam = solrt.camera_look_at(c["eye"], c["center"], c["up"], c["vfov"], W / H)
+    out = {"workload": cfg["workload"]}
+    out["rmse_vs_fp64"] = rmse_vs_fp64(local, data, kw, cam, solrt.BVH2, (H // 2 - 1, H // 2 + 1), frames=4)
+    ps = precision_study(local, data, kw, cam, None, None, None, None, n_rays=n_rays,
+                         kinds=("bvh2_fp32", "bvh8_q8", "bvh8_q8_sah"))
+    out.update(ps)
+    return out
+
+
+def reference_semantics(local, data, kw, cam, budget_s=3.0):
+    """The workload's scene and image under the settings the reference's
+    shaders fix (pathtrace.rgen:41-45, pathtrace.rchit:90-111,
+    pathtrace.rmiss:8-21): 8 samples per launch, at most 32 bounces, the
+    reference materials and sky, one RNG stream per pixel, mix accumulation.
+    Device Mrays/s over the whole image (CUDA events, one launch = one
+    frame), and the reference's own pathtrace.rgen / .rchit / .rmiss compiled
+    as C++ (oracle/_ref) on all host cores over a central band of rows of the
+    same launch, traceRayEXT answered by the oracle's LBVH closest hit; the
+    device rows are compared with the reference pipeline's bit for bit."""
+    import torch
+    import oracle
+    solrt = importlib.import_module("sol-rs_gb300")
+    W, H = kw["width"], kw["height"]
+    p = solrt.render_params(W, H, spp=8, max_bounces=32, material_mode=solrt.MATERIAL_REF,
+                            miss_mode=solrt.MISS_REF_SKY, rng_mode=solrt.RNG_REF_STREAM,
+                            accum_mode=solrt.ACCUM_REF_MIX)
+    out = {"settings": "8 spp per launch, 32 bounces, reference materials, reference sky, per-pixel RNG stream, "
+                       "mix accumulation (the reference shaders' own)"}
+    with solrt.Context(local) as ctx:
+        sc = solrt.SceneDescription(ctx, data, keep_data=False)
+        img = solrt.Image(ctx, W, H)
+        r = solrt.Renderer(ctx)
+        for f in range(2):
+            r.cmd_trace_rays(sc, cam, solrt.render_params(**dict(_params_dict(p), frame=f)), img)
+        ext = torch.cuda.ExternalStream(ctx.stream())
+        ctx.synchronize()
+        ctx.reset_stats()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        for f in range(5):
+            r.cmd_trace_rays(sc, cam, solrt.render_params(**dict(_params_dict(p), frame=2 + f)), img)
+        e1.record(ext)
+        ctx.synchronize()
+        gpu = ctx.stats().segments / (e0.elapsed_time(e1) / 1000.0) / 1e6
+        img.close()
+        img = solrt.Image(ctx, W, H)
+        r.cmd_trace_rays(sc, cam, p, img)
+        acc, _ = img.read()
+        img.close()
+        sc.close()
+    out["device_mrays_s"] = round(gpu, 1)
+    if oracle.ref_lib() is None:
+        out["reference_shaders"] = {"unavailable": "oracle/_ref not built (no reference checkout and no generated "
+                                                   "sources)"}
+        return out
+    o = oracle.OracleScene(data)
+    st = {}
+    t0 = time.perf_counter()
+    oracle.ref_path_render(o, cam, W, H, rows=(H // 2 - 1, H // 2 + 1), sky=True, stats=st)
+    per_row = (time.perf_counter() - t0) / 2
+    rows = int(min(H, max(2, budget_s / max(per_row, 1e-6))))
+    r0 = max(0, H // 2 - rows // 2)
+    t0 = time.perf_counter()
+    ra, _ = oracle.ref_path_render(o, cam, W, H, rows=(r0, r0 + rows), sky=True, stats=st)
+    dt = time.perf_counter() - t0
+    o.close()
+    cpu = st["rays"] / dt / 1e6
+    out["reference_shaders"] = {"mrays_s": round(cpu, 3), "cores": os.cpu_count() or 1, "rows": [r0, r0 + rows],
+                                "traced": int(st["rays"]), "seconds": round(dt, 2)}
+    out["device_over_reference_shaders"] = round(gpu / cpu, 1) if cpu > 0 else None
+    out["band_bit_exact_vs_reference_shaders"] = bool(
+        np.array_equal(acc[r0:r0 + rows].view(np.uint32), ra[r0:r0 + rows].view(np.uint32)))
+    return out
+
+
+def _params_dict(p):
+    return {"width": p.width, "height": p.height, "spp": p.spp, "max_bounces": p.max_bounces, "frame": p.frame,
+            "seed": p.seed, "miss_mode": p.miss_mode, "material_mode": p.material_mode,
+            "accum_mode": p.accum_mode, "rng_mode": p.rng_mode}
 
 
 def run_batch(args, world, rank, local, pg, njobs=None, steps=None, emit=True):
@@ -511,82 +689,59 @@ def run_serve(local, rate, duration, n_scenes=16, seed=5, policy=0):
 
 
 def run_reference(args, world, rank, pg):
+    """The reference arm: the CPU port of the reference's path (the oracle:
+    pathtrace.rgen / .rchit / .rmiss restated in C++ with its LBVH, pinned bit
+    for bit against the reference's own shaders compiled as C++) on all host
+    cores, on this workload's exact settings, over a central band of rows at
+    the full spp per step. The reference itself (Rust + Vulkan ray tracing)
+    cannot run on this machine, and its shaders fix settings (8 spp, 32
+    bounces, reference materials and sky) other than the configuration's, so
+    the port is the implementation that renders this configuration. This arm
+    never loads the CUDA library: the camera comes from the oracle."""
     if rank != 0:
         return 0
-    solrt = importlib.import_module("sol-rs_gb300")
-    data, kw, cfg = workload(args.workload)
-    c = data.camera
-    cam = solrt.camera_look_at(c["eye"], c["center"], c["up"], c["vfov"], kw["width"] / kw["height"])
     import oracle
-    o = oracle.OracleScene(data)
-    if oracle.ref_lib() is not None:
-        return run_reference_shaders(args, world, oracle, o, data, kw, cfg, cam)
-    p = solrt.render_params(**dict(kw, spp=1))
-    h = kw["height"]
-    # size one step to ~2 s of CPU work: a central band of rows at 1 spp
-    t0 = time.perf_counter()
-    _, _, st = o.render(cam, p, rows=(h // 2, h // 2 + 4))
-    per_row = (time.perf_counter() - t0) / 4
-    rows = int(min(h, max(1, 2.0 / max(per_row, 1e-6))))
-    r0 = max(0, h // 2 - rows // 2)
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        o.render(cam, p, rows=(r0, r0 + rows))
-    seg, tt = 0, 0.0
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        _, _, st = o.render(cam, p, rows=(r0, r0 + rows))
-        tt += time.perf_counter() - t0
-        seg += st.segments
-    v = seg / tt / 1e6
-    cores = os.cpu_count() or 1
-    line = {"impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * tt / args.steps, 3),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": dict(cfg, parallelism="cpu"),
-            "cpu_baseline": {"value": round(v, 3), "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": "%d rows x %d px x 1 spp per step (central band), FP32 oracle port of the "
-                                       "reference shaders with its LBVH; the reference (Rust + Vulkan RT) cannot "
-                                       "run on this machine" % (rows, kw["width"])},
-            "e2e": {"value": round(v, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
-    return 0
-
-
-def run_reference_shaders(args, world, oracle, o, data, kw, cfg, cam):
-    """The reference's own pathtrace.rgen / .rchit / .rmiss, rewritten to C++
-    (oracle/_ref), run as a ray-tracing pipeline on all host cores over a
-    central band of the workload's image; traceRayEXT is the oracle's LBVH
-    closest hit (the reference's is the GPU driver's). The shaders fix 8
-    spp, 32 bounces and the reference materials; sky on."""
+    data, kw, cfg = workload(args.workload)
+    solrt_api = importlib.import_module("sol-rs_gb300.api")
     W, H = kw["width"], kw["height"]
-    rows = 2
-    st = {}
+    c = data.camera
+    cam = oracle.camera_look_at(c["eye"], c["center"], c["up"], c["vfov"], W / H)
+    o = oracle.OracleScene(data)
+    p = solrt_api.render_params(**kw)
+    # one step = a central band of rows at the full spp, sized to ~1 s
     t0 = time.perf_counter()
-    oracle.ref_path_render(o, cam, W, H, rows=(H // 2 - 1, H // 2 + 1), sky=True, stats=st)
-    per_row = (time.perf_counter() - t0) / rows
-    rows = int(min(H, max(1, 3.0 / max(per_row, 1e-6))))
+    o.render(cam, p, rows=(H // 2, H // 2 + 1))
+    per_row = time.perf_counter() - t0
+    rows = int(min(H, max(1, 1.0 / max(per_row, 1e-6))))
     r0 = max(0, H // 2 - rows // 2)
-    acc = np.zeros((H, W, 4), np.float32)
-    oracle.ref_path_render(o, cam, W, H, rows=(r0, r0 + rows), sky=True, accum=acc)
+    for i in range(args.warmup):
+        o.render(cam, solrt_api.render_params(**dict(kw, frame=i)), rows=(r0, r0 + rows))
     seg, tt = 0, 0.0
     for i in range(args.steps):
         t0 = time.perf_counter()
-        oracle.ref_path_render(o, cam, W, H, frame=i + 1, rows=(r0, r0 + rows), sky=True, accum=acc, stats=st)
+        _, _, st = o.render(cam, solrt_api.render_params(**dict(kw, frame=args.warmup + i)), rows=(r0, r0 + rows))
         tt += time.perf_counter() - t0
-        seg += st["rays"]
+        seg += st.segments
+    o.close()
     v = seg / tt / 1e6
     cores = os.cpu_count() or 1
-    sample = ("%d rows x %d px x 8 spp per step (central band of the %dx%d launch): the reference's pathtrace.rgen / "
-              ".rchit / .rmiss compiled as C++ from its sources (32 bounces, reference materials, sky, as the shaders "
-              "fix), traceRayEXT answered by the oracle's watertight LBVH traversal on %d threads" % (rows, W, W, H, cores))
+    sample = ("%d rows x %d px x %d spp per step (central band of the %dx%d frame, the workload's own settings): "
+              "FP32 CPU port of the reference's pathtrace shaders with its LBVH, %d threads" % (
+                  rows, W, kw["spp"], W, H, cores))
     line = {"impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000 * tt / args.steps, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": dict(cfg, parallelism="cpu"),
-            "cpu_baseline": {"value": round(v, 3), "unit": UNIT, "cores": cores, "kind": "reference", "sample": sample},
+            "config": run_config(cfg, args, world),
+            "cpu_baseline": {"value": round(v, 3), "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": round(v, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def run_config(cfg, args, world):
+    """The config object of the JSON line, the same for both arms."""
+    return dict(cfg, parallelism="replicas" if world > 1 else "single", bvh=args.bvh,
+                l2="inputs larger than L2 (scene + BVH + path queues > 129 MB)")
 
 
 def main():
@@ -781,37 +936,17 @@ def main():
         roofline["l2"] = {"peak": round(l2, 1), "unit": "GB/s", "frac": round(achieved / l2, 4) if l2 else None,
                           "peak_source": "measured here: 32 MB device-to-device copy, L2-resident, best of 20"}
 
-    # RMSE of the device image (one fresh frame) against the FP64 oracle on the
-    # same RNG streams, over a central band of rows (the oracle is the checker)
-    # (frames accumulated: more for the tunnel, whose sun-lit sky makes FP32
-    # and FP64 paths that part ways differ by a lot for a few samples)
+    # RMSE of the device image against the FP64 oracle on the same RNG
+    # streams, over a central band of rows (the oracle is the checker); the
+    # tunnel accumulates four frames (its sun-lit sky makes FP32 and FP64
+    # paths that part ways differ by a lot for a few samples)
     rmse = None
     if rank == 0 and not args.no_cpu_baseline:
         try:
-            import oracle
             frames = 4 if args.workload == "tunnel" else 1
-            fresh = solrt.Image(ctx, W, H, kw["accum_mode"])
-            for f in range(frames):
-                r.cmd_trace_rays(sc, cam, solrt.render_params(**dict(kw, frame=f)), fresh)
-            acc, _ = fresh.read()
-            fresh.close()
-            band = (H // 2 - 2, H // 2 + 2)
-            t0 = time.perf_counter()
-            # flattened FP64 scene for every kind (the two-level oracle mode is
-            # a brute force, too slow for a million triangles)
-            o64 = oracle.OracleScene(data)
-            a64 = np.zeros((H, W, 4), np.float32)
-            kahan = kw["accum_mode"] == solrt.ACCUM_KAHAN
-            ks = np.zeros((H, W, 4), np.float32) if kahan else None
-            kc = np.zeros((H, W, 4), np.float32) if kahan else None
-            for f in range(frames):
-                a64, _, _ = o64.render(cam, solrt.render_params(**dict(kw, frame=f)), accum=a64, ksum=ks, kcomp=kc,
-                                       rows=band, precision=64)
-            d = acc[band[0]:band[1], :, :3].astype(np.float64) - a64[band[0]:band[1], :, :3].astype(np.float64)
-            v = float(np.sqrt(np.mean(d * d)))
-            rmse = {"rmse": v, "bound": 1e-3, "within_bound": v <= 1e-3, "rows": list(band), "spp": kw["spp"] * frames,
-                    "frames": frames, "fp64_seconds": round(time.perf_counter() - t0, 2),
-                    "how": "device RGBA32F after %d frame(s) vs FP64 oracle, identical RNG streams" % frames}
+            band = {"soup": 32, "tunnel": 1}.get(args.workload, H // 2)
+            rows = (max(0, H // 2 - band), min(H, H // 2 + band))
+            rmse = rmse_vs_fp64(local, data, kw, cam, bvh, rows, frames=frames, sah=args.sah)
         except Exception as ex:
             rmse = {"error": str(ex)}
     img.close()
@@ -823,6 +958,21 @@ def main():
             precision = precision_study(local, data, kw, cam, value / max(world, 1), info, nodes_per_seg, tris_per_seg)
         except Exception as ex:
             precision = {"error": str(ex)}
+    # parity and convergence of the other single-scene configurations at
+    # their stated sizes, and the workload under the reference shaders' own
+    # settings next to those shaders on the host cores
+    configs = refsem = None
+    if rank == 0 and args.workload == "soup" and not args.no_precision:
+        configs = {}
+        for name, fn in (("cornell", parity_cornell), ("tunnel", parity_tunnel)):
+            try:
+                configs[name] = fn(local)
+            except Exception as ex:
+                configs[name] = {"error": str(ex)}
+        try:
+            refsem = reference_semantics(local, data, kw, cam)
+        except Exception as ex:
+            refsem = {"error": str(ex)}
     # the other two parts of the headline metric, measured on smaller runs:
     # batched vs plain (first 32 jobs of the mixed-scene workload) and the
     # p99 latency of served jobs
@@ -845,13 +995,12 @@ def main():
         out = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 3), "higher_is_better": True,
                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-               "config": dict(cfg, parallelism="replicas" if world > 1 else "single", bvh=args.bvh,
-                              l2="inputs larger than L2 (scene + BVH + path queues > 129 MB)",
-                              bvh_build_ms=round(info.build_ms, 3), bvh_node_count=info.node_count),
+               "config": run_config(cfg, args, world),
+               "bvh": {"kind": args.bvh, "build_ms": round(info.build_ms, 3), "node_count": int(info.node_count)},
                "segments_per_step": int(st.segments // args.steps), "fp64_fallbacks_per_segment": fb_per_seg,
                "gpu_launches": int(st.launches), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                "clocks": clk, "rmse_vs_fp64": rmse, "precision_study": precision, "batched_vs_plain": batched,
-               "serving": serving}
+               "serving": serving, "configs_at_stated_size": configs, "reference_semantics": refsem}
         if regen is not None:
             out["regenerate_ms"] = regen
         if args.nee:

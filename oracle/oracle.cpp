@@ -1277,10 +1277,14 @@ static int render_impl(const oracle_scene* s, const solrt_camera* cam, const sol
     row_end = std::min(row_end, p->height);
     threads = resolve_threads(threads);
     std::vector<Counters> cn(threads);
+    // work items are runs of up to 64 pixels of a row, so that a band of a
+    // few rows still keeps every thread busy (pixels are independent)
     const uint32_t rows = row_end - row_begin;
-    parallel_for(rows, threads, [&](uint32_t r, int t) {
-        const uint32_t y = row_begin + r;
-        for (uint32_t x = 0; x < p->width; ++x) {
+    const uint32_t runs = (p->width + 63u) / 64u;
+    parallel_for(rows * runs, threads, [&](uint32_t item, int t) {
+        const uint32_t y = row_begin + item / runs;
+        const uint32_t x0 = (item % runs) * 64u, x1 = std::min(p->width, x0 + 64u);
+        for (uint32_t x = x0; x < x1; ++x) {
             if (p->integrator == SOLRT_INTEGRATOR_DEBUG) {
                 if (precision == 64) render_pixel_debug<double>(s, cam, p, x, y, accum, rgba8, cn[t]);
                 else render_pixel_debug<float>(s, cam, p, x, y, accum, rgba8, cn[t]);

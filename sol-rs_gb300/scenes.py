@@ -296,6 +296,46 @@ def mixed_scene(i, seed_base=4, min_tris=1000, max_tris=500000):
     return data, dict(width=res, height=res, spp=spp, max_bounces=5, seed=seed_base + i)
 
 
+def probe_rays(data, camera, width, height, n, seed=7, tmin=1e-3, tmax=1e4):
+    """Ray set of the hit-record studies: every pixel-centre camera ray of a
+    width x height image of `camera` (row-major, first), then seeded rays
+    from uniform points of the scene's bounding box in uniform directions,
+    n rays in all. Returns a structured array (origin, tmin, dir, tmax);
+    camera directions are normalize(P^-1 (x, y, 1, 1)) through the view
+    inverse, computed in FP64 and rounded to FP32."""
+    ray_dtype = np.dtype([("origin", "<f4", 3), ("tmin", "<f4"), ("dir", "<f4", 3), ("tmax", "<f4")])
+    n_cam = min(n, width * height)
+    rays = np.zeros(n, ray_dtype)
+    V = np.array(camera.view_inverse, np.float64).reshape(4, 4).T
+    P = np.array(camera.projection_inverse, np.float64).reshape(4, 4).T
+    ys, xs = np.mgrid[0:height, 0:width]
+    d = np.stack([(xs + 0.5) / width * 2 - 1, (ys + 0.5) / height * 2 - 1, np.ones(xs.shape), np.ones(xs.shape)], -1)
+    t = d.reshape(-1, 4)[:n_cam] @ P.T
+    t = t[:, :3] / np.linalg.norm(t[:, :3], axis=1, keepdims=True)
+    rays["origin"][:n_cam] = V[:3, 3].astype(np.float32)
+    rays["dir"][:n_cam] = (t @ V[:3, :3].T).astype(np.float32)
+    rng = np.random.default_rng(seed)
+    pos = data.vertices["pos"][:, :3]
+    lo, hi = pos.min(0).astype(np.float64), pos.max(0).astype(np.float64)
+    m = n - n_cam
+    rays["origin"][n_cam:] = (lo + rng.random((m, 3)) * (hi - lo)).astype(np.float32)
+    dd = rng.normal(size=(m, 3))
+    rays["dir"][n_cam:] = (dd / np.linalg.norm(dd, axis=1, keepdims=True)).astype(np.float32)
+    rays["tmin"] = tmin
+    rays["tmax"] = tmax
+    return rays
+
+
+def near_edge(hits):
+    """Hits within about one float ulp of a triangle edge: a barycentric
+    (u, v or 1 - u - v) below 2^-23. `hits` is a (t, prim, u, v) array."""
+    h = np.asarray(hits)
+    u = h["u"].astype(np.float64)
+    v = h["v"].astype(np.float64)
+    hit = h["prim"] != 0xFFFFFFFF
+    return hit & (np.minimum(np.minimum(u, v), 1.0 - u - v) < 2.0 ** -23)
+
+
 def write_gltf(data, path, view=None, yfov=None, znear=0.01, zfar=100.0, node_transforms=None,
                index_type="u32", external_bin=False):
     """Writes a SceneData as glTF 2.0 that load_scene reads back

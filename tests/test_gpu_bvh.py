@@ -24,7 +24,9 @@ def _oracle_refs(child):
 
 
 @pytest.mark.parametrize("maker", [lambda: S.cornell(), lambda: S.soup(50000, seed=2),
-                                   lambda: S.tunnel(n_ang=128, n_ax=64, length=20.0)])
+                                   lambda: S.tunnel(n_ang=128, n_ax=64, length=20.0),
+                                   lambda: S.soup(1_000_000, seed=2), lambda: S.tunnel()],
+                         ids=["cornell", "soup50k", "tunnel_small", "soup1M_full", "tunnel4M_full"])
 def test_bvh2_topology_bit_exact(solrt, oracle, ctx, maker):
     d = maker()
     sc = solrt.SceneDescription(ctx, d, bvh=solrt.BVH2)
