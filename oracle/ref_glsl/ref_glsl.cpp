@@ -401,4 +401,14 @@ void ref_gamma(const float c[3], float power, float out[3]) {
     out[0] = r.x; out[1] = r.y; out[2] = r.z;
 }
 
+void ref_tonemap_uncharted2(const float c[3], float out[3]) {
+    const glsl::vec3 r = glsl::golden::tonemapUncharted2(glsl::vec3{c[0], c[1], c[2]});
+    out[0] = r.x; out[1] = r.y; out[2] = r.z;
+}
+
+void ref_tonemap_aces(const float c[3], float out[3]) {
+    const glsl::vec3 r = glsl::golden::ACESFilm(glsl::vec3{c[0], c[1], c[2]});
+    out[0] = r.x; out[1] = r.y; out[2] = r.z;
+}
+
 }  // extern "C"

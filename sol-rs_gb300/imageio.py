@@ -41,20 +41,31 @@ def gamma_correct(c, power=2.2):
     return np.power(np.maximum(c, 0.0), np.float32(1.0) / np.float32(power))
 
 
+_F = np.float32
+
+
 def tonemap_uncharted2(c):
-    """postprocess.glsl:5-22 (Hable's filmic curve, exposure bias 2, white 11.2)."""
-    A, B, C, D, E, F = 0.15, 0.50, 0.10, 0.20, 0.02, 0.30
+    """postprocess.glsl:5-22 (Hable's filmic curve, exposure bias 2, white
+    11.2), in FP32 with the shader's operation order: constant products are
+    single-precision products (C*B, D*E, D*F, E/F), then
+    ((x*(A*x+CB)+DE)/(x*(A*x+B)+DF))-EF of 2*c, times 1/curve(11.2)."""
+    A, B, C, D, E, F = _F(0.15), _F(0.50), _F(0.10), _F(0.20), _F(0.02), _F(0.30)
+    CB, DE, DF, EF = C * B, D * E, D * F, E / F
 
     def curve(x):
-        return ((x * (A * x + C * B) + D * E) / (x * (A * x + B) + D * F)) - E / F
+        return ((x * (A * x + CB) + DE) / (x * (A * x + B) + DF)) - EF
 
-    return curve(2.0 * c) * (1.0 / curve(np.float32(11.2)))
+    x = np.asarray(c, _F)
+    white = _F(1.0) / curve(_F(11.2))
+    return curve(_F(2.0) * x) * white
 
 
 def tonemap_aces(c):
-    """postprocess.glsl:24-31 (Narkowicz's ACES fit)."""
-    a, b, cc, d, e = 2.51, 0.03, 2.43, 0.59, 0.14
-    return np.clip((c * (a * c + b)) / (c * (cc * c + d) + e), 0.0, 1.0)
+    """postprocess.glsl:24-31 (Narkowicz's ACES fit) in FP32:
+    clamp((x*(a*x+b))/(x*(c*x+d)+e), 0, 1)."""
+    a, b, cc, d, e = _F(2.51), _F(0.03), _F(2.43), _F(0.59), _F(0.14)
+    x = np.asarray(c, _F)
+    return np.minimum(np.maximum((x * (a * x + b)) / (x * (cc * x + d) + e), _F(0.0)), _F(1.0))
 
 
 def to_rgba8(rgb, tonemap=None):

@@ -108,6 +108,18 @@ def main():
         gam.append([fbits(c), fbits(o[0])])
     out["gamma"] = gam
 
+    # postprocess.glsl tonemaps (Hable's filmic curve, Narkowicz's ACES fit)
+    lib.ref_tonemap_uncharted2.argtypes = [f3, f3]
+    lib.ref_tonemap_aces.argtypes = [f3, f3]
+    tm = {"uncharted2": [], "aces": []}
+    xs = np.concatenate([[0.0, 1e-6, 0.5, 1.0, 2.0, 11.2, 100.0], rng.random(57) * 4.0]).astype(np.float32)
+    for c in xs:
+        for name, fn in (("uncharted2", lib.ref_tonemap_uncharted2), ("aces", lib.ref_tonemap_aces)):
+            o = f3()
+            fn(f3(c, c, c), o)
+            tm[name].append([fbits(c), fbits(o[0])])
+    out["tonemap"] = tm
+
     path = os.path.join(HERE, "glsl_sampling.json")
     with open(path, "w") as f:
         json.dump(out, f, separators=(",", ":"))

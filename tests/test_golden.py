@@ -88,3 +88,16 @@ def test_sincos_accuracy(oracle):
         s, c = oracle.sincos(float(x))
         err = max(err, abs(s - np.sin(np.float64(x))), abs(c - np.cos(np.float64(x))))
     assert err < 2.5e-7
+
+
+def test_tonemaps_match_reference_postprocess(solrt):
+    """imageio's tonemaps against postprocess.glsl's tonemapUncharted2 and
+    ACESFilm compiled as C++ (golden vectors): bit for bit."""
+    io = solrt.imageio
+    for name, fn in (("uncharted2", io.tonemap_uncharted2), ("aces", io.tonemap_aces)):
+        xs = np.array([bf(c) for c, _ in GOLD["tonemap"][name]], np.float32)
+        want = np.array([bf(r) for _, r in GOLD["tonemap"][name]], np.float32)
+        got = fn(np.repeat(xs[:, None], 3, axis=1))
+        assert got.dtype == np.float32
+        assert np.array_equal(got[:, 0].view(np.uint32), want.view(np.uint32)), name
+        assert np.array_equal(got[:, 1], got[:, 0]) and np.array_equal(got[:, 2], got[:, 0])
