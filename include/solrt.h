@@ -37,7 +37,7 @@ extern "C" {
 #endif
 
 /* 2: solrt_stats gained shadow_segments and shadow_unoccluded. */
-#define SOLRT_ABI_VERSION 2u
+#define SOLRT_ABI_VERSION 3u
 
 typedef enum solrt_status {
     SOLRT_OK = 0,
@@ -514,20 +514,35 @@ typedef enum solrt_serve_policy {
 
 typedef struct solrt_server_desc {
     uint64_t memory_budget;   /* bytes of job images + scenes in use; 0 = 150 GB */
-    uint32_t tick_paths;      /* paths per tick; 0 = min(8M, the context's path capacity) */
+    /* paths per tick; 0 = adaptive: each tick is sized to about tick_ms of
+     * device time at the rate measured over the previous ticks, between 1M
+     * paths and the context's path capacity (the first tick: 8M) */
+    uint32_t tick_paths;
     uint32_t policy;          /* solrt_serve_policy */
     /* host-side fault injection for tests: the next this-many admissions
      * fail as if their image allocation had failed (SOLRT_ERR_OOM) */
     uint32_t inject_alloc_failures;
-    uint32_t reserved[3];
+    /* > 0: convergence stopping rule. After each tick, once a job has at
+     * least stop_min_spp samples, its image's RMSE against the converged
+     * image (the mean over all samples it could take) is estimated from the
+     * per-pixel sample variance: sqrt(mean over pixels and RGB of
+     * variance / samples). The job completes early, with the samples it has,
+     * once the estimate is at most stop_rmse; otherwise it runs its spp.
+     * The server keeps one float of squared sample sums per pixel for such
+     * jobs. 0 = every job runs all of its spp. */
+    float stop_rmse;
+    uint32_t stop_min_spp;    /* samples before the first estimate; 0 = 4 */
+    uint32_t tick_ms;         /* adaptive ticks: target device time per tick; 0 = 40 ms */
 } solrt_server_desc;
 
 typedef struct solrt_job_result {
     uint32_t status;          /* SOLRT_OK when done, SOLRT_ERR_NOT_READY before */
-    uint32_t spp_done;
+    uint32_t spp_done;        /* samples accumulated (below spp when the job stopped early) */
     uint64_t latency_ns;      /* submit -> last sample accumulated and image final */
     uint64_t queue_ns;        /* submit -> admitted */
     solrt_image* image;       /* owned by the server until released or evicted */
+    float rmse_estimate;      /* last convergence estimate (stop_rmse > 0), else -1 */
+    uint32_t stopped_early;   /* 1 when the stopping rule ended the job before its spp */
 } solrt_job_result;
 
 typedef struct solrt_server_stats {
@@ -538,6 +553,9 @@ typedef struct solrt_server_stats {
     uint32_t active;          /* admitted, not yet complete */
     uint64_t bytes_in_use;
     double busy_ms;           /* device time of all ticks */
+    uint64_t stopped_early;   /* jobs completed by the stopping rule */
+    uint32_t tick_paths;      /* size of the last tick */
+    uint32_t reserved;
 } solrt_server_stats;
 
 /* A serving thread owns the context's stream until solrt_server_destroy:
@@ -548,7 +566,8 @@ typedef struct solrt_server_stats {
  * then it runs one wavefront pass in which every active job advances by its
  * share of tick_paths (at least one sample; a job with more pixels than a
  * tick runs one sample per tick), and finalizes the jobs that reached their
- * spp. A job's image equals solrt_render of the same job alone. */
+ * spp (or, with stop_rmse, converged). A job's image equals solrt_render of
+ * the same job alone with the samples it took (spp_done). */
 solrt_status solrt_server_create(solrt_context* ctx, const solrt_server_desc* desc, solrt_server** out);
 /* Queues a job: the server allocates its image (params.width x height). */
 solrt_status solrt_server_submit(solrt_server* srv, solrt_scene* scene, const solrt_camera* camera,

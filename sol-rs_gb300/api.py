@@ -104,19 +104,22 @@ SERVE_FAIR, SERVE_SHORTEST_FIRST = 0, 1
 
 class ServerDesc(ctypes.Structure):
     _fields_ = [("memory_budget", ctypes.c_uint64), ("tick_paths", ctypes.c_uint32), ("policy", ctypes.c_uint32),
-                ("inject_alloc_failures", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 3)]
+                ("inject_alloc_failures", ctypes.c_uint32), ("stop_rmse", ctypes.c_float),
+                ("stop_min_spp", ctypes.c_uint32), ("tick_ms", ctypes.c_uint32)]
 
 
 class JobResult(ctypes.Structure):
     _fields_ = [("status", ctypes.c_uint32), ("spp_done", ctypes.c_uint32), ("latency_ns", ctypes.c_uint64),
-                ("queue_ns", ctypes.c_uint64), ("image", ctypes.c_void_p)]
+                ("queue_ns", ctypes.c_uint64), ("image", ctypes.c_void_p), ("rmse_estimate", ctypes.c_float),
+                ("stopped_early", ctypes.c_uint32)]
 
 
 class ServerStats(ctypes.Structure):
     _fields_ = [("submitted", ctypes.c_uint64), ("admitted", ctypes.c_uint64), ("completed", ctypes.c_uint64),
                 ("evicted", ctypes.c_uint64), ("ticks", ctypes.c_uint64), ("segments", ctypes.c_uint64),
                 ("queue_depth", ctypes.c_uint32), ("active", ctypes.c_uint32), ("bytes_in_use", ctypes.c_uint64),
-                ("busy_ms", ctypes.c_double)]
+                ("busy_ms", ctypes.c_double), ("stopped_early", ctypes.c_uint64), ("tick_paths", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
 
 
 class TuneConfig(ctypes.Structure):
@@ -210,7 +213,7 @@ _PROTOS = {
 }
 
 _lib = None
-ABI_VERSION = 2  # SOLRT_ABI_VERSION of the structs mirrored here
+ABI_VERSION = 3  # SOLRT_ABI_VERSION of the structs mirrored here
 
 
 def lib():
@@ -559,12 +562,15 @@ class Server:
     """Continuous-batching render server (solrt_server): a serving thread
     admits jobs by memory budget and advances all active jobs each tick."""
 
-    def __init__(self, context, memory_budget=0, tick_paths=0, policy=0, inject_alloc_failures=0):
-        """policy: SERVE_FAIR (0) or SERVE_SHORTEST_FIRST (1);
-        inject_alloc_failures: host-side fault injection for tests."""
+    def __init__(self, context, memory_budget=0, tick_paths=0, policy=0, inject_alloc_failures=0, stop_rmse=0.0,
+                 stop_min_spp=0, tick_ms=0):
+        """policy: SERVE_FAIR (0) or SERVE_SHORTEST_FIRST (1); tick_paths 0 =
+        adaptive ticks of about tick_ms of device time; stop_rmse > 0: jobs
+        stop once their estimated RMSE against the converged image is at most
+        this; inject_alloc_failures: host-side fault injection for tests."""
         self.context = context
         h = ctypes.c_void_p()
-        desc = ServerDesc(memory_budget, tick_paths, policy, inject_alloc_failures)
+        desc = ServerDesc(memory_budget, tick_paths, policy, inject_alloc_failures, stop_rmse, stop_min_spp, tick_ms)
         check(lib().solrt_server_create(context.handle, ctypes.byref(desc), ctypes.byref(h)))
         self.handle = h
         self._scenes = {}

@@ -28,6 +28,8 @@ static_assert(sizeof(solrt_instance) == 144, "SceneInstance is 144 bytes (src/ra
 static_assert(sizeof(solrt_ray) == 32, "solrt_ray is two float4");
 static_assert(sizeof(solrt_hit) == 16, "solrt_hit is one float4");
 static_assert(sizeof(solrt_camera) == 256, "four mat4");
+static_assert(sizeof(solrt_server_desc) == 32 && sizeof(solrt_job_result) == 40 && sizeof(solrt_server_stats) == 88,
+              "server structs (mirrored by the Python binding)");
 
 struct solrt_context : solrt::Context {};
 struct solrt_scene : solrt::Scene {};

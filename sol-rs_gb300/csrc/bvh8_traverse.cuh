@@ -31,9 +31,54 @@ SOLRT_D float byte_biased(uint32_t word, uint32_t k) {
     return __uint_as_float(__byte_perm(word, 0x4B000000u, 0x7440u | k));
 }
 
+// 8-bit mask of the non-empty slots of a node from its meta bytes (m0:
+// slots 0-3, m1: slots 4-7): a slot is used iff one of its meta bits 5-7 is
+// set (internal children 0b001xxxxx, leaves (2^k - 1) << 5 with k >= 1).
+// Bit 7 of each byte collects bits 5-7, moves to bit 0, and one multiply
+// gathers the four byte bits into bits 24-27.
+SOLRT_D uint32_t bvh8_used_mask(uint32_t m0, uint32_t m1) {
+    const uint32_t v0 = ((m0 | (m0 << 1) | (m0 << 2)) >> 7) & 0x01010101u;
+    const uint32_t v1 = ((m1 | (m1 << 1) | (m1 << 2)) >> 7) & 0x01010101u;
+    return ((v0 * 0x01020408u) >> 24) | (((v1 * 0x01020408u) >> 24) << 4);
+}
+
+// Bit s of an 8-bit slot mask moved to bit s ^ oct (visiting order).
+SOLRT_D uint32_t octant_order(uint32_t x, uint32_t oct) {
+    if (oct & 1u) x = ((x & 0x55u) << 1) | ((x >> 1) & 0x55u);
+    if (oct & 2u) x = ((x & 0x33u) << 2) | ((x >> 2) & 0x33u);
+    if (oct & 4u) x = ((x & 0x0Fu) << 4) | ((x >> 4) & 0x0Fu);
+    return x;
+}
+
+// Two lanes of a*b, each correctly rounded (PTX mul.rn.f32x2, sm_100 and
+// later; see fma_x2).
+SOLRT_D float2 mul_x2(float a0, float a1, float b) {
+    float2 r;
+#if SOLRT_SLAB_F32X2
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\t"
+        "mov.b64 rb, {%4, %4};\n\t"
+        "mul.rn.f32x2 rd, ra, rb;\n\t"
+        "mov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a0), "f"(a1), "f"(b));
+#else
+    r.x = a0 * b;
+    r.y = a1 * b;
+#endif
+    return r;
+}
+
 // Tests the 8 children of one node. Returns the hit internal children in
 // visiting order (bit s ^ oct for slot s) and the hit leaf triangles
 // (bit o of the node's triangle range).
+// Children are tested in pairs: each plane distance of two neighbouring
+// slots is one packed two-lane FMA (every lane the same correctly rounded
+// fma as a scalar one), and the far distances are widened in pairs, so the
+// hit decisions are those of one child at a time. The 8-bit hit mask is
+// then cut to the used slots, split into internal children (put in
+// visiting order once per node) and leaves (only the hit leaf slots read
+// their meta byte).
 SOLRT_D void bvh8_node_test(const uint4& w0, const uint4& w1, const uint4& w2, const uint4& w3, const uint4& w4,
                             float ox, float oy, float oz, float ix, float iy, float iz, bool negx, bool negy,
                             bool negz, uint32_t oct, float tmin, float tmax, uint32_t& hit_inner,
@@ -58,24 +103,31 @@ SOLRT_D void bvh8_node_test(const uint4& w0, const uint4& w1, const uint4& w2, c
     const uint32_t fy0 = negy ? w2.z : w4.x, fy1 = negy ? w2.w : w4.y;
     const uint32_t nz0 = negz ? w4.z : w3.x, nz1 = negz ? w4.w : w3.y;
     const uint32_t fz0 = negz ? w3.x : w4.z, fz1 = negz ? w3.y : w4.w;
-    hit_inner = 0;
-    hit_tri = 0;
+    uint32_t hit = 0;
 #pragma unroll
-    for (int s = 0; s < 8; ++s) {
-        const uint32_t k = (uint32_t)(s & 3);
-        const uint32_t meta = ((s < 4 ? w1.z : w1.w) >> (8u * k)) & 0xffu;
-        const float tnx = fmaf(byte_biased(s < 4 ? nx0 : nx1, k), sx, ax);
-        const float tny = fmaf(byte_biased(s < 4 ? ny0 : ny1, k), sy, ay);
-        const float tnz = fmaf(byte_biased(s < 4 ? nz0 : nz1, k), sz, az);
-        const float tfx = fmaf(byte_biased(s < 4 ? fx0 : fx1, k), sx, ax);
-        const float tfy = fmaf(byte_biased(s < 4 ? fy0 : fy1, k), sy, ay);
-        const float tfz = fmaf(byte_biased(s < 4 ? fz0 : fz1, k), sz, az);
-        const float tn = max3(tnx, tny, fmaxf(tnz, tmin));
-        const float tf = min3(tfx, tfy, fminf(tfz, tmax));
-        if (meta != 0u && tn <= tf * 1.0000153f) {
-            if (imask & (1u << s)) hit_inner |= 1u << ((uint32_t)s ^ oct);
-            else hit_tri |= (meta >> 5) << (meta & 31u);
-        }
+    for (int p = 0; p < 4; ++p) {
+        const uint32_t k0 = (uint32_t)((2 * p) & 3), k1 = k0 + 1u;
+        const uint32_t nxw = p < 2 ? nx0 : nx1, nyw = p < 2 ? ny0 : ny1, nzw = p < 2 ? nz0 : nz1;
+        const uint32_t fxw = p < 2 ? fx0 : fx1, fyw = p < 2 ? fy0 : fy1, fzw = p < 2 ? fz0 : fz1;
+        const float2 tnx = fma_x2(byte_biased(nxw, k0), byte_biased(nxw, k1), sx, ax);
+        const float2 tny = fma_x2(byte_biased(nyw, k0), byte_biased(nyw, k1), sy, ay);
+        const float2 tnz = fma_x2(byte_biased(nzw, k0), byte_biased(nzw, k1), sz, az);
+        const float2 tfx = fma_x2(byte_biased(fxw, k0), byte_biased(fxw, k1), sx, ax);
+        const float2 tfy = fma_x2(byte_biased(fyw, k0), byte_biased(fyw, k1), sy, ay);
+        const float2 tfz = fma_x2(byte_biased(fzw, k0), byte_biased(fzw, k1), sz, az);
+        const float tn0 = max3(tnx.x, tny.x, fmaxf(tnz.x, tmin)), tn1 = max3(tnx.y, tny.y, fmaxf(tnz.y, tmin));
+        const float2 tf = mul_x2(min3(tfx.x, tfy.x, fminf(tfz.x, tmax)), min3(tfx.y, tfy.y, fminf(tfz.y, tmax)),
+                                 1.0000153f);
+        if (tn0 <= tf.x) hit |= 1u << (2 * p);
+        if (tn1 <= tf.y) hit |= 2u << (2 * p);
+    }
+    hit &= bvh8_used_mask(w1.z, w1.w);
+    hit_inner = octant_order(hit & imask, oct);
+    hit_tri = 0;
+    for (uint32_t leaves = hit & ~imask; leaves; leaves &= leaves - 1u) {
+        const uint32_t s = (uint32_t)(__ffs(leaves) - 1);
+        const uint32_t meta = __byte_perm(w1.z, w1.w, s) & 0xffu;
+        hit_tri |= (meta >> 5) << (meta & 31u);
     }
 }
 

@@ -116,6 +116,9 @@ struct DevJob {
     float4* ksum;
     float4* kcomp;
     uint32_t* rng_state;
+    // served jobs with a stopping rule: per pixel the sum over its samples of
+    // r^2 + g^2 + b^2 (null otherwise)
+    float* sq;
 };
 
 // A work item of one pass: samples [s0, s0 + k) of pixels [pix0, pix0 + npix)
@@ -343,7 +346,16 @@ solrt_status render_frame(Context& ctx, const Scene& sc, const solrt_camera& cam
                           Image& img);
 struct TickBuffers {
     DeviceBuffer jobs, items, fin_jobs, fin_pix;
+    DeviceBuffer est_jobs, est_pix, est_n, est_sum;  // convergence estimates
 };
+
+// Convergence estimates of served jobs: for job i (its DevJob with `sq`,
+// n[i] samples per pixel so far) the sum over its pixels of the variance of
+// the pixel mean summed over RGB; out[i] / (3 * pixels) is the estimated
+// squared RMSE against the converged image (infinite when a pixel sum is
+// not finite). Synchronises.
+solrt_status estimate_rmse(Context& ctx, TickBuffers& tb, const std::vector<DevJob>& jobs,
+                           const std::vector<uint32_t>& n, std::vector<double>& out);
 solrt_status serve_tick(Context& ctx, TickBuffers& tb, uint32_t kind, const std::vector<DevJob>& jobs,
                         const std::vector<DevItem>& items, const PassPlan& pp, const std::vector<DevJob>& fin);
 DevJob job_for(const Scene& sc, const Image& img, const solrt_camera& cam, const solrt_render_params& p);

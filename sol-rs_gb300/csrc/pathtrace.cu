@@ -217,6 +217,48 @@ __global__ void k_accumulate(const DevJob* __restrict__ jobs, const DevItem* __r
         for (uint32_t j = 0; j < it.k; ++j) add_sample(s, r[j]);
         J.fsum[pix] = make_float4(s.x, s.y, s.z, 0.0f);
     }
+    if (J.sq) {  // squared sample sums of the stopping rule (samples the sums above keep)
+        float q = J.sq[pix];
+        for (uint32_t j = 0; j < it.k; ++j) {
+            const float4 c = r[j];
+            if (J.accum_mode != SOLRT_ACCUM_KAHAN || (isfinite(c.x) && isfinite(c.y) && isfinite(c.z)))
+                q = q + (c.x * c.x + c.y * c.y + c.z * c.z);
+        }
+        J.sq[pix] = q;
+    }
+}
+
+// Per job, the sum over its pixels of the variance of the pixel mean summed
+// over RGB: with n samples (Kahan mode: the finite ones it kept), sums S_c
+// and squared sums Q = sum of r^2 + g^2 + b^2, the unbiased sample variance
+// summed over channels is (Q - sum_c S_c^2 / n) / (n - 1), and the mean's is
+// that over n. A non-finite pixel makes the job's sum infinite.
+__global__ void k_rmse_estimate(const DevJob* __restrict__ jobs, const uint32_t* __restrict__ job_pix,
+                                const uint32_t* __restrict__ nsamp, uint32_t njobs, uint32_t pixels,
+                                double* __restrict__ sums) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool in = t < pixels;
+    const uint32_t j = in ? find_last_le(njobs, t, [&](uint32_t i) { return job_pix[i]; }) : 0u;
+    double v = 0.0;
+    if (in) {
+        const DevJob& J = jobs[j];
+        const uint32_t pix = t - job_pix[j];
+        const float4 s = J.accum_mode == SOLRT_ACCUM_KAHAN ? J.ksum[pix] : J.fsum[pix];
+        const double n = J.accum_mode == SOLRT_ACCUM_KAHAN ? (double)s.w : (double)nsamp[j];
+        const double q = (double)J.sq[pix];
+        const double ss = (double)s.x * s.x + (double)s.y * s.y + (double)s.z * s.z;
+        if (!isfinite(ss) || !isfinite(q)) v = __longlong_as_double(0x7ff0000000000000LL);
+        else if (n >= 2.0) v = fmax(q - ss / n, 0.0) / (n - 1.0) / n;
+        else v = __longlong_as_double(0x7ff0000000000000LL);
+    }
+    // warps whose lanes share one job add once; others lane by lane
+    const uint32_t first = __shfl_sync(0xffffffffu, j, 0);
+    if (__all_sync(0xffffffffu, !in || j == first)) {
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0) atomicAdd(sums + first, v);
+    } else if (in) {
+        atomicAdd(sums + j, v);
+    }
 }
 
 // The reference's structure (pathtrace.rgen:39-104): one thread per pixel
@@ -917,6 +959,32 @@ solrt_status serve_tick(Context& ctx, TickBuffers& tb, uint32_t kind, const std:
         ++ctx.launches;
     }
     SOLRT_CUDA(cudaGetLastError());
+    return SOLRT_OK;
+}
+
+solrt_status estimate_rmse(Context& ctx, TickBuffers& tb, const std::vector<DevJob>& jobs,
+                           const std::vector<uint32_t>& n, std::vector<double>& out) {
+    out.assign(jobs.size(), 0.0);
+    if (jobs.empty()) return SOLRT_OK;
+    cudaStream_t st = ctx.stream;
+    std::vector<uint32_t> pix(1, 0u);
+    for (const DevJob& J : jobs) pix.push_back(pix.back() + J.width * J.height);
+    SOLRT_TRY(tb.est_jobs.alloc(sizeof(DevJob) * jobs.size()));
+    SOLRT_TRY(tb.est_pix.alloc(sizeof(uint32_t) * pix.size()));
+    SOLRT_TRY(tb.est_n.alloc(sizeof(uint32_t) * n.size()));
+    SOLRT_TRY(tb.est_sum.alloc(sizeof(double) * jobs.size()));
+    cudaGetLastError();
+    SOLRT_CUDA(cudaMemcpyAsync(tb.est_jobs.ptr, jobs.data(), sizeof(DevJob) * jobs.size(), cudaMemcpyHostToDevice, st));
+    SOLRT_CUDA(cudaMemcpyAsync(tb.est_pix.ptr, pix.data(), sizeof(uint32_t) * pix.size(), cudaMemcpyHostToDevice, st));
+    SOLRT_CUDA(cudaMemcpyAsync(tb.est_n.ptr, n.data(), sizeof(uint32_t) * n.size(), cudaMemcpyHostToDevice, st));
+    SOLRT_CUDA(cudaMemsetAsync(tb.est_sum.ptr, 0, sizeof(double) * jobs.size(), st));
+    k_rmse_estimate<<<cdiv(pix.back(), 256), 256, 0, st>>>(tb.est_jobs.as<DevJob>(), tb.est_pix.as<uint32_t>(),
+                                                           tb.est_n.as<uint32_t>(), (uint32_t)jobs.size(), pix.back(),
+                                                           tb.est_sum.as<double>());
+    ++ctx.launches;
+    SOLRT_CUDA(cudaGetLastError());
+    SOLRT_CUDA(cudaMemcpyAsync(out.data(), tb.est_sum.ptr, sizeof(double) * jobs.size(), cudaMemcpyDeviceToHost, st));
+    SOLRT_CUDA(cudaStreamSynchronize(st));
     return SOLRT_OK;
 }
 

@@ -9,11 +9,17 @@
 //   2. one wavefront pass in which every active job advances by a share of
 //      tick_paths (at least one sample; REF_STREAM jobs one sample);
 //   3. jobs whose last samples were in the pass are finalized in the same
-//      tick and reported with their latency.
+//      tick and reported with their latency; with a stopping rule
+//      (stop_rmse), jobs whose estimated RMSE against their converged image
+//      fell to the bound are finalized right after it, with the samples they
+//      have.
+// Ticks are sized to about tick_ms of device time at the measured rate
+// unless the server was given a fixed tick_paths.
 // Jobs arriving while a tick runs join at the next tick. A job's image is
 // the same as solrt_render of that job alone: its samples are accumulated
 // in order whatever ticks they fall in, and nothing is shared between jobs.
 #include <algorithm>
+#include <cmath>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -53,11 +59,14 @@ struct ServerJob {
     uint64_t image_bytes = 0;
     bool counted = false;  // image and scene counted against the budget
     bool cancel = false;   // cancelled while running: leaves after the tick in flight
+    float* sq = nullptr;   // stopping rule: per-pixel squared sample sums (device)
+    float rmse_est = -1.0f;
+    bool stopped_early = false;
 };
 
-uint64_t image_bytes_of(const solrt_render_params& p) {
+uint64_t image_bytes_of(const solrt_render_params& p, bool stop_rule) {
     const uint64_t np = (uint64_t)p.width * p.height;
-    return np * (16 + 4 + 16 + 4) + (p.accum_mode == SOLRT_ACCUM_KAHAN ? np * 32 : 0);
+    return np * (16 + 4 + 16 + 4) + (p.accum_mode == SOLRT_ACCUM_KAHAN ? np * 32 : 0) + (stop_rule ? np * 4 : 0);
 }
 
 }  // namespace
@@ -66,6 +75,11 @@ struct solrt_server {
     solrt_context* ctx = nullptr;
     uint64_t budget = 0;
     uint32_t tick_paths = 0;
+    bool adaptive = false;    // tick_paths follows tick_ms at the measured rate
+    double tick_ms = 40.0;
+    double rate = 0.0;        // paths per ms of device time (moving average)
+    float stop_rmse = 0.0f;
+    uint32_t stop_min_spp = 4;
     uint32_t policy = SOLRT_SERVE_FAIR;
     uint32_t inject_alloc_failures = 0;
     std::mutex mu;
@@ -97,6 +111,10 @@ uint64_t scene_bytes(solrt_scene* s) {
 void drop_job_memory(solrt_server* srv, ServerJob& j) {
     if (!j.counted) return;
     j.counted = false;
+    if (j.sq) {
+        cudaFree(j.sq);
+        j.sq = nullptr;
+    }
     if (j.image) {
         solrt_image_destroy(j.image);
         j.image = nullptr;
@@ -112,7 +130,8 @@ void drop_job_memory(solrt_server* srv, ServerJob& j) {
 void admit(solrt_server* srv) {
     while (!srv->queue.empty()) {
         ServerJob& j = srv->jobs[srv->queue.front()];
-        const uint64_t need = image_bytes_of(j.p) + (srv->scene_refs.count(j.scene) ? 0 : scene_bytes(j.scene));
+        const bool rule = srv->stop_rmse > 0.0f;
+        const uint64_t need = image_bytes_of(j.p, rule) + (srv->scene_refs.count(j.scene) ? 0 : scene_bytes(j.scene));
         while (srv->bytes_in_use + need > srv->budget && !srv->done_lru.empty()) {
             const uint64_t victim = srv->done_lru.front();
             srv->done_lru.pop_front();
@@ -140,6 +159,19 @@ void admit(solrt_server* srv) {
             s = SOLRT_ERR_OOM;
         } else {
             s = solrt_image_create(srv->ctx, j.p.width, j.p.height, j.p.accum_mode, &img);
+            if (s == SOLRT_OK && rule) {
+                const size_t b = sizeof(float) * (size_t)j.p.width * j.p.height;
+                if (cudaMalloc(&j.sq, b) != cudaSuccess ||
+                    cudaMemsetAsync(j.sq, 0, b, srv->ctx->stream) != cudaSuccess) {
+                    cudaGetLastError();
+                    if (j.sq) cudaFree(j.sq);
+                    j.sq = nullptr;
+                    solrt_image_destroy(img);
+                    img = nullptr;
+                    solrt::set_error("cannot allocate the squared sums of the stopping rule");
+                    s = SOLRT_ERR_OOM;
+                }
+            }
         }
         srv->queue.pop_front();
         if (s != SOLRT_OK) {
@@ -151,7 +183,7 @@ void admit(solrt_server* srv) {
         }
         j.image = img;
         j.counted = true;
-        j.image_bytes = image_bytes_of(j.p);
+        j.image_bytes = image_bytes_of(j.p, rule);
         srv->bytes_in_use += j.image_bytes;
         if (srv->scene_refs[j.scene]++ == 0) srv->bytes_in_use += scene_bytes(j.scene);
         j.state = kActive;
@@ -167,10 +199,11 @@ void serve_loop(solrt_server* srv) {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    std::vector<solrt::DevJob> jobs, fin;
+    std::vector<solrt::DevJob> jobs, fin, est_jobs;
     std::vector<solrt::DevItem> items;
-    std::vector<uint64_t> tick_tickets, fin_tickets;
-    std::vector<uint32_t> tick_k;
+    std::vector<uint64_t> tick_tickets, fin_tickets, est_tickets;
+    std::vector<uint32_t> tick_k, est_n;
+    std::vector<double> est_sum;
     for (;;) {
         solrt::PassPlan pp{0, 0, 0, 0, 0};
         {
@@ -233,6 +266,7 @@ void serve_loop(solrt_server* srv) {
                 const solrt::Scene& sc = *static_cast<solrt::Scene*>(j.scene);
                 const solrt::Image& img = *static_cast<solrt::Image*>(j.image);
                 jobs.push_back(solrt::job_for(sc, img, j.cam, j.p));
+                jobs.back().sq = j.sq;
                 items.push_back(it);
                 pp.item_count += 1;
                 pp.paths += np * k;
@@ -258,6 +292,14 @@ void serve_loop(solrt_server* srv) {
         std::lock_guard<std::mutex> lock(srv->mu);
         ++srv->st.ticks;
         srv->st.busy_ms += ms;
+        srv->st.tick_paths = pp.paths;
+        if (srv->adaptive && pp.paths > 0 && ms > 0.0f) {
+            // next tick: about tick_ms at the rate of the recent ticks
+            const double r = (double)pp.paths / (double)ms;
+            srv->rate = srv->rate > 0.0 ? 0.7 * srv->rate + 0.3 * r : r;
+            const double want = srv->rate * srv->tick_ms;
+            srv->tick_paths = (uint32_t)std::min<double>(ctx.capacity, std::max<double>(1u << 20, want));
+        }
         for (size_t i = 0; i < tick_tickets.size(); ++i) {
             ServerJob& j = srv->jobs[tick_tickets[i]];
             if (s != SOLRT_OK || e != cudaSuccess) {
@@ -276,6 +318,62 @@ void serve_loop(solrt_server* srv) {
                 ++srv->st.completed;
             }
         }
+        // stopping rule: estimate the jobs of this tick that continue
+        est_jobs.clear();
+        est_tickets.clear();
+        est_n.clear();
+        if (s == SOLRT_OK && e == cudaSuccess && srv->stop_rmse > 0.0f) {
+            for (size_t i = 0; i < tick_tickets.size(); ++i) {
+                ServerJob& j = srv->jobs[tick_tickets[i]];
+                if (j.state != kActive || !j.sq || j.cancel || j.spp_done < srv->stop_min_spp) continue;
+                est_jobs.push_back(jobs[i]);
+                est_tickets.push_back(j.ticket);
+                est_n.push_back(j.spp_done);
+            }
+        }
+        if (!est_jobs.empty() && solrt::estimate_rmse(ctx, srv->tb, est_jobs, est_n, est_sum) == SOLRT_OK) {
+            fin.clear();
+            fin_tickets.clear();
+            for (size_t i = 0; i < est_jobs.size(); ++i) {
+                ServerJob& j = srv->jobs[est_tickets[i]];
+                const double px = 3.0 * est_jobs[i].width * est_jobs[i].height;
+                const double v = std::sqrt(est_sum[i] / px);
+                j.rmse_est = (float)v;
+                if (v <= (double)srv->stop_rmse) {  // converged: finalize with the samples it has
+                    solrt_render_params q = j.p;
+                    q.spp = j.spp_done;
+                    const solrt::Scene& sc = *static_cast<solrt::Scene*>(j.scene);
+                    const solrt::Image& img = *static_cast<solrt::Image*>(j.image);
+                    fin.push_back(solrt::job_for(sc, img, j.cam, q));
+                    fin_tickets.push_back(j.ticket);
+                }
+            }
+            if (!fin.empty()) {
+                const std::vector<solrt::DevJob> none_j;
+                const std::vector<solrt::DevItem> none_i;
+                const solrt::PassPlan none_p{0, 0, 0, 0, 0};
+                const solrt_status fs = solrt::serve_tick(ctx, srv->tb, srv->kind, none_j, none_i, none_p, fin);
+                const cudaError_t fe = cudaStreamSynchronize(ctx.stream);
+                const uint64_t t_fin = now_ns();
+                for (uint64_t t : fin_tickets) {
+                    ServerJob& j = srv->jobs[t];
+                    if (fs != SOLRT_OK || fe != cudaSuccess) {
+                        j.state = kFailed;
+                        j.status = fs != SOLRT_OK ? fs : SOLRT_ERR_DEVICE;
+                        j.t_done = t_fin;
+                        continue;
+                    }
+                    j.state = kDone;
+                    j.status = SOLRT_OK;
+                    j.stopped_early = true;
+                    j.t_done = t_fin;
+                    j.last_use = t_fin;
+                    srv->done_lru.push_back(j.ticket);
+                    ++srv->st.completed;
+                    ++srv->st.stopped_early;
+                }
+            }
+        }
         srv->active.erase(std::remove_if(srv->active.begin(), srv->active.end(),
                                          [&](uint64_t t) { return srv->jobs[t].state != kActive; }),
                           srv->active.end());
@@ -291,6 +389,8 @@ void fill_result(const ServerJob& j, solrt_job_result* out) {
     out->latency_ns = j.t_done ? j.t_done - j.t_submit : 0;
     out->queue_ns = j.t_admit ? j.t_admit - j.t_submit : 0;
     out->image = j.image;
+    out->rmse_estimate = j.rmse_est;
+    out->stopped_early = j.stopped_early ? 1u : 0u;
 }
 
 }  // namespace
@@ -313,9 +413,18 @@ solrt_status solrt_server_create(solrt_context* ctx, const solrt_server_desc* de
     if (!srv) return SOLRT_ERR_OOM;
     srv->ctx = ctx;
     srv->budget = desc && desc->memory_budget ? desc->memory_budget : 150ull * 1000 * 1000 * 1000;
-    // default tick: 8M paths (tens of ms), so that short jobs finish within a few ticks
+    // a fixed tick size, or adaptive ticks starting at 8M paths
+    srv->adaptive = !(desc && desc->tick_paths);
     srv->tick_paths = desc && desc->tick_paths ? std::min(desc->tick_paths, ctx->capacity)
                                                : std::min(8u << 20, ctx->capacity);
+    srv->tick_ms = desc && desc->tick_ms ? (double)desc->tick_ms : 40.0;
+    if (desc && !(desc->stop_rmse >= 0.0f)) {
+        delete srv;
+        set_error("stop_rmse must be >= 0");
+        return SOLRT_ERR_INVALID;
+    }
+    srv->stop_rmse = desc ? desc->stop_rmse : 0.0f;
+    srv->stop_min_spp = desc && desc->stop_min_spp ? std::max(2u, desc->stop_min_spp) : 4u;
     srv->policy = desc ? desc->policy : (uint32_t)SOLRT_SERVE_FAIR;
     srv->inject_alloc_failures = desc ? desc->inject_alloc_failures : 0u;
     try {
@@ -499,8 +608,10 @@ solrt_status solrt_server_destroy(solrt_server* srv) {
     }
     srv->cv_work.notify_all();
     if (srv->th.joinable()) srv->th.join();
-    for (auto& kv : srv->jobs)
+    for (auto& kv : srv->jobs) {
         if (kv.second.image) solrt_image_destroy(kv.second.image);
+        if (kv.second.sq) cudaFree(kv.second.sq);
+    }
     delete srv;
     return SOLRT_OK;
 }

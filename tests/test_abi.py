@@ -37,12 +37,14 @@ def test_struct_sizes(solrt):
     assert ctypes.sizeof(api.Camera) == 256
     assert ctypes.sizeof(api.RenderParams) == 64
     assert solrt.RAY_DTYPE.itemsize == 32 and solrt.HIT_DTYPE.itemsize == 16
+    assert ctypes.sizeof(api.ServerDesc) == 32 and ctypes.sizeof(api.JobResult) == 40
+    assert ctypes.sizeof(api.ServerStats) == 88
     assert solrt.scenes.VERTEX_DTYPE.itemsize == 64 and solrt.scenes.INSTANCE_DTYPE.itemsize == 144
 
 
 def test_abi_version_and_status_strings(solrt):
     L = solrt.lib()
-    assert L.solrt_abi_version() == 2
+    assert L.solrt_abi_version() == 3
     assert L.solrt_status_string(0) == b"ok"
     assert L.solrt_status_string(5) == b"capacity exceeded"
 

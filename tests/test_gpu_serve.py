@@ -30,13 +30,18 @@ def _job(solrt, i):
     return int(rng.integers(0, 3)), solrt.render_params(w, h, **kw)
 
 
+@pytest.mark.parametrize("ticks", ["fixed", "adaptive"])
 @pytest.mark.parametrize("policy", [0, 1])
-def test_served_results_equal_alone(solrt, policy):
+def test_served_results_equal_alone(solrt, policy, ticks):
     ctx = solrt.Context(0)
     scenes = _scenes(solrt, ctx)
     datas = [S.cornell(), S.soup(20000, seed=2), S.tunnel(n_ang=128, n_ax=64, length=20.0)]
-    # small ticks: jobs span many ticks and overlap
-    srv = solrt.Server(ctx, tick_paths=3000, policy=policy)
+    # small ticks: jobs span many ticks and overlap (adaptive: ticks of about
+    # 1 ms of device time, resized after every tick)
+    if ticks == "fixed":
+        srv = solrt.Server(ctx, tick_paths=3000, policy=policy)
+    else:
+        srv = solrt.Server(ctx, tick_paths=0, tick_ms=1, policy=policy)
     tickets = []
     for i in range(24):
         si, p = _job(solrt, i)
@@ -231,3 +236,66 @@ def test_injected_allocation_failure(solrt):
         assert r.status == 0
     assert srv.stats().completed == 2
     srv.close()
+
+
+def _host_estimate(oracle, data, cam, p):
+    """The stopping rule's estimate recomputed on the host from the oracle's
+    per-sample radiance (FP64 sums): sqrt(mean over pixels of the variance
+    of the pixel mean summed over RGB / 3)."""
+    o = oracle.OracleScene(data)
+    x = o.render_samples(cam, p).astype(np.float64)[..., :3]      # pixels, samples, rgb
+    n = x.shape[1]
+    var = (np.sum(x * x, axis=(1, 2)) - np.sum(x.sum(1) ** 2, axis=1) / n) / (n - 1) / n
+    return float(np.sqrt(np.mean(np.maximum(var, 0.0)) / 3.0))
+
+
+@pytest.mark.parametrize("accum", ["mix", "kahan"])
+def test_stopping_rule(solrt, oracle, accum):
+    """With a loose bound every job stops once its estimated RMSE against
+    its converged image is below it: fewer samples than asked, the estimate
+    matches the host's recomputation from the oracle's samples, and the
+    image equals solrt_render of the same job with spp = the samples taken.
+    With a bound no image reaches, every job runs all of its samples."""
+    ctx = solrt.Context(0)
+    data = S.cornell()
+    sc = solrt.SceneDescription(ctx, data)
+    mode = solrt.ACCUM_KAHAN if accum == "kahan" else solrt.ACCUM_REF_MIX
+    jobs = []
+    for i, (w, h) in enumerate([(32, 32)] * 3):
+        p = solrt.render_params(w, h, spp=64, max_bounces=4, seed=11 + i, job_id=i, accum_mode=mode,
+                                material_mode=solrt.MATERIAL_LAMBERT, rng_mode=solrt.RNG_PER_SAMPLE)
+        jobs.append((camera_of(data, w / h), p))
+    # (on this box the estimate falls from about 0.44 after 4 samples to 0.12
+    # after 64, so a 0.2 bound stops the jobs midway)
+    for bound, early in ((0.2, True), (1e-9, False)):
+        # ticks of 4 samples per job while all three run: estimates after 4,
+        # 8, ... samples
+        srv = solrt.Server(ctx, tick_paths=3 * 32 * 32 * 4, stop_rmse=bound, stop_min_spp=4)
+        tickets = [srv.submit(sc, cam, p) for cam, p in jobs]
+        res = [srv.wait(t, 60000) for t in tickets]
+        imgs = [srv.read(t, r) for t, r in zip(tickets, res)]
+        st = srv.stats()
+        srv.close()
+        r_ = solrt.Renderer(ctx)
+        for (cam, p), r, (a32, _) in zip(jobs, res, imgs):
+            assert r.status == 0
+            assert r.rmse_estimate > 0
+            if early:
+                assert r.stopped_early == 1 and 4 <= r.spp_done < p.spp and r.rmse_estimate <= bound
+            else:
+                assert r.stopped_early == 0 and r.spp_done == p.spp and r.rmse_estimate > bound
+            q = solrt.RenderParams.from_buffer_copy(p)
+            q.spp = r.spp_done
+            if not early:   # the last estimate was taken before the last tick's samples
+                q.spp = r.spp_done - 4
+            want = _host_estimate(oracle, data, cam, q)
+            assert abs(r.rmse_estimate - want) <= 1e-3 * want, (r.rmse_estimate, want)
+            q.spp = r.spp_done
+            img = solrt.Image(ctx, p.width, p.height, mode)
+            r_.cmd_trace_rays(sc, cam, q, img)
+            b32, _ = img.read()
+            img.close()
+            assert np.array_equal(a32.view(np.uint32), b32.view(np.uint32))
+        assert st.stopped_early == (len(jobs) if early else 0)
+    sc.close()
+    ctx.close()
