@@ -41,11 +41,22 @@ METRIC = "Mrays/s at RMSE≤1e-3 vs FP64 oracle, batched vs plain on 1 GB300; p9
 UNIT = "Mrays/s"
 
 NODE_BYTES = {0: 64, 1: 80, 2: 64, 3: 224, 4: 32, 5: 64}
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per traced segment
-# of the BVH2 extend kernel on the default soup workload, from one ncu
-# capture of the last 15 k_extend launches of a timed frame (3 of its 4
-# passes, 15.24 GB for ~242.7M segments; one-pass metrics, full size).
-EXTEND_DRAM_BYTES_PER_SEGMENT_SOUP = 62.8
+# What ncu measured of the BVH2 extend kernel on the full-size workloads.
+# dram_bytes_per_segment: dram__bytes_read.sum + dram__bytes_write.sum over
+# all extend launches of one full wavefront pass, divided by the segments
+# the pass traced (profiles/extend_dram_soup1M_tunnel4M.md). limiter: the
+# counters of one `ncu --set full` launch (profiles/extend_soup1M_bvh2_full.md,
+# profiles/extend_tunnel_640x360_full.md).
+EXTEND_CAPTURES = {
+    "soup": {"dram_bytes_per_segment": 62.4, "dram_source": "profiles/extend_dram_soup1M_tunnel4M.md",
+             "limiter": {"l1tex_lsu_wavefronts_pct": 83.8, "l1tex_throughput_pct": 87.8, "issue_active_pct": 60.7,
+                         "threads_per_instruction": 14.27, "warps_active_pct": 48.0, "l2_hit_pct": 96.7,
+                         "dram_throughput_pct": 1.4, "source": "profiles/extend_soup1M_bvh2_full.md"}},
+    "tunnel": {"dram_bytes_per_segment": 78.8, "dram_source": "profiles/extend_dram_soup1M_tunnel4M.md",
+               "limiter": {"l1tex_lsu_wavefronts_pct": 61.8, "l1tex_throughput_pct": 71.0, "issue_active_pct": 58.0,
+                           "threads_per_instruction": 13.39, "warps_active_pct": 43.5, "l2_hit_pct": 91.6,
+                           "dram_throughput_pct": 2.2, "source": "profiles/extend_tunnel_640x360_full.md"}},
+}
 
 
 def workload(name):
@@ -508,7 +519,7 @@ def _params_dict(p):
             "accum_mode": p.accum_mode, "rng_mode": p.rng_mode}
 
 
-def run_batch(args, world, rank, local, pg, njobs=None, steps=None, emit=True):
+def run_batch(args, world, rank, local, pg, njobs=None, steps=None, emit=True, warmup=None):
     """Batched mixed scenes (256 randomised Cornell boxes with log-uniform
     1k-500k-triangle soups, 128^2..1024^2, 4-64 spp, depth 5): one CUDA-graph
     replay per step vs the same jobs rendered one solrt_render at a time,
@@ -520,6 +531,7 @@ def run_batch(args, world, rank, local, pg, njobs=None, steps=None, emit=True):
            "bvh8": solrt.BVH8_Q8, "bvh8f": solrt.BVH8_F32}[args.bvh]
     njobs = args.jobs if njobs is None else njobs
     steps = args.steps if steps is None else steps
+    warmup = args.warmup if warmup is None else warmup
     ctx = solrt.Context(local)
     jobs, tris, pixels, samples = [], 0, 0, 0
     t0 = time.perf_counter()
@@ -576,7 +588,7 @@ def run_batch(args, world, rank, local, pg, njobs=None, steps=None, emit=True):
         for (sc, img, cam, _), q in zip(jobs, mega_params):
             r.cmd_trace_rays(sc, cam, q, img)
 
-    for _ in range(args.warmup):
+    for _ in range(max(1, warmup)):
         batch.launch()
     plain_wavefront()
     plain_mega()
@@ -586,8 +598,13 @@ def run_batch(args, world, rank, local, pg, njobs=None, steps=None, emit=True):
         time.sleep(0.3)
     barrier(pg)
     ms_b, seg_b, launches_b = timed(batch.launch, steps)
-    ms_w, seg_w, _ = timed(plain_wavefront, 1)
-    ms_m, seg_m, _ = timed(plain_mega, 1)
+    ms_w, seg_w, launches_w = timed(plain_wavefront, 1)
+    ms_m, seg_m, launches_m = timed(plain_mega, 1)
+    # the same jobs in one persistent per-pixel launch (device work counter)
+    pbatch = solrt.Batch(ctx, jobs, persistent=True)
+    pbatch.launch()
+    ms_p, seg_p, launches_p = timed(pbatch.launch, 1)
+    pbatch.close()
     clk = clocks.stop() if clocks else None
     ms_b_max = max_over_ranks(pg, ms_b)
     value = sum_over_ranks(pg, float(seg_b)) / (ms_b_max / 1000.0) / 1e6
@@ -597,7 +614,12 @@ def run_batch(args, world, rank, local, pg, njobs=None, steps=None, emit=True):
            "ratio": round(value / plain_v, 3) if plain_v > 0 else None,
            "wavefront_scene_by_scene": round(wave_v, 3),
            "ratio_vs_wavefront": round(value / wave_v, 3) if wave_v > 0 else None,
-           "batch_ms": round(ms_b_max / steps, 3), "passes": info["passes"],
+           "persistent_one_launch": round(seg_p / (ms_p / 1000.0) / 1e6, 3),
+           "batch_ms": round(ms_b_max / steps, 3), "passes": info["passes"], "items": info["items"],
+           "pass_fill": round(info["paths"] / max(1, info["passes"] * ctx.capacity()), 3),
+           "launches_per_step": {"batched": int(launches_b // steps), "wavefront_scene_by_scene": int(launches_w),
+                                 "megakernel_scene_by_scene": int(launches_m), "persistent_one_launch": int(launches_p)},
+           "tris": int(tris), "pixels": int(pixels), "samples": int(samples), "setup_s": round(setup_s, 1),
            "autotune": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in tune.items()}}
     if rank == 0 and emit:
         out = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": steps,
@@ -620,12 +642,16 @@ def run_batch(args, world, rank, local, pg, njobs=None, steps=None, emit=True):
     return cmp
 
 
-def run_serve(local, rate, duration, n_scenes=16, seed=5, policy=0):
+def run_serve(local, rate, duration, n_scenes=16, seed=5, policy=0, stop_rmse=0.0, drain_s=300.0):
     """Served render jobs: Poisson arrivals at `rate` jobs/s for `duration`
     seconds; each job draws a scene from a resident pool of config-4 scenes
     (randomised Cornell box + log-uniform soup), a resolution from
-    {128^2, 256^2, 512^2, 1024^2}, spp uniform 1..256, depth 5. Returns
-    p50 / p99 job latency, sustained Mrays/s and admission-queue depth."""
+    {128^2, 256^2, 512^2, 1024^2}, spp uniform 1..256, depth 5. With
+    stop_rmse > 0 the server's stopping rule ends a job once its estimated
+    RMSE against its converged image is at most that. Jobs still unfinished
+    drain_s seconds after the last arrival are cancelled and counted.
+    Returns p50 / p99 job latency of the completed jobs, the throughput over
+    the arrival window and over the whole run, and admission-queue depth."""
     solrt = importlib.import_module("sol-rs_gb300")
     S = solrt.scenes
     ctx = solrt.Context(local)
@@ -633,7 +659,7 @@ def run_serve(local, rate, duration, n_scenes=16, seed=5, policy=0):
     c = S.CORNELL_CAMERA
     cam = solrt.camera_look_at(c["eye"], c["center"], c["up"], c["vfov"], 1.0)
     rng = np.random.default_rng(seed)
-    srv = solrt.Server(ctx, policy=policy)
+    srv = solrt.Server(ctx, policy=policy, stop_rmse=stop_rmse)
     arrivals = []
     t = 0.0
     while True:
@@ -643,15 +669,21 @@ def run_serve(local, rate, duration, n_scenes=16, seed=5, policy=0):
         res = int(rng.choice([128, 256, 512, 1024]))
         arrivals.append((t, int(rng.integers(0, n_scenes)), res, int(rng.integers(1, 257))))
     ctx.reset_stats()
-    pending, lat, qdepth, paths = {}, [], [], 0
+    pending, lat, qdepth, paths, est, early, spp_frac = {}, [], [], 0, [], 0, []
     t0 = time.perf_counter()
     i = 0
+    seg_window = None
 
     def drain():
+        nonlocal early
         for tk in list(pending):
-            s, r = srv.poll(tk)
-            if s == 0:
+            st_, r = srv.poll(tk)
+            if st_ == 0:
                 lat.append(r.latency_ns / 1e6)
+                if r.rmse_estimate >= 0:
+                    est.append(r.rmse_estimate)
+                early += int(r.stopped_early)
+                spp_frac.append(r.spp_done / pending[tk][1])
                 srv.release(tk)
                 del pending[tk]
 
@@ -661,15 +693,20 @@ def run_serve(local, rate, duration, n_scenes=16, seed=5, policy=0):
             _, si, res, spp = arrivals[i]
             p = solrt.render_params(res, res, spp=spp, max_bounces=5, seed=seed + i, job_id=i,
                                     material_mode=solrt.MATERIAL_LAMBERT, rng_mode=solrt.RNG_PER_SAMPLE)
-            pending[srv.submit(pool[si], cam, p)] = i
+            pending[srv.submit(pool[si], cam, p)] = (i, spp)
             paths += res * res * spp
             i += 1
+        if seg_window is None and now >= duration:
+            seg_window = srv.stats().segments
         qdepth.append(srv.stats().queue_depth)
         drain()
-        if now > duration + 300:
+        if now > duration + drain_s:
             break
         time.sleep(0.002)
     wall = time.perf_counter() - t0
+    unfinished = len(pending)
+    for tk in list(pending):
+        srv.cancel(tk)
     st = srv.stats()
     srv.close()
     for sc in pool:
@@ -677,15 +714,28 @@ def run_serve(local, rate, duration, n_scenes=16, seed=5, policy=0):
     seg = ctx.stats().segments
     ctx.close()
     lat = np.array(lat) if lat else np.zeros(1)
-    return {"rate_jobs_per_s": rate, "duration_s": duration, "policy": ["fair", "shortest_first"][policy],
-            "jobs": len(arrivals), "completed": int(st.completed),
-            "p50_latency_ms": round(float(np.percentile(lat, 50)), 2),
-            "p99_latency_ms": round(float(np.percentile(lat, 99)), 2),
-            "sustained_mrays_s": round(seg / wall / 1e6, 2), "wall_s": round(wall, 2),
-            "busy_fraction": round(st.busy_ms / 1000.0 / wall, 3),
-            "max_queue_depth": int(max(qdepth) if qdepth else 0),
-            "mean_queue_depth": round(float(np.mean(qdepth)) if qdepth else 0.0, 2),
-            "paths_submitted": int(paths), "ticks": int(st.ticks)}
+    out = {"rate_jobs_per_s": rate, "duration_s": duration, "policy": ["fair", "shortest_first"][policy],
+           "jobs": len(arrivals), "completed": int(len(arrivals) - unfinished),
+           "unfinished_cancelled": int(unfinished), "drain_cap_s": drain_s,
+           "p50_latency_ms": round(float(np.percentile(lat, 50)), 2),
+           "p99_latency_ms": round(float(np.percentile(lat, 99)), 2),
+           "latency_of": "completed jobs",
+           "sustained_mrays_s": round(seg / wall / 1e6, 2),
+           "window_mrays_s": round((seg_window if seg_window is not None else seg) / min(wall, duration) / 1e6, 2),
+           "wall_s": round(wall, 2),
+           "busy_fraction": round(st.busy_ms / 1000.0 / wall, 3),
+           "max_queue_depth": int(max(qdepth) if qdepth else 0),
+           "mean_queue_depth": round(float(np.mean(qdepth)) if qdepth else 0.0, 2),
+           "paths_submitted": int(paths), "ticks": int(st.ticks), "last_tick_paths": int(st.tick_paths),
+           "tick_size": "adaptive (about 40 ms of device time each)"}
+    if stop_rmse > 0:
+        out["stop"] = {"rule": "rmse", "bound": stop_rmse, "stopped_early": int(early),
+                       "rmse_estimate_median": round(float(np.median(est)), 5) if est else None,
+                       "rmse_estimate_min": round(float(np.min(est)), 5) if est else None,
+                       "spp_done_over_spp_median": round(float(np.median(spp_frac)), 3) if spp_frac else None,
+                       "how": "per job, after each tick: sqrt(mean over pixels and RGB of the sample variance / "
+                              "samples), from per-pixel sums and squared sums on the device"}
+    return out
 
 
 def run_reference(args, world, rank, pg):
@@ -758,8 +808,12 @@ def main():
     ap.add_argument("--nee", action="store_true",
                     help="next-event estimation (shadow-ray queue); shadow rays are reported apart from the metric")
     ap.add_argument("--jobs", type=int, default=256)
-    ap.add_argument("--rate", type=float, default=6.0, help="serve: Poisson arrival rate, jobs/s")
-    ap.add_argument("--duration", type=float, default=8.0, help="serve: arrival window, s")
+    ap.add_argument("--rate", type=float, default=50.0, help="serve: Poisson arrival rate, jobs/s")
+    ap.add_argument("--duration", type=float, default=60.0, help="serve: arrival window, s")
+    ap.add_argument("--drain", type=float, default=30.0,
+                    help="serve: seconds after the last arrival before unfinished jobs are cancelled")
+    ap.add_argument("--stop-rmse", type=float, default=1e-3,
+                    help="serve: stopping rule, estimated RMSE against the converged image (0 = run every sample)")
     ap.add_argument("--policy", default="shortest", choices=["fair", "shortest"], help="serve: scheduling policy")
     ap.add_argument("--no-serve", action="store_true", help="skip the short serving run of the default line")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -780,7 +834,8 @@ def main():
         return 0
     if args.workload == "serve":
         importlib.import_module("sol-rs_gb300.build").build_lib()
-        out = run_serve(local, args.rate, args.duration, policy=1 if args.policy == "shortest" else 0)
+        out = run_serve(local, args.rate, args.duration, policy=1 if args.policy == "shortest" else 0,
+                        stop_rmse=args.stop_rmse, drain_s=args.drain)
         if rank == 0:
             print(json.dumps({"metric": "p99 job latency (served render jobs)", "value": out["p99_latency_ms"],
                               "unit": "ms", "higher_is_better": False, "n_gpus": world, "serving": out}), flush=True)
@@ -911,14 +966,22 @@ def main():
         ext_s = ms / 1000.0
     # extend launches also trace the shadow rays of --nee (same bytes per ray assumed)
     achieved = ((st.segments + st.shadow_segments) * b_seg) / ext_s / 1e9 if ext_s > 0 else 0.0
-    traffic = None
-    if args.workload == "soup" and info.kind == solrt.BVH2 and not (args.width or args.height or args.spp):
+    traffic = dram = None
+    cap = EXTEND_CAPTURES.get(args.workload)
+    if cap and info.kind == solrt.BVH2 and args.kernel != "mega" and not args.nee and ext_s > 0:
         seg_per_launch = st.segments / max(st.extend_launches, 1)
-        traffic = round(EXTEND_DRAM_BYTES_PER_SEGMENT_SOUP * seg_per_launch)
+        traffic = round(cap["dram_bytes_per_segment"] * seg_per_launch)
+        dram_gbs = cap["dram_bytes_per_segment"] * st.segments / ext_s / 1e9
+        dram = {"bytes_per_segment": cap["dram_bytes_per_segment"], "gbs": round(dram_gbs, 1),
+                "frac": round(dram_gbs / peak, 4), "source": cap["dram_source"],
+                "how": "ncu DRAM bytes per segment of this workload's extend launches x this run's segments / "
+                       "this run's extend time"}
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": traffic,
-                "traffic_note": "DRAM bytes per launch from an ncu capture of this workload (62.8 B per segment); "
-                                "the algorithmic bytes are mostly served by L1 / L2" if traffic else None,
+                "frac_note": "achieved counts algorithmic bytes (node, triangle, ray and hit bytes of every visit) "
+                             "with no cache reuse; L1 / L2 serve nearly all of them, so frac > 1 is not HBM "
+                             "traffic: dram is what reaches HBM, limiter what binds" if cap else None,
+                "dram": dram, "limiter": cap["limiter"] if (cap and dram) else None,
                 "peak_source": peak_kind + " (MEASURED_PEAKS hbm_gbs)",
                 "kernel": "k_megakernel (traversal + shading, whole render time)" if args.kernel == "mega"
                           else "k_extend (BVH traversal)", "bytes_per_segment": round(b_seg, 1),
@@ -979,11 +1042,14 @@ def main():
     batched = serving = None
     if args.workload == "soup" and not args.no_serve:
         try:
-            batched = run_batch(args, world, rank, local, pg, njobs=32, steps=2, emit=False)
-            serving = run_serve(local, args.rate, args.duration, policy=1 if args.policy == "shortest" else 0)
+            batched = run_batch(args, world, rank, local, pg, njobs=args.jobs, steps=1, emit=False, warmup=1)
         except Exception as ex:
-            batched = batched or {"error": str(ex)}
-            serving = serving or {"error": str(ex)}
+            batched = {"error": str(ex)}
+        try:
+            serving = run_serve(local, args.rate, args.duration, policy=1 if args.policy == "shortest" else 0,
+                                stop_rmse=args.stop_rmse, drain_s=args.drain)
+        except Exception as ex:
+            serving = {"error": str(ex)}
     out = None
     if rank == 0:
         cpu = None

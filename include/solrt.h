@@ -446,7 +446,13 @@ typedef struct solrt_job {
 typedef struct solrt_batch solrt_batch;
 
 enum {
-    SOLRT_BATCH_GRAPH = 1u  /* capture the batch's launches once into a CUDA graph and replay it */
+    SOLRT_BATCH_GRAPH = 1u,      /* capture the batch's launches once into a CUDA graph and replay it */
+    /* one persistent launch per step instead of wavefront passes: warps take
+     * 32 pixels at a time of all jobs' pixels from a device work counter and
+     * each thread traces all samples of its pixel to the end (the per-pixel
+     * structure of the reference's raygen loop); same images. Path
+     * integrator only (no next-event estimation). */
+    SOLRT_BATCH_PERSISTENT = 2u
 };
 
 /* Plans a batch: the paths of all jobs share the wavefront queues, each pass

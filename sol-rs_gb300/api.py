@@ -99,6 +99,7 @@ class Job(ctypes.Structure):
 
 
 BATCH_GRAPH = 1
+BATCH_PERSISTENT = 2
 SERVE_FAIR, SERVE_SHORTEST_FIRST = 0, 1
 
 
@@ -257,6 +258,11 @@ class Context:
         h = ctypes.c_void_p()
         check(lib().solrt_context_create(ctypes.byref(d), ctypes.byref(h)))
         self.handle = h
+        self._capacity = path_capacity or (32 << 20)   # the library's default (solrt_context_desc)
+
+    def capacity(self):
+        """Paths in flight per pass."""
+        return self._capacity
 
     def close(self):
         if getattr(self, "handle", None):
@@ -522,12 +528,15 @@ class Batch:
     """Many render jobs over many scenes in shared wavefront passes
     (solrt_batch); each job's image equals rendering it alone."""
 
-    def __init__(self, context, jobs, graph=False):
+    def __init__(self, context, jobs, graph=False, persistent=False):
+        """graph: replay one captured CUDA graph per launch; persistent: one
+        persistent per-pixel launch over all jobs instead of wavefront passes."""
         self.context = context
         self._keep = list(jobs)
         arr = make_jobs(jobs)
         h = ctypes.c_void_p()
-        check(lib().solrt_batch_create(context.handle, arr, len(jobs), BATCH_GRAPH if graph else 0, ctypes.byref(h)))
+        flags = (BATCH_GRAPH if graph else 0) | (BATCH_PERSISTENT if persistent else 0)
+        check(lib().solrt_batch_create(context.handle, arr, len(jobs), flags, ctypes.byref(h)))
         self.handle = h
 
     def close(self):

@@ -273,6 +273,70 @@ __global__ void k_rmse_estimate(const DevJob* __restrict__ jobs, const uint32_t*
 #ifndef SOLRT_MEGA_MINB
 #define SOLRT_MEGA_MINB 8
 #endif
+__device__ __forceinline__ void flush_stats(DevStats* stats, uint32_t segs, uint32_t paths, uint32_t fb,
+                                            uint32_t ef) {
+    const uint32_t wsegs = __reduce_add_sync(0xffffffffu, segs);
+    const uint32_t wpaths = __reduce_add_sync(0xffffffffu, paths);
+    const uint32_t wfb = __reduce_add_sync(0xffffffffu, fb);
+    const uint32_t wef = __reduce_or_sync(0xffffffffu, ef);
+    if ((threadIdx.x & 31) == 0) {
+        if (wsegs) atomicAdd(&stats->segments, (unsigned long long)wsegs);
+        if (wpaths) atomicAdd(&stats->paths, (unsigned long long)wpaths);
+        if (wfb) atomicAdd(&stats->fp64_fallbacks, (unsigned long long)wfb);
+        if (wef) atomicOr(&stats->eflags, wef);
+    }
+}
+
+// All samples of pixel `pix` of job J, each path traced and shaded to its
+// end by this thread; the pixel's sums are written once (the body of
+// k_megakernel's per-pixel loop, for the persistent batch launch).
+template <int KIND>
+__device__ __forceinline__ void mega_pixel(const DevJob& J, uint32_t pix, uint32_t& segs, TraceCounters& cnt,
+                                           uint32_t& ef) {
+    const TravScene ts = trav_scene(J.sc);
+    f3 s{0.0f, 0.0f, 0.0f}, ks{0.0f, 0.0f, 0.0f}, kc{0.0f, 0.0f, 0.0f};
+    float kn = 0.0f;
+    if (J.accum_mode == SOLRT_ACCUM_KAHAN) {
+        const float4 s4 = J.ksum[pix], c4 = J.kcomp[pix];
+        ks = f3{s4.x, s4.y, s4.z};
+        kc = f3{c4.x, c4.y, c4.z};
+        kn = s4.w;
+    }
+    uint32_t rng = 0;
+    for (uint32_t smp = 0; smp < J.spp; ++smp) {
+        rng = sample_seed(J, pix, smp, rng);
+        float4 o, d;
+        camera_ray(J, pix, rng, o, d);
+        f3 acc{1.0f, 1.0f, 1.0f};
+        uint32_t depth = 0;
+        for (;;) {
+            HitRec h;
+            if (KIND == SOLRT_BVH8_Q8) trace_bvh8<false>(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, ef);
+            else if (KIND == SOLRT_BVH8_F32) trace_bvh8<false, true>(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, ef);
+            else if (KIND == SOLRT_BVH4_Q8) trace_bvh4_ray(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, ef);
+            else if (KIND == SOLRT_BVH2_Q16) trace_bvh2_ray<true>(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, ef);
+            else if (KIND == SOLRT_BVH2_TWO_LEVEL) trace_bvh2_2l_ray(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, ef);
+            else trace_bvh2_ray(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, ef);
+            ++segs;
+            float4 on, dn;
+            if (!shade_step(J, o, d, make_float4(h.t, __uint_as_float(h.prim), h.u, h.v), acc, rng, depth, on, dn,
+                            ef))
+                break;
+            o = on;
+            d = dn;
+        }
+        const float4 c = make_float4(acc.x, acc.y, acc.z, 0.0f);
+        if (J.accum_mode == SOLRT_ACCUM_KAHAN) add_sample_kahan(ks, kc, kn, c);
+        else add_sample(s, c);
+    }
+    if (J.accum_mode == SOLRT_ACCUM_KAHAN) {
+        J.ksum[pix] = make_float4(ks.x, ks.y, ks.z, kn);
+        J.kcomp[pix] = make_float4(kc.x, kc.y, kc.z, 0.0f);
+    } else {
+        J.fsum[pix] = make_float4(s.x, s.y, s.z, 0.0f);
+    }
+}
+
 template <int KIND>
 __global__ void __launch_bounds__(128, SOLRT_MEGA_MINB) k_megakernel(const DevJob* __restrict__ job, DevStats* stats) {
     const DevJob& J = *job;
@@ -336,6 +400,34 @@ __global__ void __launch_bounds__(128, SOLRT_MEGA_MINB) k_megakernel(const DevJo
     }
 }
 
+// The persistent multi-scene launch: one grid of (SMs x resident blocks)
+// whose warps take 32 consecutive pixels of the batch's pixel space (all
+// jobs, job after job) from an atomic work counter until it passes the end;
+// each lane renders all samples of its pixel (mega_pixel). No thread waits
+// on another, so nothing needs a bounded wait.
+template <int KIND>
+__global__ void __launch_bounds__(128, SOLRT_MEGA_MINB)
+    k_megakernel_batch(const DevJob* __restrict__ jobs, const uint32_t* __restrict__ job_pix, uint32_t njobs,
+                       uint32_t total_pix, unsigned int* __restrict__ work, DevStats* stats) {
+    const int lane = threadIdx.x & 31;
+    uint32_t segs = 0, paths = 0, ef = 0;
+    TraceCounters cnt{0, 0, 0};
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(work, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= total_pix) break;
+        const uint32_t t = base + (uint32_t)lane;
+        if (t < total_pix) {
+            const uint32_t j = find_last_le(njobs, t, [&](uint32_t i) { return job_pix[i]; });
+            mega_pixel<KIND>(jobs[j], t - job_pix[j], segs, cnt, ef);
+            paths += jobs[j].spp;
+        }
+        __syncwarp();
+    }
+    flush_stats(stats, segs, paths, cnt.fallbacks, ef);
+}
+
 // Zeroes the per-frame sample sums of running-mix jobs.
 __global__ void k_begin(const DevJob* __restrict__ jobs, const uint32_t* __restrict__ job_pix, uint32_t njobs,
                         uint32_t pixels) {
@@ -378,20 +470,6 @@ __device__ __forceinline__ void trace_one(const TravScene& ts, float ox, float o
     else if (KIND == SOLRT_BVH2_Q16) trace_bvh2_ray<true>(ts, ox, oy, oz, dx, dy, dz, tmin, tmax, h, cnt, ef);
     else if (KIND == SOLRT_BVH2_TWO_LEVEL) trace_bvh2_2l_ray(ts, ox, oy, oz, dx, dy, dz, tmin, tmax, h, cnt, ef);
     else trace_bvh2_ray(ts, ox, oy, oz, dx, dy, dz, tmin, tmax, h, cnt, ef);
-}
-
-__device__ __forceinline__ void flush_stats(DevStats* stats, uint32_t segs, uint32_t paths, uint32_t fb,
-                                            uint32_t ef) {
-    const uint32_t wsegs = __reduce_add_sync(0xffffffffu, segs);
-    const uint32_t wpaths = __reduce_add_sync(0xffffffffu, paths);
-    const uint32_t wfb = __reduce_add_sync(0xffffffffu, fb);
-    const uint32_t wef = __reduce_or_sync(0xffffffffu, ef);
-    if ((threadIdx.x & 31) == 0) {
-        if (wsegs) atomicAdd(&stats->segments, (unsigned long long)wsegs);
-        if (wpaths) atomicAdd(&stats->paths, (unsigned long long)wpaths);
-        if (wfb) atomicAdd(&stats->fp64_fallbacks, (unsigned long long)wfb);
-        if (wef) atomicOr(&stats->eflags, wef);
-    }
 }
 
 // debug.rgen:18-36, debug.rchit:9-13, debug.rmiss: barycentrics of the
@@ -682,6 +760,18 @@ solrt_status issue_pass(Context& ctx, uint32_t kind, const DevJob* dj, const Dev
 }
 
 // Issues the batch's launches on the context stream.
+// The persistent launch of a SOLRT_BATCH_PERSISTENT batch: a grid of (SMs x
+// resident blocks) of k_megakernel_batch over the batch's pixels.
+template <int KIND>
+void launch_mega_batch(Context& ctx, const DevJob* dj, const uint32_t* jp, uint32_t njobs, uint32_t total_pix,
+                       unsigned int* work) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_megakernel_batch<KIND>, 128, 0);
+    const uint32_t grid = std::min<uint32_t>((uint32_t)ctx.sm_count * (uint32_t)std::max(per_sm, 1),
+                                             cdiv(total_pix, 128u));
+    k_megakernel_batch<KIND><<<grid, 128, 0, ctx.stream>>>(dj, jp, njobs, total_pix, work, ctx.stats.as<DevStats>());
+}
+
 solrt_status batch_issue(Batch& b, bool record_timing) {
     Context& ctx = *b.ctx;
     cudaStream_t st = ctx.stream;
@@ -690,6 +780,25 @@ solrt_status batch_issue(Batch& b, bool record_timing) {
     const uint32_t* jp = b.d_job_pix.as<uint32_t>();
     const uint32_t njobs = (uint32_t)b.jobs.size();
     const uint32_t total_pix = b.job_pix_base[njobs];
+    if (b.flags & SOLRT_BATCH_PERSISTENT) {
+        unsigned int* work = ctx.trace_work.as<unsigned int>();
+        SOLRT_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned int), st));
+        const int tm = record_timing ? ctx.timing_begin(0) : -1;  // traversal and shading in one launch
+        if (b.kind == SOLRT_BVH8_Q8) launch_mega_batch<SOLRT_BVH8_Q8>(ctx, dj, jp, njobs, total_pix, work);
+        else if (b.kind == SOLRT_BVH4_Q8) launch_mega_batch<SOLRT_BVH4_Q8>(ctx, dj, jp, njobs, total_pix, work);
+        else if (b.kind == SOLRT_BVH8_F32) launch_mega_batch<SOLRT_BVH8_F32>(ctx, dj, jp, njobs, total_pix, work);
+        else if (b.kind == SOLRT_BVH2_Q16) launch_mega_batch<SOLRT_BVH2_Q16>(ctx, dj, jp, njobs, total_pix, work);
+        else if (b.kind == SOLRT_BVH2_TWO_LEVEL)
+            launch_mega_batch<SOLRT_BVH2_TWO_LEVEL>(ctx, dj, jp, njobs, total_pix, work);
+        else launch_mega_batch<SOLRT_BVH2>(ctx, dj, jp, njobs, total_pix, work);
+        ctx.timing_end(tm);
+        const int tf = record_timing ? ctx.timing_begin(3) : -1;
+        k_finalize<<<cdiv(total_pix, 256), 256, 0, st>>>(dj, jp, njobs, total_pix);
+        ctx.timing_end(tf);
+        ctx.launches += 2;
+        SOLRT_CUDA(cudaGetLastError());
+        return SOLRT_OK;
+    }
     const int tb = record_timing ? ctx.timing_begin(3) : -1;
     k_begin<<<cdiv(total_pix, 256), 256, 0, st>>>(dj, jp, njobs, total_pix);
     ctx.timing_end(tb);
@@ -729,6 +838,10 @@ solrt_status batch_plan(Context& ctx, const solrt_job* jobs, uint32_t n, uint32_
             set_error("job %u: batches run the path integrators", j);
             return SOLRT_ERR_INVALID;
         }
+        if (jb.params.integrator == SOLRT_INTEGRATOR_PATH_NEE && (flags & SOLRT_BATCH_PERSISTENT)) {
+            set_error("job %u: persistent batches run the path integrator without next-event estimation", j);
+            return SOLRT_ERR_INVALID;
+        }
         if (jb.params.integrator == SOLRT_INTEGRATOR_PATH_NEE) SOLRT_TRY(ensure_shadow_queue(ctx));
         if (j == 0) b.kind = sc.info.kind;
         if (sc.info.kind != b.kind) { set_error("job %u: all scenes of a batch need the same BVH kind", j); return SOLRT_ERR_INVALID; }
@@ -736,6 +849,17 @@ solrt_status batch_plan(Context& ctx, const solrt_job* jobs, uint32_t n, uint32_
         const uint64_t np = (uint64_t)jb.params.width * jb.params.height;
         if (b.job_pix_base.back() + np >= (1ull << 31)) { set_error("batch has too many pixels"); return SOLRT_ERR_CAPACITY; }
         b.job_pix_base.push_back(b.job_pix_base.back() + (uint32_t)np);
+    }
+    if (flags & SOLRT_BATCH_PERSISTENT) {  // no passes: one launch over all pixels
+        for (const DevJob& J : b.jobs) b.total_paths += (uint64_t)J.width * J.height * J.spp;
+        SOLRT_TRY(b.d_jobs.alloc(sizeof(DevJob) * b.jobs.size()));
+        SOLRT_TRY(b.d_items.alloc(sizeof(DevItem)));
+        SOLRT_TRY(b.d_job_pix.alloc(sizeof(uint32_t) * b.job_pix_base.size()));
+        SOLRT_CUDA(cudaMemcpyAsync(b.d_jobs.ptr, b.jobs.data(), sizeof(DevJob) * b.jobs.size(), cudaMemcpyHostToDevice,
+                                   ctx.stream));
+        SOLRT_CUDA(cudaMemcpyAsync(b.d_job_pix.ptr, b.job_pix_base.data(), sizeof(uint32_t) * b.job_pix_base.size(),
+                                   cudaMemcpyHostToDevice, ctx.stream));
+        return SOLRT_OK;
     }
     // work items, round-robin over jobs so that passes mix jobs
     struct Chunk { uint32_t job, pix0, npix, k, spp; };
@@ -746,40 +870,51 @@ solrt_status batch_plan(Context& ctx, const solrt_job* jobs, uint32_t n, uint32_
         const uint32_t k = J.rng_mode == SOLRT_RNG_REF_STREAM ? 1u : std::max(1u, std::min(J.spp, cap / std::max(np, 1u)));
         for (uint32_t p0 = 0; p0 < np; p0 += cap) chunks.push_back(Chunk{j, p0, std::min(cap, np - p0), k, J.spp});
     }
-    std::vector<DevItem> order;
-    for (uint32_t round = 0;; ++round) {
-        bool any = false;
-        for (const Chunk& c : chunks) {
-            const uint64_t s0 = (uint64_t)round * c.k;
-            if (s0 >= c.spp) continue;
-            any = true;
-            order.push_back(DevItem{c.job, c.pix0, c.npix, (uint32_t)s0, std::min(c.k, c.spp - (uint32_t)s0), 0, 0, 0});
-        }
-        if (!any) break;
-    }
-    PassPlan cur{0, 0, 0, 0, 0};
-    auto close_pass = [&]() {
-        if (cur.item_count) b.passes.push_back(cur);
-        cur = PassPlan{(uint32_t)b.items.size(), 0, 0, 0, 0};
+    // Passes are filled first fit: round r of every chunk (its samples
+    // [r k, r k + k)), largest items first, goes to the first pass after the
+    // pass of the chunk's round r - 1 that has room, so a pixel's samples are
+    // still accumulated in order and passes run close to the capacity.
+    struct Bin {
+        PassPlan plan;
+        std::vector<DevItem> items;
     };
-    for (const DevItem& it0 : order) {
-        const uint64_t paths = (uint64_t)it0.npix * it0.k;
-        bool conflict = false;
-        for (uint32_t t = cur.item_begin; t < cur.item_begin + cur.item_count; ++t)
-            if (b.items[t].job == it0.job && b.items[t].pix0 == it0.pix0) conflict = true;
-        if (conflict || cur.paths + paths > cap) close_pass();
-        DevItem it = it0;
-        it.path_base = cur.paths;
-        it.pix_base = cur.pixels;
-        b.items.push_back(it);
-        cur.item_count += 1;
-        cur.paths += (uint32_t)paths;
-        cur.pixels += it.npix;
-        cur.bounces = std::max(cur.bounces, b.jobs[it.job].max_bounces + 1u);
-        if (b.jobs[it.job].integrator == SOLRT_INTEGRATOR_PATH_NEE) cur.nee = 1u;
-        b.total_paths += paths;
+    std::vector<Bin> bins;
+    std::vector<int64_t> last(chunks.size(), -1);
+    std::vector<uint32_t> live;
+    for (uint32_t round = 0;; ++round) {
+        live.clear();
+        for (uint32_t c = 0; c < (uint32_t)chunks.size(); ++c)
+            if ((uint64_t)round * chunks[c].k < chunks[c].spp) live.push_back(c);
+        if (live.empty()) break;
+        auto paths_of = [&](uint32_t c) {
+            const uint32_t s0 = round * chunks[c].k;
+            return (uint64_t)chunks[c].npix * std::min(chunks[c].k, chunks[c].spp - s0);
+        };
+        std::stable_sort(live.begin(), live.end(), [&](uint32_t a, uint32_t b2) { return paths_of(a) > paths_of(b2); });
+        for (uint32_t c : live) {
+            const Chunk& ch = chunks[c];
+            const uint32_t s0 = round * ch.k;
+            const uint64_t paths = paths_of(c);
+            size_t p = (size_t)(last[c] + 1);
+            while (p < bins.size() && bins[p].plan.paths + paths > cap) ++p;
+            if (p == bins.size()) bins.push_back(Bin{PassPlan{0, 0, 0, 0, 0}, {}});
+            Bin& bn = bins[p];
+            DevItem it{ch.job, ch.pix0, ch.npix, s0, std::min(ch.k, ch.spp - s0), bn.plan.paths, bn.plan.pixels, 0};
+            bn.items.push_back(it);
+            bn.plan.item_count += 1;
+            bn.plan.paths += (uint32_t)paths;
+            bn.plan.pixels += it.npix;
+            bn.plan.bounces = std::max(bn.plan.bounces, b.jobs[it.job].max_bounces + 1u);
+            if (b.jobs[it.job].integrator == SOLRT_INTEGRATOR_PATH_NEE) bn.plan.nee = 1u;
+            b.total_paths += paths;
+            last[c] = (int64_t)p;
+        }
     }
-    close_pass();
+    for (Bin& bn : bins) {
+        bn.plan.item_begin = (uint32_t)b.items.size();
+        b.items.insert(b.items.end(), bn.items.begin(), bn.items.end());
+        b.passes.push_back(bn.plan);
+    }
     SOLRT_TRY(b.d_jobs.alloc(sizeof(DevJob) * b.jobs.size()));
     SOLRT_TRY(b.d_items.alloc(sizeof(DevItem) * b.items.size()));
     SOLRT_TRY(b.d_job_pix.alloc(sizeof(uint32_t) * b.job_pix_base.size()));

@@ -186,3 +186,38 @@ def test_every_tune_config_renders_the_same(solrt):
     with pytest.raises(solrt.SolrtError):
         c.set_tune(128, 32, 1 << 20)
     c.close()
+
+
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh2t", "bvh8"])
+def test_persistent_batch_equals_alone(solrt, ctx, bvh):
+    """SOLRT_BATCH_PERSISTENT: all jobs in one persistent per-pixel launch
+    (warps take pixels from a device work counter, each thread traces its
+    pixel's samples to the end) render every job's image bit for bit as
+    solrt_render of that job alone; two launches accumulate two frames. Jobs
+    with next-event estimation are refused."""
+    kind = bvh_kind(solrt, bvh)
+    jobs = [j for j, (_, _, _, kw) in zip(_make(solrt, ctx, kind), _specs(solrt))
+            if kw.get("integrator", solrt.INTEGRATOR_PATH) == solrt.INTEGRATOR_PATH]
+    batch = solrt.Batch(ctx, jobs, persistent=True)
+    ctx.reset_stats()
+    batch.launch()
+    upd = []
+    for sc, img, cam, p in jobs:
+        q = solrt.RenderParams.from_buffer_copy(p)
+        q.frame = 1
+        upd.append((sc, img, cam, q))
+    batch.update(upd)
+    batch.launch()
+    ctx.synchronize()
+    st = ctx.stats()
+    assert st.error_flags == 0 and st.launches <= 2 * 2
+    got = [img.read() for _, img, _, _ in jobs]
+    want = _alone(solrt, ctx, jobs, frames=2)
+    for (a32, a8), (b32, b8) in zip(got, want):
+        assert np.array_equal(a32.view(np.uint32), b32.view(np.uint32))
+        assert np.array_equal(a8, b8)
+    batch.close()
+    nee = [j for j, (_, _, _, kw) in zip(_make(solrt, ctx, kind), _specs(solrt))
+           if kw.get("integrator", solrt.INTEGRATOR_PATH) == solrt.INTEGRATOR_PATH_NEE]
+    with pytest.raises(solrt.SolrtError):
+        solrt.Batch(ctx, nee, persistent=True)
