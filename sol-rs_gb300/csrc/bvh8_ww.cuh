@@ -26,11 +26,33 @@ namespace solrt {
 #define SOLRT_BVH8_NODE_MIN 12
 #endif
 
-template <class IO, bool kCount, bool kF32 = false>
+// Per-thread stack of node groups: entries [0, kSmem) in shared memory
+// (slot-major, one column per thread), the rest in local memory.
+template <int kBlock, int kSmem>
+struct Bvh8Stack {
+    uint2* sh;  // entry k at sh[k * kBlock]
+    uint2 lo[SOLRT_BVH8_STACK - kSmem];
+    SOLRT_D void put(int k, uint2 v) {
+        if (k < kSmem) sh[k * kBlock] = v;
+        else lo[k - kSmem] = v;
+    }
+    SOLRT_D uint2 get(int k) const { return k < kSmem ? sh[k * kBlock] : lo[k - kSmem]; }
+};
+template <int kBlock>
+struct Bvh8Stack<kBlock, 0> {
+    uint2* sh;
+    uint2 lo[SOLRT_BVH8_STACK];
+    SOLRT_D void put(int k, uint2 v) { lo[k] = v; }
+    SOLRT_D uint2 get(int k) const { return lo[k]; }
+};
+
+template <class IO, bool kCount, bool kF32 = false, int kBlock = 128, int kSmem = 0>
 SOLRT_D void extend_bvh8_ww(const IO& io, uint32_t n, unsigned int* work, TraceCounters& cnt, uint32_t& ef) {
     const int lane = threadIdx.x & 31;
     const uint32_t lane_lt = (1u << lane) - 1u;
-    uint2 stack[SOLRT_BVH8_STACK];
+    Bvh8Stack<kBlock, kSmem> stack;
+    __shared__ uint2 s_stack8[(kSmem > 0 ? kSmem : 1) * kBlock];
+    stack.sh = s_stack8 + threadIdx.x;
     int sp = 0;
     uint2 grp = make_uint2(0u, 0u);   // (child base, hit bits << 24 | internal mask)
     uint2 tgrp = make_uint2(0u, 0u);  // parked triangles: (triangle base, hit bits)
@@ -97,13 +119,13 @@ SOLRT_D void extend_bvh8_ww(const IO& io, uint32_t n, unsigned int* work, TraceC
             if (wb == 0u) break;
             if (__popc(wb) < SOLRT_BVH8_NODE_MIN && __any_sync(0xffffffffu, tgrp.y != 0u)) break;
             if (want) {
-                if ((grp.y >> 24) == 0u) grp = stack[--sp];
+                if ((grp.y >> 24) == 0u) grp = stack.get(--sp);
                 const uint32_t j = (uint32_t)(__ffs(grp.y >> 24) - 1);
                 grp.y &= ~(1u << (24u + j));
                 const uint32_t s = j ^ oct;
                 const uint32_t node = grp.x + (uint32_t)__popc(grp.y & ((1u << s) - 1u) & 0xffu);
                 if (grp.y >> 24) {
-                    if (sp < SOLRT_BVH8_STACK) stack[sp++] = grp;
+                    if (sp < SOLRT_BVH8_STACK) stack.put(sp++, grp);
                     else ef |= SOLRT_EFLAG_STACK;
                 }
                 grp = make_uint2(0u, 0u);

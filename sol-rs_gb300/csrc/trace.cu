@@ -27,6 +27,16 @@ namespace {
 #ifndef SOLRT_EXTEND_MINB
 #define SOLRT_EXTEND_MINB 0
 #endif
+// The same for the 8-wide kinds (their node test holds a whole 80-byte node
+// in registers).
+#ifndef SOLRT_BVH8_MINB
+#define SOLRT_BVH8_MINB 0
+#endif
+// Group-stack entries of the 8-wide traversal kept in shared memory (the
+// rest in local memory), 0..SOLRT_BVH8_STACK.
+#ifndef SOLRT_BVH8_SMEM
+#define SOLRT_BVH8_SMEM 0
+#endif
 constexpr int kExtendBlock = SOLRT_EXTEND_BLOCK;
 
 SOLRT_D void flush_counters(DevStats* stats, const TraceCounters& cnt, uint32_t ef, bool count_nodes) {
@@ -103,7 +113,9 @@ struct RayFileIO {
 // (as the single-level BVH2 kernel does by itself).
 template <int KIND, int kBlock>
 constexpr int extend_min_blocks() {
-    return KIND == SOLRT_BVH2_TWO_LEVEL ? 1024 / kBlock : SOLRT_EXTEND_MINB;
+    return KIND == SOLRT_BVH2_TWO_LEVEL ? 1024 / kBlock
+           : (KIND == SOLRT_BVH8_Q8 || KIND == SOLRT_BVH8_F32) ? SOLRT_BVH8_MINB * 128 / kBlock
+                                                                : SOLRT_EXTEND_MINB;
 }
 
 template <int KIND, class IO, bool kCount, int kBlock, int kSmem>
@@ -123,9 +135,9 @@ __global__ void __launch_bounds__(kBlock, (extend_min_blocks<KIND, kBlock>())) k
     } else if constexpr (KIND == SOLRT_BVH4_Q8) {
         extend_bvh4_ww<IO, kCount, kBlock, kSmem>(io, n, work, cnt, ef);
     } else if constexpr (KIND == SOLRT_BVH8_F32) {
-        extend_bvh8_ww<IO, kCount, true>(io, n, work, cnt, ef);
+        extend_bvh8_ww<IO, kCount, true, kBlock, kSmem>(io, n, work, cnt, ef);
     } else {
-        extend_bvh8_ww<IO, kCount, false>(io, n, work, cnt, ef);
+        extend_bvh8_ww<IO, kCount, false, kBlock, kSmem>(io, n, work, cnt, ef);
     }
     flush_counters(stats, cnt, ef, kCount);
 }
@@ -148,26 +160,36 @@ void launch_variant(const Context& ctx, const IO& io, const unsigned int* count,
 template <int KIND, class IO>
 solrt_status launch_tuned(const Context& ctx, const IO& io, const unsigned int* count, uint32_t n_static,
                           uint32_t n_cap, unsigned int* work, DevStats* st) {
-    constexpr int S = (KIND == SOLRT_BVH8_Q8 || KIND == SOLRT_BVH8_F32) ? 0 : 1;  // BVH8: local-memory stack
-    if (ctx.counters) {
-        launch_variant<KIND, IO, true, kExtendBlock, S * SOLRT_SMEM_STACK>(ctx, io, count, n_static, n_cap, work, st);
+    if constexpr (KIND == SOLRT_BVH8_Q8 || KIND == SOLRT_BVH8_F32) {
+        // 8-wide kinds: SOLRT_BVH8_SMEM group-stack entries (8 B each) in
+        // shared memory whatever the tuned depth; the block size is tuned
+        constexpr int M8 = SOLRT_BVH8_SMEM;
+        if (ctx.counters) launch_variant<KIND, IO, true, kExtendBlock, M8>(ctx, io, count, n_static, n_cap, work, st);
+        else if (ctx.tune.block == 64) launch_variant<KIND, IO, false, 64, M8>(ctx, io, count, n_static, n_cap, work, st);
+        else if (ctx.tune.block == 256) launch_variant<KIND, IO, false, 256, M8>(ctx, io, count, n_static, n_cap, work, st);
+        else launch_variant<KIND, IO, false, 128, M8>(ctx, io, count, n_static, n_cap, work, st);
         return SOLRT_OK;
-    }
-    const uint32_t blk = ctx.tune.block, sm = S ? ctx.tune.smem : 0u;
+    } else {
+        if (ctx.counters) {
+            launch_variant<KIND, IO, true, kExtendBlock, SOLRT_SMEM_STACK>(ctx, io, count, n_static, n_cap, work, st);
+            return SOLRT_OK;
+        }
+        const uint32_t blk = ctx.tune.block, sm = ctx.tune.smem;
 #define SOLRT_VARIANT(B, M)                                                                              \
-    if (blk == B && sm == S * M) {                                                                       \
-        launch_variant<KIND, IO, false, B, S * M>(ctx, io, count, n_static, n_cap, work, st);            \
-        return SOLRT_OK;                                                                                 \
-    }
-    SOLRT_VARIANT(64, 16)
-    SOLRT_VARIANT(64, 32)
-    SOLRT_VARIANT(128, 16)
-    SOLRT_VARIANT(128, 32)
-    SOLRT_VARIANT(256, 16)
-    SOLRT_VARIANT(256, 32)
+        if (blk == B && sm == M) {                                                                       \
+            launch_variant<KIND, IO, false, B, M>(ctx, io, count, n_static, n_cap, work, st);            \
+            return SOLRT_OK;                                                                             \
+        }
+        SOLRT_VARIANT(64, 16)
+        SOLRT_VARIANT(64, 32)
+        SOLRT_VARIANT(128, 16)
+        SOLRT_VARIANT(128, 32)
+        SOLRT_VARIANT(256, 16)
+        SOLRT_VARIANT(256, 32)
 #undef SOLRT_VARIANT
-    set_error("no extend kernel for block %u, stack %u", blk, sm);
-    return SOLRT_ERR_INVALID;
+        set_error("no extend kernel for block %u, stack %u", blk, sm);
+        return SOLRT_ERR_INVALID;
+    }
 }
 
 }  // namespace
