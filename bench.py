@@ -53,9 +53,9 @@ EXTEND_CAPTURES = {
                          "threads_per_instruction": 14.27, "warps_active_pct": 48.0, "l2_hit_pct": 96.7,
                          "dram_throughput_pct": 1.4, "source": "profiles/extend_soup1M_bvh2_full.md"}},
     "tunnel": {"dram_bytes_per_segment": 78.8, "dram_source": "profiles/extend_dram_soup1M_tunnel4M.md",
-               "limiter": {"l1tex_lsu_wavefronts_pct": 61.8, "l1tex_throughput_pct": 71.0, "issue_active_pct": 58.0,
-                           "threads_per_instruction": 13.39, "warps_active_pct": 43.5, "l2_hit_pct": 91.6,
-                           "dram_throughput_pct": 2.2, "source": "profiles/extend_tunnel_640x360_full.md"}},
+               "limiter": {"l1tex_lsu_wavefronts_pct": 71.9, "l1tex_throughput_pct": 77.7, "issue_active_pct": 65.0,
+                           "threads_per_instruction": 14.52, "warps_active_pct": 46.9, "l2_hit_pct": 91.7,
+                           "source": "profiles/extend_tunnel_640x360_full.md (bounce level 1)"}},
 }
 
 
