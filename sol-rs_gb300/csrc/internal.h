@@ -124,14 +124,9 @@ struct DevJob {
 // A work item of one pass: samples [s0, s0 + k) of pixels [pix0, pix0 + npix)
 // of one job. Its paths occupy slots [path_base, path_base + npix * k) of the
 // pass (pixel-major), its pixels [pix_base, pix_base + npix) of the pass's
-// pixel space. A chained item (chain = 1: per-pixel RNG streams, whose
-// sample s + 1 starts from the stream state sample s ended with) has one
-// slot per pixel: its paths occupy [path_base, path_base + npix), each slot
-// runs the pixel's samples one after the other (k_shade starts the next
-// sample when a path ends and adds the finished one to the pixel's sums),
-// and the slot's radiance word holds the running sample index.
+// pixel space.
 struct DevItem {
-    uint32_t job, pix0, npix, s0, k, path_base, pix_base, chain;
+    uint32_t job, pix0, npix, s0, k, path_base, pix_base, pad;
 };
 
 // The depth field of a path's meta word also carries its job.

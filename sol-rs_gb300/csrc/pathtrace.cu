@@ -58,8 +58,7 @@ __global__ void k_generate(const DevJob* __restrict__ jobs, const DevItem* __res
     const DevItem it = items[find_last_le(nitems, i, [&](uint32_t t) { return items[t].path_base; })];
     const DevJob& J = jobs[it.job];
     const uint32_t local = i - it.path_base;
-    const uint32_t kk = it.chain ? 1u : it.k;  // chained items: one slot per pixel, first sample s0
-    const uint32_t lp = local / kk, j = local - lp * kk;
+    const uint32_t lp = local / it.k, j = local - lp * it.k;
     const uint32_t pix = it.pix0 + lp, s = it.s0 + j;
     uint32_t rng = sample_seed(J, pix, s, J.rng_mode == SOLRT_RNG_REF_STREAM && s > 0 ? J.rng_state[pix] : 0u);
     float4 o, d;
@@ -69,7 +68,6 @@ __global__ void k_generate(const DevJob* __restrict__ jobs, const DevItem* __res
     q.thr_rng[i] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(rng));
     q.meta[i] = make_uint2(i, it.job << kDepthBits);
     if (J.integrator == SOLRT_INTEGRATOR_PATH_NEE) rad[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // sums shadow terms
-    else if (it.chain) rad[i] = make_float4(__uint_as_float(s), 0.0f, 0.0f, 0.0f);  // the slot's sample index
 }
 
 // kNee: the variant for passes with SOLRT_INTEGRATOR_PATH_NEE jobs (shadow
@@ -95,7 +93,7 @@ __global__ void __launch_bounds__(256, SOLRT_SHADE_MINB)
     uint32_t ef = 0;
     for (uint32_t base = warp_global * 32u; base < n; base += warps * 32u) {
         const uint32_t i = base + lane;
-        bool alive = false, shadow = false, fresh = false;  // fresh: a chained pixel's next camera ray
+        bool alive = false, shadow = false;
         float4 out_o = make_float4(0, 0, 0, 0), out_d = make_float4(0, 0, 0, 0), out_t = make_float4(0, 0, 0, 0);
         float4 s_o = make_float4(0, 0, 0, 0), s_d = make_float4(0, 0, 0, 0), s_c = make_float4(0, 0, 0, 0);
         float4 out_prev = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -123,49 +121,15 @@ __global__ void __launch_bounds__(256, SOLRT_SHADE_MINB)
                 out_t = make_float4(acc.x, acc.y, acc.z, __uint_as_float(rng));
                 m.y = (job << kDepthBits) | depth;
             } else {
-                const DevItem* itp = J.rng_mode == SOLRT_RNG_REF_STREAM
-                                         ? &items[find_last_le(nitems, m.x, [&](uint32_t t) { return items[t].path_base; })]
-                                         : nullptr;
-                if (itp && itp->chain) {
-                    // chained samples: this sample goes into the pixel's sums
-                    // now (k_accumulate skips chained items), in sample order
-                    // since the pixel's next sample starts only here; it
-                    // starts from the stream state this one ended with
-                    const uint32_t pix = itp->pix0 + (m.x - itp->path_base);
-                    const float4 c = make_float4(acc.x, acc.y, acc.z, 0.0f);
-                    if (J.accum_mode == SOLRT_ACCUM_KAHAN) {
-                        const float4 s4 = J.ksum[pix], c4 = J.kcomp[pix];
-                        f3 ks{s4.x, s4.y, s4.z}, kc{c4.x, c4.y, c4.z};
-                        float kn = s4.w;
-                        add_sample_kahan(ks, kc, kn, c);
-                        J.ksum[pix] = make_float4(ks.x, ks.y, ks.z, kn);
-                        J.kcomp[pix] = make_float4(kc.x, kc.y, kc.z, 0.0f);
-                    } else {
-                        const float4 s4 = J.fsum[pix];
-                        f3 sm{s4.x, s4.y, s4.z};
-                        add_sample(sm, c);
-                        J.fsum[pix] = make_float4(sm.x, sm.y, sm.z, 0.0f);
-                    }
-                    const uint32_t s = __float_as_uint(rad[m.x].x) + 1u;
-                    if (s < itp->s0 + itp->k) {
-                        rng = sample_seed(J, pix, s, rng);
-                        camera_ray(J, pix, rng, out_o, out_d);
-                        rad[m.x] = make_float4(__uint_as_float(s), 0.0f, 0.0f, 0.0f);
-                        out_t = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(rng));
-                        m.y = job << kDepthBits;
-                        alive = true;
-                        fresh = true;
-                    } else {
-                        J.rng_state[pix] = rng;
-                    }
+                if (nee) {  // after this path's earlier shadow terms (resolved in bounce order)
+                    const float4 r = rad[m.x];
+                    rad[m.x] = make_float4(r.x + acc.x, r.y + acc.y, r.z + acc.z, 0.0f);
                 } else {
-                    if (nee) {  // after this path's earlier shadow terms (resolved in bounce order)
-                        const float4 r = rad[m.x];
-                        rad[m.x] = make_float4(r.x + acc.x, r.y + acc.y, r.z + acc.z, 0.0f);
-                    } else {
-                        rad[m.x] = make_float4(acc.x, acc.y, acc.z, 0.0f);
-                    }
-                    if (itp) J.rng_state[itp->pix0 + (m.x - itp->path_base) / itp->k] = rng;
+                    rad[m.x] = make_float4(acc.x, acc.y, acc.z, 0.0f);
+                }
+                if (J.rng_mode == SOLRT_RNG_REF_STREAM) {
+                    const DevItem it = items[find_last_le(nitems, m.x, [&](uint32_t t) { return items[t].path_base; })];
+                    J.rng_state[it.pix0 + (m.x - it.path_base) / it.k] = rng;
                 }
             }
         }
@@ -188,8 +152,6 @@ __global__ void __launch_bounds__(256, SOLRT_SHADE_MINB)
                 }
             }
         }
-        const uint32_t fmask = __ballot_sync(0xffffffffu, fresh);
-        if (fmask && lane == __ffs(fmask) - 1) atomicAdd(&stats->paths, (unsigned long long)__popc(fmask));
         const uint32_t smask = kNee ? __ballot_sync(0xffffffffu, shadow) : 0u;
         if (smask) {
             const int leader = __ffs(smask) - 1;
@@ -238,7 +200,6 @@ __global__ void k_accumulate(const DevJob* __restrict__ jobs, const DevItem* __r
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= pixels) return;
     const DevItem it = items[find_last_le(nitems, t, [&](uint32_t i) { return items[i].pix_base; })];
-    if (it.chain) return;  // its samples were added by k_shade as they ended
     const DevJob& J = jobs[it.job];
     const uint32_t lp = t - it.pix_base;
     const uint32_t pix = it.pix0 + lp;
@@ -901,23 +862,13 @@ solrt_status batch_plan(Context& ctx, const solrt_job* jobs, uint32_t n, uint32_
         return SOLRT_OK;
     }
     // work items, round-robin over jobs so that passes mix jobs
-    // Per-pixel-stream jobs (sample s + 1 continues the stream of sample s)
-    // chain their samples inside a pass: one slot per pixel runs up to
-    // kChain samples back to back, so the queue stays full while samples
-    // remain instead of draining to the longest path after every sample;
-    // the pass then needs k x (max_bounces + 1) bounce launches. Jobs with
-    // next-event estimation take one sample per pass.
-    struct Chunk { uint32_t job, pix0, npix, k, spp, chain; };
+    struct Chunk { uint32_t job, pix0, npix, k, spp; };
     std::vector<Chunk> chunks;
     for (uint32_t j = 0; j < n; ++j) {
         const DevJob& J = b.jobs[j];
         const uint32_t np = J.width * J.height;
-        const bool chain = J.rng_mode == SOLRT_RNG_REF_STREAM && J.integrator != SOLRT_INTEGRATOR_PATH_NEE;
-        uint32_t k;
-        if (chain) k = std::max(1u, std::min(J.spp, (SOLRT_MAX_BOUNCES + 1u) / (J.max_bounces + 1u)));
-        else k = J.rng_mode == SOLRT_RNG_REF_STREAM ? 1u : std::max(1u, std::min(J.spp, cap / std::max(np, 1u)));
-        for (uint32_t p0 = 0; p0 < np; p0 += cap)
-            chunks.push_back(Chunk{j, p0, std::min(cap, np - p0), k, J.spp, chain ? 1u : 0u});
+        const uint32_t k = J.rng_mode == SOLRT_RNG_REF_STREAM ? 1u : std::max(1u, std::min(J.spp, cap / std::max(np, 1u)));
+        for (uint32_t p0 = 0; p0 < np; p0 += cap) chunks.push_back(Chunk{j, p0, std::min(cap, np - p0), k, J.spp});
     }
     // Passes are filled first fit: round r of every chunk (its samples
     // [r k, r k + k)), largest items first, goes to the first pass after the
@@ -937,7 +888,7 @@ solrt_status batch_plan(Context& ctx, const solrt_job* jobs, uint32_t n, uint32_
         if (live.empty()) break;
         auto paths_of = [&](uint32_t c) {
             const uint32_t s0 = round * chunks[c].k;
-            return (uint64_t)chunks[c].npix * (chunks[c].chain ? 1u : std::min(chunks[c].k, chunks[c].spp - s0));
+            return (uint64_t)chunks[c].npix * std::min(chunks[c].k, chunks[c].spp - s0);
         };
         std::stable_sort(live.begin(), live.end(), [&](uint32_t a, uint32_t b2) { return paths_of(a) > paths_of(b2); });
         for (uint32_t c : live) {
@@ -948,15 +899,14 @@ solrt_status batch_plan(Context& ctx, const solrt_job* jobs, uint32_t n, uint32_
             while (p < bins.size() && bins[p].plan.paths + paths > cap) ++p;
             if (p == bins.size()) bins.push_back(Bin{PassPlan{0, 0, 0, 0, 0}, {}});
             Bin& bn = bins[p];
-            DevItem it{ch.job, ch.pix0, ch.npix, s0, std::min(ch.k, ch.spp - s0), bn.plan.paths, bn.plan.pixels,
-                       ch.chain};
+            DevItem it{ch.job, ch.pix0, ch.npix, s0, std::min(ch.k, ch.spp - s0), bn.plan.paths, bn.plan.pixels, 0};
             bn.items.push_back(it);
             bn.plan.item_count += 1;
             bn.plan.paths += (uint32_t)paths;
             bn.plan.pixels += it.npix;
-            bn.plan.bounces = std::max(bn.plan.bounces, (b.jobs[it.job].max_bounces + 1u) * (ch.chain ? it.k : 1u));
+            bn.plan.bounces = std::max(bn.plan.bounces, b.jobs[it.job].max_bounces + 1u);
             if (b.jobs[it.job].integrator == SOLRT_INTEGRATOR_PATH_NEE) bn.plan.nee = 1u;
-            b.total_paths += ch.chain ? (uint64_t)it.npix * it.k : paths;
+            b.total_paths += paths;
             last[c] = (int64_t)p;
         }
     }
