@@ -812,6 +812,10 @@ def main():
     ap.add_argument("--duration", type=float, default=60.0, help="serve: arrival window, s")
     ap.add_argument("--drain", type=float, default=30.0,
                     help="serve: seconds after the last arrival before unfinished jobs are cancelled")
+    ap.add_argument("--steady-rate", type=float, default=8.0,
+                    help="serve: arrival rate of the second, below-capacity serving run of the default line")
+    ap.add_argument("--steady-duration", type=float, default=30.0, help="serve: arrival window of that run, s")
+    ap.add_argument("--no-serve-steady", action="store_true", help="skip the below-capacity serving run")
     ap.add_argument("--stop-rmse", type=float, default=1e-3,
                     help="serve: stopping rule, estimated RMSE against the converged image (0 = run every sample)")
     ap.add_argument("--policy", default="shortest", choices=["fair", "shortest"], help="serve: scheduling policy")
@@ -1050,6 +1054,15 @@ def main():
                                 stop_rmse=args.stop_rmse, drain_s=args.drain)
         except Exception as ex:
             serving = {"error": str(ex)}
+        # the same distribution at a rate the GPU keeps up with (about half
+        # of what it traces), where p99 is a steady-state latency, not backlog
+        if not args.no_serve_steady:
+            try:
+                serving["below_capacity"] = run_serve(local, args.steady_rate, args.steady_duration,
+                                                      policy=1 if args.policy == "shortest" else 0,
+                                                      stop_rmse=args.stop_rmse, drain_s=args.drain, seed=6)
+            except Exception as ex:
+                serving["below_capacity"] = {"error": str(ex)}
     out = None
     if rank == 0:
         cpu = None
