@@ -276,7 +276,7 @@ def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, mai
                     "threads, %.1f s" % (os.cpu_count() or 1, oracle_s),
           "rays_desc": "%d pixel-centre camera rays of the %dx%d frame + %d seeded rays from inside the scene "
                        "bounds" % (min(n_rays, W * H), W, H, max(0, n_rays - W * H))}
-    all_kinds = (("bvh2_fp32", solrt.BVH2, False), ("bvh2_q16", solrt.BVH2_Q16, False),
+    all_kinds = (("bvh2_fp32", solrt.BVH2, False), ("bvh2_treelet", solrt.BVH2, True), ("bvh2_q16", solrt.BVH2_Q16, False),
                  ("bvh4_q8", solrt.BVH4_Q8, False), ("bvh8_q8", solrt.BVH8_Q8, False),
                  ("bvh8_q8_sah", solrt.BVH8_Q8, True), ("bvh8_fp32", solrt.BVH8_F32, False))
     with solrt.Context(local, enable_timing=True) as ctx, solrt.Context(local, enable_counters=True) as cctx:
@@ -286,6 +286,7 @@ def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, mai
             sc = solrt.SceneDescription(ctx, data, bvh=kind, leaf_max=0 if kind in (solrt.BVH2, solrt.BVH2_Q16) else 1,
                                         sah=sah)
             info = sc.bvh_info()
+            depth = int(info.depth)
             h = torch.zeros((n_rays, 4), dtype=torch.float32, device=dev)
             ctx.reset_stats()
             sc.trace_rays_device(rays_d.data_ptr(), n_rays, h.data_ptr())
@@ -328,7 +329,8 @@ def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, mai
                          "nodes_per_segment": round(nodes, 2) if nodes is not None else None,
                          "tris_per_segment": round(tris, 2) if tris is not None else None,
                          "node_bytes_per_segment": round(nb * nodes, 1) if nodes is not None else None,
-                         "fp64_fallbacks_in_compared_rays": int(fb_trace), "build_ms": round(info.build_ms, 3)}
+                         "fp64_fallbacks_in_compared_rays": int(fb_trace), "build_ms": round(info.build_ms, 3),
+                         "depth": depth}
             sc.close()
     out["hit_ids_vs_oracle"] = vs
     return out
@@ -442,7 +444,7 @@ def parity_tunnel(local, n_rays=1 << 22):
     out = {"workload": cfg["workload"]}
     out["rmse_vs_fp64"] = rmse_vs_fp64(local, data, kw, cam, solrt.BVH2, (H // 2 - 1, H // 2 + 1), frames=4)
     ps = precision_study(local, data, kw, cam, None, None, None, None, n_rays=n_rays,
-                         kinds=("bvh2_fp32", "bvh8_q8", "bvh8_q8_sah"))
+                         kinds=("bvh2_fp32", "bvh2_treelet", "bvh8_q8", "bvh8_q8_sah"))
     out.update(ps)
     return out
 
@@ -790,7 +792,7 @@ def run_reference(args, world, rank, pg):
 
 def run_config(cfg, args, world):
     """The config object of the JSON line, the same for both arms."""
-    return dict(cfg, parallelism="replicas" if world > 1 else "single", bvh=args.bvh,
+    return dict(cfg, parallelism="replicas" if world > 1 else "single", bvh=args.bvh + ("+sah" if args.sah else ""),
                 l2="inputs larger than L2 (scene + BVH + path queues > 129 MB)")
 
 
@@ -802,7 +804,8 @@ def main():
     ap.add_argument("--impl", default="solrt", choices=["solrt", "reference"])
     ap.add_argument("--workload", default="soup", choices=["soup", "cornell", "tunnel", "instances", "batch", "serve"])
     ap.add_argument("--bvh", default="bvh2", choices=["bvh2", "bvh2q", "bvh2t", "bvh4", "bvh8", "bvh8f"])
-    ap.add_argument("--sah", action="store_true", help="wide BVH kinds: SAH-optimal collapse")
+    ap.add_argument("--sah", action="store_true",
+                    help="wide BVH kinds: SAH-optimal collapse; binary kinds: treelet restructuring toward the SAH")
     ap.add_argument("--kernel", default="wavefront", choices=["wavefront", "mega"],
                     help="mega: the plain per-pixel kernel (the reference's loop structure) on the same workload")
     ap.add_argument("--nee", action="store_true",

@@ -820,10 +820,236 @@ static solrt_status build_two_level(Context& ctx, Scene& sc) {
 
 // The single-level kinds: one LBVH over the world-space triangles, then the
 // wide collapse or the 16-bit quantisation when asked.
+// ---------------------------------------------------------------------------
+// Treelet restructuring of the LBVH toward the SAH (Karras and Aila, "Fast
+// parallel construction of high-quality bounding volume hierarchies", HPG
+// 2013), for the binary kinds with SOLRT_BVH_SAH. Bottom up, as the refit
+// walks: the second thread to reach an internal node owns its subtree; it
+// grows a treelet from the node's two children by replacing the internal
+// treelet leaf of largest surface area with its two children until the
+// treelet has kTreeletLeaves leaves (or only triangles are left), finds by
+// a dynamic program over the subsets of those leaves the binary tree of
+// least SAH cost (node visit 1, triangle test kSahTri, per unit of surface
+// area), and, when it is cheaper than the subtree as it is, rewrites the
+// treelet's internal nodes (the node itself stays the treelet's root, the
+// expanded nodes are reused in expansion order). Leaves keep their positions
+// in the leaf order, so the triangle stream is unchanged; only child and
+// parent links, exact boxes and subtree costs change. Deterministic: a
+// node's result depends only on its subtree, which is final when the node
+// is processed, and ties go to the first candidate in a fixed order.
+// ---------------------------------------------------------------------------
+
+namespace {
+
+constexpr int kTreeletLeaves = 7;
+constexpr int kTreeletRounds = 3;
+constexpr float kSahTri = 0.3f;
+
+SOLRT_D float box_area(const float b[6]) {
+    const float ex = fmaxf(b[3] - b[0], 0.0f), ey = fmaxf(b[4] - b[1], 0.0f), ez = fmaxf(b[5] - b[2], 0.0f);
+    return 2.0f * ((ex * ey + ey * ez) + ez * ex);
+}
+
+// Exact box (lo.xyz, hi.xyz) of a child reference: a leaf's triangle from
+// the leaf-ordered stream, an internal node's from `nbox` (written by other
+// threads: read through L2).
+SOLRT_D void ref_box(uint32_t ref, const float4* __restrict__ tri_wt, const float4* nbox, float b[6]) {
+    if (ref & 0x80000000u) {
+        const size_t k = ref & 0x7fffffffu;
+        const float4 a = tri_wt[3 * k], c = tri_wt[3 * k + 1], d = tri_wt[3 * k + 2];
+        b[0] = fminf(fminf(a.x, c.x), d.x); b[1] = fminf(fminf(a.y, c.y), d.y); b[2] = fminf(fminf(a.z, c.z), d.z);
+        b[3] = fmaxf(fmaxf(a.x, c.x), d.x); b[4] = fmaxf(fmaxf(a.y, c.y), d.y); b[5] = fmaxf(fmaxf(a.z, c.z), d.z);
+    } else {
+        const float4 lo = __ldcg(nbox + 2 * (size_t)ref), hi = __ldcg(nbox + 2 * (size_t)ref + 1);
+        b[0] = lo.x; b[1] = lo.y; b[2] = lo.z; b[3] = hi.x; b[4] = hi.y; b[5] = hi.z;
+    }
+}
+
+__global__ void k_treelet(const float4* __restrict__ tri_wt, uint32_t* child, uint32_t* par_int,
+                          uint32_t* par_leaf, float4* nbox, float* cost, unsigned int* __restrict__ flags,
+                          uint32_t n) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n || n < 3) return;
+    uint32_t p = par_leaf[k];
+    float cs[1 << kTreeletLeaves];          // least SAH cost of each subset of treelet leaves
+    uint8_t part[1 << kTreeletLeaves];      // its best first part (a subset holding the lowest leaf)
+    for (uint32_t steps = 0; steps < n; ++steps) {
+        if (p >= n - 1) return;  // malformed parent link
+        __threadfence();
+        if (atomicAdd(flags + p, 1u) == 0u) return;  // the sibling subtree is not done yet
+        __threadfence();
+        // the treelet of p
+        uint32_t lref[kTreeletLeaves], inner[kTreeletLeaves - 2];
+        float lb[kTreeletLeaves][6], la[kTreeletLeaves];
+        int nl = 2, nin = 0;
+        lref[0] = __ldcg(child + 2 * (size_t)p);
+        lref[1] = __ldcg(child + 2 * (size_t)p + 1);
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            ref_box(lref[q], tri_wt, nbox, lb[q]);
+            la[q] = box_area(lb[q]);
+        }
+        while (nl < kTreeletLeaves) {
+            int j = -1;
+            float best = -1.0f;
+            for (int q = 0; q < nl; ++q)
+                if (!(lref[q] & 0x80000000u) && la[q] > best) {
+                    best = la[q];
+                    j = q;
+                }
+            if (j < 0) break;
+            const uint32_t r = lref[j];
+            inner[nin++] = r;
+            lref[j] = __ldcg(child + 2 * (size_t)r);
+            lref[nl] = __ldcg(child + 2 * (size_t)r + 1);
+            ref_box(lref[j], tri_wt, nbox, lb[j]);
+            la[j] = box_area(lb[j]);
+            ref_box(lref[nl], tri_wt, nbox, lb[nl]);
+            la[nl] = box_area(lb[nl]);
+            ++nl;
+        }
+        float lc[kTreeletLeaves];
+        for (int q = 0; q < nl; ++q) lc[q] = (lref[q] & 0x80000000u) ? kSahTri * la[q] : __ldcg(cost + lref[q]);
+        const uint32_t full = (1u << nl) - 1u;
+        float pb[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+        for (int q = 0; q < nl; ++q)
+            for (int a = 0; a < 3; ++a) {
+                pb[a] = fminf(pb[a], lb[q][a]);
+                pb[3 + a] = fmaxf(pb[3 + a], lb[q][3 + a]);
+            }
+        // cost of the subtree as it stands: its two children are final, their
+        // costs known (treelet slots 0 and 1 before any expansion)
+        float cur;
+        {
+            const uint32_t c0 = __ldcg(child + 2 * (size_t)p), c1 = __ldcg(child + 2 * (size_t)p + 1);
+            float b0[6], b1[6];
+            ref_box(c0, tri_wt, nbox, b0);
+            ref_box(c1, tri_wt, nbox, b1);
+            const float k0 = (c0 & 0x80000000u) ? kSahTri * box_area(b0) : __ldcg(cost + c0);
+            const float k1 = (c1 & 0x80000000u) ? kSahTri * box_area(b1) : __ldcg(cost + c1);
+            cur = box_area(pb) + (k0 + k1);
+        }
+        bool rebuild = false;
+        if (nl >= 3) {
+            for (uint32_t S = 1; S <= full; ++S) {
+                const uint32_t low = S & (0u - S);
+                if (S == low) {
+                    cs[S] = lc[__ffs(S) - 1];
+                    part[S] = 0;
+                    continue;
+                }
+                float b[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+                for (int q = 0; q < nl; ++q)
+                    if (S & (1u << q))
+                        for (int a = 0; a < 3; ++a) {
+                            b[a] = fminf(b[a], lb[q][a]);
+                            b[3 + a] = fmaxf(b[3 + a], lb[q][3 + a]);
+                        }
+                float best = INFINITY;
+                uint32_t bp = low;
+                for (uint32_t P = (S - 1u) & S; P != 0u; P = (P - 1u) & S) {
+                    if (!(P & low)) continue;
+                    const float v = cs[P] + cs[S ^ P];
+                    if (v < best) {
+                        best = v;
+                        bp = P;
+                    }
+                }
+                cs[S] = box_area(b) + best;
+                part[S] = (uint8_t)bp;
+            }
+            rebuild = cs[full] < cur * (1.0f - 1e-5f);
+        }
+        if (rebuild) {
+            // rewrite the treelet top down: (subset, node) pairs
+            uint32_t stS[kTreeletLeaves], stN[kTreeletLeaves];
+            int sp = 0, used = 0;
+            stS[sp] = full;
+            stN[sp++] = p;
+            while (sp > 0) {
+                const uint32_t S = stS[--sp], node = stN[sp];
+                float b[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
+                for (int q = 0; q < nl; ++q)
+                    if (S & (1u << q))
+                        for (int a = 0; a < 3; ++a) {
+                            b[a] = fminf(b[a], lb[q][a]);
+                            b[3 + a] = fmaxf(b[3 + a], lb[q][3 + a]);
+                        }
+                nbox[2 * (size_t)node] = make_float4(b[0], b[1], b[2], 0.0f);
+                nbox[2 * (size_t)node + 1] = make_float4(b[3], b[4], b[5], 0.0f);
+                cost[node] = cs[S];
+                const uint32_t sides[2] = {part[S], S ^ part[S]};
+#pragma unroll
+                for (int side = 0; side < 2; ++side) {
+                    const uint32_t T = sides[side];
+                    uint32_t ref;
+                    if ((T & (T - 1u)) == 0u) {
+                        ref = lref[__ffs(T) - 1];
+                        if (ref & 0x80000000u) par_leaf[ref & 0x7fffffffu] = node;
+                        else par_int[ref] = node;
+                    } else {
+                        ref = inner[used++];
+                        par_int[ref] = node;
+                        stS[sp] = T;
+                        stN[sp++] = ref;
+                    }
+                    child[2 * (size_t)node + side] = ref;
+                }
+            }
+        } else {
+            nbox[2 * (size_t)p] = make_float4(pb[0], pb[1], pb[2], 0.0f);
+            nbox[2 * (size_t)p + 1] = make_float4(pb[3], pb[4], pb[5], 0.0f);
+            cost[p] = cur;
+        }
+        if (p == 0) return;
+        p = __ldcg(par_int + p);
+    }
+}
+
+}  // namespace
+
+// Restructures the binary LBVH `L` in place (rounds of k_treelet), then
+// writes its nodes again (k_refit) and its depth. Synchronises.
+static solrt_status treelet_restructure(Context& ctx, const float4* vpos, const uint4* tri_idx, uint32_t prim_base,
+                                        Lbvh& L, int rounds) {
+    const uint32_t n = L.n;
+    if (n < 3) return SOLRT_OK;
+    cudaStream_t st = ctx.stream;
+    DeviceBuffer flags, cost, depth;
+    SOLRT_TRY(flags.alloc(sizeof(unsigned int) * (size_t)L.ni));
+    SOLRT_TRY(cost.alloc(sizeof(float) * (size_t)L.ni));
+    SOLRT_TRY(depth.alloc(sizeof(unsigned int)));
+    for (int r = 0; r < rounds; ++r) {
+        SOLRT_CUDA(cudaMemsetAsync(flags.ptr, 0, flags.bytes, st));
+        k_treelet<<<blocks_for(n, 128), 128, 0, st>>>(L.tri_wt.as<float4>(), L.child.as<uint32_t>(),
+                                                      L.par_int.as<uint32_t>(), L.par_leaf.as<uint32_t>(),
+                                                      L.nbox.as<float4>(), cost.as<float>(),
+                                                      flags.as<unsigned int>(), n);
+        ++ctx.launches;
+    }
+    SOLRT_CUDA(cudaMemsetAsync(flags.ptr, 0, flags.bytes, st));
+    SOLRT_CUDA(cudaMemsetAsync(depth.ptr, 0, depth.bytes, st));
+    k_refit<<<blocks_for(n, 256), 256, 0, st>>>(vpos, tri_idx, L.order.as<uint32_t>(), L.child.as<uint32_t>(),
+                                                L.par_int.as<uint32_t>(), L.par_leaf.as<uint32_t>(), n,
+                                                flags.as<unsigned int>(), L.nbox.as<float4>(), L.nodes.as<float4>(),
+                                                L.tri_wt.as<float4>(), prim_base);
+    k_depth<<<blocks_for(n, 256), 256, 0, st>>>(L.par_int.as<uint32_t>(), L.par_leaf.as<uint32_t>(), n,
+                                                depth.as<unsigned int>());
+    ctx.launches += 2;
+    SOLRT_CUDA(cudaGetLastError());
+    unsigned int dh = 0;
+    SOLRT_CUDA(cudaMemcpyAsync(&dh, depth.ptr, sizeof(dh), cudaMemcpyDeviceToHost, st));
+    SOLRT_CUDA(cudaStreamSynchronize(st));
+    L.depth = dh;
+    return SOLRT_OK;
+}
+
 static solrt_status build_single_level(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
     const uint32_t n = sc.tri_count;
     Lbvh L;
     SOLRT_TRY(lbvh_build(ctx, sc.vpos.as<float4>(), sc.tri_idx.as<uint4>(), n, 0u, L));
+    if ((desc.flags & SOLRT_BVH_SAH) && (desc.kind == SOLRT_BVH2 || desc.kind == SOLRT_BVH2_Q16))
+        SOLRT_TRY(treelet_restructure(ctx, sc.vpos.as<float4>(), sc.tri_idx.as<uint4>(), 0u, L, kTreeletRounds));
     const uint32_t ni = L.ni;
     if (desc.kind == SOLRT_BVH8_Q8 || desc.kind == SOLRT_BVH4_Q8 || desc.kind == SOLRT_BVH8_F32) {
         const uint32_t width = desc.kind == SOLRT_BVH4_Q8 ? 4u : 8u;

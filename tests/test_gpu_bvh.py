@@ -264,3 +264,74 @@ def test_sah_collapse_not_worse_than_greedy(solrt, ctx, maker, width):
         tv = tris.view(np.float32).reshape(-1, 3, 4)[:, :, :3].astype(np.float64)
         costs[sah] = _wide_sah_cost(dec, tv, width)
     assert costs[True] <= costs[False] * (1 + 1e-5), costs
+
+
+def _bvh2_sah_cost(refs, c0, c1, c_tri=0.3):
+    """SAH cost (node visit 1, triangle test c_tri, per unit of surface area,
+    over the root's area) of a decoded BVH2 from its (widened) child boxes."""
+    def area(b):
+        e = np.maximum(b[:, 3:] - b[:, :3], 0.0).astype(np.float64)
+        return 2.0 * (e[:, 0] * e[:, 1] + e[:, 1] * e[:, 2] + e[:, 2] * e[:, 0])
+    a0, a1 = area(c0), area(c1)
+    root = area(np.concatenate([np.minimum(c0[:1, :3], c1[:1, :3]), np.maximum(c0[:1, 3:], c1[:1, 3:])], 1))[0]
+    inner = (a0 * (refs[:, 0] >= 0)).sum() + (a1 * (refs[:, 1] >= 0)).sum() + root
+    leaves = (a0 * (refs[:, 0] < 0)).sum() + (a1 * (refs[:, 1] < 0)).sum()
+    return (inner + c_tri * leaves) / root
+
+
+@pytest.mark.parametrize("maker", [lambda: S.cornell(), lambda: S.soup(50000, seed=2),
+                                   lambda: S.tunnel(n_ang=256, n_ax=128, length=25.0), lambda: single_triangle(),
+                                   lambda: S.soup(2, seed=4), lambda: S.soup(3, seed=4)],
+                         ids=["cornell", "soup50k", "tunnel", "tri1", "tri2", "tri3"])
+def test_bvh2_treelet_restructure(solrt, ctx, maker):
+    """SOLRT_BVH_SAH on the binary kind restructures the LBVH by treelets:
+    the same triangles in the same leaf order, every triangle in exactly one
+    leaf, every child slot's (widened) box containing everything below it,
+    a SAH cost no higher than the LBVH's, and the same bytes when built
+    again."""
+    d = maker()
+    lb = solrt.SceneDescription(ctx, d, bvh=solrt.BVH2)
+    sb = solrt.SceneDescription(ctx, d, bvh=solrt.BVH2, sah=True)
+    ln, lt = lb.bvh_export()
+    sn, st = sb.bvh_export()
+    assert np.array_equal(lt, st)              # leaf order and triangle stream unchanged
+    n = sb.bvh_info().tri_count
+    refs, c0, c1 = _decode_bvh2(sn)
+    ni = refs.shape[0]
+    assert ni == max(n - 1, 1) and sb.bvh_info().node_count == lb.bvh_info().node_count
+    tv = st.view(np.float32).reshape(-1, 3, 4)[:, :, :3]
+    tlo, thi = tv.min(1), tv.max(1)
+    # every leaf once, every internal node but the root once as a child
+    leaf = refs < 0
+    pos = ~refs[leaf]
+    if n > 1:
+        assert np.array_equal(np.sort(pos), np.arange(n))
+        inner = np.sort(refs[~leaf])
+        assert np.array_equal(inner, np.arange(1, ni))
+    # exact subtree boxes bottom-up (children have no fixed order: iterate
+    # to a fixed point over the node list)
+    lo = np.full((ni, 3), np.inf, np.float32)
+    hi = np.full((ni, 3), -np.inf, np.float32)
+    for _ in range(200):
+        changed = False
+        for side in (0, 1):
+            r = refs[:, side]
+            clo = np.where((r < 0)[:, None], tlo[np.where(r < 0, ~r, 0)], lo[np.where(r >= 0, r, 0)])
+            chi = np.where((r < 0)[:, None], thi[np.where(r < 0, ~r, 0)], hi[np.where(r >= 0, r, 0)])
+            nlo, nhi = np.minimum(lo, clo), np.maximum(hi, chi)
+            changed |= not (np.array_equal(nlo, lo) and np.array_equal(nhi, hi))
+            lo, hi = nlo, nhi
+        if not changed:
+            break
+    for side, cb in ((0, c0), (1, c1)):
+        r = refs[:, side]
+        want_lo = np.where((r < 0)[:, None], tlo[np.where(r < 0, ~r, 0)], lo[np.where(r >= 0, r, 0)])
+        want_hi = np.where((r < 0)[:, None], thi[np.where(r < 0, ~r, 0)], hi[np.where(r >= 0, r, 0)])
+        assert np.all(cb[:, :3] <= want_lo) and np.all(cb[:, 3:] >= want_hi)
+    if n > 2:
+        lr, l0, l1 = _decode_bvh2(ln)
+        assert _bvh2_sah_cost(refs, c0, c1) <= _bvh2_sah_cost(lr, l0, l1) * (1 + 1e-6)
+    sb.tlas_regenerate()
+    again, _ = sb.bvh_export()
+    assert np.array_equal(again, sn)
+    assert sb.bvh_info().depth <= 64

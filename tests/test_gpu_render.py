@@ -93,10 +93,11 @@ def test_render_bit_exact(solrt, oracle, ctx, name, bvh):
     assert np.isfinite(ga).all() and ga[..., :3].mean() > 0
 
 
-@pytest.mark.parametrize("bvh", ["bvh4", "bvh8"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh4", "bvh8"])
 @pytest.mark.parametrize("name", ["cornell_ref_sky", "soup_gradient", "tunnel_kahan"])
 def test_render_bit_exact_sah_collapse(solrt, oracle, ctx, name, bvh):
-    """Wide BVHs collapsed by SAH render the oracle's image too."""
+    """Wide BVHs collapsed by SAH, and binary BVHs restructured by treelets,
+    render the oracle's image too."""
     data, w, h, kw = _case(name)
     ga, g8, oa, o8, stats, seg_o = _render_both(solrt, oracle, ctx, data, w, h, kw, bvh=bvh_kind(solrt, bvh), sah=True)
     assert np.array_equal(ga.view(np.uint32), oa.view(np.uint32))
