@@ -48,11 +48,11 @@ NODE_BYTES = {0: 64, 1: 80, 2: 64, 3: 224, 4: 32, 5: 64}
 # counters of one `ncu --set full` launch (profiles/extend_soup1M_bvh2_full.md,
 # profiles/extend_tunnel_640x360_full.md).
 EXTEND_CAPTURES = {
-    "soup": {"dram_bytes_per_segment": 62.4, "dram_source": "profiles/extend_dram_soup1M_tunnel4M.md",
+    ("soup", "lbvh"): {"dram_bytes_per_segment": 62.4, "dram_source": "profiles/extend_dram_soup1M_tunnel4M.md",
              "limiter": {"l1tex_lsu_wavefronts_pct": 83.8, "l1tex_throughput_pct": 87.8, "issue_active_pct": 60.7,
                          "threads_per_instruction": 14.27, "warps_active_pct": 48.0, "l2_hit_pct": 96.7,
                          "dram_throughput_pct": 1.4, "source": "profiles/extend_soup1M_bvh2_full.md"}},
-    "tunnel": {"dram_bytes_per_segment": 78.8, "dram_source": "profiles/extend_dram_soup1M_tunnel4M.md",
+    ("tunnel", "lbvh"): {"dram_bytes_per_segment": 78.8, "dram_source": "profiles/extend_dram_soup1M_tunnel4M.md",
                "limiter": {"l1tex_lsu_wavefronts_pct": 71.9, "l1tex_throughput_pct": 77.7, "issue_active_pct": 65.0,
                            "threads_per_instruction": 14.52, "warps_active_pct": 46.9, "l2_hit_pct": 91.7,
                            "source": "profiles/extend_tunnel_640x360_full.md (bounce level 1)"}},
@@ -246,7 +246,7 @@ def cpu_baseline(data, kw, cam, budget_s=10.0, threads=0):
 
 
 def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, main_tris, n_rays=1 << 22,
-                    kinds=None, render=True):
+                    kinds=None, render=True, main_sah=False):
     """The 16-bit quantised binary BVH, the 8-bit quantised 4- and 8-wide BVHs
     and the FP32 8-wide BVH next to the FP32 binary BVH on the same scene:
     hit records of 4M rays (every pixel-centre camera ray of the frame, then
@@ -298,7 +298,7 @@ def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, mai
             vs["near_edge_mismatches"][name] = int((bad & edge).sum())
             del h
             mr = nodes = tris = None
-            if main_info is not None and kind == main_info.kind and not sah and main_mrays is not None:
+            if main_info is not None and kind == main_info.kind and sah == main_sah and main_mrays is not None:
                 mr, nodes, tris = main_mrays, main_nodes, main_tris
             elif render:
                 img = solrt.Image(ctx, W, H, kw["accum_mode"])
@@ -644,7 +644,7 @@ def run_batch(args, world, rank, local, pg, njobs=None, steps=None, emit=True, w
     return cmp
 
 
-def run_serve(local, rate, duration, n_scenes=16, seed=5, policy=0, stop_rmse=0.0, drain_s=300.0):
+def run_serve(local, rate, duration, n_scenes=16, seed=5, policy=0, stop_rmse=0.0, drain_s=300.0, sah=False):
     """Served render jobs: Poisson arrivals at `rate` jobs/s for `duration`
     seconds; each job draws a scene from a resident pool of config-4 scenes
     (randomised Cornell box + log-uniform soup), a resolution from
@@ -657,7 +657,7 @@ def run_serve(local, rate, duration, n_scenes=16, seed=5, policy=0, stop_rmse=0.
     solrt = importlib.import_module("sol-rs_gb300")
     S = solrt.scenes
     ctx = solrt.Context(local)
-    pool = [solrt.SceneDescription(ctx, S.mixed_scene(i)[0], keep_data=False) for i in range(n_scenes)]
+    pool = [solrt.SceneDescription(ctx, S.mixed_scene(i)[0], keep_data=False, sah=sah) for i in range(n_scenes)]
     c = S.CORNELL_CAMERA
     cam = solrt.camera_look_at(c["eye"], c["center"], c["up"], c["vfov"], 1.0)
     rng = np.random.default_rng(seed)
@@ -804,8 +804,9 @@ def main():
     ap.add_argument("--impl", default="solrt", choices=["solrt", "reference"])
     ap.add_argument("--workload", default="soup", choices=["soup", "cornell", "tunnel", "instances", "batch", "serve"])
     ap.add_argument("--bvh", default="bvh2", choices=["bvh2", "bvh2q", "bvh2t", "bvh4", "bvh8", "bvh8f"])
-    ap.add_argument("--sah", action="store_true",
-                    help="wide BVH kinds: SAH-optimal collapse; binary kinds: treelet restructuring toward the SAH")
+    ap.add_argument("--sah", action="store_true", help="(the default) SOLRT_BVH_SAH: binary kinds restructured by "
+                                                        "treelets toward the SAH, wide kinds collapsed by SAH")
+    ap.add_argument("--lbvh", action="store_true", help="plain LBVH (no SOLRT_BVH_SAH)")
     ap.add_argument("--kernel", default="wavefront", choices=["wavefront", "mega"],
                     help="mega: the plain per-pixel kernel (the reference's loop structure) on the same workload")
     ap.add_argument("--nee", action="store_true",
@@ -832,6 +833,7 @@ def main():
     ap.add_argument("--capacity", type=int, default=0,
                     help="paths per pass of the timed context (0 = library default; small profiler captures)")
     args = ap.parse_args()
+    args.sah = not args.lbvh
     world, rank, local, pg = dist_setup(args)
     if args.impl == "reference":
         return run_reference(args, world, rank, pg)
@@ -842,7 +844,7 @@ def main():
     if args.workload == "serve":
         importlib.import_module("sol-rs_gb300.build").build_lib()
         out = run_serve(local, args.rate, args.duration, policy=1 if args.policy == "shortest" else 0,
-                        stop_rmse=args.stop_rmse, drain_s=args.drain)
+                        stop_rmse=args.stop_rmse, drain_s=args.drain, sah=args.sah)
         if rank == 0:
             print(json.dumps({"metric": "p99 job latency (served render jobs)", "value": out["p99_latency_ms"],
                               "unit": "ms", "higher_is_better": False, "n_gpus": world, "serving": out}), flush=True)
@@ -974,7 +976,7 @@ def main():
     # extend launches also trace the shadow rays of --nee (same bytes per ray assumed)
     achieved = ((st.segments + st.shadow_segments) * b_seg) / ext_s / 1e9 if ext_s > 0 else 0.0
     traffic = dram = None
-    cap = EXTEND_CAPTURES.get(args.workload)
+    cap = EXTEND_CAPTURES.get((args.workload, "treelet" if args.sah else "lbvh"))
     if cap and info.kind == solrt.BVH2 and args.kernel != "mega" and not args.nee and ext_s > 0:
         seg_per_launch = st.segments / max(st.extend_launches, 1)
         traffic = round(cap["dram_bytes_per_segment"] * seg_per_launch)
@@ -1025,7 +1027,8 @@ def main():
     precision = None
     if rank == 0 and args.workload == "soup" and not args.no_precision:
         try:
-            precision = precision_study(local, data, kw, cam, value / max(world, 1), info, nodes_per_seg, tris_per_seg)
+            precision = precision_study(local, data, kw, cam, value / max(world, 1), info, nodes_per_seg, tris_per_seg,
+                                        main_sah=args.sah)
         except Exception as ex:
             precision = {"error": str(ex)}
     # parity and convergence of the other single-scene configurations at
@@ -1054,7 +1057,7 @@ def main():
             batched = {"error": str(ex)}
         try:
             serving = run_serve(local, args.rate, args.duration, policy=1 if args.policy == "shortest" else 0,
-                                stop_rmse=args.stop_rmse, drain_s=args.drain)
+                                stop_rmse=args.stop_rmse, drain_s=args.drain, sah=args.sah)
         except Exception as ex:
             serving = {"error": str(ex)}
         # the same distribution at a rate the GPU keeps up with (about half
@@ -1063,7 +1066,8 @@ def main():
             try:
                 serving["below_capacity"] = run_serve(local, args.steady_rate, args.steady_duration,
                                                       policy=1 if args.policy == "shortest" else 0,
-                                                      stop_rmse=args.stop_rmse, drain_s=args.drain, seed=6)
+                                                      stop_rmse=args.stop_rmse, drain_s=args.drain, seed=6,
+                                                      sah=args.sah)
             except Exception as ex:
                 serving["below_capacity"] = {"error": str(ex)}
     out = None

@@ -340,6 +340,7 @@ class SceneDescription:
         self.dynamic = dynamic or bvh == BVH2_TWO_LEVEL   # two-level scenes take instances too
         d = scene_desc(data)
         bd = BvhDesc(kind=bvh, leaf_max=leaf_max, flags=(BVH_DYNAMIC if dynamic else 0) | (BVH_SAH if sah else 0))
+        self._build = (leaf_max, sah)   # what a static rebuild repeats
         h = ctypes.c_void_p()
         check(lib().solrt_scene_create(context.handle, ctypes.byref(d), ctypes.byref(bd), ctypes.byref(h)))
         self.handle = h
@@ -383,15 +384,17 @@ class SceneDescription:
     def build_bvh(self, bvh=BVH2, leaf_max=0, sah=False):
         check(lib().solrt_scene_build_bvh(self.handle, ctypes.byref(
             BvhDesc(kind=bvh, leaf_max=leaf_max, flags=BVH_SAH if sah else 0))))
+        self._build = (leaf_max, sah)
 
     def tlas_regenerate(self, mode=REGEN_REBUILD):
         """Dynamic scene: applies the staged instance transforms on the
         device and rebuilds (or refits) the BVH. Static scene: rebuilds the
-        BVH with its current kind."""
+        BVH with its current kind, leaf size and SAH option."""
         if self.dynamic:
             check(lib().solrt_scene_regenerate(self.handle, mode))
         else:
-            self.build_bvh(self.bvh_info().kind)
+            leaf_max, sah = self._build
+            self.build_bvh(self.bvh_info().kind, leaf_max=leaf_max, sah=sah)
 
     def bvh_info(self):
         i = BvhInfo()

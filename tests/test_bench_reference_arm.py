@@ -35,7 +35,7 @@ def test_reference_arm_line():
     cfg = d["config"]
     assert cfg["workload"].startswith("procedural Cornell box 32 tris, 256x256, 16 spp")
     assert cfg["width"] == 256 and cfg["spp"] == 16 and cfg["max_depth"] == 5
-    assert cfg["parallelism"] == "single" and cfg["bvh"] == "bvh2" and "l2" in cfg
+    assert cfg["parallelism"] == "single" and cfg["bvh"] == "bvh2+sah" and "l2" in cfg
     mapped = [l for l in r.stdout.splitlines() if l.startswith("MAPPED")][0].split()
     assert mapped[1] == "False", "the reference arm loaded the CUDA library"
     assert mapped[2] == "True"
