@@ -52,6 +52,13 @@ EXTEND_CAPTURES = {
              "limiter": {"l1tex_lsu_wavefronts_pct": 83.8, "l1tex_throughput_pct": 87.8, "issue_active_pct": 60.7,
                          "threads_per_instruction": 14.27, "warps_active_pct": 48.0, "l2_hit_pct": 96.7,
                          "dram_throughput_pct": 1.4, "source": "profiles/extend_soup1M_bvh2_full.md"}},
+    ("soup", "treelet"): {"dram_bytes_per_segment": 62.2, "dram_source": "profiles/extend_dram_soup1M_tunnel4M.md",
+                          "limiter": None},
+    ("tunnel", "treelet"): {"dram_bytes_per_segment": 78.0, "dram_source": "profiles/extend_dram_soup1M_tunnel4M.md",
+                            "limiter": {"l1tex_lsu_wavefronts_pct": 70.0, "l1tex_throughput_pct": 75.1,
+                                        "issue_active_pct": 65.2, "threads_per_instruction": 14.55,
+                                        "warps_active_pct": 46.7, "l2_hit_pct": 90.1,
+                                        "source": "profiles/extend_tunnel_640x360_full.md (treelet BVH2, bounce level 1)"}},
     ("tunnel", "lbvh"): {"dram_bytes_per_segment": 78.8, "dram_source": "profiles/extend_dram_soup1M_tunnel4M.md",
                "limiter": {"l1tex_lsu_wavefronts_pct": 71.9, "l1tex_throughput_pct": 77.7, "issue_active_pct": 65.0,
                            "threads_per_instruction": 14.52, "warps_active_pct": 46.9, "l2_hit_pct": 91.7,
