@@ -46,14 +46,18 @@ NODE_BYTES = {0: 64, 1: 80, 2: 64, 3: 224, 4: 32, 5: 64}
 # all extend launches of one full wavefront pass, divided by the segments
 # the pass traced (profiles/extend_dram_soup1M_tunnel4M.md). limiter: the
 # counters of one `ncu --set full` launch (profiles/extend_soup1M_bvh2_full.md,
-# profiles/extend_tunnel_640x360_full.md).
+# profiles/extend_soup1M_treelet_full.md, profiles/extend_tunnel_640x360_full.md).
+# Keys: (workload, "lbvh" or "treelet" BVH2).
 EXTEND_CAPTURES = {
     ("soup", "lbvh"): {"dram_bytes_per_segment": 62.4, "dram_source": "profiles/extend_dram_soup1M_tunnel4M.md",
              "limiter": {"l1tex_lsu_wavefronts_pct": 83.8, "l1tex_throughput_pct": 87.8, "issue_active_pct": 60.7,
                          "threads_per_instruction": 14.27, "warps_active_pct": 48.0, "l2_hit_pct": 96.7,
                          "dram_throughput_pct": 1.4, "source": "profiles/extend_soup1M_bvh2_full.md"}},
     ("soup", "treelet"): {"dram_bytes_per_segment": 62.2, "dram_source": "profiles/extend_dram_soup1M_tunnel4M.md",
-                          "limiter": None},
+                          "limiter": {"l1tex_lsu_wavefronts_pct": 85.2, "l1tex_throughput_pct": 87.9,
+                                      "issue_active_pct": 66.1, "threads_per_instruction": 14.83,
+                                      "warps_active_pct": 48.7, "l2_hit_pct": 94.2,
+                                      "source": "profiles/extend_soup1M_treelet_full.md"}},
     ("tunnel", "treelet"): {"dram_bytes_per_segment": 78.0, "dram_source": "profiles/extend_dram_soup1M_tunnel4M.md",
                             "limiter": {"l1tex_lsu_wavefronts_pct": 70.0, "l1tex_throughput_pct": 75.1,
                                         "issue_active_pct": 65.2, "threads_per_instruction": 14.55,
