@@ -135,11 +135,12 @@ typedef enum solrt_bvh_kind {
 #define SOLRT_BVH_SAH 2u      /* BVH8 / BVH4 kinds: choose each wide node's children
                                  by the SAH-optimal collapse of the binary tree
                                  (dynamic program over the binary nodes) instead of
-                                 opening the largest child first. BVH2 / BVH2-q16
-                                 kinds: restructure the LBVH toward the SAH by
-                                 treelets of 7 leaves (three bottom-up rounds on the
-                                 device; a longer build, fewer node visits). Same
-                                 hits either way */
+                                 opening the largest child first, from a binary
+                                 tree restructured as below when leaf_max <= 1.
+                                 BVH2 / BVH2-q16 kinds: restructure the LBVH toward
+                                 the SAH by treelets of 7 leaves (three bottom-up
+                                 rounds on the device; a longer build, fewer node
+                                 visits). Same hits either way */
 
 typedef struct solrt_bvh_desc {
     uint32_t kind;       /* solrt_bvh_kind */

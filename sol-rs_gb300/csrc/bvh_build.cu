@@ -1048,7 +1048,12 @@ static solrt_status build_single_level(Context& ctx, Scene& sc, const solrt_bvh_
     const uint32_t n = sc.tri_count;
     Lbvh L;
     SOLRT_TRY(lbvh_build(ctx, sc.vpos.as<float4>(), sc.tri_idx.as<uint4>(), n, 0u, L));
-    if ((desc.flags & SOLRT_BVH_SAH) && (desc.kind == SOLRT_BVH2 || desc.kind == SOLRT_BVH2_Q16))
+    // Treelets for the binary kinds, and for the wide kinds when every leaf
+    // slot holds one triangle: their collapse then reads a node's leaf range
+    // only as "more than one triangle", which restructuring keeps true (a
+    // restructured node's leaves need not be contiguous any more).
+    const bool wide = desc.kind == SOLRT_BVH8_Q8 || desc.kind == SOLRT_BVH4_Q8 || desc.kind == SOLRT_BVH8_F32;
+    if ((desc.flags & SOLRT_BVH_SAH) && (!wide || desc.leaf_max <= 1u))
         SOLRT_TRY(treelet_restructure(ctx, sc.vpos.as<float4>(), sc.tri_idx.as<uint4>(), 0u, L, kTreeletRounds));
     const uint32_t ni = L.ni;
     if (desc.kind == SOLRT_BVH8_Q8 || desc.kind == SOLRT_BVH4_Q8 || desc.kind == SOLRT_BVH8_F32) {
