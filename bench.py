@@ -964,7 +964,7 @@ def main():
     if args.workload == "instances":
         S = solrt.scenes
         moved = S.instanced_soups(4, 16384, seed=5, angle=10.0).instances
-        dyn = solrt.SceneDescription(ctx, data, bvh=bvh, keep_data=False, dynamic=True)
+        dyn = solrt.SceneDescription(ctx, data, bvh=bvh, keep_data=False, dynamic=True, sah=args.sah)
         regen = {}
         for name, mode in (("rebuild", solrt.REGEN_REBUILD), ("refit", solrt.REGEN_REFIT)):
             ts = []

@@ -137,7 +137,8 @@ typedef enum solrt_bvh_kind {
                                  (dynamic program over the binary nodes) instead of
                                  opening the largest child first, from a binary
                                  tree restructured as below when leaf_max <= 1.
-                                 BVH2 / BVH2-q16 kinds: restructure the LBVH toward
+                                 BVH2 / BVH2-q16 kinds (and each BLAS of the
+                                 two-level kind): restructure the LBVH toward
                                  the SAH by treelets of 7 leaves (three bottom-up
                                  rounds on the device; a longer build, fewer node
                                  visits). Same hits either way */

@@ -773,6 +773,10 @@ static solrt_status build_tlas(Context& ctx, Scene& sc) {
 // The BLASes of a two-level scene: one LBVH per non-empty section over its
 // object-space triangles, concatenated (nodes, then triangles in the
 // sections' order), then the TLAS.
+static solrt_status treelet_restructure(Context& ctx, const float4* vpos, const uint4* tri_idx, uint32_t prim_base,
+                                        Lbvh& L, int rounds);
+constexpr int kTreeletRoundsTwoLevel = 3;
+
 static solrt_status build_two_level(Context& ctx, Scene& sc) {
     cudaStream_t st = ctx.stream;
     const uint32_t S = sc.section_count;
@@ -794,6 +798,9 @@ static solrt_status build_two_level(Context& ctx, Scene& sc) {
         if (cnt == 0) continue;
         Lbvh L;
         SOLRT_TRY(lbvh_build(ctx, sc.opos.as<float4>(), sc.tri_idx.as<uint4>() + first, cnt, first, L));
+        if (sc.desc.flags & SOLRT_BVH_SAH)  // each BLAS restructured by treelets
+            SOLRT_TRY(treelet_restructure(ctx, sc.opos.as<float4>(), sc.tri_idx.as<uint4>() + first, first, L,
+                                          kTreeletRoundsTwoLevel));
         SOLRT_CUDA(cudaMemcpyAsync(sc.nodes.as<float4>() + 4 * (size_t)node_off, L.nodes.ptr,
                                    4 * sizeof(float4) * (size_t)L.ni, cudaMemcpyDeviceToDevice, st));
         SOLRT_CUDA(cudaMemcpyAsync(sc.tri_wt.as<float4>() + 3 * (size_t)first, L.tri_wt.ptr,

@@ -131,9 +131,10 @@ def transformed_cornell():
 
 def bvh_args(solrt_mod, name):
     """SceneDescription keyword arguments of a BVH name: bvh_kind's names,
-    plus "bvh8s" / "bvh4s" for the wide kinds with the SAH collapse and
-    "bvh2s" for the binary tree restructured by treelets."""
-    if name in ("bvh8s", "bvh4s", "bvh2s"):
+    plus "bvh8s" / "bvh4s" for the wide kinds with the SAH collapse,
+    "bvh2s" for the binary tree restructured by treelets and "bvh2ts" for
+    the two-level kind with every BLAS restructured so."""
+    if name in ("bvh8s", "bvh4s", "bvh2s", "bvh2ts"):
         return dict(bvh=bvh_kind(solrt_mod, name[:-1]), sah=True)
     return dict(bvh=bvh_kind(solrt_mod, name))
 

@@ -6,7 +6,7 @@ same closest hits), and like the oracle."""
 import numpy as np
 import pytest
 
-from helpers import S, bvh_kind, camera_of, hits_equal, random_rays
+from helpers import S, bvh_args, camera_of, hits_equal, random_rays
 
 pytestmark = pytest.mark.gpu
 
@@ -42,11 +42,14 @@ def _render(solrt, ctx, sc, cam, w, h, p):
 
 @pytest.mark.parametrize("integ", ["path", "nee"])
 @pytest.mark.parametrize("mode", ["rebuild", "refit"])
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh2t", "bvh4", "bvh8", "bvh8f"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh2s", "bvh2q", "bvh2t", "bvh2ts", "bvh4", "bvh8", "bvh8f"])
 def test_regenerate_matches_fresh_scene(solrt, oracle, ctx, bvh, mode, integ):
     """nee: the light tree of next-event estimation is rebuilt from the moved
-    vertices, as a fresh scene builds it (the light section moves too)."""
-    kind = bvh_kind(solrt, bvh)
+    vertices, as a fresh scene builds it (the light section moves too).
+    bvh2s / bvh2ts: the treelet restructuring (of the whole tree, or of each
+    BLAS) gives a rebuilt dynamic scene the fresh scene's bytes too."""
+    args = bvh_args(solrt, bvh)
+    kind = args["bvh"]
     regen = solrt.REGEN_REBUILD if mode == "rebuild" else solrt.REGEN_REFIT
     base = S.cornell()
     w, h = 32, 32
@@ -54,13 +57,13 @@ def test_regenerate_matches_fresh_scene(solrt, oracle, ctx, bvh, mode, integ):
     p = solrt.render_params(w, h, spp=2, max_bounces=4, material_mode=solrt.MATERIAL_LAMBERT,
                             rng_mode=solrt.RNG_PER_SAMPLE, seed=9,
                             integrator=solrt.INTEGRATOR_PATH_NEE if integ == "nee" else solrt.INTEGRATOR_PATH)
-    dyn = solrt.SceneDescription(ctx, base, bvh=kind, dynamic=True)
+    dyn = solrt.SceneDescription(ctx, base, dynamic=True, **args)
     rays = random_rays(4000, -0.2, 1.2, seed=21)
     for f, transforms in enumerate(_frames(len(base.sections))):
         dyn.blas_transforms(transforms)
         dyn.tlas_regenerate(regen)
         moved = _with_instances(solrt, base, transforms)
-        fresh = solrt.SceneDescription(ctx, moved, bvh=kind)
+        fresh = solrt.SceneDescription(ctx, moved, **args)
         a = _render(solrt, ctx, dyn, cam, w, h, p)
         b = _render(solrt, ctx, fresh, cam, w, h, p)
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), f

@@ -25,7 +25,7 @@ from helpers import S, bvh_args, camera_of
 
 pytestmark = pytest.mark.gpu
 
-KINDS = ["bvh2", "bvh2s", "bvh2q", "bvh2t", "bvh4", "bvh4s", "bvh8", "bvh8s", "bvh8f"]
+KINDS = ["bvh2", "bvh2s", "bvh2q", "bvh2t", "bvh2ts", "bvh4", "bvh4s", "bvh8", "bvh8s", "bvh8f"]
 N_RAYS = 1 << 22
 _cache = {}
 

@@ -93,8 +93,8 @@ def test_render_bit_exact(solrt, oracle, ctx, name, bvh):
     assert np.isfinite(ga).all() and ga[..., :3].mean() > 0
 
 
-@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh4", "bvh8"])
-@pytest.mark.parametrize("name", ["cornell_ref_sky", "soup_gradient", "tunnel_kahan"])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh2t", "bvh4", "bvh8"])
+@pytest.mark.parametrize("name", ["cornell_ref_sky", "soup_gradient", "tunnel_kahan", "transformed"])
 def test_render_bit_exact_sah_collapse(solrt, oracle, ctx, name, bvh):
     """Wide BVHs collapsed by SAH, and binary BVHs restructured by treelets,
     render the oracle's image too."""
