@@ -831,25 +831,31 @@ static solrt_status build_two_level(Context& ctx, Scene& sc) {
 // Treelet restructuring of the LBVH toward the SAH (Karras and Aila, "Fast
 // parallel construction of high-quality bounding volume hierarchies", HPG
 // 2013), for the binary kinds with SOLRT_BVH_SAH. Bottom up, as the refit
-// walks: the second thread to reach an internal node owns its subtree; it
-// grows a treelet from the node's two children by replacing the internal
-// treelet leaf of largest surface area with its two children until the
-// treelet has kTreeletLeaves leaves (or only triangles are left), finds by
-// a dynamic program over the subsets of those leaves the binary tree of
-// least SAH cost (node visit 1, triangle test kSahTri, per unit of surface
-// area), and, when it is cheaper than the subtree as it is, rewrites the
-// treelet's internal nodes (the node itself stays the treelet's root, the
-// expanded nodes are reused in expansion order). Leaves keep their positions
-// in the leaf order, so the triangle stream is unchanged; only child and
-// parent links, exact boxes and subtree costs change. Deterministic: a
-// node's result depends only on its subtree, which is final when the node
-// is processed, and ties go to the first candidate in a fixed order.
+// walks: the second thread to reach an internal node owns its subtree, and
+// its warp processes the node's treelet, all 32 lanes together, one owned
+// node after another (the top of the tree, where one node at a time is
+// ready, is the latency of the whole pass). The treelet grows from the
+// node's two children by replacing the internal treelet leaf of largest
+// surface area with its two children until it has kTreeletLeaves leaves (or
+// only triangles are left; lane q holds leaf q); a dynamic program over the
+// subsets of those leaves, one subset size after another with a subset per
+// lane, finds the binary tree of least SAH cost (node visit 1, triangle test
+// kSahTri, per unit of surface area); when that is cheaper than the subtree
+// as it is, the treelet's internal nodes are rewritten (the node itself
+// stays the treelet's root, the expanded nodes are reused in expansion
+// order). Leaves keep their positions in the leaf order, so the triangle
+// stream is unchanged; only child and parent links, exact boxes and subtree
+// costs change. Deterministic: a node's result depends only on its subtree,
+// which is final when the node is processed, and ties go to the first
+// candidate in a fixed order (the lowest leaf; the first partition in the
+// submask order).
 // ---------------------------------------------------------------------------
 
 namespace {
 
 constexpr int kTreeletLeaves = 7;
 constexpr int kTreeletRounds = 3;
+constexpr int kTreeletWarps = 4;  // warps per block of k_treelet
 constexpr float kSahTri = 0.3f;
 
 SOLRT_D float box_area(const float b[6]) {
@@ -859,7 +865,7 @@ SOLRT_D float box_area(const float b[6]) {
 
 // Exact box (lo.xyz, hi.xyz) of a child reference: a leaf's triangle from
 // the leaf-ordered stream, an internal node's from `nbox` (written by other
-// threads: read through L2).
+// warps: read through L2).
 SOLRT_D void ref_box(uint32_t ref, const float4* __restrict__ tri_wt, const float4* nbox, float b[6]) {
     if (ref & 0x80000000u) {
         const size_t k = ref & 0x7fffffffu;
@@ -872,101 +878,108 @@ SOLRT_D void ref_box(uint32_t ref, const float4* __restrict__ tri_wt, const floa
     }
 }
 
-__global__ void k_treelet(const float4* __restrict__ tri_wt, uint32_t* child, uint32_t* par_int,
-                          uint32_t* par_leaf, float4* nbox, float* cost, unsigned int* __restrict__ flags,
-                          uint32_t n) {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= n || n < 3) return;
-    uint32_t p = par_leaf[k];
-    float cs[1 << kTreeletLeaves];          // least SAH cost of each subset of treelet leaves
-    uint8_t part[1 << kTreeletLeaves];      // its best first part (a subset holding the lowest leaf)
-    for (uint32_t steps = 0; steps < n; ++steps) {
-        if (p >= n - 1) return;  // malformed parent link
-        __threadfence();
-        if (atomicAdd(flags + p, 1u) == 0u) return;  // the sibling subtree is not done yet
-        __threadfence();
-        // the treelet of p
-        uint32_t lref[kTreeletLeaves], inner[kTreeletLeaves - 2];
-        float lb[kTreeletLeaves][6], la[kTreeletLeaves];
-        int nl = 2, nin = 0;
-        lref[0] = __ldcg(child + 2 * (size_t)p);
-        lref[1] = __ldcg(child + 2 * (size_t)p + 1);
-#pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            ref_box(lref[q], tri_wt, nbox, lb[q]);
-            la[q] = box_area(lb[q]);
-        }
-        while (nl < kTreeletLeaves) {
-            int j = -1;
-            float best = -1.0f;
-            for (int q = 0; q < nl; ++q)
-                if (!(lref[q] & 0x80000000u) && la[q] > best) {
-                    best = la[q];
-                    j = q;
-                }
-            if (j < 0) break;
-            const uint32_t r = lref[j];
-            inner[nin++] = r;
-            lref[j] = __ldcg(child + 2 * (size_t)r);
-            lref[nl] = __ldcg(child + 2 * (size_t)r + 1);
-            ref_box(lref[j], tri_wt, nbox, lb[j]);
-            la[j] = box_area(lb[j]);
-            ref_box(lref[nl], tri_wt, nbox, lb[nl]);
-            la[nl] = box_area(lb[nl]);
-            ++nl;
-        }
-        float lc[kTreeletLeaves];
-        for (int q = 0; q < nl; ++q) lc[q] = (lref[q] & 0x80000000u) ? kSahTri * la[q] : __ldcg(cost + lref[q]);
-        const uint32_t full = (1u << nl) - 1u;
-        float pb[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
-        for (int q = 0; q < nl; ++q)
+// A warp's working set for one treelet.
+struct TreeletSmem {
+    float cs[1 << kTreeletLeaves];    // least SAH cost of each subset of treelet leaves
+    float ar[1 << kTreeletLeaves];    // surface area of each subset's box
+    uint8_t part[1 << kTreeletLeaves];  // its best first part (a subset holding the lowest leaf)
+    float lb[kTreeletLeaves][6];      // leaf boxes
+    uint32_t lref[kTreeletLeaves];    // leaf references
+    uint32_t inner[kTreeletLeaves - 2];  // expanded internal nodes, in expansion order
+};
+
+SOLRT_D void subset_box(const TreeletSmem& s, uint32_t S, int nl, float b[6]) {
+    b[0] = b[1] = b[2] = INFINITY;
+    b[3] = b[4] = b[5] = -INFINITY;
+    for (int q = 0; q < nl; ++q)
+        if (S & (1u << q))
             for (int a = 0; a < 3; ++a) {
-                pb[a] = fminf(pb[a], lb[q][a]);
-                pb[3 + a] = fmaxf(pb[3 + a], lb[q][3 + a]);
+                b[a] = fminf(b[a], s.lb[q][a]);
+                b[3 + a] = fmaxf(b[3 + a], s.lb[q][3 + a]);
             }
-        // cost of the subtree as it stands: its two children are final, their
-        // costs known (treelet slots 0 and 1 before any expansion)
-        float cur;
-        {
-            const uint32_t c0 = __ldcg(child + 2 * (size_t)p), c1 = __ldcg(child + 2 * (size_t)p + 1);
-            float b0[6], b1[6];
-            ref_box(c0, tri_wt, nbox, b0);
-            ref_box(c1, tri_wt, nbox, b1);
-            const float k0 = (c0 & 0x80000000u) ? kSahTri * box_area(b0) : __ldcg(cost + c0);
-            const float k1 = (c1 & 0x80000000u) ? kSahTri * box_area(b1) : __ldcg(cost + c1);
-            cur = box_area(pb) + (k0 + k1);
+}
+
+// The treelet of node p, by all 32 lanes of the calling warp.
+SOLRT_D void treelet_warp(uint32_t p, TreeletSmem& s, const float4* __restrict__ tri_wt, uint32_t* child,
+                          uint32_t* par_int, uint32_t* par_leaf, float4* nbox, float* cost) {
+    const uint32_t lane = threadIdx.x & 31u;
+    // lanes 0 and 1 start with the node's children; lane q holds leaf q
+    uint32_t ref = 0xffffffffu;
+    float b[6], area = -1.0f, kinit = 0.0f;
+    if (lane < 2) {
+        ref = __ldcg(child + 2 * (size_t)p + lane);
+        ref_box(ref, tri_wt, nbox, b);
+        area = box_area(b);
+        kinit = (ref & 0x80000000u) ? kSahTri * area : __ldcg(cost + ref);
+    }
+    const float k0 = __shfl_sync(0xffffffffu, kinit, 0), k1 = __shfl_sync(0xffffffffu, kinit, 1);
+    int nl = 2, nin = 0;
+    uint32_t inner = 0;  // lane i holds the i-th expanded node
+    while (nl < kTreeletLeaves) {
+        // the internal leaf of largest area, the lowest index among equals
+        float best = ((int)lane < nl && !(ref & 0x80000000u) && area >= 0.0f) ? area : -1.0f;
+        uint32_t bi = lane;
+#pragma unroll
+        for (int off = 16; off; off >>= 1) {
+            const float ob = __shfl_xor_sync(0xffffffffu, best, off);
+            const uint32_t oi = __shfl_xor_sync(0xffffffffu, bi, off);
+            if (ob > best || (ob == best && oi < bi)) {
+                best = ob;
+                bi = oi;
+            }
         }
-        bool rebuild = false;
-        if (nl >= 3) {
-            for (uint32_t S = 1; S <= full; ++S) {
+        if (best < 0.0f) break;  // only triangles left
+        const uint32_t r = __shfl_sync(0xffffffffu, ref, bi);
+        if ((int)lane == nin) inner = r;
+        ++nin;
+        if (lane == bi || (int)lane == nl) {
+            ref = __ldcg(child + 2 * (size_t)r + (lane == bi ? 0u : 1u));
+            ref_box(ref, tri_wt, nbox, b);
+            area = box_area(b);
+        }
+        ++nl;
+    }
+    if ((int)lane < nl) {
+        for (int a = 0; a < 6; ++a) s.lb[lane][a] = b[a];
+        s.lref[lane] = ref;
+        s.cs[1u << lane] = (ref & 0x80000000u) ? kSahTri * area : __ldcg(cost + ref);
+        s.part[1u << lane] = 0;
+    }
+    if ((int)lane < nin) s.inner[lane] = inner;
+    __syncwarp();
+    const uint32_t full = (1u << nl) - 1u;
+    for (uint32_t S = lane + 1u; S <= full; S += 32u) {
+        float u[6];
+        subset_box(s, S, nl, u);
+        s.ar[S] = box_area(u);
+    }
+    __syncwarp();
+    // cost of the subtree as it stands: its two children are final
+    const float cur = s.ar[full] + (k0 + k1);
+    bool rebuild = false;
+    if (nl >= 3) {
+        for (int sz = 2; sz <= nl; ++sz) {
+            for (uint32_t S = lane + 1u; S <= full; S += 32u) {
+                if (__popc(S) != sz) continue;
                 const uint32_t low = S & (0u - S);
-                if (S == low) {
-                    cs[S] = lc[__ffs(S) - 1];
-                    part[S] = 0;
-                    continue;
-                }
-                float b[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
-                for (int q = 0; q < nl; ++q)
-                    if (S & (1u << q))
-                        for (int a = 0; a < 3; ++a) {
-                            b[a] = fminf(b[a], lb[q][a]);
-                            b[3 + a] = fmaxf(b[3 + a], lb[q][3 + a]);
-                        }
-                float best = INFINITY;
+                float bestv = INFINITY;
                 uint32_t bp = low;
                 for (uint32_t P = (S - 1u) & S; P != 0u; P = (P - 1u) & S) {
                     if (!(P & low)) continue;
-                    const float v = cs[P] + cs[S ^ P];
-                    if (v < best) {
-                        best = v;
+                    const float v = s.cs[P] + s.cs[S ^ P];
+                    if (v < bestv) {
+                        bestv = v;
                         bp = P;
                     }
                 }
-                cs[S] = box_area(b) + best;
-                part[S] = (uint8_t)bp;
+                s.cs[S] = s.ar[S] + bestv;
+                s.part[S] = (uint8_t)bp;
             }
-            rebuild = cs[full] < cur * (1.0f - 1e-5f);
+            __syncwarp();
         }
+        rebuild = s.cs[full] < cur * (1.0f - 1e-5f);
+    }
+    if (lane == 0) {
         if (rebuild) {
             // rewrite the treelet top down: (subset, node) pairs
             uint32_t stS[kTreeletLeaves], stN[kTreeletLeaves];
@@ -975,41 +988,76 @@ __global__ void k_treelet(const float4* __restrict__ tri_wt, uint32_t* child, ui
             stN[sp++] = p;
             while (sp > 0) {
                 const uint32_t S = stS[--sp], node = stN[sp];
-                float b[6] = {INFINITY, INFINITY, INFINITY, -INFINITY, -INFINITY, -INFINITY};
-                for (int q = 0; q < nl; ++q)
-                    if (S & (1u << q))
-                        for (int a = 0; a < 3; ++a) {
-                            b[a] = fminf(b[a], lb[q][a]);
-                            b[3 + a] = fmaxf(b[3 + a], lb[q][3 + a]);
-                        }
-                nbox[2 * (size_t)node] = make_float4(b[0], b[1], b[2], 0.0f);
-                nbox[2 * (size_t)node + 1] = make_float4(b[3], b[4], b[5], 0.0f);
-                cost[node] = cs[S];
-                const uint32_t sides[2] = {part[S], S ^ part[S]};
+                float u[6];
+                subset_box(s, S, nl, u);
+                nbox[2 * (size_t)node] = make_float4(u[0], u[1], u[2], 0.0f);
+                nbox[2 * (size_t)node + 1] = make_float4(u[3], u[4], u[5], 0.0f);
+                cost[node] = s.cs[S];
+                const uint32_t sides[2] = {s.part[S], S ^ s.part[S]};
 #pragma unroll
                 for (int side = 0; side < 2; ++side) {
                     const uint32_t T = sides[side];
-                    uint32_t ref;
+                    uint32_t cref;
                     if ((T & (T - 1u)) == 0u) {
-                        ref = lref[__ffs(T) - 1];
-                        if (ref & 0x80000000u) par_leaf[ref & 0x7fffffffu] = node;
-                        else par_int[ref] = node;
+                        cref = s.lref[__ffs(T) - 1];
+                        if (cref & 0x80000000u) par_leaf[cref & 0x7fffffffu] = node;
+                        else par_int[cref] = node;
                     } else {
-                        ref = inner[used++];
-                        par_int[ref] = node;
+                        cref = s.inner[used++];
+                        par_int[cref] = node;
                         stS[sp] = T;
-                        stN[sp++] = ref;
+                        stN[sp++] = cref;
                     }
-                    child[2 * (size_t)node + side] = ref;
+                    child[2 * (size_t)node + side] = cref;
                 }
             }
         } else {
-            nbox[2 * (size_t)p] = make_float4(pb[0], pb[1], pb[2], 0.0f);
-            nbox[2 * (size_t)p + 1] = make_float4(pb[3], pb[4], pb[5], 0.0f);
+            float u[6];
+            subset_box(s, full, nl, u);
+            nbox[2 * (size_t)p] = make_float4(u[0], u[1], u[2], 0.0f);
+            nbox[2 * (size_t)p + 1] = make_float4(u[3], u[4], u[5], 0.0f);
             cost[p] = cur;
         }
-        if (p == 0) return;
-        p = __ldcg(par_int + p);
+    }
+    __syncwarp();
+}
+
+// One round over the tree: one thread per leaf walks up; the lanes that own
+// a node this step hand it to their warp in turn. Every lane stays in the
+// loop until its warp is done, so the warp-wide steps see all 32 lanes.
+__global__ void __launch_bounds__(32 * kTreeletWarps) k_treelet(const float4* __restrict__ tri_wt, uint32_t* child,
+                                                                uint32_t* par_int, uint32_t* par_leaf, float4* nbox,
+                                                                float* cost, unsigned int* __restrict__ flags,
+                                                                uint32_t n) {
+    __shared__ TreeletSmem smem[kTreeletWarps];
+    TreeletSmem& s = smem[threadIdx.x >> 5];
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    bool active = k < n;
+    uint32_t p = active ? par_leaf[k] : 0u;
+    for (uint32_t steps = 0; steps < n; ++steps) {
+        bool own = false;
+        if (active) {
+            if (p >= n - 1) {
+                active = false;  // malformed parent link
+            } else {
+                __threadfence();
+                if (atomicAdd(flags + p, 1u) == 0u) active = false;  // the sibling subtree is not done yet
+                else own = true;
+            }
+        }
+        __threadfence();
+        uint32_t m = __ballot_sync(0xffffffffu, own);
+        if (m == 0u) break;  // every lane has stopped
+        while (m) {
+            const int l = __ffs(m) - 1;
+            m &= m - 1u;
+            treelet_warp(__shfl_sync(0xffffffffu, p, l), s, tri_wt, child, par_int, par_leaf, nbox, cost);
+        }
+        __threadfence();
+        if (own) {
+            if (p == 0) active = false;
+            else p = __ldcg(par_int + p);
+        }
     }
 }
 
@@ -1028,10 +1076,9 @@ static solrt_status treelet_restructure(Context& ctx, const float4* vpos, const 
     SOLRT_TRY(depth.alloc(sizeof(unsigned int)));
     for (int r = 0; r < rounds; ++r) {
         SOLRT_CUDA(cudaMemsetAsync(flags.ptr, 0, flags.bytes, st));
-        k_treelet<<<blocks_for(n, 128), 128, 0, st>>>(L.tri_wt.as<float4>(), L.child.as<uint32_t>(),
-                                                      L.par_int.as<uint32_t>(), L.par_leaf.as<uint32_t>(),
-                                                      L.nbox.as<float4>(), cost.as<float>(),
-                                                      flags.as<unsigned int>(), n);
+        k_treelet<<<blocks_for(n, 32 * kTreeletWarps), 32 * kTreeletWarps, 0, st>>>(
+            L.tri_wt.as<float4>(), L.child.as<uint32_t>(), L.par_int.as<uint32_t>(), L.par_leaf.as<uint32_t>(),
+            L.nbox.as<float4>(), cost.as<float>(), flags.as<unsigned int>(), n);
         ++ctx.launches;
     }
     SOLRT_CUDA(cudaMemsetAsync(flags.ptr, 0, flags.bytes, st));
