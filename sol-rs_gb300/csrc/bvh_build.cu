@@ -19,6 +19,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
+#include <new>
 #include <vector>
 
 #include "bvh8.cuh"
@@ -773,8 +775,14 @@ static solrt_status build_tlas(Context& ctx, Scene& sc) {
 // The BLASes of a two-level scene: one LBVH per non-empty section over its
 // object-space triangles, concatenated (nodes, then triangles in the
 // sections' order), then the TLAS.
-static solrt_status treelet_restructure(Context& ctx, const float4* vpos, const uint4* tri_idx, uint32_t prim_base,
-                                        Lbvh& L, int rounds);
+// A binary LBVH to restructure by treelets, with the geometry lbvh_build got.
+struct TreeletInput {
+    const float4* vpos;
+    const uint4* tri_idx;
+    uint32_t prim_base;
+    Lbvh* L;
+};
+static solrt_status treelet_restructure(Context& ctx, const std::vector<TreeletInput>& in, int rounds);
 constexpr int kTreeletRoundsTwoLevel = 3;
 
 static solrt_status build_two_level(Context& ctx, Scene& sc) {
@@ -792,15 +800,24 @@ static solrt_status build_two_level(Context& ctx, Scene& sc) {
     sc.blas_box.assign(6 * (size_t)S, 0.0f);
     sc.blas_root.assign(S, -1);
     sc.blas_depth = 0;
+    // every section's LBVH, then (SOLRT_BVH_SAH) all of them restructured
+    // together, one k_treelet launch per round
+    std::unique_ptr<Lbvh[]> Ls(new (std::nothrow) Lbvh[S]);
+    if (!Ls) return SOLRT_ERR_OOM;
+    std::vector<TreeletInput> tin;
+    for (uint32_t s = 0; s < S; ++s) {
+        const uint32_t cnt = sc.sec_tri_count[s], first = sc.sec_tri_first[s];
+        if (cnt == 0) continue;
+        SOLRT_TRY(lbvh_build(ctx, sc.opos.as<float4>(), sc.tri_idx.as<uint4>() + first, cnt, first, Ls[s]));
+        tin.push_back(TreeletInput{sc.opos.as<float4>(), sc.tri_idx.as<uint4>() + first, first, &Ls[s]});
+    }
+    if (sc.desc.flags & SOLRT_BVH_SAH) SOLRT_TRY(treelet_restructure(ctx, tin, kTreeletRoundsTwoLevel));
+    std::vector<float4> boxes(2 * (size_t)S);
     uint32_t node_off = 0;
     for (uint32_t s = 0; s < S; ++s) {
         const uint32_t cnt = sc.sec_tri_count[s], first = sc.sec_tri_first[s];
         if (cnt == 0) continue;
-        Lbvh L;
-        SOLRT_TRY(lbvh_build(ctx, sc.opos.as<float4>(), sc.tri_idx.as<uint4>() + first, cnt, first, L));
-        if (sc.desc.flags & SOLRT_BVH_SAH)  // each BLAS restructured by treelets
-            SOLRT_TRY(treelet_restructure(ctx, sc.opos.as<float4>(), sc.tri_idx.as<uint4>() + first, first, L,
-                                          kTreeletRoundsTwoLevel));
+        const Lbvh& L = Ls[s];
         SOLRT_CUDA(cudaMemcpyAsync(sc.nodes.as<float4>() + 4 * (size_t)node_off, L.nodes.ptr,
                                    4 * sizeof(float4) * (size_t)L.ni, cudaMemcpyDeviceToDevice, st));
         SOLRT_CUDA(cudaMemcpyAsync(sc.tri_wt.as<float4>() + 3 * (size_t)first, L.tri_wt.ptr,
@@ -809,14 +826,18 @@ static solrt_status build_two_level(Context& ctx, Scene& sc) {
                                                             node_off, first);
         ++ctx.launches;
         SOLRT_CUDA(cudaGetLastError());
-        float4 box[2];
-        SOLRT_CUDA(cudaMemcpyAsync(box, L.nbox.ptr, sizeof(box), cudaMemcpyDeviceToHost, st));
-        SOLRT_CUDA(cudaStreamSynchronize(st));
-        const float b[6] = {box[0].x, box[0].y, box[0].z, box[1].x, box[1].y, box[1].z};
-        for (int i = 0; i < 6; ++i) sc.blas_box[6 * s + i] = b[i];
+        SOLRT_CUDA(cudaMemcpyAsync(boxes.data() + 2 * (size_t)s, L.nbox.ptr, 2 * sizeof(float4),
+                                   cudaMemcpyDeviceToHost, st));
         sc.blas_root[s] = (int32_t)node_off;
         node_off += L.ni;
         sc.blas_depth = std::max(sc.blas_depth, L.depth);
+    }
+    SOLRT_CUDA(cudaStreamSynchronize(st));
+    for (uint32_t s = 0; s < S; ++s) {
+        if (sc.sec_tri_count[s] == 0) continue;
+        const float4 lo = boxes[2 * (size_t)s], hi = boxes[2 * (size_t)s + 1];
+        const float b[6] = {lo.x, lo.y, lo.z, hi.x, hi.y, hi.z};
+        for (int i = 0; i < 6; ++i) sc.blas_box[6 * s + i] = b[i];
     }
     sc.info.node_count = node_off;
     sc.info.node_bytes = 64ull * node_off;
@@ -1022,16 +1043,42 @@ SOLRT_D void treelet_warp(uint32_t p, TreeletSmem& s, const float4* __restrict__
     __syncwarp();
 }
 
-// One round over the tree: one thread per leaf walks up; the lanes that own
-// a node this step hand it to their warp in turn. Every lane stays in the
-// loop until its warp is done, so the warp-wide steps see all 32 lanes.
-__global__ void __launch_bounds__(32 * kTreeletWarps) k_treelet(const float4* __restrict__ tri_wt, uint32_t* child,
-                                                                uint32_t* par_int, uint32_t* par_leaf, float4* nbox,
-                                                                float* cost, unsigned int* __restrict__ flags,
-                                                                uint32_t n) {
+// One binary LBVH of a k_treelet launch: its arrays, its triangle count
+// (at least 3) and its first block (blocks [block0, block0 + its leaves /
+// block size) of the launch are its own).
+struct TreeletTree {
+    const float4* tri_wt;
+    uint32_t* child;
+    uint32_t* par_int;
+    uint32_t* par_leaf;
+    float4* nbox;
+    float* cost;
+    unsigned int* flags;
+    uint32_t n, block0;
+};
+
+// One round over each tree of `trees` (ascending block0, the first 0): one
+// thread per leaf walks up; the lanes that own a node this step hand it to
+// their warp in turn. Every lane stays in the loop until its warp is done,
+// so the warp-wide steps see all 32 lanes.
+__global__ void __launch_bounds__(32 * kTreeletWarps) k_treelet(const TreeletTree* __restrict__ trees,
+                                                                uint32_t ntrees) {
     __shared__ TreeletSmem smem[kTreeletWarps];
     TreeletSmem& s = smem[threadIdx.x >> 5];
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    uint32_t lo = 0, hi = ntrees - 1u;  // the last tree with block0 <= blockIdx.x
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1u) >> 1;
+        if (trees[mid].block0 <= blockIdx.x) lo = mid;
+        else hi = mid - 1u;
+    }
+    const TreeletTree T = trees[lo];
+    const float4* tri_wt = T.tri_wt;
+    uint32_t *child = T.child, *par_int = T.par_int, *par_leaf = T.par_leaf;
+    float4* nbox = T.nbox;
+    float* cost = T.cost;
+    unsigned int* flags = T.flags;
+    const uint32_t n = T.n;
+    const uint32_t k = (blockIdx.x - T.block0) * blockDim.x + threadIdx.x;
     bool active = k < n;
     uint32_t p = active ? par_leaf[k] : 0u;
     for (uint32_t steps = 0; steps < n; ++steps) {
@@ -1063,38 +1110,63 @@ __global__ void __launch_bounds__(32 * kTreeletWarps) k_treelet(const float4* __
 
 }  // namespace
 
-// Restructures the binary LBVH `L` in place (rounds of k_treelet), then
-// writes its nodes again (k_refit) and its depth. Synchronises.
-static solrt_status treelet_restructure(Context& ctx, const float4* vpos, const uint4* tri_idx, uint32_t prim_base,
-                                        Lbvh& L, int rounds) {
-    const uint32_t n = L.n;
-    if (n < 3) return SOLRT_OK;
+// Restructures the binary LBVHs of `in` in place (rounds of k_treelet, each
+// one launch over all of them), then writes each one's nodes again (k_refit)
+// and its depth. Synchronises.
+static solrt_status treelet_restructure(Context& ctx, const std::vector<TreeletInput>& in, int rounds) {
     cudaStream_t st = ctx.stream;
-    DeviceBuffer flags, cost, depth;
-    SOLRT_TRY(flags.alloc(sizeof(unsigned int) * (size_t)L.ni));
-    SOLRT_TRY(cost.alloc(sizeof(float) * (size_t)L.ni));
-    SOLRT_TRY(depth.alloc(sizeof(unsigned int)));
+    std::vector<TreeletTree> trees;
+    std::vector<size_t> off;  // each tree's first entry in flags / cost
+    size_t total = 0;
+    uint32_t blocks = 0;
+    for (const TreeletInput& t : in) {
+        if (t.L->n < 3) continue;
+        trees.push_back(TreeletTree{t.L->tri_wt.as<float4>(), t.L->child.as<uint32_t>(), t.L->par_int.as<uint32_t>(),
+                                    t.L->par_leaf.as<uint32_t>(), t.L->nbox.as<float4>(), nullptr, nullptr, t.L->n,
+                                    blocks});
+        off.push_back(total);
+        total += t.L->ni;
+        blocks += blocks_for(t.L->n, 32 * kTreeletWarps);
+    }
+    if (trees.empty()) return SOLRT_OK;
+    const uint32_t nt = (uint32_t)trees.size();
+    DeviceBuffer flags, cost, depth, table;
+    SOLRT_TRY(flags.alloc(sizeof(unsigned int) * total));
+    SOLRT_TRY(cost.alloc(sizeof(float) * total));
+    SOLRT_TRY(depth.alloc(sizeof(unsigned int) * (size_t)nt));
+    SOLRT_TRY(table.alloc(sizeof(TreeletTree) * (size_t)nt));
+    for (uint32_t i = 0; i < nt; ++i) {
+        trees[i].flags = flags.as<unsigned int>() + off[i];
+        trees[i].cost = cost.as<float>() + off[i];
+    }
+    SOLRT_CUDA(cudaMemcpyAsync(table.ptr, trees.data(), sizeof(TreeletTree) * (size_t)nt, cudaMemcpyHostToDevice, st));
     for (int r = 0; r < rounds; ++r) {
         SOLRT_CUDA(cudaMemsetAsync(flags.ptr, 0, flags.bytes, st));
-        k_treelet<<<blocks_for(n, 32 * kTreeletWarps), 32 * kTreeletWarps, 0, st>>>(
-            L.tri_wt.as<float4>(), L.child.as<uint32_t>(), L.par_int.as<uint32_t>(), L.par_leaf.as<uint32_t>(),
-            L.nbox.as<float4>(), cost.as<float>(), flags.as<unsigned int>(), n);
+        k_treelet<<<blocks, 32 * kTreeletWarps, 0, st>>>(table.as<TreeletTree>(), nt);
         ++ctx.launches;
     }
     SOLRT_CUDA(cudaMemsetAsync(flags.ptr, 0, flags.bytes, st));
     SOLRT_CUDA(cudaMemsetAsync(depth.ptr, 0, depth.bytes, st));
-    k_refit<<<blocks_for(n, 256), 256, 0, st>>>(vpos, tri_idx, L.order.as<uint32_t>(), L.child.as<uint32_t>(),
-                                                L.par_int.as<uint32_t>(), L.par_leaf.as<uint32_t>(), n,
-                                                flags.as<unsigned int>(), L.nbox.as<float4>(), L.nodes.as<float4>(),
-                                                L.tri_wt.as<float4>(), prim_base);
-    k_depth<<<blocks_for(n, 256), 256, 0, st>>>(L.par_int.as<uint32_t>(), L.par_leaf.as<uint32_t>(), n,
-                                                depth.as<unsigned int>());
-    ctx.launches += 2;
+    uint32_t i = 0;
+    for (const TreeletInput& t : in) {
+        Lbvh& L = *t.L;
+        if (L.n < 3) continue;
+        k_refit<<<blocks_for(L.n, 256), 256, 0, st>>>(t.vpos, t.tri_idx, L.order.as<uint32_t>(), L.child.as<uint32_t>(),
+                                                      L.par_int.as<uint32_t>(), L.par_leaf.as<uint32_t>(), L.n,
+                                                      flags.as<unsigned int>() + off[i], L.nbox.as<float4>(),
+                                                      L.nodes.as<float4>(), L.tri_wt.as<float4>(), t.prim_base);
+        k_depth<<<blocks_for(L.n, 256), 256, 0, st>>>(L.par_int.as<uint32_t>(), L.par_leaf.as<uint32_t>(), L.n,
+                                                      depth.as<unsigned int>() + i);
+        ctx.launches += 2;
+        ++i;
+    }
     SOLRT_CUDA(cudaGetLastError());
-    unsigned int dh = 0;
-    SOLRT_CUDA(cudaMemcpyAsync(&dh, depth.ptr, sizeof(dh), cudaMemcpyDeviceToHost, st));
+    std::vector<unsigned int> dh(nt);
+    SOLRT_CUDA(cudaMemcpyAsync(dh.data(), depth.ptr, sizeof(unsigned int) * (size_t)nt, cudaMemcpyDeviceToHost, st));
     SOLRT_CUDA(cudaStreamSynchronize(st));
-    L.depth = dh;
+    i = 0;
+    for (const TreeletInput& t : in)
+        if (t.L->n >= 3) t.L->depth = dh[i++];
     return SOLRT_OK;
 }
 
@@ -1108,7 +1180,8 @@ static solrt_status build_single_level(Context& ctx, Scene& sc, const solrt_bvh_
     // restructured node's leaves need not be contiguous any more).
     const bool wide = desc.kind == SOLRT_BVH8_Q8 || desc.kind == SOLRT_BVH4_Q8 || desc.kind == SOLRT_BVH8_F32;
     if ((desc.flags & SOLRT_BVH_SAH) && (!wide || desc.leaf_max <= 1u))
-        SOLRT_TRY(treelet_restructure(ctx, sc.vpos.as<float4>(), sc.tri_idx.as<uint4>(), 0u, L, kTreeletRounds));
+        SOLRT_TRY(treelet_restructure(ctx, {TreeletInput{sc.vpos.as<float4>(), sc.tri_idx.as<uint4>(), 0u, &L}},
+                                      kTreeletRounds));
     const uint32_t ni = L.ni;
     if (desc.kind == SOLRT_BVH8_Q8 || desc.kind == SOLRT_BVH4_Q8 || desc.kind == SOLRT_BVH8_F32) {
         const uint32_t width = desc.kind == SOLRT_BVH4_Q8 ? 4u : 8u;
