@@ -257,7 +257,7 @@ def cpu_baseline(data, kw, cam, budget_s=10.0, threads=0):
 
 
 def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, main_tris, n_rays=1 << 22,
-                    kinds=None, render=True, main_sah=False):
+                    kinds=None, render=True, main_sah=False, capacity=0):
     """The 16-bit quantised binary BVH, the 8-bit quantised 4- and 8-wide BVHs
     and the FP32 8-wide BVH next to the FP32 binary BVH on the same scene:
     hit records of 4M rays (every pixel-centre camera ray of the frame, then
@@ -290,7 +290,8 @@ def precision_study(local, data, kw, cam, main_mrays, main_info, main_nodes, mai
     all_kinds = (("bvh2_fp32", solrt.BVH2, False), ("bvh2_treelet", solrt.BVH2, True), ("bvh2_q16", solrt.BVH2_Q16, False),
                  ("bvh4_q8", solrt.BVH4_Q8, False), ("bvh8_q8", solrt.BVH8_Q8, False),
                  ("bvh8_q8_sah", solrt.BVH8_Q8, True), ("bvh8_fp32", solrt.BVH8_F32, False))
-    with solrt.Context(local, enable_timing=True) as ctx, solrt.Context(local, enable_counters=True) as cctx:
+    with solrt.Context(local, enable_timing=True, path_capacity=capacity) as ctx, \
+            solrt.Context(local, enable_counters=True) as cctx:
         for name, kind, sah in all_kinds:
             if kinds is not None and name not in kinds:
                 continue
@@ -441,7 +442,7 @@ def parity_cornell(local):
             "oracle_seconds": round(time.perf_counter() - t0, 2)}
 
 
-def parity_tunnel(local, n_rays=1 << 22):
+def parity_tunnel(local, n_rays=1 << 22, capacity=0):
     """The procedural tunnel at its stated size (4.19M triangles, 2560x1440,
     128 spp, depth 8, Kahan sums): RMSE against the FP64 oracle over two
     central rows after four frames (512 spp), and the hit records of 4M probe
@@ -455,7 +456,7 @@ def parity_tunnel(local, n_rays=1 << 22):
     out = {"workload": cfg["workload"]}
     out["rmse_vs_fp64"] = rmse_vs_fp64(local, data, kw, cam, solrt.BVH2, (H // 2 - 1, H // 2 + 1), frames=4)
     ps = precision_study(local, data, kw, cam, None, None, None, None, n_rays=n_rays,
-                         kinds=("bvh2_fp32", "bvh2_treelet", "bvh8_q8", "bvh8_q8_sah"))
+                         kinds=("bvh2_fp32", "bvh2_treelet", "bvh8_q8", "bvh8_q8_sah"), capacity=capacity)
     out.update(ps)
     return out
 
@@ -841,8 +842,9 @@ def main():
     ap.add_argument("--width", type=int, default=0, help="override the workload's image width (profiling runs)")
     ap.add_argument("--height", type=int, default=0, help="override the workload's image height")
     ap.add_argument("--spp", type=int, default=0, help="override the workload's samples per pixel")
-    ap.add_argument("--capacity", type=int, default=0,
-                    help="paths per pass of the timed context (0 = library default; small profiler captures)")
+    ap.add_argument("--capacity", type=int, default=128 << 20,
+                    help="paths per pass of the single-scene contexts (default 128M: a 64-spp 1080p frame in one "
+                         "pass, 19 GB of queues; 0 = the library default, 32M)")
     args = ap.parse_args()
     args.sah = not args.lbvh
     world, rank, local, pg = dist_setup(args)
@@ -901,6 +903,9 @@ def main():
         csc.close()
 
     ctx = solrt.Context(local, enable_timing=True, path_capacity=args.capacity)
+    ctx_capacity = ctx.capacity()
+    spp_per_pass = max(1, min(kw["spp"], ctx_capacity // (W * H)))
+    passes_per_step = -(-kw["spp"] // spp_per_pass)
     sc = solrt.SceneDescription(ctx, data, bvh=bvh, sah=args.sah)
     info = sc.bvh_info()
     img = solrt.Image(ctx, W, H, kw["accum_mode"])
@@ -1039,7 +1044,7 @@ def main():
     if rank == 0 and args.workload == "soup" and not args.no_precision:
         try:
             precision = precision_study(local, data, kw, cam, value / max(world, 1), info, nodes_per_seg, tris_per_seg,
-                                        main_sah=args.sah)
+                                        main_sah=args.sah, capacity=args.capacity)
         except Exception as ex:
             precision = {"error": str(ex)}
     # parity and convergence of the other single-scene configurations at
@@ -1050,7 +1055,7 @@ def main():
         configs = {}
         for name, fn in (("cornell", parity_cornell), ("tunnel", parity_tunnel)):
             try:
-                configs[name] = fn(local)
+                configs[name] = fn(local, capacity=args.capacity) if name == "tunnel" else fn(local)
             except Exception as ex:
                 configs[name] = {"error": str(ex)}
         try:
@@ -1094,6 +1099,7 @@ def main():
                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                "config": run_config(cfg, args, world),
                "bvh": {"kind": args.bvh, "build_ms": round(info.build_ms, 3), "node_count": int(info.node_count)},
+               "path_capacity": int(ctx_capacity), "passes_per_step": passes_per_step,
                "segments_per_step": int(st.segments // args.steps), "fp64_fallbacks_per_segment": fb_per_seg,
                "gpu_launches": int(st.launches), "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
                "clocks": clk, "rmse_vs_fp64": rmse, "precision_study": precision, "batched_vs_plain": batched,

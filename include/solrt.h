@@ -601,7 +601,8 @@ solrt_status solrt_server_get_stats(solrt_server* srv, solrt_server_stats* out);
 /* Stops the serving thread (unfinished jobs are dropped) and frees images. */
 solrt_status solrt_server_destroy(solrt_server* srv);
 
-/* Closest-hit queries (one traceRayEXT each, opaque, no culling).
+/* Closest-hit queries (one traceRayEXT each, opaque, no culling); n below
+ * 2^31 (SOLRT_ERR_INVALID otherwise).
  * Host arrays; synchronises. */
 solrt_status solrt_trace_rays(solrt_context* ctx, solrt_scene* scene, const solrt_ray* rays,
                               uint32_t n, solrt_hit* hits);

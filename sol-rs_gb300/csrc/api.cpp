@@ -946,6 +946,7 @@ solrt_status solrt_trace_rays(solrt_context* ctx, solrt_scene* scene, const solr
                               solrt_hit* hits) {
     CHECK_ARG(ctx && scene, "null argument");
     CHECK_ARG(n == 0 || (rays && hits), "null ray or hit array");
+    CHECK_ARG(n < (1u << 31), "more than 2^31 - 1 rays in one call");
     if (n == 0) return SOLRT_OK;
     DeviceBuffer dr, dh;
     SOLRT_TRY(dr.alloc(sizeof(solrt_ray) * (size_t)n));
@@ -961,6 +962,7 @@ solrt_status solrt_trace_rays_device(solrt_context* ctx, solrt_scene* scene, con
                                      solrt_hit* hits_dev) {
     CHECK_ARG(ctx && scene, "null argument");
     CHECK_ARG(n == 0 || (rays_dev && hits_dev), "null ray or hit array");
+    CHECK_ARG(n < (1u << 31), "more than 2^31 - 1 rays in one call");
     return launch_trace_rays(*ctx, *scene, rays_dev, n, hits_dev);
 }
 

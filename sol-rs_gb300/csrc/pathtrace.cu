@@ -79,6 +79,18 @@ __global__ void k_generate(const DevJob* __restrict__ jobs, const DevItem* __res
 #ifndef SOLRT_SHADE_MINB
 #define SOLRT_SHADE_MINB 4
 #endif
+// 1: in the plain variant the continuing paths of a block's 256 slots take
+// their queue positions with one atomic per block (two barriers per step);
+// 0, and the next-event-estimation variant: one atomic per warp. Atomics on
+// the one queue counter are serialised at its L2 slice (about 1.5 G warp
+// atomics per second on GB300 when nothing else runs) and a 64-spp soup
+// frame makes 10M of them: per block, the soup's shade stage takes 12.5
+// instead of 12.5-16.3 ms per frame (the higher figure on some boxes). The
+// NEE variant, bound by the latency of its light-tree walks, loses 9 % to
+// the barriers, so it keeps the warp atomics.
+#ifndef SOLRT_SHADE_BLOCK_COMPACT
+#define SOLRT_SHADE_BLOCK_COMPACT 1
+#endif
 template <bool kNee>
 __global__ void __launch_bounds__(256, SOLRT_SHADE_MINB)
     k_shade(const DevJob* __restrict__ jobs, const DevItem* __restrict__ items, uint32_t nitems, PathQueue qin,
@@ -88,11 +100,17 @@ __global__ void __launch_bounds__(256, SOLRT_SHADE_MINB)
     const unsigned int n = *count_in;
     const int lane = threadIdx.x & 31;
     const uint32_t lane_lt = (1u << lane) - 1u;
-    const uint32_t warp_global = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    constexpr bool kBlock = SOLRT_SHADE_BLOCK_COMPACT && !kNee;
+    // kBlock: a block-uniform loop, slots [base, base + 256) per block and
+    // step; else a warp-uniform one, 32 slots per warp and step
+    __shared__ uint32_t s_cnt[8], s_pre[8], s_base;
+    const uint32_t warp = threadIdx.x >> 5;
+    const uint32_t start = kBlock ? blockIdx.x * blockDim.x : ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32u;
+    const uint32_t stride = kBlock ? gridDim.x * blockDim.x : ((gridDim.x * blockDim.x) >> 5) * 32u;
+    const uint32_t off = kBlock ? threadIdx.x : (uint32_t)lane;
     uint32_t ef = 0;
-    for (uint32_t base = warp_global * 32u; base < n; base += warps * 32u) {
-        const uint32_t i = base + lane;
+    for (uint32_t base = start; base < n; base += stride) {
+        const uint32_t i = base + off;
         bool alive = false, shadow = false;
         float4 out_o = make_float4(0, 0, 0, 0), out_d = make_float4(0, 0, 0, 0), out_t = make_float4(0, 0, 0, 0);
         float4 s_o = make_float4(0, 0, 0, 0), s_d = make_float4(0, 0, 0, 0), s_c = make_float4(0, 0, 0, 0);
@@ -134,11 +152,29 @@ __global__ void __launch_bounds__(256, SOLRT_SHADE_MINB)
             }
         }
         const uint32_t mask = __ballot_sync(0xffffffffu, alive);
+        const uint32_t smask = kNee ? __ballot_sync(0xffffffffu, shadow) : 0u;
+        if constexpr (kBlock) {
+            if (lane == 0) s_cnt[warp] = (uint32_t)__popc(mask);
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                uint32_t t = 0;
+                for (uint32_t w = 0; w < (blockDim.x >> 5); ++w) {
+                    s_pre[w] = t;
+                    t += s_cnt[w];
+                }
+                s_base = t ? atomicAdd(count_out, t) : 0u;
+            }
+            __syncthreads();
+        }
         if (mask) {
-            const int leader = __ffs(mask) - 1;
             uint32_t pos0 = 0;
-            if (lane == leader) pos0 = atomicAdd(count_out, (unsigned int)__popc(mask));
-            pos0 = __shfl_sync(0xffffffffu, pos0, leader);
+            if constexpr (kBlock) {
+                pos0 = s_base + s_pre[warp];
+            } else {
+                const int leader = __ffs(mask) - 1;
+                if (lane == leader) pos0 = atomicAdd(count_out, (unsigned int)__popc(mask));
+                pos0 = __shfl_sync(0xffffffffu, pos0, leader);
+            }
             if (alive) {
                 const uint32_t pos = pos0 + __popc(mask & lane_lt);
                 if (pos < capacity) {
@@ -152,7 +188,6 @@ __global__ void __launch_bounds__(256, SOLRT_SHADE_MINB)
                 }
             }
         }
-        const uint32_t smask = kNee ? __ballot_sync(0xffffffffu, shadow) : 0u;
         if (smask) {
             const int leader = __ffs(smask) - 1;
             uint32_t pos0 = 0;

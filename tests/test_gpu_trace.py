@@ -95,6 +95,9 @@ def test_zero_rays_and_device_api(solrt, ctx):
     ctx.synchronize()
     dev = dh.cpu().numpy().view(solrt.HIT_DTYPE)
     assert hits_equal(host, dev)
+    with pytest.raises(solrt.SolrtError) as e:  # refused before any launch
+        sc.trace_rays_device(dr.data_ptr(), 1 << 31, dh.data_ptr())
+    assert e.value.status == 1
 
 
 def test_invalid_scene_rejected(solrt, ctx):
