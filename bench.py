@@ -619,6 +619,16 @@ def run_batch(args, world, rank, local, pg, njobs=None, steps=None, emit=True, w
     pbatch.launch()
     ms_p, seg_p, launches_p = timed(pbatch.launch, 1)
     pbatch.close()
+    # the wavefront passes as phases of one cooperative launch (grid-wide
+    # barriers between stages), in a CUDA graph; every launch renders the
+    # same frame, so its images must equal the batched ones bit for bit
+    check = [img.read()[0].copy() for _, img, _, _ in jobs[:8]]
+    cbatch = solrt.Batch(ctx, jobs, graph=True, cooperative=True)
+    cbatch.launch()
+    ms_c, seg_c, launches_c = timed(cbatch.launch, 1)
+    coop_equal = all(np.array_equal(x.view(np.uint32), img.read()[0].view(np.uint32))
+                     for x, (_, img, _, _) in zip(check, jobs))
+    cbatch.close()
     clk = clocks.stop() if clocks else None
     ms_b_max = max_over_ranks(pg, ms_b)
     value = sum_over_ranks(pg, float(seg_b)) / (ms_b_max / 1000.0) / 1e6
@@ -629,10 +639,13 @@ def run_batch(args, world, rank, local, pg, njobs=None, steps=None, emit=True, w
            "wavefront_scene_by_scene": round(wave_v, 3),
            "ratio_vs_wavefront": round(value / wave_v, 3) if wave_v > 0 else None,
            "persistent_one_launch": round(seg_p / (ms_p / 1000.0) / 1e6, 3),
+           "cooperative_one_launch": round(seg_c / (ms_c / 1000.0) / 1e6, 3),
+           "cooperative_images_equal_batched": bool(coop_equal),
            "batch_ms": round(ms_b_max / steps, 3), "passes": info["passes"], "items": info["items"],
            "pass_fill": round(info["paths"] / max(1, info["passes"] * ctx.capacity()), 3),
            "launches_per_step": {"batched": int(launches_b // steps), "wavefront_scene_by_scene": int(launches_w),
-                                 "megakernel_scene_by_scene": int(launches_m), "persistent_one_launch": int(launches_p)},
+                                 "megakernel_scene_by_scene": int(launches_m), "persistent_one_launch": int(launches_p),
+                                 "cooperative_one_launch": int(launches_c)},
            "tris": int(tris), "pixels": int(pixels), "samples": int(samples), "setup_s": round(setup_s, 1),
            "autotune": {k: (round(v, 3) if isinstance(v, float) else v) for k, v in tune.items()}}
     if rank == 0 and emit:

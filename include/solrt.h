@@ -458,7 +458,16 @@ enum {
      * each thread traces all samples of its pixel to the end (the per-pixel
      * structure of the reference's raygen loop); same images. Path
      * integrator only (no next-event estimation). */
-    SOLRT_BATCH_PERSISTENT = 2u
+    SOLRT_BATCH_PERSISTENT = 2u,
+    /* the wavefront passes of a step (generate, extend and shade per bounce,
+     * accumulate, finalize) as phases of one cooperative launch: a grid of
+     * (SMs x resident blocks) that meets at grid-wide barriers between
+     * stages instead of one launch per stage; same images. Each barrier wait
+     * is bounded: a launch whose blocks do not all arrive ends with
+     * SOLRT_ERR_TIMEOUT. Path integrator only (no next-event estimation);
+     * node / triangle counters are not gathered. Not with
+     * SOLRT_BATCH_PERSISTENT. */
+    SOLRT_BATCH_COOPERATIVE = 4u
 };
 
 /* Plans a batch: the paths of all jobs share the wavefront queues, each pass
@@ -613,7 +622,12 @@ solrt_status solrt_trace_rays_device(solrt_context* ctx, solrt_scene* scene,
 /* Device-side unit functions for known-answer tests (host in, host out).
  * op: 0 = tea(a[i], b[i]) -> out_u32; 1 = nextRand sequence of length b[0]
  * from seed a[0] -> out_f32 + final state in out_u32[0]; 2 = sincos of
- * in_f32[i] -> out_f32[2i], out_f32[2i+1]. Synchronises. */
+ * in_f32[i] -> out_f32[2i], out_f32[2i+1]; 3-7 = the sampling functions,
+ * miss colour and gamma (see the tests); 8 = the bounded wait of the
+ * cooperative batch's grid barrier: a cooperative grid in which one block
+ * never arrives, each wait limited to in_f32[0] seconds (at most 10), its
+ * error flags -> out_u32[0] (SOLRT_EFLAG_TIMEOUT when the waits gave up).
+ * Synchronises. */
 solrt_status solrt_debug_unit(solrt_context* ctx, uint32_t op, uint32_t n, const uint32_t* a,
                               const uint32_t* b, const float* in_f32, uint32_t* out_u32,
                               float* out_f32);

@@ -100,6 +100,7 @@ class Job(ctypes.Structure):
 
 BATCH_GRAPH = 1
 BATCH_PERSISTENT = 2
+BATCH_COOPERATIVE = 4
 SERVE_FAIR, SERVE_SHORTEST_FIRST = 0, 1
 
 
@@ -531,14 +532,17 @@ class Batch:
     """Many render jobs over many scenes in shared wavefront passes
     (solrt_batch); each job's image equals rendering it alone."""
 
-    def __init__(self, context, jobs, graph=False, persistent=False):
+    def __init__(self, context, jobs, graph=False, persistent=False, cooperative=False):
         """graph: replay one captured CUDA graph per launch; persistent: one
-        persistent per-pixel launch over all jobs instead of wavefront passes."""
+        persistent per-pixel launch over all jobs instead of wavefront passes;
+        cooperative: the wavefront passes as phases of one cooperative
+        launch (grid-wide barriers between stages)."""
         self.context = context
         self._keep = list(jobs)
         arr = make_jobs(jobs)
         h = ctypes.c_void_p()
-        flags = (BATCH_GRAPH if graph else 0) | (BATCH_PERSISTENT if persistent else 0)
+        flags = ((BATCH_GRAPH if graph else 0) | (BATCH_PERSISTENT if persistent else 0)
+                 | (BATCH_COOPERATIVE if cooperative else 0))
         check(lib().solrt_batch_create(context.handle, arr, len(jobs), flags, ctypes.byref(h)))
         self.handle = h
 

@@ -27,7 +27,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-prec-div=true", "-prec-sqrt=true",
               "-ftz=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
               "-Xcompiler", "-fno-fast-math", "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
-SOURCES = ["api.cpp", "bvh_build.cu", "bvh8_build.cu", "trace.cu", "pathtrace.cu", "server.cpp", "gltf.cpp"]
+SOURCES = ["api.cpp", "bvh_build.cu", "bvh8_build.cu", "trace.cu", "pathtrace.cu", "coop.cu", "server.cpp",
+           "gltf.cpp"]
 
 
 def nvcc():

@@ -871,7 +871,11 @@ solrt_status solrt_batch_create(solrt_context* ctx, const solrt_job* jobs, uint3
                                 solrt_batch** out) {
     CHECK_ARG(ctx && jobs && out, "null argument");
     *out = nullptr;
-    CHECK_ARG((flags & ~(uint32_t)(SOLRT_BATCH_GRAPH | SOLRT_BATCH_PERSISTENT)) == 0u, "unknown batch flags");
+    CHECK_ARG((flags & ~(uint32_t)(SOLRT_BATCH_GRAPH | SOLRT_BATCH_PERSISTENT | SOLRT_BATCH_COOPERATIVE)) == 0u,
+              "unknown batch flags");
+    CHECK_ARG((flags & (SOLRT_BATCH_PERSISTENT | SOLRT_BATCH_COOPERATIVE)) !=
+                  (uint32_t)(SOLRT_BATCH_PERSISTENT | SOLRT_BATCH_COOPERATIVE),
+              "SOLRT_BATCH_PERSISTENT and SOLRT_BATCH_COOPERATIVE exclude each other");
     solrt_batch* b = new (std::nothrow) solrt_batch();
     if (!b) return SOLRT_ERR_OOM;
     const solrt_status s = batch_plan(*ctx, jobs, n, flags, *b);

@@ -154,6 +154,10 @@ struct Batch {
     uint64_t total_paths = 0;
     uint64_t graph_launches = 0;
     DeviceBuffer d_jobs, d_items, d_job_pix;
+    // SOLRT_BATCH_COOPERATIVE: the pass table on the device and the launch's
+    // barrier word + per-pass queue counts (coop_buffer_bytes)
+    DeviceBuffer d_passes, d_coop;
+    uint32_t coop_stride = 0;  // counters per pass and kind (count / work): max bounces + 2
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     std::vector<solrt_job> src;  // the jobs as given (re-planned by the autotuner)
@@ -336,6 +340,19 @@ solrt_status launch_extend(Context& ctx, uint32_t kind, const DevJob* jobs, cons
                            bool any_hit = false);
 // Whether an extend kernel exists for this block size / shared stack slots.
 bool extend_variant_ok(uint32_t block, uint32_t smem);
+
+// coop.cu: SOLRT_BATCH_COOPERATIVE. Bytes of the barrier word and counters
+// of a batch of `npasses` passes with `stride` counters per pass and kind.
+size_t coop_buffer_bytes(uint32_t npasses, uint32_t stride);
+// Zeroes `coop` (coop_buffer_bytes) and runs every pass of the batch in one
+// cooperative launch on the context stream.
+solrt_status launch_batch_coop(Context& ctx, uint32_t kind, const DevJob* jobs, const DevItem* items,
+                               const PassPlan* passes, uint32_t npasses, uint32_t ctr_stride, const uint32_t* job_pix,
+                               uint32_t njobs, uint32_t total_pix, void* coop);
+// A cooperative grid whose block 0 never reaches the barrier the others wait
+// at, each wait bounded by `seconds`; returns the error flags it raised
+// (SOLRT_EFLAG_TIMEOUT expected). Synchronises.
+solrt_status coop_wait_test(Context& ctx, double seconds, uint32_t* eflags);
 
 // pathtrace.cu
 solrt_status batch_plan(Context& ctx, const solrt_job* jobs, uint32_t n, uint32_t flags, Batch& b);

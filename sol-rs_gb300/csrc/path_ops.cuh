@@ -295,4 +295,123 @@ SOLRT_D void add_sample_kahan(f3& ks, f3& kc, float& kn, float4 c) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Stage bodies shared by the one-stage-per-launch kernels (pathtrace.cu) and
+// the cooperative one-launch batch (coop.cu). `Ld` loads what an earlier
+// stage wrote: plain loads when stages are separate launches, loads through
+// L2 (ld.global.cg) when they are phases of one launch, where this SM's L1
+// may still hold lines from before another SM's writes.
+// ---------------------------------------------------------------------------
+struct LdPlain {
+    template <class T> SOLRT_D static T ld(const T* p) { return *p; }
+};
+struct LdL2 {
+    template <class T> SOLRT_D static T ld(const T* p) { return __ldcg(p); }
+};
+
+// Largest index i in [0, n) with key(i) <= v (key increasing, key(0) = 0).
+template <class F>
+SOLRT_D uint32_t find_last_le(uint32_t n, uint32_t v, F key) {
+    uint32_t lo = 0, hi = n;  // invariant: key(lo) <= v, answer in [lo, hi)
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (key(mid) <= v) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Zeroes the frame sample sum of pixel t of the batch's pixel space (running
+// mix jobs).
+SOLRT_D void begin_pixel(const DevJob* jobs, const uint32_t* job_pix, uint32_t njobs, uint32_t t) {
+    const uint32_t j = find_last_le(njobs, t, [&](uint32_t i) { return job_pix[i]; });
+    const DevJob& J = jobs[j];
+    if (J.accum_mode != SOLRT_ACCUM_KAHAN) J.fsum[t - job_pix[j]] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+}
+
+// Camera ray of path slot i of a pass (rgen:47-61) into queue q.
+template <class Ld>
+SOLRT_D void generate_path(const DevJob* jobs, const DevItem* items, uint32_t nitems, uint32_t i, const PathQueue& q,
+                           float4* rad) {
+    const DevItem it = items[find_last_le(nitems, i, [&](uint32_t t) { return items[t].path_base; })];
+    const DevJob& J = jobs[it.job];
+    const uint32_t local = i - it.path_base;
+    const uint32_t lp = local / it.k, j = local - lp * it.k;
+    const uint32_t pix = it.pix0 + lp, s = it.s0 + j;
+    uint32_t rng = sample_seed(J, pix, s, J.rng_mode == SOLRT_RNG_REF_STREAM && s > 0 ? Ld::ld(J.rng_state + pix) : 0u);
+    float4 o, d;
+    camera_ray(J, pix, rng, o, d);
+    q.o_tmin[i] = o;
+    q.d_tmax[i] = d;
+    q.thr_rng[i] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(rng));
+    q.meta[i] = make_uint2(i, it.job << kDepthBits);
+    if (J.integrator == SOLRT_INTEGRATOR_PATH_NEE) rad[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // sums shadow terms
+}
+
+// Adds the pass's samples of pass pixel t to its pixel's sums, in sample
+// order (rgen:86).
+template <class Ld>
+SOLRT_D void accumulate_pixel(const DevJob* jobs, const DevItem* items, uint32_t nitems, uint32_t t,
+                              const float4* rad) {
+    const DevItem it = items[find_last_le(nitems, t, [&](uint32_t i) { return items[i].pix_base; })];
+    const DevJob& J = jobs[it.job];
+    const uint32_t lp = t - it.pix_base;
+    const uint32_t pix = it.pix0 + lp;
+    const float4* r = rad + it.path_base + (size_t)lp * it.k;
+    if (J.accum_mode == SOLRT_ACCUM_KAHAN) {
+        const float4 s4 = Ld::ld(J.ksum + pix), c4 = Ld::ld(J.kcomp + pix);
+        f3 ks{s4.x, s4.y, s4.z}, kc{c4.x, c4.y, c4.z};
+        float kn = s4.w;
+        for (uint32_t j = 0; j < it.k; ++j) add_sample_kahan(ks, kc, kn, Ld::ld(r + j));
+        J.ksum[pix] = make_float4(ks.x, ks.y, ks.z, kn);
+        J.kcomp[pix] = make_float4(kc.x, kc.y, kc.z, 0.0f);
+    } else {
+        const float4 s4 = Ld::ld(J.fsum + pix);
+        f3 s{s4.x, s4.y, s4.z};
+        for (uint32_t j = 0; j < it.k; ++j) add_sample(s, Ld::ld(r + j));
+        J.fsum[pix] = make_float4(s.x, s.y, s.z, 0.0f);
+    }
+    if (J.sq) {  // squared sample sums of the stopping rule (samples the sums above keep)
+        float q = Ld::ld(J.sq + pix);
+        for (uint32_t j = 0; j < it.k; ++j) {
+            const float4 c = Ld::ld(r + j);
+            if (J.accum_mode != SOLRT_ACCUM_KAHAN || (isfinite(c.x) && isfinite(c.y) && isfinite(c.z)))
+                q = q + (c.x * c.x + c.y * c.y + c.z * c.z);
+        }
+        J.sq[pix] = q;
+    }
+}
+
+SOLRT_D unsigned char to_unorm8(float c) {
+    const float cl = glsl_min(glsl_max(c, 0.0f), 1.0f);
+    return (unsigned char)(cl * 255.0f + 0.5f);
+}
+
+// rgen:88-103 (REF_MIX) or the Kahan mean, for pixel t of the batch's pixel
+// space.
+template <class Ld>
+SOLRT_D void finalize_pixel(const DevJob* jobs, const uint32_t* job_pix, uint32_t njobs, uint32_t t) {
+    const uint32_t j = find_last_le(njobs, t, [&](uint32_t i) { return job_pix[i]; });
+    const DevJob& J = jobs[j];
+    const uint32_t pix = t - job_pix[j];
+    const float4 a = J.accum[pix];
+    const f3 old{a.x, a.y, a.z};
+    f3 out;
+    if (J.accum_mode == SOLRT_ACCUM_KAHAN) {
+        const float4 s = Ld::ld(J.ksum + pix);
+        out = s.w > 0.0f ? f3{s.x / s.w, s.y / s.w, s.z / s.w} : old;
+    } else {
+        const float4 s = Ld::ld(J.fsum + pix);
+        const float inv = 1.0f / __uint2float_rn(J.spp);
+        const f3 mean = inv * f3{s.x, s.y, s.z};
+        const float alpha = 1.0f / __uint2float_rn(J.frame + 1u - J.start);
+        out = mix(old, mean, alpha);
+        if (isnan(out.x) || isnan(out.y) || isnan(out.z)) out = old;
+        if (isinf(out.x) || isinf(out.y) || isinf(out.z)) out = old;
+    }
+    J.accum[pix] = make_float4(out.x, out.y, out.z, 1.0f);
+    const float g = 1.0f / 2.2f;
+    J.rgba8[pix] = make_uchar4(to_unorm8(powf(out.x, g)), to_unorm8(powf(out.y, g)), to_unorm8(powf(out.z, g)), 255);
+}
+
 }  // namespace solrt

@@ -34,18 +34,6 @@ namespace solrt {
 
 namespace {
 
-// Largest index i in [0, n) with key(i) <= v (key increasing, key(0) = 0).
-template <class F>
-SOLRT_D uint32_t find_last_le(uint32_t n, uint32_t v, F key) {
-    uint32_t lo = 0, hi = n;  // invariant: key(lo) <= v, answer in [lo, hi)
-    while (hi - lo > 1) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (key(mid) <= v) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
-
 __global__ void k_generate(const DevJob* __restrict__ jobs, const DevItem* __restrict__ items, uint32_t nitems,
                            uint32_t P, PathQueue q, unsigned int* __restrict__ count0, DevStats* stats,
                            float4* __restrict__ rad) {
@@ -55,19 +43,7 @@ __global__ void k_generate(const DevJob* __restrict__ jobs, const DevItem* __res
         atomicAdd(&stats->paths, (unsigned long long)P);
     }
     if (i >= P) return;
-    const DevItem it = items[find_last_le(nitems, i, [&](uint32_t t) { return items[t].path_base; })];
-    const DevJob& J = jobs[it.job];
-    const uint32_t local = i - it.path_base;
-    const uint32_t lp = local / it.k, j = local - lp * it.k;
-    const uint32_t pix = it.pix0 + lp, s = it.s0 + j;
-    uint32_t rng = sample_seed(J, pix, s, J.rng_mode == SOLRT_RNG_REF_STREAM && s > 0 ? J.rng_state[pix] : 0u);
-    float4 o, d;
-    camera_ray(J, pix, rng, o, d);
-    q.o_tmin[i] = o;
-    q.d_tmax[i] = d;
-    q.thr_rng[i] = make_float4(1.0f, 1.0f, 1.0f, __uint_as_float(rng));
-    q.meta[i] = make_uint2(i, it.job << kDepthBits);
-    if (J.integrator == SOLRT_INTEGRATOR_PATH_NEE) rad[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // sums shadow terms
+    generate_path<LdPlain>(jobs, items, nitems, i, q, rad);
 }
 
 // kNee: the variant for passes with SOLRT_INTEGRATOR_PATH_NEE jobs (shadow
@@ -234,33 +210,7 @@ __global__ void k_accumulate(const DevJob* __restrict__ jobs, const DevItem* __r
                              uint32_t pixels, const float4* __restrict__ rad) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= pixels) return;
-    const DevItem it = items[find_last_le(nitems, t, [&](uint32_t i) { return items[i].pix_base; })];
-    const DevJob& J = jobs[it.job];
-    const uint32_t lp = t - it.pix_base;
-    const uint32_t pix = it.pix0 + lp;
-    const float4* r = rad + it.path_base + (size_t)lp * it.k;
-    if (J.accum_mode == SOLRT_ACCUM_KAHAN) {
-        const float4 s4 = J.ksum[pix], c4 = J.kcomp[pix];
-        f3 ks{s4.x, s4.y, s4.z}, kc{c4.x, c4.y, c4.z};
-        float kn = s4.w;
-        for (uint32_t j = 0; j < it.k; ++j) add_sample_kahan(ks, kc, kn, r[j]);
-        J.ksum[pix] = make_float4(ks.x, ks.y, ks.z, kn);
-        J.kcomp[pix] = make_float4(kc.x, kc.y, kc.z, 0.0f);
-    } else {
-        const float4 s4 = J.fsum[pix];
-        f3 s{s4.x, s4.y, s4.z};
-        for (uint32_t j = 0; j < it.k; ++j) add_sample(s, r[j]);
-        J.fsum[pix] = make_float4(s.x, s.y, s.z, 0.0f);
-    }
-    if (J.sq) {  // squared sample sums of the stopping rule (samples the sums above keep)
-        float q = J.sq[pix];
-        for (uint32_t j = 0; j < it.k; ++j) {
-            const float4 c = r[j];
-            if (J.accum_mode != SOLRT_ACCUM_KAHAN || (isfinite(c.x) && isfinite(c.y) && isfinite(c.z)))
-                q = q + (c.x * c.x + c.y * c.y + c.z * c.z);
-        }
-        J.sq[pix] = q;
-    }
+    accumulate_pixel<LdPlain>(jobs, items, nitems, t, rad);
 }
 
 // Per job, the sum over its pixels of the variance of the pixel mean summed
@@ -468,14 +418,7 @@ __global__ void k_begin(const DevJob* __restrict__ jobs, const uint32_t* __restr
                         uint32_t pixels) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= pixels) return;
-    const uint32_t j = find_last_le(njobs, t, [&](uint32_t i) { return job_pix[i]; });
-    const DevJob& J = jobs[j];
-    if (J.accum_mode != SOLRT_ACCUM_KAHAN) J.fsum[t - job_pix[j]] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-}
-
-__device__ __forceinline__ unsigned char to_unorm8(float c) {
-    const float cl = glsl_min(glsl_max(c, 0.0f), 1.0f);
-    return (unsigned char)(cl * 255.0f + 0.5f);
+    begin_pixel(jobs, job_pix, njobs, t);
 }
 
 // ---------------------------------------------------------------------------
@@ -621,27 +564,7 @@ __global__ void k_finalize(const DevJob* __restrict__ jobs, const uint32_t* __re
                            uint32_t pixels) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= pixels) return;
-    const uint32_t j = find_last_le(njobs, t, [&](uint32_t i) { return job_pix[i]; });
-    const DevJob& J = jobs[j];
-    const uint32_t pix = t - job_pix[j];
-    const float4 a = J.accum[pix];
-    const f3 old{a.x, a.y, a.z};
-    f3 out;
-    if (J.accum_mode == SOLRT_ACCUM_KAHAN) {
-        const float4 s = J.ksum[pix];
-        out = s.w > 0.0f ? f3{s.x / s.w, s.y / s.w, s.z / s.w} : old;
-    } else {
-        const float4 s = J.fsum[pix];
-        const float inv = 1.0f / __uint2float_rn(J.spp);
-        const f3 mean = inv * f3{s.x, s.y, s.z};
-        const float alpha = 1.0f / __uint2float_rn(J.frame + 1u - J.start);
-        out = mix(old, mean, alpha);
-        if (isnan(out.x) || isnan(out.y) || isnan(out.z)) out = old;
-        if (isinf(out.x) || isinf(out.y) || isinf(out.z)) out = old;
-    }
-    J.accum[pix] = make_float4(out.x, out.y, out.z, 1.0f);
-    const float g = 1.0f / 2.2f;
-    J.rgba8[pix] = make_uchar4(to_unorm8(powf(out.x, g)), to_unorm8(powf(out.y, g)), to_unorm8(powf(out.z, g)), 255);
+    finalize_pixel<LdPlain>(jobs, job_pix, njobs, t);
 }
 
 // Known-answer kernels for the unit functions.
@@ -834,6 +757,14 @@ solrt_status batch_issue(Batch& b, bool record_timing) {
         SOLRT_CUDA(cudaGetLastError());
         return SOLRT_OK;
     }
+    if (b.flags & SOLRT_BATCH_COOPERATIVE) {
+        const int tm = record_timing ? ctx.timing_begin(0) : -1;  // every stage in one launch
+        SOLRT_TRY(launch_batch_coop(ctx, b.kind, dj, di, b.d_passes.as<PassPlan>(), (uint32_t)b.passes.size(),
+                                    b.coop_stride, jp, njobs, total_pix, b.d_coop.ptr));
+        ctx.timing_end(tm);
+        SOLRT_CUDA(cudaGetLastError());
+        return SOLRT_OK;
+    }
     const int tb = record_timing ? ctx.timing_begin(3) : -1;
     k_begin<<<cdiv(total_pix, 256), 256, 0, st>>>(dj, jp, njobs, total_pix);
     ctx.timing_end(tb);
@@ -875,6 +806,10 @@ solrt_status batch_plan(Context& ctx, const solrt_job* jobs, uint32_t n, uint32_
         }
         if (jb.params.integrator == SOLRT_INTEGRATOR_PATH_NEE && (flags & SOLRT_BATCH_PERSISTENT)) {
             set_error("job %u: persistent batches run the path integrator without next-event estimation", j);
+            return SOLRT_ERR_INVALID;
+        }
+        if (jb.params.integrator == SOLRT_INTEGRATOR_PATH_NEE && (flags & SOLRT_BATCH_COOPERATIVE)) {
+            set_error("job %u: cooperative batches run the path integrator without next-event estimation", j);
             return SOLRT_ERR_INVALID;
         }
         if (jb.params.integrator == SOLRT_INTEGRATOR_PATH_NEE) SOLRT_TRY(ensure_shadow_queue(ctx));
@@ -958,6 +893,17 @@ solrt_status batch_plan(Context& ctx, const solrt_job* jobs, uint32_t n, uint32_
     SOLRT_CUDA(cudaMemcpyAsync(b.d_items.ptr, b.items.data(), sizeof(DevItem) * b.items.size(), cudaMemcpyHostToDevice, st));
     SOLRT_CUDA(cudaMemcpyAsync(b.d_job_pix.ptr, b.job_pix_base.data(), sizeof(uint32_t) * b.job_pix_base.size(),
                                cudaMemcpyHostToDevice, st));
+    if (flags & SOLRT_BATCH_COOPERATIVE) {
+        int coop = 0;
+        SOLRT_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx.device));
+        if (!coop) { set_error("the device has no cooperative launches"); return SOLRT_ERR_DEVICE; }
+        b.coop_stride = 2;
+        for (const PassPlan& pp : b.passes) b.coop_stride = std::max(b.coop_stride, pp.bounces + 2u);
+        SOLRT_TRY(b.d_passes.alloc(sizeof(PassPlan) * b.passes.size()));
+        SOLRT_TRY(b.d_coop.alloc(coop_buffer_bytes((uint32_t)b.passes.size(), b.coop_stride)));
+        SOLRT_CUDA(cudaMemcpyAsync(b.d_passes.ptr, b.passes.data(), sizeof(PassPlan) * b.passes.size(),
+                                   cudaMemcpyHostToDevice, st));
+    }
     return SOLRT_OK;
 }
 
@@ -1261,6 +1207,13 @@ solrt_status render_frame(Context& ctx, const Scene& sc, const solrt_camera& cam
 
 solrt_status debug_unit(Context& ctx, uint32_t op, uint32_t n, const uint32_t* a, const uint32_t* b,
                         const float* in_f32, uint32_t* out_u32, float* out_f32) {
+    if (op == 8) {  // bounded grid-barrier wait: in_f32[0] = seconds, out_u32[0] = error flags raised
+        if (!in_f32 || !out_u32 || !(in_f32[0] > 0.0f && in_f32[0] <= 10.0f)) {
+            set_error("debug op 8 needs a wait of (0, 10] seconds and an output word");
+            return SOLRT_ERR_INVALID;
+        }
+        return coop_wait_test(ctx, in_f32[0], out_u32);
+    }
     if (op > 7) {
         set_error("unknown debug op %u", op);
         return SOLRT_ERR_INVALID;

@@ -221,3 +221,91 @@ def test_persistent_batch_equals_alone(solrt, ctx, bvh):
            if kw.get("integrator", solrt.INTEGRATOR_PATH) == solrt.INTEGRATOR_PATH_NEE]
     with pytest.raises(solrt.SolrtError):
         solrt.Batch(ctx, nee, persistent=True)
+
+
+def _plain_jobs(solrt, ctx, kind):
+    return [j for j, (_, _, _, kw) in zip(_make(solrt, ctx, kind), _specs(solrt))
+            if kw.get("integrator", solrt.INTEGRATOR_PATH) == solrt.INTEGRATOR_PATH]
+
+
+@pytest.mark.parametrize("graph", [False, True])
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh2t", "bvh4", "bvh8", "bvh8f"])
+def test_cooperative_batch_equals_alone(solrt, ctx, bvh, graph):
+    """SOLRT_BATCH_COOPERATIVE: every wavefront pass of the batch as phases
+    of one cooperative launch (grid-wide barriers between generate, extend,
+    shade and accumulate) renders each job bit for bit as solrt_render of
+    that job alone, over two frames, with and without a CUDA graph; one
+    kernel launch per step."""
+    kind = bvh_kind(solrt, bvh)
+    jobs = _plain_jobs(solrt, ctx, kind)
+    batch = solrt.Batch(ctx, jobs, graph=graph, cooperative=True)
+    ctx.reset_stats()
+    batch.launch()
+    ctx.synchronize()
+    st = ctx.stats()
+    assert st.error_flags == 0 and st.launches == 1
+    upd = []
+    for sc, img, cam, p in jobs:
+        q = solrt.RenderParams.from_buffer_copy(p)
+        q.frame = 1
+        upd.append((sc, img, cam, q))
+    batch.update(upd)
+    batch.launch()
+    ctx.synchronize()
+    assert ctx.stats().error_flags == 0
+    got = [img.read() for _, img, _, _ in jobs]
+    want = _alone(solrt, ctx, jobs, frames=2)
+    for (a32, a8), (b32, b8) in zip(got, want):
+        assert np.array_equal(a32.view(np.uint32), b32.view(np.uint32))
+        assert np.array_equal(a8, b8)
+    batch.close()
+
+
+def test_cooperative_many_passes_and_counts(solrt):
+    """A capacity of 2000 paths makes dozens of mixed passes inside the one
+    launch; images and segment / path counts equal the per-stage launches'."""
+    res = []
+    for coop in (False, True):
+        c = solrt.Context(0, path_capacity=2000)
+        jobs = _plain_jobs(solrt, c, solrt.BVH2)
+        b = solrt.Batch(c, jobs, cooperative=coop)
+        c.reset_stats()
+        b.launch()
+        c.synchronize()
+        st = c.stats()
+        assert st.error_flags == 0
+        res.append(([img.read()[0].copy() for _, img, _, _ in jobs], b.info(), st.segments, st.paths))
+        b.close()
+        c.close()
+    assert res[0][1]["passes"] > 10 and res[0][1] == res[1][1]
+    assert res[0][2:] == res[1][2:]
+    for x, y in zip(res[0][0], res[1][0]):
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
+
+
+def test_cooperative_batch_refusals(solrt, ctx):
+    nee = [j for j, (_, _, _, kw) in zip(_make(solrt, ctx, solrt.BVH2), _specs(solrt))
+           if kw.get("integrator", solrt.INTEGRATOR_PATH) == solrt.INTEGRATOR_PATH_NEE]
+    with pytest.raises(solrt.SolrtError):
+        solrt.Batch(ctx, nee, cooperative=True)
+    plain = _plain_jobs(solrt, ctx, solrt.BVH2)
+    with pytest.raises(solrt.SolrtError):
+        solrt.Batch(ctx, plain, persistent=True, cooperative=True)
+
+
+def test_grid_barrier_wait_is_bounded(solrt, ctx):
+    """The cooperative launch's barrier wait gives up after its budget: a
+    grid whose block 0 never arrives ends with SOLRT_EFLAG_TIMEOUT raised by
+    the waiting blocks (no hang, no fault), and the context keeps working."""
+    import time
+    flags = np.zeros(1, np.uint32)
+    t0 = time.time()
+    ctx.debug_unit(8, 0, fin=np.array([0.05], np.float32), out_u=flags)
+    assert flags[0] & solrt.api.EFLAG_TIMEOUT
+    assert time.time() - t0 < 30.0
+    jobs = _plain_jobs(solrt, ctx, solrt.BVH2)[:1]
+    b = solrt.Batch(ctx, jobs, cooperative=True)
+    b.launch()
+    ctx.synchronize()
+    assert ctx.stats().error_flags == 0
+    b.close()
