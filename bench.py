@@ -703,7 +703,9 @@ def run_serve(local, rate, duration, n_scenes=16, seed=5, policy=0, stop_rmse=0.
 
     def drain():
         nonlocal early
-        for tk in list(pending):
+        for tk in srv.finished():   # the completion queue: only jobs that finished since the last look
+            if tk not in pending:
+                continue
             st_, r = srv.poll(tk)
             if st_ == 0:
                 lat.append(r.latency_ns / 1e6)

@@ -520,6 +520,31 @@ solrt_status solrt_context_set_tune(solrt_context* ctx, const solrt_tune_config*
  * them before rendering for real). */
 solrt_status solrt_batch_autotune(solrt_batch* batch, solrt_tune_result* out);
 
+/* ---- autotune cache ---------------------------------------------------------
+ * The winner of solrt_batch_autotune kept in a small text file (one JSON
+ * object per line: key, block_size, smem_stack, pass_paths, best_ms) so that
+ * a later process with a batch of the same shape skips the timing. The key
+ * names the GPU (name and SM count), the BVH kind, the context's path
+ * capacity, the batch flags and the jobs' shapes (sizes, spp, bounces,
+ * modes, triangle counts; a 64-bit hash of them), not the cameras. */
+#define SOLRT_TUNE_KEY_MAX 256u
+/* The batch's cache key, NUL-terminated, into key[0..key_bytes). */
+solrt_status solrt_batch_tune_key(solrt_batch* batch, char* key, size_t key_bytes);
+/* Host only. SOLRT_OK with the entry of `key`; SOLRT_ERR_NOT_FOUND when the
+ * file or the key is missing (lines that do not parse, or hold a launch
+ * shape no kernel exists for, are skipped). */
+solrt_status solrt_tune_cache_lookup(const char* path, const char* key, solrt_tune_config* cfg, float* best_ms);
+/* Host only. Adds or replaces the entry of `key` (the file is rewritten
+ * through a temporary file and a rename, so readers never see half a
+ * file). Keys hold no quote, backslash or control character. */
+solrt_status solrt_tune_cache_store(const char* path, const char* key, const solrt_tune_config* cfg, float best_ms);
+/* solrt_batch_autotune through the cache at `path`: when it holds the
+ * batch's key, applies that configuration to the context and re-plans the
+ * batch (no timing; out->candidates = 0, *hit = 1); otherwise autotunes and
+ * stores the winner (*hit = 0). */
+solrt_status solrt_batch_autotune_cached(solrt_batch* batch, const char* path, solrt_tune_result* out,
+                                         uint32_t* hit);
+
 /* ------------------------------------------------------------------------ */
 /* Serving: continuous batching of render jobs                              */
 /* ------------------------------------------------------------------------ */
@@ -606,6 +631,11 @@ solrt_status solrt_server_release(solrt_server* srv, uint64_t ticket);
  * SOLRT_ERR_CANCELLED until it is released. SOLRT_ERR_INVALID for a job that
  * has already finished. */
 solrt_status solrt_server_cancel(solrt_server* srv, uint64_t ticket);
+/* The completion queue: tickets of jobs that reached their final state
+ * (done, failed, cancelled) since the last call, oldest first, at most
+ * `max` of them (the rest stay for the next call); *n = how many. A client
+ * with thousands of jobs in flight fetches these and polls only them. */
+solrt_status solrt_server_finished(solrt_server* srv, uint64_t* tickets, uint32_t max, uint32_t* n);
 solrt_status solrt_server_get_stats(solrt_server* srv, solrt_server_stats* out);
 /* Stops the serving thread (unfinished jobs are dropped) and frees images. */
 solrt_status solrt_server_destroy(solrt_server* srv);

@@ -193,6 +193,13 @@ _PROTOS = {
     "solrt_context_get_tune": (ctypes.c_int, [_P, ctypes.POINTER(TuneConfig)]),
     "solrt_context_set_tune": (ctypes.c_int, [_P, ctypes.POINTER(TuneConfig)]),
     "solrt_batch_autotune": (ctypes.c_int, [_P, ctypes.POINTER(TuneResult)]),
+    "solrt_batch_tune_key": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_size_t]),
+    "solrt_tune_cache_lookup": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(TuneConfig),
+                                               ctypes.POINTER(ctypes.c_float)]),
+    "solrt_tune_cache_store": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(TuneConfig),
+                                              ctypes.c_float]),
+    "solrt_batch_autotune_cached": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.POINTER(TuneResult),
+                                                   ctypes.POINTER(ctypes.c_uint32)]),
     "solrt_server_create": (ctypes.c_int, [_P, ctypes.POINTER(ServerDesc), ctypes.POINTER(_P)]),
     "solrt_server_submit": (ctypes.c_int, [_P, _P, ctypes.POINTER(Camera), ctypes.POINTER(RenderParams),
                                            ctypes.POINTER(ctypes.c_uint64)]),
@@ -201,6 +208,8 @@ _PROTOS = {
     "solrt_server_release": (ctypes.c_int, [_P, ctypes.c_uint64]),
     "solrt_server_cancel": (ctypes.c_int, [_P, ctypes.c_uint64]),
     "solrt_server_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(ServerStats)]),
+    "solrt_server_finished": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.c_uint32,
+                                             ctypes.POINTER(ctypes.c_uint32)]),
     "solrt_server_destroy": (ctypes.c_int, [_P]),
     "solrt_trace_rays": (ctypes.c_int, [_P, _P, _P, _U32, _P]),
     "solrt_trace_rays_device": (ctypes.c_int, [_P, _P, _P, _U32, _P]),
@@ -573,6 +582,35 @@ class Batch:
         return dict(block_size=r.best.block_size, smem_stack=r.best.smem_stack, pass_paths=r.best.pass_paths,
                     best_ms=r.best_ms, initial_ms=r.initial_ms, candidates=r.candidates)
 
+    def autotune_cached(self, path):
+        """solrt_batch_autotune_cached: the configuration cached for this
+        batch's shape at `path` (no timing), or autotune and store it."""
+        r, hit = TuneResult(), ctypes.c_uint32()
+        check(lib().solrt_batch_autotune_cached(self.handle, os.fsencode(path), ctypes.byref(r), ctypes.byref(hit)))
+        return dict(block_size=r.best.block_size, smem_stack=r.best.smem_stack, pass_paths=r.best.pass_paths,
+                    best_ms=r.best_ms, initial_ms=r.initial_ms, candidates=r.candidates, cache_hit=bool(hit.value))
+
+    def tune_key(self):
+        buf = ctypes.create_string_buffer(256)
+        check(lib().solrt_batch_tune_key(self.handle, buf, len(buf)))
+        return buf.value.decode()
+
+
+def tune_cache_lookup(path, key):
+    """The cached configuration of `key` as a dict, or None (host only)."""
+    c, ms = TuneConfig(), ctypes.c_float()
+    st = lib().solrt_tune_cache_lookup(os.fsencode(path), key.encode(), ctypes.byref(c), ctypes.byref(ms))
+    if st == ERR_NOT_FOUND:
+        return None
+    check(st)
+    return dict(block_size=c.block_size, smem_stack=c.smem_stack, pass_paths=c.pass_paths, best_ms=ms.value)
+
+
+def tune_cache_store(path, key, block_size, smem_stack, pass_paths=0, best_ms=0.0):
+    """Adds or replaces the cache entry of `key` (host only)."""
+    check(lib().solrt_tune_cache_store(os.fsencode(path), key.encode(), ctypes.byref(
+        TuneConfig(block_size=block_size, smem_stack=smem_stack, pass_paths=pass_paths)), best_ms))
+
 
 class Server:
     """Continuous-batching render server (solrt_server): a serving thread
@@ -625,6 +663,18 @@ class Server:
     def release(self, ticket):
         self._scenes.pop(ticket, None)
         return lib().solrt_server_release(self.handle, ticket)
+
+    def finished(self, max_tickets=4096):
+        """Tickets that reached their final state since the last call
+        (solrt_server_finished), oldest first."""
+        buf = (ctypes.c_uint64 * max_tickets)()
+        n = ctypes.c_uint32()
+        out = []
+        while True:
+            check(lib().solrt_server_finished(self.handle, buf, max_tickets, ctypes.byref(n)))
+            out.extend(buf[:n.value])
+            if n.value < max_tickets:
+                return out
 
     def cancel(self, ticket):
         """solrt_server_cancel: returns the status code."""

@@ -28,7 +28,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-prec-div=true",
               "-ftz=false", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
               "-Xcompiler", "-fno-fast-math", "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 SOURCES = ["api.cpp", "bvh_build.cu", "bvh8_build.cu", "trace.cu", "pathtrace.cu", "coop.cu", "server.cpp",
-           "gltf.cpp"]
+           "gltf.cpp", "tune_cache.cpp"]
 
 
 def nvcc():

@@ -357,6 +357,8 @@ solrt_status coop_wait_test(Context& ctx, double seconds, uint32_t* eflags);
 // pathtrace.cu
 solrt_status batch_plan(Context& ctx, const solrt_job* jobs, uint32_t n, uint32_t flags, Batch& b);
 solrt_status batch_autotune(Batch& b, solrt_tune_result* out);
+// Sets the context's launch shape / pass size and re-plans the batch with it.
+solrt_status batch_apply_tune(Batch& b, const TuneConfig& cfg);
 solrt_status batch_set_jobs(Batch& b, const solrt_job* jobs);
 solrt_status batch_launch(Batch& b);
 solrt_status render_frame(Context& ctx, const Scene& sc, const solrt_camera& cam, const solrt_render_params& p,

@@ -1051,6 +1051,21 @@ solrt_status batch_autotune(Batch& b, solrt_tune_result* out) {
     return s;
 }
 
+solrt_status batch_apply_tune(Batch& b, const TuneConfig& cfg) {
+    Context& ctx = *b.ctx;
+    const TuneConfig initial = ctx.tune;
+    const std::vector<solrt_job> src = b.src;
+    ctx.tune = cfg;
+    if (b.exec) { cudaGraphExecDestroy(b.exec); b.exec = nullptr; }
+    if (b.graph) { cudaGraphDestroy(b.graph); b.graph = nullptr; }
+    const solrt_status s = batch_plan(ctx, src.data(), (uint32_t)src.size(), b.flags, b);
+    if (s != SOLRT_OK) {  // back to the plan the call started from
+        ctx.tune = initial;
+        batch_plan(ctx, src.data(), (uint32_t)src.size(), b.flags, b);
+    }
+    return s;
+}
+
 // One serving tick: uploads the active jobs and this tick's items, runs one
 // pass, then finalizes the jobs listed in `fin` (their last samples were in
 // this pass). Asynchronous on the context stream.

@@ -91,6 +91,7 @@ struct solrt_server {
     std::deque<uint64_t> queue;
     std::vector<uint64_t> active;
     std::list<uint64_t> done_lru;                     // completed, unreleased; front = least recently used
+    std::deque<uint64_t> finished;                    // done / failed / cancelled, not yet fetched (completion queue)
     std::unordered_map<solrt_scene*, int> scene_refs;  // admitted (active or done) jobs per scene
     uint64_t bytes_in_use = 0;
     solrt_server_stats st{};
@@ -100,6 +101,10 @@ struct solrt_server {
 };
 
 namespace {
+
+// A job reached its final state (done, failed or cancelled): its ticket
+// joins the completion queue of solrt_server_finished. Caller holds the lock.
+void mark_finished(solrt_server* srv, uint64_t ticket) { srv->finished.push_back(ticket); }
 
 uint64_t scene_bytes(solrt_scene* s) {
     uint64_t b = 0;
@@ -145,6 +150,7 @@ void admit(solrt_server* srv) {
                 j.state = kFailed;
                 j.status = SOLRT_ERR_BUDGET;
                 j.t_done = now_ns();
+                mark_finished(srv, j.ticket);
                 srv->queue.pop_front();
                 srv->cv_done.notify_all();
                 continue;
@@ -178,6 +184,7 @@ void admit(solrt_server* srv) {
             j.state = kFailed;
             j.status = s;
             j.t_done = now_ns();
+            mark_finished(srv, j.ticket);
             srv->cv_done.notify_all();
             continue;
         }
@@ -220,6 +227,7 @@ void serve_loop(solrt_server* srv) {
                     j.state = kFailed;
                     j.status = SOLRT_ERR_CANCELLED;
                     j.t_done = now_ns();
+                    mark_finished(srv, j.ticket);
                 }
             }
             srv->active.erase(std::remove_if(srv->active.begin(), srv->active.end(),
@@ -306,6 +314,7 @@ void serve_loop(solrt_server* srv) {
                 j.state = kFailed;
                 j.status = s != SOLRT_OK ? s : SOLRT_ERR_DEVICE;
                 j.t_done = t_end;
+                mark_finished(srv, j.ticket);
                 continue;
             }
             j.spp_done += tick_k[i];
@@ -313,6 +322,7 @@ void serve_loop(solrt_server* srv) {
                 j.state = kDone;
                 j.status = SOLRT_OK;
                 j.t_done = t_end;
+                mark_finished(srv, j.ticket);
                 j.last_use = t_end;
                 srv->done_lru.push_back(j.ticket);
                 ++srv->st.completed;
@@ -361,12 +371,14 @@ void serve_loop(solrt_server* srv) {
                         j.state = kFailed;
                         j.status = fs != SOLRT_OK ? fs : SOLRT_ERR_DEVICE;
                         j.t_done = t_fin;
+                        mark_finished(srv, j.ticket);
                         continue;
                     }
                     j.state = kDone;
                     j.status = SOLRT_OK;
                     j.stopped_early = true;
                     j.t_done = t_fin;
+                    mark_finished(srv, j.ticket);
                     j.last_use = t_fin;
                     srv->done_lru.push_back(j.ticket);
                     ++srv->st.completed;
@@ -573,6 +585,7 @@ solrt_status solrt_server_cancel(solrt_server* srv, uint64_t ticket) {
         j.state = kFailed;
         j.status = SOLRT_ERR_CANCELLED;
         j.t_done = now_ns();
+        mark_finished(srv, j.ticket);
         srv->cv_done.notify_all();
         return SOLRT_OK;
     }
@@ -583,6 +596,21 @@ solrt_status solrt_server_cancel(solrt_server* srv, uint64_t ticket) {
     }
     set_error("job already finished");
     return SOLRT_ERR_INVALID;
+}
+
+solrt_status solrt_server_finished(solrt_server* srv, uint64_t* tickets, uint32_t max, uint32_t* n) {
+    if (!srv || !n || (max && !tickets)) {
+        set_error("null argument");
+        return SOLRT_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lock(srv->mu);
+    uint32_t k = 0;
+    while (k < max && !srv->finished.empty()) {
+        tickets[k++] = srv->finished.front();
+        srv->finished.pop_front();
+    }
+    *n = k;
+    return SOLRT_OK;
 }
 
 solrt_status solrt_server_get_stats(solrt_server* srv, solrt_server_stats* out) {

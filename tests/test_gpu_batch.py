@@ -309,3 +309,39 @@ def test_grid_barrier_wait_is_bounded(solrt, ctx):
     ctx.synchronize()
     assert ctx.stats().error_flags == 0
     b.close()
+
+
+def test_autotune_cache_miss_then_hit(solrt, tmp_path):
+    """solrt_batch_autotune_cached: the first call times the candidates and
+    stores the winner under the batch's key; a new batch of the same shape
+    (other cameras) finds it, re-plans with it without timing, and renders
+    the same images as the tuned batch."""
+    path = str(tmp_path / "tune.jsonl")
+    c = solrt.Context(0, path_capacity=1 << 18)
+    jobs = _plain_jobs(solrt, c, solrt.BVH2)
+    b = solrt.Batch(c, jobs, graph=True)
+    r1 = b.autotune_cached(path)
+    assert not r1["cache_hit"] and r1["candidates"] >= 8
+    key = b.tune_key()
+    assert key.startswith("gpu=") and "|kind=0|" in key
+    assert solrt.api.tune_cache_lookup(path, key)["block_size"] == r1["block_size"]
+    for _, img, _, _ in jobs:
+        img.clear()
+    b.launch()
+    c.synchronize()
+    want = [img.read()[0].copy() for _, img, _, _ in jobs]
+    b.close()
+    c.set_tune(128, 32, 0)
+    b2 = solrt.Batch(c, jobs, graph=True)
+    assert b2.tune_key() == key
+    r2 = b2.autotune_cached(path)
+    assert r2["cache_hit"] and r2["candidates"] == 0
+    assert c.get_tune() == {k: r1[k] for k in ("block_size", "smem_stack", "pass_paths")}
+    for _, img, _, _ in jobs:
+        img.clear()
+    b2.launch()
+    c.synchronize()
+    for (_, img, _, _), w in zip(jobs, want):
+        assert img.read()[0].view(np.uint32).tobytes() == w.view(np.uint32).tobytes()
+    b2.close()
+    c.close()

@@ -208,6 +208,12 @@ def test_cancel_queued_and_running(solrt):
     done = srv.submit(scenes[0], cam, keep[0])
     srv.wait(done, 60000)
     assert srv.cancel(done) == solrt.api.ERR_INVALID      # already finished
+    # the completion queue holds every finished ticket once, cancelled ones
+    # included, and is empty once fetched
+    fin = srv.finished(max_tickets=2)
+    assert sorted(fin) == sorted([t_long, t_queued, done] + t_keep) and len(set(fin)) == len(fin)
+    assert fin.index(t_queued) < fin.index(t_long)       # cancelled first while queued
+    assert srv.finished() == []
     assert srv.release(t_long) == 0
     srv.close()
     r = solrt.Renderer(ctx)
