@@ -536,7 +536,9 @@ solrt_status solrt_batch_tune_key(solrt_batch* batch, char* key, size_t key_byte
 solrt_status solrt_tune_cache_lookup(const char* path, const char* key, solrt_tune_config* cfg, float* best_ms);
 /* Host only. Adds or replaces the entry of `key` (the file is rewritten
  * through a temporary file and a rename, so readers never see half a
- * file). Keys hold no quote, backslash or control character. */
+ * file; of two processes storing at once, the later rename wins and the
+ * other's new entry is lost). Keys hold no quote, backslash or control
+ * character. */
 solrt_status solrt_tune_cache_store(const char* path, const char* key, const solrt_tune_config* cfg, float best_ms);
 /* solrt_batch_autotune through the cache at `path`: when it holds the
  * batch's key, applies that configuration to the context and re-plans the
