@@ -461,7 +461,7 @@ def parity_tunnel(local, n_rays=1 << 22, capacity=0):
     return out
 
 
-def reference_semantics(local, data, kw, cam, budget_s=3.0):
+def reference_semantics(local, data, kw, cam, budget_s=3.0, sah=True):
     """The workload's scene and image under the settings the reference's
     shaders fix (pathtrace.rgen:41-45, pathtrace.rchit:90-111,
     pathtrace.rmiss:8-21): 8 samples per launch, at most 32 bounces, the
@@ -481,7 +481,7 @@ def reference_semantics(local, data, kw, cam, budget_s=3.0):
     out = {"settings": "8 spp per launch, 32 bounces, reference materials, reference sky, per-pixel RNG stream, "
                        "mix accumulation (the reference shaders' own)"}
     with solrt.Context(local) as ctx:
-        sc = solrt.SceneDescription(ctx, data, keep_data=False)
+        sc = solrt.SceneDescription(ctx, data, keep_data=False, sah=sah)  # the BVH of the headline
         img = solrt.Image(ctx, W, H)
         r = solrt.Renderer(ctx)
         for f in range(2):
@@ -1074,7 +1074,7 @@ def main():
             except Exception as ex:
                 configs[name] = {"error": str(ex)}
         try:
-            refsem = reference_semantics(local, data, kw, cam)
+            refsem = reference_semantics(local, data, kw, cam, sah=args.sah)
         except Exception as ex:
             refsem = {"error": str(ex)}
     # the other two parts of the headline metric, measured on smaller runs:
