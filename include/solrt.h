@@ -512,8 +512,9 @@ solrt_status solrt_context_get_tune(solrt_context* ctx, solrt_tune_config* out);
  * graph keeps its launch shape until it is re-planned). */
 solrt_status solrt_context_set_tune(solrt_context* ctx, const solrt_tune_config* cfg);
 /* Times the batch (at most 32 of its jobs, spread over it) under each extend
- * block size x shared stack depth, then under pass sizes of 1/4, 1/2 and all
- * of the path capacity with the best of those, keeps the fastest on the
+ * block size x shared stack depth (not for SOLRT_BATCH_COOPERATIVE batches,
+ * whose kernel has one launch shape), then under pass sizes of 1/4, 1/2 and
+ * all of the path capacity with the best of those, keeps the fastest on the
  * context and re-plans the batch with it. Each candidate is launched three
  * times (one warm-up): REF_MIX images of the timed jobs hold the last
  * launch's frame afterwards, KAHAN images the sum of all of them (clear

@@ -1002,7 +1002,10 @@ solrt_status batch_autotune(Batch& b, solrt_tune_result* out) {
         float best_ms = initial_ms;
         const uint32_t smems[2] = {16u, 32u};
         const uint32_t blocks[3] = {64u, 128u, 256u};
-        for (uint32_t bl : blocks) {
+        // a cooperative batch's kernel has one launch shape: only the pass size is tuned
+        const uint32_t nblocks = (b.flags & SOLRT_BATCH_COOPERATIVE) ? 0u : 3u;
+        for (uint32_t bi = 0; bi < nblocks; ++bi) {
+            const uint32_t bl = blocks[bi];
             for (uint32_t sm : smems) {
                 if ((b.kind == SOLRT_BVH8_Q8 || b.kind == SOLRT_BVH8_F32) && sm != initial.smem) continue;  // no shared stack
                 TuneConfig c = initial;

@@ -345,3 +345,26 @@ def test_autotune_cache_miss_then_hit(solrt, tmp_path):
         assert img.read()[0].view(np.uint32).tobytes() == w.view(np.uint32).tobytes()
     b2.close()
     c.close()
+
+
+def test_cooperative_autotune_tunes_the_pass_size_only(solrt):
+    """A cooperative batch has one launch shape: the autotuner times only
+    the pass sizes (at most 3 candidates besides the start) and the
+    re-planned batch renders the same images."""
+    c = solrt.Context(0, path_capacity=1 << 18)
+    jobs = _plain_jobs(solrt, c, solrt.BVH2)
+    b = solrt.Batch(c, jobs, graph=True, cooperative=True)
+    b.launch()
+    c.synchronize()
+    want = [img.read()[0].copy() for _, img, _, _ in jobs]
+    r = b.autotune()
+    assert 1 <= r["candidates"] <= 4
+    assert (r["block_size"], r["smem_stack"]) == (128, 32)
+    for _, img, _, _ in jobs:
+        img.clear()
+    b.launch()
+    c.synchronize()
+    for (_, img, _, _), w in zip(jobs, want):
+        assert np.array_equal(img.read()[0].view(np.uint32), w.view(np.uint32))
+    b.close()
+    c.close()
