@@ -440,6 +440,9 @@ solrt_status solrt_render(solrt_context* ctx, solrt_scene* scene, const solrt_ca
 /* ------------------------------------------------------------------------ */
 /* Batched rendering: many scenes, one wavefront                            */
 /* ------------------------------------------------------------------------ */
+/* No counterpart in the reference, which renders one scene per
+ * ShaderBindingTable::cmd_trace_rays (src/ray/sbt.rs:167-180): this is the
+ * batched mixed-scene workload built on the same per-job semantics. */
 
 /* One render job: what one solrt_render call takes. */
 typedef struct solrt_job {
@@ -551,6 +554,8 @@ solrt_status solrt_batch_autotune_cached(solrt_batch* batch, const char* path, s
 /* ------------------------------------------------------------------------ */
 /* Serving: continuous batching of render jobs                              */
 /* ------------------------------------------------------------------------ */
+/* No counterpart in the reference (an interactive single-window renderer):
+ * the served-jobs workload, each job rendered as solrt_render renders it. */
 
 typedef enum solrt_serve_policy {
     /* every active job gets an equal share of each tick's paths */
