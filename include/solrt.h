@@ -465,11 +465,11 @@ enum {
     /* the wavefront passes of a step (generate, extend and shade per bounce,
      * accumulate, finalize) as phases of one cooperative launch: a grid of
      * (SMs x resident blocks) that meets at grid-wide barriers between
-     * stages instead of one launch per stage; same images. Each barrier wait
-     * is bounded: a launch whose blocks do not all arrive ends with
-     * SOLRT_ERR_TIMEOUT. Path integrator only (no next-event estimation);
-     * node / triangle counters are not gathered. Not with
-     * SOLRT_BATCH_PERSISTENT. */
+     * stages instead of one launch per stage (next-event-estimation jobs add
+     * a shadow-ray extend and a resolve phase per bounce); same images. Each
+     * barrier wait is bounded: a launch whose blocks do not all arrive ends
+     * with SOLRT_ERR_TIMEOUT. Node / triangle counters are not gathered.
+     * Not with SOLRT_BATCH_PERSISTENT. */
     SOLRT_BATCH_COOPERATIVE = 4u
 };
 

@@ -23,6 +23,11 @@
 // hits, path radiance, queue counts, pixel sums, REF_STREAM states) is read
 // through L2 (ld.global.cg): the SM's L1 is not coherent with other SMs'
 // writes within a launch. Scene data is read-only for the launch.
+//
+// Batches with next-event-estimation jobs run the kNee variant: after each
+// shade phase (which also pushes shadow rays), an any-hit extend phase over
+// the shadow queue and a resolve phase that adds the unoccluded shadow
+// rays' terms to their paths, as issue_pass does with separate launches.
 #include <algorithm>
 
 #include "bvh2_2l.cuh"
@@ -85,24 +90,29 @@ struct CoopArgs {
     uint32_t njobs;
     uint32_t total_pix;
     PathQueue q0, q1;
+    PathQueue qs;         // shadow rays (kNee)
     float4* hits;
     float4* rad;
     uint32_t capacity;
     CoopSync* sync;
-    unsigned int* ctr;    // per pass: count[ctr_stride] (queue length per bounce), then work[ctr_stride]
+    unsigned int* ctr;    // per pass: count, work, shadow count, shadow work (ctr_stride each, by bounce)
     uint32_t ctr_stride;
     DevStats* stats;
     long long wait_cycles;  // budget of one barrier wait in SM clock cycles
 };
 
 // Wavefront queue through L2 (QueueIO of trace.cu with ld.global.cg loads).
-struct CoopIO {
+// kNee: any_hit is a run-time field, so that the closest-hit and the shadow
+// (any-hit) phases share one instantiation of the traversal loop and its
+// shared-memory stack.
+template <bool kNee>
+struct CoopIOT {
     const float4* o_tmin;
     const float4* d_tmax;
     const uint2* meta;
     const DevJob* jobs;
     float4* hits;
-    static constexpr bool any_hit = false;
+    bool any_hit;
     SOLRT_D void load(uint32_t i, float4& o, float4& d, TravScene& ts) const {
         o = __ldcg(o_tmin + i);
         d = __ldcg(d_tmax + i);
@@ -115,6 +125,26 @@ struct CoopIO {
         ts.inst = s->inst;
         ts.tlas_count = s->tlas_count;
         ts.inst_count = s->inst_count;
+    }
+    SOLRT_D void load_ray(uint32_t i, float4& o, float4& d) const {
+        o = __ldcg(o_tmin + i);
+        d = __ldcg(d_tmax + i);
+    }
+    SOLRT_D void store(uint32_t i, const HitRec& h) const {
+        hits[i] = make_float4(h.t, __uint_as_float(h.prim), h.u, h.v);
+    }
+};
+template <>
+struct CoopIOT<false> {
+    const float4* o_tmin;
+    const float4* d_tmax;
+    const uint2* meta;
+    const DevJob* jobs;
+    float4* hits;
+    bool unused;
+    static constexpr bool any_hit = false;
+    SOLRT_D void load(uint32_t i, float4& o, float4& d, TravScene& ts) const {
+        CoopIOT<true>{o_tmin, d_tmax, meta, jobs, hits, false}.load(i, o, d, ts);
     }
     SOLRT_D void load_ray(uint32_t i, float4& o, float4& d) const {
         o = __ldcg(o_tmin + i);
@@ -142,6 +172,8 @@ struct CoopCtl {
     uint32_t ok;   // 0: the launch is being abandoned
     uint32_t fb;   // FP64 fallbacks of the block's traversals
     uint32_t ef;   // error flags of the block
+    uint32_t sfb;  // FP64 fallbacks of its shadow-ray traversals (kNee)
+    uint32_t unocc;  // shadow rays it found unoccluded (kNee)
 };
 enum CoopAdvance { kStay = 0, kNextBounce = 1, kNextPass = 2 };
 
@@ -259,11 +291,124 @@ SOLRT_COOP_SHADE_ATTR uint32_t coop_shade(const DevJob* jobs, const DevItem* ite
     return ef;
 }
 
+// The shade stage of k_shade's next-event-estimation variant over the n
+// paths of queue qin: survivors go to qout and their shadow rays to qs, both
+// with one atomic per warp; a path that ends adds its term to its radiance
+// slot after the shadow terms resolved so far. Returns the error flags.
+SOLRT_COOP_SHADE_ATTR uint32_t coop_shade_nee(const DevJob* jobs, const DevItem* items, uint32_t nitems,
+                                              const PathQueue& qin, const float4* hits, uint32_t n,
+                                              const PathQueue& qout, unsigned int* count_out, uint32_t capacity,
+                                              float4* rad, const PathQueue& qs, unsigned int* count_s) {
+    uint32_t ef = 0;
+    const int lane = threadIdx.x & 31;
+    const uint32_t lane_lt = (1u << lane) - 1u;
+    const uint32_t start = ((blockIdx.x * kCoopBlock + threadIdx.x) >> 5) * 32u;
+    const uint32_t stride = ((gridDim.x * kCoopBlock) >> 5) * 32u;
+    for (uint32_t base = start; base < n; base += stride) {
+        const uint32_t i = base + (uint32_t)lane;
+        bool alive = false, shadow = false, out_nee = false;
+        float4 out_o = make_float4(0, 0, 0, 0), out_d = make_float4(0, 0, 0, 0), out_t = make_float4(0, 0, 0, 0);
+        float4 s_o = make_float4(0, 0, 0, 0), s_d = make_float4(0, 0, 0, 0), s_c = make_float4(0, 0, 0, 0);
+        float4 out_prev = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        uint2 m = make_uint2(0, 0);
+        if (i < n) {
+            const float4 o = __ldcg(qin.o_tmin + i), d = __ldcg(qin.d_tmax + i), tr = __ldcg(qin.thr_rng + i);
+            m = __ldcg(qin.meta + i);
+            const uint32_t job = m.y >> kDepthBits;
+            const DevJob& J = jobs[job];
+            const bool nee = J.integrator == SOLRT_INTEGRATOR_PATH_NEE;
+            uint32_t rng = __float_as_uint(tr.w);
+            uint32_t depth = m.y & kDepthMask;
+            f3 acc{tr.x, tr.y, tr.z};
+            f3 n_o{0.0f, 0.0f, 0.0f};
+            const float4 prev = nee && depth > 0u ? __ldcg(qin.prev + i) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (shade_step<true>(J, o, d, __ldcg(hits + i), acc, rng, depth, out_o, out_d, ef, &n_o, prev,
+                                 &out_prev)) {
+                alive = true;
+                if (nee) {
+                    out_nee = true;
+                    f3 cn;
+                    shadow = nee_sample(J.sc, f3{out_o.x, out_o.y, out_o.z}, n_o, acc, o.w, rng, s_o, s_d, cn);
+                    s_c = make_float4(cn.x, cn.y, cn.z, 0.0f);
+                }
+                out_t = make_float4(acc.x, acc.y, acc.z, __uint_as_float(rng));
+                m.y = (job << kDepthBits) | depth;
+            } else {
+                if (nee) {  // after this path's earlier shadow terms (resolved in bounce order)
+                    const float4 r = __ldcg(rad + m.x);
+                    rad[m.x] = make_float4(r.x + acc.x, r.y + acc.y, r.z + acc.z, 0.0f);
+                } else {
+                    rad[m.x] = make_float4(acc.x, acc.y, acc.z, 0.0f);
+                }
+                if (J.rng_mode == SOLRT_RNG_REF_STREAM) {
+                    const DevItem it = items[find_last_le(nitems, m.x, [&](uint32_t t) { return items[t].path_base; })];
+                    J.rng_state[it.pix0 + (m.x - it.path_base) / it.k] = rng;
+                }
+            }
+        }
+        const uint32_t mask = __ballot_sync(0xffffffffu, alive);
+        const uint32_t smask = __ballot_sync(0xffffffffu, shadow);
+        if (mask) {
+            const int leader = __ffs(mask) - 1;
+            uint32_t pos0 = 0;
+            if (lane == leader) pos0 = atomicAdd(count_out, (unsigned int)__popc(mask));
+            pos0 = __shfl_sync(0xffffffffu, pos0, leader);
+            if (alive) {
+                const uint32_t pos = pos0 + (uint32_t)__popc(mask & lane_lt);
+                if (pos < capacity) {
+                    qout.o_tmin[pos] = out_o;
+                    qout.d_tmax[pos] = out_d;
+                    qout.thr_rng[pos] = out_t;
+                    qout.meta[pos] = m;
+                    if (out_nee) qout.prev[pos] = out_prev;
+                } else {
+                    ef |= SOLRT_EFLAG_QUEUE;
+                }
+            }
+        }
+        if (smask) {
+            const int leader = __ffs(smask) - 1;
+            uint32_t pos0 = 0;
+            if (lane == leader) pos0 = atomicAdd(count_s, (unsigned int)__popc(smask));
+            pos0 = __shfl_sync(0xffffffffu, pos0, leader);
+            if (shadow) {
+                const uint32_t pos = pos0 + (uint32_t)__popc(smask & lane_lt);
+                if (pos < capacity) {
+                    qs.o_tmin[pos] = s_o;
+                    qs.d_tmax[pos] = s_d;
+                    qs.thr_rng[pos] = s_c;
+                    qs.meta[pos] = m;
+                } else {
+                    ef |= SOLRT_EFLAG_QUEUE;
+                }
+            }
+        }
+    }
+    return ef;
+}
+
+// k_shadow_resolve over the ns shadow rays of qs: an unoccluded one adds its
+// term to its path's slot (one shadow ray per path and bounce, so no two
+// threads share a slot). Returns the unoccluded rays this thread resolved.
+SOLRT_D uint32_t coop_resolve(const PathQueue& qs, const float4* hits, uint32_t ns, float4* rad) {
+    uint32_t reached = 0;
+    for (uint32_t i = blockIdx.x * kCoopBlock + threadIdx.x; i < ns; i += gridDim.x * kCoopBlock) {
+        if (__float_as_uint(__ldcg(hits + i).y) != SOLRT_NO_HIT) continue;
+        const float4 c = __ldcg(qs.thr_rng + i);
+        const uint32_t slot = __ldcg(&qs.meta[i].x);
+        const float4 r = __ldcg(rad + slot);
+        rad[slot] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, 0.0f);
+        ++reached;
+    }
+    return reached;
+}
+
 // The closest hits of the n rays of queue q (the extend kernel's loop for
 // the kind, 32 shared-memory stack slots for the binary kinds). Returns
 // (FP64 fallbacks, error flags).
-template <int KIND>
-SOLRT_COOP_EXTEND_ATTR uint2 coop_extend(const CoopIO& io, uint32_t n, unsigned int* work) {
+template <int KIND, bool kNee>
+SOLRT_COOP_EXTEND_ATTR uint2 coop_extend(const CoopIOT<kNee>& io, uint32_t n, unsigned int* work) {
+    using CoopIO = CoopIOT<kNee>;
     TraceCounters cnt{0, 0, 0};
     uint32_t ef = 0;
     if constexpr (KIND == SOLRT_BVH2) {
@@ -290,7 +435,7 @@ constexpr int coop_min_blocks() {
     return (KIND == SOLRT_BVH8_Q8 || KIND == SOLRT_BVH8_F32 || KIND == SOLRT_BVH4_Q8) ? 7 : SOLRT_COOP_MINB;
 }
 
-template <int KIND>
+template <int KIND, bool kNee>
 __global__ void __launch_bounds__(kCoopBlock, (coop_min_blocks<KIND>())) k_batch_coop(const CoopArgs a) {
     volatile __shared__ CoopCtl c;
     if (threadIdx.x == 0) {
@@ -300,8 +445,12 @@ __global__ void __launch_bounds__(kCoopBlock, (coop_min_blocks<KIND>())) k_batch
         c.ok = 1u;
         c.fb = 0u;
         c.ef = 0u;
+        c.sfb = 0u;
+        c.unocc = 0u;
     }
     __syncthreads();
+    // counters of pass p: count, work, shadow count, shadow work, by bounce
+    auto counters = [&](uint32_t p) { return a.ctr + (size_t)p * 4u * a.ctr_stride; };
     for (uint32_t t = blockIdx.x * kCoopBlock + threadIdx.x; t < a.total_pix; t += gridDim.x * kCoopBlock)
         begin_pixel(a.jobs, a.job_pix, a.njobs, t);
     while (c.p < a.npasses) {
@@ -318,27 +467,52 @@ __global__ void __launch_bounds__(kCoopBlock, (coop_min_blocks<KIND>())) k_batch
             {   // extend of bounce level b
                 const uint32_t p = c.p, b = c.b;
                 if (b >= a.passes[p].bounces) break;
-                unsigned int* count = a.ctr + (size_t)p * 2u * a.ctr_stride;
+                unsigned int* count = counters(p);
                 const uint32_t nq = b == 0 ? a.passes[p].paths : __ldcg(count + b);
                 const uint32_t n = nq < a.capacity ? nq : a.capacity;
                 if (n == 0) break;  // every block reads the same count: the exit is grid-uniform
                 if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&a.stats->segments, (unsigned long long)n);
                 const PathQueue& qin = (b & 1u) ? a.q1 : a.q0;
-                const uint2 r = coop_extend<KIND>(CoopIO{qin.o_tmin, qin.d_tmax, qin.meta, a.jobs, a.hits}, n,
-                                                  count + a.ctr_stride + b);
+                const uint2 r = coop_extend<KIND, kNee>(
+                    CoopIOT<kNee>{qin.o_tmin, qin.d_tmax, qin.meta, a.jobs, a.hits, false}, n,
+                    count + a.ctr_stride + b);
                 coop_flush(c, r.x, r.y);
             }
             if (!coop_barrier(a, c, kStay)) break;
             {   // shade of the same level: survivors into the other queue
                 const uint32_t p = c.p, b = c.b;
                 const PassPlan pp = a.passes[p];
-                unsigned int* count = a.ctr + (size_t)p * 2u * a.ctr_stride;
+                unsigned int* count = counters(p);
                 const uint32_t nq = b == 0 ? pp.paths : __ldcg(count + b);
                 const uint32_t n = nq < a.capacity ? nq : a.capacity;
                 const PathQueue& qin = (b & 1u) ? a.q1 : a.q0;
                 const PathQueue& qout = (b & 1u) ? a.q0 : a.q1;
-                coop_flush(c, 0u, coop_shade(a.jobs, a.items + pp.item_begin, pp.item_count, qin, a.hits, n, qout,
-                                             count + b + 1, a.capacity, a.rad));
+                if constexpr (kNee)
+                    coop_flush(c, 0u, coop_shade_nee(a.jobs, a.items + pp.item_begin, pp.item_count, qin, a.hits, n,
+                                                     qout, count + b + 1, a.capacity, a.rad, a.qs,
+                                                     count + 2u * a.ctr_stride + b));
+                else
+                    coop_flush(c, 0u, coop_shade(a.jobs, a.items + pp.item_begin, pp.item_count, qin, a.hits, n,
+                                                 qout, count + b + 1, a.capacity, a.rad));
+            }
+            if constexpr (kNee) {  // shadow rays of this level (none at the last: depth > max)
+                if (!coop_barrier(a, c, kStay)) break;
+                const uint32_t p = c.p, b = c.b;
+                unsigned int* count = counters(p);
+                const uint32_t nq = b + 1u < a.passes[p].bounces ? __ldcg(count + 2u * a.ctr_stride + b) : 0u;
+                const uint32_t ns = nq < a.capacity ? nq : a.capacity;
+                if (ns) {
+                    if (blockIdx.x == 0 && threadIdx.x == 0)
+                        atomicAdd(&a.stats[1].segments, (unsigned long long)ns);
+                    const uint2 r = coop_extend<KIND, kNee>(
+                        CoopIOT<kNee>{a.qs.o_tmin, a.qs.d_tmax, a.qs.meta, a.jobs, a.hits, true}, ns,
+                        count + 3u * a.ctr_stride + b);
+                    if (r.x) atomicAdd(const_cast<uint32_t*>(&c.sfb), r.x);
+                    if (r.y) atomicOr(const_cast<uint32_t*>(&c.ef), r.y);
+                    if (!coop_barrier(a, c, kStay)) break;
+                    const uint32_t u = coop_resolve(a.qs, a.hits, ns, a.rad);
+                    if (u) atomicAdd(const_cast<uint32_t*>(&c.unocc), u);
+                }
             }
             if (!coop_barrier(a, c, kNextBounce)) break;
         }
@@ -363,6 +537,8 @@ __global__ void __launch_bounds__(kCoopBlock, (coop_min_blocks<KIND>())) k_batch
     if (threadIdx.x == 0) {
         if (c.fb) atomicAdd(&a.stats->fp64_fallbacks, (unsigned long long)c.fb);
         if (c.ef) atomicOr(&a.stats->eflags, c.ef);
+        if (kNee && c.sfb) atomicAdd(&a.stats[1].fp64_fallbacks, (unsigned long long)c.sfb);
+        if (kNee && c.unocc) atomicAdd(&a.stats[1].unoccluded, (unsigned long long)c.unocc);
     }
 }
 
@@ -380,8 +556,8 @@ __global__ void k_coop_wait_test(const CoopArgs a) {
 }
 
 template <int KIND>
-solrt_status launch_kind(Context& ctx, const CoopArgs& args) {
-    auto kern = k_batch_coop<KIND>;
+solrt_status launch_kind(Context& ctx, const CoopArgs& args, bool nee) {
+    auto kern = nee ? k_batch_coop<KIND, true> : k_batch_coop<KIND, false>;
     int per_sm = 0;
     SOLRT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCoopBlock, 0));
     if (per_sm < 1) {
@@ -414,12 +590,12 @@ long long wait_budget_cycles(const Context& ctx, double seconds) {
 }  // namespace
 
 size_t coop_buffer_bytes(uint32_t npasses, uint32_t stride) {
-    return sizeof(CoopSync) + sizeof(unsigned int) * 2u * (size_t)npasses * stride;
+    return sizeof(CoopSync) + sizeof(unsigned int) * 4u * (size_t)npasses * stride;
 }
 
 solrt_status launch_batch_coop(Context& ctx, uint32_t kind, const DevJob* jobs, const DevItem* items,
                                const PassPlan* passes, uint32_t npasses, uint32_t ctr_stride, const uint32_t* job_pix,
-                               uint32_t njobs, uint32_t total_pix, void* coop) {
+                               uint32_t njobs, uint32_t total_pix, void* coop, bool nee) {
     SOLRT_CUDA(cudaMemsetAsync(coop, 0, coop_buffer_bytes(npasses, ctr_stride), ctx.stream));
     CoopArgs a;
     a.jobs = jobs;
@@ -431,6 +607,11 @@ solrt_status launch_batch_coop(Context& ctx, uint32_t kind, const DevJob* jobs, 
     a.total_pix = total_pix;
     a.q0 = ctx.queue(0);
     a.q1 = ctx.queue(1);
+    a.qs = ctx.queue(2);
+    if (nee && !a.qs.o_tmin) {
+        set_error("shadow queue not allocated");
+        return SOLRT_ERR_INVALID;
+    }
     a.hits = ctx.hits.as<float4>();
     a.rad = ctx.rad.as<float4>();
     a.capacity = ctx.capacity;
@@ -439,12 +620,12 @@ solrt_status launch_batch_coop(Context& ctx, uint32_t kind, const DevJob* jobs, 
     a.ctr_stride = ctr_stride;
     a.stats = ctx.stats.as<DevStats>();
     a.wait_cycles = wait_budget_cycles(ctx, 4.0);
-    if (kind == SOLRT_BVH8_Q8) SOLRT_TRY(launch_kind<SOLRT_BVH8_Q8>(ctx, a));
-    else if (kind == SOLRT_BVH4_Q8) SOLRT_TRY(launch_kind<SOLRT_BVH4_Q8>(ctx, a));
-    else if (kind == SOLRT_BVH8_F32) SOLRT_TRY(launch_kind<SOLRT_BVH8_F32>(ctx, a));
-    else if (kind == SOLRT_BVH2_Q16) SOLRT_TRY(launch_kind<SOLRT_BVH2_Q16>(ctx, a));
-    else if (kind == SOLRT_BVH2_TWO_LEVEL) SOLRT_TRY(launch_kind<SOLRT_BVH2_TWO_LEVEL>(ctx, a));
-    else SOLRT_TRY(launch_kind<SOLRT_BVH2>(ctx, a));
+    if (kind == SOLRT_BVH8_Q8) SOLRT_TRY(launch_kind<SOLRT_BVH8_Q8>(ctx, a, nee));
+    else if (kind == SOLRT_BVH4_Q8) SOLRT_TRY(launch_kind<SOLRT_BVH4_Q8>(ctx, a, nee));
+    else if (kind == SOLRT_BVH8_F32) SOLRT_TRY(launch_kind<SOLRT_BVH8_F32>(ctx, a, nee));
+    else if (kind == SOLRT_BVH2_Q16) SOLRT_TRY(launch_kind<SOLRT_BVH2_Q16>(ctx, a, nee));
+    else if (kind == SOLRT_BVH2_TWO_LEVEL) SOLRT_TRY(launch_kind<SOLRT_BVH2_TWO_LEVEL>(ctx, a, nee));
+    else SOLRT_TRY(launch_kind<SOLRT_BVH2>(ctx, a, nee));
     ++ctx.launches;
     return SOLRT_OK;
 }

@@ -157,7 +157,7 @@ struct Batch {
     // SOLRT_BATCH_COOPERATIVE: the pass table on the device and the launch's
     // barrier word + per-pass queue counts (coop_buffer_bytes)
     DeviceBuffer d_passes, d_coop;
-    uint32_t coop_stride = 0;  // counters per pass and kind (count / work): max bounces + 2
+    uint32_t coop_stride = 0;  // counters per pass and kind (count, work, shadow count, shadow work): max bounces + 2
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     std::vector<solrt_job> src;  // the jobs as given (re-planned by the autotuner)
@@ -348,7 +348,7 @@ size_t coop_buffer_bytes(uint32_t npasses, uint32_t stride);
 // cooperative launch on the context stream.
 solrt_status launch_batch_coop(Context& ctx, uint32_t kind, const DevJob* jobs, const DevItem* items,
                                const PassPlan* passes, uint32_t npasses, uint32_t ctr_stride, const uint32_t* job_pix,
-                               uint32_t njobs, uint32_t total_pix, void* coop);
+                               uint32_t njobs, uint32_t total_pix, void* coop, bool nee);
 // A cooperative grid whose block 0 never reaches the barrier the others wait
 // at, each wait bounded by `seconds`; returns the error flags it raised
 // (SOLRT_EFLAG_TIMEOUT expected). Synchronises.

@@ -759,8 +759,10 @@ solrt_status batch_issue(Batch& b, bool record_timing) {
     }
     if (b.flags & SOLRT_BATCH_COOPERATIVE) {
         const int tm = record_timing ? ctx.timing_begin(0) : -1;  // every stage in one launch
+        bool nee = false;
+        for (const PassPlan& pp : b.passes) nee = nee || pp.nee;
         SOLRT_TRY(launch_batch_coop(ctx, b.kind, dj, di, b.d_passes.as<PassPlan>(), (uint32_t)b.passes.size(),
-                                    b.coop_stride, jp, njobs, total_pix, b.d_coop.ptr));
+                                    b.coop_stride, jp, njobs, total_pix, b.d_coop.ptr, nee));
         ctx.timing_end(tm);
         SOLRT_CUDA(cudaGetLastError());
         return SOLRT_OK;
@@ -806,10 +808,6 @@ solrt_status batch_plan(Context& ctx, const solrt_job* jobs, uint32_t n, uint32_
         }
         if (jb.params.integrator == SOLRT_INTEGRATOR_PATH_NEE && (flags & SOLRT_BATCH_PERSISTENT)) {
             set_error("job %u: persistent batches run the path integrator without next-event estimation", j);
-            return SOLRT_ERR_INVALID;
-        }
-        if (jb.params.integrator == SOLRT_INTEGRATOR_PATH_NEE && (flags & SOLRT_BATCH_COOPERATIVE)) {
-            set_error("job %u: cooperative batches run the path integrator without next-event estimation", j);
             return SOLRT_ERR_INVALID;
         }
         if (jb.params.integrator == SOLRT_INTEGRATOR_PATH_NEE) SOLRT_TRY(ensure_shadow_queue(ctx));

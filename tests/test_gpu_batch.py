@@ -233,11 +233,11 @@ def _plain_jobs(solrt, ctx, kind):
 def test_cooperative_batch_equals_alone(solrt, ctx, bvh, graph):
     """SOLRT_BATCH_COOPERATIVE: every wavefront pass of the batch as phases
     of one cooperative launch (grid-wide barriers between generate, extend,
-    shade and accumulate) renders each job bit for bit as solrt_render of
-    that job alone, over two frames, with and without a CUDA graph; one
-    kernel launch per step."""
+    shade, the shadow-ray phases of next-event estimation and accumulate)
+    renders each job bit for bit as solrt_render of that job alone, over two
+    frames, with and without a CUDA graph; one kernel launch per step."""
     kind = bvh_kind(solrt, bvh)
-    jobs = _plain_jobs(solrt, ctx, kind)
+    jobs = _make(solrt, ctx, kind)   # next-event-estimation jobs included
     batch = solrt.Batch(ctx, jobs, graph=graph, cooperative=True)
     ctx.reset_stats()
     batch.launch()
@@ -263,31 +263,29 @@ def test_cooperative_batch_equals_alone(solrt, ctx, bvh, graph):
 
 def test_cooperative_many_passes_and_counts(solrt):
     """A capacity of 2000 paths makes dozens of mixed passes inside the one
-    launch; images and segment / path counts equal the per-stage launches'."""
+    launch; images and segment / path / shadow-ray counts equal the
+    per-stage launches'."""
     res = []
     for coop in (False, True):
         c = solrt.Context(0, path_capacity=2000)
-        jobs = _plain_jobs(solrt, c, solrt.BVH2)
+        jobs = _make(solrt, c, solrt.BVH2)
         b = solrt.Batch(c, jobs, cooperative=coop)
         c.reset_stats()
         b.launch()
         c.synchronize()
         st = c.stats()
         assert st.error_flags == 0
-        res.append(([img.read()[0].copy() for _, img, _, _ in jobs], b.info(), st.segments, st.paths))
+        res.append(([img.read()[0].copy() for _, img, _, _ in jobs], b.info(), st.segments, st.paths,
+                    st.shadow_segments, st.shadow_unoccluded))
         b.close()
         c.close()
     assert res[0][1]["passes"] > 10 and res[0][1] == res[1][1]
-    assert res[0][2:] == res[1][2:]
+    assert res[0][2:] == res[1][2:] and res[0][4] > 0
     for x, y in zip(res[0][0], res[1][0]):
         assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
 
 
 def test_cooperative_batch_refusals(solrt, ctx):
-    nee = [j for j, (_, _, _, kw) in zip(_make(solrt, ctx, solrt.BVH2), _specs(solrt))
-           if kw.get("integrator", solrt.INTEGRATOR_PATH) == solrt.INTEGRATOR_PATH_NEE]
-    with pytest.raises(solrt.SolrtError):
-        solrt.Batch(ctx, nee, cooperative=True)
     plain = _plain_jobs(solrt, ctx, solrt.BVH2)
     with pytest.raises(solrt.SolrtError):
         solrt.Batch(ctx, plain, persistent=True, cooperative=True)
