@@ -506,7 +506,7 @@ solrt_status solrt_scene_create(solrt_context* ctx, const solrt_scene_desc* d, c
     // world positions for the BVH; object-space positions and normals for
     // shading, which interpolates them and then applies the section's
     // transform / transform_it (pathtrace.rchit:80-90)
-    std::vector<float4> pos(nv), col(nv), opos(nv), onrm(nv);
+    std::vector<float4> pos(nv), opos(nv), vnc(2 * nv);  // vnc: (normal, colour) per vertex
     std::vector<uint32_t> vsec_start(d->section_count), sec_mat(d->section_count);
     std::vector<solrt_instance> inst(d->section_count);
     std::vector<uint32_t> sec_first(d->section_count), sec_count(d->section_count);
@@ -532,11 +532,11 @@ solrt_status solrt_scene_create(solrt_context* ctx, const solrt_scene_desc* d, c
         for (uint32_t v = 0; v < sec.vertex_count; ++v) {
             const solrt_vertex& in = d->vertices[sec.vertex_offset + v];
             opos[vb + v] = make_float4(in.pos[0], in.pos[1], in.pos[2], 0.0f);
-            onrm[vb + v] = make_float4(in.normal[0], in.normal[1], in.normal[2], 0.0f);
+            vnc[2 * (vb + v)] = make_float4(in.normal[0], in.normal[1], in.normal[2], 0.0f);
             float o[4];
             mat4_mul(T, in.pos[0], in.pos[1], in.pos[2], 1.0f, o);       // the BVH's world positions
             pos[vb + v] = make_float4(o[0], o[1], o[2], 0.0f);
-            col[vb + v] = make_float4(in.color[0], in.color[1], in.color[2], 0.0f);
+            vnc[2 * (vb + v) + 1] = make_float4(in.color[0], in.color[1], in.color[2], 0.0f);
         }
         for (uint32_t t = 0; t < sec.index_count / 3; ++t) {
             uint32_t id[3];
@@ -565,16 +565,15 @@ solrt_status solrt_scene_create(solrt_context* ctx, const solrt_scene_desc* d, c
     cudaStream_t st = ctx->stream;
     solrt_status s;
     const size_t ns = d->section_count;
-    if ((s = sc->vpos.alloc(16 * nv)) || (s = sc->vcol.alloc(16 * nv)) || (s = sc->opos.alloc(16 * nv)) ||
-        (s = sc->onrm.alloc(16 * nv)) || (s = sc->tri_idx.alloc(16 * nt)) ||
+    if ((s = sc->vpos.alloc(16 * nv)) || (s = sc->opos.alloc(16 * nv)) || (s = sc->vnc.alloc(32 * nv)) ||
+        (s = sc->tri_idx.alloc(16 * nt)) ||
         (s = sc->materials.alloc(48 * (size_t)d->material_count)) || (s = sc->sec_mat.alloc(4 * ns)) ||
         (s = sc->vsec_start.alloc(4 * ns)) || (s = sc->instances.alloc(sizeof(solrt_instance) * ns)))
         return fail(s);
     if (nv) {
         if (cudaMemcpyAsync(sc->vpos.ptr, pos.data(), 16 * nv, cudaMemcpyHostToDevice, st) != cudaSuccess ||
-            cudaMemcpyAsync(sc->vcol.ptr, col.data(), 16 * nv, cudaMemcpyHostToDevice, st) != cudaSuccess ||
             cudaMemcpyAsync(sc->opos.ptr, opos.data(), 16 * nv, cudaMemcpyHostToDevice, st) != cudaSuccess ||
-            cudaMemcpyAsync(sc->onrm.ptr, onrm.data(), 16 * nv, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+            cudaMemcpyAsync(sc->vnc.ptr, vnc.data(), 32 * nv, cudaMemcpyHostToDevice, st) != cudaSuccess) {
             set_error("scene upload failed");
             return fail(SOLRT_ERR_DEVICE);
         }
@@ -676,7 +675,7 @@ solrt_status solrt_scene_bvh_export(solrt_scene* scene, void* nodes, size_t node
 
 solrt_status solrt_scene_bytes(solrt_scene* scene, uint64_t* out) {
     CHECK_ARG(scene && out, "null argument");
-    *out = scene->vpos.bytes + scene->opos.bytes + scene->onrm.bytes + scene->vcol.bytes + scene->tri_idx.bytes +
+    *out = scene->vpos.bytes + scene->opos.bytes + scene->vnc.bytes + scene->tri_idx.bytes +
            scene->materials.bytes + scene->sec_mat.bytes + scene->nodes.bytes + scene->tri_wt.bytes +
            scene->vsec_start.bytes + scene->instances.bytes + scene->topo_order.bytes + scene->topo_child.bytes +
            scene->topo_par_int.bytes + scene->topo_par_leaf.bytes + scene->topo_range.bytes + scene->tlas.bytes +

@@ -1244,7 +1244,7 @@ solrt_status build_bvh(Context& ctx, Scene& sc, const solrt_bvh_desc& desc) {
     if (desc.kind == SOLRT_BVH2_TWO_LEVEL) SOLRT_TRY(build_two_level(ctx, sc));
     else SOLRT_TRY(build_single_level(ctx, sc, desc));
     sc.info.tri_bytes = sc.tri_wt.bytes;
-    sc.info.shade_bytes = sc.opos.bytes + sc.onrm.bytes + sc.vcol.bytes + sc.tri_idx.bytes + sc.materials.bytes +
+    sc.info.shade_bytes = sc.opos.bytes + sc.vnc.bytes + sc.tri_idx.bytes + sc.materials.bytes +
                           sc.instances.bytes + sc.sec_mat.bytes;
     SOLRT_CUDA(cudaEventRecord(ctx.ev1, st));
     SOLRT_CUDA(cudaEventSynchronize(ctx.ev1));

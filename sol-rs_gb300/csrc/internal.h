@@ -255,7 +255,7 @@ struct Scene {
     // world positions (BVH builds), object-space positions and normals and
     // colours (shading), triangles (v0, v1, v2, section), materials, and per
     // section its material index
-    DeviceBuffer vpos, vcol, tri_idx, materials, sec_mat;
+    DeviceBuffer vpos, tri_idx, materials, sec_mat;
     DeviceBuffer nodes, tri_wt;
     solrt_bvh_info info{};
     solrt_bvh_desc desc{};
@@ -266,7 +266,7 @@ struct Scene {
     // build (leaf order, children, parents, key ranges) for refits.
     bool dynamic = false;
     uint32_t section_count = 0;
-    DeviceBuffer opos, onrm, vsec_start, instances;
+    DeviceBuffer opos, vnc, vsec_start, instances;
     DeviceBuffer topo_order, topo_child, topo_par_int, topo_par_leaf, topo_range;
     // Host copies: each section's first triangle and triangle count, and the
     // staged instances (one per section).
@@ -302,8 +302,7 @@ struct Scene {
         d.inst = two ? inst_table.as<float4>() : nullptr;
         d.vpos = vpos.as<float4>();
         d.opos = opos.as<float4>();
-        d.onrm = onrm.as<float4>();
-        d.vcol = vcol.as<float4>();
+        d.vnc = vnc.as<float4>();
         d.tri_idx = tri_idx.as<uint4>();
         d.sections = instances.as<float4>();
         d.sec_mat = sec_mat.as<uint32_t>();

@@ -50,9 +50,16 @@ SOLRT_D f3 mat4_xyz(const float4* m, float x, float y, float z, float w) {
 // ao.rchit:66-75) compute them: object-space vertex normals and positions
 // interpolated with the barycentrics, then the section instance's
 // transform_it (normal, w = 0, normalised) and transform (position, w = 1).
-SOLRT_D void hit_frame(const DevScene& sc, uint4 ti, float b0, float b1, float b2, f3& normal, f3& pos) {
-    const float4 n0 = __ldg(sc.onrm + ti.x), n1 = __ldg(sc.onrm + ti.y), n2 = __ldg(sc.onrm + ti.z);
+// `vcol`, when given, receives the interpolated vertex colour (rchit:87),
+// which each vertex's 256-bit normal load brings along.
+SOLRT_D void hit_frame(const DevScene& sc, uint4 ti, float b0, float b1, float b2, f3& normal, f3& pos,
+                       f3* vcol = nullptr) {
+    float4 n0, n1, n2, c0, c1, c2;
+    ldg_2x4(sc.vnc + 2 * (size_t)ti.x, n0, c0);
+    ldg_2x4(sc.vnc + 2 * (size_t)ti.y, n1, c1);
+    ldg_2x4(sc.vnc + 2 * (size_t)ti.z, n2, c2);
     const float4 p0 = __ldg(sc.opos + ti.x), p1 = __ldg(sc.opos + ti.y), p2 = __ldg(sc.opos + ti.z);
+    if (vcol) *vcol = f3{c0.x, c0.y, c0.z} * b0 + f3{c1.x, c1.y, c1.z} * b1 + f3{c2.x, c2.y, c2.z} * b2;
     const f3 n = f3{n0.x, n0.y, n0.z} * b0 + f3{n1.x, n1.y, n1.z} * b1 + f3{n2.x, n2.y, n2.z} * b2;
     const f3 p = f3{p0.x, p0.y, p0.z} * b0 + f3{p1.x, p1.y, p1.z} * b1 + f3{p2.x, p2.y, p2.z} * b2;
     const float4* inst = sc.sections + 9 * (size_t)ti.w;  // (id, ..), transform, transform_it
@@ -113,10 +120,8 @@ SOLRT_D bool shade_step(const DevJob& J, float4 o, float4 d, float4 h, f3& acc, 
     }
     const float b1 = h.z, b2 = h.w;
     const float b0 = (1.0f - b1) - b2;                                       // rchit:82
-    f3 normal, pos;
-    hit_frame(sc, ti, b0, b1, b2, normal, pos);                              // rchit:82-90
-    const float4 c0 = __ldg(sc.vcol + ti.x), c1 = __ldg(sc.vcol + ti.y), c2 = __ldg(sc.vcol + ti.z);
-    const f3 vcol = f3{c0.x, c0.y, c0.z} * b0 + f3{c1.x, c1.y, c1.z} * b1 + f3{c2.x, c2.y, c2.z} * b2;
+    f3 normal, pos, vcol;
+    hit_frame(sc, ti, b0, b1, b2, normal, pos, &vcol);                       // rchit:82-90
     const f3 wi = normalize(dir);                                            // rchit:94-95
     const f3 n_o = normal * glsl_sign(dot(normal, -wi));
     const float alpha2 = m2.y * m2.y;

@@ -29,8 +29,8 @@ struct DevScene {
     const float4* inst;       // SOLRT_BVH2_TWO_LEVEL: per section inverse-transform rows 0-2, BLAS root
     const float4* vpos;       // world position per vertex (.w unused): the BVH builds
     const float4* opos;       // object-space position per vertex: shading
-    const float4* onrm;       // object-space normal per vertex: shading
-    const float4* vcol;       // vertex colour
+    const float4* vnc;        // per vertex its object-space normal and its colour (2 float4, 32 B: one
+                              // 256-bit load and one DRAM sector): shading
     const uint4* tri_idx;     // (v0, v1, v2, section) per original triangle
     const float4* sections;   // per section its solrt_instance as 9 float4: (id, ..), transform
                               // columns, transform_it columns (column-major)
