@@ -642,7 +642,8 @@ solrt_status solrt_server_cancel(solrt_server* srv, uint64_t ticket);
 /* The completion queue: tickets of jobs that reached their final state
  * (done, failed, cancelled) since the last call, oldest first, at most
  * `max` of them (the rest stay for the next call); *n = how many. A client
- * with thousands of jobs in flight fetches these and polls only them. */
+ * with thousands of jobs in flight fetches these and polls only them. The
+ * queue holds the newest 2^20 tickets not yet fetched (older ones drop). */
 solrt_status solrt_server_finished(solrt_server* srv, uint64_t* tickets, uint32_t max, uint32_t* n);
 solrt_status solrt_server_get_stats(solrt_server* srv, solrt_server_stats* out);
 /* Stops the serving thread (unfinished jobs are dropped) and frees images. */

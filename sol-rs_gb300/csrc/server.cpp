@@ -103,8 +103,14 @@ struct solrt_server {
 namespace {
 
 // A job reached its final state (done, failed or cancelled): its ticket
-// joins the completion queue of solrt_server_finished. Caller holds the lock.
-void mark_finished(solrt_server* srv, uint64_t ticket) { srv->finished.push_back(ticket); }
+// joins the completion queue of solrt_server_finished, which keeps the
+// newest kFinishedMax tickets (a client that never fetches them does not
+// grow it without bound). Caller holds the lock.
+constexpr size_t kFinishedMax = size_t(1) << 20;
+void mark_finished(solrt_server* srv, uint64_t ticket) {
+    if (srv->finished.size() >= kFinishedMax) srv->finished.pop_front();
+    srv->finished.push_back(ticket);
+}
 
 uint64_t scene_bytes(solrt_scene* s) {
     uint64_t b = 0;
