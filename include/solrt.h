@@ -241,18 +241,20 @@ typedef enum solrt_integrator {
     /* Path tracing with next-event estimation, an estimator the reference
      * does not have (it finds emitters only by hitting them). At every
      * diffuse vertex that continues the path, after the vertex's three
-     * pathtrace.rchit draws, three more draws pick an emissive triangle
-     * (probability proportional to its world area when the scene was
-     * created) and a uniform point on it; one shadow ray per vertex goes
-     * through a second wavefront queue, and an unoccluded one adds
-     * throughput * albedo * Le * cos_x * cos_y * area / (pi * r^2 * p_pick)
-     * to the sample. Emitters hit after a bounce then add nothing (their
-     * light came through the shadow rays); camera rays that hit an emitter
-     * and misses keep the reference's terms. Same expected image as
-     * SOLRT_INTEGRATOR_PATH with material_mode SOLRT_MATERIAL_LAMBERT, less
-     * noise under small lights. Needs material_mode SOLRT_MATERIAL_LAMBERT
-     * and the wavefront kernel; runs in batches and the server. Shadow
-     * segments are counted in solrt_stats.shadow_segments, not segments. */
+     * pathtrace.rchit draws, two draws pick a uniform point on an emissive
+     * triangle that a walk down the scene's light tree chooses (one draw
+     * per level, each child with probability proportional to its power
+     * over its distance, bounded by the receiver's cosine); one shadow ray
+     * per vertex goes through a second wavefront queue (or, in the
+     * per-pixel kernel, is traced at once), and an unoccluded one adds its
+     * light weighted by the power heuristic against the BSDF sample. An
+     * emitter hit after a bounce adds its term with the complementary
+     * weight; camera rays that hit an emitter and misses keep the
+     * reference's terms. Same expected image as SOLRT_INTEGRATOR_PATH with
+     * material_mode SOLRT_MATERIAL_LAMBERT, less noise under small lights.
+     * Needs material_mode SOLRT_MATERIAL_LAMBERT; runs in both kernels, in
+     * every batch mode and in the server. Shadow segments are counted in
+     * solrt_stats.shadow_segments, not segments. */
     SOLRT_INTEGRATOR_PATH_NEE = 3
 } solrt_integrator;
 
@@ -459,8 +461,8 @@ enum {
     /* one persistent launch per step instead of wavefront passes: warps take
      * 32 pixels at a time of all jobs' pixels from a device work counter and
      * each thread traces all samples of its pixel to the end (the per-pixel
-     * structure of the reference's raygen loop); same images. Path
-     * integrator only (no next-event estimation). */
+     * structure of the reference's raygen loop; a next-event-estimation
+     * job's shadow rays are traced at their vertices); same images. */
     SOLRT_BATCH_PERSISTENT = 2u,
     /* the wavefront passes of a step (generate, extend and shade per bounce,
      * accumulate, finalize) as phases of one cooperative launch: a grid of

@@ -450,6 +450,152 @@ __global__ void __launch_bounds__(128, SOLRT_MEGA_MINB)
     flush_stats(stats, segs, paths, cnt.fallbacks, ef);
 }
 
+// ---------------------------------------------------------------------------
+// Next-event estimation in the per-pixel structure (KERNEL_MEGA renders and
+// SOLRT_BATCH_PERSISTENT batches with SOLRT_INTEGRATOR_PATH_NEE jobs): the
+// same estimator as the wavefront's shadow queue, one path at a time.
+// ---------------------------------------------------------------------------
+
+// Closest hit of one ray with the kind's per-ray loop.
+template <int KIND>
+SOLRT_D void trace_one(const TravScene& ts, const float4& o, const float4& d, HitRec& h, TraceCounters& cnt,
+                       uint32_t& ef) {
+    if (KIND == SOLRT_BVH8_Q8) trace_bvh8<false>(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, ef);
+    else if (KIND == SOLRT_BVH8_F32) trace_bvh8<false, true>(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, ef);
+    else if (KIND == SOLRT_BVH4_Q8) trace_bvh4_ray(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, ef);
+    else if (KIND == SOLRT_BVH2_Q16) trace_bvh2_ray<true>(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, ef);
+    else if (KIND == SOLRT_BVH2_TWO_LEVEL) trace_bvh2_2l_ray(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, ef);
+    else trace_bvh2_ray(ts, o.x, o.y, o.z, d.x, d.y, d.z, o.w, d.w, h, cnt, ef);
+}
+
+// Per-thread counts of the per-pixel NEE kernels.
+struct MegaCounts {
+    uint32_t segs = 0, paths = 0, shadow = 0, unoccluded = 0, ef = 0;
+    TraceCounters cnt{0, 0, 0}, scnt{0, 0, 0};  // path / shadow-ray traversals
+};
+
+// One path to its end: at each continuing vertex of a NEE job the shadow
+// ray of k_shade<true> (same draws, same order) is traced at once; closest-
+// hit traversal gives the same occlusion answer as the wavefront's any-hit
+// one. The sample is (0 + unoccluded shadow terms in bounce order) + the end
+// term, as the wavefront's radiance slot sums them.
+template <int KIND>
+SOLRT_D f3 mega_path_nee(const DevJob& J, const TravScene& ts, float4 o, float4 d, uint32_t& rng, MegaCounts& mc) {
+    const bool nee = J.integrator == SOLRT_INTEGRATOR_PATH_NEE;
+    f3 acc{1.0f, 1.0f, 1.0f}, rsum{0.0f, 0.0f, 0.0f};
+    uint32_t depth = 0;
+    float4 prev = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    for (;;) {
+        HitRec h;
+        trace_one<KIND>(ts, o, d, h, mc.cnt, mc.ef);
+        ++mc.segs;
+        float4 on, dn, prev_out = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        f3 n_o{0.0f, 0.0f, 0.0f};
+        const float4 pv = nee && depth > 0u ? prev : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (!shade_step<true>(J, o, d, make_float4(h.t, __uint_as_float(h.prim), h.u, h.v), acc, rng, depth, on, dn,
+                              mc.ef, &n_o, pv, &prev_out))
+            break;
+        if (nee) {
+            float4 so, sd;
+            f3 cn;
+            if (nee_sample(J.sc, f3{on.x, on.y, on.z}, n_o, acc, o.w, rng, so, sd, cn)) {
+                HitRec sh;
+                trace_one<KIND>(ts, so, sd, sh, mc.scnt, mc.ef);
+                ++mc.shadow;
+                if (sh.prim == SOLRT_NO_HIT) {
+                    rsum = rsum + cn;
+                    ++mc.unoccluded;
+                }
+            }
+            prev = prev_out;
+        }
+        o = on;
+        d = dn;
+    }
+    return nee ? rsum + acc : acc;
+}
+
+// All samples of pixel `pix` of job J with mega_path_nee; the pixel's sums
+// are written once.
+template <int KIND>
+SOLRT_D void mega_pixel_nee(const DevJob& J, uint32_t pix, MegaCounts& mc) {
+    const TravScene ts = trav_scene(J.sc);
+    f3 s{0.0f, 0.0f, 0.0f}, ks{0.0f, 0.0f, 0.0f}, kc{0.0f, 0.0f, 0.0f};
+    float kn = 0.0f;
+    if (J.accum_mode == SOLRT_ACCUM_KAHAN) {
+        const float4 s4 = J.ksum[pix], c4 = J.kcomp[pix];
+        ks = f3{s4.x, s4.y, s4.z};
+        kc = f3{c4.x, c4.y, c4.z};
+        kn = s4.w;
+    }
+    uint32_t rng = 0;
+    for (uint32_t smp = 0; smp < J.spp; ++smp) {
+        rng = sample_seed(J, pix, smp, rng);
+        float4 o, d;
+        camera_ray(J, pix, rng, o, d);
+        const f3 v = mega_path_nee<KIND>(J, ts, o, d, rng, mc);
+        const float4 c = make_float4(v.x, v.y, v.z, 0.0f);
+        if (J.accum_mode == SOLRT_ACCUM_KAHAN) add_sample_kahan(ks, kc, kn, c);
+        else add_sample(s, c);
+    }
+    mc.paths += J.spp;
+    if (J.accum_mode == SOLRT_ACCUM_KAHAN) {
+        J.ksum[pix] = make_float4(ks.x, ks.y, ks.z, kn);
+        J.kcomp[pix] = make_float4(kc.x, kc.y, kc.z, 0.0f);
+    } else {
+        J.fsum[pix] = make_float4(s.x, s.y, s.z, 0.0f);
+    }
+}
+
+// Path segments into stats[0], shadow rays into stats[1] (the split of the
+// wavefront's launches).
+SOLRT_D void flush_mega_counts(DevStats* stats, const MegaCounts& mc) {
+    flush_stats(stats, mc.segs, mc.paths, mc.cnt.fallbacks, mc.ef);
+    const uint32_t ws = __reduce_add_sync(0xffffffffu, mc.shadow);
+    const uint32_t wu = __reduce_add_sync(0xffffffffu, mc.unoccluded);
+    const uint32_t wf = __reduce_add_sync(0xffffffffu, mc.scnt.fallbacks);
+    if ((threadIdx.x & 31) == 0) {
+        if (ws) atomicAdd(&stats[1].segments, (unsigned long long)ws);
+        if (wu) atomicAdd(&stats[1].unoccluded, (unsigned long long)wu);
+        if (wf) atomicAdd(&stats[1].fp64_fallbacks, (unsigned long long)wf);
+    }
+}
+
+// k_megakernel for a NEE job: one thread per pixel.
+template <int KIND>
+__global__ void __launch_bounds__(128, SOLRT_MEGA_MINB) k_megakernel_nee(const DevJob* __restrict__ job,
+                                                                        DevStats* stats) {
+    const DevJob& J = *job;
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    MegaCounts mc;
+    if (pix < J.width * J.height) mega_pixel_nee<KIND>(J, pix, mc);
+    flush_mega_counts(stats, mc);
+}
+
+// k_megakernel_batch for batches with NEE jobs (every job of the batch runs
+// through mega_pixel_nee; a job without NEE gets the plain estimator's
+// image there too).
+template <int KIND>
+__global__ void __launch_bounds__(128, SOLRT_MEGA_MINB)
+    k_megakernel_batch_nee(const DevJob* __restrict__ jobs, const uint32_t* __restrict__ job_pix, uint32_t njobs,
+                           uint32_t total_pix, unsigned int* __restrict__ work, DevStats* stats) {
+    const int lane = threadIdx.x & 31;
+    MegaCounts mc;
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(work, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= total_pix) break;
+        const uint32_t t = base + (uint32_t)lane;
+        if (t < total_pix) {
+            const uint32_t j = find_last_le(njobs, t, [&](uint32_t i) { return job_pix[i]; });
+            mega_pixel_nee<KIND>(jobs[j], t - job_pix[j], mc);
+        }
+        __syncwarp();
+    }
+    flush_mega_counts(stats, mc);
+}
+
 // Zeroes the per-frame sample sums of running-mix jobs.
 __global__ void k_begin(const DevJob* __restrict__ jobs, const uint32_t* __restrict__ job_pix, uint32_t njobs,
                         uint32_t pixels) {
@@ -759,12 +905,13 @@ solrt_status issue_pass(Context& ctx, uint32_t kind, const DevJob* dj, const Dev
 // resident blocks) of k_megakernel_batch over the batch's pixels.
 template <int KIND>
 void launch_mega_batch(Context& ctx, const DevJob* dj, const uint32_t* jp, uint32_t njobs, uint32_t total_pix,
-                       unsigned int* work) {
+                       unsigned int* work, bool nee) {
+    auto kern = nee ? k_megakernel_batch_nee<KIND> : k_megakernel_batch<KIND>;
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_megakernel_batch<KIND>, 128, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 128, 0);
     const uint32_t grid = std::min<uint32_t>((uint32_t)ctx.sm_count * (uint32_t)std::max(per_sm, 1),
                                              cdiv(total_pix, 128u));
-    k_megakernel_batch<KIND><<<grid, 128, 0, ctx.stream>>>(dj, jp, njobs, total_pix, work, ctx.stats.as<DevStats>());
+    kern<<<grid, 128, 0, ctx.stream>>>(dj, jp, njobs, total_pix, work, ctx.stats.as<DevStats>());
 }
 
 solrt_status batch_issue(Batch& b, bool record_timing) {
@@ -779,13 +926,15 @@ solrt_status batch_issue(Batch& b, bool record_timing) {
         unsigned int* work = ctx.trace_work.as<unsigned int>();
         SOLRT_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned int), st));
         const int tm = record_timing ? ctx.timing_begin(0) : -1;  // traversal and shading in one launch
-        if (b.kind == SOLRT_BVH8_Q8) launch_mega_batch<SOLRT_BVH8_Q8>(ctx, dj, jp, njobs, total_pix, work);
-        else if (b.kind == SOLRT_BVH4_Q8) launch_mega_batch<SOLRT_BVH4_Q8>(ctx, dj, jp, njobs, total_pix, work);
-        else if (b.kind == SOLRT_BVH8_F32) launch_mega_batch<SOLRT_BVH8_F32>(ctx, dj, jp, njobs, total_pix, work);
-        else if (b.kind == SOLRT_BVH2_Q16) launch_mega_batch<SOLRT_BVH2_Q16>(ctx, dj, jp, njobs, total_pix, work);
+        bool nee = false;
+        for (const DevJob& J : b.jobs) nee = nee || J.integrator == SOLRT_INTEGRATOR_PATH_NEE;
+        if (b.kind == SOLRT_BVH8_Q8) launch_mega_batch<SOLRT_BVH8_Q8>(ctx, dj, jp, njobs, total_pix, work, nee);
+        else if (b.kind == SOLRT_BVH4_Q8) launch_mega_batch<SOLRT_BVH4_Q8>(ctx, dj, jp, njobs, total_pix, work, nee);
+        else if (b.kind == SOLRT_BVH8_F32) launch_mega_batch<SOLRT_BVH8_F32>(ctx, dj, jp, njobs, total_pix, work, nee);
+        else if (b.kind == SOLRT_BVH2_Q16) launch_mega_batch<SOLRT_BVH2_Q16>(ctx, dj, jp, njobs, total_pix, work, nee);
         else if (b.kind == SOLRT_BVH2_TWO_LEVEL)
-            launch_mega_batch<SOLRT_BVH2_TWO_LEVEL>(ctx, dj, jp, njobs, total_pix, work);
-        else launch_mega_batch<SOLRT_BVH2>(ctx, dj, jp, njobs, total_pix, work);
+            launch_mega_batch<SOLRT_BVH2_TWO_LEVEL>(ctx, dj, jp, njobs, total_pix, work, nee);
+        else launch_mega_batch<SOLRT_BVH2>(ctx, dj, jp, njobs, total_pix, work, nee);
         ctx.timing_end(tm);
         const int tf = record_timing ? ctx.timing_begin(3) : -1;
         k_finalize<<<cdiv(total_pix, 256), 256, 0, st>>>(dj, jp, njobs, total_pix);
@@ -841,10 +990,6 @@ solrt_status batch_plan(Context& ctx, const solrt_job* jobs, uint32_t n, uint32_
         if (jb.params.kernel != SOLRT_KERNEL_WAVEFRONT) { set_error("job %u: batches run the wavefront kernel", j); return SOLRT_ERR_INVALID; }
         if (jb.params.integrator != SOLRT_INTEGRATOR_PATH && jb.params.integrator != SOLRT_INTEGRATOR_PATH_NEE) {
             set_error("job %u: batches run the path integrators", j);
-            return SOLRT_ERR_INVALID;
-        }
-        if (jb.params.integrator == SOLRT_INTEGRATOR_PATH_NEE && (flags & SOLRT_BATCH_PERSISTENT)) {
-            set_error("job %u: persistent batches run the path integrator without next-event estimation", j);
             return SOLRT_ERR_INVALID;
         }
         if (jb.params.integrator == SOLRT_INTEGRATOR_PATH_NEE) SOLRT_TRY(ensure_shadow_queue(ctx));
@@ -1220,10 +1365,6 @@ static solrt_status render_sibling(Context& ctx, const Scene& sc, const solrt_ca
 
 solrt_status render_frame(Context& ctx, const Scene& sc, const solrt_camera& cam, const solrt_render_params& p,
                           Image& img) {
-    if (p.integrator == SOLRT_INTEGRATOR_PATH_NEE && p.kernel != SOLRT_KERNEL_WAVEFRONT) {
-        set_error("next-event estimation runs in the wavefront kernel");
-        return SOLRT_ERR_INVALID;
-    }
     if (p.integrator != SOLRT_INTEGRATOR_PATH && p.integrator != SOLRT_INTEGRATOR_PATH_NEE)
         return render_sibling(ctx, sc, cam, p, img);
     solrt_job jb;
@@ -1239,7 +1380,18 @@ solrt_status render_frame(Context& ctx, const Scene& sc, const solrt_camera& cam
     cudaGetLastError();
     const uint32_t npix = p.width * p.height;
     SOLRT_CUDA(cudaEventRecord(ctx.ev0, ctx.stream));
-    if (b.kind == SOLRT_BVH8_Q8)
+    const DevJob* dj = b.d_jobs.as<DevJob>();
+    DevStats* dst = ctx.stats.as<DevStats>();
+    const uint32_t g = cdiv(npix, 128);
+    if (p.integrator == SOLRT_INTEGRATOR_PATH_NEE) {
+        if (b.kind == SOLRT_BVH8_Q8) k_megakernel_nee<SOLRT_BVH8_Q8><<<g, 128, 0, ctx.stream>>>(dj, dst);
+        else if (b.kind == SOLRT_BVH4_Q8) k_megakernel_nee<SOLRT_BVH4_Q8><<<g, 128, 0, ctx.stream>>>(dj, dst);
+        else if (b.kind == SOLRT_BVH8_F32) k_megakernel_nee<SOLRT_BVH8_F32><<<g, 128, 0, ctx.stream>>>(dj, dst);
+        else if (b.kind == SOLRT_BVH2_Q16) k_megakernel_nee<SOLRT_BVH2_Q16><<<g, 128, 0, ctx.stream>>>(dj, dst);
+        else if (b.kind == SOLRT_BVH2_TWO_LEVEL)
+            k_megakernel_nee<SOLRT_BVH2_TWO_LEVEL><<<g, 128, 0, ctx.stream>>>(dj, dst);
+        else k_megakernel_nee<SOLRT_BVH2><<<g, 128, 0, ctx.stream>>>(dj, dst);
+    } else if (b.kind == SOLRT_BVH8_Q8)
         k_megakernel<SOLRT_BVH8_Q8><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(b.d_jobs.as<DevJob>(), ctx.stats.as<DevStats>());
     else if (b.kind == SOLRT_BVH4_Q8)
         k_megakernel<SOLRT_BVH4_Q8><<<cdiv(npix, 128), 128, 0, ctx.stream>>>(b.d_jobs.as<DevJob>(), ctx.stats.as<DevStats>());

@@ -193,8 +193,7 @@ def test_persistent_batch_equals_alone(solrt, ctx, bvh):
     """SOLRT_BATCH_PERSISTENT: all jobs in one persistent per-pixel launch
     (warps take pixels from a device work counter, each thread traces its
     pixel's samples to the end) render every job's image bit for bit as
-    solrt_render of that job alone; two launches accumulate two frames. Jobs
-    with next-event estimation are refused."""
+    solrt_render of that job alone; two launches accumulate two frames."""
     kind = bvh_kind(solrt, bvh)
     jobs = [j for j, (_, _, _, kw) in zip(_make(solrt, ctx, kind), _specs(solrt))
             if kw.get("integrator", solrt.INTEGRATOR_PATH) == solrt.INTEGRATOR_PATH]
@@ -217,10 +216,31 @@ def test_persistent_batch_equals_alone(solrt, ctx, bvh):
         assert np.array_equal(a32.view(np.uint32), b32.view(np.uint32))
         assert np.array_equal(a8, b8)
     batch.close()
-    nee = [j for j, (_, _, _, kw) in zip(_make(solrt, ctx, kind), _specs(solrt))
-           if kw.get("integrator", solrt.INTEGRATOR_PATH) == solrt.INTEGRATOR_PATH_NEE]
-    with pytest.raises(solrt.SolrtError):
-        solrt.Batch(ctx, nee, persistent=True)
+
+
+@pytest.mark.parametrize("bvh", ["bvh2", "bvh2t", "bvh8"])
+def test_persistent_batch_with_nee_equals_alone(solrt, ctx, bvh):
+    """A persistent per-pixel batch holding next-event-estimation jobs (each
+    thread traces a vertex's shadow ray at once) renders every job as
+    solrt_render of that job alone, with the same shadow-ray counts."""
+    kind = bvh_kind(solrt, bvh)
+    jobs = _make(solrt, ctx, kind)
+    batch = solrt.Batch(ctx, jobs, persistent=True)
+    ctx.reset_stats()
+    batch.launch()
+    ctx.synchronize()
+    st = ctx.stats()
+    assert st.error_flags == 0 and st.shadow_segments > 0
+    got = [img.read() for _, img, _, _ in jobs]
+    batch.close()
+    ctx.reset_stats()
+    want = _alone(solrt, ctx, jobs, frames=1)
+    st2 = ctx.stats()
+    assert (st.segments, st.shadow_segments, st.shadow_unoccluded) == (st2.segments, st2.shadow_segments,
+                                                                         st2.shadow_unoccluded)
+    for (a32, a8), (b32, b8) in zip(got, want):
+        assert np.array_equal(a32.view(np.uint32), b32.view(np.uint32))
+        assert np.array_equal(a8, b8)
 
 
 def _plain_jobs(solrt, ctx, kind):

@@ -56,10 +56,14 @@ def _render_both(solrt, oracle, ctx, data, w, h, kw, frames=2, bvh=None):
     return ga, acc, ctx.stats(), (seg, shadow, unocc)
 
 
+@pytest.mark.parametrize("kernel", ["wavefront", "mega"])
 @pytest.mark.parametrize("bvh", ["bvh2", "bvh2q", "bvh2t", "bvh4", "bvh8", "bvh8f"])
 @pytest.mark.parametrize("name", ["cornell", "cornell_ref_stream", "transformed", "tunnel_kahan"])
-def test_nee_bit_exact(solrt, oracle, ctx, name, bvh):
+def test_nee_bit_exact(solrt, oracle, ctx, name, bvh, kernel):
+    """The shadow-ray queue of the wavefront, and the per-pixel kernel
+    tracing each shadow ray at its vertex, against the oracle."""
     data, w, h, kw = _case(solrt, name)
+    kw = dict(kw, kernel=solrt.KERNEL_MEGA if kernel == "mega" else solrt.KERNEL_WAVEFRONT)
     ga, oa, st, (seg, shadow, unocc) = _render_both(solrt, oracle, ctx, data, w, h, kw, bvh=bvh_kind(solrt, bvh))
     diff = np.nonzero(np.any(ga.view(np.uint32) != oa.view(np.uint32), axis=-1))
     assert len(diff[0]) == 0, (len(diff[0]), list(zip(diff[0][:5], diff[1][:5])), ga[diff][:3], oa[diff][:3])
@@ -116,7 +120,7 @@ def test_nee_rejects_unsupported(solrt, ctx):
     cam = camera_of(d, 1.0)
     r = solrt.Renderer(ctx)
     bad = [dict(material_mode=solrt.MATERIAL_REF),
-           dict(material_mode=solrt.MATERIAL_LAMBERT, kernel=solrt.KERNEL_MEGA)]
+           dict(material_mode=solrt.MATERIAL_REF, kernel=solrt.KERNEL_MEGA)]
     for kw in bad:
         p = solrt.render_params(8, 8, spp=1, max_bounces=2, integrator=solrt.INTEGRATOR_PATH_NEE, **kw)
         with pytest.raises(solrt.SolrtError):
